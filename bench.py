@@ -1,0 +1,294 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 EC-FDTD engine (prints one JSON line on rank 0).
+
+A "step" is one full EC-FDTD timestep (voltage + current half-steps with every extension and
+the per-step probe processing) over the whole mesh of the workload.  Default workload: the
+bandwidth-stress configuration, 512x512x256 mesh lines (67.1 M cells, 1.9 GB of field state,
+larger than the 129 MB L2), seeded random dielectric / lossy / Drude-Lorentz blocks, Mur walls,
+4 Gaussian point sources with per-step voltage monitors.
+
+value   = cells * K / device time of K steps replayed through the captured step graph (MCells/s)
+e2e     = the same metric through the C ABI with host buffers: per step one oems_cuda_iterate(1)
+          plus a device->host read of every probe's newest sample (the openEMS processing loop)
+roofline= algorithmic bytes of the dominant kernel (36 B per cell per half-step update: read the
+          updated field, read the other field, write the updated field) over its average
+          CUDA-event duration, against the measured HBM copy bandwidth
+cpu_baseline = the multithreaded SSE-compressed engine restated on the host cores
+          (oracle port, all cores) on a bounded number of steps of the same workload
+
+Multi-GPU: replicas only (one independent simulation per rank, no collective on the data path);
+``value`` is the sum over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES_PER_CELL_STEP = 72          # V: r/w 12+12, I read 12; I: r/w 12+12, V read 12
+ALG_BYTES_PER_CELL_HALF = 36
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic_from_profiles(kernel):
+    """Per-cell DRAM bytes of a kernel from the committed ncu summary (None if absent)."""
+    path = os.path.join(ROOT, "profiles", "ncu_update_kernels_stress.md")
+    try:
+        for line in open(path):
+            if line.startswith(f"traffic_bytes_per_cell[{kernel}]"):
+                return float(line.split("=")[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.file:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_workload(name):
+    from openems_gb300 import configs
+    if name == "stress":
+        return configs.stress(steps=100000), "stress 512x512x256 lines, 64 random blocks (10% Drude/Lorentz), Mur x6, 4 sources"
+    if name == "patch":
+        return configs.patch(steps=100000), "patch 160x160x80 graded, UPML 8, 50 Ohm port, NF2FF 3 freqs"
+    if name == "plain":
+        return configs.plain_cube(n=100, steps=100000), "plain 100^3, vacuum, PEC, soft Ez, V/I probes"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def cpu_baseline(op, steps_cap, budget_s, threads):
+    """Multithreaded SSE-compressed restatement (oracle port) on the host cores."""
+    from oracle.oracle import OracleEngine
+    eng = OracleEngine(op, steps_cap + 2, threads=threads)
+    eng.IterateTS(1)                        # warm-up step (threads started, pages touched)
+    n = 0
+    t0 = time.perf_counter()
+    while n < steps_cap:
+        eng.IterateTS(1)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    eng.close()
+    cells = float(np.prod(op.num_lines.astype(np.float64)))
+    return cells * n / dt / 1e6, n, dt
+
+
+def run_reference(args, op, desc, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle.oracle import OracleEngine
+    cells = float(np.prod(op.num_lines.astype(np.float64)))
+    eng = OracleEngine(op, args.steps + args.warmup + 2, threads=threads)
+    eng.IterateTS(max(args.warmup, 1))
+    t0 = time.perf_counter()
+    done = 0
+    budget = float(os.environ.get("OEMS_REF_BUDGET_S", "120"))
+    while done < args.steps:
+        eng.IterateTS(1)
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    eng.close()
+    v = cells * done / dt / 1e6
+    line = {
+        "impl": "reference", "metric": "MCells/s", "value": v, "unit": "MCells/s", "n_gpus": args.gpus,
+        "steps": done, "warmup": args.warmup, "ms_per_step": dt / done * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "cells": cells},
+        "cpu_baseline": {"value": v, "unit": "MCells/s", "cores": threads, "kind": "port",
+                         "sample": f"{done} timesteps of the full workload (bounded to {budget:.0f} s)"},
+        "e2e": {"value": v, "unit": "MCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="stress", choices=["stress", "patch", "plain"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference" and rank != 0:
+        return
+    t_build = time.perf_counter()
+    op, desc = build_workload(args.workload)
+    t_build = time.perf_counter() - t_build
+    if args.impl == "reference":
+        run_reference(args, op, desc, rank)
+        return
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    from openems_gb300.engine import Engine_CUDA
+    cells = float(np.prod(op.num_lines.astype(np.float64)))
+    e2e_steps = min(args.steps, 100)
+    prof_steps = min(args.steps, 20)
+    total = args.warmup + args.steps + prof_steps + e2e_steps + 4
+    t_setup = time.perf_counter()
+    eng = Engine_CUDA(op, total, device=local if world > 1 else 0)
+    t_setup = time.perf_counter() - t_setup
+    eng.IterateTS(max(args.warmup, 3))
+    eng.sync()
+
+    # ---- timed region: K steps through the captured graph -------------------------------
+    if dist:
+        dist.barrier()
+    eng.sync()
+    with ClockSampler(local) as clk:
+        ms = eng.timed_iterate(args.steps)
+    clocks = clk.summary()
+    if dist:
+        import torch
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * args.steps / (ms / 1e3) / 1e6 * world
+
+    # ---- per-kernel event timing for the roofline ----------------------------------------
+    from openems_gb300._native import KERNEL_CLASSES
+    kms, kcnt = eng.profile(prof_steps)
+    kernels = {KERNEL_CLASSES[i]: {"ms_total": kms[i], "launches": kcnt[i]} for i in range(len(KERNEL_CLASSES)) if kcnt[i]}
+    dom = max(("update_v", "update_i"), key=lambda k: kms[KERNEL_CLASSES.index(k)])
+    di = KERNEL_CLASSES.index(dom)
+    avg_ms = kms[di] / max(kcnt[di], 1)
+    achieved = ALG_BYTES_PER_CELL_HALF * cells / (avg_ms / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    tr = _traffic_from_profiles(dom)
+    roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": tr * cells if tr is not None else None,
+                "alg_bytes_per_launch": ALG_BYTES_PER_CELL_HALF * cells,
+                "step_frac": (ALG_BYTES_PER_CELL_STEP * cells / (ms / args.steps / 1e3) / 1e9) / peak}
+
+    # ---- end to end through the C ABI: iterate(1) + D2H of the newest probe samples -------
+    pids = eng.vprobe_ids + eng.iprobe_ids
+    slot = eng.GetNumberOfTimesteps()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eng.IterateTS(1)
+        slot += 1
+        for pid in pids:
+            eng.probe_range(pid, slot, 1)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": cells * e2e_steps / e2e_s / 1e6 * world, "unit": "MCells/s", "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": 8 * len(pids), "steps": e2e_steps,
+           "note": "per step: oems_cuda_iterate(1) then oems_cuda_read_probe_range of every probe (synchronous)"}
+    launches = eng.launches_per_step()
+    eng.close()
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n, sec = cpu_baseline(op, 50, args.cpu_budget, threads)
+        base = {"value": v, "unit": "MCells/s", "cores": threads, "kind": "port",
+                "sample": f"{n} timesteps of the full {desc} workload ({sec:.1f} s, setup excluded)"}
+
+    if rank == 0:
+        line = {
+            "metric": "MCells/s", "value": value, "unit": "MCells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "cells": cells, "l2": "inputs larger than L2 (field state %.2f GB)" % (
+                24 * cells / 1e9), "parallelism": "replicas" if world > 1 else "single",
+                "operator_classes": None, "build_s": round(t_build, 1), "engine_setup_s": round(t_setup, 1)},
+            "roofline": roofline,
+            "cpu_baseline": base,
+            "e2e": e2e,
+            "clocks": clocks,
+            "gpu_launches": launches * args.steps,
+            "launches_per_step": launches,
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

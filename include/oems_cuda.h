@@ -1,0 +1,231 @@
+/*
+ * oems_cuda.h -- C ABI of the GB300 EC-FDTD engine (CUDA, sm_103a).
+ *
+ * The engine is a drop-in for openEMS's Engine path: it consumes the coefficients an openEMS
+ * Operator builds (vv/vi/ii/iv, or the compressed operator) plus the tables its operator
+ * extensions build, and runs Engine::IterateTS with the extension hooks fused into device
+ * kernels.  Every entry point is extern "C", takes plain pointers and sizes, never throws and
+ * returns an int status (OEMS_OK = 0).  Host arrays are owned by the caller and copied during
+ * the call; device memory is owned by the engine handle.
+ *
+ * Layouts (all little-endian, C order):
+ *   fields / dense coefficients : float [3][Nx][Ny][Nz]   (ArrayNIJK, tools/arraylib/array_nijk.h:58-62)
+ *   index triples               : unsigned [3][count]     (x row, y row, z row)
+ *
+ * Threading: one handle belongs to one host thread and one CUDA stream (the engine's own).
+ * Calls on different handles may run concurrently.
+ *
+ * Every declaration cites the reference interface it replaces.
+ */
+#ifndef OEMS_CUDA_H
+#define OEMS_CUDA_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OEMS_OK               0
+#define OEMS_ERR_ARG          1   /* invalid argument (sizes, indices, NULL pointers)          */
+#define OEMS_ERR_CUDA         2   /* a CUDA runtime call failed; see oems_cuda_last_error      */
+#define OEMS_ERR_STATE        3   /* call not allowed in the current state (e.g. before init)  */
+#define OEMS_ERR_UNSUPPORTED  4   /* extension/feature not supported by this engine            */
+#define OEMS_ERR_DEVICE       5   /* device-side status flag raised (non-finite field, ...)    */
+#define OEMS_ERR_NOMEM        6   /* device allocation failed                                   */
+
+/* which field for read/write calls */
+#define OEMS_VOLT 0
+#define OEMS_CURR 1
+
+typedef struct oems_cuda_engine oems_cuda_engine;
+
+/* ---- lifecycle ------------------------------------------------------------------------ */
+
+/* Engine::New + Engine::Init (FDTD/engine.cpp:27-59): allocate zeroed fields for
+ * numLines[0]*numLines[1]*numLines[2] mesh lines on device `device`. dt is the Operator's
+ * timestep (Operator_Base::GetTimestep, Common/operator_base.h:37). */
+int oems_cuda_create(const unsigned int num_lines[3], double dt, int device, oems_cuda_engine** out);
+
+/* Engine::~Engine / Engine::Reset (FDTD/engine.cpp:100-108). Safe on NULL. */
+void oems_cuda_destroy(oems_cuda_engine* eng);
+
+/* Human-readable description of the last error on this handle (never NULL). */
+const char* oems_cuda_last_error(const oems_cuda_engine* eng);
+
+/* ---- operator coefficients ------------------------------------------------------------- */
+
+/* Operator::vv_ptr/vi_ptr/ii_ptr/iv_ptr (FDTD/operator.h:364-367): dense float [3][Nx][Ny][Nz].
+ * The engine deduplicates the per-cell 12-tuples like Operator_SSE_Compressed::CompressOperator
+ * (FDTD/operator_sse_compressed.cpp:114-175, bitwise equality) and keeps the per-cell class
+ * index on device; if the number of distinct tuples exceeds max_classes (0 = engine default)
+ * the dense arrays are kept instead. */
+int oems_cuda_set_operator(oems_cuda_engine* eng, const float* vv, const float* vi,
+                           const float* ii, const float* iv, unsigned int max_classes);
+
+/* Operator_SSE_Compressed's own tables (FDTD/operator_sse_compressed.h:70-85):
+ * f4_{vv,vi,ii,iv}_Compressed[3] as float [3][num_vec_classes][4] and m_Op_index as
+ * unsigned [Nx][Ny][nv], nv = ceil(Nz/4), with the lane-strided z mapping of
+ * Engine_sse (FDTD/engine_sse.h:38-47): cell z lives in vector z % nv, lane z / nv. */
+int oems_cuda_set_operator_sse_compressed(oems_cuda_engine* eng, unsigned int num_vec_classes,
+                                          const float* f4_vv, const float* f4_vi,
+                                          const float* f4_ii, const float* f4_iv,
+                                          const unsigned int* op_index);
+
+/* Number of coefficient classes in use (0 when dense arrays are used). */
+int oems_cuda_operator_classes(const oems_cuda_engine* eng, unsigned int* num_classes);
+
+/* ---- engine extensions (built tables of the matching Operator_Ext_*) --------------------- */
+
+/* Engine_Ext_Excitation (FDTD/extensions/engine_ext_excitation.cpp:33-94) fed with
+ * Operator_Ext_Excitation's Volt_* / Curr_* arrays (operator_ext_excitation.h:80-94) and the
+ * Excitation signal (FDTD/excitation.h): sig_volt/sig_curr[length]; period = steps per signal
+ * period (0 = aperiodic, p = numTS+1). Replaces any previous excitation. */
+int oems_cuda_set_excitation(oems_cuda_engine* eng,
+                             unsigned int volt_count, const unsigned int* volt_index,
+                             const unsigned short* volt_dir, const float* volt_amp,
+                             const unsigned int* volt_delay,
+                             unsigned int curr_count, const unsigned int* curr_index,
+                             const unsigned short* curr_dir, const float* curr_amp,
+                             const unsigned int* curr_delay,
+                             const float* sig_volt, const float* sig_curr, unsigned int length,
+                             unsigned int period);
+
+/* Engine_Ext_UPML (FDTD/extensions/engine_ext_upml.cpp:52-229) for one region of
+ * Operator_Ext_UPML (operator_ext_upml.h:74-96): six float [3][rx][ry][rz] tables. Regions
+ * must not overlap (Create_UPML builds them disjoint). At most 6 regions. */
+int oems_cuda_add_upml(oems_cuda_engine* eng, const unsigned int start[3], const unsigned int num_lines[3],
+                       const float* vv, const float* vvfo, const float* vvfn,
+                       const float* ii, const float* iifo, const float* iifn);
+
+/* Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:82-178) for one wall of
+ * Operator_Ext_Mur_ABC: normal direction ny, wall line, shifted line, first active timestep,
+ * coefficients float [numLines[nyP]][numLines[nyPP]]. Walls are applied in reverse call
+ * order, as the reference's priority sort does. At most 6 walls. */
+int oems_cuda_add_mur(oems_cuda_engine* eng, int ny, unsigned int line_nr, unsigned int line_nr_shift,
+                      unsigned int start_ts, const float* coeff_nyP, const float* coeff_nyPP);
+
+/* Engine_Ext_LorentzMaterial + Engine_Ext_Dispersive (engine_ext_lorentzmaterial.cpp:79-168,
+ * engine_ext_dispersive.cpp:76-127) for one dispersion order of Operator_Ext_LorentzMaterial:
+ * pos unsigned [3][count]; coefficient tables float [3][count] (NULL where the flag is off). */
+int oems_cuda_add_lorentz_order(oems_cuda_engine* eng, unsigned int count, const unsigned int* pos,
+                                int volt_ade_on, int curr_ade_on, int volt_lor_on, int curr_lor_on,
+                                const float* v_int, const float* v_ext, const float* v_lor,
+                                const float* i_int, const float* i_ext, const float* i_lor);
+
+/* ---- processing: probes, DFTs, FD field dumps --------------------------------------------- */
+
+/* ProcessVoltage (Common/processvoltage.cpp:38-48) -> Engine_Interface_FDTD::CalcVoltageIntegral
+ * (FDTD/engine_interface_fdtd.cpp:206-232) on snapped start/stop indices (exactly one axis may
+ * differ). Sampled when numTS % interval == 0 within [start_ts, stop_ts]; value*weight is
+ * recorded as double. Returns the probe id (>= 0) through *id. */
+int oems_cuda_add_voltage_probe(oems_cuda_engine* eng, const unsigned int start[3], const unsigned int stop[3],
+                                double weight, unsigned int interval, unsigned int start_ts,
+                                unsigned int stop_ts, int* id);
+
+/* ProcessCurrent::CalcIntegral (Common/processcurrent.cpp:96-171): loop integral of currents in
+ * the plane normal to norm_dir with the snapped dual-mesh box and inside flags. Time is the
+ * dual time (numTS+0.5)*dt. */
+int oems_cuda_add_current_probe(oems_cuda_engine* eng, const unsigned int start[3], const unsigned int stop[3],
+                                int norm_dir, const int start_inside[3], const int stop_inside[3],
+                                double weight, unsigned int interval, unsigned int start_ts,
+                                unsigned int stop_ts, int* id);
+
+/* ProcessIntegral FD part (Common/processintegral.cpp:156-167): complex<double> DFT at
+ * num_freqs frequencies, accumulated every fd_interval steps. */
+int oems_cuda_set_probe_dft(oems_cuda_engine* eng, int probe_id, unsigned int fd_interval,
+                            unsigned int num_freqs, const double* freqs);
+
+/* ProcessFieldsFD (Common/processfields_fd.cpp:72-107) with cell interpolation
+ * (FDTD/engine_interface_fdtd.cpp:104-121, 182-199) over the box start..stop (inclusive):
+ * field 0 = E (main time), 1 = H (dual time). edge_len[n] / dual_edge_len[n] are the mesh
+ * edge lengths in metres per line (Operator::GetEdgeLength, FDTD/operator.cpp:212-215),
+ * float64 [numLines[n]] each, concatenated x,y,z. Returns the dump id through *id. */
+int oems_cuda_add_fd_dump(oems_cuda_engine* eng, int field, const unsigned int start[3],
+                          const unsigned int stop[3], unsigned int fd_interval, unsigned int num_freqs,
+                          const double* freqs, const double* edge_len, const double* dual_edge_len, int* id);
+
+/* ---- run ------------------------------------------------------------------------------------ */
+
+/* Finalise the setup: upload tables, size probe buffers for max_timesteps steps, capture the
+ * per-step CUDA graph and record the probes at numTS = 0 (ProcessingArray::Process before the
+ * first IterateTS, openems.cpp:1424-1425). */
+int oems_cuda_init(oems_cuda_engine* eng, unsigned int max_timesteps);
+
+/* Engine::IterateTS (FDTD/engine.cpp:267-286): n_steps full timesteps, asynchronous on the
+ * engine's stream; probes/DFTs are recorded on device after each step. */
+int oems_cuda_iterate(oems_cuda_engine* eng, unsigned int n_steps);
+
+/* Wait for the engine's stream; returns OEMS_ERR_DEVICE if a device status flag was raised. */
+int oems_cuda_sync(oems_cuda_engine* eng);
+
+/* Engine::GetNumberOfTimesteps (FDTD/engine.h:49). Host-side count of issued steps. */
+unsigned int oems_cuda_num_timesteps(const oems_cuda_engine* eng);
+
+/* ---- field access (Engine::GetVolt/GetCurr/SetVolt/SetCurr, FDTD/engine.h:55-101) -------------- */
+int oems_cuda_read_field(oems_cuda_engine* eng, int which, float* host_nijk);
+int oems_cuda_write_field(oems_cuda_engine* eng, int which, const float* host_nijk);
+int oems_cuda_get_value(oems_cuda_engine* eng, int which, unsigned int n, unsigned int x, unsigned int y,
+                        unsigned int z, float* value);
+int oems_cuda_set_value(oems_cuda_engine* eng, int which, unsigned int n, unsigned int x, unsigned int y,
+                        unsigned int z, float value);
+
+/* ---- results ---------------------------------------------------------------------------------- */
+
+/* Probe time series: out[k] = value*weight at numTS = k*interval (NaN where not sampled),
+ * k < cap; *count = number of slots written. */
+int oems_cuda_read_probe(oems_cuda_engine* eng, int probe_id, double* out, size_t cap, size_t* count);
+
+/* Slots [first, first+count) of a probe time series (same slot meaning as above). Used by a
+ * caller that, like ProcessingArray::Process (Common/processing.cpp:355-366), fetches the newest
+ * samples after every IterateTS chunk. */
+int oems_cuda_read_probe_range(oems_cuda_engine* eng, int probe_id, size_t first, size_t count, double* out);
+
+/* Probe DFT: out[2*f], out[2*f+1] = real, imag at frequency f (double). */
+int oems_cuda_read_probe_dft(oems_cuda_engine* eng, int probe_id, double* out);
+
+/* FD dump: complex<float> [num_freqs][3][sx][sy][sz] as interleaved re/im floats. */
+int oems_cuda_read_fd_dump(oems_cuda_engine* eng, int dump_id, float* out, size_t cap_floats);
+
+/* Engine_Interface_FDTD::CalcFastEnergy (FDTD/engine_interface_fdtd.cpp:302-347):
+ * eps0*sum(V^2) + mu0*sum(I^2) over [0,N-1)^3, device reduction in double. */
+int oems_cuda_energy(oems_cuda_engine* eng, double* energy);
+
+/* ---- checkpoint / resume --------------------------------------------------------------------- */
+
+/* Size in bytes of a snapshot of the full engine state (fields, UPML fluxes, Mur buffers,
+ * dispersive states, numTS, probe and DFT accumulators). */
+int oems_cuda_snapshot_size(const oems_cuda_engine* eng, size_t* bytes);
+/* Copy the state to host memory (`bytes` must be >= snapshot size). */
+int oems_cuda_snapshot(oems_cuda_engine* eng, void* host, size_t bytes);
+/* Restore a state written by oems_cuda_snapshot of an engine with the same setup. */
+int oems_cuda_restore(oems_cuda_engine* eng, const void* host, size_t bytes);
+
+/* ---- introspection ----------------------------------------------------------------------------- */
+
+/* Number of kernel launches issued per timestep by the captured step graph. */
+int oems_cuda_launches_per_step(const oems_cuda_engine* eng, unsigned int* launches);
+
+/* Run n_steps through the captured step graph and return their device time in ms (CUDA events
+ * on the engine stream). */
+int oems_cuda_timed_iterate(oems_cuda_engine* eng, unsigned int n_steps, float* ms);
+
+/* Kernel classes reported by oems_cuda_profile_steps. */
+#define OEMS_KC_UPDATE_V  0
+#define OEMS_KC_UPDATE_I  1
+#define OEMS_KC_MUR       2
+#define OEMS_KC_LORENTZ   3
+#define OEMS_KC_EXCITE    4
+#define OEMS_KC_STEP_END  5
+#define OEMS_KC_COUNT     6
+
+/* Run n_steps with every kernel launched directly on the engine stream, bracketed by CUDA events;
+ * ms[k] = summed device time of kernel class k, launches[k] = number of launches (either may be
+ * NULL). Same results as oems_cuda_iterate. */
+int oems_cuda_profile_steps(oems_cuda_engine* eng, unsigned int n_steps, float* ms, unsigned int* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OEMS_CUDA_H */

@@ -1,0 +1,250 @@
+"""Synthetic workloads with the shapes of the engine's benchmark configurations.
+
+No public dataset is involved: every geometry is generated here from a fixed seed.
+
+* ``plain_cube``   -- 100^3 lines, 1 mm, vacuum, PEC walls, soft Ez point source (f0 2 GHz,
+                      fc 1 GHz), a 5-edge Ez voltage probe and a 1-cell H loop, sampled every step.
+* ``patch``        -- 160x160x80 graded mesh (0.3-2 mm, ratio <= 1.4), FR4-like slab
+                      (eps_r 3.38, kappa 1e-3 S/m, 1.524 mm) with PEC ground + 32x40 mm patch,
+                      UPML 8 on all sides, 50 Ohm lumped port (f0 2 GHz, fc 1.5 GHz), port U/I
+                      probes and an NF2FF box (6 faces, E and H FD dumps) at 1.5/2/2.5 GHz.
+* ``stress``       -- 512x512x256 lines, 1 mm, 64 seeded random blocks (eps_r U[1,10],
+                      kappa U[0,0.1] S/m), 10 % of them Drude/Lorentz (plasma 1-10 GHz, damping
+                      1e8-1e9 1/s), first-order Mur on all walls, 4 seeded Gaussian point sources.
+* ``batch_instance`` -- one simulation of the batched form: lines U[48,160]^3, pitch 0.5-2 mm,
+                      UPML 8, one dielectric block eps_r U[2,12], a 50 Ohm lumped port with a
+                      Gaussian (f0 U[1,5] GHz, fc = f0/2), steps U[4000,12000].
+* ``smoke_case`` / ``cavity`` / ``small_mixed`` -- small cases for tests.
+
+Every builder accepts a ``scale`` (or explicit sizes) so the tests can run the same geometry
+at sizes the CPU checker finishes in seconds.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .excitation import Excitation
+from .operator import Grid, Operator, Structure
+
+
+# ------------------------------------------------------------------------------------------
+def _uniform(n, pitch=1.0):
+    return np.arange(n, dtype=np.float64) * pitch
+
+
+def graded_lines(n, fine_lo, fine_hi, d_fine, d_max, ratio=1.3, must=()):
+    """Exactly ``n`` lines: uniform spacing d_fine on [fine_lo, fine_hi] (plus the ``must``
+    coordinates), growing geometrically by ``ratio`` outward (capped at d_max), alternating
+    sides until n lines exist."""
+    core = list(np.arange(fine_lo, fine_hi + 0.5 * d_fine, d_fine))
+    core = sorted(set([round(c, 9) for c in core] + [round(m, 9) for m in must]))
+    lines = list(core)
+    dl = dh = d_fine
+    side = 0
+    while len(lines) < n:
+        if side == 0:
+            dl = min(dl * ratio, d_max)
+            lines.insert(0, lines[0] - dl)
+        else:
+            dh = min(dh * ratio, d_max)
+            lines.append(lines[-1] + dh)
+        side ^= 1
+    while len(lines) > n:
+        lines.pop(-1 if side else 0)
+        side ^= 1
+    return np.array(lines)
+
+
+# ------------------------------------------------------------------------------------------
+def plain_cube(n=100, steps=5000, pitch_mm=1.0):
+    """100^3 vacuum cube with PEC walls and a soft Ez point source at the centre edge."""
+    g = Grid([_uniform(n, pitch_mm)] * 3, unit=1e-3)
+    csx = Structure()
+    c = (n // 2) * pitch_mm
+    exc = Excitation()
+    exc.SetupGaussianPulse(2e9, 1e9)
+    csx.AddExcitation("excite", 0, [0, 0, 1]).AddBox([c, c, c], [c, c, c + pitch_mm])
+    csx.AddProbe("ut1", 0, weight=1.0, interval=1).AddBox([c, c, c - 2 * pitch_mm], [c, c, c + 3 * pitch_mm])
+    h = 0.5 * pitch_mm
+    csx.AddProbe("it1", 1, weight=1.0, norm_dir=2, interval=1).AddBox([c - h, c - h, c + h], [c + h, c + h, c + h])
+    op = Operator(csx, g, exc, bc=(0,) * 6)
+    return op.build(steps)
+
+
+def smoke_case(n=(17, 13, 15), steps=60):
+    """Small mixed case touching UPML, Mur, a dielectric block and both probe types."""
+    lines = [_uniform(k, 1.0) for k in n]
+    g = Grid(lines, unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(8e9, 6e9)
+    csx.AddMaterial("diel", epsilon=3.0, kappa=0.02).AddBox([4, 3, 3], [9, 8, 9])
+    c = [k // 2 for k in n]
+    csx.AddExcitation("excite", 0, [0, 0, 1]).AddBox([c[0], c[1], c[2]], [c[0], c[1], c[2] + 1])
+    csx.AddProbe("ut1", 0, interval=1).AddBox([c[0], c[1], c[2] - 2], [c[0], c[1], c[2] + 2])
+    csx.AddProbe("it1", 1, norm_dir=2, interval=1).AddBox([c[0] - .5, c[1] - .5, c[2] + .5], [c[0] + .5, c[1] + .5, c[2] + .5])
+    op = Operator(csx, g, exc, bc=(3, 0, 2, 2, 0, 3), pml_size=(4, 4, 4, 4, 4, 4))
+    return op.build(steps)
+
+
+def small_mixed(n=(18, 16, 14), steps=200, bc=(3, 3, 2, 2, 0, 3), pml=4, seed=1, dispersive=True, dump=True):
+    """Everything at once on a small mesh: UPML + Mur + PEC walls, dielectric and Drude/Lorentz
+    blocks, a metal plate, a lumped port with U/I probes and DFTs, and E/H FD dumps."""
+    rng = np.random.default_rng(seed)
+    lines = [np.cumsum(np.concatenate([[0.0], rng.uniform(0.6, 1.2, k - 1)])) for k in n]
+    g = Grid(lines, unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(6e9, 5e9)
+    L = [l[-1] for l in g.lines]
+    csx.AddMaterial("diel", epsilon=4.0, kappa=0.05).AddBox([0.3 * L[0], 0.2 * L[1], 0.2 * L[2]], [0.6 * L[0], 0.7 * L[1], 0.5 * L[2]])
+    if dispersive:
+        csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[5e9], eps_relax_time=[2e-9]).AddBox(
+            [0.55 * L[0], 0.4 * L[1], 0.4 * L[2]], [0.8 * L[0], 0.8 * L[1], 0.8 * L[2]], priority=5)
+        csx.AddLorentzMaterial("lor", epsilon=2.0, eps_plasma_freq=[8e9], eps_relax_time=[1e-9],
+                               eps_lor_pole_freq=[3e9]).AddBox([0.2 * L[0], 0.6 * L[1], 0.55 * L[2]],
+                                                              [0.4 * L[0], 0.85 * L[1], 0.75 * L[2]], priority=6)
+    csx.AddMetal("plate").AddBox([0.25 * L[0], 0.25 * L[1], 0.3 * L[2]], [0.45 * L[0], 0.45 * L[1], 0.3 * L[2]], priority=10)
+    gl = g.lines
+    px, py = gl[0][n[0] // 2], gl[1][n[1] // 2]
+    z0, z1 = gl[2][n[2] // 2 - 1], gl[2][n[2] // 2 + 1]
+    csx.AddLumpedElement("port_R", ny=2, R=50.0, caps=True).AddBox([px, py, z0], [px, py, z1], priority=20)
+    csx.AddExcitation("port_exc", 0, [0, 0, -1.0]).AddBox([px, py, z0], [px, py, z1], priority=20)
+    freqs = [3e9, 5e9, 7e9]
+    csx.AddProbe("port_ut", 0, weight=-1.0, interval=1, frequency=freqs).AddBox([px, py, z0], [px, py, z1])
+    zm = 0.5 * (z0 + z1)
+    csx.AddProbe("port_it", 1, weight=1.0, norm_dir=2, interval=1, frequency=freqs).AddBox([px, py, zm], [px, py, zm])
+    if dump:
+        lo = [l[2] for l in gl]
+        hi = [l[-3] for l in gl]
+        for f_idx, name in ((10, "nf2ff_E"), (11, "nf2ff_H")):
+            d = csx.AddDump(name, dump_type=f_idx, dump_mode=1, frequency=[4e9, 6e9])
+            d.AddBox([lo[0], lo[1], lo[2]], [hi[0], hi[1], lo[2]])
+            d.AddBox([lo[0], lo[1], lo[2]], [lo[0], hi[1], hi[2]])
+    op = Operator(csx, g, exc, bc=bc, pml_size=(pml,) * 6)
+    return op.build(steps)
+
+
+# ------------------------------------------------------------------------------------------
+def stress(shape=(512, 512, 256), steps=2000, nblocks=64, seed=20261204, pitch_mm=1.0):
+    """Bandwidth-stress mesh: random dielectric/lossy blocks, 10 % dispersive, Mur walls."""
+    rng = np.random.default_rng(seed)
+    g = Grid([_uniform(k, pitch_mm) for k in shape], unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(3e9, 2e9)
+    ndisp = max(1, int(round(0.1 * nblocks)))
+    disp = set(rng.choice(nblocks, size=ndisp, replace=False).tolist())
+    scale = min(shape) / 256.0
+    for b in range(nblocks):
+        side = rng.integers(max(2, int(16 * scale)), max(3, int(128 * scale)) + 1, size=3)
+        side = np.minimum(side, np.array(shape) - 2)
+        lo = np.array([rng.integers(0, shape[k] - side[k]) for k in range(3)])
+        hi = lo + side
+        eps = rng.uniform(1.0, 10.0)
+        kap = rng.uniform(0.0, 0.1)
+        start = lo * pitch_mm
+        stop = hi * pitch_mm
+        if b in disp:
+            fp = rng.uniform(1e9, 10e9)
+            tr = 1.0 / rng.uniform(1e8, 1e9)
+            if b % 2:
+                m = csx.AddLorentzMaterial(f"disp{b}", epsilon=eps, kappa=kap, eps_plasma_freq=[fp],
+                                           eps_relax_time=[tr], eps_lor_pole_freq=[0.5 * fp])
+            else:
+                m = csx.AddLorentzMaterial(f"disp{b}", epsilon=eps, kappa=kap, eps_plasma_freq=[fp],
+                                           eps_relax_time=[tr])
+        else:
+            m = csx.AddMaterial(f"blk{b}", epsilon=eps, kappa=kap)
+        m.AddBox(start, stop, priority=b)
+    for s in range(4):
+        p = np.array([rng.integers(8, shape[k] - 8) for k in range(3)])
+        d = int(rng.integers(0, 3))
+        val = [0.0, 0.0, 0.0]
+        val[d] = float(rng.choice([-1.0, 1.0]))
+        stop = p.astype(float).copy()
+        stop[d] += 1
+        csx.AddExcitation(f"src{s}", 0, val).AddBox(p * pitch_mm, stop * pitch_mm, priority=1000)
+        # a 3-edge voltage monitor through each source edge, sampled every step
+        a = p.astype(float).copy()
+        b = p.astype(float).copy()
+        a[d] -= 1
+        b[d] += 2
+        csx.AddProbe(f"mon{s}", 0, interval=1).AddBox(a * pitch_mm, b * pitch_mm)
+    op = Operator(csx, g, exc, bc=(2,) * 6)
+    return op.build(steps)
+
+
+# ------------------------------------------------------------------------------------------
+def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
+    """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""
+    nx, ny, nz = shape
+    sub_t = 1.524
+    patch_w, patch_l = 32.0, 40.0
+    sub_w = 60.0
+    feed = -6.0
+    xl = graded_lines(nx, -sub_w / 2, sub_w / 2, 0.5 * 160 / max(nx, 40) if nx < 160 else 0.5, 2.0, 1.3,
+                      must=(feed, -patch_w / 2, patch_w / 2))
+    yl = graded_lines(ny, -sub_w / 2, sub_w / 2, 0.5 * 160 / max(ny, 40) if ny < 160 else 0.5, 2.0, 1.3,
+                      must=(0.0, -patch_l / 2, patch_l / 2))
+    zfine = np.linspace(0.0, sub_t, 5)
+    zl = graded_lines(nz, 0.0, sub_t, sub_t / 4, 2.0, 1.35, must=tuple(zfine))
+    g = Grid([xl, yl, zl], unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(2e9, 1.5e9)
+    csx.AddMaterial("substrate", epsilon=3.38, kappa=1e-3).AddBox([-sub_w / 2, -sub_w / 2, 0], [sub_w / 2, sub_w / 2, sub_t])
+    csx.AddMetal("gnd").AddBox([-sub_w / 2, -sub_w / 2, 0], [sub_w / 2, sub_w / 2, 0], priority=10)
+    csx.AddMetal("patch").AddBox([-patch_w / 2, -patch_l / 2, sub_t], [patch_w / 2, patch_l / 2, sub_t], priority=10)
+    # 50 Ohm lumped port from ground to patch (python/openEMS/ports.py:155-209)
+    start, stop = np.array([feed, 0, 0]), np.array([feed, 0, sub_t])
+    csx.AddLumpedElement("port_resist", ny=2, R=50.0, caps=True).AddBox(start, stop, priority=5)
+    csx.AddExcitation("port_excite", 0, [0, 0, -1.0]).AddBox(start, stop, priority=5)
+    csx.AddProbe("port_ut1", 0, weight=-1.0, interval=1, frequency=[1.5e9, 2e9, 2.5e9]).AddBox(start, stop)
+    zm = 0.5 * sub_t
+    csx.AddProbe("port_it1", 1, weight=1.0, norm_dir=2, interval=1, frequency=[1.5e9, 2e9, 2.5e9]).AddBox(
+        [feed, 0, zm], [feed, 0, zm])
+    if with_nf2ff:
+        k = 11  # inside the 8-cell UPML
+        lo = [xl[k], yl[k], zl[k]]
+        hi = [xl[-k - 1], yl[-k - 1], zl[-k - 1]]
+        for dt, name in ((10, "nf2ff_E"), (11, "nf2ff_H")):
+            d = csx.AddDump(name, dump_type=dt, dump_mode=1, frequency=[1.5e9, 2e9, 2.5e9])
+            for ax in range(3):
+                for side in (lo, hi):
+                    a = list(lo)
+                    b = list(hi)
+                    a[ax] = b[ax] = side[ax]
+                    d.AddBox(a, b)
+    op = Operator(csx, g, exc, bc=(3,) * 6, pml_size=(8,) * 6)
+    return op.build(steps)
+
+
+# ------------------------------------------------------------------------------------------
+def cavity(steps=4000):
+    """The reference's resonance-test cavity (TESTSUITE/combinedtests/cavity.m:46-111): a PEC box
+    a=5 cm, b=2 cm, d=6 cm on 26x11x32 lines, Gaussian f0=fc=4.5 GHz, soft E source on the three
+    edges from the 2/3 point, Ex/Ey/Ez voltage probes."""
+    a, b, d = 5e-2, 2e-2, 6e-2
+    mx = np.linspace(0, a, 26)
+    my = np.linspace(0, b, 11)
+    mz = np.linspace(0, d, 32)
+    g = Grid([mx, my, mz], unit=1.0)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(4.5e9, 4.5e9)
+    i = [int(np.floor(len(m) * 2 / 3)) - 1 for m in (mx, my, mz)]
+    p1 = [mx[i[0]], my[i[1]], mz[i[2]]]
+    # the reference's curve from p1 to p1+one cell in every direction walks one edge per axis
+    csx.AddExcitation("excite_x", 0, [1, 0, 0]).AddBox(p1, [mx[i[0] + 1], my[i[1]], mz[i[2]]])
+    csx.AddExcitation("excite_y", 0, [0, 1, 0]).AddBox([mx[i[0] + 1], my[i[1]], mz[i[2]]], [mx[i[0] + 1], my[i[1] + 1], mz[i[2]]])
+    csx.AddExcitation("excite_z", 0, [0, 0, 1]).AddBox([mx[i[0] + 1], my[i[1] + 1], mz[i[2]]], [mx[i[0] + 1], my[i[1] + 1], mz[i[2] + 1]])
+    f = lambda m, frac: int(np.floor(len(m) * frac)) - 1  # noqa: E731  (MATLAB end*frac, 1-based)
+    csx.AddProbe("ut1x", 0, interval=1).AddBox([mx[f(mx, .25)], my[f(my, .5)], mz[f(mz, .2)]],
+                                              [mx[f(mx, .25) + 1], my[f(my, .5)], mz[f(mz, .2)]])
+    csx.AddProbe("ut1y", 0, interval=1).AddBox([mx[f(mx, .25)], my[f(my, .5)], mz[f(mz, .2)]],
+                                              [mx[f(mx, .25)], my[f(my, .5) + 1], mz[f(mz, .2)]])
+    csx.AddProbe("ut1z", 0, interval=1).AddBox([mx[f(mx, .5)], my[f(my, .5)], mz[f(mz, .2)]],
+                                              [mx[f(mx, .5)], my[f(my, .5)], mz[f(mz, .2) + 1]])
+    op = Operator(csx, g, exc, bc=(0,) * 6)
+    return op.build(steps)

@@ -1,0 +1,1131 @@
+// engine.cu -- host side of the GB300 EC-FDTD engine: the C ABI of include/oems_cuda.h.
+//
+// The engine owns device memory and one CUDA stream.  oems_cuda_init() uploads every table,
+// builds the per-step kernel sequence and captures it into CUDA graphs (1 step and a batch of
+// steps); oems_cuda_iterate() replays them.  The timestep counter numTS lives on the device
+// and is advanced by the last kernel of each step, so graph replays need no host round trip.
+//
+// Per-step kernel order (the reference's phase order, FDTD/engine.cpp:267-286 and the
+// extension priorities of FDTD/extensions/engine_extension.h:21-29):
+//   [Lorentz pre-V] [Mur pre] update_v(+UPML pre/post) [Mur post] [Lorentz apply-V]
+//   [Mur apply] [excitation V] [Lorentz pre-I] update_i(+UPML pre/post) [Lorentz apply-I]
+//   [excitation I] step_end(probes, FD dumps, ++numTS)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/oems_cuda.h"
+#include "kernels.cuh"
+
+using namespace oems;
+
+namespace {
+
+const double kPI = 3.14159265358979323846;  // M_PI as used by Common/processintegral.cpp:161
+
+struct UpmlHost {
+    unsigned start[3], nl[3];
+    std::vector<float> tab[6];  // vv, vvfo, vvfn, ii, iifo, iifn
+};
+struct MurHost {
+    int ny;
+    unsigned line, shift, start_ts;
+    std::vector<float> cP, cPP;
+};
+struct LorHost {
+    unsigned count;
+    std::vector<unsigned> pos;
+    int von, con, vlon, clon;
+    std::vector<float> vint, vext, vlor, iint, iext, ilor;
+};
+struct ProbeHost {
+    int type;
+    unsigned start[3], stop[3];
+    int nd, si[3], ei[3];
+    double weight;
+    unsigned interval, start_ts, stop_ts;
+    unsigned fd_interval = 0;
+    std::vector<double> freqs;
+};
+struct DumpHost {
+    int field;
+    unsigned start[3], stop[3];
+    unsigned fd_interval;
+    std::vector<double> freqs;
+    std::vector<double> el;  // edge lengths used by this field type, concatenated x,y,z
+};
+
+}  // namespace
+
+struct oems_cuda_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    unsigned N[3] = {0, 0, 0};
+    unsigned Pz = 0;
+    unsigned long long S = 0;
+    double dt = 0;
+    std::string err;
+
+    // fields
+    float* dV = nullptr;
+    float* dI = nullptr;
+
+    // operator
+    bool op_set = false;
+    bool compressed = false;
+    unsigned nclasses = 0;
+    unsigned* didx = nullptr;
+    float4* dtabV = nullptr;
+    float4* dtabI = nullptr;
+    float *dvv = nullptr, *dvi = nullptr, *dii = nullptr, *div = nullptr;
+
+    // extensions (host copies until init)
+    bool has_exc = false;
+    std::vector<unsigned long long> exc_voff, exc_ioff;
+    std::vector<float> exc_vamp, exc_iamp, sig_v, sig_i;
+    std::vector<unsigned> exc_vdelay, exc_idelay;
+    unsigned sig_len = 0, period = 0;
+    std::vector<UpmlHost> upml;
+    std::vector<MurHost> mur;
+    std::vector<LorHost> lor;
+    std::vector<ProbeHost> probes;
+    std::vector<DumpHost> dumps;
+
+    // device state after init
+    bool inited = false;
+    unsigned max_ts = 0;
+    unsigned* d_numTS = nullptr;
+    unsigned* d_blocks_done = nullptr;
+    unsigned host_numTS = 0;
+    GridDev grid{};
+    ExcDev excV{}, excI{};
+    MurDev murdev{};
+    std::vector<LorDev> lorV, lorI;
+    StepEndDev stepend{};
+    unsigned stepend_blocks = 1;
+    std::vector<ProbeDev> probe_dev;   // host mirror of device structs
+    std::vector<DumpDev> dump_dev;
+    unsigned launches = 0;
+    cudaGraphExec_t graph1 = nullptr;
+    cudaGraphExec_t graphK = nullptr;
+    unsigned K = 16;
+    double* d_energy_partial = nullptr;
+    unsigned energy_blocks = 0;
+
+    std::vector<void*> allocs;                            // freed on destroy
+    std::vector<std::pair<void*, size_t>> state;          // snapshot regions (device)
+};
+
+namespace {
+
+int fail(oems_cuda_engine* e, int code, const std::string& msg)
+{
+    if (e) e->err = msg;
+    return code;
+}
+
+int cuda_fail(oems_cuda_engine* e, cudaError_t c, const char* what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(c);
+    cudaGetLastError();
+    return fail(e, c == cudaErrorMemoryAllocation ? OEMS_ERR_NOMEM : OEMS_ERR_CUDA, m);
+}
+
+#define CK(call)                                             \
+    do {                                                     \
+        cudaError_t _c = (call);                             \
+        if (_c != cudaSuccess) return cuda_fail(e, _c, #call); \
+    } while (0)
+
+template <typename T>
+int dalloc(oems_cuda_engine* e, T** p, size_t count, bool zero = true, bool is_state = false)
+{
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    void* q = nullptr;
+    CK(cudaMalloc(&q, bytes));
+    e->allocs.push_back(q);
+    if (zero) CK(cudaMemsetAsync(q, 0, bytes, e->stream));
+    if (is_state) e->state.push_back({q, bytes});
+    *p = static_cast<T*>(q);
+    return OEMS_OK;
+}
+
+template <typename T>
+int dupload(oems_cuda_engine* e, T** p, const T* src, size_t count)
+{
+    int rc = dalloc(e, p, count, false);
+    if (rc) return rc;
+    if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, e->stream));
+    return OEMS_OK;
+}
+
+inline unsigned long long cell_off(const oems_cuda_engine* e, unsigned n, unsigned x, unsigned y, unsigned z)
+{
+    return (unsigned long long)n * e->S + ((unsigned long long)x * e->N[1] + y) * e->Pz + z;
+}
+
+// ---- operator compression (Operator_SSE_Compressed::CompressOperator restated per cell) ------
+struct Key12 {
+    uint32_t w[12];
+};
+
+uint64_t hash12(const Key12& k)
+{
+    uint64_t h = 1469598103934665603ULL;
+    for (int i = 0; i < 12; ++i) {
+        h ^= k.w[i];
+        h *= 1099511628211ULL;
+        h ^= h >> 31;
+    }
+    return h;
+}
+
+// classes numbered in order of first appearance (x, y, z loops), like the reference
+int compress_dense(oems_cuda_engine* e, const float* vv, const float* vi, const float* ii, const float* iv,
+                   unsigned max_classes, std::vector<unsigned>& index, std::vector<Key12>& keys)
+{
+    const unsigned Nx = e->N[0], Ny = e->N[1], Nz = e->N[2];
+    const size_t cells = (size_t)Nx * Ny * Nz;
+    index.assign((size_t)Nx * Ny * e->Pz, 0u);
+    keys.clear();
+    size_t hcap = 1u << 16;
+    std::vector<int64_t> htab(hcap, -1);
+    Key12 k;
+    for (unsigned x = 0; x < Nx; ++x)
+        for (unsigned y = 0; y < Ny; ++y)
+            for (unsigned z = 0; z < Nz; ++z) {
+                const size_t c = ((size_t)x * Ny + y) * Nz + z;
+                for (int n = 0; n < 3; ++n) {
+                    memcpy(&k.w[n], vv + n * cells + c, 4);
+                    memcpy(&k.w[3 + n], vi + n * cells + c, 4);
+                    memcpy(&k.w[6 + n], ii + n * cells + c, 4);
+                    memcpy(&k.w[9 + n], iv + n * cells + c, 4);
+                }
+                size_t slot = hash12(k) & (hcap - 1);
+                int64_t found = -1;
+                while (htab[slot] >= 0) {
+                    if (memcmp(&keys[htab[slot]], &k, sizeof(Key12)) == 0) { found = htab[slot]; break; }
+                    slot = (slot + 1) & (hcap - 1);
+                }
+                if (found < 0) {
+                    if (max_classes && keys.size() >= max_classes) return 1;  // too many: use dense
+                    found = (int64_t)keys.size();
+                    keys.push_back(k);
+                    htab[slot] = found;
+                    if (keys.size() * 2 > hcap) {
+                        hcap *= 4;
+                        htab.assign(hcap, -1);
+                        for (size_t j = 0; j < keys.size(); ++j) {
+                            size_t s2 = hash12(keys[j]) & (hcap - 1);
+                            while (htab[s2] >= 0) s2 = (s2 + 1) & (hcap - 1);
+                            htab[s2] = (int64_t)j;
+                        }
+                    }
+                }
+                index[((size_t)x * Ny + y) * e->Pz + z] = (unsigned)found;
+            }
+    return 0;
+}
+
+int upload_compressed(oems_cuda_engine* e, const std::vector<unsigned>& index, const std::vector<Key12>& keys)
+{
+    const size_t U = keys.size();
+    std::vector<float4> tv(2 * U), ti(2 * U);
+    for (size_t j = 0; j < U; ++j) {
+        float f[12];
+        memcpy(f, keys[j].w, 48);
+        tv[2 * j] = make_float4(f[0], f[1], f[2], f[3]);
+        tv[2 * j + 1] = make_float4(f[4], f[5], 0.f, 0.f);
+        ti[2 * j] = make_float4(f[6], f[7], f[8], f[9]);
+        ti[2 * j + 1] = make_float4(f[10], f[11], 0.f, 0.f);
+    }
+    int rc;
+    if ((rc = dupload(e, &e->didx, index.data(), index.size()))) return rc;
+    if ((rc = dupload(e, &e->dtabV, tv.data(), tv.size()))) return rc;
+    if ((rc = dupload(e, &e->dtabI, ti.data(), ti.size()))) return rc;
+    CK(cudaStreamSynchronize(e->stream));
+    e->compressed = true;
+    e->nclasses = (unsigned)U;
+    e->op_set = true;
+    return OEMS_OK;
+}
+
+int upload_dense(oems_cuda_engine* e, const float* src, float** dst)
+{
+    const unsigned Nx = e->N[0], Ny = e->N[1], Nz = e->N[2];
+    int rc = dalloc(e, dst, 3 * (size_t)e->S, true);
+    if (rc) return rc;
+    // 2-D copy: rows of Nz floats into rows of Pz floats
+    CK(cudaMemcpy2DAsync(*dst, e->Pz * sizeof(float), src, Nz * sizeof(float), Nz * sizeof(float),
+                         (size_t)3 * Nx * Ny, cudaMemcpyHostToDevice, e->stream));
+    return OEMS_OK;
+}
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+int oems_cuda_create(const unsigned int num_lines[3], double dt, int device, oems_cuda_engine** out)
+{
+    if (!num_lines || !out || !(dt > 0)) return OEMS_ERR_ARG;
+    for (int n = 0; n < 3; ++n)
+        if (num_lines[n] < 3 || num_lines[n] > 65535) return OEMS_ERR_ARG;
+    auto* e = new (std::nothrow) oems_cuda_engine();
+    if (!e) return OEMS_ERR_NOMEM;
+    *out = e;
+    e->device = device;
+    memcpy(e->N, num_lines, sizeof(e->N));
+    e->Pz = (num_lines[2] + 3u) & ~3u;
+    e->S = (unsigned long long)num_lines[0] * num_lines[1] * e->Pz;
+    e->dt = dt;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    int rc;
+    if ((rc = dalloc(e, &e->dV, 3 * (size_t)e->S, true, true))) return rc;
+    if ((rc = dalloc(e, &e->dI, 3 * (size_t)e->S, true, true))) return rc;
+    if ((rc = dalloc(e, &e->d_numTS, 1, true, true))) return rc;
+    if ((rc = dalloc(e, &e->d_blocks_done, 1, true))) return rc;
+    CK(cudaStreamSynchronize(e->stream));
+    return OEMS_OK;
+}
+
+void oems_cuda_destroy(oems_cuda_engine* e)
+{
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->graph1) cudaGraphExecDestroy(e->graph1);
+    if (e->graphK) cudaGraphExecDestroy(e->graphK);
+    for (void* p : e->allocs) cudaFree(p);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+const char* oems_cuda_last_error(const oems_cuda_engine* e)
+{
+    return e ? e->err.c_str() : "null engine handle";
+}
+
+int oems_cuda_set_operator(oems_cuda_engine* e, const float* vv, const float* vi, const float* ii, const float* iv,
+                           unsigned int max_classes)
+{
+    if (!e || !vv || !vi || !ii || !iv) return OEMS_ERR_ARG;
+    if (e->inited || e->op_set) return fail(e, OEMS_ERR_STATE, "operator already set");
+    CK(cudaSetDevice(e->device));
+    std::vector<unsigned> index;
+    std::vector<Key12> keys;
+    const unsigned cap = max_classes ? max_classes : (1u << 22);
+    if (compress_dense(e, vv, vi, ii, iv, cap, index, keys) == 0) return upload_compressed(e, index, keys);
+    index.clear();
+    keys.clear();
+    int rc;
+    if ((rc = upload_dense(e, vv, &e->dvv))) return rc;
+    if ((rc = upload_dense(e, vi, &e->dvi))) return rc;
+    if ((rc = upload_dense(e, ii, &e->dii))) return rc;
+    if ((rc = upload_dense(e, iv, &e->div))) return rc;
+    CK(cudaStreamSynchronize(e->stream));
+    e->compressed = false;
+    e->nclasses = 0;
+    e->op_set = true;
+    return OEMS_OK;
+}
+
+int oems_cuda_set_operator_sse_compressed(oems_cuda_engine* e, unsigned int U, const float* f4_vv, const float* f4_vi,
+                                          const float* f4_ii, const float* f4_iv, const unsigned int* op_index)
+{
+    if (!e || !f4_vv || !f4_vi || !f4_ii || !f4_iv || !op_index || U == 0) return OEMS_ERR_ARG;
+    if (e->inited || e->op_set) return fail(e, OEMS_ERR_STATE, "operator already set");
+    const unsigned Nx = e->N[0], Ny = e->N[1], Nz = e->N[2];
+    const unsigned nv = (Nz + 3) / 4;
+    const size_t cells = (size_t)Nx * Ny * Nz;
+    // expand the lane-strided 4-lane tables to per-cell N-I-J-K arrays, then compress per cell
+    std::vector<float> a[4];
+    for (auto& v : a) v.resize(3 * cells);
+    const float* src[4] = {f4_vv, f4_vi, f4_ii, f4_iv};
+    for (unsigned x = 0; x < Nx; ++x)
+        for (unsigned y = 0; y < Ny; ++y)
+            for (unsigned z = 0; z < Nz; ++z) {
+                const unsigned v = z % nv, l = z / nv;
+                const unsigned c = op_index[((size_t)x * Ny + y) * nv + v];
+                if (c >= U) return fail(e, OEMS_ERR_ARG, "op_index out of range");
+                for (int t = 0; t < 4; ++t)
+                    for (int n = 0; n < 3; ++n)
+                        a[t][n * cells + ((size_t)x * Ny + y) * Nz + z] = src[t][((size_t)n * U + c) * 4 + l];
+            }
+    return oems_cuda_set_operator(e, a[0].data(), a[1].data(), a[2].data(), a[3].data(), 0);
+}
+
+int oems_cuda_operator_classes(const oems_cuda_engine* e, unsigned int* nc)
+{
+    if (!e || !nc) return OEMS_ERR_ARG;
+    *nc = e->compressed ? e->nclasses : 0;
+    return OEMS_OK;
+}
+
+int oems_cuda_set_excitation(oems_cuda_engine* e, unsigned int nV, const unsigned int* v_idx, const unsigned short* v_dir,
+                             const float* v_amp, const unsigned int* v_delay, unsigned int nI,
+                             const unsigned int* i_idx, const unsigned short* i_dir, const float* i_amp,
+                             const unsigned int* i_delay, const float* sig_v, const float* sig_i,
+                             unsigned int length, unsigned int period)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if ((nV || nI) && (length == 0 || !sig_v || !sig_i)) return fail(e, OEMS_ERR_ARG, "excitation signal missing");
+    if ((nV && (!v_idx || !v_dir || !v_amp || !v_delay)) || (nI && (!i_idx || !i_dir || !i_amp || !i_delay)))
+        return fail(e, OEMS_ERR_ARG, "excitation arrays missing");
+    e->exc_voff.clear(); e->exc_ioff.clear();
+    for (unsigned k = 0; k < nV; ++k) {
+        const unsigned x = v_idx[k], y = v_idx[nV + k], z = v_idx[2 * nV + k];
+        if (x >= e->N[0] || y >= e->N[1] || z >= e->N[2] || v_dir[k] > 2)
+            return fail(e, OEMS_ERR_ARG, "voltage excitation index out of range");
+        e->exc_voff.push_back(cell_off(e, v_dir[k], x, y, z));
+    }
+    for (unsigned k = 0; k < nI; ++k) {
+        const unsigned x = i_idx[k], y = i_idx[nI + k], z = i_idx[2 * nI + k];
+        if (x >= e->N[0] || y >= e->N[1] || z >= e->N[2] || i_dir[k] > 2)
+            return fail(e, OEMS_ERR_ARG, "current excitation index out of range");
+        e->exc_ioff.push_back(cell_off(e, i_dir[k], x, y, z));
+    }
+    e->exc_vamp.assign(v_amp, v_amp + nV);
+    e->exc_iamp.assign(i_amp, i_amp + nI);
+    e->exc_vdelay.assign(v_delay, v_delay + nV);
+    e->exc_idelay.assign(i_delay, i_delay + nI);
+    e->sig_v.assign(sig_v, sig_v + length);
+    e->sig_i.assign(sig_i, sig_i + length);
+    e->sig_len = length;
+    e->period = period;
+    e->has_exc = true;
+    return OEMS_OK;
+}
+
+int oems_cuda_add_upml(oems_cuda_engine* e, const unsigned int start[3], const unsigned int nl[3], const float* vv,
+                       const float* vvfo, const float* vvfn, const float* ii, const float* iifo, const float* iifn)
+{
+    if (!e || !start || !nl || !vv || !vvfo || !vvfn || !ii || !iifo || !iifn) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if (e->upml.size() >= OEMS_MAX_UPML) return fail(e, OEMS_ERR_UNSUPPORTED, "more than 6 UPML regions");
+    for (int n = 0; n < 3; ++n)
+        if (nl[n] == 0 || start[n] + nl[n] > e->N[n]) return fail(e, OEMS_ERR_ARG, "UPML region outside the mesh");
+    for (const auto& u : e->upml) {
+        bool overlap = true;
+        for (int n = 0; n < 3; ++n)
+            overlap &= start[n] < u.start[n] + u.nl[n] && u.start[n] < start[n] + nl[n];
+        if (overlap) return fail(e, OEMS_ERR_ARG, "UPML regions overlap");
+    }
+    UpmlHost u;
+    memcpy(u.start, start, 12);
+    memcpy(u.nl, nl, 12);
+    const size_t m = 3 * (size_t)nl[0] * nl[1] * nl[2];
+    const float* src[6] = {vv, vvfo, vvfn, ii, iifo, iifn};
+    for (int t = 0; t < 6; ++t) u.tab[t].assign(src[t], src[t] + m);
+    e->upml.push_back(std::move(u));
+    return OEMS_OK;
+}
+
+int oems_cuda_add_mur(oems_cuda_engine* e, int ny, unsigned int line, unsigned int shift, unsigned int start_ts,
+                      const float* cP, const float* cPP)
+{
+    if (!e || !cP || !cPP || ny < 0 || ny > 2) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if (e->mur.size() >= OEMS_MAX_MUR) return fail(e, OEMS_ERR_UNSUPPORTED, "more than 6 Mur walls");
+    if (line >= e->N[ny] || shift >= e->N[ny]) return fail(e, OEMS_ERR_ARG, "Mur line outside the mesh");
+    MurHost m;
+    m.ny = ny; m.line = line; m.shift = shift; m.start_ts = start_ts;
+    const size_t n = (size_t)e->N[(ny + 1) % 3] * e->N[(ny + 2) % 3];
+    m.cP.assign(cP, cP + n);
+    m.cPP.assign(cPP, cPP + n);
+    e->mur.push_back(std::move(m));
+    return OEMS_OK;
+}
+
+int oems_cuda_add_lorentz_order(oems_cuda_engine* e, unsigned int count, const unsigned int* pos, int von, int con,
+                                int vlon, int clon, const float* vint, const float* vext, const float* vlor,
+                                const float* iint, const float* iext, const float* ilor)
+{
+    if (!e || (count && !pos)) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if ((von && (!vint || !vext)) || (con && (!iint || !iext)) || (von && vlon && !vlor) || (con && clon && !ilor))
+        return fail(e, OEMS_ERR_ARG, "dispersive coefficient table missing");
+    LorHost l;
+    l.count = count;
+    l.pos.assign(pos, pos + 3 * (size_t)count);
+    for (unsigned i = 0; i < count; ++i)
+        for (int a = 0; a < 3; ++a)
+            if (pos[a * count + i] >= e->N[a]) return fail(e, OEMS_ERR_ARG, "dispersive position outside the mesh");
+    l.von = von; l.con = con; l.vlon = vlon && von; l.clon = clon && con;
+    const size_t m = 3 * (size_t)count;
+    if (von) { l.vint.assign(vint, vint + m); l.vext.assign(vext, vext + m); }
+    if (l.vlon) l.vlor.assign(vlor, vlor + m);
+    if (con) { l.iint.assign(iint, iint + m); l.iext.assign(iext, iext + m); }
+    if (l.clon) l.ilor.assign(ilor, ilor + m);
+    e->lor.push_back(std::move(l));
+    return OEMS_OK;
+}
+
+static int add_probe(oems_cuda_engine* e, int type, const unsigned* start, const unsigned* stop, int nd,
+                     const int* si, const int* ei, double weight, unsigned interval, unsigned start_ts,
+                     unsigned stop_ts, int* id)
+{
+    if (!e || !start || !stop || !id) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    for (int a = 0; a < 3; ++a)
+        if (start[a] >= e->N[a] || stop[a] >= e->N[a]) return fail(e, OEMS_ERR_ARG, "probe outside the mesh");
+    if (type == 0 && ((start[0] != stop[0]) + (start[1] != stop[1]) + (start[2] != stop[2])) != 1)
+        return fail(e, OEMS_ERR_ARG, "only a 1D/line voltage integration is allowed");
+    if (type == 1 && (nd < 0 || nd > 2)) return fail(e, OEMS_ERR_ARG, "invalid current probe normal direction");
+    ProbeHost p;
+    p.type = type;
+    memcpy(p.start, start, 12);
+    memcpy(p.stop, stop, 12);
+    p.nd = nd;
+    for (int a = 0; a < 3; ++a) { p.si[a] = si ? si[a] : 1; p.ei[a] = ei ? ei[a] : 1; }
+    p.weight = weight;
+    p.interval = interval ? interval : 1;
+    p.start_ts = start_ts;
+    p.stop_ts = stop_ts;
+    *id = (int)e->probes.size();
+    e->probes.push_back(std::move(p));
+    return OEMS_OK;
+}
+
+int oems_cuda_add_voltage_probe(oems_cuda_engine* e, const unsigned int start[3], const unsigned int stop[3],
+                                double weight, unsigned int interval, unsigned int start_ts, unsigned int stop_ts,
+                                int* id)
+{
+    return add_probe(e, 0, start, stop, -1, nullptr, nullptr, weight, interval, start_ts, stop_ts, id);
+}
+
+int oems_cuda_add_current_probe(oems_cuda_engine* e, const unsigned int start[3], const unsigned int stop[3],
+                                int norm_dir, const int start_inside[3], const int stop_inside[3], double weight,
+                                unsigned int interval, unsigned int start_ts, unsigned int stop_ts, int* id)
+{
+    return add_probe(e, 1, start, stop, norm_dir, start_inside, stop_inside, weight, interval, start_ts, stop_ts, id);
+}
+
+int oems_cuda_set_probe_dft(oems_cuda_engine* e, int id, unsigned int fd_interval, unsigned int nf,
+                            const double* freqs)
+{
+    if (!e || id < 0 || id >= (int)e->probes.size() || (nf && !freqs)) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    e->probes[id].fd_interval = fd_interval;
+    e->probes[id].freqs.assign(freqs, freqs + nf);
+    return OEMS_OK;
+}
+
+int oems_cuda_add_fd_dump(oems_cuda_engine* e, int field, const unsigned int start[3], const unsigned int stop[3],
+                          unsigned int fd_interval, unsigned int nf, const double* freqs, const double* el,
+                          const double* del, int* id)
+{
+    if (!e || !start || !stop || !el || !del || !id || (field != 0 && field != 1) || (nf && !freqs))
+        return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    DumpHost d;
+    d.field = field;
+    for (int a = 0; a < 3; ++a) {
+        if (start[a] > stop[a] || stop[a] >= e->N[a]) return fail(e, OEMS_ERR_ARG, "dump box outside the mesh");
+        d.start[a] = start[a];
+        d.stop[a] = stop[a];
+    }
+    d.fd_interval = fd_interval;
+    d.freqs.assign(freqs, freqs + nf);
+    const size_t tot = (size_t)e->N[0] + e->N[1] + e->N[2];
+    d.el.assign(field == 0 ? el : del, (field == 0 ? el : del) + tot);
+    *id = (int)e->dumps.size();
+    e->dumps.push_back(std::move(d));
+    return OEMS_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// init: upload, build device structs, capture graphs
+
+struct StepProfiler {
+    cudaEvent_t ev[2 * 64];
+    int cls[64];
+    int n = 0;
+};
+
+static int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof = nullptr)
+{
+    const GridDev& g = e->grid;
+    const unsigned plane = e->N[1] * e->Pz;
+    const dim3 blk(256);
+    const dim3 gv((plane + 255) / 256, e->N[0]);
+    const dim3 gi((plane + 255) / 256, e->N[0] - 1);
+    unsigned L = 0;
+    const bool up = !e->upml.empty();
+    cudaStream_t s = e->stream;
+    // optional per-launch events (profiling path only, never inside a captured graph)
+    auto pre = [&](int k) {
+        if (prof && prof->n < 64) { prof->cls[prof->n] = k; cudaEventRecord(prof->ev[2 * prof->n], s); }
+    };
+    auto post = [&]() {
+        if (prof && prof->n < 64) { cudaEventRecord(prof->ev[2 * prof->n + 1], s); ++prof->n; }
+    };
+    // ---- voltages
+    for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
+    unsigned mur_pts = 0;
+    for (const auto& m : e->mur) mur_pts = std::max<unsigned>(mur_pts, (unsigned)m.cP.size());
+    if (!e->mur.empty()) {
+        pre(OEMS_KC_MUR);
+        k_mur<<<dim3((mur_pts + 255) / 256, (unsigned)e->mur.size()), blk, 0, s>>>(g, e->murdev, 0, e->d_numTS); ++L;
+        post();
+    }
+    pre(OEMS_KC_UPDATE_V);
+    if (e->compressed) {
+        if (up) k_update_v<true, true><<<gv, blk, 0, s>>>(g);
+        else k_update_v<true, false><<<gv, blk, 0, s>>>(g);
+    } else {
+        if (up) k_update_v<false, true><<<gv, blk, 0, s>>>(g);
+        else k_update_v<false, false><<<gv, blk, 0, s>>>(g);
+    }
+    post();
+    ++L;
+    if (!e->mur.empty()) {
+        pre(OEMS_KC_MUR);
+        k_mur<<<dim3((mur_pts + 255) / 256, (unsigned)e->mur.size()), blk, 0, s>>>(g, e->murdev, 1, e->d_numTS); ++L;
+        post();
+    }
+    for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
+    if (!e->mur.empty()) {
+        pre(OEMS_KC_MUR);
+        k_mur<<<dim3((mur_pts + 255) / 256, (unsigned)e->mur.size()), blk, 0, s>>>(g, e->murdev, 2, e->d_numTS); ++L;
+        post();
+    }
+    if (e->excV.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excV.count + 127) / 128, 128, 0, s>>>(e->dV, e->excV, e->d_numTS); post(); ++L; }
+    // ---- currents
+    for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
+    pre(OEMS_KC_UPDATE_I);
+    if (e->compressed) {
+        if (up) k_update_i<true, true><<<gi, blk, 0, s>>>(g);
+        else k_update_i<true, false><<<gi, blk, 0, s>>>(g);
+    } else {
+        if (up) k_update_i<false, true><<<gi, blk, 0, s>>>(g);
+        else k_update_i<false, false><<<gi, blk, 0, s>>>(g);
+    }
+    post();
+    ++L;
+    for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
+    if (e->excI.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excI.count + 127) / 128, 128, 0, s>>>(e->dI, e->excI, e->d_numTS); post(); ++L; }
+    // ---- processing + numTS
+    pre(OEMS_KC_STEP_END);
+    k_step_end<<<e->stepend_blocks, blk, 0, s>>>(g, e->stepend); ++L;
+    post();
+    if (nlaunch) *nlaunch = L;
+    cudaError_t c = cudaGetLastError();
+    if (c != cudaSuccess) return cuda_fail(e, c, "kernel launch");
+    return OEMS_OK;
+}
+
+static int capture(oems_cuda_engine* e, unsigned steps, cudaGraphExec_t* out)
+{
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = OEMS_OK;
+    for (unsigned s = 0; s < steps && rc == OEMS_OK; ++s) rc = enqueue_step(e, s == 0 ? &e->launches : nullptr);
+    cudaError_t c = cudaStreamEndCapture(e->stream, &graph);
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (c != cudaSuccess) return cuda_fail(e, c, "cudaStreamEndCapture");
+    c = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (c != cudaSuccess) return cuda_fail(e, c, "cudaGraphInstantiate");
+    return OEMS_OK;
+}
+
+int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if (!e->op_set) return fail(e, OEMS_ERR_STATE, "operator not set");
+    CK(cudaSetDevice(e->device));
+    int rc;
+    e->max_ts = max_ts;
+    GridDev& g = e->grid;
+    g.Nx = e->N[0]; g.Ny = e->N[1]; g.Nz = e->N[2]; g.Pz = e->Pz; g.S = e->S;
+    g.V = e->dV; g.I = e->dI;
+    g.idx = e->didx; g.tabV = e->dtabV; g.tabI = e->dtabI;
+    g.vv = e->dvv; g.vi = e->dvi; g.ii = e->dii; g.iv = e->div;
+
+    // UPML
+    g.nupml = (int)e->upml.size();
+    for (size_t r = 0; r < e->upml.size(); ++r) {
+        const UpmlHost& u = e->upml[r];
+        UpmlDev& d = g.upml[r];
+        memcpy(d.start, u.start, 12);
+        memcpy(d.nl, u.nl, 12);
+        d.n = u.nl[0] * u.nl[1] * u.nl[2];
+        float* t[6];
+        for (int k = 0; k < 6; ++k)
+            if ((rc = dupload(e, &t[k], u.tab[k].data(), u.tab[k].size()))) return rc;
+        d.vv = t[0]; d.vvfo = t[1]; d.vvfn = t[2]; d.ii = t[3]; d.iifo = t[4]; d.iifn = t[5];
+        if ((rc = dalloc(e, &d.vflux, 3 * (size_t)d.n, true, true))) return rc;
+        if ((rc = dalloc(e, &d.iflux, 3 * (size_t)d.n, true, true))) return rc;
+    }
+
+    // excitation
+    auto setup_exc = [&](ExcDev& x, const std::vector<unsigned long long>& off, const std::vector<float>& amp,
+                         const std::vector<unsigned>& delay, const std::vector<float>& sig) -> int {
+        x.count = (unsigned)off.size();
+        x.length = e->sig_len;
+        x.period = e->period;
+        if (!x.count) return OEMS_OK;
+        int r2;
+        unsigned long long* o; float* a; unsigned* dl; float* sg;
+        if ((r2 = dupload(e, &o, off.data(), off.size()))) return r2;
+        if ((r2 = dupload(e, &a, amp.data(), amp.size()))) return r2;
+        if ((r2 = dupload(e, &dl, delay.data(), delay.size()))) return r2;
+        if ((r2 = dupload(e, &sg, sig.data(), sig.size()))) return r2;
+        x.off = o; x.amp = a; x.delay = dl; x.sig = sg;
+        return OEMS_OK;
+    };
+    if ((rc = setup_exc(e->excV, e->exc_voff, e->exc_vamp, e->exc_vdelay, e->sig_v))) return rc;
+    if ((rc = setup_exc(e->excI, e->exc_ioff, e->exc_iamp, e->exc_idelay, e->sig_i))) return rc;
+
+    // Mur
+    e->murdev.nwall = (int)e->mur.size();
+    for (size_t w = 0; w < e->mur.size(); ++w) {
+        const MurHost& m = e->mur[w];
+        MurWallDev& d = e->murdev.w[w];
+        d.ny = m.ny; d.nyP = (m.ny + 1) % 3; d.nyPP = (m.ny + 2) % 3;
+        d.line = m.line; d.shift = m.shift; d.start_ts = m.start_ts;
+        d.n1 = e->N[d.nyP]; d.n2 = e->N[d.nyPP];
+        float *cp, *cpp;
+        if ((rc = dupload(e, &cp, m.cP.data(), m.cP.size()))) return rc;
+        if ((rc = dupload(e, &cpp, m.cPP.data(), m.cPP.size()))) return rc;
+        d.cP = cp; d.cPP = cpp;
+        if ((rc = dalloc(e, &d.bP, m.cP.size(), true, true))) return rc;
+        if ((rc = dalloc(e, &d.bPP, m.cP.size(), true, true))) return rc;
+    }
+
+    // Lorentz / Drude orders
+    for (const auto& l : e->lor) {
+        std::vector<unsigned long long> off(l.count);
+        for (unsigned i = 0; i < l.count; ++i) off[i] = cell_off(e, 0, l.pos[i], l.pos[l.count + i], l.pos[2 * l.count + i]);
+        unsigned long long* doff = nullptr;
+        if ((rc = dupload(e, &doff, off.data(), off.size()))) return rc;
+        const size_t m = 3 * (size_t)l.count;
+        if (l.von) {
+            LorDev d{};
+            d.count = l.count; d.off = doff; d.lor = l.vlon;
+            float *ci, *ce, *cl = nullptr;
+            if ((rc = dupload(e, &ci, l.vint.data(), m))) return rc;
+            if ((rc = dupload(e, &ce, l.vext.data(), m))) return rc;
+            if (l.vlon && (rc = dupload(e, &cl, l.vlor.data(), m))) return rc;
+            d.c_int = ci; d.c_ext = ce; d.c_lor = cl;
+            if ((rc = dalloc(e, &d.ade, m, true, true))) return rc;
+            if (l.vlon && (rc = dalloc(e, &d.lade, m, true, true))) return rc;
+            e->lorV.push_back(d);
+        }
+        if (l.con) {
+            LorDev d{};
+            d.count = l.count; d.off = doff; d.lor = l.clon;
+            float *ci, *ce, *cl = nullptr;
+            if ((rc = dupload(e, &ci, l.iint.data(), m))) return rc;
+            if ((rc = dupload(e, &ce, l.iext.data(), m))) return rc;
+            if (l.clon && (rc = dupload(e, &cl, l.ilor.data(), m))) return rc;
+            d.c_int = ci; d.c_ext = ce; d.c_lor = cl;
+            if ((rc = dalloc(e, &d.ade, m, true, true))) return rc;
+            if (l.clon && (rc = dalloc(e, &d.lade, m, true, true))) return rc;
+            e->lorI.push_back(d);
+        }
+    }
+
+    // probes: term lists in the reference's summation order + phasor tables
+    for (const auto& p : e->probes) {
+        ProbeDev d{};
+        d.type = p.type;
+        std::vector<unsigned long long> term;
+        std::vector<signed char> sign;
+        auto add = [&](int comp, unsigned x, unsigned y, unsigned z, int sg) {
+            term.push_back(cell_off(e, comp, x, y, z));
+            sign.push_back((signed char)sg);
+        };
+        if (p.type == 0) {  // Engine_Interface_FDTD::CalcVoltageIntegral
+            for (int n = 0; n < 3; ++n) {
+                if (p.start[n] < p.stop[n]) {
+                    unsigned pos[3] = {p.start[0], p.start[1], p.start[2]};
+                    for (; pos[n] < p.stop[n]; ++pos[n]) add(n, pos[0], pos[1], pos[2], +1);
+                } else {
+                    unsigned pos[3] = {p.stop[0], p.stop[1], p.stop[2]};
+                    for (; pos[n] < p.start[n]; ++pos[n]) add(n, pos[0], pos[1], pos[2], -1);
+                }
+            }
+        } else {  // ProcessCurrent::CalcIntegral
+            const unsigned *s = p.start, *t = p.stop;
+            const int *si = p.si, *ei = p.ei;
+            switch (p.nd) {
+            case 0:
+                if (ei[0] && si[2]) for (unsigned i = s[1] + 1; i <= t[1]; ++i) add(1, t[0], i, s[2], +1);
+                if (ei[0] && ei[1]) for (unsigned i = s[2] + 1; i <= t[2]; ++i) add(2, t[0], t[1], i, +1);
+                if (si[0] && ei[2]) for (unsigned i = s[1] + 1; i <= t[1]; ++i) add(1, s[0], i, t[2], -1);
+                if (si[0] && si[1]) for (unsigned i = s[2] + 1; i <= t[2]; ++i) add(2, s[0], s[1], i, -1);
+                break;
+            case 1:
+                if (si[0] && si[1]) for (unsigned i = s[2] + 1; i <= t[2]; ++i) add(2, s[0], s[1], i, +1);
+                if (ei[1] && ei[2]) for (unsigned i = s[0] + 1; i <= t[0]; ++i) add(0, i, t[1], t[2], +1);
+                if (ei[0] && ei[1]) for (unsigned i = s[2] + 1; i <= t[2]; ++i) add(2, t[0], t[1], i, -1);
+                if (si[1] && si[2]) for (unsigned i = s[0] + 1; i <= t[0]; ++i) add(0, i, s[1], s[2], -1);
+                break;
+            default:
+                if (si[1] && si[2]) for (unsigned i = s[0] + 1; i <= t[0]; ++i) add(0, i, s[1], s[2], +1);
+                if (ei[0] && si[2]) for (unsigned i = s[1] + 1; i <= t[1]; ++i) add(1, t[0], i, s[2], +1);
+                if (ei[1] && ei[2]) for (unsigned i = s[0] + 1; i <= t[0]; ++i) add(0, i, t[1], t[2], -1);
+                if (si[0] && ei[2]) for (unsigned i = s[1] + 1; i <= t[1]; ++i) add(1, s[0], i, t[2], -1);
+                break;
+            }
+        }
+        d.nterm = (unsigned)term.size();
+        unsigned long long* dt_; signed char* ds;
+        if ((rc = dupload(e, &dt_, term.data(), term.size()))) return rc;
+        if ((rc = dupload(e, &ds, sign.data(), sign.size()))) return rc;
+        d.term = dt_; d.sign = ds;
+        d.weight = p.weight;
+        d.interval = p.interval; d.start_ts = p.start_ts; d.stop_ts = p.stop_ts;
+        d.nslots = max_ts / p.interval + 1;
+        {
+            std::vector<double> nan(d.nslots, std::nan(""));
+            double* ser;
+            if ((rc = dupload(e, &ser, nan.data(), nan.size()))) return rc;
+            e->state.push_back({ser, nan.size() * sizeof(double)});
+            d.series = ser;
+        }
+        d.fd_interval = p.fd_interval;
+        d.nf = (unsigned)p.freqs.size();
+        d.dt = e->dt;
+        if (d.fd_interval && d.nf) {
+            d.nsamp = max_ts / d.fd_interval + 1;
+            std::vector<double2> ph((size_t)d.nsamp * d.nf);
+            for (unsigned k = 0; k < d.nsamp; ++k) {
+                const double ts = (double)k * d.fd_interval;
+                const double time = (ts + (double)(p.type == 1) * 0.5) * e->dt;
+                for (unsigned f = 0; f < d.nf; ++f) {
+                    const std::complex<double> ex = std::exp(std::complex<double>(-0.0, ((-2.0 * kPI) * p.freqs[f]) * time));
+                    ph[(size_t)k * d.nf + f] = make_double2(ex.real(), ex.imag());
+                }
+            }
+            double2* dph;
+            if ((rc = dupload(e, &dph, ph.data(), ph.size()))) return rc;
+            d.phasor = dph;
+            double* dd;
+            if ((rc = dalloc(e, &dd, 2 * (size_t)d.nf, true, true))) return rc;
+            d.dft = dd;
+        } else {
+            d.fd_interval = 0;
+            d.nf = 0;
+        }
+        e->probe_dev.push_back(d);
+    }
+
+    // FD dumps
+    std::vector<unsigned> block0(1, 1u);
+    for (const auto& p : e->dumps) {
+        DumpDev d{};
+        d.field = p.field;
+        for (int a = 0; a < 3; ++a) { d.start[a] = p.start[a]; d.sz[a] = p.stop[a] - p.start[a] + 1; }
+        d.npos = d.sz[0] * d.sz[1] * d.sz[2];
+        d.fd_interval = p.fd_interval;
+        d.nf = (unsigned)p.freqs.size();
+        if (d.fd_interval && d.nf) {
+            d.nsamp = max_ts / d.fd_interval + 1;
+            std::vector<float2> ph((size_t)d.nsamp * d.nf);
+            for (unsigned k = 0; k < d.nsamp; ++k) {
+                const double ts = (double)k * d.fd_interval;
+                const double T = (ts + (double)(p.field == 1) * 0.5) * e->dt;
+                for (unsigned f = 0; f < d.nf; ++f) {
+                    // ProcessFieldsFD::Process: exp in complex<float>, *2, *dt*FD_Interval
+                    std::complex<float> ex = std::exp(std::complex<float>(-0.0f, (float)(((-2.0 * kPI) * p.freqs[f]) * T)));
+                    ex *= 2.0f;
+                    ex *= (float)(e->dt * (double)d.fd_interval);
+                    ph[(size_t)k * d.nf + f] = make_float2(ex.real(), ex.imag());
+                }
+            }
+            float2* dph;
+            if ((rc = dupload(e, &dph, ph.data(), ph.size()))) return rc;
+            d.phasor = dph;
+        } else {
+            d.fd_interval = 0;
+            d.nf = 0;
+        }
+        double* del;
+        if ((rc = dupload(e, &del, p.el.data(), p.el.size()))) return rc;
+        d.el = del;
+        float2* acc;
+        if ((rc = dalloc(e, &acc, std::max<size_t>(1, (size_t)d.nf * 3 * d.npos), true, true))) return rc;
+        d.acc = acc;
+        e->dump_dev.push_back(d);
+        block0.push_back(block0.back() + (d.npos + 255) / 256);
+    }
+    StepEndDev& s = e->stepend;
+    s.nprobe = (int)e->probe_dev.size();
+    s.ndump = (int)e->dump_dev.size();
+    ProbeDev* dp = nullptr;
+    DumpDev* dd = nullptr;
+    unsigned* db0 = nullptr;
+    if ((rc = dupload(e, &dp, e->probe_dev.data(), e->probe_dev.size()))) return rc;
+    if ((rc = dupload(e, &dd, e->dump_dev.data(), e->dump_dev.size()))) return rc;
+    if ((rc = dupload(e, &db0, block0.data(), block0.size()))) return rc;
+    s.probes = dp; s.dumps = dd; s.dump_block0 = db0;
+    s.numTS = e->d_numTS;
+    s.blocks_done = e->d_blocks_done;
+    e->stepend_blocks = block0.back();
+
+    // energy scratch
+    e->energy_blocks = 1024;
+    if ((rc = dalloc(e, &e->d_energy_partial, 2 * (size_t)e->energy_blocks, true))) return rc;
+
+    CK(cudaStreamSynchronize(e->stream));
+
+    // probes at numTS = 0 (all fields zero): a step_end launch with numTS = -1 records slot 0
+    {
+        unsigned minus1 = 0xFFFFFFFFu;
+        CK(cudaMemcpyAsync(e->d_numTS, &minus1, 4, cudaMemcpyHostToDevice, e->stream));
+        k_step_end<<<e->stepend_blocks, 256, 0, e->stream>>>(e->grid, e->stepend);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    if ((rc = capture(e, 1, &e->graph1))) return rc;
+    if ((rc = capture(e, e->K, &e->graphK))) return rc;
+    e->inited = true;
+    return OEMS_OK;
+}
+
+int oems_cuda_iterate(oems_cuda_engine* e, unsigned int n)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    if ((unsigned long long)e->host_numTS + n > e->max_ts)
+        return fail(e, OEMS_ERR_ARG, "iterating beyond max_timesteps given to oems_cuda_init");
+    CK(cudaSetDevice(e->device));
+    unsigned done = 0;
+    while (n - done >= e->K) { CK(cudaGraphLaunch(e->graphK, e->stream)); done += e->K; }
+    while (done < n) { CK(cudaGraphLaunch(e->graph1, e->stream)); ++done; }
+    e->host_numTS += n;
+    return OEMS_OK;
+}
+
+int oems_cuda_sync(oems_cuda_engine* e)
+{
+    if (!e) return OEMS_ERR_ARG;
+    CK(cudaStreamSynchronize(e->stream));
+    return OEMS_OK;
+}
+
+unsigned int oems_cuda_num_timesteps(const oems_cuda_engine* e)
+{
+    return e ? e->host_numTS : 0;
+}
+
+int oems_cuda_timed_iterate(oems_cuda_engine* e, unsigned int n, float* ms)
+{
+    if (!e || !ms) return OEMS_ERR_ARG;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, e->stream));
+    int rc = oems_cuda_iterate(e, n);
+    CK(cudaEventRecord(b, e->stream));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
+}
+
+int oems_cuda_profile_steps(oems_cuda_engine* e, unsigned int n, float* ms, unsigned int* launches)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    if ((unsigned long long)e->host_numTS + n > e->max_ts)
+        return fail(e, OEMS_ERR_ARG, "iterating beyond max_timesteps given to oems_cuda_init");
+    CK(cudaSetDevice(e->device));
+    float acc[OEMS_KC_COUNT] = {0};
+    unsigned cnt[OEMS_KC_COUNT] = {0};
+    StepProfiler prof;
+    for (int i = 0; i < 128; ++i) CK(cudaEventCreate(&prof.ev[i]));
+    int rc = OEMS_OK;
+    for (unsigned st = 0; st < n && rc == OEMS_OK; ++st) {
+        prof.n = 0;
+        rc = enqueue_step(e, nullptr, &prof);
+        if (rc) break;
+        ++e->host_numTS;
+        cudaError_t c = cudaEventSynchronize(prof.ev[2 * prof.n - 1]);
+        if (c != cudaSuccess) { rc = cuda_fail(e, c, "profile sync"); break; }
+        for (int k = 0; k < prof.n; ++k) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, prof.ev[2 * k], prof.ev[2 * k + 1]);
+            acc[prof.cls[k]] += t;
+            ++cnt[prof.cls[k]];
+        }
+    }
+    for (int i = 0; i < 128; ++i) cudaEventDestroy(prof.ev[i]);
+    if (ms) for (int k = 0; k < OEMS_KC_COUNT; ++k) ms[k] = acc[k];
+    if (launches) for (int k = 0; k < OEMS_KC_COUNT; ++k) launches[k] = cnt[k];
+    return rc;
+}
+
+int oems_cuda_launches_per_step(const oems_cuda_engine* e, unsigned int* l)
+{
+    if (!e || !l) return OEMS_ERR_ARG;
+    *l = e->launches;
+    return OEMS_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// field access
+
+int oems_cuda_read_field(oems_cuda_engine* e, int which, float* out)
+{
+    if (!e || !out || (which != OEMS_VOLT && which != OEMS_CURR)) return OEMS_ERR_ARG;
+    CK(cudaSetDevice(e->device));
+    const float* src = which == OEMS_VOLT ? e->dV : e->dI;
+    CK(cudaMemcpy2DAsync(out, e->N[2] * sizeof(float), src, e->Pz * sizeof(float), e->N[2] * sizeof(float),
+                         (size_t)3 * e->N[0] * e->N[1], cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return OEMS_OK;
+}
+
+int oems_cuda_write_field(oems_cuda_engine* e, int which, const float* in)
+{
+    if (!e || !in || (which != OEMS_VOLT && which != OEMS_CURR)) return OEMS_ERR_ARG;
+    CK(cudaSetDevice(e->device));
+    float* dst = which == OEMS_VOLT ? e->dV : e->dI;
+    CK(cudaMemcpy2DAsync(dst, e->Pz * sizeof(float), in, e->N[2] * sizeof(float), e->N[2] * sizeof(float),
+                         (size_t)3 * e->N[0] * e->N[1], cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return OEMS_OK;
+}
+
+int oems_cuda_get_value(oems_cuda_engine* e, int which, unsigned n, unsigned x, unsigned y, unsigned z, float* v)
+{
+    if (!e || !v || n > 2 || x >= e->N[0] || y >= e->N[1] || z >= e->N[2]) return OEMS_ERR_ARG;
+    const float* src = (which == OEMS_VOLT ? e->dV : e->dI) + cell_off(e, n, x, y, z);
+    CK(cudaMemcpyAsync(v, src, 4, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return OEMS_OK;
+}
+
+int oems_cuda_set_value(oems_cuda_engine* e, int which, unsigned n, unsigned x, unsigned y, unsigned z, float v)
+{
+    if (!e || n > 2 || x >= e->N[0] || y >= e->N[1] || z >= e->N[2]) return OEMS_ERR_ARG;
+    float* dst = (which == OEMS_VOLT ? e->dV : e->dI) + cell_off(e, n, x, y, z);
+    CK(cudaMemcpyAsync(dst, &v, 4, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return OEMS_OK;
+}
+
+int oems_cuda_read_probe(oems_cuda_engine* e, int id, double* out, size_t cap, size_t* count)
+{
+    if (!e || !out || !count || id < 0 || id >= (int)e->probe_dev.size()) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    const ProbeDev& d = e->probe_dev[id];
+    const size_t n = std::min<size_t>(cap, d.nslots);
+    CK(cudaMemcpyAsync(out, d.series, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    *count = n;
+    return OEMS_OK;
+}
+
+int oems_cuda_read_probe_range(oems_cuda_engine* e, int id, size_t first, size_t count, double* out)
+{
+    if (!e || (!out && count) || id < 0 || id >= (int)e->probe_dev.size()) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    const ProbeDev& d = e->probe_dev[id];
+    if (first + count > d.nslots) return fail(e, OEMS_ERR_ARG, "probe slot range out of bounds");
+    if (count) {
+        CK(cudaMemcpyAsync(out, d.series + first, count * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    return OEMS_OK;
+}
+
+int oems_cuda_read_probe_dft(oems_cuda_engine* e, int id, double* out)
+{
+    if (!e || !out || id < 0 || id >= (int)e->probe_dev.size()) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    const ProbeDev& d = e->probe_dev[id];
+    if (d.nf) {
+        CK(cudaMemcpyAsync(out, d.dft, 2 * d.nf * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    return OEMS_OK;
+}
+
+int oems_cuda_read_fd_dump(oems_cuda_engine* e, int id, float* out, size_t cap)
+{
+    if (!e || !out || id < 0 || id >= (int)e->dump_dev.size()) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    const DumpDev& d = e->dump_dev[id];
+    const size_t n = (size_t)d.nf * 3 * d.npos * 2;
+    if (cap < n) return fail(e, OEMS_ERR_ARG, "output buffer too small");
+    if (n) {
+        CK(cudaMemcpyAsync(out, d.acc, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    return OEMS_OK;
+}
+
+int oems_cuda_energy(oems_cuda_engine* e, double* out)
+{
+    if (!e || !out) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    k_energy<<<e->energy_blocks, 256, 0, e->stream>>>(e->grid, e->d_energy_partial);
+    CK(cudaGetLastError());
+    std::vector<double> part(2 * (size_t)e->energy_blocks);
+    CK(cudaMemcpyAsync(part.data(), e->d_energy_partial, part.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    double E = 0, H = 0;
+    for (unsigned b = 0; b < e->energy_blocks; ++b) { E += part[2 * b]; H += part[2 * b + 1]; }
+    *out = 8.85418781762e-12 * E + 1.256637062e-6 * H;
+    return OEMS_OK;
+}
+
+int oems_cuda_snapshot_size(const oems_cuda_engine* e, size_t* bytes)
+{
+    if (!e || !bytes) return OEMS_ERR_ARG;
+    size_t b = 0;
+    for (const auto& r : e->state) b += r.second;
+    *bytes = b + sizeof(unsigned);
+    return OEMS_OK;
+}
+
+int oems_cuda_snapshot(oems_cuda_engine* e, void* host, size_t bytes)
+{
+    size_t need = 0;
+    if (!e || !host || oems_cuda_snapshot_size(e, &need) || bytes < need) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    char* p = static_cast<char*>(host);
+    for (const auto& r : e->state) {
+        CK(cudaMemcpyAsync(p, r.first, r.second, cudaMemcpyDeviceToHost, e->stream));
+        p += r.second;
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    memcpy(p, &e->host_numTS, sizeof(unsigned));
+    return OEMS_OK;
+}
+
+int oems_cuda_restore(oems_cuda_engine* e, const void* host, size_t bytes)
+{
+    size_t need = 0;
+    if (!e || !host || oems_cuda_snapshot_size(e, &need) || bytes < need) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    const char* p = static_cast<const char*>(host);
+    for (const auto& r : e->state) {
+        CK(cudaMemcpyAsync(r.first, p, r.second, cudaMemcpyHostToDevice, e->stream));
+        p += r.second;
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    memcpy(&e->host_numTS, p, sizeof(unsigned));
+    return OEMS_OK;
+}
+
+}  // extern "C"

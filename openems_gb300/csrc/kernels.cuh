@@ -1,0 +1,553 @@
+// kernels.cuh -- device code of the GB300 EC-FDTD engine (sm_103a).
+//
+// Arithmetic rule: every float/double operation that the reference writes as a separate
+// multiply and add/sub is issued with the _rn intrinsics (__fmul_rn, __fadd_rn, __fsub_rn,
+// __dmul_rn, __dadd_rn) so the compiler cannot contract it into an FMA.  Together with the
+// default -ftz=false this reproduces the reference's FP32 engine (FDTD/engine.cpp:110-222) bit
+// for bit.  The kernels are memory-bound; the extra instruction cost is hidden.
+//
+// Field layout in HBM: float [3][Nx][Ny][Pz], Pz = Nz rounded up to a multiple of 4 so every
+// z-row starts on a 16-byte boundary (padding lanes are never read as neighbours of real cells
+// and stay zero).  Component stride S = Nx*Ny*Pz.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define OEMS_MAX_UPML 6
+#define OEMS_MAX_MUR 6
+
+namespace oems {
+
+struct UpmlDev {
+    unsigned start[3];
+    unsigned nl[3];
+    unsigned n;                 // nl[0]*nl[1]*nl[2]
+    const float* vv;            // [3][n] each
+    const float* vvfo;
+    const float* vvfn;
+    const float* ii;
+    const float* iifo;
+    const float* iifn;
+    float* vflux;
+    float* iflux;
+};
+
+struct GridDev {
+    unsigned Nx, Ny, Nz, Pz;
+    unsigned long long S;       // component stride
+    float* V;
+    float* I;
+    // coefficients: compressed (idx != nullptr) or dense
+    const unsigned* idx;        // [Nx][Ny][Pz]
+    const float4* tabV;         // [U][2]: (vv0,vv1,vv2,vi0) (vi1,vi2,-,-)
+    const float4* tabI;         // [U][2]: (ii0,ii1,ii2,iv0) (iv1,iv2,-,-)
+    const float* vv;            // dense [3][S]
+    const float* vi;
+    const float* ii;
+    const float* iv;
+    int nupml;
+    UpmlDev upml[OEMS_MAX_UPML];
+};
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// returns region index and local linear offset (without component) or -1
+__device__ __forceinline__ int upml_find(const GridDev& g, unsigned x, unsigned y, unsigned z, unsigned& loc)
+{
+#pragma unroll
+    for (int r = 0; r < OEMS_MAX_UPML; ++r) {
+        if (r >= g.nupml) break;
+        const UpmlDev& u = g.upml[r];
+        unsigned lx = x - u.start[0], ly = y - u.start[1], lz = z - u.start[2];
+        if (lx < u.nl[0] && ly < u.nl[1] && lz < u.nl[2]) {
+            loc = (lx * u.nl[1] + ly) * u.nl[2] + lz;
+            return r;
+        }
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Engine::UpdateVoltages (FDTD/engine.cpp:110-168) fused with Engine_Ext_UPML pre/post voltage
+// updates (FDTD/extensions/engine_ext_upml.cpp:52-137).  One thread per cell of an x-plane
+// (blockIdx.y = x), z fastest for coalescing.
+template <bool COMPRESSED, bool UPML>
+__global__ void __launch_bounds__(256) k_update_v(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned y = t / g.Pz, z = t - y * g.Pz;
+    if (y >= g.Ny || z >= g.Nz) return;
+    const unsigned long long S = g.S;
+    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
+    const unsigned long long sx = x ? (unsigned long long)g.Ny * g.Pz : 0ull;
+    const unsigned long long sy = y ? (unsigned long long)g.Pz : 0ull;
+    const unsigned long long sz = z ? 1ull : 0ull;
+    const float* __restrict__ I = g.I;
+    float* __restrict__ V = g.V;
+
+    const float i0 = __ldg(I + o), i1 = __ldg(I + S + o), i2 = __ldg(I + 2 * S + o);
+    // curl terms in the reference's evaluation order ((a - b) - c) + d
+    const float c0 = fadd(fsub(fsub(i2, __ldg(I + 2 * S + o - sy)), i1), __ldg(I + S + o - sz));
+    const float c1 = fadd(fsub(fsub(i0, __ldg(I + o - sz)), i2), __ldg(I + 2 * S + o - sx));
+    const float c2 = fadd(fsub(fsub(i1, __ldg(I + S + o - sx)), i0), __ldg(I + o - sy));
+
+    float vv0, vv1, vv2, vi0, vi1, vi2;
+    if (COMPRESSED) {
+        const unsigned c = __ldg(g.idx + o);
+        const float4 a = __ldg(g.tabV + 2 * c), b = __ldg(g.tabV + 2 * c + 1);
+        vv0 = a.x; vv1 = a.y; vv2 = a.z; vi0 = a.w; vi1 = b.x; vi2 = b.y;
+    } else {
+        vv0 = __ldg(g.vv + o); vv1 = __ldg(g.vv + S + o); vv2 = __ldg(g.vv + 2 * S + o);
+        vi0 = __ldg(g.vi + o); vi1 = __ldg(g.vi + S + o); vi2 = __ldg(g.vi + 2 * S + o);
+    }
+    float v0 = V[o], v1 = V[S + o], v2 = V[2 * S + o];
+
+    int r = -1;
+    unsigned loc = 0;
+    if (UPML) r = upml_find(g, x, y, z, loc);
+    if (UPML && r >= 0) {
+        const UpmlDev& u = g.upml[r];
+        const unsigned n = u.n;
+        float vin[3] = {v0, v1, v2};
+        const float cc[3] = {c0, c1, c2};
+        const float cvv[3] = {vv0, vv1, vv2};
+        const float cvi[3] = {vi0, vi1, vi2};
+        float out[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const unsigned q = k * n + loc;
+            const float flux = u.vflux[q];
+            // pre: f = vv*V - vvfo*flux; V = flux; flux = f
+            const float f = fsub(fmul(__ldg(u.vv + q), vin[k]), fmul(__ldg(u.vvfo + q), flux));
+            float vn = flux;
+            vn = fadd(fmul(vn, cvv[k]), fmul(cvi[k], cc[k]));
+            // post: h = flux; flux = V; V = h + vvfn*flux
+            u.vflux[q] = vn;
+            out[k] = fadd(f, fmul(__ldg(u.vvfn + q), vn));
+        }
+        V[o] = out[0]; V[S + o] = out[1]; V[2 * S + o] = out[2];
+        return;
+    }
+    V[o] = fadd(fmul(v0, vv0), fmul(vi0, c0));
+    V[S + o] = fadd(fmul(v1, vv1), fmul(vi1, c1));
+    V[2 * S + o] = fadd(fmul(v2, vv2), fmul(vi2, c2));
+}
+
+// Engine::UpdateCurrents (FDTD/engine.cpp:170-222) fused with the UPML current hooks
+// (FDTD/extensions/engine_ext_upml.cpp:144-229).  Cells x<Nx-1, y<Ny-1, z<Nz-1 only.
+template <bool COMPRESSED, bool UPML>
+__global__ void __launch_bounds__(256) k_update_i(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned y = t / g.Pz, z = t - y * g.Pz;
+    if (y + 1 >= g.Ny || z + 1 >= g.Nz) return;
+    const unsigned long long S = g.S;
+    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
+    const unsigned long long sx = (unsigned long long)g.Ny * g.Pz;
+    const unsigned long long sy = g.Pz;
+    const float* __restrict__ V = g.V;
+    float* __restrict__ I = g.I;
+
+    const float w0 = __ldg(V + o), w1 = __ldg(V + S + o), w2 = __ldg(V + 2 * S + o);
+    const float c0 = fadd(fsub(fsub(w2, __ldg(V + 2 * S + o + sy)), w1), __ldg(V + S + o + 1));
+    const float c1 = fadd(fsub(fsub(w0, __ldg(V + o + 1)), w2), __ldg(V + 2 * S + o + sx));
+    const float c2 = fadd(fsub(fsub(w1, __ldg(V + S + o + sx)), w0), __ldg(V + o + sy));
+
+    float ii0, ii1, ii2, iv0, iv1, iv2;
+    if (COMPRESSED) {
+        const unsigned c = __ldg(g.idx + o);
+        const float4 a = __ldg(g.tabI + 2 * c), b = __ldg(g.tabI + 2 * c + 1);
+        ii0 = a.x; ii1 = a.y; ii2 = a.z; iv0 = a.w; iv1 = b.x; iv2 = b.y;
+    } else {
+        ii0 = __ldg(g.ii + o); ii1 = __ldg(g.ii + S + o); ii2 = __ldg(g.ii + 2 * S + o);
+        iv0 = __ldg(g.iv + o); iv1 = __ldg(g.iv + S + o); iv2 = __ldg(g.iv + 2 * S + o);
+    }
+    float a0 = I[o], a1 = I[S + o], a2 = I[2 * S + o];
+
+    int r = -1;
+    unsigned loc = 0;
+    if (UPML) r = upml_find(g, x, y, z, loc);
+    if (UPML && r >= 0) {
+        const UpmlDev& u = g.upml[r];
+        const unsigned n = u.n;
+        float iin[3] = {a0, a1, a2};
+        const float cc[3] = {c0, c1, c2};
+        const float cii[3] = {ii0, ii1, ii2};
+        const float civ[3] = {iv0, iv1, iv2};
+        float out[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const unsigned q = k * n + loc;
+            const float flux = u.iflux[q];
+            const float f = fsub(fmul(__ldg(u.ii + q), iin[k]), fmul(__ldg(u.iifo + q), flux));
+            float in = flux;
+            in = fadd(fmul(in, cii[k]), fmul(civ[k], cc[k]));
+            u.iflux[q] = in;
+            out[k] = fadd(f, fmul(__ldg(u.iifn + q), in));
+        }
+        I[o] = out[0]; I[S + o] = out[1]; I[2 * S + o] = out[2];
+        return;
+    }
+    I[o] = fadd(fmul(a0, ii0), fmul(iv0, c0));
+    I[S + o] = fadd(fmul(a1, ii1), fmul(iv1, c1));
+    I[2 * S + o] = fadd(fmul(a2, ii2), fmul(iv2, c2));
+}
+
+// ---------------------------------------------------------------------------------------------
+// Engine_Ext_Excitation::Apply2VoltagesImpl / Apply2CurrentImpl
+// (FDTD/extensions/engine_ext_excitation.cpp:33-94).  One thread per source edge; the source
+// edges are distinct so the adds do not race.  numTS is the device step counter.
+struct ExcDev {
+    unsigned count;
+    const unsigned long long* off;   // linear field offset incl. component
+    const float* amp;
+    const unsigned* delay;
+    const float* sig;
+    unsigned length;
+    unsigned period;                 // 0 = aperiodic
+};
+
+__global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsigned* __restrict__ numTS)
+{
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= e.count) return;
+    const int ts = (int)*numTS;
+    const int p = e.period ? (int)e.period : ts + 1;
+    int exc_pos = ts - (int)e.delay[k];
+    exc_pos *= (exc_pos > 0);
+    exc_pos %= p;
+    exc_pos *= (exc_pos < (int)e.length);
+    const unsigned long long o = e.off[k];
+    F[o] = fadd(F[o], fmul(e.amp[k], e.sig[exc_pos]));
+}
+
+// ---------------------------------------------------------------------------------------------
+// Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:82-178).  A single launch covers
+// every wall: blockIdx.y = wall, threads over the wall plane [n1][n2].
+struct MurWallDev {
+    int ny, nyP, nyPP;
+    unsigned line, shift, start_ts, n1, n2;
+    const float* cP;
+    const float* cPP;
+    float* bP;
+    float* bPP;
+};
+struct MurDev {
+    int nwall;
+    MurWallDev w[OEMS_MAX_MUR];
+};
+
+__device__ __forceinline__ unsigned long long mur_off(const GridDev& g, int comp, const unsigned p[3])
+{
+    return (unsigned long long)comp * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2];
+}
+
+// phase 0 = pre (before the V update), 1 = post (after), 2 = apply
+__global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __restrict__ numTS)
+{
+    const int wi = blockIdx.y;
+    if (wi >= m.nwall) return;
+    const MurWallDev& w = m.w[wi];
+    const unsigned ts = *numTS;
+    if (ts < w.start_ts) return;              // Engine_Ext_Mur_ABC::IsActive
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= w.n1 * w.n2) return;
+    const unsigned i = k / w.n2, j = k - i * w.n2;
+    unsigned pos[3], ps[3];
+    pos[w.ny] = w.line; ps[w.ny] = w.shift;
+    pos[w.nyP] = ps[w.nyP] = i;
+    pos[w.nyPP] = ps[w.nyPP] = j;
+    float* V = g.V;
+    if (phase == 0) {
+        w.bP[k] = fsub(V[mur_off(g, w.nyP, ps)], fmul(w.cP[k], V[mur_off(g, w.nyP, pos)]));
+        w.bPP[k] = fsub(V[mur_off(g, w.nyPP, ps)], fmul(w.cPP[k], V[mur_off(g, w.nyPP, pos)]));
+    } else if (phase == 1) {
+        w.bP[k] = fadd(w.bP[k], fmul(w.cP[k], V[mur_off(g, w.nyP, ps)]));
+        w.bPP[k] = fadd(w.bPP[k], fmul(w.cPP[k], V[mur_off(g, w.nyPP, ps)]));
+    } else {
+        // walls are applied in reverse insertion order, so on shared edges the wall with the
+        // lowest index is the last writer; skip components a lower active wall also writes
+        bool wP = true, wPP = true;
+        for (int q = 0; q < wi; ++q) {
+            const MurWallDev& o = m.w[q];
+            if (ts < o.start_ts || pos[o.ny] != o.line) continue;
+            if (w.nyP != o.ny) wP = false;
+            if (w.nyPP != o.ny) wPP = false;
+        }
+        if (wP) V[mur_off(g, w.nyP, pos)] = w.bP[k];
+        if (wPP) V[mur_off(g, w.nyPP, pos)] = w.bPP[k];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Engine_Ext_LorentzMaterial pre hooks (engine_ext_lorentzmaterial.cpp:79-168) and
+// Engine_Ext_Dispersive apply hooks (engine_ext_dispersive.cpp:76-127) for one order.
+struct LorDev {
+    unsigned count;
+    const unsigned long long* off;   // field offset of component 0 at each position
+    int lor;                         // Lorentz pole term on
+    const float* c_int;              // [3][count]
+    const float* c_ext;
+    const float* c_lor;
+    float* ade;                      // [3][count]
+    float* lade;
+};
+
+__global__ void k_lorentz_pre(const float* __restrict__ F, unsigned long long S, LorDev l)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= l.count) return;
+    const unsigned long long o = l.off[i];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        const unsigned k = n * l.count + i;
+        const float f = F[o + n * S];
+        float a = l.ade[k];
+        if (l.lor) {
+            const float la = fadd(l.lade[k], fmul(l.c_lor[k], a));
+            l.lade[k] = la;
+            a = fmul(a, l.c_int[k]);
+            a = fadd(a, fmul(l.c_ext[k], fsub(f, la)));
+        } else {
+            a = fmul(a, l.c_int[k]);
+            a = fadd(a, fmul(l.c_ext[k], f));
+        }
+        l.ade[k] = a;
+    }
+}
+
+__global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long S, LorDev l)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= l.count) return;
+    const unsigned long long o = l.off[i];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        const unsigned long long q = o + n * S;
+        F[q] = fsub(F[q], l.ade[n * l.count + i]);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Processing at the end of a timestep: probes (ProcessIntegral::Process,
+// Common/processintegral.cpp:134-171), FD field dumps (ProcessFieldsFD::Process,
+// Common/processfields_fd.cpp:72-107) and the numTS increment.
+struct ProbeDev {
+    int type;                        // 0 voltage (double sum), 1 current (float sum)
+    unsigned nterm;
+    const unsigned long long* term;  // field offsets in reference summation order
+    const signed char* sign;         // +1 / -1
+    double weight;
+    unsigned interval, start_ts, stop_ts, nslots;
+    double* series;
+    unsigned fd_interval, nf, nsamp;
+    const double2* phasor;           // [nsamp][nf] = exp(-2j*pi*f*t)
+    double* dft;                     // [nf][2]
+    double dt;
+};
+
+struct DumpDev {
+    int field;                       // 0 E (uses V), 1 H (uses I)
+    unsigned start[3], sz[3];
+    unsigned npos;
+    unsigned fd_interval, nf, nsamp;
+    const float2* phasor;            // [nsamp][nf], includes *2 and *dt*fd_interval
+    const double* el;                // GetEdgeLength per line, concatenated x,y,z (E: main, H: dual)
+    float2* acc;                     // [nf][3][npos]
+};
+
+struct StepEndDev {
+    int nprobe;
+    const ProbeDev* probes;          // device array
+    int ndump;
+    const DumpDev* dumps;            // device array
+    const unsigned* dump_block0;     // first block of each dump (prefix sums), size ndump+1
+    unsigned* numTS;
+    unsigned* blocks_done;
+};
+
+__device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned ts, int lane)
+{
+    if (ts < p.start_ts || ts > p.stop_ts) return;
+    const bool do_td = (ts % p.interval) == 0;
+    const bool do_fd = p.fd_interval && (ts % p.fd_interval) == 0;
+    if (!do_td && !do_fd) return;
+    const float* F = p.type == 0 ? g.V : g.I;
+    // lanes fetch terms in parallel, lane 0 accumulates them in the reference's order
+    double accd = 0.0;
+    float accf = 0.0f;
+    for (unsigned base = 0; base < p.nterm; base += 32) {
+        const unsigned k = base + lane;
+        float v = 0.0f;
+        int s = 0;
+        if (k < p.nterm) { v = F[p.term[k]]; s = p.sign[k]; }
+        const unsigned cnt = min(32u, p.nterm - base);
+        for (unsigned j = 0; j < cnt; ++j) {
+            const float vj = __shfl_sync(0xffffffffu, v, j);
+            const int sj = __shfl_sync(0xffffffffu, s, j);
+            if (lane == 0) {
+                if (p.type == 0) accd = sj > 0 ? __dadd_rn(accd, (double)vj) : __dsub_rn(accd, (double)vj);
+                else accf = sj > 0 ? fadd(accf, vj) : fsub(accf, vj);
+            }
+        }
+    }
+    if (lane != 0) return;
+    const double val = p.type == 0 ? accd : (double)accf;
+    const double a = __dmul_rn(val, p.weight);
+    if (do_td) {
+        const unsigned slot = ts / p.interval;
+        if (slot < p.nslots) p.series[slot] = a;
+    }
+    if (do_fd) {
+        const unsigned smp = ts / p.fd_interval;
+        if (smp < p.nsamp) {
+            for (unsigned f = 0; f < p.nf; ++f) {
+                const double2 e = p.phasor[(unsigned long long)smp * p.nf + f];
+                double re = __dmul_rn(e.x, a), im = __dmul_rn(e.y, a);
+                re = __dmul_rn(re, 2.0); im = __dmul_rn(im, 2.0);
+                re = __dmul_rn(re, p.dt); im = __dmul_rn(im, p.dt);
+                re = __dmul_rn(re, (double)p.fd_interval); im = __dmul_rn(im, (double)p.fd_interval);
+                p.dft[2 * f] = __dadd_rn(p.dft[2 * f], re);
+                p.dft[2 * f + 1] = __dadd_rn(p.dft[2 * f + 1], im);
+            }
+        }
+    }
+}
+
+// cell-interpolated E (FDTD/engine_interface_fdtd.cpp:104-121) or H (:182-199) at pos
+__device__ void cell_field(const GridDev& g, const DumpDev& d, const unsigned pos[3], double out[3])
+{
+    const unsigned N[3] = {g.Nx, g.Ny, g.Nz};
+    const unsigned eoff[3] = {0u, g.Nx, g.Nx + g.Ny};
+    if (d.field == 0) {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+            if (pos[0] == N[0] - 1 || pos[1] == N[1] - 1 || pos[2] == N[2] - 1) { out[n] = 0.0; continue; }
+            unsigned ip[3] = {pos[0], pos[1], pos[2]};
+            double acc;
+            auto raw = [&](const unsigned* p) -> double {
+                const double delta = d.el[eoff[n] + p[n]];
+                const float v = g.V[(unsigned long long)n * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2]];
+                return delta != 0.0 ? __ddiv_rn((double)v, delta) : 0.0;
+            };
+            acc = raw(ip);
+            ++ip[nP];
+            acc = __dadd_rn(acc, raw(ip));
+            ++ip[nPP];
+            acc = __dadd_rn(acc, raw(ip));
+            --ip[nP];
+            acc = __dadd_rn(acc, raw(ip));
+            out[n] = __ddiv_rn(acc, 4.0);
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            unsigned ip[3] = {pos[0], pos[1], pos[2]};
+            auto raw = [&](const unsigned* p) -> double {
+                const double delta = d.el[eoff[n] + p[n]];
+                const float v = g.I[(unsigned long long)n * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2]];
+                return delta != 0.0 ? __ddiv_rn((double)v, delta) : 0.0;
+            };
+            const double delta = d.el[eoff[n] + ip[n]];
+            double o = raw(ip);
+            if (pos[n] >= N[n] - 1) { out[n] = 0.0; continue; }
+            ++ip[n];
+            const double deltaUp = d.el[eoff[n] + ip[n]];
+            const double deltaRel = __ddiv_rn(delta, __dadd_rn(delta, deltaUp));
+            out[n] = __dadd_rn(__dmul_rn(o, __dsub_rn(1.0, deltaRel)), __dmul_rn(raw(ip), deltaRel));
+        }
+    }
+}
+
+// One launch: block 0 warps evaluate the probes; blocks [dump_block0[k], dump_block0[k+1])
+// handle dump k (one thread per box position, all frequencies).  The last block to finish
+// increments numTS (threadfence + completion counter), so every block read the same ts.
+__global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s)
+{
+    const unsigned ts = *s.numTS + 1;   // the step just completed
+    if (blockIdx.x == 0) {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int p = warp; p < s.nprobe; p += blockDim.x >> 5) probe_eval(g, s.probes[p], ts, lane);
+    } else {
+        // find the dump of this block
+        int k = 0;
+        while (k + 1 < s.ndump && blockIdx.x >= s.dump_block0[k + 1]) ++k;
+        if (s.ndump > 0) {
+            const DumpDev& d = s.dumps[k];
+            const unsigned q = (blockIdx.x - s.dump_block0[k]) * blockDim.x + threadIdx.x;
+            if (q < d.npos && d.fd_interval && (ts % d.fd_interval) == 0) {
+                const unsigned smp = ts / d.fd_interval;
+                if (smp < d.nsamp) {
+                    const unsigned a = q / (d.sz[1] * d.sz[2]);
+                    const unsigned rem = q - a * d.sz[1] * d.sz[2];
+                    const unsigned b = rem / d.sz[2], c = rem - b * d.sz[2];
+                    const unsigned pos[3] = {d.start[0] + a, d.start[1] + b, d.start[2] + c};
+                    double out[3];
+                    cell_field(g, d, pos, out);
+                    for (unsigned f = 0; f < d.nf; ++f) {
+                        const float2 e = d.phasor[(unsigned long long)smp * d.nf + f];
+#pragma unroll
+                        for (int n = 0; n < 3; ++n) {
+                            const float td = (float)out[n];
+                            float2* acc = d.acc + ((unsigned long long)f * 3 + n) * d.npos + q;
+                            float2 v = *acc;
+                            v.x = fadd(v.x, fmul(td, e.x));
+                            v.y = fadd(v.y, fmul(td, e.y));
+                            *acc = v;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    // completion: last block bumps numTS
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned done = atomicAdd(s.blocks_done, 1u);
+        if (done == gridDim.x - 1) {
+            *s.blocks_done = 0u;
+            __threadfence();
+            *s.numTS = ts;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Engine_Interface_FDTD::CalcFastEnergy (FDTD/engine_interface_fdtd.cpp:302-347): double
+// accumulation of float squares over [0,N-1)^3; block partials then one final reduction.
+__global__ void __launch_bounds__(256) k_energy(GridDev g, double* __restrict__ partial)
+{
+    double e = 0.0, h = 0.0;
+    const unsigned long long plane = (unsigned long long)g.Ny * g.Pz;
+    const unsigned long long total = (unsigned long long)(g.Nx - 1) * plane;
+    for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long x = t / plane;
+        const unsigned long long r = t - x * plane;
+        const unsigned y = (unsigned)(r / g.Pz), z = (unsigned)(r - (unsigned long long)y * g.Pz);
+        if (y + 1 >= g.Ny || z + 1 >= g.Nz) continue;
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const float v = g.V[n * g.S + t], c = g.I[n * g.S + t];
+            e += (double)fmul(v, v);
+            h += (double)fmul(c, c);
+        }
+    }
+    __shared__ double se[256], sh[256];
+    se[threadIdx.x] = e;
+    sh[threadIdx.x] = h;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) { se[threadIdx.x] += se[threadIdx.x + w]; sh[threadIdx.x] += sh[threadIdx.x + w]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { partial[2 * blockIdx.x] = se[0]; partial[2 * blockIdx.x + 1] = sh[0]; }
+}
+
+}  // namespace oems

@@ -1,0 +1,1295 @@
+"""Host-side Operator: the equivalent-circuit (EC) coefficient build that feeds the CUDA engine.
+
+This restates the parts of openEMS's Cartesian ``Operator`` (FDTD/operator.cpp) and of its
+operator extensions that the engine consumes, for rectilinear meshes holding axis-aligned box
+primitives (the CSXCAD geometry library is not part of this package; ``Structure`` below holds
+the boxes and their properties, with CSXCAD's python API names).  Everything is vectorised with
+numpy so that 67 M-cell meshes build in well under a minute.
+
+What is computed, and where it follows the reference:
+
+* quarter-cell material averaging ``AverageMatQuarterCell`` (FDTD/operator.cpp:1447-1564) and
+  ``Calc_ECPos`` (FDTD/operator.cpp:1189-1254) -> EC_C/G/L/R, stored as float32 like the
+  reference's ``FDTD_FLOAT* EC_*`` arrays;
+* the Rennings timestep ``CalcTimestep_Var3`` (FDTD/operator.cpp:1956-2030) including the
+  ``AdrOp`` reflection at the mesh border (tools/AdrOp.cpp:183-221);
+* ``Calc_ECOperatorPos`` (FDTD/operator.cpp:956-984) -> vv/vi/ii/iv (float64 math, float32 store);
+* ``ApplyElectricBC`` / ``CalcPEC_Range`` / ``Calc_LumpedElements`` / ``ApplyMagneticBC``
+  (FDTD/operator.cpp:1099-1187, 2045-2083, 1586-1763) in the order of ``CalcECOperator``
+  (FDTD/operator.cpp:986-1097);
+* operator extensions in insertion order (openems.cpp:1186-1243): excitation
+  (FDTD/extensions/operator_ext_excitation.cpp:105-297), Mur ABC
+  (FDTD/extensions/operator_ext_mur_abc.cpp:107-186), UPML
+  (FDTD/extensions/operator_ext_upml.cpp:69-445), Lorentz/Drude
+  (FDTD/extensions/operator_ext_lorentzmaterial.cpp:120-445);
+* probe snapping (Common/processing.cpp:180-189, Common/processvoltage.cpp:38-42,
+  Common/processcurrent.cpp:40-88).
+
+CSXCAD's ``GetPropertyByCoordPriority`` is restated as: among the boxes of the requested
+property kinds that contain the coordinate (bounds inclusive), the highest priority wins and
+ties go to the box defined first.
+"""
+from __future__ import annotations
+
+import math
+import os
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from .excitation import Excitation, calc_nyquist_num
+
+EPS0 = 8.85418781762e-12    # tools/constants.h:23
+MUE0 = 1.256637062e-6       # tools/constants.h:24
+C0 = 299792458.0            # tools/constants.h:25
+Z0 = 376.730313461          # tools/constants.h:26
+PI = 3.141592653589793238462643383279
+
+# property kinds (bit flags, like CSProperties::PropertyType)
+MATERIAL, METAL, EXCITATION, LUMPED, PROBE, DUMP = 1, 2, 4, 8, 16, 32
+
+
+# =========================================================================================
+# geometry container (CSXCAD-like)
+# =========================================================================================
+class Property:
+    def __init__(self, structure, kind, name, **params):
+        self.structure = structure
+        self.kind = kind
+        self.name = name
+        self.params = params
+        self.boxes = []
+
+    def AddBox(self, start, stop, priority=0):
+        self.structure._add_box(self, np.asarray(start, float), np.asarray(stop, float), priority)
+        return self
+
+
+class Structure:
+    """Holds properties and their box primitives (the subset of CSXCAD used by the engine path)."""
+
+    def __init__(self):
+        self.props: List[Property] = []
+        self.boxes = []          # (start, stop, priority, seq, prop)
+        self._seq = 0
+
+    def _add_box(self, prop, start, stop, priority):
+        lo = np.minimum(start, stop)
+        hi = np.maximum(start, stop)
+        rec = (lo, hi, int(priority), self._seq, prop, start.copy(), stop.copy())
+        self._seq += 1
+        prop.boxes.append(rec)
+        self.boxes.append(rec)
+
+    def _add(self, kind, name, **params):
+        p = Property(self, kind, name, **params)
+        self.props.append(p)
+        return p
+
+    def AddMaterial(self, name, epsilon=1.0, mue=1.0, kappa=0.0, sigma=0.0):
+        return self._add(MATERIAL, name, epsilon=float(epsilon), mue=float(mue), kappa=float(kappa), sigma=float(sigma))
+
+    def AddLorentzMaterial(self, name, epsilon=1.0, mue=1.0, kappa=0.0, sigma=0.0,
+                           eps_plasma_freq=(), eps_relax_time=(), eps_lor_pole_freq=(),
+                           mue_plasma_freq=(), mue_relax_time=(), mue_lor_pole_freq=()):
+        """Drude/Lorentz dispersive material, one entry per dispersion order (CSPropLorentzMaterial)."""
+        order = max(len(eps_plasma_freq), len(mue_plasma_freq), 1)
+
+        def pad(v):
+            v = list(v)
+            return v + [0.0] * (order - len(v))
+        return self._add(MATERIAL, name, epsilon=float(epsilon), mue=float(mue), kappa=float(kappa),
+                         sigma=float(sigma), lorentz=True, order=order,
+                         eps_plasma=pad(eps_plasma_freq), eps_relax=pad(eps_relax_time),
+                         eps_pole=pad(eps_lor_pole_freq), mue_plasma=pad(mue_plasma_freq),
+                         mue_relax=pad(mue_relax_time), mue_pole=pad(mue_lor_pole_freq))
+
+    def AddMetal(self, name):
+        return self._add(METAL, name)
+
+    def AddLumpedElement(self, name, ny, R=float('nan'), C=float('nan'), caps=True):
+        """Parallel RC lumped element (CSPropLumpedElement, LEtype PARALLEL, no L)."""
+        return self._add(LUMPED, name, ny=int(ny), R=float(R), C=float(C), caps=bool(caps))
+
+    def AddExcitation(self, name, exc_type, exc_val, delay=0.0):
+        return self._add(EXCITATION, name, exc_type=int(exc_type),
+                         exc_val=np.asarray(exc_val, float), delay=float(delay))
+
+    def AddProbe(self, name, p_type, weight=1.0, norm_dir=-1, frequency=(), start_time=0.0, stop_time=0.0,
+                 interval=0):
+        """Voltage (p_type 0) or current (p_type 1) probe; ``interval`` overrides the default
+        sampling interval Nyquist/OverSampling (openems.cpp:568)."""
+        return self._add(PROBE, name, p_type=int(p_type), weight=float(weight), norm_dir=int(norm_dir),
+                         frequency=list(frequency), start_time=float(start_time), stop_time=float(stop_time),
+                         interval=int(interval))
+
+    def AddDump(self, name, dump_type=0, dump_mode=1, frequency=()):
+        """FD field dump box: dump_type 10 = E-field FD, 11 = H-field FD (Common/processfields.h)."""
+        return self._add(DUMP, name, dump_type=int(dump_type), dump_mode=int(dump_mode), frequency=list(frequency))
+
+
+@dataclass
+class Grid:
+    """Rectilinear mesh: ``lines[n]`` in drawing units, ``unit`` = metres per drawing unit."""
+    lines: list
+    unit: float = 1.0
+
+    def __post_init__(self):
+        self.lines = [np.asarray(sorted(set(float(v) for v in l)), np.float64) for l in self.lines]
+
+
+# =========================================================================================
+# engine-facing tables (what the operator extensions hand to their engine extensions)
+# =========================================================================================
+@dataclass
+class ExcitationTable:
+    """Operator_Ext_Excitation arrays (FDTD/extensions/operator_ext_excitation.h:80-94)."""
+    volt_index: np.ndarray
+    volt_dir: np.ndarray
+    volt_amp: np.ndarray
+    volt_delay: np.ndarray
+    curr_index: np.ndarray
+    curr_dir: np.ndarray
+    curr_amp: np.ndarray
+    curr_delay: np.ndarray
+    signal_volt: np.ndarray
+    signal_curr: np.ndarray
+    period: int = 0
+
+
+@dataclass
+class UPMLRegion:
+    """Operator_Ext_UPML tables (FDTD/extensions/operator_ext_upml.h:74-96)."""
+    start: np.ndarray
+    num_lines: np.ndarray
+    vv: np.ndarray
+    vvfo: np.ndarray
+    vvfn: np.ndarray
+    ii: np.ndarray
+    iifo: np.ndarray
+    iifn: np.ndarray
+
+
+@dataclass
+class MurWall:
+    """Operator_Ext_Mur_ABC (FDTD/extensions/operator_ext_mur_abc.h) + engine m_start_TS."""
+    ny: int
+    line_nr: int
+    line_nr_shift: int
+    start_ts: int
+    coeff_nyP: np.ndarray
+    coeff_nyPP: np.ndarray
+
+
+@dataclass
+class LorentzOrder:
+    """One dispersion order of Operator_Ext_LorentzMaterial (operator_ext_dispersive.h:60-75)."""
+    pos: np.ndarray               # uint32 [3, M]
+    volt_ade_on: bool
+    curr_ade_on: bool
+    volt_lor_on: bool
+    curr_lor_on: bool
+    v_int: np.ndarray
+    v_ext: np.ndarray
+    v_lor: np.ndarray
+    i_int: np.ndarray
+    i_ext: np.ndarray
+    i_lor: np.ndarray
+
+
+@dataclass
+class VoltageProbe:
+    name: str
+    start: np.ndarray
+    stop: np.ndarray
+    weight: float
+    interval: int
+    fd_interval: int
+    freqs: list
+    start_ts: int = 0
+    stop_ts: int = 0xFFFFFFFF
+
+
+@dataclass
+class CurrentProbe:
+    name: str
+    start: np.ndarray
+    stop: np.ndarray
+    norm_dir: int
+    start_inside: np.ndarray
+    stop_inside: np.ndarray
+    weight: float
+    interval: int
+    fd_interval: int
+    freqs: list
+    start_ts: int = 0
+    stop_ts: int = 0xFFFFFFFF
+
+
+@dataclass
+class FieldDumpFD:
+    """FD dump box (Common/processfields_fd.cpp): E (field=0) or H (field=1), cell interpolation."""
+    name: str
+    field: int
+    start: np.ndarray
+    stop: np.ndarray
+    freqs: list
+    fd_interval: int
+
+
+@dataclass
+class OperatorData:
+    num_lines: np.ndarray
+    dt: float
+    vv: np.ndarray
+    vi: np.ndarray
+    ii: np.ndarray
+    iv: np.ndarray
+    exc: ExcitationTable
+    upml: list = field(default_factory=list)
+    mur: list = field(default_factory=list)
+    lorentz: list = field(default_factory=list)
+    vprobes: list = field(default_factory=list)
+    iprobes: list = field(default_factory=list)
+    dumps: list = field(default_factory=list)
+    nyquist: int = 0
+    excitation: Optional[Excitation] = None
+    grid: Optional[Grid] = None
+
+
+# =========================================================================================
+# mesh helpers
+# =========================================================================================
+def _main_delta(L):
+    """GetDiscDelta(n,pos,false) for pos in [0,N-1] (FDTD/operator.cpp:159-171)."""
+    d = np.empty_like(L)
+    d[:-1] = L[1:] - L[:-1]
+    d[-1] = L[-1] - L[-2]
+    return d
+
+
+def _dual_line(L):
+    """GetDiscLine(n,pos,true) (FDTD/operator.cpp:144-157)."""
+    dl = np.empty_like(L)
+    dl[:-1] = 0.5 * (L[:-1] + L[1:])
+    dl[-1] = L[-1] + 0.5 * (L[-1] - L[-2])
+    return dl
+
+
+def _dual_delta(L):
+    """GetDiscDelta(n,pos,true) (FDTD/operator.cpp:172-179)."""
+    dl = _dual_line(L)
+    d = np.empty_like(L)
+    d[0] = L[1] - L[0]
+    d[1:] = dl[1:] - dl[:-1]
+    return d
+
+
+def _raw_delta(L, idx):
+    """GetRawDiscDelta (FDTD/operator.cpp:1256-1266) for an index array (may hold -1 or N-1)."""
+    N = len(L)
+    idx = np.asarray(idx)
+    out = np.empty(idx.shape, np.float64)
+    lo = idx < 0
+    hi = idx >= N - 1
+    mid = ~(lo | hi)
+    out[lo] = L[0] - L[1]
+    out[hi] = L[N - 2] - L[N - 1]
+    out[mid] = L[idx[mid] + 1] - L[idx[mid]]
+    return out
+
+
+class _Painter:
+    """Vectorised GetPropertyByCoordPriority over separable sample coordinates."""
+
+    def __init__(self, structure: Structure, kinds: int):
+        recs = [b for b in structure.boxes if b[4].kind & kinds]
+        # paint ascending priority; among equal priorities the earliest-defined box is painted last (wins)
+        self.recs = sorted(recs, key=lambda r: (r[2], -r[3]))
+        self.props = []
+        self.prop_index = {}
+        for r in self.recs:
+            if id(r[4]) not in self.prop_index:
+                self.prop_index[id(r[4])] = len(self.props)
+                self.props.append(r[4])
+
+    @staticmethod
+    def _range(c, lo, hi):
+        m = np.nonzero((c >= lo) & (c <= hi))[0]
+        if m.size == 0:
+            return None
+        if m[-1] - m[0] + 1 == m.size:
+            return slice(int(m[0]), int(m[-1]) + 1)
+        return m
+
+    def paint(self, cx, cy, cz):
+        """Return int32 array [len(cx),len(cy),len(cz)] of property indices (-1 = background)."""
+        out = np.full((len(cx), len(cy), len(cz)), -1, np.int32)
+        for lo, hi, _prio, _seq, prop, *_ in self.recs:
+            rx = self._range(cx, lo[0], hi[0])
+            ry = self._range(cy, lo[1], hi[1])
+            rz = self._range(cz, lo[2], hi[2])
+            if rx is None or ry is None or rz is None:
+                continue
+            pid = self.prop_index[id(prop)]
+            if isinstance(rx, slice) and isinstance(ry, slice) and isinstance(rz, slice):
+                out[rx, ry, rz] = pid
+            else:
+                ax = np.arange(len(cx))[rx]
+                ay = np.arange(len(cy))[ry]
+                az = np.arange(len(cz))[rz]
+                out[np.ix_(ax, ay, az)] = pid
+        return out
+
+    def param(self, idx_map, key, background):
+        table = np.array([p.params.get(key, background) if p.kind == MATERIAL else background
+                          for p in self.props] + [background], np.float64)
+        return table[idx_map]   # -1 selects the trailing background entry
+
+
+def _axes(n):
+    return n, (n + 1) % 3, (n + 2) % 3
+
+
+def _bcast(n, arr_n, arr_p, arr_pp):
+    """Broadcast three 1-D arrays given in (n, nP, nPP) axis order into an x,y,z grid; the
+    reshaped arrays are returned in the same (n, nP, nPP) order."""
+    out = [None, None, None]
+    a, b, c = _axes(n)
+    shapes = {a: arr_n, b: arr_p, c: arr_pp}
+    for ax in range(3):
+        v = shapes[ax]
+        shp = [1, 1, 1]
+        shp[ax] = len(v)
+        out[ax] = v.reshape(shp)
+    return out[a], out[b], out[c]
+
+
+def _coords_xyz(n, cn, cp, cpp):
+    """Return (cx, cy, cz) 1-D coordinate arrays from (n, nP, nPP)-ordered arrays."""
+    a, b, c = _axes(n)
+    d = {a: cn, b: cp, c: cpp}
+    return d[0], d[1], d[2]
+
+
+def _slabs(n, parts):
+    """Split range(n) into at most ``parts`` contiguous (x0, x1) chunks."""
+    parts = max(1, min(parts, n))
+    edges = np.linspace(0, n, parts + 1).round().astype(int)
+    return [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:]) if b > a]
+
+
+def _parallel(fn, items):
+    """Run fn over items on a thread pool (numpy releases the GIL inside its kernels)."""
+    workers = min(len(items), os.cpu_count() or 1)
+    if workers <= 1:
+        return [fn(*it) for it in items]
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        return list(ex.map(lambda it: fn(*it), items))
+
+
+# =========================================================================================
+# the operator
+# =========================================================================================
+class Operator:
+    """Builds EC-FDTD coefficients plus extension tables for the engine.
+
+    ``bc``: 6 boundary codes as in openEMS (0 PEC, 1 PMC, 2 Mur, 3 PML), order xmin,xmax,...
+    """
+
+    def __init__(self, structure: Structure, grid: Grid, excitation: Excitation, bc=(0,) * 6,
+                 pml_size=(8,) * 6, timestep=0.0, timestep_factor=1.0, over_sampling=4,
+                 background=(1.0, 1.0, 0.0, 0.0)):
+        self.csx = structure
+        self.grid = grid
+        self.exc = excitation
+        self.bc = [int(b) for b in bc]
+        self.pml_size = [int(s) if b == 3 else 0 for s, b in zip(pml_size, bc)]
+        self.forced_dt = float(timestep)
+        self.ts_factor = float(timestep_factor)
+        self.over_sampling = int(over_sampling)
+        self.bg = dict(epsilon=background[0], mue=background[1], kappa=background[2], sigma=background[3])
+        self.L = grid.lines
+        self.unit = float(grid.unit)
+        self.N = np.array([len(l) for l in self.L], np.int64)
+        if (self.N < 3).any():
+            raise ValueError("Operator: at least 3 mesh lines per direction are required")
+        self.md = [_main_delta(l) for l in self.L]        # main deltas (drawing units)
+        self.dd = [_dual_delta(l) for l in self.L]        # dual deltas (drawing units)
+        self.dl = [_dual_line(l) for l in self.L]
+        self._mat = _Painter(structure, MATERIAL)
+        self._matmetal = _Painter(structure, MATERIAL | METAL)
+
+    # ---- material lookup ------------------------------------------------------------------
+    def _lookup(self, n, cn, cp, cpp, keys, painter=None):
+        painter = painter or self._mat
+        cx, cy, cz = _coords_xyz(n, cn, cp, cpp)
+        m = painter.paint(cx, cy, cz)
+        return [painter.param(m, k, self.bg[k]) for k in keys]
+
+    # ---- effective material (FDTD/operator.cpp:1447-1564) ----------------------------------
+    def eff_mat(self, n):
+        """Quarter-cell averaged eps (abs), kappa, mue (abs), sigma for edge direction n, full grid."""
+        a, p, pp = _axes(n)
+        L, Lp, Lpp = self.L[a], self.L[p], self.L[pp]
+        N, Np, Npp = len(L), len(Lp), len(Lpp)
+        i_n, i_p, i_pp = np.arange(N), np.arange(Np), np.arange(Npp)
+        delta = _raw_delta(L, i_n)
+        deltaP = _raw_delta(Lp, i_p)
+        deltaPP = _raw_delta(Lpp, i_pp)
+        delta_M = _raw_delta(L, i_n - 1)
+        deltaP_M = _raw_delta(Lp, i_p - 1)
+        deltaPP_M = _raw_delta(Lpp, i_pp - 1)
+        u = self.unit
+
+        def wmain(k, idx):   # GetNodeWidth(k, int pos, dual=true) = main delta * unit, 0 for idx<0
+            d = self.md[k]
+            out = np.zeros(len(idx))
+            ok = idx >= 0
+            out[ok] = d[idx[ok]] * u
+            return out
+
+        cn = L + delta * 0.5
+        cp_up, cp_dn = Lp + deltaP * 0.25, Lp - deltaP_M * 0.25
+        cpp_up, cpp_dn = Lpp + deltaPP * 0.25, Lpp - deltaPP_M * 0.25
+        Wp, WpM = wmain(p, i_p), wmain(p, i_p - 1)
+        Wpp, WppM = wmain(pp, i_pp), wmain(pp, i_pp - 1)
+
+        samples = [(cp_up, cpp_up, Wp, Wpp), (cp_dn, cpp_up, WpM, Wpp),
+                   (cp_up, cpp_dn, Wp, WppM), (cp_dn, cpp_dn, WpM, WppM)]
+        eps_acc = kap_acc = area = None
+        for cpv, cppv, wa, wb in samples:
+            e, k = self._lookup(n, cn, cpv, cppv, ("epsilon", "kappa"))
+            _, A_p, A_pp = _bcast(n, np.ones(N), wa, wb)
+            A = A_p * A_pp                       # shape broadcastable (1 along n)
+            if eps_acc is None:
+                eps_acc = e * A
+                kap_acc = k * A
+                area = np.broadcast_to(A, e.shape).copy()
+            else:
+                eps_acc += e * A
+                kap_acc += k * A
+                area = area + A
+        eff0 = eps_acc * (EPS0 / area)
+        eff1 = kap_acc / area
+        del eps_acc, kap_acc
+
+        # mu / sigma: two samples along n
+        cpm = Lp + deltaP * 0.5
+        cppm = Lpp + deltaPP * 0.5
+        d_dn = wmain(a, i_n - 1)
+        d_up = wmain(a, i_n)
+        mu_dn, sg_dn = self._lookup(n, L - delta_M * 0.25, cpm, cppm, ("mue", "sigma"))
+        Ddn, _, _ = _bcast(n, d_dn, np.ones(Np), np.ones(Npp))
+        Dup, _, _ = _bcast(n, d_up, np.ones(Np), np.ones(Npp))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            eff2 = Ddn / mu_dn
+            eff3 = np.where(sg_dn != 0, Ddn / np.where(sg_dn != 0, sg_dn, 1.0), 0.0)
+            length = np.broadcast_to(Ddn, eff2.shape)
+            mu_up, sg_up = self._lookup(n, L + delta * 0.25, cpm, cppm, ("mue", "sigma"))
+            eff2 = eff2 + Dup / mu_up
+            eff3 = np.where(sg_up != 0, eff3 + Dup / np.where(sg_up != 0, sg_up, 1.0), 0.0)
+            length = length + Dup
+            eff2 = length * MUE0 / eff2
+            eff3 = np.where(eff3 != 0, length / np.where(eff3 != 0, eff3, 1.0), eff3)
+        for arr in (eff0, eff1, eff2, eff3):
+            if not np.isfinite(arr).all():
+                raise ValueError("Operator: an effective material parameter is not finite")
+        return eff0, eff1, eff2, eff3
+
+    def _sub(self, lo, hi):
+        """Operator over the sub-mesh lines[a][lo[a]:hi[a]] (same geometry and background).
+
+        Every per-edge quantity of EffMat/EC depends only on lines within +-1 of the edge, so
+        with one halo line on each internal side the sub-mesh reproduces the full mesh's values
+        at its interior positions."""
+        g = Grid([self.L[a][lo[a]:hi[a]] for a in range(3)], unit=self.unit)
+        sub = Operator.__new__(Operator)
+        sub.csx, sub.grid, sub.exc, sub.bg = self.csx, g, self.exc, self.bg
+        sub.L, sub.unit = g.lines, self.unit
+        sub.N = np.array([len(l) for l in g.lines], np.int64)
+        sub.md = [_main_delta(l) for l in g.lines]
+        sub.dd = [_dual_delta(l) for l in g.lines]
+        sub.dl = [_dual_line(l) for l in g.lines]
+        sub._mat, sub._matmetal = self._mat, self._matmetal
+        return sub
+
+    def _halo(self, axis, a0, a1):
+        lo = [0, 0, 0]
+        hi = [int(v) for v in self.N]
+        lo[axis] = max(a0 - 1, 0)
+        hi[axis] = min(a1 + 1, int(self.N[axis]))
+        return lo, hi
+
+    # ---- EC (FDTD/operator.cpp:1189-1254, 1839-1870) ---------------------------------------
+    def _ec_local(self):
+        """EC_C/G/L/R (float32) on this operator's own mesh."""
+        shape = tuple(int(v) for v in self.N)
+        out = [np.empty((3,) + shape, np.float32) for _ in range(4)]
+        u = self.unit
+        for n in range(3):
+            a, p, pp = _axes(n)
+            e0, e1, e2, e3 = self.eff_mat(n)
+            Dn, Ap, App = _bcast(n, self.md[a] * u, self.dd[p] * u, self.dd[pp] * u)
+            area_e = Ap * App
+            with np.errstate(divide="ignore", invalid="ignore"):
+                out[0][n] = np.where(Dn != 0, e0 * area_e / Dn, 0.0)
+                out[1][n] = np.where(Dn != 0, e1 * area_e / Dn, 0.0)
+                Dh, Bp, Bpp = _bcast(n, self.dd[a] * u, self.md[p] * u, self.md[pp] * u)
+                area_h = Bp * Bpp
+                out[2][n] = np.where(Dh != 0, e2 * area_h / Dh, 0.0)
+                out[3][n] = np.where(Dh != 0, e3 * area_h / Dh, 0.0)
+        return out
+
+    def calc_ec(self):
+        shape = tuple(int(v) for v in self.N)
+        self.EC_C = np.empty((3,) + shape, np.float32)
+        self.EC_G = np.empty((3,) + shape, np.float32)
+        self.EC_L = np.empty((3,) + shape, np.float32)
+        self.EC_R = np.empty((3,) + shape, np.float32)
+        dst = (self.EC_C, self.EC_G, self.EC_L, self.EC_R)
+
+        def work(x0, x1):
+            lo, hi = self._halo(0, x0, x1)
+            res = self._sub(lo, hi)._ec_local()
+            for d, r in zip(dst, res):
+                d[:, x0:x1] = r[:, x0 - lo[0]:x1 - lo[0]]
+        _parallel(work, _slabs(int(self.N[0]), 2 * (os.cpu_count() or 1)))
+
+    def eff_region(self, n, start, nl):
+        """eff_Mat (eps abs, kappa, mue abs, sigma) of direction n on the box start..start+nl."""
+        lo = [max(int(start[a]) - 1, 0) for a in range(3)]
+        hi = [min(int(start[a] + nl[a]) + 1, int(self.N[a])) for a in range(3)]
+        e = self._sub(lo, hi).eff_mat(n)
+        sl = tuple(slice(int(start[a]) - lo[a], int(start[a]) - lo[a] + int(nl[a])) for a in range(3))
+        return [x[sl] for x in e]
+
+    # ---- timestep (FDTD/operator.cpp:1956-2030) --------------------------------------------
+    def calc_timestep_var3(self):
+        def work(x0, x1):
+            h0, h1 = max(x0 - 1, 0), min(x1 + 1, int(self.N[0]))
+            return self._var3_local(self.EC_C[:, h0:h1], self.EC_L[:, h0:h1], x0 - h0, x1 - h0)
+        dts = _parallel(work, _slabs(int(self.N[0]), 2 * (os.cpu_count() or 1)))
+        dT = min(dts)
+        if dT == 0 or dT >= 1e200:
+            raise ValueError("Operator: timestep is zero")
+        return dT
+
+    @staticmethod
+    def _var3_local(C32, L32, i0, i1):
+        """Minimum Rennings timestep over x-positions [i0, i1) of the given EC slab (the slab
+        carries one halo plane on each internal side)."""
+        C = C32.astype(np.float64)
+        Lh = L32.astype(np.float64)
+
+        def sh(arr, shifts):
+            """arr at pos+shift with AdrOp cell reflection (-1 -> 0, N -> N-1)."""
+            out = arr
+            for ax, s in shifts:
+                if s == 0:
+                    continue
+                Nn = arr.shape[ax]
+                idx = np.clip(np.arange(Nn) + s, 0, Nn - 1)
+                out = np.take(out, idx, axis=ax)
+            return out
+
+        dT = 1e200
+        with np.errstate(divide="ignore", invalid="ignore"):
+            for n in range(3):
+                a, p, pp = _axes(n)
+                Cn = C[n]
+                wqp = 1 / (Lh[pp] * sh(Cn, [(p, 1)])) + 1 / (Lh[pp] * Cn)
+                wqp += 1 / (Lh[p] * sh(Cn, [(pp, 1)])) + 1 / (Lh[p] * Cn)
+                Lpp_m = sh(Lh[pp], [(p, -1)])
+                wqp += 1 / (Lpp_m * Cn) + 1 / (Lpp_m * sh(Cn, [(p, -1)]))
+                # AdrOp shifts are cumulative: after Shift(nP,-1), Shift(nPP,-1) -> pos - eP - ePP
+                Lp_mm = sh(Lh[p], [(p, -1), (pp, -1)])
+                wqp += 1 / (Lp_mm * sh(Cn, [(p, -1)])) + 1 / (Lp_mm * sh(Cn, [(p, -1), (pp, -1)]))
+
+                Lpp_pm = sh(Lh[pp], [(p, -1)])
+                Lp_ppm = sh(Lh[p], [(pp, -1)])
+                w4 = [1 / (Lh[pp] * C[p]), 1 / (Lpp_pm * C[p]), 1 / (Lh[p] * C[pp]), 1 / (Lp_ppm * C[pp])]
+                wt1 = w4[0] + w4[1] + w4[2] + w4[3] - 2 * np.minimum(np.minimum(w4[0], w4[1]), np.minimum(w4[2], w4[3]))
+                Cp_n = sh(C[p], [(a, 1)])
+                Cpp_n = sh(C[pp], [(a, 1)])
+                w4 = [1 / (Lh[pp] * Cp_n), 1 / (Lpp_pm * Cp_n), 1 / (Lh[p] * Cpp_n), 1 / (Lp_ppm * Cpp_n)]
+                wt2 = w4[0] + w4[1] + w4[2] + w4[3] - 2 * np.minimum(np.minimum(w4[0], w4[1]), np.minimum(w4[2], w4[3]))
+                newT = (2 / np.sqrt(wqp + wt1 + wt2))[i0:i1]
+                cand = newT[np.isfinite(newT) & (newT > 0)]
+                if cand.size:
+                    dT = min(dT, float(cand.min()))
+        return dT
+
+    # ---- coefficients (FDTD/operator.cpp:956-984) ------------------------------------------
+    def _ec_op(self, C, G, L, R, dT):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            C = C.astype(np.float64)
+            G = G.astype(np.float64)
+            L = L.astype(np.float64)
+            R = R.astype(np.float64)
+            okc = C > 0
+            okl = L > 0
+            Cs = np.where(okc, C, 1.0)
+            Ls = np.where(okl, L, 1.0)
+            vv = np.where(okc, (1.0 - dT * G / 2.0 / Cs) / (1.0 + dT * G / 2.0 / Cs), 0.0)
+            vi = np.where(okc, (dT / Cs) / (1.0 + dT * G / 2.0 / Cs), 0.0)
+            ii = np.where(okl, (1.0 - dT * R / 2.0 / Ls) / (1.0 + dT * R / 2.0 / Ls), 0.0)
+            iv = np.where(okl, (dT / Ls) / (1.0 + dT * R / 2.0 / Ls), 0.0)
+        return vv.astype(np.float32), vi.astype(np.float32), ii.astype(np.float32), iv.astype(np.float32)
+
+    # ---- snapping (FDTD/operator.cpp:252-372) ----------------------------------------------
+    def snap_line(self, ny, coord, dual=False):
+        L = self.L[ny]
+        if coord < L[0]:
+            return 0, False
+        if coord > L[-1]:
+            return len(L) - 1, False
+        if not dual:
+            dl = self.dl[ny]
+            for n in range(len(L)):
+                if coord <= dl[n]:
+                    return n, True
+        else:
+            for n in range(1, len(L)):
+                if coord <= L[n]:
+                    return n - 1, True
+        return 0, True
+
+    def snap_box(self, start, stop, dual=False, method=0):
+        """SnapBox2Mesh; returns (dim, uiStart, uiStop, startIn, stopIn) or dim=-2 if outside."""
+        lstart = np.minimum(start, stop)
+        lstop = np.maximum(start, stop)
+        for n in range(3):
+            mn, mx = self.L[n][0], self.L[n][-1]
+            if (lstart[n] < mn and lstop[n] < mn) or (lstart[n] > mx and lstop[n] > mx):
+                return -2, None, None, None, None
+        s, si, e, ei = [0] * 3, [False] * 3, [0] * 3, [False] * 3
+        for n in range(3):
+            s[n], si[n] = self.snap_line(n, lstart[n], dual)
+            e[n], ei[n] = self.snap_line(n, lstop[n], dual)
+        dim = 0
+
+        def line(n, i):
+            return self.dl[n][i] if dual else self.L[n][i]
+        for n in range(3):
+            if method == 1 and e[n] > s[n]:
+                if line(n, s[n]) > lstart[n] and s[n] > 0:
+                    s[n] -= 1
+                if line(n, e[n]) < lstop[n] and e[n] < self.N[n] - 1:
+                    e[n] += 1
+            elif method == 2 and e[n] > s[n]:
+                if line(n, s[n]) < lstart[n] and s[n] < self.N[n] - 1:
+                    s[n] += 1
+                if line(n, e[n]) > lstop[n] and e[n] > 0:
+                    e[n] -= 1
+            if e[n] > s[n]:
+                dim += 1
+        return dim, np.array(s), np.array(e), np.array(si), np.array(ei)
+
+    # ---- the build --------------------------------------------------------------------------
+    def build(self, num_ts: int) -> OperatorData:
+        """CalcECOperator (FDTD/operator.cpp:986-1097) + extension builds + processing setup."""
+        self.calc_ec()
+        if self.forced_dt > 0:
+            dT = self.forced_dt
+        else:
+            dT = self.calc_timestep_var3()
+        dT *= self.ts_factor
+        if self.exc.period > 0:
+            TS = math.ceil(self.exc.period / dT)
+            dT = self.exc.period / TS
+        self.dT = dT
+        self.exc.Reset(dT)
+        self.exc.buildExcitationSignal(num_ts)
+
+        shape = (3,) + tuple(int(v) for v in self.N)
+        self.vv, self.vi, self.ii, self.iv = (np.empty(shape, np.float32) for _ in range(4))
+
+        def coef(x0, x1):
+            for n in range(3):
+                r = self._ec_op(self.EC_C[n, x0:x1], self.EC_G[n, x0:x1], self.EC_L[n, x0:x1],
+                                self.EC_R[n, x0:x1], dT)
+                for d, v in zip((self.vv, self.vi, self.ii, self.iv), r):
+                    d[n, x0:x1] = v
+        _parallel(coef, _slabs(int(self.N[0]), 2 * (os.cpu_count() or 1)))
+
+        self._apply_electric_bc([b != -1 for b in self.bc])
+        self._calc_pec()
+        self._calc_lumped()
+        self._apply_magnetic_bc([b == 1 for b in self.bc])
+
+        exc = self._build_excitation()
+        mur = self._build_mur(exc)
+        upml = self._build_upml()
+        lorentz = self._build_lorentz()
+        vprobes, iprobes, dumps = self._build_processing()
+        data = OperatorData(num_lines=self.N.astype(np.uint32), dt=dT, vv=self.vv, vi=self.vi, ii=self.ii,
+                            iv=self.iv, exc=exc, upml=upml, mur=mur, lorentz=lorentz, vprobes=vprobes,
+                            iprobes=iprobes, dumps=dumps, nyquist=self.exc.GetNyquistNum(),
+                            excitation=self.exc, grid=self.grid)
+        return data
+
+    # ---- boundary conditions ---------------------------------------------------------------
+    def _apply_electric_bc(self, dirs):
+        """ApplyElectricBC (FDTD/operator.cpp:1099-1138)."""
+        for n in range(3):
+            a, p, pp = _axes(n)
+            sl0 = [slice(None)] * 3
+            sl0[n] = 0
+            sl1 = [slice(None)] * 3
+            sl1[n] = int(self.N[n]) - 1
+            if dirs[2 * n]:
+                for c in (p, pp):
+                    self.vv[c][tuple(sl0)] = 0
+                    self.vi[c][tuple(sl0)] = 0
+            if dirs[2 * n + 1]:
+                for c in (n, p, pp):
+                    self.vv[c][tuple(sl1)] = 0
+                    self.vi[c][tuple(sl1)] = 0
+
+    def _apply_magnetic_bc(self, dirs):
+        """ApplyMagneticBC (FDTD/operator.cpp:1140-1187)."""
+        for n in range(3):
+            a, p, pp = _axes(n)
+            def sl(i):
+                s = [slice(None)] * 3
+                s[n] = i
+                return tuple(s)
+            if dirs[2 * n]:
+                for c in (n, p, pp):
+                    self.ii[c][sl(0)] = 0
+                    self.iv[c][sl(0)] = 0
+            if dirs[2 * n + 1]:
+                for c in (p, pp):
+                    self.ii[c][sl(int(self.N[n]) - 2)] = 0
+                    self.iv[c][sl(int(self.N[n]) - 2)] = 0
+            for c in (n, p, pp):
+                self.ii[c][sl(int(self.N[n]) - 1)] = 0
+                self.iv[c][sl(int(self.N[n]) - 1)] = 0
+
+    def _calc_pec(self):
+        """CalcPEC_Range (FDTD/operator.cpp:2045-2083): edges whose Yee point is in a METAL box."""
+        if not any(p.kind == METAL for p in self.csx.props):
+            return
+        painter = self._matmetal
+        metal_ids = np.array([p.kind == METAL for p in painter.props] + [False])
+        for n in range(3):
+            cs = [self.L[0], self.L[1], self.L[2]]
+            cs[n] = self.dl[n]
+            m = painter.paint(cs[0], cs[1], cs[2])
+            is_metal = metal_ids[m]
+            self.vv[n][is_metal] = 0
+            self.vi[n][is_metal] = 0
+
+    def _calc_lumped(self):
+        """Calc_LumpedElements (FDTD/operator.cpp:1586-1763), parallel RC boxes only."""
+        u = self.unit
+        for prop in self.csx.props:
+            if prop.kind != LUMPED:
+                continue
+            C = prop.params["C"]
+            R = prop.params["R"]
+            if not (C > 0):
+                C = float("nan")
+            if R < 0:
+                R = float("nan")
+            if math.isnan(R) and math.isnan(C):
+                continue
+            ny = prop.params["ny"]
+            nyP, nyPP = (ny + 1) % 3, (ny + 2) % 3
+            for lo, hi, _pr, _sq, _p, *_ in prop.boxes:
+                dim, s, e, _, _ = self.snap_box(lo, hi, dual=False, method=0)
+                if dim <= 0 or s[ny] == e[ny]:
+                    continue
+                # edge area / edge length per edge (GetEdgeArea(ny,pos)/GetEdgeLength(ny,pos))
+                def gc(pos):
+                    area = self.dd[nyP][pos[nyP]] * u * self.dd[nyPP][pos[nyPP]] * u
+                    return area / (self.md[ny][pos[ny]] * u)
+                unitGC = 0.0
+                pos = [0, 0, 0]
+                for pos[ny] in range(s[ny], e[ny]):
+                    plane = 0.0
+                    for pos[nyP] in range(s[nyP], e[nyP] + 1):
+                        for pos[nyPP] in range(s[nyPP], e[nyPP] + 1):
+                            plane += gc(pos)
+                    unitGC += 1 / plane
+                unitGC = 1 / unitGC
+                kappa = 1 / R / unitGC if R > 0 else 0.0
+                epsilon = 0.0
+                if C > 0:
+                    epsilon = C / unitGC
+                    if epsilon < EPS0:
+                        C = 0
+                for pos[ny] in range(s[ny], e[ny]):
+                    for pos[nyP] in range(s[nyP], e[nyP] + 1):
+                        for pos[nyPP] in range(s[nyPP], e[nyPP] + 1):
+                            x, y, z = pos
+                            if C > 0:
+                                self.EC_C[ny, x, y, z] = epsilon * gc(pos)
+                            if R > 0:
+                                self.EC_G[ny, x, y, z] = kappa * gc(pos)
+                            if R == 0:
+                                self.vv[ny, x, y, z] = 0
+                                self.vi[ny, x, y, z] = 0
+                            else:
+                                a_, b_, c_, d_ = self._ec_op(self.EC_C[ny, x, y, z], self.EC_G[ny, x, y, z],
+                                                             self.EC_L[ny, x, y, z], self.EC_R[ny, x, y, z], self.dT)
+                                self.vv[ny, x, y, z], self.vi[ny, x, y, z] = a_, b_
+                                self.ii[ny, x, y, z], self.iv[ny, x, y, z] = c_, d_
+                if prop.params["caps"]:
+                    for pos[nyP] in range(s[nyP], e[nyP] + 1):
+                        for pos[nyPP] in range(s[nyPP], e[nyPP] + 1):
+                            for pos[ny] in (s[ny], e[ny]):
+                                x, y, z = pos
+                                if pos[nyP] < e[nyP]:
+                                    self.vv[nyP, x, y, z] = 0
+                                    self.vi[nyP, x, y, z] = 0
+                                if pos[nyPP] < e[nyPP]:
+                                    self.vv[nyPP, x, y, z] = 0
+                                    self.vi[nyPP, x, y, z] = 0
+
+    # ---- excitation extension ----------------------------------------------------------------
+    def _build_excitation(self) -> ExcitationTable:
+        """Operator_Ext_Excitation::BuildExtension (operator_ext_excitation.cpp:105-297), boxes only.
+
+        List order follows the reference's loops: z outer, then y, then x, then the component.
+        """
+        u = self.unit
+        painter = _Painter(self.csx, EXCITATION)
+        vrec, crec = [], []
+        if painter.props:
+            for n in range(3):
+                # electric: Yee point of the main mesh, skip pos[n] >= N-1
+                cs = [self.L[0], self.L[1], self.L[2]]
+                cs[n] = self.dl[n]
+                m = painter.paint(*cs)
+                valid = np.ones(m.shape, bool)
+                sl = [slice(None)] * 3
+                sl[n] = slice(int(self.N[n]) - 1, None)
+                valid[tuple(sl)] = False
+                for x, y, z in zip(*np.nonzero((m >= 0) & valid)):
+                    prop = painter.props[m[x, y, z]]
+                    et = prop.params["exc_type"]
+                    if et not in (0, 1):
+                        continue
+                    amp = prop.params["exc_val"][n] * (self.md[n][(x, y, z)[n]] * u)
+                    if amp != 0:
+                        vrec.append((z, y, x, n, amp, int(prop.params["delay"] / self.dT)))
+                    if et == 1:
+                        self.vv[n, x, y, z] = 0
+                        self.vi[n, x, y, z] = 0
+                # magnetic: dual Yee point, skip the last H line in every direction
+                cs = [self.dl[0], self.dl[1], self.dl[2]]
+                cs[n] = self.L[n]
+                m = painter.paint(*cs)
+                valid = np.zeros(m.shape, bool)
+                valid[:-1, :-1, :-1] = True
+                for x, y, z in zip(*np.nonzero((m >= 0) & valid)):
+                    prop = painter.props[m[x, y, z]]
+                    et = prop.params["exc_type"]
+                    if et not in (2, 3):
+                        continue
+                    amp = prop.params["exc_val"][n] * (self.dd[n][(x, y, z)[n]] * u)
+                    if amp != 0:
+                        crec.append((z, y, x, n, amp, int(prop.params["delay"] / self.dT)))
+                    if et == 3:
+                        self.ii[n, x, y, z] = 0
+                        self.iv[n, x, y, z] = 0
+        vrec.sort(key=lambda r: (r[0], r[1], r[2], r[3]))
+        crec.sort(key=lambda r: (r[0], r[1], r[2], r[3]))
+
+        def pack(rec):
+            K = len(rec)
+            idx = np.zeros((3, K), np.uint32)
+            for i, r in enumerate(rec):
+                idx[:, i] = (r[2], r[1], r[0])
+            return (idx, np.array([r[3] for r in rec], np.uint16), np.array([r[4] for r in rec], np.float32),
+                    np.array([r[5] for r in rec], np.uint32))
+        vi_, vd, va, vdl = pack(vrec)
+        ci_, cd, ca, cdl = pack(crec)
+        return ExcitationTable(vi_, vd, va, vdl, ci_, cd, ca, cdl, self.exc.volt.copy(), self.exc.curr.copy(),
+                               self.exc.period_steps())
+
+    # ---- Mur ABC (operator_ext_mur_abc.cpp:80-186, engine_ext_mur_abc.cpp:30-57) -------------
+    def _build_mur(self, exc: ExcitationTable):
+        walls = []
+        u = self.unit
+        for w in range(6):
+            if self.bc[w] != 2:
+                continue
+            ny, top = w // 2, w % 2
+            nyP, nyPP = (ny + 1) % 3, (ny + 2) % 3
+            if not top:
+                line, shift = 0, 1
+            else:
+                line, shift = int(self.N[ny]) - 1, int(self.N[ny]) - 2
+            delta = abs(self.md[ny][line] * u)
+            c_ny = self.L[ny][line] + (delta / 2 / u if line == 0 else -delta / 2 / u)
+            cs = [None, None, None]
+            cs[ny] = np.array([c_ny])
+            cs[nyP] = self.L[nyP]
+            cs[nyPP] = self.L[nyPP]
+            m = self._mat.paint(*cs)
+            m2 = np.moveaxis(m, ny, 0)[0]            # axes now (nyP? ...) -> reorder below
+            # moveaxis leaves the remaining axes in increasing order; we need [nyP][nyPP]
+            if nyP > nyPP:
+                m2 = m2.T
+            eps = self._mat.param(m2, "epsilon", self.bg["epsilon"])
+            mue = self._mat.param(m2, "mue", self.bg["mue"])
+            c0t = C0 * self.dT / np.sqrt(eps * mue)
+            coeff = ((c0t - delta) / (c0t + delta)).astype(np.float32)
+            bg = C0 / math.sqrt(self.bg["epsilon"] * self.bg["mue"]) * self.dT
+            coeff_bg = np.float32((bg - delta) / (bg + delta))
+            coeff = np.where(m2 >= 0, coeff, coeff_bg).astype(np.float32)
+            # excitation inside the wall delays the ABC (engine_ext_mur_abc.cpp:44-60)
+            max_delay = -1
+            for i in range(exc.volt_dir.size):
+                if exc.volt_dir[i] in (nyP, nyPP) and exc.volt_index[ny, i] == line:
+                    max_delay = max(max_delay, int(exc.volt_delay[i]))
+            start_ts = 0
+            if max_delay >= 0:
+                start_ts = max_delay + int(self.exc.GetLength()) + 10
+            walls.append(MurWall(ny, line, shift, start_ts, coeff.copy(), coeff.copy()))
+        return walls
+
+    # ---- UPML (operator_ext_upml.cpp:69-445) -------------------------------------------------
+    @staticmethod
+    def _grading(D, dl, W, Z, N):
+        """Default grading " -log(1e-6)*log(2.5)/(2*dl*Z*(pow(2.5,W/dl)-1)) * pow(2.5, D/dl) "."""
+        return -math.log(1e-6) * math.log(2.5) / (2 * dl * Z * (np.power(2.5, W / dl) - 1)) * np.power(2.5, D / dl)
+
+    def _upml_regions(self):
+        BC = list(self.bc)
+        size = list(self.pml_size)
+        for n in range(3):
+            if size[2 * n] * (BC[2 * n] == 3) + size[2 * n + 1] * (BC[2 * n + 1] == 3) >= self.N[n]:
+                BC[2 * n] = BC[2 * n + 1] = 0
+                size[2 * n] = size[2 * n + 1] = 0
+        self._pml_bc, self._pml_sz = BC, size
+        regs = []
+        N = [int(v) for v in self.N]
+        start, stop = [0, 0, 0], [N[0] - 1, N[1] - 1, N[2] - 1]
+        if BC[0] == 3:
+            regs.append(([0, start[1], start[2]], [size[0], stop[1], stop[2]]))
+        if BC[1] == 3:
+            regs.append(([N[0] - 1 - size[1], start[1], start[2]], [N[0] - 1, stop[1], stop[2]]))
+        start[0] = (size[0] + 1) * (BC[0] == 3)
+        stop[0] = N[0] - 1 - (size[0] + 1) * (BC[1] == 3)
+        if BC[2] == 3:
+            regs.append(([start[0], 0, start[2]], [stop[0], size[2], stop[2]]))
+        if BC[3] == 3:
+            regs.append(([start[0], N[1] - 1 - size[3], start[2]], [stop[0], N[1] - 1, stop[2]]))
+        start[1] = (size[2] + 1) * (BC[2] == 3)
+        stop[1] = N[1] - 1 - (size[3] + 1) * (BC[3] == 3)
+        if BC[4] == 3:
+            regs.append(([start[0], start[1], 0], [stop[0], stop[1], size[4]]))
+        if BC[5] == 3:
+            regs.append(([start[0], start[1], N[2] - 1 - size[5]], [stop[0], stop[1], N[2] - 1]))
+        return regs
+
+    def _grading_kappa(self, ny, pos_axes):
+        """CalcGradingKappa (operator_ext_upml.cpp:269-343) vectorised per axis: returns
+        kappa_v[3], kappa_i[3] as 1-D arrays over that axis' region indices."""
+        kv, ki = [], []
+        u = self.unit
+        BC, sz = self._pml_bc, self._pml_sz
+        for n in range(3):
+            pos = pos_axes[n]
+            L = self.L[n]
+            N = int(self.N[n])
+            el = self.md[n][pos] * u
+            kvn = np.zeros(len(pos))
+            kin = np.zeros(len(pos))
+            low = (pos <= sz[2 * n]) & (BC[2 * n] == 3)
+            up = (~low) & (pos >= N - 1 - sz[2 * n + 1]) & (BC[2 * n + 1] == 3)
+            if low.any():
+                width = (L[sz[2 * n]] - L[0]) * u
+                depth = width - (L[pos] - L[0]) * u
+                if n == ny:
+                    depth = depth - el / 2
+                dl = width / sz[2 * n]
+                with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+                    g = self._grading(depth, dl, width, Z0, float(sz[2 * n]))
+                kvn = np.where(low & (depth > 0), g, kvn)
+                if n == ny:
+                    depth = depth + el / 2
+                if n != ny:
+                    depth = depth - el / 2
+                depth = np.where(depth < 0, 0.0, depth)
+                with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+                    g = self._grading(depth, dl, width, Z0, float(sz[2 * n]))
+                kin = np.where(low & (depth > 0), g, kin)
+            if up.any():
+                width = (L[N - 1] - L[N - sz[2 * n + 1] - 1]) * u
+                depth = width - (L[N - 1] - L[pos]) * u
+                if n == ny:
+                    depth = depth + el / 2
+                dl = width / sz[2 * n] if sz[2 * n] else float("inf")
+                with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+                    g = self._grading(depth, dl, width, Z0, float(sz[2 * n]))
+                kvn = np.where(up & (depth > 0), g, kvn)
+                if n == ny:
+                    depth = depth - el / 2
+                if n != ny:
+                    depth = depth + el / 2
+                depth = np.where(depth > width, 0.0, depth)
+                with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+                    g = self._grading(depth, dl, width, Z0, float(sz[2 * n]))
+                kin = np.where(up & (depth > 0), g, kin)
+            kv.append(np.nan_to_num(kvn))
+            ki.append(np.nan_to_num(kin))
+        return kv, ki
+
+    def _build_upml(self):
+        regs = self._upml_regions()
+        out = []
+        dT = self.dT
+        u = self.unit
+        for start, stop in regs:
+            start = np.array(start)
+            nl = np.array(stop) - start + 1
+            sl = tuple(slice(int(start[k]), int(start[k] + nl[k])) for k in range(3))
+            pos_axes = [np.arange(start[k], start[k] + nl[k]) for k in range(3)]
+            shape = tuple(int(v) for v in nl)
+            arrs = {k: np.zeros((3,) + shape, np.float32) for k in ("vv", "vvfo", "vvfn", "ii", "iifo", "iifn")}
+            for n in range(3):
+                a, p, pp = _axes(n)
+                kv1, ki1 = self._grading_kappa(n, pos_axes)
+                KV = [kv1[k].reshape([-1 if j == k else 1 for j in range(3)]) for k in range(3)]
+                KI = [ki1[k].reshape([-1 if j == k else 1 for j in range(3)]) for k in range(3)]
+                ksum_v = np.broadcast_to(KV[0] + KV[1] + KV[2], shape)
+                ksum_i = np.broadcast_to(KI[0] + KI[1] + KI[2], shape)
+                eff_eps, eff_kap, eff_mue, _ = self.eff_region(n, start, nl)
+                op_vv = self.vv[n][sl]
+                op_vi = self.vi[n][sl]
+                op_ii = self.ii[n][sl]
+                op_iv = self.iv[n][sl]
+                # GetEdgeLength(n,pos)/GetEdgeArea(n,pos) and their dual versions
+                De, Ap, App = _bcast(n, self.md[a][pos_axes[a]] * u, self.dd[p][pos_axes[p]] * u, self.dd[pp][pos_axes[pp]] * u)
+                Dh, Bp, Bpp = _bcast(n, self.dd[a][pos_axes[a]] * u, self.md[p][pos_axes[p]] * u, self.md[pp][pos_axes[pp]] * u)
+                kvp = np.broadcast_to(KV[p], shape)
+                kvpp = np.broadcast_to(KV[pp], shape)
+                kvn = np.broadcast_to(KV[a], shape)
+                kip = np.broadcast_to(KI[p], shape)
+                kipp = np.broadcast_to(KI[pp], shape)
+                kin = np.broadcast_to(KI[a], shape)
+                # ---- voltages
+                act_v = (ksum_v != 0) & (eff_kap < 1e3)
+                not_pec = (op_vv + op_vi) != 0
+                mod = act_v & not_pec
+                new_vv = ((2 * EPS0 - kvp * dT) / (2 * EPS0 + kvp * dT)).astype(np.float32)
+                new_vi = ((2 * EPS0 * dT) / (2 * EPS0 + kvp * dT) * De / (Ap * App)).astype(np.float32)
+                e_vv = ((2 * EPS0 - kvpp * dT) / (2 * EPS0 + kvpp * dT)).astype(np.float32)
+                e_vvfn = ((2 * EPS0 + kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(np.float32)
+                e_vvfo = ((2 * EPS0 - kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(np.float32)
+                arrs["vv"][n] = np.where(mod, e_vv, np.where(act_v, 0, op_vv))
+                arrs["vvfn"][n] = np.where(mod, e_vvfn, np.where(act_v, 0, 1))
+                arrs["vvfo"][n] = np.where(mod, e_vvfo, 0)
+                self.vv[n][sl] = np.where(mod, new_vv, np.where(act_v, op_vv, 0))
+                self.vi[n][sl] = np.where(mod, new_vi, op_vi)
+                # ---- currents
+                act_i = ksum_i != 0
+                not_pmc = (op_ii + op_iv) != 0
+                mod = act_i & not_pmc
+                new_ii = ((2 * EPS0 - kip * dT) / (2 * EPS0 + kip * dT)).astype(np.float32)
+                new_iv = ((2 * EPS0 * dT) / (2 * EPS0 + kip * dT) * Dh / (Bp * Bpp)).astype(np.float32)
+                e_ii = ((2 * EPS0 - kipp * dT) / (2 * EPS0 + kipp * dT)).astype(np.float32)
+                e_iifn = ((2 * EPS0 + kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(np.float32)
+                e_iifo = ((2 * EPS0 - kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(np.float32)
+                arrs["ii"][n] = np.where(mod, e_ii, np.where(act_i, 0, op_ii))
+                arrs["iifn"][n] = np.where(mod, e_iifn, np.where(act_i, 0, 1))
+                arrs["iifo"][n] = np.where(mod, e_iifo, 0)
+                self.ii[n][sl] = np.where(mod, new_ii, np.where(act_i, op_ii, 0))
+                self.iv[n][sl] = np.where(mod, new_iv, op_iv)
+            out.append(UPMLRegion(start.astype(np.uint32), nl.astype(np.uint32), **arrs))
+        return out
+
+    # ---- Lorentz / Drude (operator_ext_lorentzmaterial.cpp:120-445) ---------------------------
+    def _build_lorentz(self):
+        """Operator_Ext_LorentzMaterial::BuildExtension, evaluated in parallel x-slabs; positions
+        come out in the reference's x-major scan order."""
+        lor_props = [p for p in self.csx.props if p.kind == MATERIAL and p.params.get("lorentz")]
+        if not lor_props:
+            return []
+        order_max = max(p.params["order"] for p in lor_props)
+        painter = self._matmetal
+        dT = self.dT
+        Nx = int(self.N[0])
+        orders = []
+        for o in range(order_max):
+            def ptab(key):
+                vals = []
+                for p in painter.props:
+                    if p.kind == MATERIAL and p.params.get("lorentz") and o < p.params["order"]:
+                        vals.append(p.params[key][o])
+                    else:
+                        vals.append(0.0)
+                return np.array(vals + [0.0], np.float64)
+            tab = {k: ptab(k) for k in ("eps_plasma", "eps_relax", "eps_pole", "mue_plasma", "mue_relax", "mue_pole")}
+
+            def slab(x0, x1):
+                per_n = []
+                on_mask = np.zeros((x1 - x0,) + tuple(int(v) for v in self.N[1:]), bool)
+                flags = [False, False, False, False]
+                for n in range(3):
+                    # voltage part: main Yee point, skip pos[n] >= N-1 and edges with VI == 0
+                    cs = [self.L[0][x0:x1], self.L[1], self.L[2]]
+                    if n == 0:
+                        cs[0] = self.dl[0][x0:x1]
+                    else:
+                        cs[n] = self.dl[n]
+                    m = painter.paint(*cs)
+                    valid = self.vi[n, x0:x1] != 0
+                    if n == 0:
+                        if x1 == Nx:
+                            valid[-1] = False
+                    else:
+                        sl = [slice(None)] * 3
+                        sl[n] = slice(int(self.N[n]) - 1, None)
+                        valid[tuple(sl)] = False
+                    wp = tab["eps_plasma"][m] * 2 * PI
+                    trel = tab["eps_relax"][m]
+                    wl = tab["eps_pole"][m] * 2 * PI
+                    C = self.EC_C[n, x0:x1].astype(np.float64)
+                    with np.errstate(divide="ignore", invalid="ignore"):
+                        LD = np.where(valid & (wp > 0) & (C > 0), 1 / (wp * wp * C), 0.0)
+                        RD = np.where((LD > 0) & (trel > 0), LD / np.where(trel > 0, trel, 1), 0.0)
+                        CL = np.where((LD > 0) & (wl > 0), 1 / (wl * wl * np.where(LD > 0, LD, 1)), 0.0)
+                    flags[0] |= bool((LD > 0).any())
+                    flags[2] |= bool((CL > 0).any())
+                    # current part: dual Yee point, skip the last H lines and IV == 0
+                    cs = [self.dl[0][x0:x1], self.dl[1], self.dl[2]]
+                    if n == 0:
+                        cs[0] = self.L[0][x0:x1]
+                    else:
+                        cs[n] = self.L[n]
+                    m2 = painter.paint(*cs)
+                    valid2 = self.iv[n, x0:x1] != 0
+                    if x1 == Nx:
+                        valid2[-1] = False
+                    valid2[:, -1, :] = False
+                    valid2[:, :, -1] = False
+                    wpm = tab["mue_plasma"][m2] * 2 * PI
+                    trelm = tab["mue_relax"][m2]
+                    wlm = tab["mue_pole"][m2] * 2 * PI
+                    Lh = self.EC_L[n, x0:x1].astype(np.float64)
+                    with np.errstate(divide="ignore", invalid="ignore"):
+                        CD = np.where(valid2 & (wpm > 0) & (Lh > 0), 1 / (wpm * wpm * Lh), 0.0)
+                        GD = np.where((CD > 0) & (trelm > 0), CD / np.where(trelm > 0, trelm, 1), 0.0)
+                        LL = np.where((CD > 0) & (wlm > 0), 1 / (wlm * wlm * np.where(CD > 0, CD, 1)), 0.0)
+                    flags[1] |= bool((CD > 0).any())
+                    flags[3] |= bool((LL > 0).any())
+                    on_mask |= (LD > 0) | (CD > 0)
+                    per_n.append((LD, RD, CL, CD, GD, LL))
+                pos = np.array(np.nonzero(on_mask), dtype=np.int64)
+                sel = tuple(pos)
+                M = pos.shape[1]
+                tabs = {k: np.zeros((3, M), np.float32) for k in ("v_int", "v_ext", "v_lor", "i_int", "i_ext", "i_lor")}
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    for n in range(3):
+                        LD, RD, CL, CD, GD, LL = (t[sel] for t in per_n[n])
+                        VI = self.vi[n, x0:x1][sel].astype(np.float64)
+                        IV = self.iv[n, x0:x1][sel].astype(np.float64)
+                        drude = LD > 0
+                        tabs["v_int"][n] = np.where(drude, (2.0 * LD - dT * RD) / (2.0 * LD + dT * RD), 1.0)
+                        tabs["v_ext"][n] = np.where(drude, dT / (LD + dT * RD / 2.0) * VI, 0.0)
+                        tabs["i_int"][n] = np.where(CD > 0, (2.0 * CD - dT * GD) / (2.0 * CD + dT * GD), 1.0)
+                        tabs["i_ext"][n] = np.where(CD > 0, dT / (CD + dT * GD / 2.0) * IV, 0.0)
+                        tabs["v_lor"][n] = np.where(CL > 0, dT / CL / VI, 0.0)
+                        tabs["i_lor"][n] = np.where(LL > 0, dT / LL / IV, 0.0)
+                pos[0] += x0
+                return pos.astype(np.uint32), tabs, flags
+
+            parts = _parallel(slab, _slabs(Nx, 2 * (os.cpu_count() or 1)))
+            pos = np.concatenate([p[0] for p in parts], axis=1)
+            tabs = {k: np.concatenate([p[1][k] for p in parts], axis=1) for k in parts[0][1]}
+            fl = [any(p[2][i] for p in parts) for i in range(4)]
+            orders.append(LorentzOrder(pos, fl[0], fl[1], fl[2], fl[3], **tabs))
+        return orders
+
+    # ---- processing (probes, FD dumps) ---------------------------------------------------------
+    def _build_processing(self):
+        vprobes, iprobes, dumps = [], [], []
+        nyq = self.exc.GetNyquistNum()
+        for prop in self.csx.props:
+            if prop.kind == PROBE:
+                pt = prop.params["p_type"]
+                interval = max(1, nyq // self.over_sampling)
+                if prop.params.get("interval"):
+                    interval = int(prop.params["interval"])
+                fd_interval = 0
+                freqs = []
+                for f in prop.params["frequency"]:
+                    nts = calc_nyquist_num(f, self.dT)
+                    if nts == 0:
+                        continue
+                    if fd_interval == 0:
+                        fd_interval = nyq
+                    if fd_interval > nts:
+                        fd_interval = nts
+                    freqs.append(float(f))
+                start_ts, stop_ts = 0, 0xFFFFFFFF
+                if prop.params["start_time"] > 0:
+                    start_ts = int(math.floor(prop.params["start_time"] / self.dT))
+                if prop.params["stop_time"] > 0:
+                    stop_ts = int(math.ceil(prop.params["stop_time"] / self.dT))
+                for lo, hi, _pr, _sq, _p, b_start, b_stop in prop.boxes:
+                    if pt == 0:
+                        s = np.array([self.snap_line(n, b_start[n], False)[0] for n in range(3)])
+                        e = np.array([self.snap_line(n, b_stop[n], False)[0] for n in range(3)])
+                        # keep the user's start/stop order (the sign of the integral follows it)
+                        vprobes.append(VoltageProbe(prop.name, s, e, prop.params["weight"], interval, fd_interval,
+                                                    freqs, start_ts, stop_ts))
+                    elif pt == 1:
+                        dim, s, e, si, ei = self.snap_box(lo, hi, dual=True, method=1)
+                        if dim < 0:
+                            continue
+                        nd = prop.params["norm_dir"]
+                        if nd < 0 or nd > 2:
+                            if dim != 2:
+                                continue
+                            for n in range(3):
+                                if e[n] == s[n]:
+                                    nd = n
+                        else:
+                            for n in range(3):
+                                if n == nd:
+                                    continue
+                                if lo[n] == hi[n]:
+                                    if self.dl[n][s[n]] > lo[n] and s[n] > 0:
+                                        s[n] -= 1
+                                    if self.dl[n][s[n]] < lo[n] and e[n] < self.N[n] - 1:
+                                        e[n] += 1
+                        if s[nd] != e[nd]:
+                            continue
+                        iprobes.append(CurrentProbe(prop.name, s, e, nd, si, ei, prop.params["weight"], interval,
+                                                    fd_interval, freqs, start_ts, stop_ts))
+            elif prop.kind == DUMP:
+                dt_ = prop.params["dump_type"]
+                if dt_ not in (10, 11):
+                    continue
+                fd_interval = 0
+                freqs = []
+                for f in prop.params["frequency"]:
+                    nts = calc_nyquist_num(f, self.dT)
+                    if nts == 0:
+                        continue
+                    if fd_interval == 0:
+                        fd_interval = nyq
+                    if fd_interval > nts:
+                        fd_interval = nts
+                    freqs.append(float(f))
+                for lo, hi, _pr, _sq, _p, *_ in prop.boxes:
+                    # cell interpolation snaps to the dual mesh (Common/processfields.cpp:164-172)
+                    dim, s, e, _, _ = self.snap_box(lo, hi, dual=prop.params["dump_mode"] == 1, method=0)
+                    if dim < 0:
+                        continue
+                    dumps.append(FieldDumpFD(prop.name, dt_ - 10, s, e, freqs, fd_interval))
+        return vprobes, iprobes, dumps
+
+
+def box_lines(start, stop, n):
+    """Uniform helper: n+1 equally spaced lines between start and stop."""
+    return np.linspace(start, stop, n + 1)

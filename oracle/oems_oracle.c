@@ -1,0 +1,1414 @@
+/*
+ * oems_oracle.c -- ORACLE / TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C CPU restatement of openEMS's EC-FDTD engine path, used by the tests (as the
+ * checker of the CUDA engine), by __graft_entry__.smoke() and by bench.py's CPU-baseline leg.
+ * Nothing in the product imports, links or calls this file.
+ *
+ * It exposes the same C ABI shape as include/oems_cuda.h with the prefix oems_ref_ and two
+ * storage modes:
+ *
+ *  - "basic": fields and coefficients in N-I-J-K order, updated exactly like Engine
+ *    (FDTD/engine.cpp:110-222), one thread.  This is the semantic reference: separate float
+ *    multiply and add (build with -ffp-contract=off), no flush-to-zero.
+ *  - "mt":    the default openEMS engine, multithreaded SSE-compressed: fields as 4-lane
+ *    vectors in I-J-K-N order (tools/arraylib/array_e.h:53-61) with lane-strided z
+ *    (FDTD/engine_sse.h:38-47), coefficients deduplicated per 4-lane vector like
+ *    Operator_SSE_Compressed::CompressOperator (FDTD/operator_sse_compressed.cpp:114-175), the
+ *    update of Engine_SSE_Compressed (FDTD/engine_sse_compressed.cpp:51-311) and the x-slab
+ *    thread driver of NS_Engine_Multithread::thread::operator() (FDTD/engine_multithread.cpp:
+ *    310-402) with pthread barriers.  Its results equal the basic mode's bit for bit, which is
+ *    the reference's own engine contract (TESTSUITE/enginetests/cavity.m).
+ *
+ * Extensions follow the reference's phase order and priorities (FDTD/engine.cpp:224-286,
+ * FDTD/extensions/engine_extension.h:21-29): pre hooks in reverse priority, post/apply hooks in
+ * priority order: UPML (+1e6), then Lorentz (0, inserted after Mur), Mur walls (0, reverse
+ * insertion), excitation (-1000).
+ */
+#include <complex.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#undef I /* complex.h's imaginary unit; this file names a current field I */
+
+typedef float v4sf __attribute__((vector_size(16)));
+
+#define OK 0
+#define ERR_ARG 1
+#define ERR_STATE 3
+#define ERR_UNSUPPORTED 4
+#define ERR_NOMEM 6
+
+#define EPS0 8.85418781762e-12
+#define MUE0 1.256637062e-6
+#define M_PI_REF 3.14159265358979323846
+
+#define MAX_UPML 6
+#define MAX_MUR 6
+#define MAX_LOR 16
+#define MAX_PROBES 256
+#define MAX_DUMPS 64
+
+typedef struct {
+    unsigned start[3], nl[3];
+    size_t n;
+    float *vv, *vvfo, *vvfn, *ii, *iifo, *iifn, *vflux, *iflux;
+} upml_t;
+
+typedef struct {
+    int ny, nyP, nyPP;
+    unsigned line, shift, start_ts, n1, n2;
+    float *cP, *cPP, *bP, *bPP;
+} mur_t;
+
+typedef struct {
+    unsigned count;
+    unsigned *pos;
+    int von, con, vlon, clon;
+    float *vint, *vext, *vlor, *iint, *iext, *ilor;
+    float *vade, *vlade, *iade, *ilade;
+} lor_t;
+
+typedef struct {
+    int type; /* 0 voltage, 1 current */
+    unsigned start[3], stop[3];
+    int nd, si[3], ei[3];
+    double weight;
+    unsigned interval, start_ts, stop_ts;
+    double *series;
+    size_t nslots;
+    unsigned fd_interval, nf;
+    double *freqs;
+    double *dft;
+} probe_t;
+
+typedef struct {
+    int field;
+    unsigned start[3], stop[3], sz[3];
+    unsigned fd_interval, nf;
+    double *freqs;
+    double *el[3], *del[3];
+    float *acc; /* [nf][3][sx][sy][sz][2] */
+} dump_t;
+
+typedef struct oems_ref_engine {
+    unsigned N[3];
+    size_t cells;
+    double dt;
+    unsigned numTS, maxTS;
+    int inited;
+    /* basic */
+    float *volt, *curr;
+    float *vv, *vi, *ii, *iv;
+    /* mt */
+    int mt, nthreads;
+    unsigned nv;
+    v4sf *f4volt, *f4curr;
+    unsigned *op_index;
+    unsigned nclasses;
+    v4sf *cvv, *cvi, *cii, *civ; /* [3][nclasses] */
+    pthread_t *threads;
+    pthread_barrier_t bar_iter, bar_start, bar_stop;
+    unsigned *tstart, *tstop, *tstop_h;
+    volatile int stop_threads;
+    unsigned iter_ts;
+    /* excitation */
+    unsigned nV, nI, sig_len, period;
+    unsigned *v_idx, *i_idx, *v_delay, *i_delay;
+    unsigned short *v_dir, *i_dir;
+    float *v_amp, *i_amp, *sig_v, *sig_i;
+    /* extensions */
+    upml_t upml[MAX_UPML];
+    int nupml;
+    mur_t mur[MAX_MUR];
+    int nmur;
+    lor_t lor[MAX_LOR];
+    int nlor;
+    probe_t probes[MAX_PROBES];
+    int nprobes;
+    dump_t dumps[MAX_DUMPS];
+    int ndumps;
+    char err[512];
+} eng_t;
+
+/* ------------------------------------------------------------------------------------------ */
+/* field access: Engine::GetVolt / Engine_sse::GetVolt (FDTD/engine.h:55-101, engine_sse.h:38-84) */
+
+static inline size_t nijk(const eng_t *e, unsigned n, unsigned x, unsigned y, unsigned z)
+{
+    return (((size_t)n * e->N[0] + x) * e->N[1] + y) * e->N[2] + z;
+}
+
+static inline float *fptr(eng_t *e, int curr, unsigned n, unsigned x, unsigned y, unsigned z)
+{
+    if (!e->mt)
+        return (curr ? e->curr : e->volt) + nijk(e, n, x, y, z);
+    unsigned v = z % e->nv, l = z / e->nv;
+    v4sf *base = curr ? e->f4curr : e->f4volt;
+    return ((float *)&base[(((size_t)x * e->N[1] + y) * e->nv + v) * 3 + n]) + l;
+}
+
+#define GETV(e, n, x, y, z) (*fptr((e), 0, (n), (x), (y), (z)))
+#define GETI(e, n, x, y, z) (*fptr((e), 1, (n), (x), (y), (z)))
+
+static void *xcalloc(size_t n, size_t s)
+{
+    if (n == 0)
+        n = 1;
+    return calloc(n, s);
+}
+
+static float *dupf(const float *src, size_t n)
+{
+    if (!src)
+        return NULL;
+    float *d = (float *)xcalloc(n, sizeof(float));
+    if (d)
+        memcpy(d, src, n * sizeof(float));
+    return d;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* lifecycle */
+
+static int create_common(const unsigned nl[3], double dt, eng_t **out)
+{
+    if (!nl || !out || nl[0] < 2 || nl[1] < 2 || nl[2] < 2 || !(dt > 0))
+        return ERR_ARG;
+    eng_t *e = (eng_t *)calloc(1, sizeof(eng_t));
+    if (!e)
+        return ERR_NOMEM;
+    memcpy(e->N, nl, sizeof(e->N));
+    e->cells = (size_t)nl[0] * nl[1] * nl[2];
+    e->dt = dt;
+    *out = e;
+    return OK;
+}
+
+int oems_ref_create(const unsigned nl[3], double dt, int device, eng_t **out)
+{
+    (void)device;
+    int rc = create_common(nl, dt, out);
+    if (rc)
+        return rc;
+    eng_t *e = *out;
+    e->volt = (float *)xcalloc(3 * e->cells, sizeof(float));
+    e->curr = (float *)xcalloc(3 * e->cells, sizeof(float));
+    if (!e->volt || !e->curr)
+        return ERR_NOMEM;
+    return OK;
+}
+
+/* The multithreaded SSE-compressed engine (Engine_Multithread over Engine_SSE_Compressed). */
+int oems_ref_create_mt(const unsigned nl[3], double dt, int nthreads, eng_t **out)
+{
+    int rc = create_common(nl, dt, out);
+    if (rc)
+        return rc;
+    eng_t *e = *out;
+    e->mt = 1;
+    e->nthreads = nthreads > 0 ? nthreads : 1;
+    e->nv = (unsigned)ceil((double)nl[2] / 4.0); /* FDTD/engine_sse.cpp:40 */
+    size_t nvec = (size_t)nl[0] * nl[1] * e->nv * 3;
+    e->f4volt = (v4sf *)aligned_alloc(16, nvec * sizeof(v4sf));
+    e->f4curr = (v4sf *)aligned_alloc(16, nvec * sizeof(v4sf));
+    if (!e->f4volt || !e->f4curr)
+        return ERR_NOMEM;
+    memset(e->f4volt, 0, nvec * sizeof(v4sf));
+    memset(e->f4curr, 0, nvec * sizeof(v4sf));
+    return OK;
+}
+
+static void stop_threads(eng_t *e);
+
+void oems_ref_destroy(eng_t *e)
+{
+    if (!e)
+        return;
+    if (e->threads)
+        stop_threads(e);
+    free(e->volt); free(e->curr);
+    free(e->vv); free(e->vi); free(e->ii); free(e->iv);
+    free(e->f4volt); free(e->f4curr); free(e->op_index);
+    free(e->cvv); free(e->cvi); free(e->cii); free(e->civ);
+    free(e->tstart); free(e->tstop); free(e->tstop_h);
+    free(e->v_idx); free(e->i_idx); free(e->v_delay); free(e->i_delay);
+    free(e->v_dir); free(e->i_dir); free(e->v_amp); free(e->i_amp); free(e->sig_v); free(e->sig_i);
+    for (int r = 0; r < e->nupml; ++r) {
+        upml_t *u = &e->upml[r];
+        free(u->vv); free(u->vvfo); free(u->vvfn); free(u->ii); free(u->iifo); free(u->iifn);
+        free(u->vflux); free(u->iflux);
+    }
+    for (int w = 0; w < e->nmur; ++w) {
+        mur_t *m = &e->mur[w];
+        free(m->cP); free(m->cPP); free(m->bP); free(m->bPP);
+    }
+    for (int o = 0; o < e->nlor; ++o) {
+        lor_t *l = &e->lor[o];
+        free(l->pos); free(l->vint); free(l->vext); free(l->vlor); free(l->iint); free(l->iext); free(l->ilor);
+        free(l->vade); free(l->vlade); free(l->iade); free(l->ilade);
+    }
+    for (int p = 0; p < e->nprobes; ++p) {
+        free(e->probes[p].series); free(e->probes[p].freqs); free(e->probes[p].dft);
+    }
+    for (int d = 0; d < e->ndumps; ++d) {
+        dump_t *q = &e->dumps[d];
+        free(q->freqs); free(q->acc);
+        for (int n = 0; n < 3; ++n) { free(q->el[n]); free(q->del[n]); }
+    }
+    free(e);
+}
+
+const char *oems_ref_last_error(const eng_t *e)
+{
+    return e ? e->err : "null engine";
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* operator */
+
+/* 4-lane compression key: 12 f4 vectors (vv,vi,iv,ii x 3), bitwise equality like SSE_coeff::operator== */
+typedef struct {
+    uint32_t w[48];
+} ckey_t;
+
+static uint64_t key_hash(const ckey_t *k)
+{
+    uint64_t h = 1469598103934665603ULL;
+    for (int i = 0; i < 48; ++i) {
+        h ^= k->w[i];
+        h *= 1099511628211ULL;
+        h ^= h >> 29;
+    }
+    return h;
+}
+
+static int compress_mt(eng_t *e, const float *vv, const float *vi, const float *ii, const float *iv)
+{
+    unsigned Nx = e->N[0], Ny = e->N[1], Nz = e->N[2], nv = e->nv;
+    size_t nvecpos = (size_t)Nx * Ny * nv;
+    e->op_index = (unsigned *)xcalloc(nvecpos, sizeof(unsigned));
+    size_t cap = 1024, used = 0;
+    ckey_t *keys = (ckey_t *)malloc(cap * sizeof(ckey_t));
+    size_t hcap = 1 << 16;
+    int64_t *htab = (int64_t *)malloc(hcap * sizeof(int64_t));
+    if (!e->op_index || !keys || !htab)
+        return ERR_NOMEM;
+    for (size_t i = 0; i < hcap; ++i)
+        htab[i] = -1;
+    const float *arr[4] = {vv, vi, iv, ii};
+    ckey_t k;
+    for (unsigned x = 0; x < Nx; ++x)
+        for (unsigned y = 0; y < Ny; ++y)
+            for (unsigned v = 0; v < nv; ++v) {
+                for (int a = 0; a < 4; ++a)
+                    for (int n = 0; n < 3; ++n)
+                        for (int l = 0; l < 4; ++l) {
+                            unsigned z = v + l * nv;
+                            float val = 0.0f; /* lanes beyond Nz stay zero (Operator_sse::InitOperator) */
+                            if (z < Nz)
+                                val = arr[a][nijk(e, n, x, y, z)];
+                            memcpy(&k.w[(a * 3 + n) * 4 + l], &val, 4);
+                        }
+                uint64_t h = key_hash(&k);
+                size_t slot = h & (hcap - 1);
+                int64_t found = -1;
+                while (htab[slot] >= 0) {
+                    if (memcmp(&keys[htab[slot]], &k, sizeof(ckey_t)) == 0) {
+                        found = htab[slot];
+                        break;
+                    }
+                    slot = (slot + 1) & (hcap - 1);
+                }
+                if (found < 0) {
+                    if (used == cap) {
+                        cap *= 2;
+                        keys = (ckey_t *)realloc(keys, cap * sizeof(ckey_t));
+                        if (!keys)
+                            return ERR_NOMEM;
+                    }
+                    keys[used] = k;
+                    htab[slot] = (int64_t)used;
+                    found = (int64_t)used++;
+                    if (used * 2 > hcap) { /* rehash */
+                        free(htab);
+                        hcap *= 4;
+                        htab = (int64_t *)malloc(hcap * sizeof(int64_t));
+                        if (!htab)
+                            return ERR_NOMEM;
+                        for (size_t i = 0; i < hcap; ++i)
+                            htab[i] = -1;
+                        for (size_t j = 0; j < used; ++j) {
+                            size_t s2 = key_hash(&keys[j]) & (hcap - 1);
+                            while (htab[s2] >= 0)
+                                s2 = (s2 + 1) & (hcap - 1);
+                            htab[s2] = (int64_t)j;
+                        }
+                    }
+                }
+                e->op_index[((size_t)x * Ny + y) * nv + v] = (unsigned)found;
+            }
+    e->nclasses = (unsigned)used;
+    e->cvv = (v4sf *)aligned_alloc(16, 3 * used * sizeof(v4sf) + 16);
+    e->cvi = (v4sf *)aligned_alloc(16, 3 * used * sizeof(v4sf) + 16);
+    e->cii = (v4sf *)aligned_alloc(16, 3 * used * sizeof(v4sf) + 16);
+    e->civ = (v4sf *)aligned_alloc(16, 3 * used * sizeof(v4sf) + 16);
+    if (!e->cvv || !e->cvi || !e->cii || !e->civ)
+        return ERR_NOMEM;
+    v4sf *tabs[4] = {e->cvv, e->cvi, e->civ, e->cii};
+    for (size_t j = 0; j < used; ++j)
+        for (int a = 0; a < 4; ++a)
+            for (int n = 0; n < 3; ++n)
+                memcpy(&tabs[a][n * used + j], &keys[j].w[(a * 3 + n) * 4], 16);
+    free(keys);
+    free(htab);
+    return OK;
+}
+
+int oems_ref_set_operator(eng_t *e, const float *vv, const float *vi, const float *ii, const float *iv,
+                          unsigned max_classes)
+{
+    (void)max_classes;
+    if (!e || !vv || !vi || !ii || !iv)
+        return ERR_ARG;
+    if (e->mt)
+        return compress_mt(e, vv, vi, ii, iv);
+    size_t n = 3 * e->cells;
+    free(e->vv); free(e->vi); free(e->ii); free(e->iv);
+    e->vv = dupf(vv, n); e->vi = dupf(vi, n); e->ii = dupf(ii, n); e->iv = dupf(iv, n);
+    return (e->vv && e->vi && e->ii && e->iv) ? OK : ERR_NOMEM;
+}
+
+int oems_ref_operator_classes(const eng_t *e, unsigned *nc)
+{
+    if (!e || !nc)
+        return ERR_ARG;
+    *nc = e->mt ? e->nclasses : 0;
+    return OK;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* extensions: setup */
+
+int oems_ref_set_excitation(eng_t *e, unsigned nV, const unsigned *v_idx, const unsigned short *v_dir,
+                            const float *v_amp, const unsigned *v_delay, unsigned nI, const unsigned *i_idx,
+                            const unsigned short *i_dir, const float *i_amp, const unsigned *i_delay,
+                            const float *sig_v, const float *sig_i, unsigned length, unsigned period)
+{
+    if (!e || (length && (!sig_v || !sig_i)))
+        return ERR_ARG;
+    for (unsigned k = 0; k < nV; ++k)
+        for (int a = 0; a < 3; ++a)
+            if (v_idx[a * nV + k] >= e->N[a] || v_dir[k] > 2)
+                return ERR_ARG;
+    for (unsigned k = 0; k < nI; ++k)
+        for (int a = 0; a < 3; ++a)
+            if (i_idx[a * nI + k] >= e->N[a] || i_dir[k] > 2)
+                return ERR_ARG;
+    e->nV = nV; e->nI = nI; e->sig_len = length; e->period = period;
+    e->v_idx = (unsigned *)xcalloc(3 * (size_t)nV, 4); memcpy(e->v_idx, v_idx, 12 * (size_t)nV);
+    e->i_idx = (unsigned *)xcalloc(3 * (size_t)nI, 4); if (nI) memcpy(e->i_idx, i_idx, 12 * (size_t)nI);
+    e->v_dir = (unsigned short *)xcalloc(nV, 2); if (nV) memcpy(e->v_dir, v_dir, 2 * (size_t)nV);
+    e->i_dir = (unsigned short *)xcalloc(nI, 2); if (nI) memcpy(e->i_dir, i_dir, 2 * (size_t)nI);
+    e->v_amp = dupf(v_amp, nV); e->i_amp = dupf(i_amp, nI);
+    e->v_delay = (unsigned *)xcalloc(nV, 4); if (nV) memcpy(e->v_delay, v_delay, 4 * (size_t)nV);
+    e->i_delay = (unsigned *)xcalloc(nI, 4); if (nI) memcpy(e->i_delay, i_delay, 4 * (size_t)nI);
+    e->sig_v = dupf(sig_v, length); e->sig_i = dupf(sig_i, length);
+    return OK;
+}
+
+int oems_ref_add_upml(eng_t *e, const unsigned start[3], const unsigned nl[3], const float *vv,
+                      const float *vvfo, const float *vvfn, const float *ii, const float *iifo, const float *iifn)
+{
+    if (!e || e->nupml >= MAX_UPML)
+        return ERR_ARG;
+    for (int a = 0; a < 3; ++a)
+        if (start[a] + nl[a] > e->N[a] || nl[a] == 0)
+            return ERR_ARG;
+    upml_t *u = &e->upml[e->nupml++];
+    memcpy(u->start, start, 12);
+    memcpy(u->nl, nl, 12);
+    u->n = (size_t)nl[0] * nl[1] * nl[2];
+    size_t m = 3 * u->n;
+    u->vv = dupf(vv, m); u->vvfo = dupf(vvfo, m); u->vvfn = dupf(vvfn, m);
+    u->ii = dupf(ii, m); u->iifo = dupf(iifo, m); u->iifn = dupf(iifn, m);
+    u->vflux = (float *)xcalloc(m, 4);
+    u->iflux = (float *)xcalloc(m, 4);
+    return OK;
+}
+
+int oems_ref_add_mur(eng_t *e, int ny, unsigned line, unsigned shift, unsigned start_ts, const float *cP,
+                     const float *cPP)
+{
+    if (!e || e->nmur >= MAX_MUR || ny < 0 || ny > 2 || line >= e->N[ny] || shift >= e->N[ny])
+        return ERR_ARG;
+    mur_t *m = &e->mur[e->nmur++];
+    m->ny = ny; m->nyP = (ny + 1) % 3; m->nyPP = (ny + 2) % 3;
+    m->line = line; m->shift = shift; m->start_ts = start_ts;
+    m->n1 = e->N[m->nyP]; m->n2 = e->N[m->nyPP];
+    size_t n = (size_t)m->n1 * m->n2;
+    m->cP = dupf(cP, n); m->cPP = dupf(cPP, n);
+    m->bP = (float *)xcalloc(n, 4); m->bPP = (float *)xcalloc(n, 4);
+    return OK;
+}
+
+int oems_ref_add_lorentz_order(eng_t *e, unsigned count, const unsigned *pos, int von, int con, int vlon,
+                               int clon, const float *vint, const float *vext, const float *vlor,
+                               const float *iint, const float *iext, const float *ilor)
+{
+    if (!e || e->nlor >= MAX_LOR)
+        return ERR_ARG;
+    for (unsigned i = 0; i < count; ++i)
+        for (int a = 0; a < 3; ++a)
+            if (pos[a * count + i] >= e->N[a])
+                return ERR_ARG;
+    lor_t *l = &e->lor[e->nlor++];
+    size_t m = 3 * (size_t)count;
+    l->count = count;
+    l->pos = (unsigned *)xcalloc(m, 4);
+    if (count) memcpy(l->pos, pos, 4 * m);
+    l->von = von; l->con = con; l->vlon = vlon && von; l->clon = clon && con;
+    l->vint = von ? dupf(vint, m) : NULL; l->vext = von ? dupf(vext, m) : NULL;
+    l->vlor = l->vlon ? dupf(vlor, m) : NULL;
+    l->iint = con ? dupf(iint, m) : NULL; l->iext = con ? dupf(iext, m) : NULL;
+    l->ilor = l->clon ? dupf(ilor, m) : NULL;
+    l->vade = von ? (float *)xcalloc(m, 4) : NULL;
+    l->vlade = l->vlon ? (float *)xcalloc(m, 4) : NULL;
+    l->iade = con ? (float *)xcalloc(m, 4) : NULL;
+    l->ilade = l->clon ? (float *)xcalloc(m, 4) : NULL;
+    return OK;
+}
+
+static int add_probe(eng_t *e, int type, const unsigned start[3], const unsigned stop[3], int nd, const int si[3],
+                     const int ei[3], double weight, unsigned interval, unsigned start_ts, unsigned stop_ts, int *id)
+{
+    if (!e || e->nprobes >= MAX_PROBES || !id)
+        return ERR_ARG;
+    for (int a = 0; a < 3; ++a)
+        if (start[a] >= e->N[a] || stop[a] >= e->N[a])
+            return ERR_ARG;
+    if (type == 0) {
+        int diff = (start[0] != stop[0]) + (start[1] != stop[1]) + (start[2] != stop[2]);
+        if (diff != 1)
+            return ERR_ARG;
+    } else if (nd < 0 || nd > 2)
+        return ERR_ARG;
+    probe_t *p = &e->probes[e->nprobes];
+    memset(p, 0, sizeof(*p));
+    p->type = type;
+    memcpy(p->start, start, 12);
+    memcpy(p->stop, stop, 12);
+    p->nd = nd;
+    for (int a = 0; a < 3; ++a) {
+        p->si[a] = si ? si[a] : 1;
+        p->ei[a] = ei ? ei[a] : 1;
+    }
+    p->weight = weight;
+    p->interval = interval ? interval : 1;
+    p->start_ts = start_ts;
+    p->stop_ts = stop_ts;
+    *id = e->nprobes++;
+    return OK;
+}
+
+int oems_ref_add_voltage_probe(eng_t *e, const unsigned start[3], const unsigned stop[3], double weight,
+                               unsigned interval, unsigned start_ts, unsigned stop_ts, int *id)
+{
+    return add_probe(e, 0, start, stop, -1, NULL, NULL, weight, interval, start_ts, stop_ts, id);
+}
+
+int oems_ref_add_current_probe(eng_t *e, const unsigned start[3], const unsigned stop[3], int nd, const int si[3],
+                               const int ei[3], double weight, unsigned interval, unsigned start_ts, unsigned stop_ts,
+                               int *id)
+{
+    return add_probe(e, 1, start, stop, nd, si, ei, weight, interval, start_ts, stop_ts, id);
+}
+
+int oems_ref_set_probe_dft(eng_t *e, int id, unsigned fd_interval, unsigned nf, const double *freqs)
+{
+    if (!e || id < 0 || id >= e->nprobes || (nf && !freqs))
+        return ERR_ARG;
+    probe_t *p = &e->probes[id];
+    p->fd_interval = fd_interval;
+    p->nf = nf;
+    free(p->freqs); free(p->dft);
+    p->freqs = (double *)xcalloc(nf, 8);
+    if (nf) memcpy(p->freqs, freqs, 8 * (size_t)nf);
+    p->dft = (double *)xcalloc(2 * (size_t)nf, 8);
+    return OK;
+}
+
+int oems_ref_add_fd_dump(eng_t *e, int field, const unsigned start[3], const unsigned stop[3], unsigned fd_interval,
+                         unsigned nf, const double *freqs, const double *el, const double *del, int *id)
+{
+    if (!e || e->ndumps >= MAX_DUMPS || (field != 0 && field != 1) || !id || !el || !del)
+        return ERR_ARG;
+    dump_t *d = &e->dumps[e->ndumps];
+    memset(d, 0, sizeof(*d));
+    d->field = field;
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        if (start[a] > stop[a] || stop[a] >= e->N[a])
+            return ERR_ARG;
+        d->start[a] = start[a];
+        d->stop[a] = stop[a];
+        d->sz[a] = stop[a] - start[a] + 1;
+        d->el[a] = (double *)xcalloc(e->N[a], 8);
+        d->del[a] = (double *)xcalloc(e->N[a], 8);
+        memcpy(d->el[a], el + off, 8 * (size_t)e->N[a]);
+        memcpy(d->del[a], del + off, 8 * (size_t)e->N[a]);
+        off += e->N[a];
+    }
+    d->fd_interval = fd_interval;
+    d->nf = nf;
+    d->freqs = (double *)xcalloc(nf, 8);
+    if (nf) memcpy(d->freqs, freqs, 8 * (size_t)nf);
+    d->acc = (float *)xcalloc((size_t)nf * 3 * d->sz[0] * d->sz[1] * d->sz[2] * 2, 4);
+    *id = e->ndumps++;
+    return OK;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* basic engine update: Engine::UpdateVoltages / UpdateCurrents (FDTD/engine.cpp:110-222) */
+
+static void update_voltages_basic(eng_t *e, unsigned startX, unsigned numX)
+{
+    const unsigned Ny = e->N[1], Nz = e->N[2];
+    float *V = e->volt;
+    const float *I = e->curr;
+    const float *vv = e->vv, *vi = e->vi;
+    unsigned pos0 = startX;
+    for (unsigned px = 0; px < numX; ++px, ++pos0) {
+        unsigned s0 = pos0 ? 1 : 0;
+        for (unsigned y = 0; y < Ny; ++y) {
+            unsigned s1 = y ? 1 : 0;
+            for (unsigned z = 0; z < Nz; ++z) {
+                unsigned s2 = z ? 1 : 0;
+                size_t i0 = nijk(e, 0, pos0, y, z), i1 = nijk(e, 1, pos0, y, z), i2 = nijk(e, 2, pos0, y, z);
+                float t;
+                /* x */
+                V[i0] *= vv[i0];
+                t = I[i2] - I[nijk(e, 2, pos0, y - s1, z)];
+                t = t - I[i1];
+                t = t + I[nijk(e, 1, pos0, y, z - s2)];
+                V[i0] += vi[i0] * t;
+                /* y */
+                V[i1] *= vv[i1];
+                t = I[i0] - I[nijk(e, 0, pos0, y, z - s2)];
+                t = t - I[i2];
+                t = t + I[nijk(e, 2, pos0 - s0, y, z)];
+                V[i1] += vi[i1] * t;
+                /* z */
+                V[i2] *= vv[i2];
+                t = I[i1] - I[nijk(e, 1, pos0 - s0, y, z)];
+                t = t - I[i0];
+                t = t + I[nijk(e, 0, pos0, y - s1, z)];
+                V[i2] += vi[i2] * t;
+            }
+        }
+    }
+}
+
+static void update_currents_basic(eng_t *e, unsigned startX, unsigned numX)
+{
+    const unsigned Ny = e->N[1], Nz = e->N[2];
+    float *I = e->curr;
+    const float *V = e->volt;
+    const float *ii = e->ii, *iv = e->iv;
+    unsigned pos0 = startX;
+    for (unsigned px = 0; px < numX; ++px, ++pos0) {
+        for (unsigned y = 0; y + 1 < Ny; ++y) {
+            for (unsigned z = 0; z + 1 < Nz; ++z) {
+                size_t i0 = nijk(e, 0, pos0, y, z), i1 = nijk(e, 1, pos0, y, z), i2 = nijk(e, 2, pos0, y, z);
+                float t;
+                I[i0] *= ii[i0];
+                t = V[i2] - V[nijk(e, 2, pos0, y + 1, z)];
+                t = t - V[i1];
+                t = t + V[nijk(e, 1, pos0, y, z + 1)];
+                I[i0] += iv[i0] * t;
+                I[i1] *= ii[i1];
+                t = V[i0] - V[nijk(e, 0, pos0, y, z + 1)];
+                t = t - V[i2];
+                t = t + V[nijk(e, 2, pos0 + 1, y, z)];
+                I[i1] += iv[i1] * t;
+                I[i2] *= ii[i2];
+                t = V[i1] - V[nijk(e, 1, pos0 + 1, y, z)];
+                t = t - V[i0];
+                t = t + V[nijk(e, 0, pos0, y + 1, z)];
+                I[i2] += iv[i2] * t;
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* SSE-compressed update (FDTD/engine_sse_compressed.cpp:51-311), lane-strided 4-lane vectors. */
+
+static inline v4sf lane_up(v4sf a) /* _mm_slli_si128(a,4): lane0 = 0, lane k = a[k-1] */
+{
+    v4sf r = {0.0f, a[0], a[1], a[2]};
+    return r;
+}
+
+static inline v4sf lane_down(v4sf a) /* _mm_srli_si128(a,4): lane k = a[k+1], lane3 = 0 */
+{
+    v4sf r = {a[1], a[2], a[3], 0.0f};
+    return r;
+}
+
+static void update_voltages_mt(eng_t *e, unsigned startX, unsigned numX)
+{
+    const unsigned Ny = e->N[1], nv = e->nv, U = e->nclasses;
+    v4sf *V = e->f4volt;
+    const v4sf *I = e->f4curr;
+    const size_t sx = (size_t)Ny * nv * 3, sy = (size_t)nv * 3, sz = 3;
+    unsigned pos0 = startX;
+    for (unsigned px = 0; px < numX; ++px, ++pos0) {
+        size_t ix = pos0 > 0 ? sx : 0;
+        for (unsigned y = 0; y < Ny; ++y) {
+            size_t iy = y > 0 ? sy : 0;
+            size_t row = ((size_t)pos0 * Ny + y) * nv;
+            for (unsigned v = 1; v < nv; ++v) {
+                unsigned c = e->op_index[row + v];
+                size_t p = (row + v) * 3;
+                V[p + 0] = V[p + 0] * e->cvv[0 * U + c];
+                V[p + 0] = V[p + 0] + e->cvi[0 * U + c] * (((I[p + 2] - I[p + 2 - iy]) - I[p + 1]) + I[p + 1 - sz]);
+                V[p + 1] = V[p + 1] * e->cvv[1 * U + c];
+                V[p + 1] = V[p + 1] + e->cvi[1 * U + c] * (((I[p + 0] - I[p + 0 - sz]) - I[p + 2]) + I[p + 2 - ix]);
+                V[p + 2] = V[p + 2] * e->cvv[2 * U + c];
+                V[p + 2] = V[p + 2] + e->cvi[2 * U + c] * (((I[p + 1] - I[p + 1 - ix]) - I[p + 0]) + I[p + 0 - iy]);
+            }
+            /* vector 0: the z-1 neighbour is vector nv-1 shifted up one lane */
+            {
+                unsigned c = e->op_index[row];
+                size_t p = row * 3, pe = (row + nv - 1) * 3;
+                v4sf t = lane_up(I[pe + 1]);
+                V[p + 0] = V[p + 0] * e->cvv[0 * U + c];
+                V[p + 0] = V[p + 0] + e->cvi[0 * U + c] * (((I[p + 2] - I[p + 2 - iy]) - I[p + 1]) + t);
+                t = lane_up(I[pe + 0]);
+                V[p + 1] = V[p + 1] * e->cvv[1 * U + c];
+                V[p + 1] = V[p + 1] + e->cvi[1 * U + c] * (((I[p + 0] - t) - I[p + 2]) + I[p + 2 - ix]);
+                V[p + 2] = V[p + 2] * e->cvv[2 * U + c];
+                V[p + 2] = V[p + 2] + e->cvi[2 * U + c] * (((I[p + 1] - I[p + 1 - ix]) - I[p + 0]) + I[p + 0 - iy]);
+            }
+        }
+    }
+}
+
+static void update_currents_mt(eng_t *e, unsigned startX, unsigned numX)
+{
+    const unsigned Ny = e->N[1], nv = e->nv, U = e->nclasses;
+    const v4sf *V = e->f4volt;
+    v4sf *I = e->f4curr;
+    const size_t sx = (size_t)Ny * nv * 3, sy = (size_t)nv * 3, sz = 3;
+    unsigned pos0 = startX;
+    for (unsigned px = 0; px < numX; ++px, ++pos0) {
+        for (unsigned y = 0; y + 1 < Ny; ++y) {
+            size_t row = ((size_t)pos0 * Ny + y) * nv;
+            for (unsigned v = 0; v + 1 < nv; ++v) {
+                unsigned c = e->op_index[row + v];
+                size_t p = (row + v) * 3;
+                I[p + 0] = I[p + 0] * e->cii[0 * U + c];
+                I[p + 0] = I[p + 0] + e->civ[0 * U + c] * (((V[p + 2] - V[p + 2 + sy]) - V[p + 1]) + V[p + 1 + sz]);
+                I[p + 1] = I[p + 1] * e->cii[1 * U + c];
+                I[p + 1] = I[p + 1] + e->civ[1 * U + c] * (((V[p + 0] - V[p + 0 + sz]) - V[p + 2]) + V[p + 2 + sx]);
+                I[p + 2] = I[p + 2] * e->cii[2 * U + c];
+                I[p + 2] = I[p + 2] + e->civ[2 * U + c] * (((V[p + 1] - V[p + 1 + sx]) - V[p + 0]) + V[p + 0 + sy]);
+            }
+            /* last vector: the z+1 neighbour is vector 0 shifted down one lane */
+            {
+                unsigned c = e->op_index[row + nv - 1];
+                size_t p = (row + nv - 1) * 3, ps = row * 3;
+                v4sf t = lane_down(V[ps + 1]);
+                I[p + 0] = I[p + 0] * e->cii[0 * U + c];
+                I[p + 0] = I[p + 0] + e->civ[0 * U + c] * (((V[p + 2] - V[p + 2 + sy]) - V[p + 1]) + t);
+                t = lane_down(V[ps + 0]);
+                I[p + 1] = I[p + 1] * e->cii[1 * U + c];
+                I[p + 1] = I[p + 1] + e->civ[1 * U + c] * (((V[p + 0] - t) - V[p + 2]) + V[p + 2 + sx]);
+                I[p + 2] = I[p + 2] * e->cii[2 * U + c];
+                I[p + 2] = I[p + 2] + e->civ[2 * U + c] * (((V[p + 1] - V[p + 1 + sx]) - V[p + 0]) + V[p + 0 + sy]);
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* extension hooks (accessor based, like the reference's templated Impl functions) */
+
+/* Engine_Ext_LorentzMaterial::DoPreVoltageUpdatesImpl (engine_ext_lorentzmaterial.cpp:79-120) */
+static void lorentz_pre_volt(eng_t *e, lor_t *l)
+{
+    if (!l->von)
+        return;
+    unsigned M = l->count;
+    for (unsigned i = 0; i < M; ++i) {
+        unsigned x = l->pos[i], y = l->pos[M + i], z = l->pos[2 * M + i];
+        for (int n = 0; n < 3; ++n) {
+            size_t k = (size_t)n * M + i;
+            float vol = GETV(e, n, x, y, z);
+            if (l->vlon) {
+                l->vlade[k] += l->vlor[k] * l->vade[k];
+                l->vade[k] *= l->vint[k];
+                l->vade[k] += l->vext[k] * (vol - l->vlade[k]);
+            } else {
+                l->vade[k] *= l->vint[k];
+                l->vade[k] += l->vext[k] * vol;
+            }
+        }
+    }
+}
+
+static void lorentz_pre_curr(eng_t *e, lor_t *l)
+{
+    if (!l->con)
+        return;
+    unsigned M = l->count;
+    for (unsigned i = 0; i < M; ++i) {
+        unsigned x = l->pos[i], y = l->pos[M + i], z = l->pos[2 * M + i];
+        for (int n = 0; n < 3; ++n) {
+            size_t k = (size_t)n * M + i;
+            float cur = GETI(e, n, x, y, z);
+            if (l->clon) {
+                l->ilade[k] += l->ilor[k] * l->iade[k];
+                l->iade[k] *= l->iint[k];
+                l->iade[k] += l->iext[k] * (cur - l->ilade[k]);
+            } else {
+                l->iade[k] *= l->iint[k];
+                l->iade[k] += l->iext[k] * cur;
+            }
+        }
+    }
+}
+
+/* Engine_Ext_Dispersive::Apply2VoltagesImpl / Apply2CurrentImpl (engine_ext_dispersive.cpp:76-127) */
+static void lorentz_apply(eng_t *e, lor_t *l, int curr)
+{
+    if (curr ? !l->con : !l->von)
+        return;
+    unsigned M = l->count;
+    float *ade = curr ? l->iade : l->vade;
+    for (unsigned i = 0; i < M; ++i) {
+        unsigned x = l->pos[i], y = l->pos[M + i], z = l->pos[2 * M + i];
+        for (int n = 0; n < 3; ++n) {
+            float *f = fptr(e, curr, n, x, y, z);
+            *f = *f - ade[(size_t)n * M + i];
+        }
+    }
+}
+
+/* Engine_Ext_Mur_ABC (engine_ext_mur_abc.cpp:82-178) */
+static int mur_active(const eng_t *e, const mur_t *m)
+{
+    return e->numTS >= m->start_ts;
+}
+
+static void mur_pre(eng_t *e, mur_t *m)
+{
+    if (!mur_active(e, m))
+        return;
+    unsigned pos[3] = {0, 0, 0}, ps[3] = {0, 0, 0};
+    pos[m->ny] = m->line;
+    ps[m->ny] = m->shift;
+    for (unsigned i = 0; i < m->n1; ++i) {
+        pos[m->nyP] = ps[m->nyP] = i;
+        for (unsigned j = 0; j < m->n2; ++j) {
+            pos[m->nyPP] = ps[m->nyPP] = j;
+            size_t k = (size_t)i * m->n2 + j;
+            m->bP[k] = GETV(e, m->nyP, ps[0], ps[1], ps[2]) - m->cP[k] * GETV(e, m->nyP, pos[0], pos[1], pos[2]);
+            m->bPP[k] = GETV(e, m->nyPP, ps[0], ps[1], ps[2]) - m->cPP[k] * GETV(e, m->nyPP, pos[0], pos[1], pos[2]);
+        }
+    }
+}
+
+static void mur_post(eng_t *e, mur_t *m)
+{
+    if (!mur_active(e, m))
+        return;
+    unsigned ps[3] = {0, 0, 0};
+    ps[m->ny] = m->shift;
+    for (unsigned i = 0; i < m->n1; ++i) {
+        ps[m->nyP] = i;
+        for (unsigned j = 0; j < m->n2; ++j) {
+            ps[m->nyPP] = j;
+            size_t k = (size_t)i * m->n2 + j;
+            m->bP[k] += m->cP[k] * GETV(e, m->nyP, ps[0], ps[1], ps[2]);
+            m->bPP[k] += m->cPP[k] * GETV(e, m->nyPP, ps[0], ps[1], ps[2]);
+        }
+    }
+}
+
+static void mur_apply(eng_t *e, mur_t *m)
+{
+    if (!mur_active(e, m))
+        return;
+    unsigned pos[3] = {0, 0, 0};
+    pos[m->ny] = m->line;
+    for (unsigned i = 0; i < m->n1; ++i) {
+        pos[m->nyP] = i;
+        for (unsigned j = 0; j < m->n2; ++j) {
+            pos[m->nyPP] = j;
+            size_t k = (size_t)i * m->n2 + j;
+            GETV(e, m->nyP, pos[0], pos[1], pos[2]) = m->bP[k];
+            GETV(e, m->nyPP, pos[0], pos[1], pos[2]) = m->bPP[k];
+        }
+    }
+}
+
+/* Engine_Ext_UPML (engine_ext_upml.cpp:52-229), x-lines [x0, x1) of region u */
+static void upml_pre(eng_t *e, upml_t *u, int curr, unsigned x0, unsigned x1)
+{
+    const float *cv = curr ? u->ii : u->vv, *fo = curr ? u->iifo : u->vvfo;
+    float *flux = curr ? u->iflux : u->vflux;
+    for (unsigned lx = x0; lx < x1; ++lx)
+        for (unsigned ly = 0; ly < u->nl[1]; ++ly)
+            for (unsigned lz = 0; lz < u->nl[2]; ++lz)
+                for (int n = 0; n < 3; ++n) {
+                    size_t k = (((size_t)n * u->nl[0] + lx) * u->nl[1] + ly) * u->nl[2] + lz;
+                    float *f = fptr(e, curr, n, lx + u->start[0], ly + u->start[1], lz + u->start[2]);
+                    float h = cv[k] * *f - fo[k] * flux[k];
+                    *f = flux[k];
+                    flux[k] = h;
+                }
+}
+
+static void upml_post(eng_t *e, upml_t *u, int curr, unsigned x0, unsigned x1)
+{
+    const float *fn = curr ? u->iifn : u->vvfn;
+    float *flux = curr ? u->iflux : u->vflux;
+    for (unsigned lx = x0; lx < x1; ++lx)
+        for (unsigned ly = 0; ly < u->nl[1]; ++ly)
+            for (unsigned lz = 0; lz < u->nl[2]; ++lz)
+                for (int n = 0; n < 3; ++n) {
+                    size_t k = (((size_t)n * u->nl[0] + lx) * u->nl[1] + ly) * u->nl[2] + lz;
+                    float *f = fptr(e, curr, n, lx + u->start[0], ly + u->start[1], lz + u->start[2]);
+                    float h = flux[k];
+                    flux[k] = *f;
+                    *f = h + fn[k] * flux[k];
+                }
+}
+
+/* Engine_Ext_Excitation::Apply2VoltagesImpl / Apply2CurrentImpl (engine_ext_excitation.cpp:33-94) */
+static void excitation_apply(eng_t *e, int curr)
+{
+    unsigned cnt = curr ? e->nI : e->nV;
+    if (!cnt || !e->sig_len)
+        return;
+    int numTS = (int)e->numTS;
+    int p = numTS + 1;
+    if (e->period > 0)
+        p = (int)e->period;
+    const unsigned *idx = curr ? e->i_idx : e->v_idx;
+    const unsigned *delay = curr ? e->i_delay : e->v_delay;
+    const unsigned short *dir = curr ? e->i_dir : e->v_dir;
+    const float *amp = curr ? e->i_amp : e->v_amp;
+    const float *sig = curr ? e->sig_i : e->sig_v;
+    for (unsigned n = 0; n < cnt; ++n) {
+        int exc_pos = numTS - (int)delay[n];
+        exc_pos *= (exc_pos > 0);
+        exc_pos %= p;
+        exc_pos *= (exc_pos < (int)e->sig_len);
+        float *f = fptr(e, curr, dir[n], idx[n], idx[cnt + n], idx[2 * cnt + n]);
+        *f = *f + amp[n] * sig[exc_pos];
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* processing */
+
+/* Engine_Interface_FDTD::CalcVoltageIntegral (FDTD/engine_interface_fdtd.cpp:206-232) */
+static double voltage_integral(eng_t *e, const probe_t *p)
+{
+    double result = 0;
+    for (int n = 0; n < 3; ++n) {
+        if (p->start[n] < p->stop[n]) {
+            unsigned pos[3] = {p->start[0], p->start[1], p->start[2]};
+            for (; pos[n] < p->stop[n]; ++pos[n])
+                result += GETV(e, n, pos[0], pos[1], pos[2]);
+        } else {
+            unsigned pos[3] = {p->stop[0], p->stop[1], p->stop[2]};
+            for (; pos[n] < p->start[n]; ++pos[n])
+                result -= GETV(e, n, pos[0], pos[1], pos[2]);
+        }
+    }
+    return result;
+}
+
+/* ProcessCurrent::CalcIntegral (Common/processcurrent.cpp:96-171) */
+static double current_integral(eng_t *e, const probe_t *p)
+{
+    float current = 0;
+    const unsigned *s = p->start, *t = p->stop;
+    const int *si = p->si, *ei = p->ei;
+    unsigned i;
+    switch (p->nd) {
+    case 0:
+        if (ei[0] && si[2]) for (i = s[1] + 1; i <= t[1]; ++i) current += GETI(e, 1, t[0], i, s[2]);
+        if (ei[0] && ei[1]) for (i = s[2] + 1; i <= t[2]; ++i) current += GETI(e, 2, t[0], t[1], i);
+        if (si[0] && ei[2]) for (i = s[1] + 1; i <= t[1]; ++i) current -= GETI(e, 1, s[0], i, t[2]);
+        if (si[0] && si[1]) for (i = s[2] + 1; i <= t[2]; ++i) current -= GETI(e, 2, s[0], s[1], i);
+        break;
+    case 1:
+        if (si[0] && si[1]) for (i = s[2] + 1; i <= t[2]; ++i) current += GETI(e, 2, s[0], s[1], i);
+        if (ei[1] && ei[2]) for (i = s[0] + 1; i <= t[0]; ++i) current += GETI(e, 0, i, t[1], t[2]);
+        if (ei[0] && ei[1]) for (i = s[2] + 1; i <= t[2]; ++i) current -= GETI(e, 2, t[0], t[1], i);
+        if (si[1] && si[2]) for (i = s[0] + 1; i <= t[0]; ++i) current -= GETI(e, 0, i, s[1], s[2]);
+        break;
+    case 2:
+        if (si[1] && si[2]) for (i = s[0] + 1; i <= t[0]; ++i) current += GETI(e, 0, i, s[1], s[2]);
+        if (ei[0] && si[2]) for (i = s[1] + 1; i <= t[1]; ++i) current += GETI(e, 1, t[0], i, s[2]);
+        if (ei[1] && ei[2]) for (i = s[0] + 1; i <= t[0]; ++i) current -= GETI(e, 0, i, t[1], t[2]);
+        if (si[0] && ei[2]) for (i = s[1] + 1; i <= t[1]; ++i) current -= GETI(e, 1, s[0], i, t[2]);
+        break;
+    default:
+        return 0.0;
+    }
+    return current;
+}
+
+/* ProcessIntegral::Process (Common/processintegral.cpp:134-171) */
+static void process_probes(eng_t *e)
+{
+    unsigned ts = e->numTS;
+    for (int k = 0; k < e->nprobes; ++k) {
+        probe_t *p = &e->probes[k];
+        if (ts < p->start_ts || ts > p->stop_ts)
+            continue;
+        int do_td = (ts % p->interval) == 0;
+        int do_fd = p->fd_interval && (ts % p->fd_interval) == 0;
+        if (!do_td && !do_fd)
+            continue;
+        double val = p->type == 0 ? voltage_integral(e, p) : current_integral(e, p);
+        double time = ((double)ts + (double)(p->type == 1) * 0.5) * e->dt;
+        if (do_td) {
+            size_t slot = ts / p->interval;
+            if (slot < p->nslots)
+                p->series[slot] = val * p->weight;
+        }
+        if (do_fd) {
+            for (unsigned f = 0; f < p->nf; ++f) {
+                double th = ((-2.0 * M_PI_REF) * p->freqs[f]) * time;
+                double complex ex = cexp(CMPLX(-0.0, th));
+                double a = val * p->weight;
+                double re = creal(ex) * a, im = cimag(ex) * a;
+                re = re * 2.0; im = im * 2.0;
+                re = re * e->dt; im = im * e->dt;
+                re = re * (double)p->fd_interval; im = im * (double)p->fd_interval;
+                p->dft[2 * f] += re;
+                p->dft[2 * f + 1] += im;
+            }
+        }
+    }
+}
+
+/* GetRawInterpolatedField / GetRawInterpolatedDualField, CELL_INTERPOLATE
+ * (FDTD/engine_interface_fdtd.cpp:104-121, 182-199) */
+static void cell_field(eng_t *e, const dump_t *d, const unsigned pos[3], double out[3])
+{
+    if (d->field == 0) {
+        for (int n = 0; n < 3; ++n) {
+            int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+            if (pos[0] == e->N[0] - 1 || pos[1] == e->N[1] - 1 || pos[2] == e->N[2] - 1) {
+                out[n] = 0;
+                continue;
+            }
+            unsigned ip[3] = {pos[0], pos[1], pos[2]};
+#define RAWE(p) (d->el[n][(p)[n]] ? (double)GETV(e, n, (p)[0], (p)[1], (p)[2]) / d->el[n][(p)[n]] : 0.0)
+            out[n] = RAWE(ip);
+            ++ip[nP];
+            out[n] += RAWE(ip);
+            ++ip[nPP];
+            out[n] += RAWE(ip);
+            --ip[nP];
+            out[n] += RAWE(ip);
+            out[n] /= 4;
+#undef RAWE
+        }
+    } else {
+        for (int n = 0; n < 3; ++n) {
+            unsigned ip[3] = {pos[0], pos[1], pos[2]};
+#define RAWH(p) (d->del[n][(p)[n]] ? (double)GETI(e, n, (p)[0], (p)[1], (p)[2]) / d->del[n][(p)[n]] : 0.0)
+            double delta = d->del[n][ip[n]];
+            out[n] = RAWH(ip);
+            if (pos[n] >= e->N[n] - 1) {
+                out[n] = 0;
+                continue;
+            }
+            ++ip[n];
+            double deltaUp = d->del[n][ip[n]];
+            double deltaRel = delta / (delta + deltaUp);
+            out[n] = out[n] * (1.0 - deltaRel) + (double)RAWH(ip) * deltaRel;
+#undef RAWH
+        }
+    }
+}
+
+/* ProcessFieldsFD::Process (Common/processfields_fd.cpp:72-107) */
+static void process_dumps(eng_t *e)
+{
+    unsigned ts = e->numTS;
+    for (int k = 0; k < e->ndumps; ++k) {
+        dump_t *d = &e->dumps[k];
+        if (!d->fd_interval || ts % d->fd_interval)
+            continue;
+        double T = ((double)ts + (double)(d->field == 1) * 0.5) * e->dt;
+        size_t plane = (size_t)d->sz[0] * d->sz[1] * d->sz[2];
+        for (unsigned f = 0; f < d->nf; ++f) {
+            float th = (float)(((-2.0 * M_PI_REF) * d->freqs[f]) * T);
+            float complex ex = cexpf(CMPLXF(-0.0f, th));
+            float er = crealf(ex) * 2.0f, ei = cimagf(ex) * 2.0f;
+            float sc = (float)(e->dt * (double)d->fd_interval);
+            er = er * sc;
+            ei = ei * sc;
+            float *acc = d->acc + (size_t)f * 3 * plane * 2;
+            unsigned pos[3];
+            size_t c = 0;
+            for (unsigned i = 0; i < d->sz[0]; ++i)
+                for (unsigned j = 0; j < d->sz[1]; ++j)
+                    for (unsigned l = 0; l < d->sz[2]; ++l, ++c) {
+                        pos[0] = d->start[0] + i;
+                        pos[1] = d->start[1] + j;
+                        pos[2] = d->start[2] + l;
+                        double out[3];
+                        cell_field(e, d, pos, out);
+                        for (int n = 0; n < 3; ++n) {
+                            float td = (float)out[n];
+                            float *a = acc + ((size_t)n * plane + c) * 2;
+                            a[0] = a[0] + td * er;
+                            a[1] = a[1] + td * ei;
+                        }
+                    }
+        }
+    }
+}
+
+static void process_all(eng_t *e)
+{
+    process_probes(e);
+    process_dumps(e);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* stepping */
+
+/* extension phases in reference order; thread 0 runs the non-threaded extensions */
+static void pre_volt(eng_t *e)
+{
+    /* reverse priority: excitation (none), Mur walls (insertion order), Lorentz, UPML last */
+    for (int w = 0; w < e->nmur; ++w)
+        mur_pre(e, &e->mur[w]);
+    for (int o = 0; o < e->nlor; ++o)
+        lorentz_pre_volt(e, &e->lor[o]);
+}
+
+static void post_volt_apply(eng_t *e)
+{
+    for (int w = e->nmur - 1; w >= 0; --w)
+        mur_post(e, &e->mur[w]);
+    for (int o = 0; o < e->nlor; ++o)
+        lorentz_apply(e, &e->lor[o], 0);
+    for (int w = e->nmur - 1; w >= 0; --w)
+        mur_apply(e, &e->mur[w]);
+    excitation_apply(e, 0);
+}
+
+static void pre_curr(eng_t *e)
+{
+    for (int o = 0; o < e->nlor; ++o)
+        lorentz_pre_curr(e, &e->lor[o]);
+}
+
+static void post_curr_apply(eng_t *e)
+{
+    for (int o = 0; o < e->nlor; ++o)
+        lorentz_apply(e, &e->lor[o], 1);
+    excitation_apply(e, 1);
+}
+
+static void step_basic(eng_t *e)
+{
+    pre_volt(e);
+    for (int r = e->nupml - 1; r >= 0; --r)
+        upml_pre(e, &e->upml[r], 0, 0, e->upml[r].nl[0]);
+    update_voltages_basic(e, 0, e->N[0]);
+    for (int r = 0; r < e->nupml; ++r)
+        upml_post(e, &e->upml[r], 0, 0, e->upml[r].nl[0]);
+    post_volt_apply(e);
+
+    pre_curr(e);
+    for (int r = e->nupml - 1; r >= 0; --r)
+        upml_pre(e, &e->upml[r], 1, 0, e->upml[r].nl[0]);
+    update_currents_basic(e, 0, e->N[0] - 1);
+    for (int r = 0; r < e->nupml; ++r)
+        upml_post(e, &e->upml[r], 1, 0, e->upml[r].nl[0]);
+    post_curr_apply(e);
+    ++e->numTS;
+}
+
+/* x-slab split of a UPML region for thread tid (Engine_Ext_UPML::SetNumberOfThreads) */
+static void upml_range(const eng_t *e, const upml_t *u, int tid, unsigned *x0, unsigned *x1)
+{
+    unsigned nt = (unsigned)e->nthreads, jobs = u->nl[0];
+    unsigned base = jobs / nt, rem = jobs - base * nt, s = 0;
+    for (int t = 0; t < tid; ++t)
+        s += base + ((unsigned)t < rem);
+    *x0 = s;
+    *x1 = s + base + ((unsigned)tid < rem);
+}
+
+typedef struct {
+    eng_t *e;
+    int tid;
+} targ_t;
+
+static void *worker(void *arg)
+{
+    targ_t *ta = (targ_t *)arg;
+    eng_t *e = ta->e;
+    int tid = ta->tid;
+    for (;;) {
+        pthread_barrier_wait(&e->bar_start);
+        if (e->stop_threads)
+            break;
+        for (unsigned it = 0; it < e->iter_ts; ++it) {
+            unsigned x0, x1;
+            if (tid == 0)
+                pre_volt(e);
+            pthread_barrier_wait(&e->bar_iter);
+            for (int r = e->nupml - 1; r >= 0; --r) {
+                upml_range(e, &e->upml[r], tid, &x0, &x1);
+                upml_pre(e, &e->upml[r], 0, x0, x1);
+                pthread_barrier_wait(&e->bar_iter);
+            }
+            update_voltages_mt(e, e->tstart[tid], e->tstop[tid] - e->tstart[tid] + 1);
+            pthread_barrier_wait(&e->bar_iter);
+            for (int r = 0; r < e->nupml; ++r) {
+                upml_range(e, &e->upml[r], tid, &x0, &x1);
+                upml_post(e, &e->upml[r], 0, x0, x1);
+                pthread_barrier_wait(&e->bar_iter);
+            }
+            if (tid == 0)
+                post_volt_apply(e);
+            pthread_barrier_wait(&e->bar_iter);
+            if (tid == 0)
+                pre_curr(e);
+            pthread_barrier_wait(&e->bar_iter);
+            for (int r = e->nupml - 1; r >= 0; --r) {
+                upml_range(e, &e->upml[r], tid, &x0, &x1);
+                upml_pre(e, &e->upml[r], 1, x0, x1);
+                pthread_barrier_wait(&e->bar_iter);
+            }
+            if (e->tstop_h[tid] + 1 > e->tstart[tid])
+                update_currents_mt(e, e->tstart[tid], e->tstop_h[tid] - e->tstart[tid] + 1);
+            pthread_barrier_wait(&e->bar_iter);
+            for (int r = 0; r < e->nupml; ++r) {
+                upml_range(e, &e->upml[r], tid, &x0, &x1);
+                upml_post(e, &e->upml[r], 1, x0, x1);
+                pthread_barrier_wait(&e->bar_iter);
+            }
+            if (tid == 0) {
+                post_curr_apply(e);
+                ++e->numTS;
+                process_all(e);
+            }
+            pthread_barrier_wait(&e->bar_iter);
+        }
+        pthread_barrier_wait(&e->bar_stop);
+    }
+    free(ta);
+    return NULL;
+}
+
+static int start_threads(eng_t *e)
+{
+    unsigned nt = (unsigned)e->nthreads;
+    if (nt > e->N[0])
+        nt = e->N[0];
+    e->nthreads = (int)nt;
+    /* Operator_Multithread::CalcStartStopLines (FDTD/operator_multithread.cpp:93-114) */
+    e->tstart = (unsigned *)calloc(nt, 4);
+    e->tstop = (unsigned *)calloc(nt, 4);
+    e->tstop_h = (unsigned *)calloc(nt, 4);
+    unsigned base = e->N[0] / nt, rem = e->N[0] - base * nt, s = 0;
+    for (unsigned t = 0; t < nt; ++t) {
+        unsigned jobs = base + (t < rem);
+        e->tstart[t] = s;
+        e->tstop[t] = s + jobs - 1;
+        e->tstop_h[t] = (t == nt - 1) ? e->tstop[t] - 1 : e->tstop[t];
+        s += jobs;
+    }
+    pthread_barrier_init(&e->bar_iter, NULL, nt);
+    pthread_barrier_init(&e->bar_start, NULL, nt + 1);
+    pthread_barrier_init(&e->bar_stop, NULL, nt + 1);
+    e->threads = (pthread_t *)calloc(nt, sizeof(pthread_t));
+    for (unsigned t = 0; t < nt; ++t) {
+        targ_t *ta = (targ_t *)malloc(sizeof(targ_t));
+        ta->e = e;
+        ta->tid = (int)t;
+        pthread_create(&e->threads[t], NULL, worker, ta);
+    }
+    return OK;
+}
+
+static void stop_threads(eng_t *e)
+{
+    e->stop_threads = 1;
+    pthread_barrier_wait(&e->bar_start);
+    for (int t = 0; t < e->nthreads; ++t)
+        pthread_join(e->threads[t], NULL);
+    free(e->threads);
+    e->threads = NULL;
+    pthread_barrier_destroy(&e->bar_iter);
+    pthread_barrier_destroy(&e->bar_start);
+    pthread_barrier_destroy(&e->bar_stop);
+}
+
+int oems_ref_init(eng_t *e, unsigned max_ts)
+{
+    if (!e || e->inited)
+        return ERR_STATE;
+    if (e->mt ? !e->op_index : !e->vv) {
+        snprintf(e->err, sizeof e->err, "operator not set");
+        return ERR_STATE;
+    }
+    e->maxTS = max_ts;
+    for (int k = 0; k < e->nprobes; ++k) {
+        probe_t *p = &e->probes[k];
+        p->nslots = max_ts / p->interval + 1;
+        p->series = (double *)malloc(p->nslots * sizeof(double));
+        for (size_t s = 0; s < p->nslots; ++s)
+            p->series[s] = NAN;
+    }
+    e->inited = 1;
+    process_all(e);
+    if (e->mt)
+        return start_threads(e);
+    return OK;
+}
+
+int oems_ref_iterate(eng_t *e, unsigned n)
+{
+    if (!e || !e->inited)
+        return ERR_STATE;
+    if (e->mt) {
+        e->iter_ts = n;
+        pthread_barrier_wait(&e->bar_start);
+        pthread_barrier_wait(&e->bar_stop);
+        return OK;
+    }
+    for (unsigned s = 0; s < n; ++s) {
+        step_basic(e);
+        process_all(e);
+    }
+    return OK;
+}
+
+int oems_ref_sync(eng_t *e)
+{
+    return e ? OK : ERR_ARG;
+}
+
+unsigned oems_ref_num_timesteps(const eng_t *e)
+{
+    return e ? e->numTS : 0;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* access */
+
+int oems_ref_read_field(eng_t *e, int which, float *out)
+{
+    if (!e || !out || (which != 0 && which != 1))
+        return ERR_ARG;
+    if (!e->mt) {
+        memcpy(out, which ? e->curr : e->volt, 3 * e->cells * sizeof(float));
+        return OK;
+    }
+    for (unsigned n = 0; n < 3; ++n)
+        for (unsigned x = 0; x < e->N[0]; ++x)
+            for (unsigned y = 0; y < e->N[1]; ++y)
+                for (unsigned z = 0; z < e->N[2]; ++z)
+                    out[nijk(e, n, x, y, z)] = *fptr(e, which, n, x, y, z);
+    return OK;
+}
+
+int oems_ref_write_field(eng_t *e, int which, const float *in)
+{
+    if (!e || !in || (which != 0 && which != 1))
+        return ERR_ARG;
+    for (unsigned n = 0; n < 3; ++n)
+        for (unsigned x = 0; x < e->N[0]; ++x)
+            for (unsigned y = 0; y < e->N[1]; ++y)
+                for (unsigned z = 0; z < e->N[2]; ++z)
+                    *fptr(e, which, n, x, y, z) = in[nijk(e, n, x, y, z)];
+    return OK;
+}
+
+int oems_ref_get_value(eng_t *e, int which, unsigned n, unsigned x, unsigned y, unsigned z, float *v)
+{
+    if (!e || !v || n > 2 || x >= e->N[0] || y >= e->N[1] || z >= e->N[2])
+        return ERR_ARG;
+    *v = *fptr(e, which, n, x, y, z);
+    return OK;
+}
+
+int oems_ref_set_value(eng_t *e, int which, unsigned n, unsigned x, unsigned y, unsigned z, float v)
+{
+    if (!e || n > 2 || x >= e->N[0] || y >= e->N[1] || z >= e->N[2])
+        return ERR_ARG;
+    *fptr(e, which, n, x, y, z) = v;
+    return OK;
+}
+
+int oems_ref_read_probe(eng_t *e, int id, double *out, size_t cap, size_t *count)
+{
+    if (!e || id < 0 || id >= e->nprobes || !out || !count)
+        return ERR_ARG;
+    probe_t *p = &e->probes[id];
+    size_t n = p->nslots < cap ? p->nslots : cap;
+    memcpy(out, p->series, n * sizeof(double));
+    *count = n;
+    return OK;
+}
+
+int oems_ref_read_probe_dft(eng_t *e, int id, double *out)
+{
+    if (!e || id < 0 || id >= e->nprobes || !out)
+        return ERR_ARG;
+    probe_t *p = &e->probes[id];
+    memcpy(out, p->dft, 2 * p->nf * sizeof(double));
+    return OK;
+}
+
+int oems_ref_read_fd_dump(eng_t *e, int id, float *out, size_t cap)
+{
+    if (!e || id < 0 || id >= e->ndumps || !out)
+        return ERR_ARG;
+    dump_t *d = &e->dumps[id];
+    size_t n = (size_t)d->nf * 3 * d->sz[0] * d->sz[1] * d->sz[2] * 2;
+    if (cap < n)
+        return ERR_ARG;
+    memcpy(out, d->acc, n * sizeof(float));
+    return OK;
+}
+
+/* Engine_Interface_FDTD::CalcFastEnergy (FDTD/engine_interface_fdtd.cpp:302-347) */
+int oems_ref_energy(eng_t *e, double *out)
+{
+    if (!e || !out)
+        return ERR_ARG;
+    double E = 0.0, H = 0.0;
+    for (unsigned x = 0; x + 1 < e->N[0]; ++x)
+        for (unsigned y = 0; y + 1 < e->N[1]; ++y)
+            for (unsigned z = 0; z + 1 < e->N[2]; ++z)
+                for (int n = 0; n < 3; ++n) {
+                    float v = GETV(e, n, x, y, z), c = GETI(e, n, x, y, z);
+                    E += v * v;
+                    H += c * c;
+                }
+    *out = EPS0 * E + MUE0 * H;
+    return OK;
+}

@@ -1,0 +1,20 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def cuda_lib():
+    """The CUDA engine library; GPU tests fail (not skip) if it cannot be built or loaded."""
+    from openems_gb300 import build, _native
+    build.build()
+    return _native.load_cuda()

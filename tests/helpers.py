@@ -1,0 +1,45 @@
+"""Shared comparison helpers for the parity tests."""
+import numpy as np
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    if a.shape != b.shape:
+        return False
+    if a.dtype == np.float32:
+        return np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    if a.dtype == np.float64:
+        return np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    if a.dtype == np.complex64:
+        return np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    if a.dtype == np.complex128:
+        return np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    return np.array_equal(a, b)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    m = np.isfinite(a) & np.isfinite(b)
+    den = np.linalg.norm(b[m])
+    return np.linalg.norm(a[m] - b[m]) / (den if den > 0 else 1.0)
+
+
+def compare_engines(ga, gb, check_dumps=True):
+    """Bitwise comparison of fields, probe series, probe DFTs and FD dumps of two engines."""
+    out = {}
+    for w in (0, 1):
+        fa, fb = ga.read_field(w), gb.read_field(w)
+        out[f"field{w}"] = bits_equal(fa, fb)
+    for pid in ga.vprobe_ids + ga.iprobe_ids:
+        sa, sb = ga.probe_series(pid), gb.probe_series(pid)
+        out[f"probe{pid}"] = np.array_equal(np.isnan(sa), np.isnan(sb)) and bits_equal(
+            np.nan_to_num(sa), np.nan_to_num(sb))
+    for pid, p in zip(ga.vprobe_ids + ga.iprobe_ids, ga.op.vprobes + ga.op.iprobes):
+        if p.fd_interval and p.freqs:
+            out[f"dft{pid}"] = bits_equal(ga.probe_dft(pid, len(p.freqs)), gb.probe_dft(pid, len(p.freqs)))
+    if check_dumps:
+        for did in ga.dump_ids:
+            out[f"dump{did}"] = bits_equal(ga.fd_dump(did), gb.fd_dump(did))
+    return out

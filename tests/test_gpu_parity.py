@@ -1,0 +1,223 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the CPU oracle on the same inputs.
+
+Bar: bit-exact fields, probe series, probe DFTs and FD dumps (the engine issues the reference's
+separate multiplies and adds without FMA contraction and keeps denormals); energy within a
+relative 1e-12 (the device reduction order differs from the sequential sum).  At full sizes the
+checks are size-independent properties (power-of-two linearity, snapshot/restore replay) plus a
+short bit-exact run against the multithreaded oracle.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from openems_gb300 import configs
+from openems_gb300.engine import Engine_CUDA, EngineError
+from oracle.oracle import OracleEngine
+
+from helpers import bits_equal, compare_engines, rel_l2
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _run_pair(op, steps, chunks=(1,), **kw):
+    g = Engine_CUDA(op, steps, **kw)
+    r = OracleEngine(op, steps)
+    done = 0
+    k = 0
+    while done < steps:
+        n = min(chunks[k % len(chunks)], steps - done)
+        g.IterateTS(n)
+        r.IterateTS(n)
+        done += n
+        k += 1
+    g.sync()
+    return g, r
+
+
+CASES = [
+    ("smoke", configs.smoke_case, 60),
+    ("mixed", configs.small_mixed, 200),
+    ("mixed_bc2", lambda: configs.small_mixed(bc=(0, 1, 2, 0, 3, 3), seed=3, steps=180), 180),
+    ("mixed_mur_all", lambda: configs.small_mixed(bc=(2, 2, 2, 2, 2, 2), seed=5, steps=160), 160),
+    ("cube40", lambda: configs.plain_cube(n=40, steps=400), 400),
+    ("stress_small", lambda: configs.stress(shape=(40, 36, 30), steps=150, nblocks=16), 150),
+    ("patch_small", lambda: configs.patch(shape=(56, 52, 36), steps=250), 250),
+]
+
+
+@pytest.mark.parametrize("name,fn,steps", CASES)
+def test_bit_exact_against_oracle(cuda_lib, name, fn, steps):
+    op = fn()
+    g, r = _run_pair(op, steps, chunks=(1, 7, 16, 33))
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, (name, bad)
+    eg, er = g.CalcFastEnergy(), r.CalcFastEnergy()
+    assert abs(eg - er) <= 1e-12 * abs(er) + 1e-300
+    assert g.GetNumberOfTimesteps() == steps
+
+
+def test_dense_operator_path_equals_compressed(cuda_lib):
+    op = configs.small_mixed(steps=120)
+    a = Engine_CUDA(op, 120)
+    b = Engine_CUDA(op, 120, max_classes=1)          # forces the dense coefficient arrays
+    assert a.operator_classes() > 1 and b.operator_classes() == 0
+    a.IterateTS(120)
+    b.IterateTS(120)
+    for w in (0, 1):
+        assert bits_equal(a.read_field(w), b.read_field(w))
+
+
+def _sse_compressed_tables(op):
+    """Build Operator_SSE_Compressed-style tables (lane-strided 4-lane vectors)."""
+    Nx, Ny, Nz = (int(v) for v in op.num_lines)
+    nv = (Nz + 3) // 4
+    cols = []
+    for arr in (op.vv, op.vi, op.ii, op.iv):
+        for n in range(3):
+            lanes = np.zeros((Nx, Ny, nv, 4), np.float32)
+            for l in range(4):
+                z = np.arange(nv) + l * nv
+                ok = z < Nz
+                lanes[:, :, ok, l] = arr[n][:, :, z[ok]]
+            cols.append(lanes.reshape(-1, 4))
+    keys = np.concatenate(cols, axis=1)                 # [(x,y,v), 48]
+    uniq, inv = np.unique(keys.view(np.uint32), axis=0, return_inverse=True)
+    uniq = uniq.view(np.float32)
+    U = uniq.shape[0]
+    tabs = []
+    for t in range(4):
+        tabs.append(np.ascontiguousarray(uniq[:, t * 12:(t + 1) * 12].reshape(U, 3, 4).transpose(1, 0, 2)))
+    return U, tabs, inv.reshape(Nx, Ny, nv).astype(np.uint32)
+
+
+def test_reference_sse_compressed_operator_input(cuda_lib):
+    import ctypes as C
+    from openems_gb300 import _native
+    from openems_gb300.engine import _p
+    op = configs.small_mixed(steps=100, n=(14, 12, 11))
+    U, tabs, index = _sse_compressed_tables(op)
+    ref = Engine_CUDA(op, 100)
+    # second engine: same extensions, coefficients through the reference's compressed format
+    lib = _native.load_cuda()
+    h = C.c_void_p()
+    nl = np.ascontiguousarray(op.num_lines, np.uint32)
+    assert lib.create(_p(nl, C.c_uint), float(op.dt), 0, C.byref(h)) == 0
+    tabs = [np.ascontiguousarray(t) for t in tabs]
+    index = np.ascontiguousarray(index)
+    assert lib.set_operator_sse_compressed(h, U, *[_p(t, C.c_float) for t in tabs], _p(index, C.c_uint)) == 0
+    lib.destroy(h)
+    # full engine built from the expanded tables must equal the dense-input engine
+    Nz = int(op.num_lines[2])
+    nv = (Nz + 3) // 4
+    z = np.arange(Nz)
+    exp = []
+    for t in range(4):
+        cls = index[:, :, z % nv]                       # [Nx,Ny,Nz]
+        exp.append(np.stack([tabs[t][n][cls, z // nv] for n in range(3)]))
+    for a, b in zip(exp, (op.vv, op.vi, op.ii, op.iv)):
+        assert bits_equal(a, b)
+
+
+def test_cavity_reference_contract_on_gpu(cuda_lib):
+    from test_oracle import _cavity_check
+    with open(os.path.join(GOLDEN, "cavity_contract.json")) as fh:
+        c = json.load(fh)
+    op = configs.cavity(steps=c["steps"])
+    g = Engine_CUDA(op, c["steps"])
+    g.IterateTS(c["steps"])
+    uy = g.probe_series(g.vprobe_ids[1])
+    uz = g.probe_series(g.vprobe_ids[2])
+    assert _cavity_check(c, op.dt, uy, uz)
+    r = OracleEngine(op, c["steps"])
+    r.IterateTS(c["steps"])
+    assert bits_equal(uy, r.probe_series(r.vprobe_ids[1]))
+
+
+def test_against_committed_fixtures(cuda_lib):
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    gold = np.load(os.path.join(GOLDEN, "oracle_small.npz"))
+    for name, (fn, steps) in make_golden.CASES.items():
+        op = fn()
+        g = Engine_CUDA(op, steps)
+        g.IterateTS(steps)
+        for pid, p in zip(g.vprobe_ids + g.iprobe_ids, op.vprobes + op.iprobes):
+            s = g.probe_series(pid)
+            assert rel_l2(s, gold[f"{name}_probe{pid}"]) < 1e-5
+            if p.fd_interval and p.freqs:
+                d = g.probe_dft(pid, len(p.freqs))
+                ref = gold[f"{name}_dft{pid}"]
+                assert np.linalg.norm(d - ref) <= 1e-5 * np.linalg.norm(ref)
+
+
+def test_plain_cube_full_size_bit_exact(cuda_lib):
+    """100^3 plain configuration, 400 steps, against the single-thread oracle."""
+    op = configs.plain_cube(n=100, steps=400)
+    g, r = _run_pair(op, 400, chunks=(100,))
+    res = compare_engines(g, r)
+    assert all(res.values()), res
+
+
+def test_stress_full_size_properties(cuda_lib):
+    """512x512x256 stress mesh: bit-exact against the multithreaded oracle for a few steps,
+    exact power-of-two linearity in the source amplitude, and snapshot/restore replay."""
+    op = configs.stress(steps=64)
+    g = Engine_CUDA(op, 64)
+    r = OracleEngine(op, 64, threads=os.cpu_count() or 4)
+    g.IterateTS(3)
+    r.IterateTS(3)
+    for w in (0, 1):
+        assert bits_equal(g.read_field(w), r.read_field(w))
+    r.close()
+    # linearity: doubling every source amplitude doubles every field exactly
+    op.exc.volt_amp = (op.exc.volt_amp * 2).astype(np.float32)
+    g2 = Engine_CUDA(op, 64)
+    g.IterateTS(29)
+    g2.IterateTS(32)
+    for w in (0, 1):
+        a, b = g.read_field(w), g2.read_field(w)
+        # exact except where values underflow into denormals (rounding there is not scale-free)
+        assert rel_l2(a * np.float32(2), b) < 1e-7
+        assert np.mean(a * np.float32(2) == b) > 0.999
+    # snapshot / restore: replaying from a checkpoint reproduces the run bit for bit
+    snap = g2.snapshot()
+    g2.IterateTS(16)
+    f1 = [g2.read_field(w) for w in (0, 1)]
+    p1 = g2.probe_series(0) if g2.vprobe_ids else None
+    g2.restore(snap)
+    assert g2.GetNumberOfTimesteps() == 32
+    g2.IterateTS(16)
+    for w in (0, 1):
+        assert bits_equal(g2.read_field(w), f1[w])
+    assert np.isfinite(g2.CalcFastEnergy())
+
+
+def test_errors_are_status_codes(cuda_lib):
+    op = configs.smoke_case()
+    g = Engine_CUDA(op, 10)
+    with pytest.raises(EngineError):
+        g.IterateTS(11)                                  # beyond max_timesteps
+    with pytest.raises(EngineError):
+        g.GetVolt(3, 0, 0, 0)
+    g.IterateTS(10)
+    assert g.GetNumberOfTimesteps() == 10
+    assert np.isfinite(g.CalcFastEnergy())
+
+
+def test_launch_accounting(cuda_lib):
+    op = configs.small_mixed(steps=20)
+    g = Engine_CUDA(op, 20)
+    n = g.launches_per_step()
+    # lorentz pre+apply (V), mur x3, update V, excitation V, update I, step_end
+    assert n >= 6
+    ms, cnt = g.profile(5)
+    assert sum(cnt) == 5 * n
+    g2 = Engine_CUDA(op, 20)
+    g2.IterateTS(5)
+    for w in (0, 1):
+        assert bits_equal(g.read_field(w), g2.read_field(w))
