@@ -191,6 +191,21 @@ int oems_cuda_read_fd_dump(oems_cuda_engine* eng, int dump_id, float* out, size_
  * eps0*sum(V^2) + mu0*sum(I^2) over [0,N-1)^3, device reduction in double. */
 int oems_cuda_energy(oems_cuda_engine* eng, double* energy);
 
+/* Allocation-free variant of the energy reduction, with no counterpart in the reference. It
+ * serves callers that must not call cudaMalloc: their device memory is owned by a host
+ * framework's pool or arena, or they run inside CUDA stream capture. The caller passes its own
+ * device fields volt_dev/curr_dev, float [3][Nx][Ny][z_stride] with z_stride >= Nz, and a host
+ * `energy`. The reduction uses a fixed 128 KB scratch array that is part of the library image,
+ * so the entry point allocates nothing. Limit: Nx-1 <= OEMS_NOALLOC_MAX_PLANES x-planes; larger
+ * meshes return OEMS_ERR_TOO_LARGE. The first call on a device resolves the scratch address
+ * with that device current, so make it before any stream capture. All calls share the scratch,
+ * so calls that overlap on the GPU (different streams at once) race. `stream` is a
+ * cudaStream_t, or NULL for the default stream. The call synchronizes that stream. */
+#define OEMS_NOALLOC_MAX_PLANES 8192
+#define OEMS_ERR_TOO_LARGE    7
+int oems_cuda_energy_noalloc(const float* volt_dev, const float* curr_dev, const unsigned int num_lines[3],
+                             unsigned int z_stride, void* stream, double* energy);
+
 /* ---- checkpoint / resume --------------------------------------------------------------------- */
 
 /* Size in bytes of a snapshot of the full engine state (fields, UPML fluxes, Mur buffers,

@@ -14,7 +14,7 @@ CUDA_LIB = os.path.join(HERE, "_build", "liboems_cuda.so")
 
 OEMS_OK = 0
 ERRORS = {1: "OEMS_ERR_ARG", 2: "OEMS_ERR_CUDA", 3: "OEMS_ERR_STATE", 4: "OEMS_ERR_UNSUPPORTED",
-          5: "OEMS_ERR_DEVICE", 6: "OEMS_ERR_NOMEM"}
+          5: "OEMS_ERR_DEVICE", 6: "OEMS_ERR_NOMEM", 7: "OEMS_ERR_TOO_LARGE"}
 
 P = C.c_void_p
 U = C.c_uint
@@ -66,6 +66,7 @@ CUDA_ONLY = {
     "timed_iterate": (I, [P, U, PF]),
     "profile_steps": (I, [P, U, PF, PU]),
     "read_probe_range": (I, [P, I, SZ, SZ, PD]),
+    "energy_noalloc": (I, [P, P, PU, U, P, PD]),
 }
 
 KERNEL_CLASSES = ["update_v", "update_i", "mur", "lorentz", "excite", "step_end"]

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC_DIR = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboems_cuda.so")
-SOURCES = ["engine.cu"]
+SOURCES = ["engine.cu", "energy_noalloc.cu"]
 HEADERS = ["kernels.cuh"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
