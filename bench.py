@@ -113,10 +113,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def build_workload(name):
+def build_workload(name, shape=None):
     from openems_gb300 import configs
     if name == "stress":
-        return configs.stress(steps=100000), "stress 512x512x256 lines, 64 random blocks (10% Drude/Lorentz), Mur x6, 4 sources"
+        shape = tuple(shape) if shape else (512, 512, 256)
+        return (configs.stress(shape=shape, steps=100000),
+                "stress %dx%dx%d lines, 64 random blocks (10%% Drude/Lorentz), Mur x6, 4 sources" % shape)
     if name == "patch":
         return configs.patch(steps=100000), "patch 160x160x80 graded, UPML 8, 50 Ohm port, NF2FF 3 freqs"
     if name == "plain":
@@ -182,6 +184,7 @@ def main():
     ap.add_argument("--workload", default="stress", choices=["stress", "patch", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--shape", default=None, help="mesh lines of the stress workload, e.g. 256,256,192")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -191,7 +194,7 @@ def main():
     if args.impl == "reference" and rank != 0:
         return
     t_build = time.perf_counter()
-    op, desc = build_workload(args.workload)
+    op, desc = build_workload(args.workload, [int(v) for v in args.shape.split(",")] if args.shape else None)
     t_build = time.perf_counter() - t_build
     if args.impl == "reference":
         run_reference(args, op, desc, rank)

@@ -254,9 +254,14 @@ __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __restrict
     const MurWallDev& w = m.w[wi];
     const unsigned ts = *numTS;
     if (ts < w.start_ts) return;              // Engine_Ext_Mur_ABC::IsActive
-    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= w.n1 * w.n2) return;
-    const unsigned i = k / w.n2, j = k - i * w.n2;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= w.n1 * w.n2) return;
+    // consecutive threads walk the tangential axis that is contiguous in memory (z when it is
+    // tangential, else y); the small per-wall tables are L2-resident either way
+    unsigned i, j;
+    if (w.nyP == 2) { i = t % w.n1; j = t / w.n1; }
+    else { i = t / w.n2; j = t - i * w.n2; }
+    const unsigned k = i * w.n2 + j;
     unsigned pos[3], ps[3];
     pos[w.ny] = w.line; ps[w.ny] = w.shift;
     pos[w.nyP] = ps[w.nyP] = i;
