@@ -144,6 +144,76 @@ def cpu_baseline(op, steps_cap, budget_s, threads):
     return cells * n / dt / 1e6, n, dt
 
 
+def measure_batched(count):
+    """Batched form: `count` seeded instances (lines U[48,160]^3, 0.5-2 mm, UPML 8, dielectric
+    block, 50 Ohm port, steps U[4000,12000]) run serially (one engine after the other, each
+    replaying its step graph) and then together (persistent launches in one graph); sims/s of
+    both, wall clock around the run calls with the device synchronised, setup excluded."""
+    from openems_gb300 import configs
+    from openems_gb300.batch import BatchEngine
+    from openems_gb300.engine import Engine_CUDA
+    t0 = time.perf_counter()
+    inst = [configs.batch_instance(1000 + k) for k in range(count)]
+    t_build = time.perf_counter() - t0
+    steps = [s for _, s in inst]
+    cells = [float(np.prod(op.num_lines.astype(np.float64))) for op, _ in inst]
+    cell_steps = sum(c * s for c, s in zip(cells, steps))
+    # serial: one engine at a time
+    serial_s = 0.0
+    per_inst = []
+    for op, s in inst:
+        e = Engine_CUDA(op, s)
+        e.sync()
+        t = time.perf_counter()
+        e.IterateTS(s)
+        e.sync()
+        dt = time.perf_counter() - t
+        serial_s += dt
+        per_inst.append([int(np.prod(op.num_lines.astype(np.float64))), s, round(dt, 4)])
+        e.close()
+    # serial in openEMS's processing-loop style (RunFDTD, openems.cpp:1427-1431): with probes
+    # sampled every step the loop runs IterateTS(1) and then reads the probes on the host
+    loop_s = 0.0
+    for op, s in inst:
+        e = Engine_CUDA(op, s)
+        pids = e.vprobe_ids + e.iprobe_ids
+        e.sync()
+        t = time.perf_counter()
+        for k in range(1, s + 1):
+            e.IterateTS(1)
+            for pid in pids:
+                e.probe_range(pid, k, 1)
+        loop_s += time.perf_counter() - t
+        e.close()
+    engines = [Engine_CUDA(op, s) for op, s in inst]
+    for e in engines:
+        e.sync()
+    be = BatchEngine(engines)
+    t = time.perf_counter()
+    be.run(steps)
+    batch_s = time.perf_counter() - t
+    cfg = be.config()
+    # every instance's port V/I series against a serial rerun of two instances (spot check)
+    same = True
+    for k in (0, count - 1):
+        e = Engine_CUDA(inst[k][0], steps[k])
+        e.IterateTS(steps[k])
+        for pid in e.vprobe_ids + e.iprobe_ids:
+            same &= bool(np.array_equal(e.probe_series(pid), engines[k].probe_series(pid), equal_nan=True))
+        e.close()
+    be.close()
+    for e in engines:
+        e.close()
+    return {"instances": count, "sims_per_s_batched": count / batch_s, "sims_per_s_serial": count / serial_s,
+            "speedup": serial_s / batch_s, "batched_s": batch_s, "serial_s": serial_s,
+            "sims_per_s_serial_processing_loop": count / loop_s, "speedup_vs_processing_loop": loop_s / batch_s,
+            "serial_processing_loop_s": loop_s,
+            "mcells_per_s_batched": cell_steps / batch_s / 1e6, "mcells_per_s_serial": cell_steps / serial_s / 1e6,
+            "total_cells": sum(cells), "steps_min_max": [min(steps), max(steps)], "tuned": cfg,
+            "series_equal_serial_spot_check": same, "build_s": round(t_build, 1),
+            "serial_per_instance_cells_steps_s": per_inst}
+
+
 def run_reference(args, op, desc, rank):
     if rank != 0:
         return
@@ -185,6 +255,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--shape", default=None, help="mesh lines of the stress workload, e.g. 256,256,192")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--batch-count", type=int, default=32)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -264,6 +336,10 @@ def main():
     launches = eng.launches_per_step()
     eng.close()
 
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = measure_batched(args.batch_count)
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -286,6 +362,7 @@ def main():
             "gpu_launches": launches * args.steps,
             "launches_per_step": launches,
             "kernels": kernels,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if dist:

@@ -206,6 +206,31 @@ int oems_cuda_energy(oems_cuda_engine* eng, double* energy);
 int oems_cuda_energy_noalloc(const float* volt_dev, const float* curr_dev, const unsigned int num_lines[3],
                              unsigned int z_stride, void* stream, double* energy);
 
+/* ---- batched form ------------------------------------------------------------------------------ */
+
+/* Many independent simulations (engine handles already through oems_cuda_init, same device),
+ * advanced together. Replaces running openEMS once per excitation/geometry variant (the loop a
+ * user writes around openEMS.Run, python/openEMS/openEMS.pyx:513-564, e.g. one run per port of an
+ * S-parameter sweep). Supported per instance: excitation, UPML, probes and probe DFTs;
+ * instances with Mur walls, dispersive materials or FD dumps give OEMS_ERR_UNSUPPORTED. The
+ * batch references the engines' device state; destroy it before the engines. */
+typedef struct oems_cuda_batch oems_cuda_batch;
+int oems_cuda_batch_create(oems_cuda_engine* const* engines, unsigned int count, oems_cuda_batch** out);
+
+/* Advance instance k by steps[k] timesteps (uneven counts allowed). Each chunk of steps over the
+ * instances active throughout it is one persistent cooperative launch; the launches are
+ * captured in one CUDA graph. block_size/depth = 0 lets the built-in autotuner time the
+ * candidate (block size, x-planes per work item) pairs on the first steps and keep the
+ * fastest. Results are bit-identical to running each engine alone with oems_cuda_iterate. */
+int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned int block_size, unsigned int depth);
+
+/* The configuration in use, whether the launches ran from a captured graph, and the autotuner's
+ * per-candidate timings (ms for the same number of steps each). */
+int oems_cuda_batch_config(const oems_cuda_batch* b, unsigned int* block_size, unsigned int* depth, int* used_graph,
+                           float* tune_ms, unsigned int* num_candidates);
+
+void oems_cuda_batch_destroy(oems_cuda_batch* b);
+
 /* ---- checkpoint / resume --------------------------------------------------------------------- */
 
 /* Size in bytes of a snapshot of the full engine state (fields, UPML fluxes, Mur buffers,

@@ -67,6 +67,10 @@ CUDA_ONLY = {
     "profile_steps": (I, [P, U, PF, PU]),
     "read_probe_range": (I, [P, I, SZ, SZ, PD]),
     "energy_noalloc": (I, [P, P, PU, U, P, PD]),
+    "batch_create": (I, [C.POINTER(P), U, C.POINTER(P)]),
+    "batch_run": (I, [P, PU, U, U]),
+    "batch_config": (I, [P, PU, PU, PI_, PF, PU]),
+    "batch_destroy": (None, [P]),
 }
 
 KERNEL_CLASSES = ["update_v", "update_i", "mur", "lorentz", "excite", "step_end"]

@@ -248,3 +248,34 @@ def cavity(steps=4000):
                                               [mx[f(mx, .5)], my[f(my, .5)], mz[f(mz, .2) + 1]])
     op = Operator(csx, g, exc, bc=(0,) * 6)
     return op.build(steps)
+
+
+# ------------------------------------------------------------------------------------------
+def batch_instance(seed, size_range=(48, 160), pitch_range=(0.5, 2.0), steps_range=(4000, 12000), pml=8):
+    """One simulation of the batched form: lines U[size_range]^3 at a uniform pitch
+    U[pitch_range] mm, UPML on all sides, one dielectric block (eps_r U[2,12]), a 50 Ohm lumped
+    port along z at the centre with a Gaussian excitation (f0 U[1,5] GHz, fc = f0/2), port U/I
+    probes every step.  Returns (OperatorData, steps)."""
+    rng = np.random.default_rng(seed)
+    n = [int(rng.integers(size_range[0], size_range[1] + 1)) for _ in range(3)]
+    pitch = float(rng.uniform(*pitch_range))
+    steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+    g = Grid([_uniform(k, pitch) for k in n], unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    f0 = float(rng.uniform(1e9, 5e9))
+    exc.SetupGaussianPulse(f0, f0 / 2)
+    lo_i = [pml + 2 + int(rng.integers(0, max(1, k // 4))) for k in n]
+    hi_i = [max(lo_i[a] + 2, n[a] - pml - 3 - int(rng.integers(0, max(1, n[a] // 4)))) for a in range(3)]
+    csx.AddMaterial("block", epsilon=float(rng.uniform(2.0, 12.0))).AddBox(
+        [lo_i[a] * pitch for a in range(3)], [hi_i[a] * pitch for a in range(3)])
+    c = [k // 2 for k in n]
+    z0, z1 = (c[2] - 1) * pitch, (c[2] + 1) * pitch
+    px, py = c[0] * pitch, c[1] * pitch
+    csx.AddLumpedElement("port_R", ny=2, R=50.0, caps=True).AddBox([px, py, z0], [px, py, z1], priority=10)
+    csx.AddExcitation("port_exc", 0, [0, 0, -1.0]).AddBox([px, py, z0], [px, py, z1], priority=10)
+    csx.AddProbe("port_ut", 0, weight=-1.0, interval=1).AddBox([px, py, z0], [px, py, z1])
+    zm = 0.5 * (z0 + z1)
+    csx.AddProbe("port_it", 1, weight=1.0, norm_dir=2, interval=1).AddBox([px, py, zm], [px, py, zm])
+    op = Operator(csx, g, exc, bc=(3,) * 6, pml_size=(pml,) * 6)
+    return op.build(steps), steps

@@ -21,107 +21,9 @@
 #include <string>
 #include <vector>
 
-#include "../../include/oems_cuda.h"
-#include "kernels.cuh"
+#include "engine_impl.h"
 
 using namespace oems;
-
-namespace {
-
-const double kPI = 3.14159265358979323846;  // M_PI as used by Common/processintegral.cpp:161
-
-struct UpmlHost {
-    unsigned start[3], nl[3];
-    std::vector<float> tab[6];  // vv, vvfo, vvfn, ii, iifo, iifn
-};
-struct MurHost {
-    int ny;
-    unsigned line, shift, start_ts;
-    std::vector<float> cP, cPP;
-};
-struct LorHost {
-    unsigned count;
-    std::vector<unsigned> pos;
-    int von, con, vlon, clon;
-    std::vector<float> vint, vext, vlor, iint, iext, ilor;
-};
-struct ProbeHost {
-    int type;
-    unsigned start[3], stop[3];
-    int nd, si[3], ei[3];
-    double weight;
-    unsigned interval, start_ts, stop_ts;
-    unsigned fd_interval = 0;
-    std::vector<double> freqs;
-};
-struct DumpHost {
-    int field;
-    unsigned start[3], stop[3];
-    unsigned fd_interval;
-    std::vector<double> freqs;
-    std::vector<double> el;  // edge lengths used by this field type, concatenated x,y,z
-};
-
-}  // namespace
-
-struct oems_cuda_engine {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    unsigned N[3] = {0, 0, 0};
-    unsigned Pz = 0;
-    unsigned long long S = 0;
-    double dt = 0;
-    std::string err;
-
-    // fields
-    float* dV = nullptr;
-    float* dI = nullptr;
-
-    // operator
-    bool op_set = false;
-    bool compressed = false;
-    unsigned nclasses = 0;
-    unsigned* didx = nullptr;
-    float4* dtabV = nullptr;
-    float4* dtabI = nullptr;
-    float *dvv = nullptr, *dvi = nullptr, *dii = nullptr, *div = nullptr;
-
-    // extensions (host copies until init)
-    bool has_exc = false;
-    std::vector<unsigned long long> exc_voff, exc_ioff;
-    std::vector<float> exc_vamp, exc_iamp, sig_v, sig_i;
-    std::vector<unsigned> exc_vdelay, exc_idelay;
-    unsigned sig_len = 0, period = 0;
-    std::vector<UpmlHost> upml;
-    std::vector<MurHost> mur;
-    std::vector<LorHost> lor;
-    std::vector<ProbeHost> probes;
-    std::vector<DumpHost> dumps;
-
-    // device state after init
-    bool inited = false;
-    unsigned max_ts = 0;
-    unsigned* d_numTS = nullptr;
-    unsigned* d_blocks_done = nullptr;
-    unsigned host_numTS = 0;
-    GridDev grid{};
-    ExcDev excV{}, excI{};
-    MurDev murdev{};
-    std::vector<LorDev> lorV, lorI;
-    StepEndDev stepend{};
-    unsigned stepend_blocks = 1;
-    std::vector<ProbeDev> probe_dev;   // host mirror of device structs
-    std::vector<DumpDev> dump_dev;
-    unsigned launches = 0;
-    cudaGraphExec_t graph1 = nullptr;
-    cudaGraphExec_t graphK = nullptr;
-    unsigned K = 16;
-    double* d_energy_partial = nullptr;
-    unsigned energy_blocks = 0;
-
-    std::vector<void*> allocs;                            // freed on destroy
-    std::vector<std::pair<void*, size_t>> state;          // snapshot regions (device)
-};
 
 namespace {
 
@@ -548,13 +450,9 @@ int oems_cuda_add_fd_dump(oems_cuda_engine* e, int field, const unsigned int sta
 // ---------------------------------------------------------------------------------------------
 // init: upload, build device structs, capture graphs
 
-struct StepProfiler {
-    cudaEvent_t ev[2 * 64];
-    int cls[64];
-    int n = 0;
-};
+}  // extern "C" (enqueue_step below is internal C++)
 
-static int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof = nullptr)
+int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
 {
     const GridDev& g = e->grid;
     const unsigned plane = e->N[1] * e->Pz;
@@ -625,6 +523,8 @@ static int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* pr
     if (c != cudaSuccess) return cuda_fail(e, c, "kernel launch");
     return OEMS_OK;
 }
+
+extern "C" {
 
 static int capture(oems_cuda_engine* e, unsigned steps, cudaGraphExec_t* out)
 {

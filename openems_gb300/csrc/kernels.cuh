@@ -71,15 +71,19 @@ __device__ __forceinline__ int upml_find(const GridDev& g, unsigned x, unsigned 
 
 // ---------------------------------------------------------------------------------------------
 // Engine::UpdateVoltages (FDTD/engine.cpp:110-168) fused with Engine_Ext_UPML pre/post voltage
-// updates (FDTD/extensions/engine_ext_upml.cpp:52-137).  One thread per cell of an x-plane
-// (blockIdx.y = x), z fastest for coalescing.
-template <bool COMPRESSED, bool UPML>
-__global__ void __launch_bounds__(256) k_update_v(GridDev g)
+// updates (FDTD/extensions/engine_ext_upml.cpp:52-137) for one cell (x, y, z < Nz).
+// COHERENT: field loads bypass L1 (ld.global.cg). Needed inside persistent launches, where the
+// other field was rewritten by other blocks earlier in the same launch; a single-phase launch
+// can use the read-only path.
+template <bool COHERENT>
+__device__ __forceinline__ float ldf(const float* p)
 {
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned y = t / g.Pz, z = t - y * g.Pz;
-    if (y >= g.Ny || z >= g.Nz) return;
+    return COHERENT ? __ldcg(p) : __ldg(p);
+}
+
+template <bool COMPRESSED, bool UPML, bool COHERENT = false>
+__device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsigned y, unsigned z)
+{
     const unsigned long long S = g.S;
     const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
     const unsigned long long sx = x ? (unsigned long long)g.Ny * g.Pz : 0ull;
@@ -88,11 +92,11 @@ __global__ void __launch_bounds__(256) k_update_v(GridDev g)
     const float* __restrict__ I = g.I;
     float* __restrict__ V = g.V;
 
-    const float i0 = __ldg(I + o), i1 = __ldg(I + S + o), i2 = __ldg(I + 2 * S + o);
+    const float i0 = ldf<COHERENT>(I + o), i1 = ldf<COHERENT>(I + S + o), i2 = ldf<COHERENT>(I + 2 * S + o);
     // curl terms in the reference's evaluation order ((a - b) - c) + d
-    const float c0 = fadd(fsub(fsub(i2, __ldg(I + 2 * S + o - sy)), i1), __ldg(I + S + o - sz));
-    const float c1 = fadd(fsub(fsub(i0, __ldg(I + o - sz)), i2), __ldg(I + 2 * S + o - sx));
-    const float c2 = fadd(fsub(fsub(i1, __ldg(I + S + o - sx)), i0), __ldg(I + o - sy));
+    const float c0 = fadd(fsub(fsub(i2, ldf<COHERENT>(I + 2 * S + o - sy)), i1), ldf<COHERENT>(I + S + o - sz));
+    const float c1 = fadd(fsub(fsub(i0, ldf<COHERENT>(I + o - sz)), i2), ldf<COHERENT>(I + 2 * S + o - sx));
+    const float c2 = fadd(fsub(fsub(i1, ldf<COHERENT>(I + S + o - sx)), i0), ldf<COHERENT>(I + o - sy));
 
     float vv0, vv1, vv2, vi0, vi1, vi2;
     if (COMPRESSED) {
@@ -103,7 +107,9 @@ __global__ void __launch_bounds__(256) k_update_v(GridDev g)
         vv0 = __ldg(g.vv + o); vv1 = __ldg(g.vv + S + o); vv2 = __ldg(g.vv + 2 * S + o);
         vi0 = __ldg(g.vi + o); vi1 = __ldg(g.vi + S + o); vi2 = __ldg(g.vi + 2 * S + o);
     }
-    float v0 = V[o], v1 = V[S + o], v2 = V[2 * S + o];
+    float v0, v1, v2;
+    if (COHERENT) { v0 = __ldcg(V + o); v1 = __ldcg(V + S + o); v2 = __ldcg(V + 2 * S + o); }
+    else { v0 = V[o]; v1 = V[S + o]; v2 = V[2 * S + o]; }
 
     int r = -1;
     unsigned loc = 0;
@@ -137,14 +143,10 @@ __global__ void __launch_bounds__(256) k_update_v(GridDev g)
 }
 
 // Engine::UpdateCurrents (FDTD/engine.cpp:170-222) fused with the UPML current hooks
-// (FDTD/extensions/engine_ext_upml.cpp:144-229).  Cells x<Nx-1, y<Ny-1, z<Nz-1 only.
-template <bool COMPRESSED, bool UPML>
-__global__ void __launch_bounds__(256) k_update_i(GridDev g)
+// (FDTD/extensions/engine_ext_upml.cpp:144-229) for one cell x<Nx-1, y<Ny-1, z<Nz-1.
+template <bool COMPRESSED, bool UPML, bool COHERENT = false>
+__device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsigned y, unsigned z)
 {
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned y = t / g.Pz, z = t - y * g.Pz;
-    if (y + 1 >= g.Ny || z + 1 >= g.Nz) return;
     const unsigned long long S = g.S;
     const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
     const unsigned long long sx = (unsigned long long)g.Ny * g.Pz;
@@ -152,10 +154,10 @@ __global__ void __launch_bounds__(256) k_update_i(GridDev g)
     const float* __restrict__ V = g.V;
     float* __restrict__ I = g.I;
 
-    const float w0 = __ldg(V + o), w1 = __ldg(V + S + o), w2 = __ldg(V + 2 * S + o);
-    const float c0 = fadd(fsub(fsub(w2, __ldg(V + 2 * S + o + sy)), w1), __ldg(V + S + o + 1));
-    const float c1 = fadd(fsub(fsub(w0, __ldg(V + o + 1)), w2), __ldg(V + 2 * S + o + sx));
-    const float c2 = fadd(fsub(fsub(w1, __ldg(V + S + o + sx)), w0), __ldg(V + o + sy));
+    const float w0 = ldf<COHERENT>(V + o), w1 = ldf<COHERENT>(V + S + o), w2 = ldf<COHERENT>(V + 2 * S + o);
+    const float c0 = fadd(fsub(fsub(w2, ldf<COHERENT>(V + 2 * S + o + sy)), w1), ldf<COHERENT>(V + S + o + 1));
+    const float c1 = fadd(fsub(fsub(w0, ldf<COHERENT>(V + o + 1)), w2), ldf<COHERENT>(V + 2 * S + o + sx));
+    const float c2 = fadd(fsub(fsub(w1, ldf<COHERENT>(V + S + o + sx)), w0), ldf<COHERENT>(V + o + sy));
 
     float ii0, ii1, ii2, iv0, iv1, iv2;
     if (COMPRESSED) {
@@ -166,7 +168,9 @@ __global__ void __launch_bounds__(256) k_update_i(GridDev g)
         ii0 = __ldg(g.ii + o); ii1 = __ldg(g.ii + S + o); ii2 = __ldg(g.ii + 2 * S + o);
         iv0 = __ldg(g.iv + o); iv1 = __ldg(g.iv + S + o); iv2 = __ldg(g.iv + 2 * S + o);
     }
-    float a0 = I[o], a1 = I[S + o], a2 = I[2 * S + o];
+    float a0, a1, a2;
+    if (COHERENT) { a0 = __ldcg(I + o); a1 = __ldcg(I + S + o); a2 = __ldcg(I + 2 * S + o); }
+    else { a0 = I[o]; a1 = I[S + o]; a2 = I[2 * S + o]; }
 
     int r = -1;
     unsigned loc = 0;
@@ -197,6 +201,27 @@ __global__ void __launch_bounds__(256) k_update_i(GridDev g)
     I[2 * S + o] = fadd(fmul(a2, ii2), fmul(iv2, c2));
 }
 
+// One thread per cell of an x-plane (blockIdx.y = x), z fastest for coalescing.
+template <bool COMPRESSED, bool UPML>
+__global__ void __launch_bounds__(256) k_update_v(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned y = t / g.Pz, z = t - y * g.Pz;
+    if (y >= g.Ny || z >= g.Nz) return;
+    update_v_cell<COMPRESSED, UPML>(g, x, y, z);
+}
+
+template <bool COMPRESSED, bool UPML>
+__global__ void __launch_bounds__(256) k_update_i(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned y = t / g.Pz, z = t - y * g.Pz;
+    if (y + 1 >= g.Ny || z + 1 >= g.Nz) return;
+    update_i_cell<COMPRESSED, UPML>(g, x, y, z);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Engine_Ext_Excitation::Apply2VoltagesImpl / Apply2CurrentImpl
 // (FDTD/extensions/engine_ext_excitation.cpp:33-94).  One thread per source edge; the source
@@ -211,7 +236,7 @@ struct ExcDev {
     unsigned period;                 // 0 = aperiodic
 };
 
-__global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsigned* __restrict__ numTS)
+static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsigned* __restrict__ numTS)
 {
     const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= e.count) return;
@@ -247,7 +272,7 @@ __device__ __forceinline__ unsigned long long mur_off(const GridDev& g, int comp
 }
 
 // phase 0 = pre (before the V update), 1 = post (after), 2 = apply
-__global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __restrict__ numTS)
+static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __restrict__ numTS)
 {
     const int wi = blockIdx.y;
     if (wi >= m.nwall) return;
@@ -302,7 +327,7 @@ struct LorDev {
     float* lade;
 };
 
-__global__ void k_lorentz_pre(const float* __restrict__ F, unsigned long long S, LorDev l)
+static __global__ void k_lorentz_pre(const float* __restrict__ F, unsigned long long S, LorDev l)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= l.count) return;
@@ -325,7 +350,7 @@ __global__ void k_lorentz_pre(const float* __restrict__ F, unsigned long long S,
     }
 }
 
-__global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long S, LorDev l)
+static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long S, LorDev l)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= l.count) return;
@@ -375,7 +400,7 @@ struct StepEndDev {
     unsigned* blocks_done;
 };
 
-__device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned ts, int lane)
+static __device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned ts, int lane)
 {
     if (ts < p.start_ts || ts > p.stop_ts) return;
     const bool do_td = (ts % p.interval) == 0;
@@ -389,7 +414,7 @@ __device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned ts, int
         const unsigned k = base + lane;
         float v = 0.0f;
         int s = 0;
-        if (k < p.nterm) { v = F[p.term[k]]; s = p.sign[k]; }
+        if (k < p.nterm) { v = __ldcg(F + p.term[k]); s = p.sign[k]; }
         const unsigned cnt = min(32u, p.nterm - base);
         for (unsigned j = 0; j < cnt; ++j) {
             const float vj = __shfl_sync(0xffffffffu, v, j);
@@ -424,7 +449,7 @@ __device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned ts, int
 }
 
 // cell-interpolated E (FDTD/engine_interface_fdtd.cpp:104-121) or H (:182-199) at pos
-__device__ void cell_field(const GridDev& g, const DumpDev& d, const unsigned pos[3], double out[3])
+static __device__ void cell_field(const GridDev& g, const DumpDev& d, const unsigned pos[3], double out[3])
 {
     const unsigned N[3] = {g.Nx, g.Ny, g.Nz};
     const unsigned eoff[3] = {0u, g.Nx, g.Nx + g.Ny};
@@ -472,7 +497,7 @@ __device__ void cell_field(const GridDev& g, const DumpDev& d, const unsigned po
 // One launch: block 0 warps evaluate the probes; blocks [dump_block0[k], dump_block0[k+1])
 // handle dump k (one thread per box position, all frequencies).  The last block to finish
 // increments numTS (threadfence + completion counter), so every block read the same ts.
-__global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s)
+static __global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s)
 {
     const unsigned ts = *s.numTS + 1;   // the step just completed
     if (blockIdx.x == 0) {
@@ -526,7 +551,7 @@ __global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s)
 // ---------------------------------------------------------------------------------------------
 // Engine_Interface_FDTD::CalcFastEnergy (FDTD/engine_interface_fdtd.cpp:302-347): double
 // accumulation of float squares over [0,N-1)^3; block partials then one final reduction.
-__global__ void __launch_bounds__(256) k_energy(GridDev g, double* __restrict__ partial)
+static __global__ void __launch_bounds__(256) k_energy(GridDev g, double* __restrict__ partial)
 {
     double e = 0.0, h = 0.0;
     const unsigned long long plane = (unsigned long long)g.Ny * g.Pz;
