@@ -231,6 +231,32 @@ int oems_cuda_batch_config(const oems_cuda_batch* b, unsigned int* block_size, u
 
 void oems_cuda_batch_destroy(oems_cuda_batch* b);
 
+/* ---- adjoint (reverse-mode) form --------------------------------------------------------------- */
+
+/* Gradients of an objective built from probe samples with respect to the voltage coefficients
+ * vv/vi of the edges in a design box. No reference counterpart: openEMS has no derivative
+ * path; this is what an optimisation loop around python/openEMS/openEMS.pyx:513-564 (one
+ * forward run per trial design) would call instead of finite differences.
+ *
+ * setup: after oems_cuda_init on a fresh engine. The design box covers the mesh nodes
+ * box_start..box_stop-1 and may not overlap a UPML region; engines with Mur walls or dispersive
+ * materials give OEMS_ERR_UNSUPPORTED. checkpoint_every = K: the forward run stores the full
+ * state every K steps, the reverse sweep recomputes one K-step segment at a time. */
+int oems_cuda_adjoint_setup(oems_cuda_engine* eng, unsigned int checkpoint_every, const unsigned int box_start[3],
+                            const unsigned int box_stop[3]);
+/* Forward run of `steps` timesteps from numTS = 0 with checkpoints; probes record as usual. */
+int oems_cuda_adjoint_forward(oems_cuda_engine* eng, unsigned int steps);
+/* Reverse sweep. sources[k*(steps+1) + n] = dJ/d(sample of probe probe_ids[k] at numTS = n)
+ * (the weighted line integral of the probe, before any DFT). Writes dJ/dvv and dJ/dvi of the
+ * design box edges, double [3][bx][by][bz] each (component-major, z fastest). The engine is
+ * left at its forward end state. */
+int oems_cuda_adjoint_backward(oems_cuda_engine* eng, unsigned int nprobe, const int* probe_ids, const double* sources,
+                               double* grad_vv, double* grad_vi);
+/* Device time (CUDA events on the engine stream) of the last adjoint forward and backward calls,
+ * and the kernel launches per reverse step (any pointer may be NULL). */
+int oems_cuda_adjoint_timing(const oems_cuda_engine* eng, float* forward_ms, float* backward_ms,
+                             unsigned int* launches_per_reverse_step);
+
 /* ---- checkpoint / resume --------------------------------------------------------------------- */
 
 /* Size in bytes of a snapshot of the full engine state (fields, UPML fluxes, Mur buffers,

@@ -71,6 +71,10 @@ CUDA_ONLY = {
     "batch_run": (I, [P, PU, U, U]),
     "batch_config": (I, [P, PU, PU, PI_, PF, PU]),
     "batch_destroy": (None, [P]),
+    "adjoint_setup": (I, [P, U, PU, PU]),
+    "adjoint_forward": (I, [P, U]),
+    "adjoint_backward": (I, [P, U, PI_, PD, PD, PD]),
+    "adjoint_timing": (I, [P, PF, PF, PU]),
 }
 
 KERNEL_CLASSES = ["update_v", "update_i", "mur", "lorentz", "excite", "step_end"]

@@ -279,3 +279,80 @@ def batch_instance(seed, size_range=(48, 160), pitch_range=(0.5, 2.0), steps_ran
     csx.AddProbe("port_it", 1, weight=1.0, norm_dir=2, interval=1).AddBox([px, py, zm], [px, py, zm])
     op = Operator(csx, g, exc, bc=(3,) * 6, pml_size=(pml,) * 6)
     return op.build(steps), steps
+
+
+# ------------------------------------------------------------------------------------------
+class DesignCase:
+    """The differentiable form: a uniform mesh with UPML on all sides, a box of per-cell
+    eps_r / kappa (the design region) and two 50 Ohm lumped ports along z, each about ``gap``
+    cells (Euclidean, diagonally in x-y) from the nearest design cell.  The input port carries
+    a Gaussian pulse; the output port has U/I probes sampled every step.
+
+    ``build(eps, kappa, fdtd_float)`` makes the operator for one design at a fixed timestep
+    (just below the one of the initial design), so every design of an optimisation or a finite-difference
+    stencil runs with the same dt and excitation signal."""
+
+    def __init__(self, lines=(200, 200, 100), pitch_mm=0.5, design=(64, 64, 16), gap=60, steps=8000, pml=8,
+                 freqs=(4e9, 5e9, 6e9), f0=5e9, fc=2e9, seed=0, eps_range=(1.0, 6.0), dt=None):
+        self.lines = tuple(int(v) for v in lines)
+        self.pitch = float(pitch_mm)
+        self.design = tuple(int(v) for v in design)
+        self.steps = int(steps)
+        self.pml = int(pml)
+        self.freqs = tuple(float(f) for f in freqs)
+        self.f0, self.fc = float(f0), float(fc)
+        cells = [n - 1 for n in self.lines]
+        self.c0 = [(cells[a] - self.design[a]) // 2 for a in range(3)]     # first design cell
+        off = int(np.ceil(gap / np.sqrt(2.0)))
+        zc = self.c0[2] + self.design[2] // 2
+        self.port_in = (self.c0[0] - off, self.c0[1] - off, zc)
+        self.port_out = (self.c0[0] + self.design[0] + off, self.c0[1] + self.design[1] + off, zc)
+        for p in (self.port_in, self.port_out):
+            for a in range(2):
+                if not (pml + 3 <= p[a] <= self.lines[a] - pml - 4):
+                    raise ValueError(f"DesignCase: port {p} is too close to the UPML")
+        if not (pml + 2 <= zc - 1 and zc + 1 <= self.lines[2] - pml - 3):
+            raise ValueError("DesignCase: ports too close to the z UPML")
+        for a in range(3):
+            if self.c0[a] < pml + 1 or self.c0[a] + self.design[a] > cells[a] - pml - 1:
+                raise ValueError("DesignCase: design region overlaps the UPML")
+        rng = np.random.default_rng(seed)
+        self.eps0 = rng.uniform(eps_range[0], eps_range[1], self.design)
+        self.kappa0 = np.zeros(self.design)
+        # fixed timestep: 0.995 x the Var3 timestep of the initial design, so that designs a
+        # little below it (finite-difference stencils at eps_r near 1) stay within the bound
+        self.dt = None
+        self.dt = float(dt) if dt else 0.995 * self.build(self.eps0, self.kappa0)[1].dt
+
+    @property
+    def box_nodes(self):
+        """Mesh nodes whose edges touch the design cells: [start, stop) per axis."""
+        return [self.c0[a] for a in range(3)], [self.c0[a] + self.design[a] + 1 for a in range(3)]
+
+    def build(self, eps, kappa=None, fdtd_float=np.float32):
+        """(Operator, OperatorData) for one design."""
+        p = self.pitch
+        g = Grid([_uniform(k, p) for k in self.lines], unit=1e-3)
+        csx = Structure()
+        exc = Excitation()
+        exc.SetupGaussianPulse(self.f0, self.fc)
+        lo = [self.c0[a] * p for a in range(3)]
+        hi = [(self.c0[a] + self.design[a]) * p for a in range(3)]
+        kap = self.kappa0 if kappa is None else kappa
+        csx.AddVoxelMaterial("design", lo, hi, np.asarray(eps, np.float64), kappa=np.asarray(kap, np.float64))
+        for name, (x, y, z), src in (("in", self.port_in, True), ("out", self.port_out, False)):
+            z0, z1 = (z - 1) * p, (z + 1) * p
+            csx.AddLumpedElement(f"port_{name}_R", ny=2, R=50.0, caps=True).AddBox([x * p, y * p, z0], [x * p, y * p, z1],
+                                                                                 priority=10)
+            if src:
+                csx.AddExcitation(f"port_{name}_exc", 0, [0, 0, -1.0]).AddBox([x * p, y * p, z0], [x * p, y * p, z1],
+                                                                             priority=10)
+            else:
+                csx.AddProbe(f"port_{name}_ut", 0, weight=-1.0, interval=1).AddBox([x * p, y * p, z0],
+                                                                                  [x * p, y * p, z1])
+                zm = 0.5 * (z0 + z1)
+                csx.AddProbe(f"port_{name}_it", 1, weight=1.0, norm_dir=2, interval=1).AddBox([x * p, y * p, zm],
+                                                                                             [x * p, y * p, zm])
+        op = Operator(csx, g, exc, bc=(3,) * 6, pml_size=(self.pml,) * 6, timestep=self.dt or 0.0,
+                      fdtd_float=fdtd_float)
+        return op, op.build(self.steps)

@@ -208,6 +208,7 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->graph1) cudaGraphExecDestroy(e->graph1);
     if (e->graphK) cudaGraphExecDestroy(e->graphK);
+    oems_adjoint_free(e->adj);
     for (void* p : e->allocs) cudaFree(p);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;

@@ -51,6 +51,10 @@ struct DumpHost {
 
 using namespace oems_host;
 
+// adjoint state (adjoint.cu); freed by oems_cuda_destroy
+struct oems_adjoint_state;
+void oems_adjoint_free(oems_adjoint_state* s);
+
 struct oems_cuda_engine {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -108,6 +112,7 @@ struct oems_cuda_engine {
 
     std::vector<void*> allocs;                            // freed on destroy
     std::vector<std::pair<void*, size_t>> state;          // snapshot regions (device)
+    oems_adjoint_state* adj = nullptr;
 };
 
 

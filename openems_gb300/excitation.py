@@ -30,6 +30,7 @@ class Excitation:
     GAUSSIAN, SINUS, DIRAC, STEP = 0, 1, 2, 3
 
     def __init__(self):
+        self.ft = np.float32       # FDTD_FLOAT (tools/constants.h:21); float64 for FP64 checks
         self.kind = None
         self.f0 = 0.0
         self.fc = 0.0
@@ -38,8 +39,8 @@ class Excitation:
         self.dt = 0.0
         self.length = 0
         self.nyquist = 0
-        self.volt = np.zeros(0, np.float32)
-        self.curr = np.zeros(0, np.float32)
+        self.volt = np.zeros(0, self.ft)
+        self.curr = np.zeros(0, self.ft)
 
     # --- setup (FDTD/excitation.cpp:55-93) -------------------------------------------------
     def SetupGaussianPulse(self, f0: float, fc: float):
@@ -67,13 +68,13 @@ class Excitation:
             self._sinus(self.f0, int(max_ts))
         elif self.kind == self.DIRAC:
             self.length = 2
-            self.volt = np.array([0.0, 1.0], np.float32)
-            self.curr = np.array([0.0, 1.0], np.float32)
+            self.volt = np.array([0.0, 1.0], self.ft)
+            self.curr = np.array([0.0, 1.0], self.ft)
             self.nyquist = 1
         elif self.kind == self.STEP:
             self.length = 2
-            self.volt = np.array([1.0, 1.0], np.float32)
-            self.curr = np.array([1.0, 1.0], np.float32)
+            self.volt = np.array([1.0, 1.0], self.ft)
+            self.curr = np.array([1.0, 1.0], self.ft)
             self.nyquist = 1
         else:
             raise ValueError("Excitation: unknown excitation type")
@@ -94,8 +95,8 @@ class Excitation:
             t += 0.5 * dt
             c[n] = math.cos(2.0 * PI * f0 * (t - 9.0 / (2.0 * PI * fc))) * math.exp(-1 * math.pow(2.0 * PI * fc * t / 3.0 - 3, 2))
         self.length = length
-        self.volt = v.astype(np.float32)
-        self.curr = c.astype(np.float32)
+        self.volt = v.astype(self.ft)
+        self.curr = c.astype(self.ft)
         self.f_max = f0 + fc
         self.nyquist = calc_nyquist_num(f0 + fc, dt)
 
@@ -111,8 +112,8 @@ class Excitation:
             t += 0.5 * dt
             c[n] = math.sin(2.0 * PI * f0 * t)
         self.length = length
-        self.volt = v.astype(np.float32)
-        self.curr = c.astype(np.float32)
+        self.volt = v.astype(self.ft)
+        self.curr = c.astype(self.ft)
         self.nyquist = calc_nyquist_num(f0, dt)
 
     def GetLength(self) -> int:

@@ -106,6 +106,17 @@ class Structure:
                          eps_pole=pad(eps_lor_pole_freq), mue_plasma=pad(mue_plasma_freq),
                          mue_relax=pad(mue_relax_time), mue_pole=pad(mue_lor_pole_freq))
 
+    def AddVoxelMaterial(self, name, start, stop, epsilon, kappa=0.0, priority=0):
+        """Per-cell relative permittivity and conductivity on a box whose faces lie on mesh lines:
+        ``epsilon`` (and ``kappa``, scalar or array) hold one value per mesh cell of the box
+        (shape = cells per axis).  Used for design regions."""
+        eps = np.asarray(epsilon, np.float64)
+        kap = np.broadcast_to(np.asarray(kappa, np.float64), eps.shape).copy()
+        p = self._add(MATERIAL, name, epsilon=1.0, mue=1.0, kappa=0.0, sigma=0.0, voxel=True,
+                      eps_array=eps, kappa_array=kap)
+        p.AddBox(start, stop, priority)
+        return p
+
     def AddMetal(self, name):
         return self._add(METAL, name)
 
@@ -401,7 +412,8 @@ class Operator:
 
     def __init__(self, structure: Structure, grid: Grid, excitation: Excitation, bc=(0,) * 6,
                  pml_size=(8,) * 6, timestep=0.0, timestep_factor=1.0, over_sampling=4,
-                 background=(1.0, 1.0, 0.0, 0.0)):
+                 background=(1.0, 1.0, 0.0, 0.0), fdtd_float=np.float32):
+        self.ft = np.dtype(fdtd_float).type   # FDTD_FLOAT: float32 like the reference, float64 for FP64 runs
         self.csx = structure
         self.grid = grid
         self.exc = excitation
@@ -421,13 +433,48 @@ class Operator:
         self.dl = [_dual_line(l) for l in self.L]
         self._mat = _Painter(structure, MATERIAL)
         self._matmetal = _Painter(structure, MATERIAL | METAL)
+        self._bind_voxels()
 
     # ---- material lookup ------------------------------------------------------------------
     def _lookup(self, n, cn, cp, cpp, keys, painter=None):
         painter = painter or self._mat
         cx, cy, cz = _coords_xyz(n, cn, cp, cpp)
         m = painter.paint(cx, cy, cz)
-        return [painter.param(m, k, self.bg[k]) for k in keys]
+        out = [painter.param(m, k, self.bg[k]) for k in keys]
+        vkeys = [(keys.index(k), k + "_array" if k == "kappa" else "eps_array")
+                 for k in ("epsilon", "kappa") if k in keys]
+        if vkeys:
+            for prop in painter.props:
+                if not prop.params.get("voxel"):
+                    continue
+                pid = painter.prop_index[id(prop)]
+                mask = m == pid
+                if not mask.any():
+                    continue
+                cl = prop.params["cell_lines"]
+                idx = [np.clip(np.searchsorted(cl[a], c, side="right") - 1, 0, len(cl[a]) - 2)
+                       for a, c in enumerate((cx, cy, cz))]
+                for ki, arr in vkeys:
+                    vox = prop.params[arr][np.ix_(*idx)]
+                    out[ki] = np.where(mask, vox, out[ki])
+        return out
+
+    def _bind_voxels(self):
+        """Record the cell boundaries of every voxel material box on this mesh."""
+        for prop in self.csx.props:
+            if not prop.params.get("voxel"):
+                continue
+            lo, hi = prop.boxes[0][0], prop.boxes[0][1]
+            cl = []
+            for a in range(3):
+                L = self.L[a]
+                tol = 1e-9 * max(1.0, abs(L[-1] - L[0]))
+                cl.append(L[(L >= lo[a] - tol) & (L <= hi[a] + tol)])
+            shape = tuple(len(c) - 1 for c in cl)
+            if shape != prop.params["eps_array"].shape:
+                raise ValueError(f"voxel material {prop.name}: {prop.params['eps_array'].shape} values for "
+                                 f"{shape} mesh cells")
+            prop.params["cell_lines"] = cl
 
     # ---- effective material (FDTD/operator.cpp:1447-1564) ----------------------------------
     def eff_mat(self, n):
@@ -507,7 +554,7 @@ class Operator:
         at its interior positions."""
         g = Grid([self.L[a][lo[a]:hi[a]] for a in range(3)], unit=self.unit)
         sub = Operator.__new__(Operator)
-        sub.csx, sub.grid, sub.exc, sub.bg = self.csx, g, self.exc, self.bg
+        sub.csx, sub.grid, sub.exc, sub.bg, sub.ft = self.csx, g, self.exc, self.bg, self.ft
         sub.L, sub.unit = g.lines, self.unit
         sub.N = np.array([len(l) for l in g.lines], np.int64)
         sub.md = [_main_delta(l) for l in g.lines]
@@ -527,7 +574,7 @@ class Operator:
     def _ec_local(self):
         """EC_C/G/L/R (float32) on this operator's own mesh."""
         shape = tuple(int(v) for v in self.N)
-        out = [np.empty((3,) + shape, np.float32) for _ in range(4)]
+        out = [np.empty((3,) + shape, self.ft) for _ in range(4)]
         u = self.unit
         for n in range(3):
             a, p, pp = _axes(n)
@@ -545,10 +592,10 @@ class Operator:
 
     def calc_ec(self):
         shape = tuple(int(v) for v in self.N)
-        self.EC_C = np.empty((3,) + shape, np.float32)
-        self.EC_G = np.empty((3,) + shape, np.float32)
-        self.EC_L = np.empty((3,) + shape, np.float32)
-        self.EC_R = np.empty((3,) + shape, np.float32)
+        self.EC_C = np.empty((3,) + shape, self.ft)
+        self.EC_G = np.empty((3,) + shape, self.ft)
+        self.EC_L = np.empty((3,) + shape, self.ft)
+        self.EC_R = np.empty((3,) + shape, self.ft)
         dst = (self.EC_C, self.EC_G, self.EC_L, self.EC_R)
 
         def work(x0, x1):
@@ -637,7 +684,7 @@ class Operator:
             vi = np.where(okc, (dT / Cs) / (1.0 + dT * G / 2.0 / Cs), 0.0)
             ii = np.where(okl, (1.0 - dT * R / 2.0 / Ls) / (1.0 + dT * R / 2.0 / Ls), 0.0)
             iv = np.where(okl, (dT / Ls) / (1.0 + dT * R / 2.0 / Ls), 0.0)
-        return vv.astype(np.float32), vi.astype(np.float32), ii.astype(np.float32), iv.astype(np.float32)
+        return vv.astype(self.ft), vi.astype(self.ft), ii.astype(self.ft), iv.astype(self.ft)
 
     # ---- snapping (FDTD/operator.cpp:252-372) ----------------------------------------------
     def snap_line(self, ny, coord, dual=False):
@@ -701,11 +748,12 @@ class Operator:
             TS = math.ceil(self.exc.period / dT)
             dT = self.exc.period / TS
         self.dT = dT
+        self.exc.ft = self.ft
         self.exc.Reset(dT)
         self.exc.buildExcitationSignal(num_ts)
 
         shape = (3,) + tuple(int(v) for v in self.N)
-        self.vv, self.vi, self.ii, self.iv = (np.empty(shape, np.float32) for _ in range(4))
+        self.vv, self.vi, self.ii, self.iv = (np.empty(shape, self.ft) for _ in range(4))
 
         def coef(x0, x1):
             for n in range(3):
@@ -905,7 +953,7 @@ class Operator:
             idx = np.zeros((3, K), np.uint32)
             for i, r in enumerate(rec):
                 idx[:, i] = (r[2], r[1], r[0])
-            return (idx, np.array([r[3] for r in rec], np.uint16), np.array([r[4] for r in rec], np.float32),
+            return (idx, np.array([r[3] for r in rec], np.uint16), np.array([r[4] for r in rec], self.ft),
                     np.array([r[5] for r in rec], np.uint32))
         vi_, vd, va, vdl = pack(vrec)
         ci_, cd, ca, cdl = pack(crec)
@@ -939,10 +987,10 @@ class Operator:
             eps = self._mat.param(m2, "epsilon", self.bg["epsilon"])
             mue = self._mat.param(m2, "mue", self.bg["mue"])
             c0t = C0 * self.dT / np.sqrt(eps * mue)
-            coeff = ((c0t - delta) / (c0t + delta)).astype(np.float32)
+            coeff = ((c0t - delta) / (c0t + delta)).astype(self.ft)
             bg = C0 / math.sqrt(self.bg["epsilon"] * self.bg["mue"]) * self.dT
-            coeff_bg = np.float32((bg - delta) / (bg + delta))
-            coeff = np.where(m2 >= 0, coeff, coeff_bg).astype(np.float32)
+            coeff_bg = self.ft((bg - delta) / (bg + delta))
+            coeff = np.where(m2 >= 0, coeff, coeff_bg).astype(self.ft)
             # excitation inside the wall delays the ABC (engine_ext_mur_abc.cpp:44-60)
             max_delay = -1
             for i in range(exc.volt_dir.size):
@@ -1053,7 +1101,7 @@ class Operator:
             sl = tuple(slice(int(start[k]), int(start[k] + nl[k])) for k in range(3))
             pos_axes = [np.arange(start[k], start[k] + nl[k]) for k in range(3)]
             shape = tuple(int(v) for v in nl)
-            arrs = {k: np.zeros((3,) + shape, np.float32) for k in ("vv", "vvfo", "vvfn", "ii", "iifo", "iifn")}
+            arrs = {k: np.zeros((3,) + shape, self.ft) for k in ("vv", "vvfo", "vvfn", "ii", "iifo", "iifn")}
             for n in range(3):
                 a, p, pp = _axes(n)
                 kv1, ki1 = self._grading_kappa(n, pos_axes)
@@ -1079,11 +1127,11 @@ class Operator:
                 act_v = (ksum_v != 0) & (eff_kap < 1e3)
                 not_pec = (op_vv + op_vi) != 0
                 mod = act_v & not_pec
-                new_vv = ((2 * EPS0 - kvp * dT) / (2 * EPS0 + kvp * dT)).astype(np.float32)
-                new_vi = ((2 * EPS0 * dT) / (2 * EPS0 + kvp * dT) * De / (Ap * App)).astype(np.float32)
-                e_vv = ((2 * EPS0 - kvpp * dT) / (2 * EPS0 + kvpp * dT)).astype(np.float32)
-                e_vvfn = ((2 * EPS0 + kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(np.float32)
-                e_vvfo = ((2 * EPS0 - kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(np.float32)
+                new_vv = ((2 * EPS0 - kvp * dT) / (2 * EPS0 + kvp * dT)).astype(self.ft)
+                new_vi = ((2 * EPS0 * dT) / (2 * EPS0 + kvp * dT) * De / (Ap * App)).astype(self.ft)
+                e_vv = ((2 * EPS0 - kvpp * dT) / (2 * EPS0 + kvpp * dT)).astype(self.ft)
+                e_vvfn = ((2 * EPS0 + kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(self.ft)
+                e_vvfo = ((2 * EPS0 - kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(self.ft)
                 arrs["vv"][n] = np.where(mod, e_vv, np.where(act_v, 0, op_vv))
                 arrs["vvfn"][n] = np.where(mod, e_vvfn, np.where(act_v, 0, 1))
                 arrs["vvfo"][n] = np.where(mod, e_vvfo, 0)
@@ -1093,11 +1141,11 @@ class Operator:
                 act_i = ksum_i != 0
                 not_pmc = (op_ii + op_iv) != 0
                 mod = act_i & not_pmc
-                new_ii = ((2 * EPS0 - kip * dT) / (2 * EPS0 + kip * dT)).astype(np.float32)
-                new_iv = ((2 * EPS0 * dT) / (2 * EPS0 + kip * dT) * Dh / (Bp * Bpp)).astype(np.float32)
-                e_ii = ((2 * EPS0 - kipp * dT) / (2 * EPS0 + kipp * dT)).astype(np.float32)
-                e_iifn = ((2 * EPS0 + kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(np.float32)
-                e_iifo = ((2 * EPS0 - kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(np.float32)
+                new_ii = ((2 * EPS0 - kip * dT) / (2 * EPS0 + kip * dT)).astype(self.ft)
+                new_iv = ((2 * EPS0 * dT) / (2 * EPS0 + kip * dT) * Dh / (Bp * Bpp)).astype(self.ft)
+                e_ii = ((2 * EPS0 - kipp * dT) / (2 * EPS0 + kipp * dT)).astype(self.ft)
+                e_iifn = ((2 * EPS0 + kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(self.ft)
+                e_iifo = ((2 * EPS0 - kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(self.ft)
                 arrs["ii"][n] = np.where(mod, e_ii, np.where(act_i, 0, op_ii))
                 arrs["iifn"][n] = np.where(mod, e_iifn, np.where(act_i, 0, 1))
                 arrs["iifo"][n] = np.where(mod, e_iifo, 0)
@@ -1186,7 +1234,7 @@ class Operator:
                 pos = np.array(np.nonzero(on_mask), dtype=np.int64)
                 sel = tuple(pos)
                 M = pos.shape[1]
-                tabs = {k: np.zeros((3, M), np.float32) for k in ("v_int", "v_ext", "v_lor", "i_int", "i_ext", "i_lor")}
+                tabs = {k: np.zeros((3, M), self.ft) for k in ("v_int", "v_ext", "v_lor", "i_int", "i_ext", "i_lor")}
                 with np.errstate(divide="ignore", invalid="ignore"):
                     for n in range(3):
                         LD, RD, CL, CD, GD, LL = (t[sel] for t in per_n[n])
