@@ -3,22 +3,27 @@
 //
 // One forward timestep (FDTD/engine.cpp:267-286 with the UPML hooks of
 // FDTD/extensions/engine_ext_upml.cpp:52-229 and the additive excitation of
-// FDTD/extensions/engine_ext_excitation.cpp:33-94) is affine in the state (V, I, UPML fluxes):
-//     V' = vv*V + vi*K_V I   (UPML pre/post around it)      I' = ii*I + iv*K_I V'
-// where K_V / K_I are the curl stencils of k_update_v / k_update_i.  Its transpose, applied to
-// the adjoint state (lV, lI, UPML adjoint fluxes), runs in reverse order:
-//   k_adj_iwi : lI += K_V^T w (finishes the previous reverse step), then I post^T, update^T
-//               (u = iv * lambda kept for the V side), pre^T
-//   k_adj_v   : lV += K_I^T u, then V post^T, update^T (w = vi * lambda kept, gradient sums
-//               dJ/dvv += lambda V^n, dJ/dvi += lambda K_V I^n in the design box), pre^T
-//   k_adj_inject : lambda += dJ/d(probe sample at numTS = n) on the probe edges
+// FDTD/extensions/engine_ext_excitation.cpp:33-94) is affine in the state:
+//     V' = vv*V + vi*K_V I          I' = ii*I + iv*K_I V'
+// with K_V / K_I the curl stencils of k_update_v / k_update_i (UPML cells add pre/post hooks).
+// For the adjoint (lambda_V, lambda_I) of one step, with a = lambda_I' and b = lambda_V' + K_I^T(iv a):
+//     lambda_I = ii*a + K_V^T(vi*b)      lambda_V = vv*b
+// In the scaled variables U = iv*a and W = vi*b the reverse step is again a pair of
+// forward-like updates with the transposed curls:
+//     U <- ii*U + iv*(K_V^T W + s_I)     W <- vv*W + vi*(K_I^T U + s_V)
+// where s_I, s_V are dJ/d(probe sample) on the probe edges (a sample at numTS = n+1 enters the
+// reverse step of forward step n).  Inside UPML regions the unscaled adjoints of V, I and of the
+// two fluxes are kept in region-local arrays and the transposed pre/post hooks are applied.
+// Gradients (design box, outside every UPML region): dJ/dvv += b V^n, dJ/dvi += b K_V I^n, with
+// b = W/vi, accumulated in double.
+//
 // The curl transposes are gathers (no atomics), derived from the forward stencils including the
 // reference's "same cell" read at index 0 (a shift of 0 makes the two terms cancel).
 //
-// Memory is bounded by checkpoints: the forward run stores the full state every K steps; the
-// reverse sweep restores one K-step segment at a time, recomputes it (field updates and
-// excitation only), keeps the design box's V^n and K_V I^n per step, and then walks the segment
-// backwards.  Gradient sums are accumulated in double.
+// The factors V^n and K_V I^n of the design box come either from checkpoints plus
+// recomputation (checkpoint_every = K > 0: the full state every K steps, each K-step segment
+// recomputed once in the reverse sweep) or from a record of every step kept during the forward
+// run (checkpoint_every = 0: 24 bytes per design edge triple and step, no recomputation).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,186 +36,251 @@ using namespace oems;
 
 namespace {
 
+struct InjList {
+    unsigned count;
+    unsigned long long lo, hi;        // range of the cell offsets (component removed)
+    const unsigned long long* cell;   // [count] cell offset
+    const int* comp;                  // [count] component
+    const int* row;                   // [count] source row (objective probe)
+    const double* coef;               // [count] weight * sign
+};
+
 struct AdjDev {
     GridDev g;
-    float* lV;            // [3][S] adjoint of V
-    float* lI;            // [3][S] adjoint of I
-    float* wv;            // [3][S] vi * lambda (V update^T), read by the next k_adj_iwi
-    float* ui;            // [3][S] iv * lambda (I update^T), 0 where I is not updated
-    float* lpsi[OEMS_MAX_UPML];
-    float* lphi[OEMS_MAX_UPML];
+    float* U;             // [3][S] iv * lambda_I (0 where I is not updated)
+    float* W;             // [3][S] vi * (lambda_V + K_I^T U)
+    float* lV[OEMS_MAX_UPML];      // [3][n] lambda_V in UPML cells
+    float* lI[OEMS_MAX_UPML];      // [3][n] lambda_I in UPML cells
+    float* lpsi[OEMS_MAX_UPML];    // [3][n] adjoint of the voltage flux
+    float* lphi[OEMS_MAX_UPML];    // [3][n] adjoint of the current flux
     unsigned b0[3], bn[3];
     unsigned B;
     const float* fv;      // [3][B] V^n in the design box
     const float* fc;      // [3][B] K_V I^n in the design box
     double* gvv;          // [3][B]
     double* gvi;          // [3][B]
+    const double* src;    // [rows][stride]
+    unsigned stride;
+    unsigned n;           // forward step being reversed; sources of sample n+1 enter
+    InjList injV, injI;
 };
 
-__device__ __forceinline__ void coef_v(const GridDev& g, unsigned long long o, int m, float& vv, float& vi)
+__device__ __forceinline__ void coef_v(const GridDev& g, unsigned long long o, float vv[3], float vi[3])
 {
     if (g.idx) {
         const unsigned c = __ldg(g.idx + o);
-        const float* t = reinterpret_cast<const float*>(g.tabV + 2 * c);
-        vv = __ldg(t + m);
-        vi = __ldg(t + 3 + m);
+        const float4 a = __ldg(g.tabV + 2 * c), b = __ldg(g.tabV + 2 * c + 1);
+        vv[0] = a.x; vv[1] = a.y; vv[2] = a.z; vi[0] = a.w; vi[1] = b.x; vi[2] = b.y;
     } else {
-        vv = __ldg(g.vv + m * g.S + o);
-        vi = __ldg(g.vi + m * g.S + o);
+#pragma unroll
+        for (int m = 0; m < 3; ++m) { vv[m] = __ldg(g.vv + m * g.S + o); vi[m] = __ldg(g.vi + m * g.S + o); }
     }
 }
 
-__device__ __forceinline__ void coef_i(const GridDev& g, unsigned long long o, int m, float& ii, float& iv)
+__device__ __forceinline__ void coef_i(const GridDev& g, unsigned long long o, float ii[3], float iv[3])
 {
     if (g.idx) {
         const unsigned c = __ldg(g.idx + o);
-        const float* t = reinterpret_cast<const float*>(g.tabI + 2 * c);
-        ii = __ldg(t + m);
-        iv = __ldg(t + 3 + m);
+        const float4 a = __ldg(g.tabI + 2 * c), b = __ldg(g.tabI + 2 * c + 1);
+        ii[0] = a.x; ii[1] = a.y; ii[2] = a.z; iv[0] = a.w; iv[1] = b.x; iv[2] = b.y;
     } else {
-        ii = __ldg(g.ii + m * g.S + o);
-        iv = __ldg(g.iv + m * g.S + o);
+#pragma unroll
+        for (int m = 0; m < 3; ++m) { ii[m] = __ldg(g.ii + m * g.S + o); iv[m] = __ldg(g.iv + m * g.S + o); }
     }
 }
 
-// lI += K_V^T w, then the transposed I sub-step.
-__global__ void __launch_bounds__(256) k_adj_iwi(AdjDev a)
+// probe sources of sample n+1 at cell o (few entries; only threads inside the probes' range look)
+__device__ __forceinline__ void add_sources(const AdjDev& a, const InjList& L, unsigned long long o, float s[3])
+{
+    if (L.count == 0 || o < L.lo || o > L.hi) return;
+    for (unsigned k = 0; k < L.count; ++k)
+        if (L.cell[k] == o) {
+            const double v = a.src[(unsigned long long)L.row[k] * a.stride + a.n + 1] * L.coef[k];
+            s[L.comp[k]] = fadd(s[L.comp[k]], (float)v);
+        }
+}
+
+// U <- ii*U + iv*(K_V^T W + s_I) for one cell with x < Nx-1, y < Ny-1, z < Nz-1 (I is never
+// updated elsewhere, so U stays 0 there).  UPML cells: transposed post/update/pre on the local
+// adjoints.  rk/lk: the cell's region and local offset when known (rk = -2: look up).
+__device__ __forceinline__ void adj_u_cell(const AdjDev& a, unsigned x, unsigned y, unsigned z, int rk, unsigned lk)
 {
     const GridDev& g = a.g;
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned y = t / g.Pz, z = t - y * g.Pz;
-    if (y >= g.Ny || z >= g.Nz) return;
     const unsigned long long S = g.S;
     const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
     const unsigned long long sx = (unsigned long long)g.Ny * g.Pz, sy = g.Pz;
-    const float* w = a.wv;
-    auto W = [&](int m, unsigned long long off, bool ok) -> float { return ok ? __ldg(w + m * S + off) : 0.f; };
-    const bool hx = x + 1 < g.Nx, hy = y + 1 < g.Ny, hz = z + 1 < g.Nz;
-    // d/dI of sum_o w(o) . K_V I (o): the forward's index-0 self reads cancel the direct term
-    const float d[3] = {
-        fadd(fsub(fsub(W(1, o, z > 0), W(1, o + 1, hz)), W(2, o, y > 0)), W(2, o + sy, hy)),
-        fadd(fsub(fsub(W(2, o, x > 0), W(2, o + sx, hx)), W(0, o, z > 0)), W(0, o + 1, hz)),
-        fadd(fsub(fsub(W(0, o, y > 0), W(0, o + sy, hy)), W(1, o, x > 0)), W(1, o + sx, hx))};
-    if (!(hx && hy && hz)) {            // I is never updated here: identity
+    const float* __restrict__ W = a.W;
+    // every independent load first: W at the cell and its +x/+y/+z neighbours, the coefficients,
+    // the cell's own adjoint state
+    const float w0 = __ldg(W + o), w1 = __ldg(W + S + o), w2 = __ldg(W + 2 * S + o);
+    const float w1z = __ldg(W + S + o + 1), w2y = __ldg(W + 2 * S + o + sy), w2x = __ldg(W + 2 * S + o + sx);
+    const float w0z = __ldg(W + o + 1), w0y = __ldg(W + o + sy), w1x = __ldg(W + S + o + sx);
+    float ii[3], iv[3];
+    coef_i(g, o, ii, iv);
+    unsigned loc = lk;
+    const int r = rk == -2 ? upml_find(g, x, y, z, loc) : rk;
+    float st[3];
+    if (r < 0) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) st[m] = a.U[m * S + o];
+    } else {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) st[m] = a.lI[r][m * g.upml[r].n + loc];
+    }
+    // d/dI of sum_o W(o) . K_V I (o); the forward's index-0 self reads cancel the direct term
+    float d[3] = {
+        fadd(fsub(fsub(z > 0 ? w1 : 0.f, w1z), y > 0 ? w2 : 0.f), w2y),
+        fadd(fsub(fsub(x > 0 ? w2 : 0.f, w2x), z > 0 ? w0 : 0.f), w0z),
+        fadd(fsub(fsub(y > 0 ? w0 : 0.f, w0y), x > 0 ? w1 : 0.f), w1x)};
+    add_sources(a, a.injI, o, d);
+    if (r < 0) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) a.U[m * S + o] = fadd(fmul(ii[m], st[m]), fmul(iv[m], d[m]));
+        return;
+    }
+    float pc[9];
+    upml_coef<true>(g.upml[r], loc, pc);
+    const unsigned n = g.upml[r].n;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const unsigned k = m * n + loc;
+        const float lam = fadd(st[m], d[m]);                    // adjoint of I after the step
+        const float lin = fadd(fmul(pc[6 + m], lam), a.lphi[r][k]);   // post^T: I = h + iifn*flux
+        a.U[m * S + o] = fmul(iv[m], lin);
+        a.lphi[r][k] = fsub(fmul(ii[m], lin), fmul(pc[3 + m], lam));  // pre^T: f = ii*I - iifo*flux
+        a.lI[r][k] = fmul(pc[m], lam);
+    }
+}
+
+// W <- vv*W + vi*(K_I^T U + s_V) for one cell, with the design-box gradient sums
+__device__ __forceinline__ void adj_w_cell(const AdjDev& a, unsigned x, unsigned y, unsigned z, int rk, unsigned lk)
+{
+    const GridDev& g = a.g;
+    const unsigned long long S = g.S;
+    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
+    // -x/-y/-z neighbours; at index 0 the cell itself is read and the term dropped below
+    const unsigned long long sx = x ? (unsigned long long)g.Ny * g.Pz : 0ull;
+    const unsigned long long sy = y ? (unsigned long long)g.Pz : 0ull;
+    const unsigned long long sz = z ? 1ull : 0ull;
+    const float* __restrict__ U = a.U;
+    const float u0 = __ldg(U + o), u1 = __ldg(U + S + o), u2 = __ldg(U + 2 * S + o);
+    const float u1z = __ldg(U + S + o - sz), u2y = __ldg(U + 2 * S + o - sy), u2x = __ldg(U + 2 * S + o - sx);
+    const float u0z = __ldg(U + o - sz), u0y = __ldg(U + o - sy), u1x = __ldg(U + S + o - sx);
+    float vv[3], vi[3];
+    coef_v(g, o, vv, vi);
+    unsigned loc = lk;
+    const int r = rk == -2 ? upml_find(g, x, y, z, loc) : rk;
+    float st[3];
+    if (r < 0) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) st[m] = a.W[m * S + o];
+    } else {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) st[m] = a.lV[r][m * g.upml[r].n + loc];
+    }
+    float gs[3] = {
+        fadd(fsub(fsub(u1, z ? u1z : 0.f), u2), y ? u2y : 0.f),
+        fsub(fadd(fsub(u2, x ? u2x : 0.f), z ? u0z : 0.f), u0),
+        fadd(fsub(fsub(u0, y ? u0y : 0.f), u1), x ? u1x : 0.f)};
+    add_sources(a, a.injV, o, gs);
+    if (r < 0) {
+        float wn[3];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-            a.lI[m * S + o] = fadd(a.lI[m * S + o], d[m]);
-            a.ui[m * S + o] = 0.f;
+            wn[m] = fadd(fmul(vv[m], st[m]), fmul(vi[m], gs[m]));
+            a.W[m * S + o] = wn[m];
+        }
+        const unsigned bx = x - a.b0[0], by = y - a.b0[1], bz = z - a.b0[2];
+        if (bx < a.bn[0] && by < a.bn[1] && bz < a.bn[2]) {
+            const unsigned kb = (bx * a.bn[1] + by) * a.bn[2] + bz;
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                if (vi[m] == 0.f) continue;                     // PEC edge: no dependence
+                const double b = (double)wn[m] / (double)vi[m];
+                const unsigned kk = m * a.B + kb;
+                a.gvv[kk] += b * (double)__ldg(a.fv + kk);
+                a.gvi[kk] += b * (double)__ldg(a.fc + kk);
+            }
         }
         return;
     }
-    unsigned loc = 0;
-    const int r = upml_find(g, x, y, z, loc);
+    float pc[9];
+    upml_coef<false>(g.upml[r], loc, pc);
+    const unsigned n = g.upml[r].n;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-        const unsigned long long q = m * S + o;
-        float l = fadd(a.lI[q], d[m]);                   // lambda of I after the step
-        float lpost = 0.f;
-        if (r >= 0) {                                    // post^T: I = h + iifn*flux, flux = I
-            const UpmlDev& u = g.upml[r];
-            const unsigned k = m * u.n + loc;
-            lpost = l;
-            l = fadd(fmul(__ldg(u.iifn + k), l), a.lphi[r][k]);
-        }
-        float ii, iv;
-        coef_i(g, o, m, ii, iv);
-        a.ui[q] = fmul(iv, l);
-        l = fmul(ii, l);
-        if (r >= 0) {                                    // pre^T: f = ii*I - iifo*flux; I = flux; flux = f
-            const UpmlDev& u = g.upml[r];
-            const unsigned k = m * u.n + loc;
-            a.lphi[r][k] = fsub(l, fmul(__ldg(u.iifo + k), lpost));
-            l = fmul(__ldg(u.ii + k), lpost);
-        }
-        a.lI[q] = l;
+        const unsigned k = m * n + loc;
+        const float b = fadd(st[m], gs[m]);                     // adjoint of V after the step
+        const float lvn = fadd(fmul(pc[6 + m], b), a.lpsi[r][k]);      // post^T: V = h + vvfn*flux
+        a.W[m * S + o] = fmul(vi[m], lvn);
+        a.lpsi[r][k] = fsub(fmul(vv[m], lvn), fmul(pc[3 + m], b));     // pre^T: f = vv*V - vvfo*flux
+        a.lV[r][k] = fmul(pc[m], b);
     }
 }
 
-// lV += K_I^T u, then the transposed V sub-step with the design-box gradient sums.
-__global__ void __launch_bounds__(256) k_adj_v(AdjDev a)
+// one thread per cell of an x-plane (blockIdx.y = x), for engines without UPML
+__global__ void __launch_bounds__(256) k_adj_u(AdjDev a)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned y = t / a.g.Pz, z = t - y * a.g.Pz;
+    if (y + 1 >= a.g.Ny || z + 1 >= a.g.Nz) return;
+    adj_u_cell(a, blockIdx.y, y, z, -2, 0);
+}
+
+__global__ void __launch_bounds__(256) k_adj_w(AdjDev a)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned y = t / a.g.Pz, z = t - y * a.g.Pz;
+    if (y >= a.g.Ny || z >= a.g.Nz) return;
+    adj_w_cell(a, blockIdx.y, y, z, -2, 0);
+}
+
+// the engine's UPML work split (k_update_split): interior blocks, then the region blocks
+template <bool CURR>
+__global__ void __launch_bounds__(256) k_adj_split(AdjDev a, SplitDev sp)
 {
     const GridDev& g = a.g;
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned y = t / g.Pz, z = t - y * g.Pz;
-    if (y >= g.Ny || z >= g.Nz) return;
-    const unsigned long long S = g.S;
-    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
-    const unsigned long long sx = (unsigned long long)g.Ny * g.Pz, sy = g.Pz;
-    const float* u = a.ui;
-    auto U = [&](int m, unsigned long long off, bool ok) -> float { return ok ? __ldg(u + m * S + off) : 0.f; };
-    const float gs[3] = {
-        fadd(fsub(fsub(U(1, o, true), U(1, o - 1, z > 0)), U(2, o, true)), U(2, o - sy, y > 0)),
-        fsub(fadd(fsub(U(2, o, true), U(2, o - sx, x > 0)), U(0, o - 1, z > 0)), U(0, o, true)),
-        fadd(fsub(fsub(U(0, o, true), U(0, o - sy, y > 0)), U(1, o, true)), U(1, o - sx, x > 0))};
-    unsigned loc = 0;
-    const int r = upml_find(g, x, y, z, loc);
-    int kb = -1;
-    {
-        const unsigned bx = x - a.b0[0], by = y - a.b0[1], bz = z - a.b0[2];
-        if (bx < a.bn[0] && by < a.bn[1] && bz < a.bn[2]) kb = (int)((bx * a.bn[1] + by) * a.bn[2] + bz);
+    unsigned b = blockIdx.x;
+    if (b < sp.main_blocks) {
+        unsigned t = b * 256u + threadIdx.x;
+        if (t >= sp.main_cells) return;
+        const unsigned z = sp.lo[2] + t % sp.n[2];
+        t /= sp.n[2];
+        const unsigned y = sp.lo[1] + t % sp.n[1];
+        const unsigned x = sp.lo[0] + t / sp.n[1];
+        int r = -1;
+        unsigned loc = 0;
+        if (sp.full) r = upml_find(g, x, y, z, loc);
+        if (r >= 0) return;
+        if (CURR) adj_u_cell(a, x, y, z, -1, 0);
+        else adj_w_cell(a, x, y, z, -1, 0);
+        return;
     }
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-        const unsigned long long q = m * S + o;
-        float l = fadd(a.lV[q], gs[m]);                 // lambda of V after the step
-        float lpost = 0.f;
-        if (r >= 0) {
-            const UpmlDev& up = g.upml[r];
-            const unsigned k = m * up.n + loc;
-            lpost = l;
-            l = fadd(fmul(__ldg(up.vvfn + k), l), a.lpsi[r][k]);
-        }
-        float vv, vi;
-        coef_v(g, o, m, vv, vi);
-        a.wv[q] = fmul(vi, l);
-        if (kb >= 0) {                                   // the design box lies outside every UPML region
-            const unsigned kk = m * a.B + kb;
-            a.gvv[kk] += (double)l * (double)__ldg(a.fv + kk);
-            a.gvi[kk] += (double)l * (double)__ldg(a.fc + kk);
-        }
-        l = fmul(vv, l);
-        if (r >= 0) {
-            const UpmlDev& up = g.upml[r];
-            const unsigned k = m * up.n + loc;
-            a.lpsi[r][k] = fsub(l, fmul(__ldg(up.vvfo + k), lpost));
-            l = fmul(__ldg(up.vv + k), lpost);
-        }
-        a.lV[q] = l;
+    b -= sp.main_blocks;
+    int r = 0;
+    while (r + 1 < (int)sp.nreg && b >= sp.first_block[r + 1]) ++r;
+    const UpmlDev& u = g.upml[r];
+    const unsigned loc = (b - sp.first_block[r]) * 256u + threadIdx.x;
+    if (loc >= u.n) return;
+    const unsigned lz = loc % u.nl[2], rest = loc / u.nl[2];
+    const unsigned x = u.start[0] + rest / u.nl[1], y = u.start[1] + rest % u.nl[1], z = u.start[2] + lz;
+    if (CURR) {
+        if (x + 1 >= g.Nx || y + 1 >= g.Ny || z + 1 >= g.Nz) return;
+        adj_u_cell(a, x, y, z, r, loc);
+    } else {
+        adj_w_cell(a, x, y, z, r, loc);
     }
 }
 
-struct InjDev {
-    int nprobe;
-    const ProbeDev* probes;    // the engine's device probe array
-    const int* ids;            // objective probes
-    const double* src;         // [nprobe][stride]
-    unsigned stride;
-    unsigned n;
-    float* lV;
-    float* lI;
-};
-
-// dJ/d(sample) * weight * sign into the probe edges; one thread, since probes may share edges
-__global__ void k_adj_inject(InjDev d)
-{
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int k = 0; k < d.nprobe; ++k) {
-        const ProbeDev& p = d.probes[d.ids[k]];
-        const double s = d.src[(unsigned long long)k * d.stride + d.n];
-        if (s == 0.0) continue;
-        float* L = p.type == 0 ? d.lV : d.lI;
-        for (unsigned j = 0; j < p.nterm; ++j)
-            L[p.term[j]] = fadd(L[p.term[j]], (float)(s * p.weight * (double)p.sign[j]));
-    }
-}
-
-// V^n and K_V I^n (the arithmetic of update_v_cell) in the design box
-__global__ void k_adj_factors(AdjDev a, float* fv, float* fc)
+// V^n and K_V I^n (the arithmetic of update_v_cell) in the design box, into slot
+// (*counter % modulo) of `base` (each slot [2][3][B]: V, then K_V I)
+__global__ void k_adj_factors(AdjDev a, float* base, const unsigned* counter, unsigned modulo)
 {
     const unsigned kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb >= a.B) return;
+    const unsigned slot = *counter % modulo;
+    float* fv = base + (size_t)slot * 6 * a.B;
+    float* fc = fv + 3 * a.B;
     const GridDev& g = a.g;
     const unsigned bz = kb % a.bn[2], by = (kb / a.bn[2]) % a.bn[1], bx = kb / (a.bn[2] * a.bn[1]);
     const unsigned x = a.b0[0] + bx, y = a.b0[1] + by, z = a.b0[2] + bz;
@@ -237,13 +307,13 @@ __global__ void k_inc(unsigned* c)
 }  // namespace
 
 struct oems_adjoint_state {
-    unsigned K = 256;
+    unsigned K = 256;                                 // 0: record mode
     unsigned steps = 0;
     std::vector<std::pair<void*, size_t>> regions;   // state: V, I, UPML fluxes
-    std::vector<char*> ckpt;                          // one per segment start + the end state
+    std::vector<char*> ckpt;                          // checkpoints: segment starts + the end state
     AdjDev dev{};
-    float* seg_fv = nullptr;
-    float* seg_fc = nullptr;
+    float* fac = nullptr;                             // factor slots [K or steps][2][3][B]
+    size_t fac_slots = 0;
     unsigned* rec_numTS = nullptr;
     std::vector<void*> allocs;
     size_t state_bytes = 0;
@@ -288,20 +358,104 @@ int copy_state(oems_cuda_engine* e, oems_adjoint_state* s, char* ck, bool save)
 // one forward step without processing, the step counter being rec_numTS; returns the launches
 unsigned recompute_step(oems_cuda_engine* e, oems_adjoint_state* s)
 {
-    const GridDev& g = e->grid;
-    const unsigned plane = e->N[1] * e->Pz;
-    const dim3 gv((plane + 255) / 256, e->N[0]), gi((plane + 255) / 256, e->N[0] - 1);
-    const bool up = !e->upml.empty();
     cudaStream_t st = e->stream;
     unsigned L = 3;
-    if (e->compressed) { if (up) k_update_v<true, true><<<gv, 256, 0, st>>>(g); else k_update_v<true, false><<<gv, 256, 0, st>>>(g); }
-    else { if (up) k_update_v<false, true><<<gv, 256, 0, st>>>(g); else k_update_v<false, false><<<gv, 256, 0, st>>>(g); }
+    launch_update(e, false, st);
     if (e->excV.count) { k_excitation<<<(e->excV.count + 127) / 128, 128, 0, st>>>(e->dV, e->excV, s->rec_numTS); ++L; }
-    if (e->compressed) { if (up) k_update_i<true, true><<<gi, 256, 0, st>>>(g); else k_update_i<true, false><<<gi, 256, 0, st>>>(g); }
-    else { if (up) k_update_i<false, true><<<gi, 256, 0, st>>>(g); else k_update_i<false, false><<<gi, 256, 0, st>>>(g); }
+    launch_update(e, true, st);
     if (e->excI.count) { k_excitation<<<(e->excI.count + 127) / 128, 128, 0, st>>>(e->dI, e->excI, s->rec_numTS); ++L; }
     k_inc<<<1, 32, 0, st>>>(s->rec_numTS);
     return L;
+}
+
+// forward run that records the factors of every step (record mode): graphs of 1 and 16 steps,
+// each step preceded by the factor kernel writing slot numTS
+int record_forward(oems_cuda_engine* e, oems_adjoint_state* s, unsigned steps)
+{
+    const unsigned KG = 16;
+    cudaGraphExec_t gx[2] = {nullptr, nullptr};
+    const unsigned counts[2] = {1, KG};
+    const unsigned fb = (s->dev.B + 255) / 256;
+    for (int k = 0; k < 2; ++k) {
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return afail(e, OEMS_ERR_CUDA, "record capture");
+        int rc = OEMS_OK;
+        for (unsigned j = 0; j < counts[k] && rc == OEMS_OK; ++j) {
+            k_adj_factors<<<fb, 256, 0, e->stream>>>(s->dev, s->fac, e->d_numTS, 0xFFFFFFFFu);
+            unsigned L = 0;
+            rc = enqueue_step(e, &L);
+        }
+        const cudaError_t c = cudaStreamEndCapture(e->stream, &graph);
+        if (rc != OEMS_OK || c != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            for (auto& x : gx) if (x) cudaGraphExecDestroy(x);
+            return rc != OEMS_OK ? rc : afail(e, OEMS_ERR_CUDA, "record capture");
+        }
+        const cudaError_t ci = cudaGraphInstantiate(&gx[k], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ci != cudaSuccess) {
+            for (auto& x : gx) if (x) cudaGraphExecDestroy(x);
+            return afail(e, OEMS_ERR_CUDA, "record graph instantiate");
+        }
+    }
+    int rc = OEMS_OK;
+    unsigned done = 0;
+    while (done < steps && rc == OEMS_OK) {
+        const int k = steps - done >= KG ? 1 : 0;
+        if (cudaGraphLaunch(gx[k], e->stream) != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "record graph launch");
+        done += counts[k];
+    }
+    e->host_numTS += done;
+    for (auto& x : gx) cudaGraphExecDestroy(x);
+    return rc;
+}
+
+// the engine's probe terms of the objective probes of one type, for the reverse kernels; the
+// device arrays are appended to `tmp` (freed by the caller)
+int build_injection(oems_cuda_engine* e, unsigned nprobe, const int* ids, int type, InjList& L,
+                    std::vector<void*>& tmp)
+{
+    std::vector<unsigned long long> cell;
+    std::vector<int> comp, row;
+    std::vector<double> coef;
+    for (unsigned k = 0; k < nprobe; ++k) {
+        const ProbeDev& p = e->probe_dev[ids[k]];
+        if (p.type != type || p.nterm == 0) continue;
+        std::vector<unsigned long long> term(p.nterm);
+        std::vector<signed char> sign(p.nterm);
+        if (cudaMemcpy(term.data(), p.term, p.nterm * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(sign.data(), p.sign, p.nterm, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return afail(e, OEMS_ERR_CUDA, "probe term copy");
+        for (unsigned j = 0; j < p.nterm; ++j) {
+            comp.push_back((int)(term[j] / e->S));
+            cell.push_back(term[j] % e->S);
+            row.push_back((int)k);
+            coef.push_back(p.weight * (double)sign[j]);
+        }
+    }
+    L = InjList{};
+    L.count = (unsigned)cell.size();
+    if (!L.count) return OEMS_OK;
+    L.lo = *std::min_element(cell.begin(), cell.end());
+    L.hi = *std::max_element(cell.begin(), cell.end());
+    void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+    const size_t bytes[4] = {cell.size() * sizeof(unsigned long long), comp.size() * sizeof(int),
+                             row.size() * sizeof(int), coef.size() * sizeof(double)};
+    for (int k = 0; k < 4; ++k) {
+        if (cudaMalloc(&p[k], bytes[k]) != cudaSuccess) return afail(e, OEMS_ERR_NOMEM, "adjoint source allocation");
+        tmp.push_back(p[k]);
+    }
+    auto* dc = static_cast<unsigned long long*>(p[0]);
+    auto* dm = static_cast<int*>(p[1]);
+    auto* dr = static_cast<int*>(p[2]);
+    auto* dw = static_cast<double*>(p[3]);
+    cudaMemcpyAsync(dc, cell.data(), cell.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(dm, comp.data(), comp.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(dr, row.data(), row.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(dw, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+    L.cell = dc; L.comp = dm; L.row = dr; L.coef = dw;
+    return OEMS_OK;
 }
 
 }  // namespace
@@ -311,7 +465,7 @@ extern "C" {
 int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, const unsigned int box_start[3],
                             const unsigned int box_stop[3])
 {
-    if (!e || !box_start || !box_stop || checkpoint_every == 0) return OEMS_ERR_ARG;
+    if (!e || !box_start || !box_stop) return OEMS_ERR_ARG;
     if (!e->inited) return afail(e, OEMS_ERR_STATE, "engine not initialised");
     if (e->adj) return afail(e, OEMS_ERR_STATE, "adjoint already set up");
     if (!e->mur.empty() || !e->lor.empty())
@@ -338,13 +492,13 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     AdjDev& d = s->dev;
     d.g = e->grid;
     int rc;
-    if ((rc = aalloc(e, s, &d.lV, 3 * e->S))) return rc;
-    if ((rc = aalloc(e, s, &d.lI, 3 * e->S))) return rc;
-    if ((rc = aalloc(e, s, &d.wv, 3 * e->S))) return rc;
-    if ((rc = aalloc(e, s, &d.ui, 3 * e->S))) return rc;
+    if ((rc = aalloc(e, s, &d.U, 3 * e->S))) return rc;
+    if ((rc = aalloc(e, s, &d.W, 3 * e->S))) return rc;
     for (int r = 0; r < e->grid.nupml; ++r) {
-        if ((rc = aalloc(e, s, &d.lpsi[r], 3ull * e->grid.upml[r].n))) return rc;
-        if ((rc = aalloc(e, s, &d.lphi[r], 3ull * e->grid.upml[r].n))) return rc;
+        const size_t n3 = 3ull * e->grid.upml[r].n;
+        if ((rc = aalloc(e, s, &d.lV[r], n3)) || (rc = aalloc(e, s, &d.lI[r], n3)) ||
+            (rc = aalloc(e, s, &d.lpsi[r], n3)) || (rc = aalloc(e, s, &d.lphi[r], n3)))
+            return rc;
     }
     d.B = 1;
     for (int a = 0; a < 3; ++a) {
@@ -354,8 +508,10 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     }
     if ((rc = aalloc(e, s, &d.gvv, 3ull * d.B))) return rc;
     if ((rc = aalloc(e, s, &d.gvi, 3ull * d.B))) return rc;
-    if ((rc = aalloc(e, s, &s->seg_fv, 3ull * d.B * s->K))) return rc;
-    if ((rc = aalloc(e, s, &s->seg_fc, 3ull * d.B * s->K))) return rc;
+    if (s->K) {
+        s->fac_slots = s->K;
+        if ((rc = aalloc(e, s, &s->fac, s->fac_slots * 6ull * d.B))) return rc;
+    }
     if ((rc = aalloc(e, s, &s->rec_numTS, 1))) return rc;
     if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess)
         return afail(e, OEMS_ERR_CUDA, "adjoint events");
@@ -372,20 +528,33 @@ int oems_cuda_adjoint_forward(oems_cuda_engine* e, unsigned int steps)
     for (char* c : s->ckpt) cudaFree(c);
     s->ckpt.clear();
     s->steps = 0;
-    const unsigned nseg = (steps + s->K - 1) / s->K;
-    for (unsigned k = 0; k <= nseg; ++k) {
+    const unsigned nseg = s->K ? (steps + s->K - 1) / s->K : 0;
+    for (unsigned k = 0; k <= nseg; ++k) {            // segment starts + the end state (record mode: end only)
         char* c = nullptr;
         if (cudaMalloc(&c, s->state_bytes) != cudaSuccess) return afail(e, OEMS_ERR_NOMEM, "checkpoint allocation");
         s->ckpt.push_back(c);
     }
-    cudaEventRecord(s->ev[0], e->stream);
-    for (unsigned k = 0; k < nseg; ++k) {
-        int rc = copy_state(e, s, s->ckpt[k], true);
+    if (!s->K && s->fac_slots < steps) {               // record mode: one factor slot per step
+        if (s->fac) {
+            cudaFree(s->fac);
+            s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void*)s->fac));
+            s->fac = nullptr;
+        }
+        int rc = aalloc(e, s, &s->fac, (size_t)steps * 6 * s->dev.B);
         if (rc) return rc;
-        const unsigned n = std::min(s->K, steps - k * s->K);
-        if ((rc = oems_cuda_iterate(e, n))) return rc;
+        s->fac_slots = steps;
     }
-    int rc = copy_state(e, s, s->ckpt[nseg], true);
+    cudaEventRecord(s->ev[0], e->stream);
+    int rc = OEMS_OK;
+    if (s->K) {
+        for (unsigned k = 0; k < nseg && rc == OEMS_OK; ++k) {
+            if ((rc = copy_state(e, s, s->ckpt[k], true))) break;
+            rc = oems_cuda_iterate(e, std::min(s->K, steps - k * s->K));
+        }
+    } else {
+        rc = record_forward(e, s, steps);
+    }
+    if (rc == OEMS_OK) rc = copy_state(e, s, s->ckpt[nseg], true);
     if (rc) return rc;
     cudaEventRecord(s->ev[1], e->stream);
     if (cudaEventSynchronize(s->ev[1]) != cudaSuccess) return afail(e, OEMS_ERR_CUDA, "adjoint forward sync");
@@ -407,65 +576,79 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     cudaStream_t st = e->stream;
     const unsigned N = s->steps;
     const size_t nsrc = (size_t)nprobe * (N + 1);
-    int* dids = nullptr;
+    std::vector<void*> tmp;
+    auto release = [&]() {
+        for (void* q : tmp) cudaFree(q);
+        tmp.clear();
+    };
+    int rc;
+    if ((rc = build_injection(e, nprobe, probe_ids, 0, d.injV, tmp)) ||
+        (rc = build_injection(e, nprobe, probe_ids, 1, d.injI, tmp))) {
+        cudaStreamSynchronize(st);
+        release();
+        return rc;
+    }
     double* dsrc = nullptr;
-    if (cudaMalloc(&dids, std::max(1u, nprobe) * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&dsrc, std::max<size_t>(1, nsrc) * sizeof(double)) != cudaSuccess) {
-        cudaFree(dids);
+    if (cudaMalloc(&dsrc, std::max<size_t>(1, nsrc) * sizeof(double)) != cudaSuccess) {
+        cudaStreamSynchronize(st);
+        release();
         return afail(e, OEMS_ERR_NOMEM, "adjoint source allocation");
     }
+    tmp.push_back(dsrc);
     cudaEventRecord(s->ev[0], st);
-    if (nprobe) {
-        cudaMemcpyAsync(dids, probe_ids, nprobe * sizeof(int), cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(dsrc, sources, nsrc * sizeof(double), cudaMemcpyHostToDevice, st);
-    }
-    cudaMemsetAsync(d.lV, 0, 3 * e->S * sizeof(float), st);
-    cudaMemsetAsync(d.lI, 0, 3 * e->S * sizeof(float), st);
-    cudaMemsetAsync(d.wv, 0, 3 * e->S * sizeof(float), st);
+    if (nsrc) cudaMemcpyAsync(dsrc, sources, nsrc * sizeof(double), cudaMemcpyHostToDevice, st);
+    d.src = dsrc;
+    d.stride = N + 1;
+    cudaMemsetAsync(d.U, 0, 3 * e->S * sizeof(float), st);
+    cudaMemsetAsync(d.W, 0, 3 * e->S * sizeof(float), st);
     for (int r = 0; r < e->grid.nupml; ++r) {
-        cudaMemsetAsync(d.lpsi[r], 0, 3ull * e->grid.upml[r].n * sizeof(float), st);
-        cudaMemsetAsync(d.lphi[r], 0, 3ull * e->grid.upml[r].n * sizeof(float), st);
+        const size_t b3 = 3ull * e->grid.upml[r].n * sizeof(float);
+        cudaMemsetAsync(d.lV[r], 0, b3, st);
+        cudaMemsetAsync(d.lI[r], 0, b3, st);
+        cudaMemsetAsync(d.lpsi[r], 0, b3, st);
+        cudaMemsetAsync(d.lphi[r], 0, b3, st);
     }
     cudaMemsetAsync(d.gvv, 0, 3ull * d.B * sizeof(double), st);
     cudaMemsetAsync(d.gvi, 0, 3ull * d.B * sizeof(double), st);
-    InjDev inj{};
-    inj.nprobe = (int)nprobe;
-    inj.probes = e->stepend.probes;
-    inj.ids = dids;
-    inj.src = dsrc;
-    inj.stride = N + 1;
-    inj.lV = d.lV;
-    inj.lI = d.lI;
-    inj.n = N;
-    k_adj_inject<<<1, 32, 0, st>>>(inj);
     const unsigned plane = e->N[1] * e->Pz;
-    const dim3 grid((plane + 255) / 256, e->N[0]);
-    const unsigned nseg = (N + s->K - 1) / s->K;
-    int rc = OEMS_OK;
-    unsigned lps = 0;
-    for (int seg = (int)nseg - 1; seg >= 0 && rc == OEMS_OK; --seg) {
-        const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
-        if ((rc = copy_state(e, s, s->ckpt[seg], false))) break;
-        cudaMemcpyAsync(s->rec_numTS, &a0, sizeof(unsigned), cudaMemcpyHostToDevice, st);
-        for (unsigned n = a0; n < a1; ++n) {
-            const size_t off = (size_t)(n - a0) * 3 * d.B;
-            k_adj_factors<<<(d.B + 255) / 256, 256, 0, st>>>(d, s->seg_fv + off, s->seg_fc + off);
-            lps = 1 + recompute_step(e, s);
+    const dim3 gu((plane + 255) / 256, e->N[0] - 1), gw((plane + 255) / 256, e->N[0]);
+    const unsigned fb = (d.B + 255) / 256;
+    rc = OEMS_OK;
+    unsigned lps = 2;
+    const unsigned bu = e->splitI.main_blocks + e->splitI.first_block[e->splitI.nreg];
+    const unsigned bw = e->splitV.main_blocks + e->splitV.first_block[e->splitV.nreg];
+    auto reverse = [&](unsigned n, const float* slot) {
+        d.n = n;
+        d.fv = slot;
+        d.fc = slot + 3 * d.B;
+        if (e->use_split) {
+            if (bu) k_adj_split<true><<<bu, 256, 0, st>>>(d, e->splitI);
+            if (bw) k_adj_split<false><<<bw, 256, 0, st>>>(d, e->splitV);
+        } else {
+            k_adj_u<<<gu, 256, 0, st>>>(d);
+            k_adj_w<<<gw, 256, 0, st>>>(d);
         }
-        for (int n = (int)a1 - 1; n >= (int)a0; --n) {
-            const size_t off = (size_t)(n - a0) * 3 * d.B;
-            d.fv = s->seg_fv + off;
-            d.fc = s->seg_fc + off;
-            k_adj_iwi<<<grid, 256, 0, st>>>(d);
-            k_adj_v<<<grid, 256, 0, st>>>(d);
-            inj.n = (unsigned)n;
-            k_adj_inject<<<1, 32, 0, st>>>(inj);
+    };
+    if (s->K) {
+        const unsigned nseg = (N + s->K - 1) / s->K;
+        for (int seg = (int)nseg - 1; seg >= 0 && rc == OEMS_OK; --seg) {
+            const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
+            if ((rc = copy_state(e, s, s->ckpt[seg], false))) break;
+            cudaMemcpyAsync(s->rec_numTS, &a0, sizeof(unsigned), cudaMemcpyHostToDevice, st);
+            for (unsigned n = a0; n < a1; ++n) {
+                k_adj_factors<<<fb, 256, 0, st>>>(d, s->fac, s->rec_numTS, s->K);
+                lps = 3 + recompute_step(e, s);
+            }
+            for (int n = (int)a1 - 1; n >= (int)a0; --n) reverse((unsigned)n, s->fac + (size_t)(n % s->K) * 6 * d.B);
+            if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
         }
+    } else {
+        for (int n = (int)N - 1; n >= 0; --n) reverse((unsigned)n, s->fac + (size_t)n * 6 * d.B);
         if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
     }
-    s->launches_per_reverse_step = lps + 3;
+    s->launches_per_reverse_step = lps;
     // leave the engine at its forward end state
-    if (rc == OEMS_OK) rc = copy_state(e, s, s->ckpt[nseg], false);
+    if (rc == OEMS_OK && s->K) rc = copy_state(e, s, s->ckpt.back(), false);
     if (rc == OEMS_OK) {
         cudaMemcpyAsync(gvv, d.gvv, 3ull * d.B * sizeof(double), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(gvi, d.gvi, 3ull * d.B * sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -475,8 +658,10 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     } else {
         cudaStreamSynchronize(st);
     }
-    cudaFree(dids);
-    cudaFree(dsrc);
+    release();
+    d.src = nullptr;
+    d.injV = InjList{};
+    d.injI = InjList{};
     return rc;
 }
 

@@ -337,11 +337,14 @@ BatchInst make_inst(const oems_cuda_engine* e, unsigned block, unsigned depth)
     return in;
 }
 
-// device bytes an instance streams per step (fields, class index, UPML tables and fluxes)
+// device bytes an instance streams per step (fields, class index, UPML fluxes and class index)
 size_t instance_bytes(const oems_cuda_engine* e)
 {
     size_t b = e->S * (3 * 4 * 2 + 4);
-    for (const auto& u : e->upml) b += (size_t)u.nl[0] * u.nl[1] * u.nl[2] * 3 * 4 * 8;
+    for (int r = 0; r < e->grid.nupml; ++r) {
+        const UpmlDev& u = e->grid.upml[r];
+        b += (size_t)u.n * (3 * 4 * 2 + (u.cls ? 2 : 3 * 4 * 6));
+    }
     return b;
 }
 

@@ -136,6 +136,62 @@ int compress_dense(oems_cuda_engine* e, const float* vv, const float* vi, const 
     return 0;
 }
 
+// UPML coefficient classes of one region: the 18 values (vv, vvfo, vvfn, ii, iifo, iifn of the
+// three components) of each cell, deduplicated; false when there are more than 65535 classes.
+bool compress_upml(const UpmlHost& u, std::vector<unsigned short>& cls, std::vector<float4>& tab)
+{
+    const size_t n = (size_t)u.nl[0] * u.nl[1] * u.nl[2];
+    struct Key18 { uint32_t w[18]; };
+    std::vector<Key18> keys;
+    cls.assign(n, 0);
+    size_t hcap = 1u << 12;
+    std::vector<int64_t> htab(hcap, -1);
+    auto hash = [](const Key18& k) {
+        uint64_t h = 1469598103934665603ULL;
+        for (int i = 0; i < 18; ++i) { h ^= k.w[i]; h *= 1099511628211ULL; h ^= h >> 31; }
+        return h;
+    };
+    Key18 k;
+    for (size_t c = 0; c < n; ++c) {
+        for (int t = 0; t < 6; ++t)
+            for (int m = 0; m < 3; ++m) memcpy(&k.w[3 * t + m], &u.tab[t][m * n + c], 4);
+        size_t slot = hash(k) & (hcap - 1);
+        int64_t found = -1;
+        while (htab[slot] >= 0) {
+            if (memcmp(&keys[htab[slot]], &k, sizeof(Key18)) == 0) { found = htab[slot]; break; }
+            slot = (slot + 1) & (hcap - 1);
+        }
+        if (found < 0) {
+            if (keys.size() >= 65535) return false;
+            found = (int64_t)keys.size();
+            keys.push_back(k);
+            htab[slot] = found;
+            if (keys.size() * 2 > hcap) {
+                hcap *= 4;
+                htab.assign(hcap, -1);
+                for (size_t j = 0; j < keys.size(); ++j) {
+                    size_t s2 = hash(keys[j]) & (hcap - 1);
+                    while (htab[s2] >= 0) s2 = (s2 + 1) & (hcap - 1);
+                    htab[s2] = (int64_t)j;
+                }
+            }
+        }
+        cls[c] = (unsigned short)found;
+    }
+    // per class: (f0 f1 f2 fo0)(fo1 fo2 fn0 fn1)(fn2 0 0 0) for the voltage and the current triple
+    tab.assign(keys.size() * 6, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (size_t j = 0; j < keys.size(); ++j)
+        for (int half = 0; half < 2; ++half) {
+            float v[12] = {0};
+            memcpy(v, &keys[j].w[9 * half], 9 * sizeof(float));
+            float4* t = &tab[6 * j + 3 * half];
+            t[0] = make_float4(v[0], v[1], v[2], v[3]);
+            t[1] = make_float4(v[4], v[5], v[6], v[7]);
+            t[2] = make_float4(v[8], v[9], v[10], v[11]);
+        }
+    return true;
+}
+
 int upload_compressed(oems_cuda_engine* e, const std::vector<unsigned>& index, const std::vector<Key12>& keys)
 {
     const size_t U = keys.size();
@@ -453,15 +509,93 @@ int oems_cuda_add_fd_dump(oems_cuda_engine* e, int field, const unsigned int sta
 
 }  // extern "C" (enqueue_step below is internal C++)
 
+void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp)
+{
+    sp = SplitDev{};
+    const GridDev& g = e->grid;
+    sp.nreg = (unsigned)g.nupml;
+    // region extents clipped to R
+    unsigned cs[OEMS_MAX_UPML][3], ce[OEMS_MAX_UPML][3];
+    unsigned long long in_r = 0;
+    for (int r = 0; r < g.nupml; ++r) {
+        unsigned long long v = 1;
+        for (int a = 0; a < 3; ++a) {
+            cs[r][a] = std::min(g.upml[r].start[a], R[a]);
+            ce[r][a] = std::min(g.upml[r].start[a] + g.upml[r].nl[a], R[a]);
+            v *= ce[r][a] - cs[r][a];
+        }
+        in_r += v;
+    }
+    const unsigned long long total = (unsigned long long)R[0] * R[1] * R[2];
+    const unsigned long long rest = total - in_r;
+    // bounding box of the cells outside every region: a plane is fully covered when the regions'
+    // (disjoint) cross-sections add up to its area
+    unsigned lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    bool any = rest > 0;
+    for (int a = 0; a < 3 && any; ++a) {
+        const int b = (a + 1) % 3, c = (a + 2) % 3;
+        const unsigned long long area = (unsigned long long)R[b] * R[c];
+        auto covered = [&](unsigned k) {
+            unsigned long long s2 = 0;
+            for (int r = 0; r < g.nupml; ++r)
+                if (k >= cs[r][a] && k < ce[r][a]) s2 += (unsigned long long)(ce[r][b] - cs[r][b]) * (ce[r][c] - cs[r][c]);
+            return s2 >= area;
+        };
+        unsigned k0 = 0;
+        while (k0 < R[a] && covered(k0)) ++k0;
+        unsigned k1 = R[a];
+        while (k1 > k0 && covered(k1 - 1)) --k1;
+        lo[a] = k0;
+        hi[a] = k1;
+    }
+    const unsigned long long box = any ? (unsigned long long)(hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]) : 0;
+    if (any && box == rest) {
+        sp.full = 0;
+        for (int a = 0; a < 3; ++a) { sp.lo[a] = lo[a]; sp.n[a] = hi[a] - lo[a]; }
+    } else {
+        sp.full = 1;
+        for (int a = 0; a < 3; ++a) { sp.lo[a] = 0; sp.n[a] = R[a]; }
+    }
+    sp.main_cells = rest ? sp.n[0] * sp.n[1] * sp.n[2] : 0;
+    sp.main_blocks = (sp.main_cells + 255) / 256;
+    sp.first_block[0] = 0;
+    for (int r = 0; r < g.nupml; ++r) sp.first_block[r + 1] = sp.first_block[r] + (g.upml[r].n + 255) / 256;
+}
+
+void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
+{
+    const GridDev& g = e->grid;
+    if (e->use_split) {
+        const SplitDev& sp = curr ? e->splitI : e->splitV;
+        const unsigned blocks = sp.main_blocks + sp.first_block[sp.nreg];
+        if (!blocks) return;
+        if (e->compressed) {
+            if (curr) k_update_split<true, true><<<blocks, 256, 0, s>>>(g, sp);
+            else k_update_split<true, false><<<blocks, 256, 0, s>>>(g, sp);
+        } else {
+            if (curr) k_update_split<false, true><<<blocks, 256, 0, s>>>(g, sp);
+            else k_update_split<false, false><<<blocks, 256, 0, s>>>(g, sp);
+        }
+        return;
+    }
+    const unsigned plane = e->N[1] * e->Pz;
+    const bool up = !e->upml.empty();
+    if (!curr) {
+        const dim3 gv((plane + 255) / 256, e->N[0]);
+        if (e->compressed) { if (up) k_update_v<true, true><<<gv, 256, 0, s>>>(g); else k_update_v<true, false><<<gv, 256, 0, s>>>(g); }
+        else { if (up) k_update_v<false, true><<<gv, 256, 0, s>>>(g); else k_update_v<false, false><<<gv, 256, 0, s>>>(g); }
+    } else {
+        const dim3 gi((plane + 255) / 256, e->N[0] - 1);
+        if (e->compressed) { if (up) k_update_i<true, true><<<gi, 256, 0, s>>>(g); else k_update_i<true, false><<<gi, 256, 0, s>>>(g); }
+        else { if (up) k_update_i<false, true><<<gi, 256, 0, s>>>(g); else k_update_i<false, false><<<gi, 256, 0, s>>>(g); }
+    }
+}
+
 int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
 {
     const GridDev& g = e->grid;
-    const unsigned plane = e->N[1] * e->Pz;
     const dim3 blk(256);
-    const dim3 gv((plane + 255) / 256, e->N[0]);
-    const dim3 gi((plane + 255) / 256, e->N[0] - 1);
     unsigned L = 0;
-    const bool up = !e->upml.empty();
     cudaStream_t s = e->stream;
     // optional per-launch events (profiling path only, never inside a captured graph)
     auto pre = [&](int k) {
@@ -480,13 +614,7 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
         post();
     }
     pre(OEMS_KC_UPDATE_V);
-    if (e->compressed) {
-        if (up) k_update_v<true, true><<<gv, blk, 0, s>>>(g);
-        else k_update_v<true, false><<<gv, blk, 0, s>>>(g);
-    } else {
-        if (up) k_update_v<false, true><<<gv, blk, 0, s>>>(g);
-        else k_update_v<false, false><<<gv, blk, 0, s>>>(g);
-    }
+    launch_update(e, false, s);
     post();
     ++L;
     if (!e->mur.empty()) {
@@ -504,13 +632,7 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     // ---- currents
     for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
     pre(OEMS_KC_UPDATE_I);
-    if (e->compressed) {
-        if (up) k_update_i<true, true><<<gi, blk, 0, s>>>(g);
-        else k_update_i<true, false><<<gi, blk, 0, s>>>(g);
-    } else {
-        if (up) k_update_i<false, true><<<gi, blk, 0, s>>>(g);
-        else k_update_i<false, false><<<gi, blk, 0, s>>>(g);
-    }
+    launch_update(e, true, s);
     post();
     ++L;
     for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
@@ -564,12 +686,32 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         memcpy(d.start, u.start, 12);
         memcpy(d.nl, u.nl, 12);
         d.n = u.nl[0] * u.nl[1] * u.nl[2];
-        float* t[6];
-        for (int k = 0; k < 6; ++k)
-            if ((rc = dupload(e, &t[k], u.tab[k].data(), u.tab[k].size()))) return rc;
-        d.vv = t[0]; d.vvfo = t[1]; d.vvfn = t[2]; d.ii = t[3]; d.iifo = t[4]; d.iifn = t[5];
+        std::vector<unsigned short> cls;
+        std::vector<float4> ctab;
+        d.cls = nullptr; d.ctab = nullptr;
+        d.vv = d.vvfo = d.vvfn = d.ii = d.iifo = d.iifn = nullptr;
+        if (compress_upml(u, cls, ctab)) {
+            unsigned short* dc;
+            float4* dt;
+            if ((rc = dupload(e, &dc, cls.data(), cls.size()))) return rc;
+            if ((rc = dupload(e, &dt, ctab.data(), ctab.size()))) return rc;
+            d.cls = dc; d.ctab = dt;
+        } else {
+            float* t[6];
+            for (int k = 0; k < 6; ++k)
+                if ((rc = dupload(e, &t[k], u.tab[k].data(), u.tab[k].size()))) return rc;
+            d.vv = t[0]; d.vvfo = t[1]; d.vvfn = t[2]; d.ii = t[3]; d.iifo = t[4]; d.iifn = t[5];
+        }
         if ((rc = dalloc(e, &d.vflux, 3 * (size_t)d.n, true, true))) return rc;
         if ((rc = dalloc(e, &d.iflux, 3 * (size_t)d.n, true, true))) return rc;
+    }
+
+    e->use_split = g.nupml > 0;
+    if (e->use_split) {
+        const unsigned RV[3] = {e->N[0], e->N[1], e->N[2]};
+        const unsigned RI[3] = {e->N[0] - 1, e->N[1] - 1, e->N[2] - 1};
+        make_split(e, RV, e->splitV);
+        make_split(e, RI, e->splitI);
     }
 
     // excitation

@@ -113,7 +113,15 @@ struct oems_cuda_engine {
     std::vector<void*> allocs;                            // freed on destroy
     std::vector<std::pair<void*, size_t>> state;          // snapshot regions (device)
     oems_adjoint_state* adj = nullptr;
+    // UPML work split of the update launches (used when the engine has UPML regions)
+    bool use_split = false;
+    SplitDev splitV{}, splitI{};
 };
+
+// the split for update range R (V: the mesh, I: one cell less per axis)
+void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp);
+// one update launch (V or I) of the engine's kernel configuration on stream s
+void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s);
 
 
 // per-launch events for oems_cuda_profile_steps (never used inside a captured graph)

@@ -22,7 +22,10 @@ struct UpmlDev {
     unsigned start[3];
     unsigned nl[3];
     unsigned n;                 // nl[0]*nl[1]*nl[2]
-    const float* vv;            // [3][n] each
+    // coefficients, class-compressed (cls != nullptr) or dense
+    const unsigned short* cls;  // [n] class of each cell
+    const float4* ctab;         // [U][6]: (vv0 vv1 vv2 vvfo0)(vvfo1 vvfo2 vvfn0 vvfn1)(vvfn2 - - -), same for ii/iifo/iifn
+    const float* vv;            // dense [3][n] each
     const float* vvfo;
     const float* vvfn;
     const float* ii;
@@ -53,6 +56,29 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 
+// UPML coefficients of one cell: c = {f0 f1 f2, fo0 fo1 fo2, fn0 fn1 fn2} with (f, fo, fn) =
+// (vv, vvfo, vvfn) for CURR == false and (ii, iifo, iifn) for CURR == true
+template <bool CURR>
+__device__ __forceinline__ void upml_coef(const UpmlDev& u, unsigned loc, float c[9])
+{
+    if (u.cls) {
+        const float4* t = u.ctab + 6u * __ldg(u.cls + loc) + (CURR ? 3 : 0);
+        const float4 a = __ldg(t), b = __ldg(t + 1), d = __ldg(t + 2);
+        c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w;
+        c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w; c[8] = d.x;
+    } else {
+        const float* f = CURR ? u.ii : u.vv;
+        const float* fo = CURR ? u.iifo : u.vvfo;
+        const float* fn = CURR ? u.iifn : u.vvfn;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            c[k] = __ldg(f + k * u.n + loc);
+            c[3 + k] = __ldg(fo + k * u.n + loc);
+            c[6 + k] = __ldg(fn + k * u.n + loc);
+        }
+    }
+}
+
 // returns region index and local linear offset (without component) or -1
 __device__ __forceinline__ int upml_find(const GridDev& g, unsigned x, unsigned y, unsigned z, unsigned& loc)
 {
@@ -81,8 +107,10 @@ __device__ __forceinline__ float ldf(const float* p)
     return COHERENT ? __ldcg(p) : __ldg(p);
 }
 
+// rk/lk: the cell's UPML region and local offset when the caller knows them (rk = -2: look up)
 template <bool COMPRESSED, bool UPML, bool COHERENT = false>
-__device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsigned y, unsigned z)
+__device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsigned y, unsigned z, int rk = -2,
+                                              unsigned lk = 0)
 {
     const unsigned long long S = g.S;
     const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
@@ -113,7 +141,10 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
 
     int r = -1;
     unsigned loc = 0;
-    if (UPML) r = upml_find(g, x, y, z, loc);
+    if (UPML) {
+        if (rk == -2) r = upml_find(g, x, y, z, loc);
+        else { r = rk; loc = lk; }
+    }
     if (UPML && r >= 0) {
         const UpmlDev& u = g.upml[r];
         const unsigned n = u.n;
@@ -121,18 +152,20 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
         const float cc[3] = {c0, c1, c2};
         const float cvv[3] = {vv0, vv1, vv2};
         const float cvi[3] = {vi0, vi1, vi2};
+        float pc[9];
+        upml_coef<false>(u, loc, pc);
         float out[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const unsigned q = k * n + loc;
             const float flux = u.vflux[q];
             // pre: f = vv*V - vvfo*flux; V = flux; flux = f
-            const float f = fsub(fmul(__ldg(u.vv + q), vin[k]), fmul(__ldg(u.vvfo + q), flux));
+            const float f = fsub(fmul(pc[k], vin[k]), fmul(pc[3 + k], flux));
             float vn = flux;
             vn = fadd(fmul(vn, cvv[k]), fmul(cvi[k], cc[k]));
             // post: h = flux; flux = V; V = h + vvfn*flux
             u.vflux[q] = vn;
-            out[k] = fadd(f, fmul(__ldg(u.vvfn + q), vn));
+            out[k] = fadd(f, fmul(pc[6 + k], vn));
         }
         V[o] = out[0]; V[S + o] = out[1]; V[2 * S + o] = out[2];
         return;
@@ -145,7 +178,8 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
 // Engine::UpdateCurrents (FDTD/engine.cpp:170-222) fused with the UPML current hooks
 // (FDTD/extensions/engine_ext_upml.cpp:144-229) for one cell x<Nx-1, y<Ny-1, z<Nz-1.
 template <bool COMPRESSED, bool UPML, bool COHERENT = false>
-__device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsigned y, unsigned z)
+__device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsigned y, unsigned z, int rk = -2,
+                                              unsigned lk = 0)
 {
     const unsigned long long S = g.S;
     const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
@@ -174,7 +208,10 @@ __device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsi
 
     int r = -1;
     unsigned loc = 0;
-    if (UPML) r = upml_find(g, x, y, z, loc);
+    if (UPML) {
+        if (rk == -2) r = upml_find(g, x, y, z, loc);
+        else { r = rk; loc = lk; }
+    }
     if (UPML && r >= 0) {
         const UpmlDev& u = g.upml[r];
         const unsigned n = u.n;
@@ -182,16 +219,18 @@ __device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsi
         const float cc[3] = {c0, c1, c2};
         const float cii[3] = {ii0, ii1, ii2};
         const float civ[3] = {iv0, iv1, iv2};
+        float pc[9];
+        upml_coef<true>(u, loc, pc);
         float out[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const unsigned q = k * n + loc;
             const float flux = u.iflux[q];
-            const float f = fsub(fmul(__ldg(u.ii + q), iin[k]), fmul(__ldg(u.iifo + q), flux));
+            const float f = fsub(fmul(pc[k], iin[k]), fmul(pc[3 + k], flux));
             float in = flux;
             in = fadd(fmul(in, cii[k]), fmul(civ[k], cc[k]));
             u.iflux[q] = in;
-            out[k] = fadd(f, fmul(__ldg(u.iifn + q), in));
+            out[k] = fadd(f, fmul(pc[6 + k], in));
         }
         I[o] = out[0]; I[S + o] = out[1]; I[2 * S + o] = out[2];
         return;
@@ -220,6 +259,53 @@ __global__ void __launch_bounds__(256) k_update_i(GridDev g)
     const unsigned y = t / g.Pz, z = t - y * g.Pz;
     if (y + 1 >= g.Ny || z + 1 >= g.Nz) return;
     update_i_cell<COMPRESSED, UPML>(g, x, y, z);
+}
+
+// Work split for meshes with UPML regions: blocks [0, main_blocks) map the cells outside every
+// region (a box when the regions are boundary slabs, else the whole range with UPML cells
+// skipped), the following blocks map the cells of each region in region order.  Every warp then
+// runs one code path, and region cells read their fluxes with region-local coalesced offsets.
+struct SplitDev {
+    unsigned lo[3], n[3];                      // main part: this box of cells
+    unsigned main_cells, main_blocks;
+    int full;                                  // 1: the box is the whole update range, skip UPML cells
+    unsigned nreg;
+    unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1]) after main
+};
+
+template <bool COMPRESSED, bool CURR>
+__global__ void __launch_bounds__(256) k_update_split(GridDev g, SplitDev sp)
+{
+    unsigned b = blockIdx.x;
+    if (b < sp.main_blocks) {
+        unsigned t = b * 256u + threadIdx.x;
+        if (t >= sp.main_cells) return;
+        const unsigned z = sp.lo[2] + t % sp.n[2];
+        t /= sp.n[2];
+        const unsigned y = sp.lo[1] + t % sp.n[1];
+        const unsigned x = sp.lo[0] + t / sp.n[1];
+        if (sp.full) {
+            unsigned loc;
+            if (upml_find(g, x, y, z, loc) >= 0) return;
+        }
+        if (CURR) update_i_cell<COMPRESSED, false>(g, x, y, z);
+        else update_v_cell<COMPRESSED, false>(g, x, y, z);
+        return;
+    }
+    b -= sp.main_blocks;
+    int r = 0;
+    while (r + 1 < (int)sp.nreg && b >= sp.first_block[r + 1]) ++r;
+    const UpmlDev& u = g.upml[r];
+    const unsigned loc = (b - sp.first_block[r]) * 256u + threadIdx.x;
+    if (loc >= u.n) return;
+    const unsigned lz = loc % u.nl[2], rest = loc / u.nl[2];
+    const unsigned x = u.start[0] + rest / u.nl[1], y = u.start[1] + rest % u.nl[1], z = u.start[2] + lz;
+    if (CURR) {
+        if (x + 1 >= g.Nx || y + 1 >= g.Ny || z + 1 >= g.Nz) return;
+        update_i_cell<COMPRESSED, true>(g, x, y, z, r, loc);
+    } else {
+        update_v_cell<COMPRESSED, true>(g, x, y, z, r, loc);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
