@@ -123,6 +123,10 @@ def build_workload(name, shape=None):
         return configs.patch(steps=100000), "patch 160x160x80 graded, UPML 8, 50 Ohm port, NF2FF 3 freqs"
     if name == "plain":
         return configs.plain_cube(n=100, steps=100000), "plain 100^3, vacuum, PEC, soft Ez, V/I probes"
+    if name == "design":
+        case = configs.DesignCase(steps=100000)
+        return (case.build(case.eps0)[1],
+                "design 200x200x100 lines, 0.5 mm, UPML 8, 64x64x16 eps_r cells, two 50 Ohm ports")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -214,7 +218,7 @@ def measure_batched(count):
             "serial_per_instance_cells_steps_s": per_inst}
 
 
-def measure_adjoint():
+def measure_adjoint(steps=8000):
     """Differentiable form: 200x200x100 lines at 0.5 mm, UPML 8, 64x64x16 design cells of eps_r
     U[1,6] (seeded), 50 Ohm input and output ports 60 cells from the region, objective = port
     power at 4/5/6 GHz over 8000 steps, checkpoints every 256 steps.  Device times (CUDA events
@@ -224,13 +228,13 @@ def measure_adjoint():
     from openems_gb300.configs import DesignCase
     from openems_gb300.engine import Engine_CUDA
     t0 = time.perf_counter()
-    case = DesignCase()
+    case = DesignCase(steps=steps)
     _, data = case.build(case.eps0)
     t_build = time.perf_counter() - t0
     eng = Engine_CUDA(data, case.steps)
     plain_ms = eng.timed_iterate(case.steps)
     eng.close()
-    out = {"config": "200x200x100 lines, 0.5 mm, UPML 8, design 64x64x16, 8000 steps",
+    out = {"config": "200x200x100 lines, 0.5 mm, UPML 8, design 64x64x16, %d steps" % steps,
            "forward_ms": plain_ms, "build_s": round(t_build, 1)}
     cells = float(np.prod(data.num_lines.astype(np.float64)))
     out["forward_mcells_per_s"] = cells * case.steps / plain_ms / 1e3
@@ -288,13 +292,15 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="stress", choices=["stress", "patch", "plain"])
+    ap.add_argument("--workload", default="stress", choices=["stress", "patch", "plain", "design"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--shape", default=None, help="mesh lines of the stress workload, e.g. 256,256,192")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batch-count", type=int, default=32)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-form measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=8000,
+                    help="timesteps of the differentiable-form measurement (8000 = its configuration)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -380,7 +386,7 @@ def main():
 
     adjoint = None
     if rank == 0 and not args.no_adjoint:
-        adjoint = measure_adjoint()
+        adjoint = measure_adjoint(args.adjoint_steps)
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:

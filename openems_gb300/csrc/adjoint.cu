@@ -95,8 +95,11 @@ __device__ __forceinline__ void add_sources(const AdjDev& a, const InjList& L, u
     if (L.count == 0 || o < L.lo || o > L.hi) return;
     for (unsigned k = 0; k < L.count; ++k)
         if (L.cell[k] == o) {
-            const double v = a.src[(unsigned long long)L.row[k] * a.stride + a.n + 1] * L.coef[k];
-            s[L.comp[k]] = fadd(s[L.comp[k]], (float)v);
+            const float v = (float)(a.src[(unsigned long long)L.row[k] * a.stride + a.n + 1] * L.coef[k]);
+            const int m = L.comp[k];                       // constant indices keep s in registers
+            if (m == 0) s[0] = fadd(s[0], v);
+            else if (m == 1) s[1] = fadd(s[1], v);
+            else s[2] = fadd(s[2], v);
         }
 }
 
@@ -193,13 +196,14 @@ __device__ __forceinline__ void adj_w_cell(const AdjDev& a, unsigned x, unsigned
         const unsigned bx = x - a.b0[0], by = y - a.b0[1], bz = z - a.b0[2];
         if (bx < a.bn[0] && by < a.bn[1] && bz < a.bn[2]) {
             const unsigned kb = (bx * a.bn[1] + by) * a.bn[2] + bz;
+            // per-step products in float (FP64 arithmetic is slow on this GPU), sums in double
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
                 if (vi[m] == 0.f) continue;                     // PEC edge: no dependence
-                const double b = (double)wn[m] / (double)vi[m];
+                const float b = fmul(wn[m], __frcp_rn(vi[m]));
                 const unsigned kk = m * a.B + kb;
-                a.gvv[kk] += b * (double)__ldg(a.fv + kk);
-                a.gvi[kk] += b * (double)__ldg(a.fc + kk);
+                a.gvv[kk] += (double)fmul(b, __ldg(a.fv + kk));
+                a.gvi[kk] += (double)fmul(b, __ldg(a.fc + kk));
             }
         }
         return;

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -591,6 +592,24 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
     }
 }
 
+int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch)
+{
+    const FusedDev& f = e->fused[parity];
+    const dim3 grid((e->N[2] + FT_Z - 1) / FT_Z, (e->N[1] + FT_Y - 1) / FT_Y, (e->N[0] + f.xchunk - 1) / f.xchunk);
+    if (e->compressed) k_step_fused<true><<<grid, FT_BLOCK, 0, e->stream>>>(f);
+    else k_step_fused<false><<<grid, FT_BLOCK, 0, e->stream>>>(f);
+    // processing on the fields this step wrote
+    GridDev g = e->grid;
+    g.V = f.Vo;
+    g.I = f.Io;
+    for (int r = 0; r < g.nupml; ++r) g.upml[r].vflux = f.vflux_o[r];
+    k_step_end<<<e->stepend_blocks, 256, 0, e->stream>>>(g, e->stepend);
+    if (nlaunch) *nlaunch = 2;
+    cudaError_t c = cudaGetLastError();
+    if (c != cudaSuccess) return cuda_fail(e, c, "fused step launch");
+    return OEMS_OK;
+}
+
 int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
 {
     const GridDev& g = e->grid;
@@ -649,12 +668,66 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
 
 extern "C" {
 
-static int capture(oems_cuda_engine* e, unsigned steps, cudaGraphExec_t* out)
+// the buffers and tables of the fused step (second field/flux set, source cells, both parities)
+static int setup_fused(oems_cuda_engine* e)
+{
+    int rc;
+    if ((rc = dalloc(e, &e->dV2, 3 * e->S, true))) return rc;
+    if ((rc = dalloc(e, &e->dI2, 3 * e->S, true))) return rc;
+    for (int r = 0; r < e->grid.nupml; ++r)
+        if ((rc = dalloc(e, &e->vflux2[r], 3 * (size_t)e->grid.upml[r].n, true))) return rc;
+    FusedDev base{};
+    base.excV = e->excV;
+    base.excI = e->excI;
+    base.numTS = e->d_numTS;
+    auto cells = [&](const std::vector<unsigned long long>& off, const unsigned long long** dptr,
+                     unsigned long long& lo, unsigned long long& hi) -> int {
+        *dptr = nullptr;
+        lo = 1;
+        hi = 0;
+        if (off.empty()) return OEMS_OK;
+        std::vector<unsigned long long> c(off.size());
+        for (size_t k = 0; k < off.size(); ++k) c[k] = off[k] % e->S;
+        lo = *std::min_element(c.begin(), c.end());
+        hi = *std::max_element(c.begin(), c.end());
+        unsigned long long* d = nullptr;
+        const int r2 = dupload(e, &d, c.data(), c.size());
+        *dptr = d;
+        return r2;
+    };
+    if ((rc = cells(e->exc_voff, &base.srcV_cell, base.srcV_lo, base.srcV_hi))) return rc;
+    if ((rc = cells(e->exc_ioff, &base.srcI_cell, base.srcI_lo, base.srcI_hi))) return rc;
+    // x-planes per block: about 8 blocks per SM of a 152-SM GPU, 4..64 planes
+    const unsigned long long tiles = (unsigned long long)((e->N[2] + FT_Z - 1) / FT_Z) * ((e->N[1] + FT_Y - 1) / FT_Y);
+    base.xchunk = (unsigned)std::min<unsigned long long>(64, std::max<unsigned long long>(4, e->N[0] * tiles / 1216));
+    FusedDev& f0 = e->fused[0];
+    FusedDev& f1 = e->fused[1];
+    f0 = base;
+    f1 = base;
+    f0.g = e->grid;                                  // A -> B
+    f0.Vo = e->dV2;
+    f0.Io = e->dI2;
+    f1.g = e->grid;                                  // B -> A
+    f1.g.V = e->dV2;
+    f1.g.I = e->dI2;
+    f1.Vo = e->dV;
+    f1.Io = e->dI;
+    for (int r = 0; r < e->grid.nupml; ++r) {
+        f0.vflux_o[r] = e->vflux2[r];
+        f1.g.upml[r].vflux = e->vflux2[r];
+        f1.vflux_o[r] = e->grid.upml[r].vflux;
+    }
+    return OEMS_OK;
+}
+
+static int capture(oems_cuda_engine* e, unsigned steps, cudaGraphExec_t* out, bool fused)
 {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     int rc = OEMS_OK;
-    for (unsigned s = 0; s < steps && rc == OEMS_OK; ++s) rc = enqueue_step(e, s == 0 ? &e->launches : nullptr);
+    for (unsigned s = 0; s < steps && rc == OEMS_OK; ++s)
+        rc = fused ? enqueue_fused_step(e, (int)(s & 1), s == 0 ? &e->fused_launches : nullptr)
+                   : enqueue_step(e, s == 0 ? &e->launches : nullptr);
     cudaError_t c = cudaStreamEndCapture(e->stream, &graph);
     if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
     if (c != cudaSuccess) return cuda_fail(e, c, "cudaStreamEndCapture");
@@ -935,8 +1008,19 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(e->stream));
     }
-    if ((rc = capture(e, 1, &e->graph1))) return rc;
-    if ((rc = capture(e, e->K, &e->graphK))) return rc;
+    // OEMS_CUDA_FUSED=1 replaces the K-step graph by the fused one-kernel step, for engines where
+    // no hook reads neighbouring lines between the half-steps (Mur walls, dispersive materials).
+    // It moves 38 % fewer bytes but its plane-serial march is latency-bound and slower than the
+    // separate update kernels on GB300, so it is not the default.
+    {
+        const char* env = getenv("OEMS_CUDA_FUSED");
+        e->use_fused = env && env[0] == '1' && e->mur.empty() && e->lor.empty() &&
+                       e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC && e->K % 2 == 0 &&
+                       3ull * e->S < (1ull << 32);        // the staged-plane offsets are 32-bit
+        if (e->use_fused && (rc = setup_fused(e))) return rc;
+    }
+    if ((rc = capture(e, 1, &e->graph1, false))) return rc;
+    if ((rc = capture(e, e->K, &e->graphK, e->use_fused))) return rc;
     e->inited = true;
     return OEMS_OK;
 }
@@ -1018,7 +1102,7 @@ int oems_cuda_profile_steps(oems_cuda_engine* e, unsigned int n, float* ms, unsi
 int oems_cuda_launches_per_step(const oems_cuda_engine* e, unsigned int* l)
 {
     if (!e || !l) return OEMS_ERR_ARG;
-    *l = e->launches;
+    *l = e->use_fused ? e->fused_launches : e->launches;
     return OEMS_OK;
 }
 

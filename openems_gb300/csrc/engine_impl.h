@@ -8,6 +8,7 @@
 
 #include "../../include/oems_cuda.h"
 #include "kernels.cuh"
+#include "fused.cuh"
 
 using namespace oems;
 
@@ -116,7 +117,19 @@ struct oems_cuda_engine {
     // UPML work split of the update launches (used when the engine has UPML regions)
     bool use_split = false;
     SplitDev splitV{}, splitI{};
+    // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
+    // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
+    // whenever the host sees it
+    bool use_fused = false;
+    float* dV2 = nullptr;
+    float* dI2 = nullptr;
+    float* vflux2[OEMS_MAX_UPML] = {};
+    FusedDev fused[2]{};
+    unsigned fused_launches = 0;
 };
+
+// enqueue one fused timestep on e->stream: parity 0 reads set A and writes B, parity 1 the reverse
+int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch);
 
 // the split for update range R (V: the mesh, I: one cell less per axis)
 void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp);
