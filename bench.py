@@ -255,6 +255,21 @@ def measure_adjoint(steps=8000):
     return out
 
 
+def max_over_ranks(value, dist=None, device="cuda"):
+    """The slowest rank's value, on every rank (the timed region is bracketed by barriers)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mcells(cells, steps, ms, world):
+    """MCells/s of all ranks together: each rank runs its own replica of `cells` cells."""
+    return cells * steps / (ms / 1e3) / 1e6 * world
+
+
 def run_reference(args, op, desc, rank):
     if rank != 0:
         return
@@ -341,12 +356,8 @@ def main():
     with ClockSampler(local) as clk:
         ms = eng.timed_iterate(args.steps)
     clocks = clk.summary()
-    if dist:
-        import torch
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = cells * args.steps / (ms / 1e3) / 1e6 * world
+    ms = max_over_ranks(ms, dist, "cuda") if dist else ms
+    value = whole_job_mcells(cells, args.steps, ms, world)
 
     # ---- per-kernel event timing for the roofline ----------------------------------------
     from openems_gb300._native import KERNEL_CLASSES
