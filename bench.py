@@ -255,6 +255,42 @@ def measure_adjoint(steps=8000):
     return out
 
 
+def measure_nf2ff(steps=2000, cpu_angles=64):
+    """NF2FF far-field transform of the patch workload's NF2FF box (160x160x80 graded lines, six
+    faces, E and H FD dumps at 1.5/2/2.5 GHz) after `steps` timesteps: the device transform over
+    the full sphere at 1 degree (181 x 361 angles) per frequency (wall clock around the call,
+    which synchronises), and the numpy restatement on the host cores for `cpu_angles` angles,
+    scaled per angle."""
+    from openems_gb300 import configs
+    from openems_gb300.engine import Engine_CUDA
+    from openems_gb300.nf2ff import box_faces, calc_nf2ff
+    from oracle.nf2ff_ref import nf2ff as nf2ff_host
+    op = configs.patch(steps=steps)
+    eng = Engine_CUDA(op, steps)
+    eng.IterateTS(steps)
+    faces = box_faces(eng)
+    samples = sum(int(np.prod([len(c) for c in f[2]])) for f in faces)
+    theta = np.deg2rad(np.arange(0, 181, 1.0))
+    phi = np.deg2rad(np.arange(0, 361, 1.0))
+    calc_nf2ff(eng, 0, theta[:8], phi[:8])                   # warm-up
+    t0 = time.perf_counter()
+    res = [calc_nf2ff(eng, fi, theta, phi) for fi in range(3)]
+    gpu_s = (time.perf_counter() - t0) / 3
+    data = [(c, eng.fd_dump(ie)[0], eng.fd_dump(ih)[0]) for ie, ih, c in faces]
+    th_s = np.deg2rad(np.linspace(0, 180, cpu_angles))
+    t0 = time.perf_counter()
+    nf2ff_host(data, res[0].freq, th_s, phi[:1])
+    cpu_s = time.perf_counter() - t0
+    eng.close()
+    nang = len(theta) * len(phi)
+    return {"config": "patch 160x160x80, NF2FF box of 6 faces, 1 deg sphere (181x361), per frequency",
+            "face_samples": samples, "angles": nang, "gpu_ms_per_freq": gpu_s * 1e3,
+            "sample_angle_pairs_per_s": samples * nang / gpu_s,
+            "cpu_oracle_ms_per_freq_scaled": cpu_s / cpu_angles * nang * 1e3,
+            "cpu_sample": f"{cpu_angles} angles, numpy restatement (oracle/nf2ff_ref.py)",
+            "Dmax": [r.Dmax for r in res], "Prad_W": [r.Prad for r in res]}
+
+
 def max_over_ranks(value, dist=None, device="cuda"):
     """The slowest rank's value, on every rank (the timed region is bracketed by barriers)."""
     if dist is None:
@@ -314,6 +350,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batch-count", type=int, default=32)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-form measurement")
+    ap.add_argument("--no-nf2ff", action="store_true", help="skip the NF2FF far-field measurement")
     ap.add_argument("--adjoint-steps", type=int, default=8000,
                     help="timesteps of the differentiable-form measurement (8000 = its configuration)")
     args = ap.parse_args()
@@ -399,6 +436,10 @@ def main():
     if rank == 0 and not args.no_adjoint:
         adjoint = measure_adjoint(args.adjoint_steps)
 
+    nf2ff = None
+    if rank == 0 and not args.no_nf2ff:
+        nf2ff = measure_nf2ff()
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -423,6 +464,7 @@ def main():
             "kernels": kernels,
             "batched": batched,
             "adjoint": adjoint,
+            "nf2ff": nf2ff,
         }
         print(json.dumps(line), flush=True)
     if dist:

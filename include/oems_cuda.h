@@ -257,6 +257,22 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* eng, unsigned int nprobe, const
 int oems_cuda_adjoint_timing(const oems_cuda_engine* eng, float* forward_ms, float* backward_ms,
                              unsigned int* launches_per_reverse_step);
 
+/* ---- NF2FF far-field transform ------------------------------------------------------------------ */
+
+/* Replaces nf2ff_calc (nf2ff/nf2ff_calc.cpp:41-160, 329-530) run on the HDF5 FD dumps of an
+ * NF2FF box: the transform reads the E/H FD-dump accumulators on the device directly. Face f
+ * is the pair (e_dumps[f], h_dumps[f]) of FD dumps (E and H, same planar box, more than two
+ * lines per tangential axis). coords holds, face after face, the sample coordinates in metres
+ * along x, then y, then z (the dual mesh lines of a cell-interpolated dump). Cartesian meshes,
+ * no mirror planes. freq_index selects the dumps' frequency, freq is its value in Hz. Outputs
+ * for theta[i], phi[j] at index i*nphi + j: e_theta and e_phi (complex, re/im interleaved),
+ * p_rad (W/m^2 at `radius` metres); rad_power (W, through the faces) and max_dir may be NULL. */
+int oems_cuda_nf2ff(oems_cuda_engine* eng, unsigned int nface, const int* e_dumps, const int* h_dumps,
+                    const double* coords, unsigned int freq_index, double freq, unsigned int ntheta,
+                    const double* theta, unsigned int nphi, const double* phi, const double center[3], double radius,
+                    double eps_r, double mu_r, double* e_theta, double* e_phi, double* p_rad, double* rad_power,
+                    double* max_dir);
+
 /* ---- checkpoint / resume --------------------------------------------------------------------- */
 
 /* Size in bytes of a snapshot of the full engine state (fields, UPML fluxes, Mur buffers,

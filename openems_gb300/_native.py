@@ -75,6 +75,7 @@ CUDA_ONLY = {
     "adjoint_forward": (I, [P, U]),
     "adjoint_backward": (I, [P, U, PI_, PD, PD, PD]),
     "adjoint_timing": (I, [P, PF, PF, PU]),
+    "nf2ff": (I, [P, U, PI_, PI_, PD, U, D, U, PD, U, PD, PD, D, D, D, PD, PD, PD, PD, PD]),
 }
 
 KERNEL_CLASSES = ["update_v", "update_i", "mur", "lorentz", "excite", "step_end"]

@@ -19,8 +19,11 @@ def bits_equal(a, b):
 
 
 def rel_l2(a, b):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
+    a = np.asarray(a)
+    b = np.asarray(b)
+    dt = np.complex128 if (np.iscomplexobj(a) or np.iscomplexobj(b)) else np.float64
+    a = a.astype(dt)
+    b = b.astype(dt)
     m = np.isfinite(a) & np.isfinite(b)
     den = np.linalg.norm(b[m])
     return np.linalg.norm(a[m] - b[m]) / (den if den > 0 else 1.0)
