@@ -361,12 +361,24 @@ def main():
 
     if args.impl == "reference" and rank != 0:
         return
-    t_build = time.perf_counter()
-    op, desc = build_workload(args.workload, [int(v) for v in args.shape.split(",")] if args.shape else None)
-    t_build = time.perf_counter() - t_build
+    shape = [int(v) for v in args.shape.split(",")] if args.shape else None
     if args.impl == "reference":
+        op, desc = build_workload(args.workload, shape)
         run_reference(args, op, desc, rank)
         return
+    # operator setup: the per-edge numerics on the GPU (bit-identical to the host build) where
+    # the geometry allows it; the host build is timed beside it once
+    from openems_gb300.operator import build_device
+    dev = "cpu" if args.workload == "design" else "cuda"
+    t_build = time.perf_counter()
+    with build_device(dev):
+        op, desc = build_workload(args.workload, shape)
+    t_build = time.perf_counter() - t_build
+    t_build_host = None
+    if rank == 0 and dev == "cuda" and not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        build_workload(args.workload, shape)
+        t_build_host = time.perf_counter() - t0
 
     dist = None
     if world > 1:
@@ -454,7 +466,9 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": desc, "cells": cells, "l2": "inputs larger than L2 (field state %.2f GB)" % (
                 24 * cells / 1e9), "parallelism": "replicas" if world > 1 else "single",
-                "operator_classes": None, "build_s": round(t_build, 1), "engine_setup_s": round(t_setup, 1)},
+                "operator_classes": None, "build_s": round(t_build, 2), "build_device": dev,
+                "host_build_s": round(t_build_host, 2) if t_build_host is not None else None,
+                "engine_setup_s": round(t_setup, 1)},
             "roofline": roofline,
             "cpu_baseline": base,
             "e2e": e2e,

@@ -273,6 +273,28 @@ int oems_cuda_nf2ff(oems_cuda_engine* eng, unsigned int nface, const int* e_dump
                     double eps_r, double mu_r, double* e_theta, double* e_phi, double* p_rad, double* rad_power,
                     double* max_dir);
 
+/* ---- operator numerics on the device --------------------------------------------------------------- */
+
+/* Replaces the per-edge loops of Operator::CalcECOperator (FDTD/operator.cpp:986-1097):
+ * AverageMatQuarterCell (:1447-1564), Calc_ECPos (:1189-1254), CalcTimestep_Var3 (:1956-2030) and
+ * Calc_ECOperatorPos (:956-984), for geometries described as material boxes. lines: the mesh lines
+ * of x, then y, then z (drawing units, num_lines each), unit: metres per drawing unit. Paint
+ * records in painting order, the last record containing a sample point wins (ascending priority,
+ * among equal priorities the earliest-defined box last): rec_lo/rec_hi [nrec][3] (drawing units,
+ * inclusive), rec_par [nrec][4] = eps_r, kappa, mu_r, sigma; background [4] the same for points
+ * outside every record. Results are bit-identical to the host restatement. */
+typedef struct oems_cuda_opbuild oems_cuda_opbuild;
+int oems_cuda_opbuild_create(const unsigned int num_lines[3], const double* lines, double unit, unsigned int nrec,
+                             const double* rec_lo, const double* rec_hi, const double* rec_par,
+                             const double background[4], oems_cuda_opbuild** out);
+/* C, G, L, R of every edge (float [3][Nx][Ny][Nz] each, x,y,z order; any may be NULL) and, if
+ * dt_var3 is not NULL, the Var3 timestep (1e200 if no node gives a finite positive one). */
+int oems_cuda_opbuild_ec(oems_cuda_opbuild* b, float* C, float* G, float* L, float* R, double* dt_var3);
+/* vv, vi, ii, iv for timestep dt (float [3][Nx][Ny][Nz] each), before boundary conditions. */
+int oems_cuda_opbuild_coefficients(oems_cuda_opbuild* b, double dt, float* vv, float* vi, float* ii, float* iv);
+const char* oems_cuda_opbuild_last_error(const oems_cuda_opbuild* b);
+void oems_cuda_opbuild_destroy(oems_cuda_opbuild* b);
+
 /* ---- checkpoint / resume --------------------------------------------------------------------- */
 
 /* Size in bytes of a snapshot of the full engine state (fields, UPML fluxes, Mur buffers,

@@ -76,6 +76,11 @@ CUDA_ONLY = {
     "adjoint_backward": (I, [P, U, PI_, PD, PD, PD]),
     "adjoint_timing": (I, [P, PF, PF, PU]),
     "nf2ff": (I, [P, U, PI_, PI_, PD, U, D, U, PD, U, PD, PD, D, D, D, PD, PD, PD, PD, PD]),
+    "opbuild_create": (I, [PU, PD, D, U, PD, PD, PD, PD, C.POINTER(P)]),
+    "opbuild_ec": (I, [P, PF, PF, PF, PF, PD]),
+    "opbuild_coefficients": (I, [P, D, PF, PF, PF, PF]),
+    "opbuild_last_error": (C.c_char_p, [P]),
+    "opbuild_destroy": (None, [P]),
 }
 
 KERNEL_CLASSES = ["update_v", "update_i", "mur", "lorentz", "excite", "step_end"]

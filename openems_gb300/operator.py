@@ -34,6 +34,7 @@ from __future__ import annotations
 import math
 import os
 from concurrent.futures import ThreadPoolExecutor
+from contextlib import contextmanager
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -404,6 +405,19 @@ def _parallel(fn, items):
 # =========================================================================================
 # the operator
 # =========================================================================================
+_BUILD_DEVICE = ["cpu"]
+
+
+@contextmanager
+def build_device(device: str):
+    """Default device of Operator.build inside the block ("cpu" or "cuda")."""
+    _BUILD_DEVICE.append(device)
+    try:
+        yield
+    finally:
+        _BUILD_DEVICE.pop()
+
+
 class Operator:
     """Builds EC-FDTD coefficients plus extension tables for the engine.
 
@@ -613,6 +627,25 @@ class Operator:
         sl = tuple(slice(int(start[a]) - lo[a], int(start[a]) - lo[a] + int(nl[a])) for a in range(3))
         return [x[sl] for x in e]
 
+    # ---- the same numerics on the GPU -----------------------------------------------------------
+    def _gpu_core(self):
+        """EC_C/G/L/R and the Var3 timestep from the device builder; returns (builder, dt_var3)."""
+        if np.dtype(self.ft) != np.float32:
+            raise ValueError("Operator.build(device='cuda'): float32 operators only")
+        recs = self._mat.recs
+        if any(r[4].params.get("voxel") for r in recs):
+            raise ValueError("Operator.build(device='cuda'): voxel materials are built on the host")
+        keys = ("epsilon", "kappa", "mue", "sigma")
+        lo = np.array([np.asarray(r[0], np.float64) for r in recs], np.float64).reshape(-1, 3)
+        hi = np.array([np.asarray(r[1], np.float64) for r in recs], np.float64).reshape(-1, 3)
+        par = np.array([[r[4].params.get(k, self.bg[k]) if r[4].kind == MATERIAL else self.bg[k] for k in keys]
+                        for r in recs], np.float64).reshape(-1, 4)
+        b = GpuOperatorBuilder(self.L, self.unit, lo, hi, par, [self.bg[k] for k in keys])
+        shape = (3,) + tuple(int(v) for v in self.N)
+        self.EC_C, self.EC_G, self.EC_L, self.EC_R = (np.empty(shape, np.float32) for _ in range(4))
+        dt = b.ec(self.EC_C, self.EC_G, self.EC_L, self.EC_R, self.forced_dt <= 0)
+        return b, dt
+
     # ---- timestep (FDTD/operator.cpp:1956-2030) --------------------------------------------
     def calc_timestep_var3(self):
         def work(x0, x1):
@@ -736,11 +769,27 @@ class Operator:
         return dim, np.array(s), np.array(e), np.array(si), np.array(ei)
 
     # ---- the build --------------------------------------------------------------------------
-    def build(self, num_ts: int) -> OperatorData:
-        """CalcECOperator (FDTD/operator.cpp:986-1097) + extension builds + processing setup."""
-        self.calc_ec()
+    def build(self, num_ts: int, device: Optional[str] = None) -> OperatorData:
+        """CalcECOperator (FDTD/operator.cpp:986-1097) + extension builds + processing setup.
+
+        device="cuda" computes the equivalent circuit, the Var3 timestep and the coefficients on
+        the GPU (oems_cuda_opbuild_*, bit-identical to the host path) for float32 operators
+        without voxel materials; everything else is built on the host either way."""
+        gpu = None
+        device = device or _BUILD_DEVICE[-1]
+        if device == "cuda":
+            gpu = self._gpu_core()
+        elif device != "cpu":
+            raise ValueError(f"Operator.build: unknown device {device!r}")
+        else:
+            self.calc_ec()
         if self.forced_dt > 0:
             dT = self.forced_dt
+        elif gpu is not None:
+            dT = gpu[1]
+            if dT == 0 or dT >= 1e200:
+                gpu[0].close()
+                raise ValueError("Operator: timestep is zero")
         else:
             dT = self.calc_timestep_var3()
         dT *= self.ts_factor
@@ -761,7 +810,13 @@ class Operator:
                                 self.EC_R[n, x0:x1], dT)
                 for d, v in zip((self.vv, self.vi, self.ii, self.iv), r):
                     d[n, x0:x1] = v
-        _parallel(coef, _slabs(int(self.N[0]), 2 * (os.cpu_count() or 1)))
+        if gpu is not None:
+            try:
+                gpu[0].coefficients(dT, self.vv, self.vi, self.ii, self.iv)
+            finally:
+                gpu[0].close()
+        else:
+            _parallel(coef, _slabs(int(self.N[0]), 2 * (os.cpu_count() or 1)))
 
         self._apply_electric_bc([b != -1 for b in self.bc])
         self._calc_pec()
@@ -1341,3 +1396,47 @@ class Operator:
 def box_lines(start, stop, n):
     """Uniform helper: n+1 equally spaced lines between start and stop."""
     return np.linspace(start, stop, n + 1)
+
+
+class GpuOperatorBuilder:
+    """ctypes handle of oems_cuda_opbuild_* (the CUDA library is required)."""
+
+    def __init__(self, lines, unit, lo, hi, par, background):
+        import ctypes as C
+        from . import _native
+        self.C = C
+        self.lib = _native.load_cuda()
+        nl = np.array([len(l) for l in lines], np.uint32)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(l, np.float64) for l in lines]))
+        self._keep = [nl, flat, np.ascontiguousarray(lo), np.ascontiguousarray(hi), np.ascontiguousarray(par),
+                      np.ascontiguousarray(background, np.float64)]
+        P = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+        self.h = C.c_void_p()
+        rc = self.lib.opbuild_create(P(nl, C.c_uint), P(flat, C.c_double), float(unit), len(lo),
+                                     P(self._keep[2], C.c_double), P(self._keep[3], C.c_double),
+                                     P(self._keep[4], C.c_double), P(self._keep[5], C.c_double), C.byref(self.h))
+        self._check(rc, "opbuild_create")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.lib.opbuild_last_error(self.h) if self.h else b""
+            self.close()
+            raise RuntimeError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def ec(self, Cc, G, L, R, var3=True):
+        C = self.C
+        P = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        dt = C.c_double(0.0)
+        self._check(self.lib.opbuild_ec(self.h, P(Cc), P(G), P(L), P(R), C.byref(dt) if var3 else None), "opbuild_ec")
+        return dt.value
+
+    def coefficients(self, dt, vv, vi, ii, iv):
+        C = self.C
+        P = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._check(self.lib.opbuild_coefficients(self.h, float(dt), P(vv), P(vi), P(ii), P(iv)),
+                    "opbuild_coefficients")
+
+    def close(self):
+        if self.h:
+            self.lib.opbuild_destroy(self.h)
+            self.h = None
