@@ -175,6 +175,38 @@ def stress(shape=(512, 512, 256), steps=2000, nblocks=64, seed=20261204, pitch_m
     return op.build(steps)
 
 
+def mur_corners(n=(16, 14, 12), steps=600, seed=7, wall_source=True):
+    """Mur on all six walls with the hooks' corner cases: dispersive blocks that reach five walls
+    (their apply hooks run between the Mur post and apply hooks; the blocks meet on the wall
+    edges), and (wall_source) a soft source on the x = 0 wall line, which switches that wall on
+    only after the excitation (engine_ext_mur_abc.cpp:44-60).  An odd z count such as 33 puts
+    the upper z wall's line and shift cells of some rows in neighbouring warps of the engine."""
+    rng = np.random.default_rng(seed)
+    lines = [np.cumsum(np.concatenate([[0.0], rng.uniform(0.6, 1.2, k - 1)])) for k in n]
+    g = Grid(lines, unit=1e-3)
+    gl = g.lines
+    L = [l[-1] for l in gl]
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(6e9, 5e9)
+    csx.AddMaterial("diel", epsilon=3.0, kappa=0.02).AddBox([0.3 * L[0], 0.3 * L[1], 0.3 * L[2]],
+                                                            [0.7 * L[0], 0.6 * L[1], 0.7 * L[2]])
+    csx.AddLorentzMaterial("drude_wall", epsilon=1.5, eps_plasma_freq=[5e9], eps_relax_time=[2e-9]).AddBox(
+        [0.0, 0.0, 0.3 * L[2]], [0.4 * L[0], 0.5 * L[1], L[2]], priority=5)
+    csx.AddLorentzMaterial("lor_wall", epsilon=2.0, eps_plasma_freq=[8e9], eps_relax_time=[1e-9],
+                           eps_lor_pole_freq=[3e9]).AddBox([0.6 * L[0], 0.5 * L[1], 0.0], [L[0], L[1], 0.4 * L[2]],
+                                                          priority=6)
+    # y-directed source on the x = 0 line (tangential to that wall) and a z-directed one inside
+    if wall_source:
+        csx.AddExcitation("wall_src", 0, [0, 1.0, 0]).AddBox([gl[0][0], gl[1][5], gl[2][6]],
+                                                             [gl[0][0], gl[1][6], gl[2][6]], priority=20)
+    cx, cy, cz = (gl[k][n[k] // 2] for k in range(3))
+    csx.AddExcitation("mid_src", 0, [0, 0, 1.0]).AddBox([cx, cy, cz], [cx, cy, gl[2][n[2] // 2 + 1]], priority=20)
+    csx.AddProbe("wall_ut", 0, interval=1).AddBox([gl[0][0], gl[1][5], gl[2][6]], [gl[0][0], gl[1][6], gl[2][6]])
+    op = Operator(csx, g, exc, bc=(2,) * 6)
+    return op.build(steps)
+
+
 # ------------------------------------------------------------------------------------------
 def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
     """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""

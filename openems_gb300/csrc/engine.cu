@@ -563,32 +563,64 @@ void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp)
     for (int r = 0; r < g.nupml; ++r) sp.first_block[r + 1] = sp.first_block[r] + (g.upml[r].n + 255) / 256;
 }
 
+template <bool C, bool U, int M, typename IX = unsigned long long>
+static void launch_v(const dim3& grid, cudaStream_t s, const GridDev& g, const MurDev& m, const unsigned* ts)
+{
+    k_update_v<C, U, M, IX><<<grid, 256, 0, s>>>(g, m, ts);
+}
+
 void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
 {
     const GridDev& g = e->grid;
+    const MurDev& m = e->murdev;
+    const unsigned* ts = e->d_numTS;
+    // the voltage update carries the Mur pre/post hooks when there are walls
+    const bool mur = !curr && !e->mur.empty() && !e->mur_separate;
     if (e->use_split) {
         const SplitDev& sp = curr ? e->splitI : e->splitV;
         const unsigned blocks = sp.main_blocks + sp.first_block[sp.nreg];
         if (!blocks) return;
         if (e->compressed) {
-            if (curr) k_update_split<true, true><<<blocks, 256, 0, s>>>(g, sp);
-            else k_update_split<true, false><<<blocks, 256, 0, s>>>(g, sp);
+            if (curr) k_update_split<true, true><<<blocks, 256, 0, s>>>(g, sp, m, ts);
+            else if (mur) k_update_split<true, false, true><<<blocks, 256, 0, s>>>(g, sp, m, ts);
+            else k_update_split<true, false><<<blocks, 256, 0, s>>>(g, sp, m, ts);
         } else {
-            if (curr) k_update_split<false, true><<<blocks, 256, 0, s>>>(g, sp);
-            else k_update_split<false, false><<<blocks, 256, 0, s>>>(g, sp);
+            if (curr) k_update_split<false, true><<<blocks, 256, 0, s>>>(g, sp, m, ts);
+            else if (mur) k_update_split<false, false, true><<<blocks, 256, 0, s>>>(g, sp, m, ts);
+            else k_update_split<false, false><<<blocks, 256, 0, s>>>(g, sp, m, ts);
         }
         return;
     }
     const unsigned plane = e->N[1] * e->Pz;
     const bool up = !e->upml.empty();
+    // 32-bit cell offsets when every component offset fits
+    const bool o32 = 3ull * e->S < (1ull << 32);
     if (!curr) {
         const dim3 gv((plane + 255) / 256, e->N[0]);
-        if (e->compressed) { if (up) k_update_v<true, true><<<gv, 256, 0, s>>>(g); else k_update_v<true, false><<<gv, 256, 0, s>>>(g); }
-        else { if (up) k_update_v<false, true><<<gv, 256, 0, s>>>(g); else k_update_v<false, false><<<gv, 256, 0, s>>>(g); }
+        const int mode = !mur ? 0 : (m.lanes ? 2 : 1);
+        if (up) {
+            if (e->compressed) { if (mode) launch_v<true, true, 1>(gv, s, g, m, ts); else launch_v<true, true, 0>(gv, s, g, m, ts); }
+            else { if (mode) launch_v<false, true, 1>(gv, s, g, m, ts); else launch_v<false, true, 0>(gv, s, g, m, ts); }
+        } else if (e->compressed) {
+            if (o32) {
+                if (mode == 2) launch_v<true, false, 2, unsigned>(gv, s, g, m, ts);
+                else if (mode == 1) launch_v<true, false, 1, unsigned>(gv, s, g, m, ts);
+                else launch_v<true, false, 0, unsigned>(gv, s, g, m, ts);
+            } else {
+                if (mode == 2) launch_v<true, false, 2>(gv, s, g, m, ts);
+                else if (mode == 1) launch_v<true, false, 1>(gv, s, g, m, ts);
+                else launch_v<true, false, 0>(gv, s, g, m, ts);
+            }
+        } else {
+            if (mode == 2) launch_v<false, false, 2>(gv, s, g, m, ts);
+            else if (mode == 1) launch_v<false, false, 1>(gv, s, g, m, ts);
+            else launch_v<false, false, 0>(gv, s, g, m, ts);
+        }
     } else {
         const dim3 gi((plane + 255) / 256, e->N[0] - 1);
-        if (e->compressed) { if (up) k_update_i<true, true><<<gi, 256, 0, s>>>(g); else k_update_i<true, false><<<gi, 256, 0, s>>>(g); }
-        else { if (up) k_update_i<false, true><<<gi, 256, 0, s>>>(g); else k_update_i<false, false><<<gi, 256, 0, s>>>(g); }
+        if (up) { if (e->compressed) k_update_i<true, true><<<gi, 256, 0, s>>>(g); else k_update_i<false, true><<<gi, 256, 0, s>>>(g); }
+        else if (e->compressed) { if (o32) k_update_i<true, false, unsigned><<<gi, 256, 0, s>>>(g); else k_update_i<true, false><<<gi, 256, 0, s>>>(g); }
+        else k_update_i<false, false><<<gi, 256, 0, s>>>(g);
     }
 }
 
@@ -627,26 +659,17 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
     unsigned mur_pts = 0;
     for (const auto& m : e->mur) mur_pts = std::max<unsigned>(mur_pts, (unsigned)m.cP.size());
-    if (!e->mur.empty()) {
-        pre(OEMS_KC_MUR);
-        k_mur<<<dim3((mur_pts + 255) / 256, (unsigned)e->mur.size()), blk, 0, s>>>(g, e->murdev, 0, e->d_numTS); ++L;
-        post();
-    }
+    const dim3 mur_grid((mur_pts + 255) / 256, (unsigned)e->mur.size());
+    // the Mur pre/post hooks run inside the voltage update unless mur_separate
+    const bool mur_sep = !e->mur.empty() && e->mur_separate;
+    if (mur_sep) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 0, e->d_numTS); post(); ++L; }
     pre(OEMS_KC_UPDATE_V);
     launch_update(e, false, s);
     post();
     ++L;
-    if (!e->mur.empty()) {
-        pre(OEMS_KC_MUR);
-        k_mur<<<dim3((mur_pts + 255) / 256, (unsigned)e->mur.size()), blk, 0, s>>>(g, e->murdev, 1, e->d_numTS); ++L;
-        post();
-    }
+    if (mur_sep) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 1, e->d_numTS); post(); ++L; }
     for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
-    if (!e->mur.empty()) {
-        pre(OEMS_KC_MUR);
-        k_mur<<<dim3((mur_pts + 255) / 256, (unsigned)e->mur.size()), blk, 0, s>>>(g, e->murdev, 2, e->d_numTS); ++L;
-        post();
-    }
+    if (!e->mur.empty()) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 2, e->d_numTS); post(); ++L; }
     if (e->excV.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excV.count + 127) / 128, 128, 0, s>>>(e->dV, e->excV, e->d_numTS); post(); ++L; }
     // ---- currents
     for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
@@ -821,6 +844,51 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         if ((rc = dalloc(e, &d.bP, m.cP.size(), true, true))) return rc;
         if ((rc = dalloc(e, &d.bPP, m.cP.size(), true, true))) return rc;
     }
+    // per axis: the walls with that normal, and the window of coordinates that are no line or
+    // shift of them (lines below the middle bound it from below, the others from above)
+    {
+        int j = 0;
+        for (int a = 0; a < 3; ++a) {
+            e->murdev.first[a] = j;
+            unsigned lo = 0, hi = e->N[a] - 1;
+            for (size_t w = 0; w < e->mur.size(); ++w) {
+                if (e->mur[w].ny != a) continue;
+                e->murdev.order[j++] = (int)w;
+                for (unsigned c : {e->mur[w].line, e->mur[w].shift}) {
+                    if (2 * c < e->N[a]) lo = std::max(lo, c + 1);
+                    else if (c >= 1) hi = std::min(hi, c - 1);
+                    else lo = e->N[a];
+                }
+            }
+            if (lo <= hi && lo < e->N[a]) { e->murdev.lo[a] = lo; e->murdev.span[a] = hi - lo; }
+            else { e->murdev.lo[a] = e->N[a]; e->murdev.span[a] = 0; }   // no window: every coordinate is checked
+        }
+        e->murdev.first[3] = j;
+    }
+    // the lane-parallel z-wall form needs at most two z walls with neighbouring line and shift
+    // and four distinct z among them (nz = -1: every wall goes through mur_cell)
+    {
+        MurDev& md = e->murdev;
+        md.nz = 0;
+        std::vector<unsigned> zs;
+        for (int q = md.first[2]; q < md.first[3]; ++q) {
+            const MurWallDev& d = md.w[md.order[q]];
+            const bool adjacent = d.line + 1 == d.shift || d.shift + 1 == d.line;
+            if (md.nz >= 2 || !adjacent) { md.nz = -1; break; }
+            md.z[md.nz++] = d;
+            zs.push_back(d.line);
+            zs.push_back(d.shift);
+        }
+        std::sort(zs.begin(), zs.end());
+        if (md.nz >= 0 && std::adjacent_find(zs.begin(), zs.end()) != zs.end()) md.nz = -1;
+        // OEMS_CUDA_MUR_SEPARATE=1: the pre/post hooks as separate launches (k_mur phases 0/1)
+        const char* ms = getenv("OEMS_CUDA_MUR_SEPARATE");
+        e->mur_separate = ms && ms[0] == '1';
+        // the lane-parallel form: no UPML (plain update kernel), every wall active from step 0
+        bool always = true;
+        for (const auto& m : e->mur) always = always && m.start_ts == 0;
+        md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
+    }
 
     // Lorentz / Drude orders
     for (const auto& l : e->lor) {
@@ -832,6 +900,21 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         if (l.von) {
             LorDev d{};
             d.count = l.count; d.off = doff; d.lor = l.vlon;
+            if (e->murdev.lanes) {
+                // the voltage update writes final Mur values: the apply leaves every component an
+                // (always active) wall owns alone, as the reference's later Mur apply overwrites it
+                std::vector<unsigned char> sk(l.count, 0);
+                bool any = false;
+                for (unsigned i = 0; i < l.count; ++i) {
+                    const unsigned p[3] = {l.pos[i], l.pos[l.count + i], l.pos[2 * l.count + i]};
+                    for (const auto& w : e->mur)
+                        if (p[w.ny] == w.line) sk[i] |= (unsigned char)(7u & ~(1u << w.ny));
+                    any = any || sk[i];
+                }
+                unsigned char* dsk = nullptr;
+                if (any && (rc = dupload(e, &dsk, sk.data(), sk.size()))) return rc;
+                d.skip = dsk;
+            }
             float *ci, *ce, *cl = nullptr;
             if ((rc = dupload(e, &ci, l.vint.data(), m))) return rc;
             if ((rc = dupload(e, &ce, l.vext.data(), m))) return rc;

@@ -117,6 +117,9 @@ struct oems_cuda_engine {
     // UPML work split of the update launches (used when the engine has UPML regions)
     bool use_split = false;
     SplitDev splitV{}, splitI{};
+    // Mur pre/post hooks as separate launches (k_mur phases 0/1) instead of inside the voltage
+    // update; set by OEMS_CUDA_MUR_SEPARATE=1 at init
+    bool mur_separate = false;
     // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
     // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
     // whenever the host sees it

@@ -95,6 +95,162 @@ __device__ __forceinline__ int upml_find(const GridDev& g, unsigned x, unsigned 
     return -1;
 }
 
+// Mur walls (FDTD/extensions/engine_ext_mur_abc.cpp:83-178): wall w updates the two tangential
+// components on mesh line `line` of axis ny from the neighbouring line `shift`; the tables and
+// the wall buffers bP/bPP are indexed k = pos[nyP] * n2 + pos[nyPP].
+struct MurWallDev {
+    int ny, nyP, nyPP;
+    unsigned line, shift, start_ts, n1, n2;
+    const float* cP;
+    const float* cPP;
+    float* bP;
+    float* bPP;
+};
+struct MurDev {
+    int nwall;
+    MurWallDev w[OEMS_MAX_MUR];      // insertion order (the apply priority)
+    // per axis a: coordinates in [lo[a], lo[a] + span[a]] are no line or shift of a wall with
+    // normal a; the walls with normal a are w[order[first[a] .. first[a+1])]
+    unsigned lo[3], span[3];
+    int first[4];
+    int order[OEMS_MAX_MUR];
+    // z walls for the lane-parallel form (mur_z_*): nz <= 2 walls with |line - shift| = 1 whose
+    // lines and shifts are four distinct z (the host checks this before choosing the form);
+    // lanes = 1 while the voltage update runs that form (k_mur then skips the direct columns)
+    int nz;
+    MurWallDev z[2];
+    int lanes;
+};
+
+// Where the Mur pre and post voltage hooks (engine_ext_mur_abc.cpp:83-149) run: inside the
+// voltage update, by the thread of each wall's shift cell,
+//   bP = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift),
+// with V_new(shift) the cell's own new value before any later hook, exactly what the post hook
+// reads.  The update of a line cell leaves the tangential components of every active wall
+// unwritten: the wall's apply (k_mur) overwrites them after the dispersive apply hooks, so the
+// raw value is never observed, and V_old(line) can still be read from memory by the shift cell
+// while the launch runs.
+
+// true when a coordinate of the cell lies outside its axis window (a possible line or shift);
+// NA = 2 checks x and y only
+template <int NA = 3>
+__device__ __forceinline__ bool mur_wall_cell(const MurDev& m, unsigned x, unsigned y, unsigned z)
+{
+    bool r = (x - m.lo[0] > m.span[0]) | (y - m.lo[1] > m.span[1]);
+    if (NA == 3) r |= (z - m.lo[2] > m.span[2]);
+    return r;
+}
+
+// The hooks of the walls with normal axis a < NA at one cell; returns the store mask of the
+// cell's three components.  Divergent and serial (its loads follow the update's loads): meant
+// for cells the caller has found outside the windows.
+template <int NA = 3>
+__device__ __forceinline__ unsigned mur_cell(const GridDev& g, const MurDev& m, unsigned ts, unsigned x, unsigned y,
+                                             unsigned z, unsigned long long o, float vo0, float vo1, float vo2,
+                                             float vn0, float vn1, float vn2)
+{
+    unsigned keep = 7u;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        const unsigned c = a == 0 ? x : (a == 1 ? y : z);
+        if (c - m.lo[a] <= m.span[a]) continue;
+        const int aP = (a + 1) % 3, aPP = (a + 2) % 3;
+        const unsigned long long stride = a == 0 ? (unsigned long long)g.Ny * g.Pz : (a == 1 ? (unsigned long long)g.Pz : 1ull);
+        const float oP = aP == 0 ? vo0 : (aP == 1 ? vo1 : vo2), oPP = aPP == 0 ? vo0 : (aPP == 1 ? vo1 : vo2);
+        const float nP = aP == 0 ? vn0 : (aP == 1 ? vn1 : vn2), nPP = aPP == 0 ? vn0 : (aPP == 1 ? vn1 : vn2);
+        const unsigned iP = aP == 0 ? x : (aP == 1 ? y : z), iPP = aPP == 0 ? x : (aPP == 1 ? y : z);
+        for (int j = m.first[a]; j < m.first[a + 1]; ++j) {
+            const MurWallDev& d = m.w[m.order[j]];
+            if (ts < d.start_ts) continue;                  // Engine_Ext_Mur_ABC::IsActive
+            if (c == d.line) keep &= ~((1u << aP) | (1u << aPP));
+            if (c == d.shift) {
+                const unsigned long long ol = o + (unsigned long long)((long long)d.line - (long long)d.shift) * stride;
+                const unsigned k = iP * d.n2 + iPP;
+                const float lP = g.V[(unsigned long long)aP * g.S + ol];
+                const float lPP = g.V[(unsigned long long)aPP * g.S + ol];
+                const float cP = __ldg(d.cP + k), cPP = __ldg(d.cPP + k);
+                d.bP[k] = fadd(fsub(oP, fmul(cP, lP)), fmul(cP, nP));
+                d.bPP[k] = fadd(fsub(oPP, fmul(cPP, lPP)), fmul(cPP, nPP));
+            }
+        }
+    }
+    return keep;
+}
+
+// Lane-parallel form for the z walls (mode 2 of update_v_cell; every wall active from step 0).
+// Threads walk z, so a z wall's line and shift cells are neighbouring lanes, usually of one warp.
+// The line lane takes V_old and V_new of the shift lane by shuffle and computes the wall value
+//   b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift)
+// itself.  In a "direct" column -- no x/y wall line or shift there (inside both windows) and both
+// lanes in one warp -- it stores b as the final value, so the apply has nothing left to do; the
+// dispersive apply hooks skip the Mur-owned components (the reference's apply overwrites them).
+// Other columns go through the wall buffer and k_mur applies them: the line lane writes bP (same
+// warp) or leaves the line unwritten while the shift lane reads V_old(line) from memory and
+// writes bP (lanes in neighbouring warps).  The tangential components of a z wall are 0 and 1;
+// the table index is x*Ny + y.
+__device__ __forceinline__ bool mur_z_direct(const MurDev& m, unsigned Pz, unsigned x, unsigned y, unsigned line,
+                                             unsigned shift)
+{
+    const unsigned r = y * Pz;
+    return (x - m.lo[0] <= m.span[0]) && (y - m.lo[1] <= m.span[1]) && ((r + line) >> 5) == ((r + shift) >> 5);
+}
+
+// before the update's loads: start the line lane's coefficient loads into L1 (prefetch holds no
+// register across the update)
+__device__ __forceinline__ void mur_z_prefetch(const MurDev& m, unsigned x, unsigned y, unsigned z, unsigned Ny)
+{
+    const MurWallDev& A = m.z[0];
+    const MurWallDev& B = m.z[1];
+    const bool la = m.nz > 0 && z == A.line, lb = m.nz > 1 && z == B.line;
+    if (la || lb) {
+        const unsigned k = x * Ny + y;
+        asm volatile("prefetch.global.L1 [%0];" ::"l"((lb ? B.cP : A.cP) + k));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"((lb ? B.cPP : A.cPP) + k));
+    }
+}
+
+// after the update (every lane of the warp calls it): sets out0/out1 of a direct line cell to the
+// wall value, writes bP/bPP of the buffered columns; returns the mask of components this cell
+// still stores
+__device__ __forceinline__ unsigned mur_z_finish(const GridDev& g, const MurDev& m, unsigned x, unsigned y,
+                                                 unsigned z, bool valid, unsigned long long o, float vo0, float vo1,
+                                                 float& out0, float& out1)
+{
+    const MurWallDev& A = m.z[0];
+    const MurWallDev& B = m.z[1];
+    const bool la = valid && m.nz > 0 && z == A.line, lb = valid && m.nz > 1 && z == B.line;
+    const bool sa = valid && m.nz > 0 && z == A.shift, sb = valid && m.nz > 1 && z == B.shift;
+    const bool wb = lb || sb;
+    const MurWallDev& W = wb ? B : A;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned src = (la || lb) ? ((lane + W.shift - W.line) & 31u) : lane;
+    const unsigned full = 0xffffffffu;
+    const float so0 = __shfl_sync(full, vo0, src), so1 = __shfl_sync(full, vo1, src);
+    const float sn0 = __shfl_sync(full, out0, src), sn1 = __shfl_sync(full, out1, src);
+    if (!(la || lb || sa || sb)) return 7u;
+    const unsigned r = y * g.Pz;
+    const bool same = ((r + W.line) >> 5) == ((r + W.shift) >> 5);
+    const unsigned k = x * g.Ny + y;
+    if (la || lb) {
+        if (!same) return 4u;           // the shift lane in the neighbouring warp writes bP
+        const float cP = __ldg(W.cP + k), cPP = __ldg(W.cPP + k);
+        const float b0 = fadd(fsub(so0, fmul(cP, vo0)), fmul(cP, sn0));
+        const float b1 = fadd(fsub(so1, fmul(cPP, vo1)), fmul(cPP, sn1));
+        if ((x - m.lo[0] <= m.span[0]) && (y - m.lo[1] <= m.span[1])) { out0 = b0; out1 = b1; return 7u; }
+        W.bP[k] = b0;
+        W.bPP[k] = b1;
+        return 4u;
+    }
+    if (!same) {                        // shift lane; the line lane left V_old(line) in memory
+        const unsigned long long ol = W.line > W.shift ? o + 1 : o - 1;
+        const float l0 = g.V[ol], l1 = g.V[g.S + ol];
+        const float cP = __ldg(W.cP + k), cPP = __ldg(W.cPP + k);
+        W.bP[k] = fadd(fsub(vo0, fmul(cP, l0)), fmul(cP, out0));
+        W.bPP[k] = fadd(fsub(vo1, fmul(cPP, l1)), fmul(cPP, out1));
+    }
+    return 7u;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Engine::UpdateVoltages (FDTD/engine.cpp:110-168) fused with Engine_Ext_UPML pre/post voltage
 // updates (FDTD/extensions/engine_ext_upml.cpp:52-137) for one cell (x, y, z < Nz).
@@ -107,24 +263,29 @@ __device__ __forceinline__ float ldf(const float* p)
     return COHERENT ? __ldcg(p) : __ldg(p);
 }
 
-// rk/lk: the cell's UPML region and local offset when the caller knows them (rk = -2: look up)
-template <bool COMPRESSED, bool UPML, bool COHERENT = false>
+// rk/lk: the cell's UPML region and local offset when the caller knows them (rk = -2: look up).
+// MUR: the Mur pre/post hooks of the walls are done here (m, ts = the walls and the step
+// number): 1 = every wall by mur_cell, 2 = the z walls lane-parallel (mur_z_*; every lane of the
+// warp must call, `valid` false for the lanes without a cell) and the x/y walls by mur_cell.
+template <bool COMPRESSED, bool UPML, bool COHERENT = false, int MUR = 0, typename IX = unsigned long long>
 __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsigned y, unsigned z, int rk = -2,
-                                              unsigned lk = 0)
+                                              unsigned lk = 0, const MurDev* m = nullptr, unsigned ts = 0,
+                                              bool valid = true)
 {
-    const unsigned long long S = g.S;
-    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
-    const unsigned long long sx = x ? (unsigned long long)g.Ny * g.Pz : 0ull;
-    const unsigned long long sy = y ? (unsigned long long)g.Pz : 0ull;
-    const unsigned long long sz = z ? 1ull : 0ull;
+    if (MUR == 2) mur_z_prefetch(*m, x, y, z, g.Ny);
+    const IX S = (IX)g.S;
+    const IX o = ((IX)x * g.Ny + y) * g.Pz + z;
+    const IX sx = x ? (IX)g.Ny * g.Pz : (IX)0;
+    const IX sy = y ? (IX)g.Pz : (IX)0;
+    const IX sz = z ? (IX)1 : (IX)0;
     const float* __restrict__ I = g.I;
     float* __restrict__ V = g.V;
 
-    const float i0 = ldf<COHERENT>(I + o), i1 = ldf<COHERENT>(I + S + o), i2 = ldf<COHERENT>(I + 2 * S + o);
+    const float i0 = ldf<COHERENT>(I + o), i1 = ldf<COHERENT>(I + (S + o)), i2 = ldf<COHERENT>(I + (2 * S + o));
     // curl terms in the reference's evaluation order ((a - b) - c) + d
-    const float c0 = fadd(fsub(fsub(i2, ldf<COHERENT>(I + 2 * S + o - sy)), i1), ldf<COHERENT>(I + S + o - sz));
-    const float c1 = fadd(fsub(fsub(i0, ldf<COHERENT>(I + o - sz)), i2), ldf<COHERENT>(I + 2 * S + o - sx));
-    const float c2 = fadd(fsub(fsub(i1, ldf<COHERENT>(I + S + o - sx)), i0), ldf<COHERENT>(I + o - sy));
+    const float c0 = fadd(fsub(fsub(i2, ldf<COHERENT>(I + (2 * S + o - sy))), i1), ldf<COHERENT>(I + (S + o - sz)));
+    const float c1 = fadd(fsub(fsub(i0, ldf<COHERENT>(I + (o - sz))), i2), ldf<COHERENT>(I + (2 * S + o - sx)));
+    const float c2 = fadd(fsub(fsub(i1, ldf<COHERENT>(I + (S + o - sx))), i0), ldf<COHERENT>(I + (o - sy)));
 
     float vv0, vv1, vv2, vi0, vi1, vi2;
     if (COMPRESSED) {
@@ -132,11 +293,11 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
         const float4 a = __ldg(g.tabV + 2 * c), b = __ldg(g.tabV + 2 * c + 1);
         vv0 = a.x; vv1 = a.y; vv2 = a.z; vi0 = a.w; vi1 = b.x; vi2 = b.y;
     } else {
-        vv0 = __ldg(g.vv + o); vv1 = __ldg(g.vv + S + o); vv2 = __ldg(g.vv + 2 * S + o);
-        vi0 = __ldg(g.vi + o); vi1 = __ldg(g.vi + S + o); vi2 = __ldg(g.vi + 2 * S + o);
+        vv0 = __ldg(g.vv + o); vv1 = __ldg(g.vv + (S + o)); vv2 = __ldg(g.vv + (2 * S + o));
+        vi0 = __ldg(g.vi + o); vi1 = __ldg(g.vi + (S + o)); vi2 = __ldg(g.vi + (2 * S + o));
     }
     float v0, v1, v2;
-    if (COHERENT) { v0 = __ldcg(V + o); v1 = __ldcg(V + S + o); v2 = __ldcg(V + 2 * S + o); }
+    if (COHERENT) { v0 = __ldcg(V + o); v1 = __ldcg(V + (S + o)); v2 = __ldcg(V + (2 * S + o)); }
     else { v0 = V[o]; v1 = V[S + o]; v2 = V[2 * S + o]; }
 
     int r = -1;
@@ -145,6 +306,7 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
         if (rk == -2) r = upml_find(g, x, y, z, loc);
         else { r = rk; loc = lk; }
     }
+    float out[3];
     if (UPML && r >= 0) {
         const UpmlDev& u = g.upml[r];
         const unsigned n = u.n;
@@ -154,7 +316,6 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
         const float cvi[3] = {vi0, vi1, vi2};
         float pc[9];
         upml_coef<false>(u, loc, pc);
-        float out[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const unsigned q = k * n + loc;
@@ -167,31 +328,41 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
             u.vflux[q] = vn;
             out[k] = fadd(f, fmul(pc[6 + k], vn));
         }
-        V[o] = out[0]; V[S + o] = out[1]; V[2 * S + o] = out[2];
-        return;
+    } else {
+        out[0] = fadd(fmul(v0, vv0), fmul(vi0, c0));
+        out[1] = fadd(fmul(v1, vv1), fmul(vi1, c1));
+        out[2] = fadd(fmul(v2, vv2), fmul(vi2, c2));
     }
-    V[o] = fadd(fmul(v0, vv0), fmul(vi0, c0));
-    V[S + o] = fadd(fmul(v1, vv1), fmul(vi1, c1));
-    V[2 * S + o] = fadd(fmul(v2, vv2), fmul(vi2, c2));
+    unsigned keep = 7u;
+    if (MUR == 1) keep = mur_cell<3>(g, *m, ts, x, y, z, o, v0, v1, v2, out[0], out[1], out[2]);
+    if (MUR == 2) {
+        // x/y walls first: their hooks read this cell's raw new values
+        if (valid && mur_wall_cell<2>(*m, x, y, z)) keep = mur_cell<2>(g, *m, ts, x, y, z, o, v0, v1, v2, out[0], out[1], out[2]);
+        keep &= mur_z_finish(g, *m, x, y, z, valid, o, v0, v1, out[0], out[1]);
+        if (!valid) keep = 0u;
+    }
+    if (keep & 1u) V[o] = out[0];
+    if (keep & 2u) V[S + o] = out[1];
+    if (keep & 4u) V[2 * S + o] = out[2];
 }
 
 // Engine::UpdateCurrents (FDTD/engine.cpp:170-222) fused with the UPML current hooks
 // (FDTD/extensions/engine_ext_upml.cpp:144-229) for one cell x<Nx-1, y<Ny-1, z<Nz-1.
-template <bool COMPRESSED, bool UPML, bool COHERENT = false>
+template <bool COMPRESSED, bool UPML, bool COHERENT = false, typename IX = unsigned long long>
 __device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsigned y, unsigned z, int rk = -2,
                                               unsigned lk = 0)
 {
-    const unsigned long long S = g.S;
-    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
-    const unsigned long long sx = (unsigned long long)g.Ny * g.Pz;
-    const unsigned long long sy = g.Pz;
+    const IX S = (IX)g.S;
+    const IX o = ((IX)x * g.Ny + y) * g.Pz + z;
+    const IX sx = (IX)g.Ny * g.Pz;
+    const IX sy = g.Pz;
     const float* __restrict__ V = g.V;
     float* __restrict__ I = g.I;
 
-    const float w0 = ldf<COHERENT>(V + o), w1 = ldf<COHERENT>(V + S + o), w2 = ldf<COHERENT>(V + 2 * S + o);
-    const float c0 = fadd(fsub(fsub(w2, ldf<COHERENT>(V + 2 * S + o + sy)), w1), ldf<COHERENT>(V + S + o + 1));
-    const float c1 = fadd(fsub(fsub(w0, ldf<COHERENT>(V + o + 1)), w2), ldf<COHERENT>(V + 2 * S + o + sx));
-    const float c2 = fadd(fsub(fsub(w1, ldf<COHERENT>(V + S + o + sx)), w0), ldf<COHERENT>(V + o + sy));
+    const float w0 = ldf<COHERENT>(V + o), w1 = ldf<COHERENT>(V + (S + o)), w2 = ldf<COHERENT>(V + (2 * S + o));
+    const float c0 = fadd(fsub(fsub(w2, ldf<COHERENT>(V + (2 * S + o + sy))), w1), ldf<COHERENT>(V + (S + o + 1)));
+    const float c1 = fadd(fsub(fsub(w0, ldf<COHERENT>(V + (o + 1))), w2), ldf<COHERENT>(V + (2 * S + o + sx)));
+    const float c2 = fadd(fsub(fsub(w1, ldf<COHERENT>(V + (S + o + sx))), w0), ldf<COHERENT>(V + (o + sy)));
 
     float ii0, ii1, ii2, iv0, iv1, iv2;
     if (COMPRESSED) {
@@ -199,11 +370,11 @@ __device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsi
         const float4 a = __ldg(g.tabI + 2 * c), b = __ldg(g.tabI + 2 * c + 1);
         ii0 = a.x; ii1 = a.y; ii2 = a.z; iv0 = a.w; iv1 = b.x; iv2 = b.y;
     } else {
-        ii0 = __ldg(g.ii + o); ii1 = __ldg(g.ii + S + o); ii2 = __ldg(g.ii + 2 * S + o);
-        iv0 = __ldg(g.iv + o); iv1 = __ldg(g.iv + S + o); iv2 = __ldg(g.iv + 2 * S + o);
+        ii0 = __ldg(g.ii + o); ii1 = __ldg(g.ii + (S + o)); ii2 = __ldg(g.ii + (2 * S + o));
+        iv0 = __ldg(g.iv + o); iv1 = __ldg(g.iv + (S + o)); iv2 = __ldg(g.iv + (2 * S + o));
     }
     float a0, a1, a2;
-    if (COHERENT) { a0 = __ldcg(I + o); a1 = __ldcg(I + S + o); a2 = __ldcg(I + 2 * S + o); }
+    if (COHERENT) { a0 = __ldcg(I + o); a1 = __ldcg(I + (S + o)); a2 = __ldcg(I + (2 * S + o)); }
     else { a0 = I[o]; a1 = I[S + o]; a2 = I[2 * S + o]; }
 
     int r = -1;
@@ -241,24 +412,44 @@ __device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsi
 }
 
 // One thread per cell of an x-plane (blockIdx.y = x), z fastest for coalescing.
-template <bool COMPRESSED, bool UPML>
-__global__ void __launch_bounds__(256) k_update_v(GridDev g)
+// MUR (the update_v_cell modes): with the Mur pre/post hooks; numTS is the device step counter.
+// IX: the type of the cell offsets (32-bit when 3 * S fits, one address instruction per access).
+// Mode 2 decides per warp: a warp without a cell outside the wall windows runs the plain update
+// (the kernel is issue-bound, so the hooks must cost those warps nothing); a warp with one keeps
+// every lane to the end for the shuffles (lanes past the mesh update a clamped cell and store
+// nothing).  Full occupancy needs 32 registers: 8 blocks of 256 threads per SM.
+template <bool COMPRESSED, bool UPML, int MUR = 0, typename IX = unsigned long long>
+__global__ void __launch_bounds__(256, (MUR == 2 ? 8 : 1)) k_update_v(GridDev g, MurDev m,
+                                                                      const unsigned* __restrict__ numTS)
 {
     const unsigned x = blockIdx.y;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned y = t / g.Pz, z = t - y * g.Pz;
-    if (y >= g.Ny || z >= g.Nz) return;
-    update_v_cell<COMPRESSED, UPML>(g, x, y, z);
+    unsigned y = t / g.Pz, z = t - y * g.Pz;
+    const bool valid = y < g.Ny && z < g.Nz;
+    static_assert(!(UPML && MUR == 2), "the clamped lanes of mode 2 would write UPML fluxes");
+    if (MUR == 2) {
+        if (__any_sync(0xffffffffu, valid && mur_wall_cell(m, x, y, z))) {
+            if (!valid) { y = g.Ny - 1; z = g.Nz - 1; }
+            update_v_cell<COMPRESSED, UPML, false, 2, IX>(g, x, y, z, -2, 0, &m, __ldg(numTS), valid);
+            return;
+        }
+        if (!valid) return;
+        update_v_cell<COMPRESSED, UPML, false, 0, IX>(g, x, y, z);
+        return;
+    }
+    if (!valid) return;
+    if (MUR == 1 && mur_wall_cell(m, x, y, z)) update_v_cell<COMPRESSED, UPML, false, 1, IX>(g, x, y, z, -2, 0, &m, __ldg(numTS));
+    else update_v_cell<COMPRESSED, UPML, false, 0, IX>(g, x, y, z);
 }
 
-template <bool COMPRESSED, bool UPML>
+template <bool COMPRESSED, bool UPML, typename IX = unsigned long long>
 __global__ void __launch_bounds__(256) k_update_i(GridDev g)
 {
     const unsigned x = blockIdx.y;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned y = t / g.Pz, z = t - y * g.Pz;
     if (y + 1 >= g.Ny || z + 1 >= g.Nz) return;
-    update_i_cell<COMPRESSED, UPML>(g, x, y, z);
+    update_i_cell<COMPRESSED, UPML, false, IX>(g, x, y, z);
 }
 
 // Work split for meshes with UPML regions: blocks [0, main_blocks) map the cells outside every
@@ -273,9 +464,10 @@ struct SplitDev {
     unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1]) after main
 };
 
-template <bool COMPRESSED, bool CURR>
-__global__ void __launch_bounds__(256) k_update_split(GridDev g, SplitDev sp)
+template <bool COMPRESSED, bool CURR, bool MUR = false>
+__global__ void __launch_bounds__(256) k_update_split(GridDev g, SplitDev sp, MurDev m, const unsigned* __restrict__ numTS)
 {
+
     unsigned b = blockIdx.x;
     if (b < sp.main_blocks) {
         unsigned t = b * 256u + threadIdx.x;
@@ -289,6 +481,7 @@ __global__ void __launch_bounds__(256) k_update_split(GridDev g, SplitDev sp)
             if (upml_find(g, x, y, z, loc) >= 0) return;
         }
         if (CURR) update_i_cell<COMPRESSED, false>(g, x, y, z);
+        else if (MUR && mur_wall_cell(m, x, y, z)) update_v_cell<COMPRESSED, false, false, 1>(g, x, y, z, -2, 0, &m, __ldg(numTS));
         else update_v_cell<COMPRESSED, false>(g, x, y, z);
         return;
     }
@@ -304,7 +497,8 @@ __global__ void __launch_bounds__(256) k_update_split(GridDev g, SplitDev sp)
         if (x + 1 >= g.Nx || y + 1 >= g.Ny || z + 1 >= g.Nz) return;
         update_i_cell<COMPRESSED, true>(g, x, y, z, r, loc);
     } else {
-        update_v_cell<COMPRESSED, true>(g, x, y, z, r, loc);
+        if (MUR && mur_wall_cell(m, x, y, z)) update_v_cell<COMPRESSED, true, false, 1>(g, x, y, z, r, loc, &m, __ldg(numTS));
+        else update_v_cell<COMPRESSED, true>(g, x, y, z, r, loc);
     }
 }
 
@@ -337,27 +531,15 @@ static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsig
 }
 
 // ---------------------------------------------------------------------------------------------
-// Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:82-178).  A single launch covers
-// every wall: blockIdx.y = wall, threads over the wall plane [n1][n2].
-struct MurWallDev {
-    int ny, nyP, nyPP;
-    unsigned line, shift, start_ts, n1, n2;
-    const float* cP;
-    const float* cPP;
-    float* bP;
-    float* bPP;
-};
-struct MurDev {
-    int nwall;
-    MurWallDev w[OEMS_MAX_MUR];
-};
-
+// Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:83-178) as separate launches: phase
+// 0 = pre (before the voltage update), 1 = post (after it), 2 = apply (after the dispersive apply
+// hooks).  With the hooks inside the voltage update (mur_cell / mur_z_*) only phase 2 runs.  A
+// single launch covers every wall: blockIdx.y = wall, threads over the wall plane [n1][n2].
 __device__ __forceinline__ unsigned long long mur_off(const GridDev& g, int comp, const unsigned p[3])
 {
     return (unsigned long long)comp * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2];
 }
 
-// phase 0 = pre (before the V update), 1 = post (after), 2 = apply
 static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __restrict__ numTS)
 {
     const int wi = blockIdx.y;
@@ -381,22 +563,26 @@ static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __r
     if (phase == 0) {
         w.bP[k] = fsub(V[mur_off(g, w.nyP, ps)], fmul(w.cP[k], V[mur_off(g, w.nyP, pos)]));
         w.bPP[k] = fsub(V[mur_off(g, w.nyPP, ps)], fmul(w.cPP[k], V[mur_off(g, w.nyPP, pos)]));
-    } else if (phase == 1) {
+        return;
+    }
+    if (phase == 1) {
         w.bP[k] = fadd(w.bP[k], fmul(w.cP[k], V[mur_off(g, w.nyP, ps)]));
         w.bPP[k] = fadd(w.bPP[k], fmul(w.cPP[k], V[mur_off(g, w.nyPP, ps)]));
-    } else {
-        // walls are applied in reverse insertion order, so on shared edges the wall with the
-        // lowest index is the last writer; skip components a lower active wall also writes
-        bool wP = true, wPP = true;
-        for (int q = 0; q < wi; ++q) {
-            const MurWallDev& o = m.w[q];
-            if (ts < o.start_ts || pos[o.ny] != o.line) continue;
-            if (w.nyP != o.ny) wP = false;
-            if (w.nyPP != o.ny) wPP = false;
-        }
-        if (wP) V[mur_off(g, w.nyP, pos)] = w.bP[k];
-        if (wPP) V[mur_off(g, w.nyPP, pos)] = w.bPP[k];
+        return;
     }
+    // a direct column of the lane-parallel z-wall form holds its final value already
+    if (m.lanes && w.ny == 2 && mur_z_direct(m, g.Pz, pos[0], pos[1], w.line, w.shift)) return;
+    // walls are applied in reverse insertion order, so on shared edges the wall with the
+    // lowest index is the last writer; skip components a lower active wall also writes
+    bool wP = true, wPP = true;
+    for (int q = 0; q < wi; ++q) {
+        const MurWallDev& o = m.w[q];
+        if (ts < o.start_ts || pos[o.ny] != o.line) continue;
+        if (w.nyP != o.ny) wP = false;
+        if (w.nyPP != o.ny) wPP = false;
+    }
+    if (wP) V[mur_off(g, w.nyP, pos)] = w.bP[k];
+    if (wPP) V[mur_off(g, w.nyPP, pos)] = w.bPP[k];
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -404,6 +590,7 @@ static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __r
 // Engine_Ext_Dispersive apply hooks (engine_ext_dispersive.cpp:76-127) for one order.
 struct LorDev {
     unsigned count;
+    const unsigned char* skip;       // optional: bit n set = the apply leaves component n alone
     const unsigned long long* off;   // field offset of component 0 at each position
     int lor;                         // Lorentz pole term on
     const float* c_int;              // [3][count]
@@ -441,8 +628,10 @@ static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= l.count) return;
     const unsigned long long o = l.off[i];
+    const unsigned sk = l.skip ? l.skip[i] : 0u;
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
+        if (sk & (1u << n)) continue;
         const unsigned long long q = o + n * S;
         F[q] = fsub(F[q], l.ade[n * l.count + i]);
     }

@@ -42,6 +42,8 @@ CASES = [
     ("mixed", configs.small_mixed, 200),
     ("mixed_bc2", lambda: configs.small_mixed(bc=(0, 1, 2, 0, 3, 3), seed=3, steps=180), 180),
     ("mixed_mur_all", lambda: configs.small_mixed(bc=(2, 2, 2, 2, 2, 2), seed=5, steps=160), 160),
+    ("mur_corners", configs.mur_corners, 600),
+    ("mur_corners_lanes", lambda: configs.mur_corners(n=(16, 14, 33), wall_source=False, steps=300), 300),
     ("cube40", lambda: configs.plain_cube(n=40, steps=400), 400),
     ("stress_small", lambda: configs.stress(shape=(40, 36, 30), steps=150, nblocks=16), 150),
     ("patch_small", lambda: configs.patch(shape=(56, 52, 36), steps=250), 250),
@@ -71,6 +73,23 @@ def test_fused_step_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, st
     op = fn()
     g, r = _run_pair(op, steps, chunks=(1, 7, 16, 33))
     assert g.launches_per_step() == 2                      # fused step + processing
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, (name, bad)
+
+
+@pytest.mark.parametrize("name,fn,steps", [c for c in CASES if c[0] in ("smoke", "mixed", "mixed_mur_all", "mur_corners",
+                                                                        "mur_corners_lanes", "stress_small")])
+def test_separate_mur_hooks_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, steps):
+    """The Mur pre/post hooks as separate launches (OEMS_CUDA_MUR_SEPARATE=1) instead of inside
+    the voltage update: the same fields, bit for bit, with two more launches per step."""
+    op = fn()
+    fused = Engine_CUDA(op, steps)
+    n_fused = fused.launches_per_step()
+    fused.close()
+    monkeypatch.setenv("OEMS_CUDA_MUR_SEPARATE", "1")
+    g, r = _run_pair(op, steps, chunks=(1, 7, 16, 33))
+    assert g.launches_per_step() == n_fused + 2
     res = compare_engines(g, r)
     bad = [k for k, v in res.items() if not v]
     assert not bad, (name, bad)
@@ -229,7 +248,7 @@ def test_launch_accounting(cuda_lib):
     op = configs.small_mixed(steps=20)
     g = Engine_CUDA(op, 20)
     n = g.launches_per_step()
-    # lorentz pre+apply (V), mur x3, update V, excitation V, update I, step_end
+    # lorentz pre+apply (V), update V (+ Mur pre/post), mur apply, excitation V, update I, step_end
     assert n >= 6
     ms, cnt = g.profile(5)
     assert sum(cnt) == 5 * n

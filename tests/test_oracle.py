@@ -31,6 +31,8 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
     ("mixed_pec", lambda: configs.small_mixed(bc=(0, 1, 2, 0, 3, 3), seed=3), 120),
     ("cube", lambda: configs.plain_cube(n=21, steps=200), 200),
     ("stress_small", lambda: configs.stress(shape=(26, 22, 18), steps=120, nblocks=12), 120),
+    ("mur_corners", configs.mur_corners, 600),
+    ("mur_corners_lanes", lambda: configs.mur_corners(n=(16, 14, 33), wall_source=False, steps=300), 300),
 ])
 def test_basic_equals_multithreaded_sse_compressed(name, fn, steps):
     op = fn()
