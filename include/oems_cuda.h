@@ -113,6 +113,24 @@ int oems_cuda_add_lorentz_order(oems_cuda_engine* eng, unsigned int count, const
                                 const float* v_int, const float* v_ext, const float* v_lor,
                                 const float* i_int, const float* i_ext, const float* i_lor);
 
+/* Engine_Ext_TFSF::DoPostVoltageUpdates / DoPostCurrentUpdates (FDTD/extensions/engine_ext_tfsf.cpp:36-215)
+ * fed with Operator_Ext_TFSF's tables (FDTD/extensions/operator_ext_tfsf.h:55-84), flattened to one
+ * term per (face plane, position, component) in the order the reference applies them: directions
+ * n = x, y, z; lower plane before upper; the nP line outer, the nPP line inner; component nP before
+ * nPP. Term k adds to field component dir[k] at cell index[.][k] ([3][count] like the excitation):
+ *   F += (1.0 - delta)*amp*sig[lookup(delay)]  +  delta*amp*sig[lookup(delay + 1)]
+ * with lookup(d) = m_DelayLookup[d] of the reference for the current numTS. The voltage terms add
+ * the current signal sig_curr and the current terms the voltage signal sig_volt, as the reference
+ * does. period = steps per signal period (0 = aperiodic); max_delay = m_maxDelay (every delay must
+ * be below it). Replaces any previous TFSF setup. Engines with a TFSF source run the Mur pre/post
+ * hooks as separate launches (the plane wave is added between the update and the Mur post hook). */
+int oems_cuda_set_tfsf(oems_cuda_engine* eng, unsigned int volt_count, const unsigned int* volt_index,
+                       const unsigned short* volt_dir, const unsigned int* volt_delay, const float* volt_delta,
+                       const float* volt_amp, unsigned int curr_count, const unsigned int* curr_index,
+                       const unsigned short* curr_dir, const unsigned int* curr_delay, const float* curr_delta,
+                       const float* curr_amp, const float* sig_volt, const float* sig_curr, unsigned int length,
+                       unsigned int period, unsigned int max_delay);
+
 /* ---- processing: probes, DFTs, FD field dumps --------------------------------------------- */
 
 /* ProcessVoltage (Common/processvoltage.cpp:38-48) -> Engine_Interface_FDTD::CalcVoltageIntegral

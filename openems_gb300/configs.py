@@ -208,6 +208,55 @@ def mur_corners(n=(16, 14, 12), steps=600, seed=7, wall_source=True):
 
 
 # ------------------------------------------------------------------------------------------
+def plane_wave(n=(28, 24, 26), steps=300, bc=(3,) * 6, pml=5, k_dir=(1.0, 0.0, 0.0), e_dir=(0.0, 0.0, 1.0),
+               frequency=0.0, graded=False, scatterer=True, dispersive=False, box=None, sinus=False, seed=3):
+    """Plane-wave (TFSF, exc_type 10) excitation of a total-field box, as the reference's
+    RCS_Sphere tutorial sets it up (python/Tutorials/RCS_Sphere.py:61-71): a metal brick and a
+    dielectric block inside the box, voltage probes inside and outside it.  ``box`` = (lo, hi)
+    line indices per axis (default: 7 lines in from every wall); a lower index of 0 or an upper
+    index of N-1 turns that face off, as in the reference."""
+    rng = np.random.default_rng(seed)
+    if graded:
+        lines = [np.cumsum(np.concatenate([[0.0], rng.uniform(0.7, 1.3, k - 1)])) for k in n]
+    else:
+        lines = [_uniform(k) for k in n]
+    g = Grid(lines, unit=1e-3)
+    gl = g.lines
+    csx = Structure()
+    exc = Excitation()
+    if sinus:
+        exc.SetupSinusoidal(10e9)
+    else:
+        exc.SetupGaussianPulse(10e9, 8e9)
+    if box is None:
+        box = ([7, 7, 7], [k - 8 for k in n])
+    lo, hi = box
+    pw = csx.AddExcitation("plane_wave", 10, list(e_dir))
+    pw.SetPropagationDir(list(k_dir))
+    if frequency:
+        pw.SetFrequency(frequency)
+    pw.AddBox([gl[a][lo[a]] for a in range(3)], [gl[a][hi[a]] for a in range(3)])
+    mid = [gl[a][(lo[a] + hi[a]) // 2] for a in range(3)]
+    if scatterer:
+        csx.AddMetal("brick").AddBox([mid[0] + 1.0, mid[1] - 2.0, mid[2] - 2.0], [mid[0] + 2.0, mid[1] + 2.0, mid[2] + 2.0],
+                                     priority=10)
+        csx.AddMaterial("diel", epsilon=4.0, kappa=0.05).AddBox([mid[0] - 4.0, mid[1] - 3.0, mid[2] - 3.0],
+                                                               [mid[0] - 1.0, mid[1] + 1.0, mid[2] + 3.0])
+    if dispersive:
+        csx.AddLorentzMaterial("drude", epsilon=1.2, eps_plasma_freq=[8e9], eps_relax_time=[1e-9]).AddBox(
+            [gl[0][lo[0] + 1], gl[1][lo[1] + 1], gl[2][lo[2] + 1]], [gl[0][lo[0] + 4], gl[1][hi[1] - 1], gl[2][lo[2] + 4]],
+            priority=5)
+    # probes: one z-line inside the total-field box, one in the scattered-field region
+    zi = (lo[2] + hi[2]) // 2
+    xi = lo[0] + 2
+    yi = (lo[1] + hi[1]) // 2
+    csx.AddProbe("ut_inside", 0, interval=1).AddBox([gl[0][xi], gl[1][yi], gl[2][zi]], [gl[0][xi], gl[1][yi], gl[2][zi + 1]])
+    xo = max(lo[0] - 2, 1)
+    csx.AddProbe("ut_outside", 0, interval=1).AddBox([gl[0][xo], gl[1][yi], gl[2][zi]], [gl[0][xo], gl[1][yi], gl[2][zi + 1]])
+    op = Operator(csx, g, exc, bc=bc, pml_size=(pml,) * 6)
+    return op.build(steps)
+
+
 def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
     """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""
     nx, ny, nz = shape

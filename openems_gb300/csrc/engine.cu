@@ -368,6 +368,49 @@ int oems_cuda_set_excitation(oems_cuda_engine* e, unsigned int nV, const unsigne
     return OEMS_OK;
 }
 
+static int tfsf_terms(oems_cuda_engine* e, unsigned n, const unsigned* idx, const unsigned short* dir,
+                      const unsigned* delay, const float* delta, const float* amp, unsigned max_delay, TfsfHost& t)
+{
+    if (n && (!idx || !dir || !delay || !delta || !amp)) return fail(e, OEMS_ERR_ARG, "TFSF arrays missing");
+    t = TfsfHost{};
+    for (unsigned k = 0; k < n; ++k) {
+        const unsigned x = idx[k], y = idx[n + k], z = idx[2 * (size_t)n + k];
+        if (x >= e->N[0] || y >= e->N[1] || z >= e->N[2] || dir[k] > 2)
+            return fail(e, OEMS_ERR_ARG, "TFSF index out of range");
+        // the reference's delay lookup table has max_delay + 1 entries and is read at delay + 1
+        if (delay[k] >= max_delay) return fail(e, OEMS_ERR_ARG, "TFSF delay exceeds max_delay");
+        t.off.push_back(cell_off(e, dir[k], x, y, z));
+    }
+    t.delay.assign(delay, delay + n);
+    t.delta.assign(delta, delta + n);
+    t.amp.assign(amp, amp + n);
+    return OEMS_OK;
+}
+
+int oems_cuda_set_tfsf(oems_cuda_engine* e, unsigned int volt_count, const unsigned int* volt_index,
+                       const unsigned short* volt_dir, const unsigned int* volt_delay, const float* volt_delta,
+                       const float* volt_amp, unsigned int curr_count, const unsigned int* curr_index,
+                       const unsigned short* curr_dir, const unsigned int* curr_delay, const float* curr_delta,
+                       const float* curr_amp, const float* sig_volt, const float* sig_curr, unsigned int length,
+                       unsigned int period, unsigned int max_delay)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if (length == 0 || !sig_volt || !sig_curr) return fail(e, OEMS_ERR_ARG, "TFSF signal missing");
+    if (period > length) return fail(e, OEMS_ERR_ARG, "TFSF signal period longer than the signal");
+    int rc;
+    if ((rc = tfsf_terms(e, volt_count, volt_index, volt_dir, volt_delay, volt_delta, volt_amp, max_delay, e->tfsf_v)))
+        return rc;
+    if ((rc = tfsf_terms(e, curr_count, curr_index, curr_dir, curr_delay, curr_delta, curr_amp, max_delay, e->tfsf_i)))
+        return rc;
+    e->tfsf_sig_v.assign(sig_volt, sig_volt + length);
+    e->tfsf_sig_i.assign(sig_curr, sig_curr + length);
+    e->tfsf_len = length;
+    e->tfsf_period = period;
+    e->has_tfsf = volt_count || curr_count;
+    return OEMS_OK;
+}
+
 int oems_cuda_add_upml(oems_cuda_engine* e, const unsigned int start[3], const unsigned int nl[3], const float* vv,
                        const float* vvfo, const float* vvfn, const float* ii, const float* iifo, const float* iifn)
 {
@@ -667,6 +710,11 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     launch_update(e, false, s);
     post();
     ++L;
+    if (e->tfsfV.ntarget) {
+        pre(OEMS_KC_EXCITE);
+        k_tfsf<<<(e->tfsfV.ntarget + 255) / 256, blk, 0, s>>>(e->dV, e->tfsfV, e->d_numTS);
+        post(); ++L;
+    }
     if (mur_sep) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 1, e->d_numTS); post(); ++L; }
     for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
     if (!e->mur.empty()) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 2, e->d_numTS); post(); ++L; }
@@ -677,6 +725,11 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     launch_update(e, true, s);
     post();
     ++L;
+    if (e->tfsfI.ntarget) {
+        pre(OEMS_KC_EXCITE);
+        k_tfsf<<<(e->tfsfI.ntarget + 255) / 256, blk, 0, s>>>(e->dI, e->tfsfI, e->d_numTS);
+        post(); ++L;
+    }
     for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
     if (e->excI.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excI.count + 127) / 128, 128, 0, s>>>(e->dI, e->excI, e->d_numTS); post(); ++L; }
     // ---- processing + numTS
@@ -881,13 +934,56 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         }
         std::sort(zs.begin(), zs.end());
         if (md.nz >= 0 && std::adjacent_find(zs.begin(), zs.end()) != zs.end()) md.nz = -1;
-        // OEMS_CUDA_MUR_SEPARATE=1: the pre/post hooks as separate launches (k_mur phases 0/1)
+        // OEMS_CUDA_MUR_SEPARATE=1: the pre/post hooks as separate launches (k_mur phases 0/1).
+        // A TFSF plane wave needs them too: its post-voltage hook (priority 5e4) runs before the
+        // Mur post hook (priority 0) and may change the values Mur reads at a shift line.
         const char* ms = getenv("OEMS_CUDA_MUR_SEPARATE");
-        e->mur_separate = ms && ms[0] == '1';
+        e->mur_separate = (ms && ms[0] == '1') || e->has_tfsf;
         // the lane-parallel form: no UPML (plain update kernel), every wall active from step 0
         bool always = true;
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
         md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
+    }
+
+    // TFSF: group the terms by target cell (stable, so each cell keeps the reference's order)
+    if (e->has_tfsf) {
+        float *sv, *si;
+        if ((rc = dupload(e, &sv, e->tfsf_sig_v.data(), e->tfsf_sig_v.size()))) return rc;
+        if ((rc = dupload(e, &si, e->tfsf_sig_i.data(), e->tfsf_sig_i.size()))) return rc;
+        for (int w = 0; w < 2; ++w) {
+            const TfsfHost& t = w ? e->tfsf_i : e->tfsf_v;
+            TfsfDev& d = w ? e->tfsfI : e->tfsfV;
+            d = TfsfDev{};
+            d.sig = w ? sv : si;   // the voltage hook adds the current signal and vice versa
+            d.length = e->tfsf_len;
+            d.period = e->tfsf_period;
+            const size_t n = t.off.size();
+            if (!n) continue;
+            std::vector<unsigned> order(n);
+            for (size_t k = 0; k < n; ++k) order[k] = (unsigned)k;
+            std::stable_sort(order.begin(), order.end(), [&](unsigned a, unsigned b) { return t.off[a] < t.off[b]; });
+            std::vector<unsigned long long> toff;
+            std::vector<unsigned> first, dl;
+            std::vector<float> dd, am;
+            for (size_t q = 0; q < n; ++q) {
+                const unsigned k = order[q];
+                if (toff.empty() || toff.back() != t.off[k]) { toff.push_back(t.off[k]); first.push_back((unsigned)q); }
+                dl.push_back(t.delay[k]);
+                dd.push_back(t.delta[k]);
+                am.push_back(t.amp[k]);
+            }
+            first.push_back((unsigned)n);
+            unsigned long long* o;
+            unsigned *f, *de;
+            float *dt, *ap;
+            if ((rc = dupload(e, &o, toff.data(), toff.size()))) return rc;
+            if ((rc = dupload(e, &f, first.data(), first.size()))) return rc;
+            if ((rc = dupload(e, &de, dl.data(), dl.size()))) return rc;
+            if ((rc = dupload(e, &dt, dd.data(), dd.size()))) return rc;
+            if ((rc = dupload(e, &ap, am.data(), am.size()))) return rc;
+            d.ntarget = (unsigned)toff.size();
+            d.off = o; d.first = f; d.delay = de; d.delta = dt; d.amp = ap;
+        }
     }
 
     // Lorentz / Drude orders
@@ -1097,7 +1193,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     // separate update kernels on GB300, so it is not the default.
     {
         const char* env = getenv("OEMS_CUDA_FUSED");
-        e->use_fused = env && env[0] == '1' && e->mur.empty() && e->lor.empty() &&
+        e->use_fused = env && env[0] == '1' && e->mur.empty() && e->lor.empty() && !e->has_tfsf &&
                        e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC && e->K % 2 == 0 &&
                        3ull * e->S < (1ull << 32);        // the staged-plane offsets are 32-bit
         if (e->use_fused && (rc = setup_fused(e))) return rc;

@@ -40,6 +40,12 @@ struct ProbeHost {
     unsigned fd_interval = 0;
     std::vector<double> freqs;
 };
+struct TfsfHost {
+    // terms in the reference's application order: target offset, delay, delta, amp
+    std::vector<unsigned long long> off;
+    std::vector<unsigned> delay;
+    std::vector<float> delta, amp;
+};
 struct DumpHost {
     int field;
     unsigned start[3], stop[3];
@@ -89,6 +95,11 @@ struct oems_cuda_engine {
     std::vector<LorHost> lor;
     std::vector<ProbeHost> probes;
     std::vector<DumpHost> dumps;
+    // TFSF plane wave (one per engine, as Operator_Ext_TFSF builds one)
+    bool has_tfsf = false;
+    TfsfHost tfsf_v, tfsf_i;
+    std::vector<float> tfsf_sig_v, tfsf_sig_i;
+    unsigned tfsf_len = 0, tfsf_period = 0;
 
     // device state after init
     bool inited = false;
@@ -98,6 +109,7 @@ struct oems_cuda_engine {
     unsigned host_numTS = 0;
     GridDev grid{};
     ExcDev excV{}, excI{};
+    TfsfDev tfsfV{}, tfsfI{};
     MurDev murdev{};
     std::vector<LorDev> lorV, lorI;
     StepEndDev stepend{};

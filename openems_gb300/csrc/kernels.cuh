@@ -531,6 +531,57 @@ static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsig
 }
 
 // ---------------------------------------------------------------------------------------------
+// Engine_Ext_TFSF::DoPostVoltageUpdates / DoPostCurrentUpdates (engine_ext_tfsf.cpp:36-215): the
+// incident plane wave added on the faces of the total-field box.  The host groups the reference's
+// term list by target cell (terms of one cell keep their reference order; at most one term per
+// face plane tangential to the component), so one thread owns one cell and no two threads touch
+// the same value.  The arithmetic follows the reference's C++ promotion exactly:
+//   V + (1.0 - dd)*amp*sig[a]   (double)   + dd*amp*sig[b]   (float product, added in double)
+// and the sum is rounded to float once per term, as each SetVolt/SetCurr stores a float.
+struct TfsfDev {
+    unsigned ntarget;
+    const unsigned long long* off;   // linear field offset (component included) of each target
+    const unsigned* first;           // terms of target k: [first[k], first[k+1])
+    const unsigned* delay;
+    const float* delta;
+    const float* amp;
+    const float* sig;                // current signal in the voltage hook, voltage signal in the current hook
+    unsigned length;
+    unsigned period;                 // 0 = aperiodic
+};
+
+// m_DelayLookup[d] of the reference for the step numTS = ts
+__device__ __forceinline__ unsigned tfsf_lookup(unsigned ts, unsigned d, unsigned length, unsigned period)
+{
+    unsigned v;
+    if (ts < d) v = 0;
+    else if (ts - d >= length && period == 0) v = 0;
+    else v = ts - d;
+    if (period > 0) v %= period;
+    return v;
+}
+
+static __global__ void k_tfsf(float* __restrict__ F, TfsfDev t, const unsigned* __restrict__ numTS)
+{
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= t.ntarget) return;
+    const unsigned ts = *numTS;
+    const unsigned long long o = t.off[k];
+    float v = F[o];
+    const unsigned q1 = t.first[k + 1];
+    for (unsigned q = t.first[k]; q < q1; ++q) {
+        const unsigned d = t.delay[q];
+        const float dd = t.delta[q], a = t.amp[q];
+        const float s0 = t.sig[tfsf_lookup(ts, d, t.length, t.period)];
+        const float s1 = t.sig[tfsf_lookup(ts, d + 1, t.length, t.period)];
+        const double A = __dmul_rn(__dmul_rn(__dsub_rn(1.0, (double)dd), (double)a), (double)s0);
+        const float B = __fmul_rn(__fmul_rn(dd, a), s1);
+        v = __double2float_rn(__dadd_rn(__dadd_rn((double)v, A), (double)B));
+    }
+    F[o] = v;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:83-178) as separate launches: phase
 // 0 = pre (before the voltage update), 1 = post (after it), 2 = apply (after the dispersive apply
 // hooks).  With the hooks inside the voltage update (mur_cell / mur_z_*) only phase 2 runs.  A

@@ -93,6 +93,19 @@ class EngineBase:
             self._ck(L.add_lorentz_order(self.h, pos.shape[1], _p(pos, C.c_uint), int(o.volt_ade_on),
                                          int(o.curr_ade_on), int(o.volt_lor_on), int(o.curr_lor_on),
                                          *[_p(a, C.c_float) for a in t]), "add_lorentz_order")
+        t = getattr(op, "tfsf", None)
+        if t is not None:
+            a = [self._a(t.volt_index, np.uint32), self._a(t.volt_dir, np.uint16), self._a(t.volt_delay, np.uint32),
+                 self._a(t.volt_delta, f32), self._a(t.volt_amp, f32)]
+            b = [self._a(t.curr_index, np.uint32), self._a(t.curr_dir, np.uint16), self._a(t.curr_delay, np.uint32),
+                 self._a(t.curr_delta, f32), self._a(t.curr_amp, f32)]
+            ctypes_of = (C.c_uint, C.c_ushort, C.c_uint, C.c_float, C.c_float)
+            sv = self._a(t.signal_volt, f32)
+            sc = self._a(t.signal_curr, f32)
+            self._ck(L.set_tfsf(self.h, a[4].size, *[_p(x, ct) for x, ct in zip(a, ctypes_of)],
+                                b[4].size, *[_p(x, ct) for x, ct in zip(b, ctypes_of)],
+                                _p(sv, C.c_float), _p(sc, C.c_float), sv.size, int(t.period), int(t.max_delay)),
+                     "set_tfsf")
         for p in op.vprobes:
             pid = C.c_int(-1)
             s = self._a(p.start, np.uint32)

@@ -67,6 +67,15 @@ class Property:
         self.structure._add_box(self, np.asarray(start, float), np.asarray(stop, float), priority)
         return self
 
+    # plane-wave excitation (exc_type 10) parameters, named like CSPropExcitation's setters
+    def SetPropagationDir(self, val):
+        self.params["prop_dir"] = np.asarray(val, float)
+        return self
+
+    def SetFrequency(self, val):
+        self.params["frequency"] = float(val)
+        return self
+
 
 class Structure:
     """Holds properties and their box primitives (the subset of CSXCAD used by the engine path)."""
@@ -212,6 +221,39 @@ class LorentzOrder:
 
 
 @dataclass
+class TFSFTable:
+    """Operator_Ext_TFSF (FDTD/extensions/operator_ext_tfsf.h:55-84), flattened.
+
+    ``volt_*`` / ``curr_*`` hold one term per (face, position, component) in the order
+    Engine_Ext_TFSF::DoPostVoltageUpdates / DoPostCurrentUpdates apply them
+    (engine_ext_tfsf.cpp:36-215): faces n = x, y, z, lower plane before upper, positions with
+    the nP line outer and the nPP line inner, component nP before nPP.  ``index`` [3, K] is the
+    cell, ``dir`` the field component, ``delay``/``delta``/``amp`` the reference's
+    m_*Delay / m_*DelayDelta / m_*Amp entries.  ``max_delay`` is m_maxDelay (already +1)."""
+    start: np.ndarray
+    stop: np.ndarray
+    active: np.ndarray            # bool [3, 2]: lower/upper plane of each direction
+    prop_dir: np.ndarray
+    e_amp: np.ndarray
+    h_amp: np.ndarray
+    phase_velocity: float
+    max_delay: int
+    volt_index: np.ndarray
+    volt_dir: np.ndarray
+    volt_delay: np.ndarray
+    volt_delta: np.ndarray
+    volt_amp: np.ndarray
+    curr_index: np.ndarray
+    curr_dir: np.ndarray
+    curr_delay: np.ndarray
+    curr_delta: np.ndarray
+    curr_amp: np.ndarray
+    signal_volt: np.ndarray
+    signal_curr: np.ndarray
+    period: int = 0
+
+
+@dataclass
 class VoltageProbe:
     name: str
     start: np.ndarray
@@ -269,6 +311,7 @@ class OperatorData:
     nyquist: int = 0
     excitation: Optional[Excitation] = None
     grid: Optional[Grid] = None
+    tfsf: Optional[TFSFTable] = None
 
 
 # =========================================================================================
@@ -824,6 +867,9 @@ class Operator:
         self._apply_magnetic_bc([b == 1 for b in self.bc])
 
         exc = self._build_excitation()
+        # Operator_Ext_TFSF is added right after the excitation extension (openems.cpp:1186-1188)
+        # and built in that order, so it reads vi/iv before any later extension rewrites them
+        tfsf = self._build_tfsf()
         mur = self._build_mur(exc)
         upml = self._build_upml()
         lorentz = self._build_lorentz()
@@ -831,7 +877,7 @@ class Operator:
         data = OperatorData(num_lines=self.N.astype(np.uint32), dt=dT, vv=self.vv, vi=self.vi, ii=self.ii,
                             iv=self.iv, exc=exc, upml=upml, mur=mur, lorentz=lorentz, vprobes=vprobes,
                             iprobes=iprobes, dumps=dumps, nyquist=self.exc.GetNyquistNum(),
-                            excitation=self.exc, grid=self.grid)
+                            excitation=self.exc, grid=self.grid, tfsf=tfsf)
         return data
 
     # ---- boundary conditions ---------------------------------------------------------------
@@ -1014,6 +1060,239 @@ class Operator:
         ci_, cd, ca, cdl = pack(crec)
         return ExcitationTable(vi_, vd, va, vdl, ci_, cd, ca, cdl, self.exc.volt.copy(), self.exc.curr.copy(),
                                self.exc.period_steps())
+
+    # ---- TFSF plane wave (operator_ext_tfsf.cpp:84-406) ----------------------------------------
+    def _disc_line(self, n, pos, dual=False):
+        """GetDiscLine (FDTD/operator.cpp:144-157); 0.0 outside the mesh, as there."""
+        if pos < 0 or pos >= self.N[n]:
+            return 0.0
+        return float(self.dl[n][pos] if dual else self.L[n][pos])
+
+    def _edge_length(self, n, pos, dual=False):
+        """GetEdgeLength (FDTD/operator.cpp:212-215) = GetDiscDelta * gridDelta."""
+        p = pos[n]
+        if p < 0 or p >= self.N[n]:
+            return 0.0
+        return float((self.dd[n][p] if dual else self.md[n][p]) * self.unit)
+
+    def _yee_coords(self, ny, pos, dual):
+        """GetYeeCoords (FDTD/operator.cpp:182-201), coordinates only."""
+        c = [self._disc_line(k, pos[k], dual) for k in range(3)]
+        c[ny] = self._disc_line(ny, pos[ny], not dual)
+        return c
+
+    def numeric_phase_velocity(self, start, stop, prop_dir, freq):
+        """Operator::CalcNumericPhaseVelocity (FDTD/operator.cpp:2150-2215).  ``freq`` is rounded
+        to float first, as the reference's signature takes a float."""
+        freq = float(np.float32(freq))
+        dT = self.dT
+        c0 = C0 / math.sqrt(self.bg["epsilon"] * self.bg["mue"])
+        avg = [abs(self._disc_line(n, int(start[n])) - self._disc_line(n, int(stop[n]))) * self.unit
+               / abs(float(int(stop[n]) - int(start[n]))) for n in range(3)]
+        for n in range(3):
+            nP, nPP = (n + 1) % 3, (n + 2) % 3
+            if abs(prop_dir[n]) == 1 and prop_dir[nP] == 0 and prop_dir[nPP] == 0:
+                # the reference uses the x-axis mean delta for every Cartesian direction
+                kx = math.asin(avg[0] / c0 / dT * math.sin(2 * PI * freq * dT / 2)) * 2 / avg[0]
+                return 2 * PI * freq / kx
+        k0 = 2 * PI * freq / c0
+        k = k0
+        rhs = math.pow(math.sin(2 * PI * freq * dT / 2) / c0 / dT, 2)
+        old_phv, phv, it = 0.0, c0, 0
+        while abs(old_phv - phv) > 1e-6:
+            it += 1
+            old_phv = phv
+            fk = 0.0
+            fdk = 0.0
+            for n in range(3):
+                fk += math.pow(math.sin(prop_dir[n] * k * avg[n] / 2) / avg[n], 2)
+                fdk += prop_dir[n] * math.sin(prop_dir[n] * k * avg[n] / 2) * math.cos(prop_dir[n] * k * avg[n] / 2) / avg[n]
+            fk -= rhs
+            k -= fk / fdk
+            if k < k0:
+                k = k0
+            phv = 2 * PI * freq / k
+            if it > 99:
+                break
+        return phv
+
+    def _build_tfsf(self):
+        """Operator_Ext_TFSF::BuildExtension (operator_ext_tfsf.cpp:84-406): the first plane-wave
+        excitation (exc_type 10) with exactly one box.  Returns None when there is none, like
+        the reference's SetActive(false); raises where the reference rejects the setup."""
+        ft = self.ft
+        for prop in self.csx.props:
+            if prop.kind != EXCITATION or prop.params.get("exc_type") != 10:
+                continue
+            if len(prop.boxes) != 1:
+                continue   # "more (or less) than one primitive, skipping"
+            rec = prop.boxes[0]
+            d = np.asarray(prop.params.get("prop_dir", (0.0, 0.0, 0.0)), float)
+            d = [float(v) for v in d]
+            norm = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+            if norm == 0:
+                raise ValueError("TFSF: plane wave direction is zero")
+            d = [d[0] / norm, d[1] / norm, d[2] / norm]
+            dim, St, Sp, _, _ = self.snap_box(rec[5], rec[6])
+            if dim != 3:
+                raise ValueError("TFSF: plane wave box dimension is invalid")
+            St = [int(v) for v in St]
+            Sp = [int(v) for v in Sp]
+            ref_index = math.sqrt(self.bg["epsilon"] * self.bg["mue"])
+            freq = float(prop.params.get("frequency", 0.0))
+            if freq <= 0:
+                phv = C0 / ref_index
+            else:
+                phv = self.numeric_phase_velocity(St, Sp, d, freq)
+            if phv < 0 or phv > C0 / ref_index or math.isnan(phv):
+                phv = C0 / ref_index
+            E = [float(v) for v in prop.params["exc_val"]]
+            nl = [Sp[n] - St[n] + 1 for n in range(3)]
+            active = np.zeros((3, 2), bool)
+            origin = [0.0] * 3
+            for n in range(3):
+                active[n, 0] = St[n] != 0
+                active[n, 1] = Sp[n] != int(self.N[n]) - 1
+                ui = St[n] - 1 if d[n] >= 0 else Sp[n] + 1   # -1 wraps to an unsigned index: 0.0
+                origin[n] = self._disc_line(n, ui)
+            dotEk = E[0] * d[0] + E[1] * d[1] + E[2] * d[2]
+            angle = math.acos(dotEk / (E[0] * E[0] + E[1] * E[1] + E[2] * E[2])) / PI * 180
+            if angle == 0:
+                raise ValueError("TFSF: plane wave direction and polarization are identical")
+            if angle != 90:
+                E = [E[n] - d[n] * dotEk for n in range(3)]
+            H = [0.0] * 3
+            for n in range(3):
+                nP, nPP = (n + 1) % 3, (n + 2) % 3
+                H[n] = d[nP] * E[nPP] - d[nPP] * E[nP]
+                H[n] /= Z0 * math.sqrt(self.bg["mue"] / self.bg["epsilon"])
+            unit, dT = self.unit, self.dT
+
+            def dist_delay(ny, pos, dual, extra):
+                c = self._yee_coords(ny, pos, dual)
+                dist = abs((c[0] - origin[0]) * d[0]) + abs((c[1] - origin[1]) * d[1]) + abs((c[2] - origin[2]) * d[2])
+                return dist * unit / phv / dT + extra
+
+            max_delay = 0
+            # per (n, l, c): lists of (delay, delta, amp) in ui_pos order
+            vt = {}
+            ct = {}
+            for n in range(3):
+                nP, nPP = (n + 1) % 3, (n + 2) % 3
+                if not active[n, 0] and not active[n, 1]:
+                    continue
+                numP = nl[nP] * nl[nPP]
+                for l in range(2):
+                    for c in range(2):
+                        if active[n, l]:
+                            vt[n, l, c] = [np.zeros(numP, np.uint32), np.zeros(numP, ft), np.zeros(numP, ft)]
+                            ct[n, l, c] = [np.zeros(numP, np.uint32), np.zeros(numP, ft), np.zeros(numP, ft)]
+                pos = [0, 0, 0]
+                pos[nP] = St[nP]
+                ui = 0
+                for i in range(nl[nP]):
+                    pos[nPP] = St[nPP]
+                    for j in range(nl[nPP]):
+                        def put(tab, key, delay, amp):
+                            nonlocal max_delay
+                            max_delay = max(int(delay), max_delay)
+                            fl = math.floor(delay)
+                            tab[key][0][ui] = int(fl)
+                            tab[key][1][ui] = ft(delay - fl)
+                            tab[key][2][ui] = ft(amp)
+                        # current updates
+                        pos[n] = St[n]
+                        if active[n, 0]:
+                            put(ct, (n, 0, 1), dist_delay(nP, pos, False, 0.0), E[nP] * self._edge_length(nP, pos))
+                            put(ct, (n, 0, 0), dist_delay(nPP, pos, False, 0.0), E[nPP] * self._edge_length(nPP, pos))
+                            pos[n] -= 1
+                            ct[n, 0, 0][2][ui] = ft(ct[n, 0, 0][2][ui] * self.iv[nP, pos[0], pos[1], pos[2]])
+                            ct[n, 0, 1][2][ui] = ft(ct[n, 0, 1][2][ui] * self.iv[nPP, pos[0], pos[1], pos[2]])
+                        if active[n, 1]:
+                            pos[n] = Sp[n]
+                            put(ct, (n, 1, 1), dist_delay(nP, pos, False, 0.0), E[nP] * self._edge_length(nP, pos))
+                            put(ct, (n, 1, 0), dist_delay(nPP, pos, False, 0.0), E[nPP] * self._edge_length(nPP, pos))
+                            ct[n, 1, 0][2][ui] = ft(ct[n, 1, 0][2][ui] * self.iv[nP, pos[0], pos[1], pos[2]])
+                            ct[n, 1, 1][2][ui] = ft(ct[n, 1, 1][2][ui] * self.iv[nPP, pos[0], pos[1], pos[2]])
+                        if active[n, 0]:
+                            ct[n, 0, 0][2][ui] = -ct[n, 0, 0][2][ui]
+                        if active[n, 1]:
+                            ct[n, 1, 1][2][ui] = -ct[n, 1, 1][2][ui]
+                        if pos[nP] == Sp[nP]:
+                            if active[n, 0]:
+                                ct[n, 0, 1][2][ui] = 0
+                            if active[n, 1]:
+                                ct[n, 1, 1][2][ui] = 0
+                        if pos[nPP] == Sp[nPP]:
+                            if active[n, 0]:
+                                ct[n, 0, 0][2][ui] = 0
+                            if active[n, 1]:
+                                ct[n, 1, 0][2][ui] = 0
+                        # voltage updates
+                        pos[n] = St[n] - 1
+                        if active[n, 0]:
+                            put(vt, (n, 0, 1), dist_delay(nP, pos, True, 1.0), H[nP] * self._edge_length(nP, pos, True))
+                            put(vt, (n, 0, 0), dist_delay(nPP, pos, True, 1.0), H[nPP] * self._edge_length(nPP, pos, True))
+                            pos[n] += 1
+                            vt[n, 0, 0][2][ui] = ft(vt[n, 0, 0][2][ui] * self.vi[nP, pos[0], pos[1], pos[2]])
+                            vt[n, 0, 1][2][ui] = ft(vt[n, 0, 1][2][ui] * self.vi[nPP, pos[0], pos[1], pos[2]])
+                        pos[n] = Sp[n]
+                        if active[n, 1]:
+                            put(vt, (n, 1, 1), dist_delay(nP, pos, True, 1.0), H[nP] * self._edge_length(nP, pos, True))
+                            put(vt, (n, 1, 0), dist_delay(nPP, pos, True, 1.0), H[nPP] * self._edge_length(nPP, pos, True))
+                            vt[n, 1, 0][2][ui] = ft(vt[n, 1, 0][2][ui] * self.vi[nP, pos[0], pos[1], pos[2]])
+                            vt[n, 1, 1][2][ui] = ft(vt[n, 1, 1][2][ui] * self.vi[nPP, pos[0], pos[1], pos[2]])
+                        if active[n, 1]:
+                            vt[n, 1, 0][2][ui] = -vt[n, 1, 0][2][ui]
+                        if active[n, 0]:
+                            vt[n, 0, 1][2][ui] = -vt[n, 0, 1][2][ui]
+                        if pos[nP] == Sp[nP]:
+                            if active[n, 0]:
+                                vt[n, 0, 0][2][ui] = 0
+                            if active[n, 1]:
+                                vt[n, 1, 0][2][ui] = 0
+                        if pos[nPP] == Sp[nPP]:
+                            if active[n, 0]:
+                                vt[n, 0, 1][2][ui] = 0
+                            if active[n, 1]:
+                                vt[n, 1, 1][2][ui] = 0
+                        pos[nPP] += 1
+                        ui += 1
+                    pos[nP] += 1
+            max_delay += 1
+            volt = self._tfsf_terms(vt, St, Sp, nl, active, False)
+            curr = self._tfsf_terms(ct, St, Sp, nl, active, True)
+            return TFSFTable(np.array(St, np.uint32), np.array(Sp, np.uint32), active, np.array(d), np.array(E),
+                             np.array(H), phv, max_delay, *volt, *curr, self.exc.volt.copy(), self.exc.curr.copy(),
+                             self.exc.period_steps())
+        return None
+
+    @staticmethod
+    def _tfsf_terms(tab, St, Sp, nl, active, curr):
+        """Flatten the per-face tables into the application order of Engine_Ext_TFSF."""
+        idx, dirs, dl, dd, am = [], [], [], [], []
+        for n in range(3):
+            nP, nPP = (n + 1) % 3, (n + 2) % 3
+            for l in range(2):
+                if not active[n, l]:
+                    continue
+                line = (St[n] - 1 if curr else St[n]) if l == 0 else Sp[n]
+                ui = 0
+                for i in range(nl[nP]):
+                    for j in range(nl[nPP]):
+                        pos = [0, 0, 0]
+                        pos[n], pos[nP], pos[nPP] = line, St[nP] + i, St[nPP] + j
+                        for c, comp in ((0, nP), (1, nPP)):
+                            t = tab[n, l, c]
+                            idx.append(pos)
+                            dirs.append(comp)
+                            dl.append(t[0][ui])
+                            dd.append(t[1][ui])
+                            am.append(t[2][ui])
+                        ui += 1
+        ft = type(dd[0]) if dd else np.float32
+        return (np.array(idx, np.uint32).T.reshape(3, -1).copy(), np.array(dirs, np.uint16),
+                np.array(dl, np.uint32), np.array(dd, ft), np.array(am, ft))
 
     # ---- Mur ABC (operator_ext_mur_abc.cpp:80-186, engine_ext_mur_abc.cpp:30-57) -------------
     def _build_mur(self, exc: ExcitationTable):

@@ -121,6 +121,11 @@ typedef struct oems_ref_engine {
     unsigned *v_idx, *i_idx, *v_delay, *i_delay;
     unsigned short *v_dir, *i_dir;
     float *v_amp, *i_amp, *sig_v, *sig_i;
+    /* TFSF plane wave: terms in the reference's application order */
+    unsigned tf_nV, tf_nI, tf_len, tf_period, tf_max_delay;
+    unsigned *tf_v_idx, *tf_i_idx, *tf_v_delay, *tf_i_delay, *tf_lut;
+    unsigned short *tf_v_dir, *tf_i_dir;
+    float *tf_v_delta, *tf_i_delta, *tf_v_amp, *tf_i_amp, *tf_sig_v, *tf_sig_i;
     /* extensions */
     upml_t upml[MAX_UPML];
     int nupml;
@@ -238,6 +243,9 @@ void oems_ref_destroy(eng_t *e)
     free(e->tstart); free(e->tstop); free(e->tstop_h);
     free(e->v_idx); free(e->i_idx); free(e->v_delay); free(e->i_delay);
     free(e->v_dir); free(e->i_dir); free(e->v_amp); free(e->i_amp); free(e->sig_v); free(e->sig_i);
+    free(e->tf_v_idx); free(e->tf_i_idx); free(e->tf_v_delay); free(e->tf_i_delay); free(e->tf_lut);
+    free(e->tf_v_dir); free(e->tf_i_dir); free(e->tf_v_delta); free(e->tf_i_delta);
+    free(e->tf_v_amp); free(e->tf_i_amp); free(e->tf_sig_v); free(e->tf_sig_i);
     for (int r = 0; r < e->nupml; ++r) {
         upml_t *u = &e->upml[r];
         free(u->vv); free(u->vvfo); free(u->vvfn); free(u->ii); free(u->iifo); free(u->iifn);
@@ -418,6 +426,54 @@ int oems_ref_set_excitation(eng_t *e, unsigned nV, const unsigned *v_idx, const 
     e->v_delay = (unsigned *)xcalloc(nV, 4); if (nV) memcpy(e->v_delay, v_delay, 4 * (size_t)nV);
     e->i_delay = (unsigned *)xcalloc(nI, 4); if (nI) memcpy(e->i_delay, i_delay, 4 * (size_t)nI);
     e->sig_v = dupf(sig_v, length); e->sig_i = dupf(sig_i, length);
+    return OK;
+}
+
+static void *dupmem(const void *src, size_t bytes)
+{
+    void *p = xcalloc(bytes ? bytes : 1, 1);
+    if (bytes)
+        memcpy(p, src, bytes);
+    return p;
+}
+
+int oems_ref_set_tfsf(eng_t *e, unsigned nV, const unsigned *v_idx, const unsigned short *v_dir,
+                      const unsigned *v_delay, const float *v_delta, const float *v_amp, unsigned nI,
+                      const unsigned *i_idx, const unsigned short *i_dir, const unsigned *i_delay,
+                      const float *i_delta, const float *i_amp, const float *sig_v, const float *sig_i,
+                      unsigned length, unsigned period, unsigned max_delay)
+{
+    if (!e || !length || !sig_v || !sig_i || period > length)
+        return ERR_ARG;
+    if (e->inited)
+        return ERR_STATE;
+    for (int w = 0; w < 2; ++w) {
+        unsigned n = w ? nI : nV;
+        const unsigned *idx = w ? i_idx : v_idx, *dl = w ? i_delay : v_delay;
+        const unsigned short *dr = w ? i_dir : v_dir;
+        for (unsigned k = 0; k < n; ++k)
+            if (idx[k] >= e->N[0] || idx[n + k] >= e->N[1] || idx[2 * n + k] >= e->N[2] || dr[k] > 2 ||
+                dl[k] >= max_delay)
+                return ERR_ARG;
+    }
+    e->tf_nV = nV;
+    e->tf_nI = nI;
+    e->tf_v_idx = (unsigned *)dupmem(v_idx, 12 * (size_t)nV);
+    e->tf_i_idx = (unsigned *)dupmem(i_idx, 12 * (size_t)nI);
+    e->tf_v_dir = (unsigned short *)dupmem(v_dir, 2 * (size_t)nV);
+    e->tf_i_dir = (unsigned short *)dupmem(i_dir, 2 * (size_t)nI);
+    e->tf_v_delay = (unsigned *)dupmem(v_delay, 4 * (size_t)nV);
+    e->tf_i_delay = (unsigned *)dupmem(i_delay, 4 * (size_t)nI);
+    e->tf_v_delta = (float *)dupmem(v_delta, 4 * (size_t)nV);
+    e->tf_i_delta = (float *)dupmem(i_delta, 4 * (size_t)nI);
+    e->tf_v_amp = (float *)dupmem(v_amp, 4 * (size_t)nV);
+    e->tf_i_amp = (float *)dupmem(i_amp, 4 * (size_t)nI);
+    e->tf_sig_v = (float *)dupmem(sig_v, 4 * (size_t)length);
+    e->tf_sig_i = (float *)dupmem(sig_i, 4 * (size_t)length);
+    e->tf_lut = (unsigned *)xcalloc((size_t)max_delay + 1, 4);
+    e->tf_len = length;
+    e->tf_period = period;
+    e->tf_max_delay = max_delay;
     return OK;
 }
 
@@ -916,6 +972,42 @@ static void excitation_apply(eng_t *e, int curr)
     }
 }
 
+/* Engine_Ext_TFSF::DoPostVoltageUpdates / DoPostCurrentUpdates (FDTD/extensions/engine_ext_tfsf.cpp:36-215)
+ * on the flattened term list (same order as the reference's face/position/component loops).
+ * The delay lookup is rebuilt per hook like m_DelayLookup: entries 0..max_delay in the voltage
+ * hook, 0..max_delay-1 in the current hook (entry max_delay keeps the voltage hook's value). */
+static void tfsf_apply(eng_t *e, int curr)
+{
+    unsigned cnt = curr ? e->tf_nI : e->tf_nV;
+    if (!e->tf_len || (!e->tf_nV && !e->tf_nI))
+        return;
+    unsigned numTS = e->numTS, length = e->tf_len;
+    int p = (int)e->tf_period;
+    unsigned top = curr ? e->tf_max_delay : e->tf_max_delay + 1;
+    for (unsigned n = 0; n < top; ++n) {
+        if (numTS < n)
+            e->tf_lut[n] = 0;
+        else if ((numTS - n >= length) && (p == 0))
+            e->tf_lut[n] = 0;
+        else
+            e->tf_lut[n] = numTS - n;
+        if (p > 0)
+            e->tf_lut[n] = (e->tf_lut[n] % p);
+    }
+    /* the voltage hook adds the current signal, the current hook the voltage signal */
+    const float *signal = curr ? e->tf_sig_v : e->tf_sig_i;
+    const unsigned *idx = curr ? e->tf_i_idx : e->tf_v_idx;
+    const unsigned *delay = curr ? e->tf_i_delay : e->tf_v_delay;
+    const unsigned short *dir = curr ? e->tf_i_dir : e->tf_v_dir;
+    const float *dd = curr ? e->tf_i_delta : e->tf_v_delta;
+    const float *amp = curr ? e->tf_i_amp : e->tf_v_amp;
+    for (unsigned k = 0; k < cnt; ++k) {
+        float *f = fptr(e, curr, dir[k], idx[k], idx[cnt + k], idx[2 * cnt + k]);
+        *f = *f + (1.0 - dd[k]) * amp[k] * signal[e->tf_lut[delay[k]]]
+                + dd[k] * amp[k] * signal[e->tf_lut[1 + delay[k]]];
+    }
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* processing */
 
@@ -1106,6 +1198,8 @@ static void pre_volt(eng_t *e)
 
 static void post_volt_apply(eng_t *e)
 {
+    /* post hooks in priority order: UPML (run by the caller), TFSF (5e4), Mur (0) */
+    tfsf_apply(e, 0);
     for (int w = e->nmur - 1; w >= 0; --w)
         mur_post(e, &e->mur[w]);
     for (int o = 0; o < e->nlor; ++o)
@@ -1123,6 +1217,7 @@ static void pre_curr(eng_t *e)
 
 static void post_curr_apply(eng_t *e)
 {
+    tfsf_apply(e, 1);
     for (int o = 0; o < e->nlor; ++o)
         lorentz_apply(e, &e->lor[o], 1);
     excitation_apply(e, 1);

@@ -47,6 +47,12 @@ CASES = [
     ("cube40", lambda: configs.plain_cube(n=40, steps=400), 400),
     ("stress_small", lambda: configs.stress(shape=(40, 36, 30), steps=150, nblocks=16), 150),
     ("patch_small", lambda: configs.patch(shape=(56, 52, 36), steps=250), 250),
+    ("plane_wave_upml", lambda: configs.plane_wave(steps=200), 200),
+    ("plane_wave_oblique_mur", lambda: configs.plane_wave(bc=(2,) * 6, k_dir=(1.0, 0.5, -0.3), e_dir=(0.0, 0.5, 1.0),
+                                                         frequency=10e9, graded=True, dispersive=True,
+                                                         box=([0, 6, 5], [20, 23, 19]), steps=220), 220),
+    ("plane_wave_sinus", lambda: configs.plane_wave(k_dir=(-0.2, -1.0, 0.4), e_dir=(1.0, 0.0, 0.5), sinus=True,
+                                                   steps=200), 200),
 ]
 
 
