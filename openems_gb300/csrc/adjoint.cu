@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256) k_adj_w(AdjDev a)
 
 // the engine's UPML work split (k_update_split): interior blocks, then the region blocks
 template <bool CURR>
-__global__ void __launch_bounds__(256) k_adj_split(AdjDev a, SplitDev sp)
+__global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
 {
     const GridDev& g = a.g;
     unsigned b = blockIdx.x;
@@ -322,6 +322,11 @@ struct oems_adjoint_state {
     std::vector<void*> allocs;
     size_t state_bytes = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    // checkpoint mode: the reverse sweep of segment k runs on `rs` while the engine stream
+    // recomputes segment k-1 into the other half of the factor slots (2K slots)
+    cudaStream_t rs = nullptr;
+    cudaEvent_t ev_recomputed[2] = {nullptr, nullptr};
+    cudaEvent_t ev_reversed[2] = {nullptr, nullptr};
     float fwd_ms = 0.f, bwd_ms = 0.f;
     unsigned launches_per_reverse_step = 0;
 };
@@ -513,8 +518,14 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     if ((rc = aalloc(e, s, &d.gvv, 3ull * d.B))) return rc;
     if ((rc = aalloc(e, s, &d.gvi, 3ull * d.B))) return rc;
     if (s->K) {
-        s->fac_slots = s->K;
+        s->fac_slots = 2ull * s->K;
         if ((rc = aalloc(e, s, &s->fac, s->fac_slots * 6ull * d.B))) return rc;
+        if (cudaStreamCreateWithFlags(&s->rs, cudaStreamNonBlocking) != cudaSuccess)
+            return afail(e, OEMS_ERR_CUDA, "adjoint stream");
+        for (int b = 0; b < 2; ++b)
+            if (cudaEventCreateWithFlags(&s->ev_recomputed[b], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&s->ev_reversed[b], cudaEventDisableTiming) != cudaSuccess)
+                return afail(e, OEMS_ERR_CUDA, "adjoint events");
     }
     if ((rc = aalloc(e, s, &s->rec_numTS, 1))) return rc;
     if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess)
@@ -621,33 +632,59 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     unsigned lps = 2;
     const unsigned bu = e->splitI.main_blocks + e->splitI.first_block[e->splitI.nreg];
     const unsigned bw = e->splitV.main_blocks + e->splitV.first_block[e->splitV.nreg];
-    auto reverse = [&](unsigned n, const float* slot) {
+    auto reverse = [&](unsigned n, const float* slot, cudaStream_t rst) {
         d.n = n;
         d.fv = slot;
         d.fc = slot + 3 * d.B;
         if (e->use_split) {
-            if (bu) k_adj_split<true><<<bu, 256, 0, st>>>(d, e->splitI);
-            if (bw) k_adj_split<false><<<bw, 256, 0, st>>>(d, e->splitV);
+            if (bu) k_adj_split<true><<<bu, 256, 0, rst>>>(d, e->splitI);
+            if (bw) k_adj_split<false><<<bw, 256, 0, rst>>>(d, e->splitV);
         } else {
-            k_adj_u<<<gu, 256, 0, st>>>(d);
-            k_adj_w<<<gw, 256, 0, st>>>(d);
+            k_adj_u<<<gu, 256, 0, rst>>>(d);
+            k_adj_w<<<gw, 256, 0, rst>>>(d);
         }
     };
     if (s->K) {
+        // Two-stage pipeline over the segments, last to first. The engine stream restores
+        // checkpoint k and recomputes segment k, recording its factors into half k % 2 of the
+        // slots; the reverse stream then sweeps segment k from those factors while the engine
+        // stream already recomputes segment k-1 into the other half (after the sweep of segment
+        // k+1 has released it). The two streams share nothing else: the sweep reads the
+        // coefficients, the factors and its own adjoint arrays, the recompute the engine state.
         const unsigned nseg = (N + s->K - 1) / s->K;
-        for (int seg = (int)nseg - 1; seg >= 0 && rc == OEMS_OK; --seg) {
+        const size_t half = (size_t)s->K * 6 * d.B;
+        auto recompute = [&](unsigned seg) -> int {
             const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
-            if ((rc = copy_state(e, s, s->ckpt[seg], false))) break;
+            float* base = s->fac + (seg & 1u) * half;
+            int r2;
+            if ((r2 = copy_state(e, s, s->ckpt[seg], false))) return r2;
             cudaMemcpyAsync(s->rec_numTS, &a0, sizeof(unsigned), cudaMemcpyHostToDevice, st);
             for (unsigned n = a0; n < a1; ++n) {
-                k_adj_factors<<<fb, 256, 0, st>>>(d, s->fac, s->rec_numTS, s->K);
+                k_adj_factors<<<fb, 256, 0, st>>>(d, base, s->rec_numTS, s->K);
                 lps = 3 + recompute_step(e, s);
             }
-            for (int n = (int)a1 - 1; n >= (int)a0; --n) reverse((unsigned)n, s->fac + (size_t)(n % s->K) * 6 * d.B);
+            cudaEventRecord(s->ev_recomputed[seg & 1u], st);
+            return OEMS_OK;
+        };
+        rc = recompute(nseg - 1);
+        for (int seg = (int)nseg - 1; seg >= 0 && rc == OEMS_OK; --seg) {
+            const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
+            if (seg > 0) {
+                // segment seg-1 reuses the half of segment seg+1: wait for that sweep
+                if (seg + 1 < (int)nseg) cudaStreamWaitEvent(st, s->ev_reversed[(seg + 1) & 1], 0);
+                if ((rc = recompute(seg - 1))) break;
+            }
+            cudaStreamWaitEvent(s->rs, s->ev_recomputed[seg & 1], 0);
+            const float* base = s->fac + (seg & 1) * half;
+            for (int n = (int)a1 - 1; n >= (int)a0; --n) reverse((unsigned)n, base + (size_t)(n % s->K) * 6 * d.B, s->rs);
+            cudaEventRecord(s->ev_reversed[seg & 1], s->rs);
             if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
         }
+        // the gradients, the timing event and the state restore follow the last sweep
+        cudaEventRecord(s->ev_reversed[0], s->rs);
+        cudaStreamWaitEvent(st, s->ev_reversed[0], 0);
     } else {
-        for (int n = (int)N - 1; n >= 0; --n) reverse((unsigned)n, s->fac + (size_t)n * 6 * d.B);
+        for (int n = (int)N - 1; n >= 0; --n) reverse((unsigned)n, s->fac + (size_t)n * 6 * d.B, st);
         if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
     }
     s->launches_per_reverse_step = lps;
@@ -662,6 +699,7 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     } else {
         cudaStreamSynchronize(st);
     }
+    if (s->rs) cudaStreamSynchronize(s->rs);
     release();
     d.src = nullptr;
     d.injV = InjList{};
@@ -688,5 +726,10 @@ void oems_adjoint_free(oems_adjoint_state* s)
     for (void* p : s->allocs) cudaFree(p);
     for (cudaEvent_t ev : s->ev)
         if (ev) cudaEventDestroy(ev);
+    for (int b = 0; b < 2; ++b) {
+        if (s->ev_recomputed[b]) cudaEventDestroy(s->ev_recomputed[b]);
+        if (s->ev_reversed[b]) cudaEventDestroy(s->ev_reversed[b]);
+    }
+    if (s->rs) cudaStreamDestroy(s->rs);
     delete s;
 }

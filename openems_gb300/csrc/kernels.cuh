@@ -464,8 +464,11 @@ struct SplitDev {
     unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1]) after main
 };
 
+// The compressed-operator form without Mur hooks fits 32 registers (a few bytes spill to L1), so
+// 8 blocks of 256 threads share an SM; the latency-bound split launches gain from the extra warps.
 template <bool COMPRESSED, bool CURR, bool MUR = false>
-__global__ void __launch_bounds__(256) k_update_split(GridDev g, SplitDev sp, MurDev m, const unsigned* __restrict__ numTS)
+__global__ void __launch_bounds__(256, (COMPRESSED && !MUR) ? 8 : 1)
+    k_update_split(GridDev g, SplitDev sp, MurDev m, const unsigned* __restrict__ numTS)
 {
 
     unsigned b = blockIdx.x;
