@@ -177,78 +177,67 @@ __device__ __forceinline__ unsigned mur_cell(const GridDev& g, const MurDev& m, 
     return keep;
 }
 
-// Lane-parallel form for the z walls (mode 2 of update_v_cell; every wall active from step 0).
-// Threads walk z, so a z wall's line and shift cells are neighbouring lanes, usually of one warp.
-// The line lane takes V_old and V_new of the shift lane by shuffle and computes the wall value
-//   b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift)
-// itself.  In a "direct" column -- no x/y wall line or shift there (inside both windows) and both
-// lanes in one warp -- it stores b as the final value, so the apply has nothing left to do; the
-// dispersive apply hooks skip the Mur-owned components (the reference's apply overwrites them).
-// Other columns go through the wall buffer and k_mur applies them: the line lane writes bP (same
-// warp) or leaves the line unwritten while the shift lane reads V_old(line) from memory and
-// writes bP (lanes in neighbouring warps).  The tangential components of a z wall are 0 and 1;
+// Shift-lane form for the z walls (mode 2 of update_v_cell; every wall active from step 0).
+// Threads walk z, so a z wall's line and shift cells are neighbouring threads. The thread of the
+// shift cell holds V_old(shift) and V_new(shift) in registers, reads V_old(line) from memory (the
+// line cell never stores its tangential components, so memory keeps the old value while the
+// launch runs; the line is the neighbouring float, in the sector the warp loads anyway) and forms
+//   b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift).
+// In a "direct" column -- no x/y wall line or shift there (inside both windows) -- it stores b as
+// the line's final value, so the apply has nothing left to do; the dispersive apply hooks skip the
+// Mur-owned components (the reference's apply overwrites them). In the other columns it writes
+// the wall buffer and k_mur applies it with the edge priorities of the walls. No other thread
+// reads the tangential components of a direct column's line cell in the voltage update: x/y wall
+// hooks only read cells outside the windows. The tangential components of a z wall are 0 and 1;
 // the table index is x*Ny + y.
-__device__ __forceinline__ bool mur_z_direct(const MurDev& m, unsigned Pz, unsigned x, unsigned y, unsigned line,
-                                             unsigned shift)
+__device__ __forceinline__ bool mur_z_direct(const MurDev& m, unsigned x, unsigned y)
 {
-    const unsigned r = y * Pz;
-    return (x - m.lo[0] <= m.span[0]) && (y - m.lo[1] <= m.span[1]) && ((r + line) >> 5) == ((r + shift) >> 5);
+    return (x - m.lo[0] <= m.span[0]) && (y - m.lo[1] <= m.span[1]);
 }
 
-// before the update's loads: start the line lane's coefficient loads into L1 (prefetch holds no
-// register across the update)
+// before the update's loads: start the shift thread's coefficient loads into L1 (a prefetch holds
+// no register across the update)
 __device__ __forceinline__ void mur_z_prefetch(const MurDev& m, unsigned x, unsigned y, unsigned z, unsigned Ny)
 {
     const MurWallDev& A = m.z[0];
     const MurWallDev& B = m.z[1];
-    const bool la = m.nz > 0 && z == A.line, lb = m.nz > 1 && z == B.line;
-    if (la || lb) {
+    const bool sa = m.nz > 0 && z == A.shift, sb = m.nz > 1 && z == B.shift;
+    if (sa || sb) {
         const unsigned k = x * Ny + y;
-        asm volatile("prefetch.global.L1 [%0];" ::"l"((lb ? B.cP : A.cP) + k));
-        asm volatile("prefetch.global.L1 [%0];" ::"l"((lb ? B.cPP : A.cPP) + k));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"((sb ? B.cP : A.cP) + k));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"((sb ? B.cPP : A.cPP) + k));
     }
 }
 
-// after the update (every lane of the warp calls it): sets out0/out1 of a direct line cell to the
-// wall value, writes bP/bPP of the buffered columns; returns the mask of components this cell
-// still stores
-__device__ __forceinline__ unsigned mur_z_finish(const GridDev& g, const MurDev& m, unsigned x, unsigned y,
-                                                 unsigned z, bool valid, unsigned long long o, float vo0, float vo1,
-                                                 float& out0, float& out1)
+// store mask of a z-wall line cell: its tangential components 0 and 1 are the wall's
+__device__ __forceinline__ unsigned mur_z_keep(const MurDev& m, unsigned z)
+{
+    const bool l = (m.nz > 0 && z == m.z[0].line) || (m.nz > 1 && z == m.z[1].line);
+    return l ? 4u : 7u;
+}
+
+// the z-wall work of a shift cell (vo = V_old, vn = V_new of its components 0 and 1)
+__device__ __forceinline__ void mur_z_shift(const GridDev& g, const MurDev& m, unsigned x, unsigned y, unsigned z,
+                                            unsigned long long o, float vo0, float vo1, float vn0, float vn1)
 {
     const MurWallDev& A = m.z[0];
     const MurWallDev& B = m.z[1];
-    const bool la = valid && m.nz > 0 && z == A.line, lb = valid && m.nz > 1 && z == B.line;
-    const bool sa = valid && m.nz > 0 && z == A.shift, sb = valid && m.nz > 1 && z == B.shift;
-    const bool wb = lb || sb;
-    const MurWallDev& W = wb ? B : A;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned src = (la || lb) ? ((lane + W.shift - W.line) & 31u) : lane;
-    const unsigned full = 0xffffffffu;
-    const float so0 = __shfl_sync(full, vo0, src), so1 = __shfl_sync(full, vo1, src);
-    const float sn0 = __shfl_sync(full, out0, src), sn1 = __shfl_sync(full, out1, src);
-    if (!(la || lb || sa || sb)) return 7u;
-    const unsigned r = y * g.Pz;
-    const bool same = ((r + W.line) >> 5) == ((r + W.shift) >> 5);
+    const bool sa = m.nz > 0 && z == A.shift, sb = m.nz > 1 && z == B.shift;
+    if (!(sa || sb)) return;
+    const MurWallDev& W = sb ? B : A;
+    const unsigned long long ol = W.line > W.shift ? o + 1 : o - 1;
+    const float l0 = g.V[ol], l1 = g.V[g.S + ol];
     const unsigned k = x * g.Ny + y;
-    if (la || lb) {
-        if (!same) return 4u;           // the shift lane in the neighbouring warp writes bP
-        const float cP = __ldg(W.cP + k), cPP = __ldg(W.cPP + k);
-        const float b0 = fadd(fsub(so0, fmul(cP, vo0)), fmul(cP, sn0));
-        const float b1 = fadd(fsub(so1, fmul(cPP, vo1)), fmul(cPP, sn1));
-        if ((x - m.lo[0] <= m.span[0]) && (y - m.lo[1] <= m.span[1])) { out0 = b0; out1 = b1; return 7u; }
+    const float cP = __ldg(W.cP + k), cPP = __ldg(W.cPP + k);
+    const float b0 = fadd(fsub(vo0, fmul(cP, l0)), fmul(cP, vn0));
+    const float b1 = fadd(fsub(vo1, fmul(cPP, l1)), fmul(cPP, vn1));
+    if (mur_z_direct(m, x, y)) {
+        g.V[ol] = b0;
+        g.V[g.S + ol] = b1;
+    } else {
         W.bP[k] = b0;
         W.bPP[k] = b1;
-        return 4u;
     }
-    if (!same) {                        // shift lane; the line lane left V_old(line) in memory
-        const unsigned long long ol = W.line > W.shift ? o + 1 : o - 1;
-        const float l0 = g.V[ol], l1 = g.V[g.S + ol];
-        const float cP = __ldg(W.cP + k), cPP = __ldg(W.cPP + k);
-        W.bP[k] = fadd(fsub(vo0, fmul(cP, l0)), fmul(cP, out0));
-        W.bPP[k] = fadd(fsub(vo1, fmul(cPP, l1)), fmul(cPP, out1));
-    }
-    return 7u;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -265,12 +254,11 @@ __device__ __forceinline__ float ldf(const float* p)
 
 // rk/lk: the cell's UPML region and local offset when the caller knows them (rk = -2: look up).
 // MUR: the Mur pre/post hooks of the walls are done here (m, ts = the walls and the step
-// number): 1 = every wall by mur_cell, 2 = the z walls lane-parallel (mur_z_*; every lane of the
-// warp must call, `valid` false for the lanes without a cell) and the x/y walls by mur_cell.
+// number): 1 = every wall by mur_cell, 2 = the z walls by their shift cells (mur_z_*) and the x/y
+// walls by mur_cell.
 template <bool COMPRESSED, bool UPML, bool COHERENT = false, int MUR = 0, typename IX = unsigned long long>
 __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsigned y, unsigned z, int rk = -2,
-                                              unsigned lk = 0, const MurDev* m = nullptr, unsigned ts = 0,
-                                              bool valid = true)
+                                              unsigned lk = 0, const MurDev* m = nullptr, unsigned ts = 0)
 {
     if (MUR == 2) mur_z_prefetch(*m, x, y, z, g.Ny);
     const IX S = (IX)g.S;
@@ -336,10 +324,10 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
     unsigned keep = 7u;
     if (MUR == 1) keep = mur_cell<3>(g, *m, ts, x, y, z, o, v0, v1, v2, out[0], out[1], out[2]);
     if (MUR == 2) {
-        // x/y walls first: their hooks read this cell's raw new values
-        if (valid && mur_wall_cell<2>(*m, x, y, z)) keep = mur_cell<2>(g, *m, ts, x, y, z, o, v0, v1, v2, out[0], out[1], out[2]);
-        keep &= mur_z_finish(g, *m, x, y, z, valid, o, v0, v1, out[0], out[1]);
-        if (!valid) keep = 0u;
+        // x/y walls: their hooks read this cell's raw new values
+        if (mur_wall_cell<2>(*m, x, y, z)) keep = mur_cell<2>(g, *m, ts, x, y, z, o, v0, v1, v2, out[0], out[1], out[2]);
+        keep &= mur_z_keep(*m, z);
+        mur_z_shift(g, *m, x, y, z, o, v0, v1, out[0], out[1]);
     }
     if (keep & 1u) V[o] = out[0];
     if (keep & 2u) V[S + o] = out[1];
@@ -415,9 +403,9 @@ __device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsi
 // MUR (the update_v_cell modes): with the Mur pre/post hooks; numTS is the device step counter.
 // IX: the type of the cell offsets (32-bit when 3 * S fits, one address instruction per access).
 // Mode 2 decides per warp: a warp without a cell outside the wall windows runs the plain update
-// (the kernel is issue-bound, so the hooks must cost those warps nothing); a warp with one keeps
-// every lane to the end for the shuffles (lanes past the mesh update a clamped cell and store
-// nothing).  Full occupancy needs 32 registers: 8 blocks of 256 threads per SM.
+// (the kernel is issue-bound, so the hooks must cost those warps nothing); in a warp with one,
+// only the wall cells' threads do extra work (x/y wall hooks, the z-wall shift thread).  Full
+// occupancy needs 32 registers: 8 blocks of 256 threads per SM.
 template <bool COMPRESSED, bool UPML, int MUR = 0, typename IX = unsigned long long>
 __global__ void __launch_bounds__(256, (MUR == 2 ? 8 : 1)) k_update_v(GridDev g, MurDev m,
                                                                       const unsigned* __restrict__ numTS)
@@ -426,15 +414,12 @@ __global__ void __launch_bounds__(256, (MUR == 2 ? 8 : 1)) k_update_v(GridDev g,
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned y = t / g.Pz, z = t - y * g.Pz;
     const bool valid = y < g.Ny && z < g.Nz;
-    static_assert(!(UPML && MUR == 2), "the clamped lanes of mode 2 would write UPML fluxes");
+    static_assert(!(UPML && MUR == 2), "mode 2 is chosen for meshes without UPML only");
     if (MUR == 2) {
-        if (__any_sync(0xffffffffu, valid && mur_wall_cell(m, x, y, z))) {
-            if (!valid) { y = g.Ny - 1; z = g.Nz - 1; }
-            update_v_cell<COMPRESSED, UPML, false, 2, IX>(g, x, y, z, -2, 0, &m, __ldg(numTS), valid);
-            return;
-        }
+        const bool wall = __any_sync(0xffffffffu, valid && mur_wall_cell(m, x, y, z));
         if (!valid) return;
-        update_v_cell<COMPRESSED, UPML, false, 0, IX>(g, x, y, z);
+        if (wall) update_v_cell<COMPRESSED, UPML, false, 2, IX>(g, x, y, z, -2, 0, &m, __ldg(numTS));
+        else update_v_cell<COMPRESSED, UPML, false, 0, IX>(g, x, y, z);
         return;
     }
     if (!valid) return;
@@ -625,7 +610,7 @@ static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __r
         return;
     }
     // a direct column of the lane-parallel z-wall form holds its final value already
-    if (m.lanes && w.ny == 2 && mur_z_direct(m, g.Pz, pos[0], pos[1], w.line, w.shift)) return;
+    if (m.lanes && w.ny == 2 && mur_z_direct(m, pos[0], pos[1])) return;
     // walls are applied in reverse insertion order, so on shared edges the wall with the
     // lowest index is the last writer; skip components a lower active wall also writes
     bool wP = true, wPP = true;
