@@ -131,6 +131,19 @@ int oems_cuda_set_tfsf(oems_cuda_engine* eng, unsigned int volt_count, const uns
                        const float* curr_amp, const float* sig_volt, const float* sig_curr, unsigned int length,
                        unsigned int period, unsigned int max_delay);
 
+/* Engine_Ext_LumpedRLC (FDTD/extensions/engine_ext_lumpedRLC.cpp:80-147) fed with
+ * Operator_Ext_LumpedRLC's tables (FDTD/extensions/operator_ext_lumpedRLC.h:58-82): count lumped
+ * edges, pos unsigned [3][count] (v_RLC_pos), dir int [count] (v_RLC_dir) and the float [count]
+ * coefficient arrays v_RLC_ilv, v_RLC_i2v, v_RLC_vv2, v_RLC_vj1, v_RLC_vj2, v_RLC_vvd, v_RLC_ib0,
+ * v_RLC_b1, v_RLC_b2. The engine keeps the parallel inductor current and the last three node
+ * voltages and auxiliary currents of every edge; they start at zero and are part of a snapshot.
+ * The apply hook runs after the post-voltage hooks and before the dispersive, Mur and excitation
+ * apply hooks, as the reference's priority order has it. Two elements on one edge give
+ * OEMS_ERR_ARG. Replaces any previous table. */
+int oems_cuda_set_lumped_rlc(oems_cuda_engine* eng, unsigned int count, const unsigned int* pos, const int* dir,
+                             const float* ilv, const float* i2v, const float* vv2, const float* vj1, const float* vj2,
+                             const float* vvd, const float* ib0, const float* b1, const float* b2);
+
 /* ---- processing: probes, DFTs, FD field dumps --------------------------------------------- */
 
 /* ProcessVoltage (Common/processvoltage.cpp:38-48) -> Engine_Interface_FDTD::CalcVoltageIntegral
@@ -336,7 +349,7 @@ int oems_cuda_timed_iterate(oems_cuda_engine* eng, unsigned int n_steps, float* 
 #define OEMS_KC_UPDATE_V  0
 #define OEMS_KC_UPDATE_I  1
 #define OEMS_KC_MUR       2
-#define OEMS_KC_LORENTZ   3
+#define OEMS_KC_LORENTZ   3   /* auxiliary-equation kernels: Drude/Lorentz and lumped RLC */
 #define OEMS_KC_EXCITE    4
 #define OEMS_KC_STEP_END  5
 #define OEMS_KC_COUNT     6

@@ -40,6 +40,7 @@ SIGNATURES = {
     "add_mur": (I, [P, I, U, U, U, PF, PF]),
     "add_lorentz_order": (I, [P, U, PU, I, I, I, I, PF, PF, PF, PF, PF, PF]),
     "set_tfsf": (I, [P, U, PU, PUS, PU, PF, PF, U, PU, PUS, PU, PF, PF, PF, PF, U, U, U]),
+    "set_lumped_rlc": (I, [P, U, PU, PI_, PF, PF, PF, PF, PF, PF, PF, PF, PF]),
     "add_voltage_probe": (I, [P, PU, PU, D, U, U, U, PI_]),
     "add_current_probe": (I, [P, PU, PU, I, PI_, PI_, D, U, U, U, PI_]),
     "set_probe_dft": (I, [P, I, U, U, PD]),

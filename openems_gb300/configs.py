@@ -257,6 +257,61 @@ def plane_wave(n=(28, 24, 26), steps=300, bc=(3,) * 6, pml=5, k_dir=(1.0, 0.0, 0
     return op.build(steps)
 
 
+def lumped_rlc(n=(22, 20, 24), steps=600, bc=(2,) * 6, dispersive=False, seed=11):
+    """Lumped RLC loads of every kind the reference's Operator_Ext_LumpedRLC builds, fed by a 50 Ohm
+    lumped port: a series RLC, a series RL (C = 0: the capacitor is a short), a parallel RLC and
+    a parallel L without C (the edge keeps its own capacitance, raised to the reference's minimum
+    if it is too small), on a graded mesh with Mur walls (or the given boundaries).  Every element
+    stays out of a 4-cell UPML: the UPML rewrites the coefficients of its cells, which a lumped
+    element rewritten after it would break."""
+    rng = np.random.default_rng(seed)
+    lines = [np.cumsum(np.concatenate([[0.0], rng.uniform(0.8, 1.2, k - 1)])) for k in n]
+    g = Grid(lines, unit=1e-3)
+    gl = g.lines
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(5e9, 4e9)
+    c = [k // 2 for k in n]
+
+    def P(i, j, k):
+        return [gl[0][i], gl[1][j], gl[2][k]]
+    csx.AddLumpedElement("port", 2, R=50.0, caps=True).AddBox(P(c[0] - 4, c[1], c[2] - 1), P(c[0] - 4, c[1], c[2] + 1))
+    csx.AddExcitation("port_exc", 0, [0, 0, -1.0]).AddBox(P(c[0] - 4, c[1], c[2] - 1), P(c[0] - 4, c[1], c[2] + 1))
+    csx.AddLumpedElement("series_rlc", 2, R=10.0, L=2e-9, C=0.5e-12, LEtype=1, caps=True).AddBox(
+        P(c[0] + 3, c[1], c[2] - 1), P(c[0] + 3, c[1], c[2] + 1))
+    csx.AddLumpedElement("series_rl", 0, R=20.0, L=1e-9, LEtype=1, caps=False).AddBox(
+        P(c[0] - 1, c[1] + 3, c[2] + 3), P(c[0] + 1, c[1] + 4, c[2] + 3))
+    csx.AddLumpedElement("parallel_rlc", 1, R=100.0, C=0.2e-12, L=3e-9, LEtype=0, caps=True).AddBox(
+        P(c[0], c[1] - 5, c[2] - 3), P(c[0], c[1] - 3, c[2] - 3))
+    csx.AddLumpedElement("parallel_l", 2, L=2e-9, LEtype=0).AddBox(P(c[0] + 5, c[1] - 2, c[2]), P(c[0] + 5, c[1] - 2, c[2] + 1))
+    if dispersive:
+        csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[6e9], eps_relax_time=[1e-9]).AddBox(
+            P(5, 5, 5), P(c[0] - 2, n[1] - 6, c[2]), priority=2)
+    csx.AddProbe("u_port", 0, interval=1).AddBox(P(c[0] - 4, c[1], c[2] - 1), P(c[0] - 4, c[1], c[2] + 1))
+    csx.AddProbe("u_series", 0, interval=1).AddBox(P(c[0] + 3, c[1], c[2] - 1), P(c[0] + 3, c[1], c[2] + 1))
+    csx.AddProbe("i_series", 1, norm_dir=2, interval=1).AddBox(P(c[0] + 3, c[1], c[2]), P(c[0] + 3, c[1], c[2]))
+    op = Operator(csx, g, exc, bc=bc, pml_size=(4,) * 6)
+    return op.build(steps)
+
+
+def lc_tank(L=1e-9, C=1e-12, steps=6000, n=20):
+    """A parallel LC lumped element (LEtype 0, R open) on one z edge at the centre of a PEC box of
+    n^3 lines at 0.5 mm, kicked by a soft source on the same edge.  After the pulse the node rings
+    at 1/(2 pi sqrt(L C)) as long as C dominates the edge's own capacitance."""
+    g = Grid([_uniform(n, 0.5) for _ in range(3)], unit=1e-3)
+    gl = g.lines
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(4e9, 4e9)
+    c = n // 2
+    box = ([gl[0][c], gl[1][c], gl[2][c]], [gl[0][c], gl[1][c], gl[2][c + 1]])
+    csx.AddLumpedElement("tank", 2, C=C, L=L, LEtype=0, caps=False).AddBox(*box)
+    csx.AddExcitation("kick", 0, [0, 0, 1.0]).AddBox(*box)
+    csx.AddProbe("u_tank", 0, interval=1).AddBox(*box)
+    op = Operator(csx, g, exc, bc=(0,) * 6)
+    return op.build(steps)
+
+
 def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
     """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""
     nx, ny, nz = shape

@@ -411,6 +411,31 @@ int oems_cuda_set_tfsf(oems_cuda_engine* e, unsigned int volt_count, const unsig
     return OEMS_OK;
 }
 
+int oems_cuda_set_lumped_rlc(oems_cuda_engine* e, unsigned int count, const unsigned int* pos, const int* dir,
+                             const float* ilv, const float* i2v, const float* vv2, const float* vj1, const float* vj2,
+                             const float* vvd, const float* ib0, const float* b1, const float* b2)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if (count && (!pos || !dir || !ilv || !i2v || !vv2 || !vj1 || !vj2 || !vvd || !ib0 || !b1 || !b2))
+        return fail(e, OEMS_ERR_ARG, "lumped RLC arrays missing");
+    RlcHost r;
+    for (unsigned k = 0; k < count; ++k) {
+        const unsigned x = pos[k], y = pos[count + k], z = pos[2 * (size_t)count + k];
+        if (x >= e->N[0] || y >= e->N[1] || z >= e->N[2] || dir[k] < 0 || dir[k] > 2)
+            return fail(e, OEMS_ERR_ARG, "lumped RLC position out of range");
+        r.off.push_back(cell_off(e, (unsigned)dir[k], x, y, z));
+    }
+    std::vector<unsigned long long> sorted(r.off);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+        return fail(e, OEMS_ERR_ARG, "two lumped RLC elements on one edge");
+    const float* src[9] = {ilv, i2v, vv2, vj1, vj2, vvd, ib0, b1, b2};
+    for (int q = 0; q < 9; ++q) r.c.insert(r.c.end(), src[q], src[q] + count);
+    e->rlc_host = std::move(r);
+    return OEMS_OK;
+}
+
 int oems_cuda_add_upml(oems_cuda_engine* e, const unsigned int start[3], const unsigned int nl[3], const float* vv,
                        const float* vvfo, const float* vvfn, const float* ii, const float* iifo, const float* iifn)
 {
@@ -716,6 +741,12 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
         post(); ++L;
     }
     if (mur_sep) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 1, e->d_numTS); post(); ++L; }
+    // apply hooks in priority order: lumped RLC, dispersive, Mur, excitation
+    if (e->rlc.count) {
+        pre(OEMS_KC_LORENTZ);
+        k_lumped_rlc<<<(e->rlc.count + 127) / 128, 128, 0, s>>>(e->dV, e->rlc, e->d_numTS);
+        post(); ++L;
+    }
     for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
     if (!e->mur.empty()) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 2, e->d_numTS); post(); ++L; }
     if (e->excV.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excV.count + 127) / 128, 128, 0, s>>>(e->dV, e->excV, e->d_numTS); post(); ++L; }
@@ -936,9 +967,11 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         if (md.nz >= 0 && std::adjacent_find(zs.begin(), zs.end()) != zs.end()) md.nz = -1;
         // OEMS_CUDA_MUR_SEPARATE=1: the pre/post hooks as separate launches (k_mur phases 0/1).
         // A TFSF plane wave needs them too: its post-voltage hook (priority 5e4) runs before the
-        // Mur post hook (priority 0) and may change the values Mur reads at a shift line.
+        // Mur post hook (priority 0) and may change the values Mur reads at a shift line.  So do
+        // lumped RLC loads: their apply reads the raw updated value of an edge that may be a
+        // Mur line, which the form inside the voltage update does not keep.
         const char* ms = getenv("OEMS_CUDA_MUR_SEPARATE");
-        e->mur_separate = (ms && ms[0] == '1') || e->has_tfsf;
+        e->mur_separate = (ms && ms[0] == '1') || e->has_tfsf || !e->rlc_host.off.empty();
         // the lane-parallel form: no UPML (plain update kernel), every wall active from step 0
         bool always = true;
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
@@ -984,6 +1017,21 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
             d.ntarget = (unsigned)toff.size();
             d.off = o; d.first = f; d.delay = de; d.delta = dt; d.amp = ap;
         }
+    }
+
+    // lumped RLC loads
+    if (!e->rlc_host.off.empty()) {
+        RlcDev& r = e->rlc;
+        r.count = (unsigned)e->rlc_host.off.size();
+        unsigned long long* o;
+        float* c;
+        if ((rc = dupload(e, &o, e->rlc_host.off.data(), e->rlc_host.off.size()))) return rc;
+        if ((rc = dupload(e, &c, e->rlc_host.c.data(), e->rlc_host.c.size()))) return rc;
+        r.off = o;
+        r.c = c;
+        if ((rc = dalloc(e, &r.il, r.count, true, true))) return rc;
+        if ((rc = dalloc(e, &r.vd, 3 * (size_t)r.count, true, true))) return rc;
+        if ((rc = dalloc(e, &r.j, 3 * (size_t)r.count, true, true))) return rc;
     }
 
     // Lorentz / Drude orders
@@ -1193,7 +1241,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     // separate update kernels on GB300, so it is not the default.
     {
         const char* env = getenv("OEMS_CUDA_FUSED");
-        e->use_fused = env && env[0] == '1' && e->mur.empty() && e->lor.empty() && !e->has_tfsf &&
+        e->use_fused = env && env[0] == '1' && e->mur.empty() && e->lor.empty() && !e->has_tfsf && !e->rlc.count &&
                        e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC && e->K % 2 == 0 &&
                        3ull * e->S < (1ull << 32);        // the staged-plane offsets are 32-bit
         if (e->use_fused && (rc = setup_fused(e))) return rc;

@@ -46,6 +46,10 @@ struct TfsfHost {
     std::vector<unsigned> delay;
     std::vector<float> delta, amp;
 };
+struct RlcHost {
+    std::vector<unsigned long long> off;
+    std::vector<float> c;   // [9][count]
+};
 struct DumpHost {
     int field;
     unsigned start[3], stop[3];
@@ -100,6 +104,8 @@ struct oems_cuda_engine {
     TfsfHost tfsf_v, tfsf_i;
     std::vector<float> tfsf_sig_v, tfsf_sig_i;
     unsigned tfsf_len = 0, tfsf_period = 0;
+    // lumped RLC loads
+    RlcHost rlc_host;
 
     // device state after init
     bool inited = false;
@@ -110,6 +116,7 @@ struct oems_cuda_engine {
     GridDev grid{};
     ExcDev excV{}, excI{};
     TfsfDev tfsfV{}, tfsfI{};
+    RlcDev rlc{};
     MurDev murdev{};
     std::vector<LorDev> lorV, lorI;
     StepEndDev stepend{};

@@ -570,6 +570,47 @@ static __global__ void k_tfsf(float* __restrict__ F, TfsfDev t, const unsigned* 
 }
 
 // ---------------------------------------------------------------------------------------------
+// Engine_Ext_LumpedRLC (FDTD/extensions/engine_ext_lumpedRLC.cpp:80-147): series RLC and parallel
+// RLC loads as an auxiliary differential equation per lumped edge.  The reference's pre-voltage
+// hook only advances the parallel inductor current from the previous step's node voltage, and
+// nothing else touches that state between the two hooks, so one launch after the voltage update
+// (in the apply slot) does both.  The reference rotates three buffers of node voltages Vd and
+// auxiliary currents J by pointer once per step; here slot numTS % 3 is the current one ([0]),
+// (numTS + 2) % 3 the previous ([1]) and (numTS + 1) % 3 the one before ([2]).  Float arithmetic
+// in the reference's evaluation order.  The element edges are distinct (checked on the host).
+struct RlcDev {
+    unsigned count;
+    const unsigned long long* off;   // field offset (component included)
+    const float* c;                  // [9][count]: ilv, i2v, vv2, vj1, vj2, vvd, ib0, b1, b2
+    float* il;                       // [count] parallel inductor current
+    float* vd;                       // [3][count] node voltages
+    float* j;                        // [3][count] auxiliary currents
+};
+
+static __global__ void k_lumped_rlc(float* __restrict__ V, RlcDev r, const unsigned* __restrict__ numTS)
+{
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= r.count) return;
+    const unsigned n = r.count;
+    const unsigned t = *numTS;
+    const unsigned s0 = t % 3u, s1 = (t + 2u) % 3u, s2 = (t + 1u) % 3u;
+    const float ilv = r.c[k], i2v = r.c[n + k], vv2 = r.c[2 * n + k], vj1 = r.c[3 * n + k];
+    const float vj2 = r.c[4 * n + k], vvd = r.c[5 * n + k], ib0 = r.c[6 * n + k], b1 = r.c[7 * n + k];
+    const float b2 = r.c[8 * n + k];
+    // DoPreVoltageUpdates: Il += i2v*ilv*Vd[n-1]
+    const float il = fadd(r.il[k], fmul(fmul(i2v, ilv), r.vd[s1 * n + k]));
+    r.il[k] = il;
+    // Apply2Voltages
+    const float vd2 = r.vd[s2 * n + k], j1 = r.j[s1 * n + k], j2 = r.j[s2 * n + k];
+    const unsigned long long o = r.off[k];
+    float vd0 = V[o];
+    vd0 = fmul(vvd, fadd(fadd(fadd(fsub(vd0, il), fmul(vv2, vd2)), fmul(vj1, j1)), fmul(vj2, j2)));
+    r.j[s0 * n + k] = fsub(fsub(fmul(ib0, fsub(vd0, vd2)), fmul(fmul(b1, ib0), j1)), fmul(fmul(b2, ib0), j2));
+    r.vd[s0 * n + k] = vd0;
+    V[o] = vd0;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:83-178) as separate launches: phase
 // 0 = pre (before the voltage update), 1 = post (after it), 2 = apply (after the dispersive apply
 // hooks).  With the hooks inside the voltage update (mur_cell / mur_z_*) only phase 2 runs.  A

@@ -106,6 +106,13 @@ class EngineBase:
                                 b[4].size, *[_p(x, ct) for x, ct in zip(b, ctypes_of)],
                                 _p(sv, C.c_float), _p(sc, C.c_float), sv.size, int(t.period), int(t.max_delay)),
                      "set_tfsf")
+        r = getattr(op, "rlc", None)
+        if r is not None:
+            pos = self._a(r.pos, np.uint32)
+            dr = self._a(r.dir, np.int32)
+            cs = [self._a(getattr(r, k), f32) for k in ("ilv", "i2v", "vv2", "vj1", "vj2", "vvd", "ib0", "b1", "b2")]
+            self._ck(L.set_lumped_rlc(self.h, dr.size, _p(pos, C.c_uint), _p(dr, C.c_int),
+                                      *[_p(c, C.c_float) for c in cs]), "set_lumped_rlc")
         for p in op.vprobes:
             pid = C.c_int(-1)
             s = self._a(p.start, np.uint32)

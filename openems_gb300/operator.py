@@ -130,9 +130,13 @@ class Structure:
     def AddMetal(self, name):
         return self._add(METAL, name)
 
-    def AddLumpedElement(self, name, ny, R=float('nan'), C=float('nan'), caps=True):
-        """Parallel RC lumped element (CSPropLumpedElement, LEtype PARALLEL, no L)."""
-        return self._add(LUMPED, name, ny=int(ny), R=float(R), C=float(C), caps=bool(caps))
+    def AddLumpedElement(self, name, ny, R=float('nan'), C=float('nan'), caps=True, L=float('nan'), LEtype=0):
+        """Lumped element (CSPropLumpedElement): LEtype 0 = parallel, 1 = series, -1 = invalid.
+        A parallel element without L > 0 is the parallel RC of the main operator
+        (Operator::Calc_LumpedElements); a parallel element with L > 0 and every series element
+        go through the lumped RLC extension (Operator_Ext_LumpedRLC)."""
+        return self._add(LUMPED, name, ny=int(ny), R=float(R), C=float(C), caps=bool(caps), L=float(L),
+                         LEtype=int(LEtype))
 
     def AddExcitation(self, name, exc_type, exc_val, delay=0.0):
         return self._add(EXCITATION, name, exc_type=int(exc_type),
@@ -254,6 +258,23 @@ class TFSFTable:
 
 
 @dataclass
+class LumpedRLCTable:
+    """Operator_Ext_LumpedRLC (FDTD/extensions/operator_ext_lumpedRLC.h:58-82): one entry per
+    lumped edge, in the reference's build order."""
+    pos: np.ndarray               # uint32 [3, K]
+    dir: np.ndarray               # int32 [K]
+    ilv: np.ndarray               # parallel inductor: dT/dL
+    i2v: np.ndarray               # parallel: (dT/dC)/(1 + dT*dG/(2*dC))
+    vv2: np.ndarray               # series coefficients
+    vj1: np.ndarray
+    vj2: np.ndarray
+    vvd: np.ndarray
+    ib0: np.ndarray
+    b1: np.ndarray
+    b2: np.ndarray
+
+
+@dataclass
 class VoltageProbe:
     name: str
     start: np.ndarray
@@ -312,6 +333,25 @@ class OperatorData:
     excitation: Optional[Excitation] = None
     grid: Optional[Grid] = None
     tfsf: Optional[TFSFTable] = None
+    rlc: Optional[LumpedRLCTable] = None
+
+
+# lumped element types (CSPropLumpedElement::LEtype)
+LE_INVALID, LE_PARALLEL, LE_SERIES = -1, 0, 1
+LUMPED_RLC_Z_FACT = 20.0      # FDTD/extensions/operator_ext_lumpedRLC.h:30
+
+
+def _is_par_rc(prop):
+    """Operator::IsLEparRC (FDTD/operator.cpp:1765-1775)."""
+    L = prop.params.get("L", float("nan"))
+    return prop.params.get("LEtype", LE_PARALLEL) == LE_PARALLEL and not (L > 0.0)
+
+
+def _is_lumped_rlc(prop):
+    """Operator_Ext_LumpedRLC::IsLElumpedRLC (operator_ext_lumpedRLC.cpp:550-561)."""
+    t = prop.params.get("LEtype", LE_PARALLEL)
+    L = prop.params.get("L", float("nan"))
+    return (t == LE_PARALLEL and L > 0.0) or t == LE_SERIES
 
 
 # =========================================================================================
@@ -873,11 +913,13 @@ class Operator:
         mur = self._build_mur(exc)
         upml = self._build_upml()
         lorentz = self._build_lorentz()
+        # Operator_Ext_LumpedRLC is added after the dispersive extensions (openems.cpp:1236-1241)
+        rlc = self._build_lumped_rlc()
         vprobes, iprobes, dumps = self._build_processing()
         data = OperatorData(num_lines=self.N.astype(np.uint32), dt=dT, vv=self.vv, vi=self.vi, ii=self.ii,
                             iv=self.iv, exc=exc, upml=upml, mur=mur, lorentz=lorentz, vprobes=vprobes,
                             iprobes=iprobes, dumps=dumps, nyquist=self.exc.GetNyquistNum(),
-                            excitation=self.exc, grid=self.grid, tfsf=tfsf)
+                            excitation=self.exc, grid=self.grid, tfsf=tfsf, rlc=rlc)
         return data
 
     # ---- boundary conditions ---------------------------------------------------------------
@@ -937,6 +979,8 @@ class Operator:
         u = self.unit
         for prop in self.csx.props:
             if prop.kind != LUMPED:
+                continue
+            if not _is_par_rc(prop):      # Operator::IsLEparRC (FDTD/operator.cpp:1765-1775)
                 continue
             C = prop.params["C"]
             R = prop.params["R"]
@@ -1489,6 +1533,139 @@ class Operator:
         return out
 
     # ---- Lorentz / Drude (operator_ext_lorentzmaterial.cpp:120-445) ---------------------------
+    def _build_lumped_rlc(self):
+        """Operator_Ext_LumpedRLC::BuildExtension (operator_ext_lumpedRLC.cpp:111-528): series RLC
+        elements and parallel elements with an inductor, boxes only.  Rewrites EC_C/EC_G and the
+        coefficients of the element edges (Calc_ECOperatorPos) and builds the ADE table; None
+        when there is no such element."""
+        dT = self.dT
+        fmax = self.exc.f0 + self.exc.fc        # GetCenterFreq() + GetCutOffFreq()
+        ft = self.ft
+        cols = {k: [] for k in ("ilv", "i2v", "vv2", "vj1", "vj2", "vvd", "ib0", "b1", "b2")}
+        P, D = [], []
+        for prop in self.csx.props:
+            if prop.kind != LUMPED:
+                continue
+            prm = prop.params
+            d = prm["ny"]
+            t = prm.get("LEtype", LE_PARALLEL)
+            if t == LE_INVALID:
+                t = LE_PARALLEL
+            C, R, L = prm["C"], prm["R"], prm.get("L", float("nan"))
+            if C < 0.0:
+                C = 0.0
+            if R < 0.0:
+                R = 0.0
+            if L < 0.0:
+                L = 0.0
+            if math.isnan(C):
+                C = 0.0
+            if math.isnan(L):
+                L = 0.0
+            if math.isnan(R):
+                R = 0.0
+            if not _is_lumped_rlc(prop):
+                continue
+            if d < 0 or d > 2:
+                continue
+            d1, d2 = (d + 1) % 3, (d + 2) % 3
+            for lo, hi, *_ in prop.boxes:
+                dim, s0, e0, _, _ = self.snap_box(lo, hi, dual=False, method=0)
+                if dim <= 0:
+                    continue
+                s0 = [int(v) for v in s0]
+                e0 = [int(v) for v in e0]
+                if s0[d] == e0[d]:
+                    continue
+                n0 = e0[d] - s0[d]
+                n1 = e0[d1] - s0[d1] + 1
+                n2 = e0[d2] - s0[d2] + 1
+                npar = n1 * n2
+                dL = L * npar / n0
+                dR = R * npar / n0
+                dG = (1 / R) * n0 / npar if R != 0 else math.inf
+                dC = C * n0 / npar
+                # series RLC coefficients (only the series elements use them); a series element
+                # with C = 0 is a short for the capacitor
+                ib0 = b1 = b2 = 0.0
+                if t == LE_SERIES and C == 0:
+                    ib0 = dT / (2.0 * dL + dT * dR)
+                    b1 = -4.0 * dL / dT
+                    b2 = (2.0 * dL - dT * dR) / dT
+                elif t == LE_SERIES:
+                    ib0 = 2.0 * dT * dC / (4.0 * dL * dC + 2.0 * dT * dR * dC + dT * dT)
+                    b1 = (dT * dT - 4.0 * dL * dC) / (dT * dC)
+                    b2 = (4.0 * dL * dC - 2.0 * dT * dR * dC + dT * dT) / (2.0 * dT * dC)
+                if t == LE_PARALLEL and R == 0.0:
+                    dG = 0.0
+                pos = [0, 0, 0]
+                for pos[d] in range(s0[d], e0[d]):
+                    for pos[d1] in range(s0[d1], e0[d1] + 1):
+                        for pos[d2] in range(s0[d2], e0[d2] + 1):
+                            x, y, z = pos
+                            if t == LE_PARALLEL:
+                                if dC > 0:
+                                    self.EC_C[d, x, y, z] = dC
+                                else:
+                                    dC = float(self.EC_C[d, x, y, z])   # the natural capacitor, kept for the next edges
+                                with np.errstate(divide="ignore", invalid="ignore"):
+                                    c64 = np.float64(dC)
+                                    cols["i2v"].append(float((dT / c64) / (1.0 + dT * dG / (2.0 * c64))))
+                                if R >= 0:
+                                    self.EC_G[d, x, y, z] = dG
+                                cols["ilv"].append(dT / dL if L > 0 else 0.0)
+                                if dC == 0:
+                                    Cd = float(self.EC_C[d, x, y, z])
+                                    zmin = max(dR, 2 * PI * fmax * dL)
+                                    zcd = 1.0 / (2.0 * PI * fmax * Cd) if Cd != 0 else math.inf
+                                    if zcd < LUMPED_RLC_Z_FACT * zmin:
+                                        self.EC_C[d, x, y, z] = 1.0 / (2 * PI * fmax * zmin * LUMPED_RLC_Z_FACT)
+                                for k, v in (("vv2", 0.0), ("vj1", 0.0), ("vj2", 0.0), ("vvd", 1.0), ("ib0", 0.0),
+                                             ("b1", 0.0), ("b2", 0.0)):
+                                    cols[k].append(v)
+                            else:
+                                self.EC_G[d, x, y, z] = 0.0
+                                Cd = float(self.EC_C[d, x, y, z])       # FDTD_FLOAT Cd
+                                if dC:
+                                    zmin = math.sqrt(math.pow(dR, 2) + math.pow(2 * PI * fmax * dL - 1.0 / (dC * 2 * PI * fmax), 2))
+                                else:
+                                    zmin = math.sqrt(math.pow(dR, 2) + math.pow(2 * PI * fmax * dL, 2))
+                                zcd = 1.0 / (2.0 * PI * fmax * Cd) if Cd != 0 else math.inf
+                                if zcd < LUMPED_RLC_Z_FACT * zmin:
+                                    Cd = float(ft(1.0 / (2 * PI * fmax * zmin * LUMPED_RLC_Z_FACT)))
+                                    self.EC_C[d, x, y, z] = Cd
+                                cols["ilv"].append(0.0)
+                                cols["i2v"].append(0.0)
+                                cols["vv2"].append(0.5 * dT * ib0 / Cd)
+                                cols["vj1"].append(0.5 * dT * (b1 * ib0 - 1.0) / Cd)
+                                cols["vj2"].append(0.5 * dT * b2 * ib0 / Cd)
+                                cols["vvd"].append(1.0 / (1.0 + 0.5 * dT * ib0 / Cd))
+                                cols["ib0"].append(ib0)
+                                cols["b1"].append(b1)
+                                cols["b2"].append(b2)
+                            a_, b_, c_, d_ = self._ec_op(self.EC_C[d, x, y, z], self.EC_G[d, x, y, z],
+                                                         self.EC_L[d, x, y, z], self.EC_R[d, x, y, z], dT)
+                            self.vv[d, x, y, z], self.vi[d, x, y, z] = a_, b_
+                            self.ii[d, x, y, z], self.iv[d, x, y, z] = c_, d_
+                            D.append(d)
+                            P.append(tuple(pos))
+                if prm["caps"]:
+                    for pos[d1] in range(s0[d1], e0[d1] + 1):
+                        for pos[d2] in range(s0[d2], e0[d2] + 1):
+                            for pos[d] in (s0[d], e0[d]):
+                                x, y, z = pos
+                                if pos[d1] < e0[d1]:
+                                    self.vv[d1, x, y, z] = 0
+                                    self.vi[d1, x, y, z] = 0
+                                if pos[d2] < e0[d2]:
+                                    self.vv[d2, x, y, z] = 0
+                                    self.vi[d2, x, y, z] = 0
+        if not D:
+            return None
+        with np.errstate(over="ignore", invalid="ignore"):
+            arr = {k: np.array(v, np.float64).astype(ft) for k, v in cols.items()}
+        return LumpedRLCTable(np.array(P, np.uint32).T.copy(), np.array(D, np.int32), **arr)
+
     def _build_lorentz(self):
         """Operator_Ext_LorentzMaterial::BuildExtension, evaluated in parallel x-slabs; positions
         come out in the reference's x-major scan order."""

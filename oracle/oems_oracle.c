@@ -126,6 +126,12 @@ typedef struct oems_ref_engine {
     unsigned *tf_v_idx, *tf_i_idx, *tf_v_delay, *tf_i_delay, *tf_lut;
     unsigned short *tf_v_dir, *tf_i_dir;
     float *tf_v_delta, *tf_i_delta, *tf_v_amp, *tf_i_amp, *tf_sig_v, *tf_sig_i;
+    /* lumped RLC loads: coefficients and the reference's rotating state buffers */
+    unsigned rlc_n;
+    unsigned *rlc_pos;
+    int *rlc_dir;
+    float *rlc_c; /* [9][n]: ilv, i2v, vv2, vj1, vj2, vvd, ib0, b1, b2 */
+    float *rlc_il, *rlc_vd[3], *rlc_j[3];
     /* extensions */
     upml_t upml[MAX_UPML];
     int nupml;
@@ -246,6 +252,8 @@ void oems_ref_destroy(eng_t *e)
     free(e->tf_v_idx); free(e->tf_i_idx); free(e->tf_v_delay); free(e->tf_i_delay); free(e->tf_lut);
     free(e->tf_v_dir); free(e->tf_i_dir); free(e->tf_v_delta); free(e->tf_i_delta);
     free(e->tf_v_amp); free(e->tf_i_amp); free(e->tf_sig_v); free(e->tf_sig_i);
+    free(e->rlc_pos); free(e->rlc_dir); free(e->rlc_c); free(e->rlc_il);
+    for (int q = 0; q < 3; ++q) { free(e->rlc_vd[q]); free(e->rlc_j[q]); }
     for (int r = 0; r < e->nupml; ++r) {
         upml_t *u = &e->upml[r];
         free(u->vv); free(u->vvfo); free(u->vvfn); free(u->ii); free(u->iifo); free(u->iifn);
@@ -474,6 +482,32 @@ int oems_ref_set_tfsf(eng_t *e, unsigned nV, const unsigned *v_idx, const unsign
     e->tf_len = length;
     e->tf_period = period;
     e->tf_max_delay = max_delay;
+    return OK;
+}
+
+int oems_ref_set_lumped_rlc(eng_t *e, unsigned n, const unsigned *pos, const int *dir, const float *ilv,
+                            const float *i2v, const float *vv2, const float *vj1, const float *vj2,
+                            const float *vvd, const float *ib0, const float *b1, const float *b2)
+{
+    if (!e)
+        return ERR_ARG;
+    if (e->inited)
+        return ERR_STATE;
+    for (unsigned k = 0; k < n; ++k)
+        if (pos[k] >= e->N[0] || pos[n + k] >= e->N[1] || pos[2 * n + k] >= e->N[2] || dir[k] < 0 || dir[k] > 2)
+            return ERR_ARG;
+    e->rlc_n = n;
+    e->rlc_pos = (unsigned *)dupmem(pos, 12 * (size_t)n);
+    e->rlc_dir = (int *)dupmem(dir, 4 * (size_t)n);
+    e->rlc_c = (float *)xcalloc(9 * (size_t)n + 1, 4);
+    const float *src[9] = {ilv, i2v, vv2, vj1, vj2, vvd, ib0, b1, b2};
+    for (int q = 0; q < 9; ++q)
+        memcpy(e->rlc_c + (size_t)q * n, src[q], 4 * (size_t)n);
+    e->rlc_il = (float *)xcalloc((size_t)n + 1, 4);
+    for (int q = 0; q < 3; ++q) {
+        e->rlc_vd[q] = (float *)xcalloc((size_t)n + 1, 4);
+        e->rlc_j[q] = (float *)xcalloc((size_t)n + 1, 4);
+    }
     return OK;
 }
 
@@ -1008,6 +1042,45 @@ static void tfsf_apply(eng_t *e, int curr)
     }
 }
 
+/* Engine_Ext_LumpedRLC::DoPreVoltageUpdates (FDTD/extensions/engine_ext_lumpedRLC.cpp:80-95) */
+static void rlc_pre(eng_t *e)
+{
+    if (!e->rlc_n)
+        return;
+    float *t = e->rlc_vd[2];
+    e->rlc_vd[2] = e->rlc_vd[1];
+    e->rlc_vd[1] = e->rlc_vd[0];
+    e->rlc_vd[0] = t;
+    unsigned n = e->rlc_n;
+    const float *ilv = e->rlc_c, *i2v = e->rlc_c + n;
+    for (unsigned k = 0; k < n; ++k)
+        e->rlc_il[k] += i2v[k] * ilv[k] * e->rlc_vd[1][k];
+}
+
+/* Engine_Ext_LumpedRLC::Apply2VoltagesImpl (engine_ext_lumpedRLC.cpp:97-141) */
+static void rlc_apply(eng_t *e)
+{
+    if (!e->rlc_n)
+        return;
+    float *t = e->rlc_j[2];
+    e->rlc_j[2] = e->rlc_j[1];
+    e->rlc_j[1] = e->rlc_j[0];
+    e->rlc_j[0] = t;
+    unsigned n = e->rlc_n;
+    const float *c = e->rlc_c;
+    const float *vv2 = c + 2 * n, *vj1 = c + 3 * n, *vj2 = c + 4 * n, *vvd = c + 5 * n, *ib0 = c + 6 * n;
+    const float *b1 = c + 7 * n, *b2 = c + 8 * n;
+    float **Vd = e->rlc_vd, **J = e->rlc_j;
+    for (unsigned k = 0; k < n; ++k)
+        Vd[0][k] = *fptr(e, 0, e->rlc_dir[k], e->rlc_pos[k], e->rlc_pos[n + k], e->rlc_pos[2 * n + k]);
+    for (unsigned k = 0; k < n; ++k) {
+        Vd[0][k] = vvd[k] * (Vd[0][k] - e->rlc_il[k] + vv2[k] * Vd[2][k] + vj1[k] * J[1][k] + vj2[k] * J[2][k]);
+        J[0][k] = ib0[k] * (Vd[0][k] - Vd[2][k]) - (b1[k] * ib0[k]) * J[1][k] - (b2[k] * ib0[k]) * J[2][k];
+    }
+    for (unsigned k = 0; k < n; ++k)
+        *fptr(e, 0, e->rlc_dir[k], e->rlc_pos[k], e->rlc_pos[n + k], e->rlc_pos[2 * n + k]) = Vd[0][k];
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* processing */
 
@@ -1194,6 +1267,7 @@ static void pre_volt(eng_t *e)
         mur_pre(e, &e->mur[w]);
     for (int o = 0; o < e->nlor; ++o)
         lorentz_pre_volt(e, &e->lor[o]);
+    rlc_pre(e);
 }
 
 static void post_volt_apply(eng_t *e)
@@ -1202,6 +1276,9 @@ static void post_volt_apply(eng_t *e)
     tfsf_apply(e, 0);
     for (int w = e->nmur - 1; w >= 0; --w)
         mur_post(e, &e->mur[w]);
+    /* apply hooks: lumped RLC (added last among the priority-0 extensions, so first after the
+       reversed stable sort), dispersive, Mur, excitation */
+    rlc_apply(e);
     for (int o = 0; o < e->nlor; ++o)
         lorentz_apply(e, &e->lor[o], 0);
     for (int w = e->nmur - 1; w >= 0; --w)

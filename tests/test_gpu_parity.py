@@ -53,6 +53,8 @@ CASES = [
                                                          box=([0, 6, 5], [20, 23, 19]), steps=220), 220),
     ("plane_wave_sinus", lambda: configs.plane_wave(k_dir=(-0.2, -1.0, 0.4), e_dir=(1.0, 0.0, 0.5), sinus=True,
                                                    steps=200), 200),
+    ("lumped_rlc_mur", lambda: configs.lumped_rlc(steps=300), 300),
+    ("lumped_rlc_upml_dispersive", lambda: configs.lumped_rlc(bc=(3,) * 6, dispersive=True, steps=240), 240),
 ]
 
 
