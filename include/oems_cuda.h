@@ -33,6 +33,7 @@ extern "C" {
 #define OEMS_ERR_UNSUPPORTED  4   /* extension/feature not supported by this engine            */
 #define OEMS_ERR_DEVICE       5   /* device-side status flag raised (non-finite field, ...)    */
 #define OEMS_ERR_NOMEM        6   /* device allocation failed                                   */
+#define OEMS_ERR_IO           8   /* a dump file could not be written                           */
 
 /* which field for read/write calls */
 #define OEMS_VOLT 0
@@ -167,14 +168,38 @@ int oems_cuda_add_current_probe(oems_cuda_engine* eng, const unsigned int start[
 int oems_cuda_set_probe_dft(oems_cuda_engine* eng, int probe_id, unsigned int fd_interval,
                             unsigned int num_freqs, const double* freqs);
 
-/* ProcessFieldsFD (Common/processfields_fd.cpp:72-107) with cell interpolation
- * (FDTD/engine_interface_fdtd.cpp:104-121, 182-199) over the box start..stop (inclusive):
- * field 0 = E (main time), 1 = H (dual time). edge_len[n] / dual_edge_len[n] are the mesh
- * edge lengths in metres per line (Operator::GetEdgeLength, FDTD/operator.cpp:212-215),
- * float64 [numLines[n]] each, concatenated x,y,z. Returns the dump id through *id. */
-int oems_cuda_add_fd_dump(oems_cuda_engine* eng, int field, const unsigned int start[3],
+/* ProcessFieldsFD (Common/processfields_fd.cpp:72-107) over the box start..stop (inclusive):
+ * field 0 = E (main time), 1 = H (dual time); interp = the dump mode, i.e. the interpolation of
+ * Engine_Interface_FDTD (FDTD/engine_interface_fdtd.cpp:63-204): 0 none (the raw Yee values),
+ * 1 node interpolation, 2 cell interpolation. start/stop are the box snapped the way
+ * ProcessFields snaps it (the dual mesh for cell interpolation and for H without interpolation).
+ * edge_len[n] / dual_edge_len[n] are the mesh edge lengths in metres per line
+ * (Operator::GetEdgeLength, FDTD/operator.cpp:212-215), float64 [numLines[n]] each,
+ * concatenated x,y,z. Returns the dump id through *id. */
+int oems_cuda_add_fd_dump(oems_cuda_engine* eng, int field, int interp, const unsigned int start[3],
                           const unsigned int stop[3], unsigned int fd_interval, unsigned int num_freqs,
                           const double* freqs, const double* edge_len, const double* dual_edge_len, int* id);
+
+/* ProcessFieldsTD (Common/processfields_td.cpp:50-91): the dump box's E (field 0, main time) or H
+ * (field 1, dual time) with interpolation `interp` (as for oems_cuda_add_fd_dump) at every step
+ * numTS with numTS % interval == 0 within [start_ts, stop_ts] (Processing::CheckTimestep), numTS = 0
+ * included. Each sample is written by a writer thread of the engine to
+ * <file_prefix>_<numTS as 8 digits>.vtr, a VTK XML rectilinear grid (tools/vtk_file_writer.cpp:
+ * 312-371 names the files the same way) holding the sample coordinates `coords` (metres, the
+ * dump's x lines, then y, then z: stop-start+1 values per axis) and the vector field "E-Field" or
+ * "H-Field" in float32, raw appended binary. The samples reach the host by asynchronous copies
+ * into pinned buffers enqueued after each chunk of steps; the simulation does not wait for the
+ * disk unless the writer falls four samples behind. Shares the id space of the FD dumps.
+ * oems_cuda_profile_steps, the batched and the adjoint forms reject engines with TD dumps. */
+int oems_cuda_add_td_dump(oems_cuda_engine* eng, int field, int interp, const unsigned int start[3],
+                          const unsigned int stop[3], unsigned int interval, unsigned int start_ts,
+                          unsigned int stop_ts, const double* edge_len, const double* dual_edge_len,
+                          const double* coords, const char* file_prefix, int* id);
+
+/* Wait until every time-domain dump sample of the steps issued so far is written to its file;
+ * OEMS_ERR_IO (with oems_cuda_last_error) if a file could not be written. oems_cuda_destroy
+ * also finishes the pending files. */
+int oems_cuda_flush_dumps(oems_cuda_engine* eng);
 
 /* ---- run ------------------------------------------------------------------------------------ */
 

@@ -14,7 +14,7 @@ CUDA_LIB = os.path.join(HERE, "_build", "liboems_cuda.so")
 
 OEMS_OK = 0
 ERRORS = {1: "OEMS_ERR_ARG", 2: "OEMS_ERR_CUDA", 3: "OEMS_ERR_STATE", 4: "OEMS_ERR_UNSUPPORTED",
-          5: "OEMS_ERR_DEVICE", 6: "OEMS_ERR_NOMEM", 7: "OEMS_ERR_TOO_LARGE"}
+          5: "OEMS_ERR_DEVICE", 6: "OEMS_ERR_NOMEM", 7: "OEMS_ERR_TOO_LARGE", 8: "OEMS_ERR_IO"}
 
 P = C.c_void_p
 U = C.c_uint
@@ -44,7 +44,8 @@ SIGNATURES = {
     "add_voltage_probe": (I, [P, PU, PU, D, U, U, U, PI_]),
     "add_current_probe": (I, [P, PU, PU, I, PI_, PI_, D, U, U, U, PI_]),
     "set_probe_dft": (I, [P, I, U, U, PD]),
-    "add_fd_dump": (I, [P, I, PU, PU, U, U, PD, PD, PD, PI_]),
+    "add_fd_dump": (I, [P, I, I, PU, PU, U, U, PD, PD, PD, PI_]),
+    "add_td_dump": (I, [P, I, I, PU, PU, U, U, U, PD, PD, PD, C.c_char_p, PI_]),
     "init": (I, [P, U]),
     "iterate": (I, [P, U]),
     "sync": (I, [P]),
@@ -68,6 +69,7 @@ CUDA_ONLY = {
     "timed_iterate": (I, [P, U, PF]),
     "profile_steps": (I, [P, U, PF, PU]),
     "read_probe_range": (I, [P, I, SZ, SZ, PD]),
+    "flush_dumps": (I, [P]),
     "energy_noalloc": (I, [P, P, PU, U, P, PD]),
     "batch_create": (I, [C.POINTER(P), U, C.POINTER(P)]),
     "batch_run": (I, [P, PU, U, U]),

@@ -10,11 +10,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC_DIR = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboems_cuda.so")
-SOURCES = ["engine.cu", "batch.cu", "energy_noalloc.cu", "adjoint.cu", "nf2ff.cu", "opbuild.cu"]
+SOURCES = ["engine.cu", "batch.cu", "energy_noalloc.cu", "adjoint.cu", "nf2ff.cu", "opbuild.cu", "tddump.cu"]
 HEADERS = ["kernels.cuh", "engine_impl.h", "fused.cuh"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-shared"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-pthread", "-shared", "-lpthread"]
 
 
 def _nvcc():

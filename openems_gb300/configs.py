@@ -121,6 +121,13 @@ def small_mixed(n=(18, 16, 14), steps=200, bc=(3, 3, 2, 2, 0, 3), pml=4, seed=1,
             d = csx.AddDump(name, dump_type=f_idx, dump_mode=1, frequency=[4e9, 6e9])
             d.AddBox([lo[0], lo[1], lo[2]], [hi[0], hi[1], lo[2]])
             d.AddBox([lo[0], lo[1], lo[2]], [lo[0], hi[1], hi[2]])
+        # the other two interpolation types: cell-interpolated (dual mesh) and raw Yee values
+        for f_idx, name in ((10, "cell_E"), (11, "cell_H")):
+            csx.AddDump(name, dump_type=f_idx, dump_mode=2, frequency=[5e9]).AddBox(
+                [lo[0], lo[1], hi[2]], [hi[0], hi[1], hi[2]])
+        for f_idx, name in ((10, "raw_E"), (11, "raw_H")):
+            csx.AddDump(name, dump_type=f_idx, dump_mode=0, frequency=[5e9]).AddBox(
+                [gl[0][0], gl[1][0], gl[2][0]], [gl[0][-1], gl[1][-1], gl[2][3]])
     op = Operator(csx, g, exc, bc=bc, pml_size=(pml,) * 6)
     return op.build(steps)
 
@@ -309,6 +316,38 @@ def lc_tank(L=1e-9, C=1e-12, steps=6000, n=20):
     csx.AddExcitation("kick", 0, [0, 0, 1.0]).AddBox(*box)
     csx.AddProbe("u_tank", 0, interval=1).AddBox(*box)
     op = Operator(csx, g, exc, bc=(0,) * 6)
+    return op.build(steps)
+
+
+def td_dumps(n=(16, 14, 12), steps=120, bc=(2, 2, 3, 3, 0, 0), seed=5):
+    """Time-domain field dumps (dump types 0/1) of every interpolation type on a small graded mesh
+    with a dielectric block and a point source: E and H volumes with node interpolation, an E plane
+    with cell interpolation, an H line without interpolation that starts and stops at given times,
+    and a two-box E dump (files named <name>_0 and <name>_1)."""
+    rng = np.random.default_rng(seed)
+    lines = [np.cumsum(np.concatenate([[0.0], rng.uniform(0.7, 1.3, k - 1)])) for k in n]
+    g = Grid(lines, unit=1e-3)
+    gl = g.lines
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(8e9, 6e9)
+    c = [k // 2 for k in n]
+    csx.AddMaterial("diel", epsilon=3.0, kappa=0.01).AddBox([gl[0][2], gl[1][2], gl[2][2]], [gl[0][c[0]], gl[1][-4], gl[2][c[2]]])
+    csx.AddExcitation("src", 0, [0, 0, 1.0]).AddBox([gl[0][c[0]], gl[1][c[1]], gl[2][c[2]]],
+                                                   [gl[0][c[0]], gl[1][c[1]], gl[2][c[2] + 1]])
+    csx.AddProbe("ut", 0, interval=1).AddBox([gl[0][c[0]], gl[1][c[1]], gl[2][c[2]]], [gl[0][c[0]], gl[1][c[1]], gl[2][c[2] + 1]])
+    lo = [l[0] for l in gl]
+    hi = [l[-1] for l in gl]
+    csx.AddDump("Et_node", dump_type=0, dump_mode=1).AddBox(lo, hi)
+    csx.AddDump("Ht_node", dump_type=1, dump_mode=1).AddBox(lo, hi)
+    csx.AddDump("Et_cell", dump_type=0, dump_mode=2).AddBox([lo[0], lo[1], gl[2][c[2]]], [hi[0], hi[1], gl[2][c[2]]])
+    dt_guess = 1.0 / (3e8 * np.sqrt(3) / 0.7e-3)     # about the mesh's timestep, for the window
+    csx.AddDump("Ht_raw", dump_type=1, dump_mode=0, start_time=20 * dt_guess, stop_time=90 * dt_guess).AddBox(
+        [gl[0][1], gl[1][c[1]], gl[2][c[2]]], [gl[0][-2], gl[1][c[1]], gl[2][c[2]]])
+    two = csx.AddDump("Et_two", dump_type=0, dump_mode=1)
+    two.AddBox([gl[0][1], gl[1][1], gl[2][1]], [gl[0][4], gl[1][3], gl[2][5]])
+    two.AddBox([gl[0][c[0]], gl[1][c[1]], gl[2][0]], [gl[0][c[0]], gl[1][c[1]], gl[2][-1]])
+    op = Operator(csx, g, exc, bc=bc, pml_size=(3,) * 6)
     return op.build(steps)
 
 

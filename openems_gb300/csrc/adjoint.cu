@@ -477,7 +477,7 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     if (!e || !box_start || !box_stop) return OEMS_ERR_ARG;
     if (!e->inited) return afail(e, OEMS_ERR_STATE, "engine not initialised");
     if (e->adj) return afail(e, OEMS_ERR_STATE, "adjoint already set up");
-    if (!e->mur.empty() || !e->lor.empty() || e->has_tfsf || e->rlc.count)
+    if (!e->mur.empty() || !e->lor.empty() || e->has_tfsf || e->rlc.count || e->has_td)
         return afail(e, OEMS_ERR_UNSUPPORTED,
                      "adjoint: Mur walls, dispersive materials, TFSF and lumped RLC loads are not supported");
     for (int a = 0; a < 3; ++a)

@@ -263,6 +263,7 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     if (!e) return;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    td_free(e);
     if (e->graph1) cudaGraphExecDestroy(e->graph1);
     if (e->graphK) cudaGraphExecDestroy(e->graphK);
     oems_adjoint_free(e->adj);
@@ -550,15 +551,17 @@ int oems_cuda_set_probe_dft(oems_cuda_engine* e, int id, unsigned int fd_interva
     return OEMS_OK;
 }
 
-int oems_cuda_add_fd_dump(oems_cuda_engine* e, int field, const unsigned int start[3], const unsigned int stop[3],
-                          unsigned int fd_interval, unsigned int nf, const double* freqs, const double* el,
-                          const double* del, int* id)
+int oems_cuda_add_fd_dump(oems_cuda_engine* e, int field, int interp, const unsigned int start[3],
+                          const unsigned int stop[3], unsigned int fd_interval, unsigned int nf, const double* freqs,
+                          const double* el, const double* del, int* id)
 {
-    if (!e || !start || !stop || !el || !del || !id || (field != 0 && field != 1) || (nf && !freqs))
+    if (!e || !start || !stop || !el || !del || !id || (field != 0 && field != 1) || (nf && !freqs) ||
+        interp < 0 || interp > 2)
         return OEMS_ERR_ARG;
     if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
     DumpHost d;
     d.field = field;
+    d.interp = interp;
     for (int a = 0; a < 3; ++a) {
         if (start[a] > stop[a] || stop[a] >= e->N[a]) return fail(e, OEMS_ERR_ARG, "dump box outside the mesh");
         d.start[a] = start[a];
@@ -571,6 +574,50 @@ int oems_cuda_add_fd_dump(oems_cuda_engine* e, int field, const unsigned int sta
     *id = (int)e->dumps.size();
     e->dumps.push_back(std::move(d));
     return OEMS_OK;
+}
+
+int oems_cuda_add_td_dump(oems_cuda_engine* e, int field, int interp, const unsigned int start[3],
+                          const unsigned int stop[3], unsigned int interval, unsigned int start_ts,
+                          unsigned int stop_ts, const double* el, const double* del, const double* coords,
+                          const char* file_prefix, int* id)
+{
+    if (!e || !start || !stop || !el || !del || !coords || !file_prefix || !id || (field != 0 && field != 1) ||
+        interp < 0 || interp > 2 || interval == 0 || !file_prefix[0])
+        return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    DumpHost d;
+    d.field = field;
+    d.interp = interp;
+    size_t nc = 0;
+    for (int a = 0; a < 3; ++a) {
+        if (start[a] > stop[a] || stop[a] >= e->N[a]) return fail(e, OEMS_ERR_ARG, "dump box outside the mesh");
+        d.start[a] = start[a];
+        d.stop[a] = stop[a];
+        nc += stop[a] - start[a] + 1;
+    }
+    d.fd_interval = 0;
+    d.td = true;
+    d.td_interval = interval;
+    d.td_start = start_ts;
+    d.td_stop = stop_ts;
+    d.prefix = file_prefix;
+    d.coords.assign(coords, coords + nc);
+    const size_t tot = (size_t)e->N[0] + e->N[1] + e->N[2];
+    d.el.assign(field == 0 ? el : del, (field == 0 ? el : del) + tot);
+    *id = (int)e->dumps.size();
+    e->dumps.push_back(std::move(d));
+    e->has_td = true;
+    return OEMS_OK;
+}
+
+int oems_cuda_flush_dumps(oems_cuda_engine* e)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (!e->inited || !e->td) return OEMS_OK;
+    CK(cudaSetDevice(e->device));
+    int rc = td_flush(e);
+    if (rc) return rc;
+    return td_wait(e);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1173,11 +1220,31 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     for (const auto& p : e->dumps) {
         DumpDev d{};
         d.field = p.field;
+        d.interp = p.interp;
         for (int a = 0; a < 3; ++a) { d.start[a] = p.start[a]; d.sz[a] = p.stop[a] - p.start[a] + 1; }
         d.npos = d.sz[0] * d.sz[1] * d.sz[2];
         d.fd_interval = p.fd_interval;
         d.nf = (unsigned)p.freqs.size();
-        if (d.fd_interval && d.nf) {
+        if (p.td) {
+            // ring of device slots: up to two K-step graphs of samples within about 1 GB
+            const size_t slot_bytes = 12ull * d.npos;
+            const size_t fit = std::max<size_t>(1, (size_t(1) << 30) / slot_bytes);
+            d.td = 1;
+            d.td_interval = p.td_interval;
+            d.td_start = p.td_start;
+            d.td_stop = p.td_stop;
+            d.nslot = (unsigned)std::min<size_t>(2ull * e->K, fit);
+            // OEMS_CUDA_TD_SLOTS=n caps the ring (small rings exercise the flush and single-step paths)
+            if (const char* ev = getenv("OEMS_CUDA_TD_SLOTS")) {
+                const long v = strtol(ev, nullptr, 10);
+                if (v >= 1 && (unsigned long)v < d.nslot) d.nslot = (unsigned)v;
+            }
+            float* ring;
+            if ((rc = dalloc(e, &ring, (size_t)d.nslot * 3 * d.npos, true))) return rc;
+            d.ring = ring;
+            d.fd_interval = 0;
+            d.nf = 0;
+        } else if (d.fd_interval && d.nf) {
             d.nsamp = max_ts / d.fd_interval + 1;
             std::vector<float2> ph((size_t)d.nsamp * d.nf);
             for (unsigned k = 0; k < d.nsamp; ++k) {
@@ -1249,6 +1316,11 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     if ((rc = capture(e, 1, &e->graph1, false))) return rc;
     if ((rc = capture(e, e->K, &e->graphK, e->use_fused))) return rc;
     e->inited = true;
+    // time-domain dumps: start the writer and hand it the numTS = 0 samples
+    if (e->has_td) {
+        if ((rc = td_start_pipeline(e))) return rc;
+        if ((rc = td_flush(e))) return rc;
+    }
     return OEMS_OK;
 }
 
@@ -1259,6 +1331,7 @@ int oems_cuda_iterate(oems_cuda_engine* e, unsigned int n)
     if ((unsigned long long)e->host_numTS + n > e->max_ts)
         return fail(e, OEMS_ERR_ARG, "iterating beyond max_timesteps given to oems_cuda_init");
     CK(cudaSetDevice(e->device));
+    if (e->has_td) return td_iterate(e, n);
     unsigned done = 0;
     while (n - done >= e->K) { CK(cudaGraphLaunch(e->graphK, e->stream)); done += e->K; }
     while (done < n) { CK(cudaGraphLaunch(e->graph1, e->stream)); ++done; }
@@ -1298,6 +1371,7 @@ int oems_cuda_profile_steps(oems_cuda_engine* e, unsigned int n, float* ms, unsi
 {
     if (!e) return OEMS_ERR_ARG;
     if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    if (e->has_td) return fail(e, OEMS_ERR_UNSUPPORTED, "profiled steps bypass the time-domain dump pipeline");
     if ((unsigned long long)e->host_numTS + n > e->max_ts)
         return fail(e, OEMS_ERR_ARG, "iterating beyond max_timesteps given to oems_cuda_init");
     CK(cudaSetDevice(e->device));
@@ -1418,6 +1492,7 @@ int oems_cuda_read_fd_dump(oems_cuda_engine* e, int id, float* out, size_t cap)
     if (!e || !out || id < 0 || id >= (int)e->dump_dev.size()) return OEMS_ERR_ARG;
     if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
     const DumpDev& d = e->dump_dev[id];
+    if (d.td) return fail(e, OEMS_ERR_ARG, "dump is a time-domain dump (written to files)");
     const size_t n = (size_t)d.nf * 3 * d.npos * 2;
     if (cap < n) return fail(e, OEMS_ERR_ARG, "output buffer too small");
     if (n) {

@@ -52,6 +52,12 @@ struct RlcHost {
 };
 struct DumpHost {
     int field;
+    int interp = 2;          // 0 none, 1 node, 2 cell interpolation
+    // time-domain dump (oems_cuda_add_td_dump): samples written to VTK files by the writer
+    bool td = false;
+    unsigned td_interval = 1, td_start = 0, td_stop = 0xFFFFFFFFu;
+    std::string prefix;
+    std::vector<double> coords;   // sample coordinates in metres, x then y then z
     unsigned start[3], stop[3];
     unsigned fd_interval;
     std::vector<double> freqs;
@@ -65,6 +71,15 @@ using namespace oems_host;
 // adjoint state (adjoint.cu); freed by oems_cuda_destroy
 struct oems_adjoint_state;
 void oems_adjoint_free(oems_adjoint_state* s);
+
+// time-domain dump pipeline (tddump.cu): device ring -> pinned host buffers -> writer thread
+struct oems_td_pipeline;
+struct oems_cuda_engine;
+int td_start_pipeline(oems_cuda_engine* e);            // after the device structs exist
+int td_iterate(oems_cuda_engine* e, unsigned n);        // oems_cuda_iterate for engines with TD dumps
+int td_flush(oems_cuda_engine* e);                      // enqueue the copies of every pending sample
+int td_wait(oems_cuda_engine* e);                       // wait until every enqueued sample is written
+void td_free(oems_cuda_engine* e);
 
 struct oems_cuda_engine {
     int device = 0;
@@ -133,6 +148,8 @@ struct oems_cuda_engine {
     std::vector<void*> allocs;                            // freed on destroy
     std::vector<std::pair<void*, size_t>> state;          // snapshot regions (device)
     oems_adjoint_state* adj = nullptr;
+    oems_td_pipeline* td = nullptr;
+    bool has_td = false;
     // UPML work split of the update launches (used when the engine has UPML regions)
     bool use_split = false;
     SplitDev splitV{}, splitI{};

@@ -737,12 +737,17 @@ struct ProbeDev {
 
 struct DumpDev {
     int field;                       // 0 E (uses V), 1 H (uses I)
+    int interp;                      // 0 none, 1 node, 2 cell interpolation
     unsigned start[3], sz[3];
     unsigned npos;
     unsigned fd_interval, nf, nsamp;
     const float2* phasor;            // [nsamp][nf], includes *2 and *dt*fd_interval
     const double* el;                // GetEdgeLength per line, concatenated x,y,z (E: main, H: dual)
     float2* acc;                     // [nf][3][npos]
+    // time-domain dump (ProcessFieldsTD): td = 1; sample ts (ts % td_interval == 0 within
+    // [td_start, td_stop]) goes to ring slot (ts / td_interval) % nslot as float [3][npos]
+    unsigned td, td_interval, td_start, td_stop, nslot;
+    float* ring;
 };
 
 struct StepEndDev {
@@ -803,48 +808,69 @@ static __device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned 
     }
 }
 
-// cell-interpolated E (FDTD/engine_interface_fdtd.cpp:104-121) or H (:182-199) at pos
-static __device__ void cell_field(const GridDev& g, const DumpDev& d, const unsigned pos[3], double out[3])
+// E (Engine_Interface_FDTD::GetRawInterpolatedField, FDTD/engine_interface_fdtd.cpp:63-123) or
+// H (GetRawInterpolatedDualField, :140-204) at pos with the dump's interpolation: 0 the raw Yee
+// value over its edge length, 1 node interpolation, 2 cell interpolation.  Double arithmetic in
+// the reference's order.
+static __device__ void dump_field(const GridDev& g, const DumpDev& d, const unsigned pos[3], double out[3])
 {
     const unsigned N[3] = {g.Nx, g.Ny, g.Nz};
     const unsigned eoff[3] = {0u, g.Nx, g.Nx + g.Ny};
-    if (d.field == 0) {
+    const float* F = d.field == 0 ? g.V : g.I;
+    // GetRawField / GetRawDualField: value / edge length (0 for a zero length)
+    auto raw = [&](int n, const unsigned* p) -> double {
+        const double delta = d.el[eoff[n] + p[n]];
+        const float v = F[(unsigned long long)n * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2]];
+        return delta != 0.0 ? __ddiv_rn((double)v, delta) : 0.0;
+    };
+    const bool edge = pos[0] == N[0] - 1 || pos[1] == N[1] - 1 || pos[2] == N[2] - 1;
 #pragma unroll
-        for (int n = 0; n < 3; ++n) {
-            const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
-            if (pos[0] == N[0] - 1 || pos[1] == N[1] - 1 || pos[2] == N[2] - 1) { out[n] = 0.0; continue; }
-            unsigned ip[3] = {pos[0], pos[1], pos[2]};
-            double acc;
-            auto raw = [&](const unsigned* p) -> double {
-                const double delta = d.el[eoff[n] + p[n]];
-                const float v = g.V[(unsigned long long)n * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2]];
-                return delta != 0.0 ? __ddiv_rn((double)v, delta) : 0.0;
-            };
-            acc = raw(ip);
-            ++ip[nP];
-            acc = __dadd_rn(acc, raw(ip));
-            ++ip[nPP];
-            acc = __dadd_rn(acc, raw(ip));
-            --ip[nP];
-            acc = __dadd_rn(acc, raw(ip));
-            out[n] = __ddiv_rn(acc, 4.0);
-        }
-    } else {
-#pragma unroll
-        for (int n = 0; n < 3; ++n) {
-            unsigned ip[3] = {pos[0], pos[1], pos[2]};
-            auto raw = [&](const unsigned* p) -> double {
-                const double delta = d.el[eoff[n] + p[n]];
-                const float v = g.I[(unsigned long long)n * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2]];
-                return delta != 0.0 ? __ddiv_rn((double)v, delta) : 0.0;
-            };
-            const double delta = d.el[eoff[n] + ip[n]];
-            double o = raw(ip);
-            if (pos[n] >= N[n] - 1) { out[n] = 0.0; continue; }
-            ++ip[n];
-            const double deltaUp = d.el[eoff[n] + ip[n]];
-            const double deltaRel = __ddiv_rn(delta, __dadd_rn(delta, deltaUp));
-            out[n] = __dadd_rn(__dmul_rn(o, __dsub_rn(1.0, deltaRel)), __dmul_rn(raw(ip), deltaRel));
+    for (int n = 0; n < 3; ++n) {
+        const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+        unsigned ip[3] = {pos[0], pos[1], pos[2]};
+        if (d.interp == 0) { out[n] = raw(n, ip); continue; }
+        if (d.field == 0) {
+            if (d.interp == 1) {
+                if (pos[n] == N[n] - 1) { --ip[n]; out[n] = raw(n, ip); continue; }   // the lower value
+                const double delta = d.el[eoff[n] + ip[n]];
+                out[n] = raw(n, ip);
+                if (delta == 0.0) { out[n] = 0.0; continue; }
+                if (pos[n] == 0) continue;                                              // the upper value
+                --ip[n];
+                const double deltaDown = d.el[eoff[n] + ip[n]];
+                const double deltaRel = __ddiv_rn(delta, __dadd_rn(delta, deltaDown));
+                out[n] = __dadd_rn(__dmul_rn(out[n], __dsub_rn(1.0, deltaRel)), __dmul_rn(raw(n, ip), deltaRel));
+            } else {
+                if (edge) { out[n] = 0.0; continue; }
+                double acc = raw(n, ip);
+                ++ip[nP];
+                acc = __dadd_rn(acc, raw(n, ip));
+                ++ip[nPP];
+                acc = __dadd_rn(acc, raw(n, ip));
+                --ip[nP];
+                acc = __dadd_rn(acc, raw(n, ip));
+                out[n] = __ddiv_rn(acc, 4.0);
+            }
+        } else {
+            if (d.interp == 1) {
+                if (edge || pos[nP] == 0 || pos[nPP] == 0) { out[n] = 0.0; continue; }
+                double acc = raw(n, ip);
+                --ip[nP];
+                acc = __dadd_rn(acc, raw(n, ip));
+                --ip[nPP];
+                acc = __dadd_rn(acc, raw(n, ip));
+                ++ip[nP];
+                acc = __dadd_rn(acc, raw(n, ip));
+                out[n] = __ddiv_rn(acc, 4.0);
+            } else {
+                const double delta = d.el[eoff[n] + ip[n]];
+                const double o = raw(n, ip);
+                if (pos[n] >= N[n] - 1) { out[n] = 0.0; continue; }
+                ++ip[n];
+                const double deltaUp = d.el[eoff[n] + ip[n]];
+                const double deltaRel = __ddiv_rn(delta, __dadd_rn(delta, deltaUp));
+                out[n] = __dadd_rn(__dmul_rn(o, __dsub_rn(1.0, deltaRel)), __dmul_rn(raw(n, ip), deltaRel));
+            }
         }
     }
 }
@@ -865,7 +891,19 @@ static __global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s
         if (s.ndump > 0) {
             const DumpDev& d = s.dumps[k];
             const unsigned q = (blockIdx.x - s.dump_block0[k]) * blockDim.x + threadIdx.x;
-            if (q < d.npos && d.fd_interval && (ts % d.fd_interval) == 0) {
+            if (d.td) {
+                if (q < d.npos && ts >= d.td_start && ts <= d.td_stop && (ts % d.td_interval) == 0) {
+                    const unsigned a = q / (d.sz[1] * d.sz[2]);
+                    const unsigned rem = q - a * d.sz[1] * d.sz[2];
+                    const unsigned b = rem / d.sz[2], c = rem - b * d.sz[2];
+                    const unsigned pos[3] = {d.start[0] + a, d.start[1] + b, d.start[2] + c};
+                    double out[3];
+                    dump_field(g, d, pos, out);
+                    float* slot = d.ring + (unsigned long long)((ts / d.td_interval) % d.nslot) * 3 * d.npos;
+#pragma unroll
+                    for (int n = 0; n < 3; ++n) slot[(unsigned long long)n * d.npos + q] = (float)out[n];
+                }
+            } else if (q < d.npos && d.fd_interval && (ts % d.fd_interval) == 0) {
                 const unsigned smp = ts / d.fd_interval;
                 if (smp < d.nsamp) {
                     const unsigned a = q / (d.sz[1] * d.sz[2]);
@@ -873,7 +911,7 @@ static __global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s
                     const unsigned b = rem / d.sz[2], c = rem - b * d.sz[2];
                     const unsigned pos[3] = {d.start[0] + a, d.start[1] + b, d.start[2] + c};
                     double out[3];
-                    cell_field(g, d, pos, out);
+                    dump_field(g, d, pos, out);
                     for (unsigned f = 0; f < d.nf; ++f) {
                         const float2 e = d.phasor[(unsigned long long)smp * d.nf + f];
 #pragma unroll

@@ -9,6 +9,7 @@ graph.  ``IterateTS``, ``GetVolt``/``GetCurr``/``SetVolt``/``SetCurr`` and
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Optional
 
 import numpy as np
@@ -30,7 +31,8 @@ class EngineError(RuntimeError):
 class EngineBase:
     """Drives any library that exports the engine ABI (``lib`` from ``_native``)."""
 
-    def __init__(self, lib: _native.Lib, handle, op: OperatorData, max_timesteps: int, max_classes: int = 0):
+    def __init__(self, lib: _native.Lib, handle, op: OperatorData, max_timesteps: int, max_classes: int = 0,
+                 dump_path: Optional[str] = None):
         self.lib = lib
         self.h = handle
         self.op = op
@@ -38,6 +40,10 @@ class EngineBase:
         self.max_ts = int(max_timesteps)
         self._keep = []
         self.vprobe_ids, self.iprobe_ids, self.dump_ids = [], [], []
+        self.td_dump_ids = []
+        # time-domain dump files go to <dump_path>/<dump name>_<numTS>.vtr, as the reference
+        # writes them into the simulation path
+        self.dump_path = dump_path if dump_path is not None else os.getcwd()
         self._setup(max_classes)
 
     # --- error handling -------------------------------------------------------------------
@@ -134,9 +140,10 @@ class EngineBase:
                      "add_current_probe")
             self._probe_dft(pid.value, p)
             self.iprobe_ids.append(pid.value)
-        if op.dumps:
+        td = list(getattr(op, "td_dumps", []) or [])
+        if op.dumps or td:
             g = op.grid
-            from .operator import _main_delta, _dual_delta
+            from .operator import _main_delta, _dual_delta, _dual_line
             el = self._a(np.concatenate([_main_delta(l) * g.unit for l in g.lines]), np.float64)
             dl = self._a(np.concatenate([_dual_delta(l) * g.unit for l in g.lines]), np.float64)
             for d in op.dumps:
@@ -144,10 +151,25 @@ class EngineBase:
                 s = self._a(d.start, np.uint32)
                 e = self._a(d.stop, np.uint32)
                 fr = self._a(d.freqs, np.float64)
-                self._ck(L.add_fd_dump(self.h, int(d.field), _p(s, C.c_uint), _p(e, C.c_uint), int(d.fd_interval),
+                self._ck(L.add_fd_dump(self.h, int(d.field), int(getattr(d, "interp", 2)), _p(s, C.c_uint),
+                                       _p(e, C.c_uint), int(d.fd_interval),
                                        fr.size, _p(fr, C.c_double), _p(el, C.c_double), _p(dl, C.c_double),
                                        C.byref(did)), "add_fd_dump")
                 self.dump_ids.append(did.value)
+            for d in td:
+                did = C.c_int(-1)
+                s = self._a(d.start, np.uint32)
+                e = self._a(d.stop, np.uint32)
+                lines = [(_dual_line(np.asarray(l, np.float64)) if d.dual else np.asarray(l, np.float64)) * g.unit
+                         for l in g.lines]
+                xyz = self._a(np.concatenate([lines[a][int(d.start[a]):int(d.stop[a]) + 1] for a in range(3)]),
+                              np.float64)
+                prefix = os.path.join(self.dump_path, d.name).encode()
+                self._ck(L.add_td_dump(self.h, int(d.field), int(d.interp), _p(s, C.c_uint), _p(e, C.c_uint),
+                                       int(d.interval), int(d.start_ts), int(min(d.stop_ts, 0xFFFFFFFF)),
+                                       _p(el, C.c_double), _p(dl, C.c_double), _p(xyz, C.c_double), prefix,
+                                       C.byref(did)), "add_td_dump")
+                self.td_dump_ids.append(did.value)
         self._ck(L.init(self.h, self.max_ts), "init")
         self._keep.clear()
 
@@ -239,7 +261,8 @@ class EngineBase:
 class Engine_CUDA(EngineBase):
     """The GB300 engine (``--engine=cuda``): the only product engine, no CPU fallback."""
 
-    def __init__(self, op: OperatorData, max_timesteps: int, device: int = 0, max_classes: int = 0):
+    def __init__(self, op: OperatorData, max_timesteps: int, device: int = 0, max_classes: int = 0,
+                 dump_path: Optional[str] = None):
         lib = _native.load_cuda()
         h = C.c_void_p()
         nl = np.ascontiguousarray(op.num_lines, np.uint32)
@@ -247,7 +270,11 @@ class Engine_CUDA(EngineBase):
         if rc != 0:
             msg = lib.last_error(h) if h.value else b""
             raise EngineError(f"oems_cuda_create failed: {_native.ERRORS.get(rc, rc)} {msg!r}")
-        super().__init__(lib, h, op, max_timesteps, max_classes)
+        super().__init__(lib, h, op, max_timesteps, max_classes, dump_path)
+
+    def flush_dumps(self):
+        """Wait until every time-domain dump file of the steps issued so far is written."""
+        self._ck(self.lib.flush_dumps(self.h), "flush_dumps")
 
     def launches_per_step(self) -> int:
         n = C.c_uint()

@@ -29,18 +29,22 @@ class NF2FFResult:
 
 def box_faces(engine) -> List[Tuple[int, int, List[np.ndarray]]]:
     """(E dump id, H dump id, sample coordinates in metres) of every planar face recorded by an
-    E FD dump with a matching H FD dump (same box).  Coordinates are the dual mesh lines of the
-    dump's cells (cell interpolation, Common/processfields.cpp:164-172, 229-243)."""
+    E FD dump with a matching H FD dump (same box and mesh).  Coordinates are the mesh lines the
+    dump was snapped to: the main lines for node interpolation, the dual lines for cell
+    interpolation (Common/processfields.cpp:200-208, 229-243)."""
     op = engine.op
     g = op.grid
+    main = [np.asarray(l, np.float64) * g.unit for l in g.lines]
     dual = [_dual_line(np.asarray(l, np.float64)) * g.unit for l in g.lines]
     faces = []
     for ie, de in zip(engine.dump_ids, op.dumps):
         if de.field != 0:
             continue
         for ih, dh in zip(engine.dump_ids, op.dumps):
-            if dh.field == 1 and np.array_equal(de.start, dh.start) and np.array_equal(de.stop, dh.stop):
-                coords = [dual[a][int(de.start[a]):int(de.stop[a]) + 1] for a in range(3)]
+            if (dh.field == 1 and np.array_equal(de.start, dh.start) and np.array_equal(de.stop, dh.stop)
+                    and de.dual == dh.dual):
+                lines = dual if de.dual else main
+                coords = [lines[a][int(de.start[a]):int(de.stop[a]) + 1] for a in range(3)]
                 faces.append((ie, ih, coords))
                 break
     return faces

@@ -150,9 +150,13 @@ class Structure:
                          frequency=list(frequency), start_time=float(start_time), stop_time=float(stop_time),
                          interval=int(interval))
 
-    def AddDump(self, name, dump_type=0, dump_mode=1, frequency=()):
-        """FD field dump box: dump_type 10 = E-field FD, 11 = H-field FD (Common/processfields.h)."""
-        return self._add(DUMP, name, dump_type=int(dump_type), dump_mode=int(dump_mode), frequency=list(frequency))
+    def AddDump(self, name, dump_type=0, dump_mode=1, frequency=(), start_time=0.0, stop_time=0.0):
+        """Field dump box: dump_type 0/1 = E/H time domain, 10/11 = E/H frequency domain;
+        dump_mode 0 = no interpolation, 1 = node interpolation, 2 = cell interpolation
+        (Common/processfields.h, Common/engine_interface_base.h:33); start/stop time in seconds
+        limit a time-domain dump (Processing::SetProcessStartStopTime)."""
+        return self._add(DUMP, name, dump_type=int(dump_type), dump_mode=int(dump_mode), frequency=list(frequency),
+                         start_time=float(start_time), stop_time=float(stop_time))
 
 
 @dataclass
@@ -305,13 +309,32 @@ class CurrentProbe:
 
 @dataclass
 class FieldDumpFD:
-    """FD dump box (Common/processfields_fd.cpp): E (field=0) or H (field=1), cell interpolation."""
+    """FD dump box (Common/processfields_fd.cpp): E (field=0) or H (field=1); interp = the dump
+    mode (0 none, 1 node, 2 cell interpolation); dual = the box was snapped to the dual mesh."""
     name: str
     field: int
     start: np.ndarray
     stop: np.ndarray
     freqs: list
     fd_interval: int
+    interp: int = 2
+    dual: bool = True
+
+
+@dataclass
+class FieldDumpTD:
+    """Time-domain dump box (Common/processfields_td.cpp): E (field=0) or H (field=1) every
+    ``interval`` steps within [start_ts, stop_ts]; interp/dual as for FieldDumpFD.  ``name`` is the
+    file name stem (the property name, with _<box number> when the property has several boxes)."""
+    name: str
+    field: int
+    start: np.ndarray
+    stop: np.ndarray
+    interval: int
+    interp: int
+    dual: bool
+    start_ts: int = 0
+    stop_ts: int = 0xFFFFFFFF
 
 
 @dataclass
@@ -334,11 +357,28 @@ class OperatorData:
     grid: Optional[Grid] = None
     tfsf: Optional[TFSFTable] = None
     rlc: Optional[LumpedRLCTable] = None
+    td_dumps: list = field(default_factory=list)
 
 
 # lumped element types (CSPropLumpedElement::LEtype)
 LE_INVALID, LE_PARALLEL, LE_SERIES = -1, 0, 1
 LUMPED_RLC_Z_FACT = 20.0      # FDTD/extensions/operator_ext_lumpedRLC.h:30
+
+
+def _dump_mesh(field, dump_mode):
+    """Interpolation type and snapping mesh of a dump box (openems.cpp:629-665,
+    Common/processfields.cpp:200-208): H dumps default to the dual mesh, cell interpolation
+    selects the dual mesh and node interpolation the main mesh; no interpolation keeps the
+    default."""
+    interp = int(dump_mode)
+    if interp not in (0, 1, 2):
+        raise ValueError(f"dump mode {dump_mode} is not 0, 1 or 2")
+    dual = field == 1
+    if interp == 2:
+        dual = True
+    elif interp == 1:
+        dual = False
+    return interp, dual
 
 
 def _is_par_rc(prop):
@@ -919,7 +959,7 @@ class Operator:
         data = OperatorData(num_lines=self.N.astype(np.uint32), dt=dT, vv=self.vv, vi=self.vi, ii=self.ii,
                             iv=self.iv, exc=exc, upml=upml, mur=mur, lorentz=lorentz, vprobes=vprobes,
                             iprobes=iprobes, dumps=dumps, nyquist=self.exc.GetNyquistNum(),
-                            excitation=self.exc, grid=self.grid, tfsf=tfsf, rlc=rlc)
+                            excitation=self.exc, grid=self.grid, tfsf=tfsf, rlc=rlc, td_dumps=self.td_dumps)
         return data
 
     # ---- boundary conditions ---------------------------------------------------------------
@@ -1771,6 +1811,7 @@ class Operator:
     # ---- processing (probes, FD dumps) ---------------------------------------------------------
     def _build_processing(self):
         vprobes, iprobes, dumps = [], [], []
+        td_dumps = self.td_dumps = []
         nyq = self.exc.GetNyquistNum()
         for prop in self.csx.props:
             if prop.kind == PROBE:
@@ -1825,6 +1866,26 @@ class Operator:
                             continue
                         iprobes.append(CurrentProbe(prop.name, s, e, nd, si, ei, prop.params["weight"], interval,
                                                     fd_interval, freqs, start_ts, stop_ts))
+            elif prop.kind == DUMP and prop.params["dump_type"] in (0, 1):
+                # ProcessFieldsTD (openems.cpp:611-690): interval Nyquist/OverSampling
+                field_ = prop.params["dump_type"]
+                interp, dual = _dump_mesh(field_, prop.params["dump_mode"])
+                interval = max(1, nyq // self.over_sampling)
+                start_ts, stop_ts = 0, 0xFFFFFFFF
+                st, sp = prop.params.get("start_time", 0.0), prop.params.get("stop_time", 0.0)
+                if st > 0:
+                    start_ts = int(math.floor(st / self.dT))
+                if sp > 0:
+                    stop_ts = int(math.ceil(sp / self.dT))
+                if stop_ts <= start_ts:
+                    start_ts, stop_ts = 0, 0xFFFFFFFF
+                multi = len(prop.boxes) > 1
+                for nb, (lo, hi, *_r) in enumerate(prop.boxes):
+                    dim, s, e, _, _ = self.snap_box(lo, hi, dual=dual, method=0)
+                    if dim < 0:
+                        continue
+                    name = f"{prop.name}_{nb}" if multi else prop.name
+                    td_dumps.append(FieldDumpTD(name, field_, s, e, interval, interp, dual, start_ts, stop_ts))
             elif prop.kind == DUMP:
                 dt_ = prop.params["dump_type"]
                 if dt_ not in (10, 11):
@@ -1840,12 +1901,13 @@ class Operator:
                     if fd_interval > nts:
                         fd_interval = nts
                     freqs.append(float(f))
+                field_ = dt_ - 10
+                interp, dual = _dump_mesh(field_, prop.params["dump_mode"])
                 for lo, hi, _pr, _sq, _p, *_ in prop.boxes:
-                    # cell interpolation snaps to the dual mesh (Common/processfields.cpp:164-172)
-                    dim, s, e, _, _ = self.snap_box(lo, hi, dual=prop.params["dump_mode"] == 1, method=0)
+                    dim, s, e, _, _ = self.snap_box(lo, hi, dual=dual, method=0)
                     if dim < 0:
                         continue
-                    dumps.append(FieldDumpFD(prop.name, dt_ - 10, s, e, freqs, fd_interval))
+                    dumps.append(FieldDumpFD(prop.name, field_, s, e, freqs, fd_interval, interp, dual))
         return vprobes, iprobes, dumps
 
 

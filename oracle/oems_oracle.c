@@ -88,6 +88,12 @@ typedef struct {
 
 typedef struct {
     int field;
+    int interp; /* 0 none, 1 node, 2 cell interpolation */
+    /* time-domain dump: samples kept in memory, float [nsamp][3][sx][sy][sz] */
+    int td;
+    unsigned td_interval, td_start, td_stop, nsamp, cap;
+    unsigned *samp_ts;
+    float *samples;
     unsigned start[3], stop[3], sz[3];
     unsigned fd_interval, nf;
     double *freqs;
@@ -273,7 +279,7 @@ void oems_ref_destroy(eng_t *e)
     }
     for (int d = 0; d < e->ndumps; ++d) {
         dump_t *q = &e->dumps[d];
-        free(q->freqs); free(q->acc);
+        free(q->freqs); free(q->acc); free(q->samp_ts); free(q->samples);
         for (int n = 0; n < 3; ++n) { free(q->el[n]); free(q->del[n]); }
     }
     free(e);
@@ -632,14 +638,16 @@ int oems_ref_set_probe_dft(eng_t *e, int id, unsigned fd_interval, unsigned nf, 
     return OK;
 }
 
-int oems_ref_add_fd_dump(eng_t *e, int field, const unsigned start[3], const unsigned stop[3], unsigned fd_interval,
-                         unsigned nf, const double *freqs, const double *el, const double *del, int *id)
+int oems_ref_add_fd_dump(eng_t *e, int field, int interp, const unsigned start[3], const unsigned stop[3],
+                         unsigned fd_interval, unsigned nf, const double *freqs, const double *el, const double *del,
+                         int *id)
 {
-    if (!e || e->ndumps >= MAX_DUMPS || (field != 0 && field != 1) || !id || !el || !del)
+    if (!e || e->ndumps >= MAX_DUMPS || (field != 0 && field != 1) || !id || !el || !del || interp < 0 || interp > 2)
         return ERR_ARG;
     dump_t *d = &e->dumps[e->ndumps];
     memset(d, 0, sizeof(*d));
     d->field = field;
+    d->interp = interp;
     size_t off = 0;
     for (int a = 0; a < 3; ++a) {
         if (start[a] > stop[a] || stop[a] >= e->N[a])
@@ -659,6 +667,46 @@ int oems_ref_add_fd_dump(eng_t *e, int field, const unsigned start[3], const uns
     if (nf) memcpy(d->freqs, freqs, 8 * (size_t)nf);
     d->acc = (float *)xcalloc((size_t)nf * 3 * d->sz[0] * d->sz[1] * d->sz[2] * 2, 4);
     *id = e->ndumps++;
+    return OK;
+}
+
+/* same arguments as oems_cuda_add_td_dump; the oracle keeps the samples in memory (coords and
+ * file_prefix are unused) and serves them through oems_ref_read_td_sample */
+int oems_ref_add_td_dump(eng_t *e, int field, int interp, const unsigned start[3], const unsigned stop[3],
+                         unsigned interval, unsigned start_ts, unsigned stop_ts, const double *el, const double *del,
+                         const double *coords, const char *file_prefix, int *id)
+{
+    (void)coords;
+    (void)file_prefix;
+    if (!interval)
+        return ERR_ARG;
+    int rc = oems_ref_add_fd_dump(e, field, interp, start, stop, 0, 0, NULL, el, del, id);
+    if (rc)
+        return rc;
+    dump_t *d = &e->dumps[*id];
+    d->td = 1;
+    d->td_interval = interval;
+    d->td_start = start_ts;
+    d->td_stop = stop_ts;
+    return OK;
+}
+
+/* number of samples through *count; sample k (if out != NULL) as float [3][sx][sy][sz] with its step */
+int oems_ref_read_td_sample(const eng_t *e, int id, unsigned k, float *out, unsigned *ts, unsigned *count)
+{
+    if (!e || id < 0 || id >= e->ndumps || !e->dumps[id].td)
+        return ERR_ARG;
+    const dump_t *d = &e->dumps[id];
+    if (count)
+        *count = d->nsamp;
+    if (!out)
+        return OK;
+    if (k >= d->nsamp)
+        return ERR_ARG;
+    size_t plane = (size_t)d->sz[0] * d->sz[1] * d->sz[2];
+    memcpy(out, d->samples + (size_t)k * 3 * plane, 12 * plane);
+    if (ts)
+        *ts = d->samp_ts[k];
     return OK;
 }
 
@@ -1171,52 +1219,129 @@ static void process_probes(eng_t *e)
 
 /* GetRawInterpolatedField / GetRawInterpolatedDualField, CELL_INTERPOLATE
  * (FDTD/engine_interface_fdtd.cpp:104-121, 182-199) */
-static void cell_field(eng_t *e, const dump_t *d, const unsigned pos[3], double out[3])
+/* Engine_Interface_FDTD::GetRawInterpolatedField (E, FDTD/engine_interface_fdtd.cpp:63-123) and
+ * GetRawInterpolatedDualField (H, :140-204) with the dump's interpolation type */
+static void dump_field(eng_t *e, const dump_t *d, const unsigned pos[3], double out[3])
 {
-    if (d->field == 0) {
-        for (int n = 0; n < 3; ++n) {
-            int nP = (n + 1) % 3, nPP = (n + 2) % 3;
-            if (pos[0] == e->N[0] - 1 || pos[1] == e->N[1] - 1 || pos[2] == e->N[2] - 1) {
-                out[n] = 0;
-                continue;
-            }
-            unsigned ip[3] = {pos[0], pos[1], pos[2]};
+    int edge = pos[0] == e->N[0] - 1 || pos[1] == e->N[1] - 1 || pos[2] == e->N[2] - 1;
+    for (int n = 0; n < 3; ++n) {
+        int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+        unsigned ip[3] = {pos[0], pos[1], pos[2]};
+        if (d->field == 0) {
 #define RAWE(p) (d->el[n][(p)[n]] ? (double)GETV(e, n, (p)[0], (p)[1], (p)[2]) / d->el[n][(p)[n]] : 0.0)
-            out[n] = RAWE(ip);
-            ++ip[nP];
-            out[n] += RAWE(ip);
-            ++ip[nPP];
-            out[n] += RAWE(ip);
-            --ip[nP];
-            out[n] += RAWE(ip);
-            out[n] /= 4;
-#undef RAWE
-        }
-    } else {
-        for (int n = 0; n < 3; ++n) {
-            unsigned ip[3] = {pos[0], pos[1], pos[2]};
-#define RAWH(p) (d->del[n][(p)[n]] ? (double)GETI(e, n, (p)[0], (p)[1], (p)[2]) / d->del[n][(p)[n]] : 0.0)
-            double delta = d->del[n][ip[n]];
-            out[n] = RAWH(ip);
-            if (pos[n] >= e->N[n] - 1) {
-                out[n] = 0;
-                continue;
+            if (d->interp == 0) {
+                out[n] = RAWE(ip);
+            } else if (d->interp == 1) {
+                if (pos[n] == e->N[n] - 1) {
+                    --ip[n];
+                    out[n] = RAWE(ip);
+                    continue;
+                }
+                double delta = d->el[n][ip[n]];
+                out[n] = RAWE(ip);
+                if (delta == 0) {
+                    out[n] = 0;
+                    continue;
+                }
+                if (pos[n] == 0)
+                    continue;
+                --ip[n];
+                double deltaDown = d->el[n][ip[n]];
+                double deltaRel = delta / (delta + deltaDown);
+                out[n] = out[n] * (1.0 - deltaRel) + (double)RAWE(ip) * deltaRel;
+            } else {
+                if (edge) {
+                    out[n] = 0;
+                    continue;
+                }
+                out[n] = RAWE(ip);
+                ++ip[nP];
+                out[n] += RAWE(ip);
+                ++ip[nPP];
+                out[n] += RAWE(ip);
+                --ip[nP];
+                out[n] += RAWE(ip);
+                out[n] /= 4;
             }
-            ++ip[n];
-            double deltaUp = d->del[n][ip[n]];
-            double deltaRel = delta / (delta + deltaUp);
-            out[n] = out[n] * (1.0 - deltaRel) + (double)RAWH(ip) * deltaRel;
+#undef RAWE
+        } else {
+#define RAWH(p) (d->del[n][(p)[n]] ? (double)GETI(e, n, (p)[0], (p)[1], (p)[2]) / d->del[n][(p)[n]] : 0.0)
+            if (d->interp == 0) {
+                out[n] = RAWH(ip);
+            } else if (d->interp == 1) {
+                if (edge || pos[nP] == 0 || pos[nPP] == 0) {
+                    out[n] = 0;
+                    continue;
+                }
+                out[n] = RAWH(ip);
+                --ip[nP];
+                out[n] += RAWH(ip);
+                --ip[nPP];
+                out[n] += RAWH(ip);
+                ++ip[nP];
+                out[n] += RAWH(ip);
+                out[n] /= 4;
+            } else {
+                double delta = d->del[n][ip[n]];
+                out[n] = RAWH(ip);
+                if (pos[n] >= e->N[n] - 1) {
+                    out[n] = 0;
+                    continue;
+                }
+                ++ip[n];
+                double deltaUp = d->del[n][ip[n]];
+                double deltaRel = delta / (delta + deltaUp);
+                out[n] = out[n] * (1.0 - deltaRel) + (double)RAWH(ip) * deltaRel;
+            }
 #undef RAWH
         }
     }
 }
 
 /* ProcessFieldsFD::Process (Common/processfields_fd.cpp:72-107) */
+/* ProcessFieldsTD::Process (Common/processfields_td.cpp:50-91): ProcessFields::CalcField of the box
+ * at a sample step, stored in float */
+static void process_td(eng_t *e, dump_t *d)
+{
+    unsigned ts = e->numTS;
+    if (ts < d->td_start || ts > d->td_stop || ts % d->td_interval)
+        return;
+    size_t plane = (size_t)d->sz[0] * d->sz[1] * d->sz[2];
+    if (d->nsamp == d->cap) {
+        d->cap = d->cap ? 2 * d->cap : 16;
+        d->samp_ts = (unsigned *)realloc(d->samp_ts, (size_t)d->cap * 4);
+        d->samples = (float *)realloc(d->samples, (size_t)d->cap * 3 * plane * 4);
+        if (!d->samp_ts || !d->samples) {
+            fprintf(stderr, "oracle: out of memory for time-domain samples\n");
+            abort();
+        }
+    }
+    float *out3 = d->samples + (size_t)d->nsamp * 3 * plane;
+    size_t c = 0;
+    unsigned pos[3];
+    for (unsigned i = 0; i < d->sz[0]; ++i)
+        for (unsigned j = 0; j < d->sz[1]; ++j)
+            for (unsigned l = 0; l < d->sz[2]; ++l, ++c) {
+                pos[0] = d->start[0] + i;
+                pos[1] = d->start[1] + j;
+                pos[2] = d->start[2] + l;
+                double out[3];
+                dump_field(e, d, pos, out);
+                for (int n = 0; n < 3; ++n)
+                    out3[(size_t)n * plane + c] = (float)out[n];
+            }
+    d->samp_ts[d->nsamp++] = ts;
+}
+
 static void process_dumps(eng_t *e)
 {
     unsigned ts = e->numTS;
     for (int k = 0; k < e->ndumps; ++k) {
         dump_t *d = &e->dumps[k];
+        if (d->td) {
+            process_td(e, d);
+            continue;
+        }
         if (!d->fd_interval || ts % d->fd_interval)
             continue;
         double T = ((double)ts + (double)(d->field == 1) * 0.5) * e->dt;
@@ -1238,7 +1363,7 @@ static void process_dumps(eng_t *e)
                         pos[1] = d->start[1] + j;
                         pos[2] = d->start[2] + l;
                         double out[3];
-                        cell_field(e, d, pos, out);
+                        dump_field(e, d, pos, out);
                         for (int n = 0; n < 3; ++n) {
                             float td = (float)out[n];
                             float *a = acc + ((size_t)n * plane + c) * 2;

@@ -30,11 +30,29 @@ def load():
         g.restype = C.c_int
         g.argtypes = [_native.PU, C.c_double, C.c_int, C.POINTER(C.c_void_p)]
         lib.fn["create_mt"] = g
+        r = cdll.oems_ref_read_td_sample
+        r.restype = C.c_int
+        r.argtypes = [C.c_void_p, C.c_int, C.c_uint, _native.PF, _native.PU, _native.PU]
+        lib.fn["read_td_sample"] = r
         _LIB = lib
     return _LIB
 
 
 class OracleEngine(EngineBase):
+    def td_samples(self, did):
+        """(steps, samples float [n][3][sx][sy][sz]) of time-domain dump `did`."""
+        cnt = C.c_uint()
+        self._ck(self.lib.read_td_sample(self.h, did, 0, None, None, C.byref(cnt)), "read_td_sample")
+        d = self.op.td_dumps[self.td_dump_ids.index(did)]
+        shape = (3,) + tuple(int(b) - int(a) + 1 for a, b in zip(d.start, d.stop))
+        out = np.zeros((cnt.value,) + shape, np.float32)
+        ts = np.zeros(cnt.value, np.int64)
+        for k in range(cnt.value):
+            t = C.c_uint()
+            self._ck(self.lib.read_td_sample(self.h, did, k, _p(out[k], C.c_float), C.byref(t), None), "read_td_sample")
+            ts[k] = t.value
+        return ts, out
+
     def __init__(self, op, max_timesteps, threads=0):
         lib = load()
         h = C.c_void_p()
