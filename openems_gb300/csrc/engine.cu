@@ -717,7 +717,10 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
             if (e->compressed) { if (mode) launch_v<true, true, 1>(gv, s, g, m, ts); else launch_v<true, true, 0>(gv, s, g, m, ts); }
             else { if (mode) launch_v<false, true, 1>(gv, s, g, m, ts); else launch_v<false, true, 0>(gv, s, g, m, ts); }
         } else if (e->compressed) {
-            if (o32) {
+            if (o32 && e->vec4 && mode == 0) {
+                const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
+                k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
+            } else if (o32) {
                 if (mode == 2) launch_v<true, false, 2, unsigned>(gv, s, g, m, ts);
                 else if (mode == 1) launch_v<true, false, 1, unsigned>(gv, s, g, m, ts);
                 else launch_v<true, false, 0, unsigned>(gv, s, g, m, ts);
@@ -734,7 +737,13 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
     } else {
         const dim3 gi((plane + 255) / 256, e->N[0] - 1);
         if (up) { if (e->compressed) k_update_i<true, true><<<gi, 256, 0, s>>>(g); else k_update_i<false, true><<<gi, 256, 0, s>>>(g); }
-        else if (e->compressed) { if (o32) k_update_i<true, false, unsigned><<<gi, 256, 0, s>>>(g); else k_update_i<true, false><<<gi, 256, 0, s>>>(g); }
+        else if (e->compressed) {
+            if (o32 && e->vec4) {
+                const dim3 gi4((plane / 4 + 255) / 256, e->N[0] - 1);
+                k_update_i4<unsigned><<<gi4, 256, 0, s>>>(g);
+            } else if (o32) k_update_i<true, false, unsigned><<<gi, 256, 0, s>>>(g);
+            else k_update_i<true, false><<<gi, 256, 0, s>>>(g);
+        }
         else k_update_i<false, false><<<gi, 256, 0, s>>>(g);
     }
 }
@@ -904,6 +913,12 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     g.V = e->dV; g.I = e->dI;
     g.idx = e->didx; g.tabV = e->dtabV; g.tabI = e->dtabI;
     g.vv = e->dvv; g.vi = e->dvi; g.ii = e->dii; g.iv = e->div;
+
+    // float4 update kernels (OEMS_CUDA_SCALAR=1 keeps the one-cell-per-thread form)
+    {
+        const char* sc = getenv("OEMS_CUDA_SCALAR");
+        e->vec4 = !(sc && sc[0] == '1');
+    }
 
     // UPML
     g.nupml = (int)e->upml.size();

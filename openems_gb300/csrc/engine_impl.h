@@ -156,6 +156,8 @@ struct oems_cuda_engine {
     // Mur pre/post hooks as separate launches (k_mur phases 0/1) instead of inside the voltage
     // update; set by OEMS_CUDA_MUR_SEPARATE=1 at init
     bool mur_separate = false;
+    // float4 forms of the update kernels (4 z cells per thread) where they exist
+    bool vec4 = true;
     // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
     // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
     // whenever the host sees it

@@ -427,6 +427,102 @@ __global__ void __launch_bounds__(256, (MUR == 2 ? 8 : 1)) k_update_v(GridDev g,
     else update_v_cell<COMPRESSED, UPML, false, 0, IX>(g, x, y, z);
 }
 
+// Vectorised current update of the compressed operator without UPML: one thread per four
+// consecutive z cells (a 16-byte aligned float4 of every component; Pz is a multiple of 4).
+// The +z neighbours are the same float4 shifted by one lane plus the next float; lanes at or past
+// z = Nz-1 keep their loaded value (the reference never updates that line, and the padding stays
+// zero).  Per cell the arithmetic is update_i_cell's.
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ float f4(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+__device__ __forceinline__ void set4(float4& v, int k, float a)
+{
+    if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
+}
+
+template <typename IX = unsigned>
+__global__ void __launch_bounds__(256) k_update_i4(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned pz4 = g.Pz >> 2;
+    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
+    if (y + 1 >= g.Ny || z0 + 1 >= g.Nz) return;
+    const IX S = (IX)g.S;
+    const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
+    const IX sx = (IX)g.Ny * g.Pz;
+    const IX sy = g.Pz;
+    const float* __restrict__ V = g.V;
+    float* __restrict__ I = g.I;
+    const float4 w0 = ldg4(V + o), w1 = ldg4(V + (S + o)), w2 = ldg4(V + (2 * S + o));
+    const float4 w2y = ldg4(V + (2 * S + o + sy)), w0y = ldg4(V + (o + sy));
+    const float4 w2x = ldg4(V + (2 * S + o + sx)), w1x = ldg4(V + (S + o + sx));
+    const float w0z4 = __ldg(V + (o + 4)), w1z4 = __ldg(V + (S + o + 4));
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    float4 a0 = ld4(I + o), a1 = ld4(I + (S + o)), a2 = ld4(I + (2 * S + o));
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (z0 + k + 1 >= g.Nz) break;
+        const float4 ca = __ldg(g.tabI + 2 * cls[k]), cb = __ldg(g.tabI + 2 * cls[k] + 1);
+        const float v1z = k < 3 ? f4(w1, k + 1) : w1z4, v0z = k < 3 ? f4(w0, k + 1) : w0z4;
+        const float c0 = fadd(fsub(fsub(f4(w2, k), f4(w2y, k)), f4(w1, k)), v1z);
+        const float c1 = fadd(fsub(fsub(f4(w0, k), v0z), f4(w2, k)), f4(w2x, k));
+        const float c2 = fadd(fsub(fsub(f4(w1, k), f4(w1x, k)), f4(w0, k)), f4(w0y, k));
+        set4(a0, k, fadd(fmul(f4(a0, k), ca.x), fmul(ca.w, c0)));
+        set4(a1, k, fadd(fmul(f4(a1, k), ca.y), fmul(cb.x, c1)));
+        set4(a2, k, fadd(fmul(f4(a2, k), ca.z), fmul(cb.y, c2)));
+    }
+    *reinterpret_cast<float4*>(I + o) = a0;
+    *reinterpret_cast<float4*>(I + (S + o)) = a1;
+    *reinterpret_cast<float4*>(I + (2 * S + o)) = a2;
+}
+
+// Vectorised voltage update of the compressed operator without UPML and without Mur walls, four
+// consecutive z cells per thread (see k_update_i4).  The -z neighbour of lane k is lane k-1, of
+// lane 0 the float before the vector (the cell itself at z = 0, the reference's "same cell"
+// read).  Lanes past z = Nz-1 are padding and keep their zero.  (With Mur walls the hooks make a
+// float4 form no faster than the one-cell form on GB300: the wall lanes of every row serialise
+// their warps, and a separate pass over the scattered row ends costs as much.)
+template <typename IX = unsigned>
+__global__ void __launch_bounds__(256) k_update_v4(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned pz4 = g.Pz >> 2;
+    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
+    if (y >= g.Ny || z0 >= g.Nz) return;
+    const IX S = (IX)g.S;
+    const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
+    const IX sx = x ? (IX)g.Ny * g.Pz : (IX)0;
+    const IX sy = y ? (IX)g.Pz : (IX)0;
+    const float* __restrict__ I = g.I;
+    float* __restrict__ V = g.V;
+    const float4 i0 = ldg4(I + o), i1 = ldg4(I + (S + o)), i2 = ldg4(I + (2 * S + o));
+    const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
+    const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
+    // the float before the vector; at z = 0 the cell's own value
+    const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (z0 + k >= g.Nz) break;
+        const float4 ca = __ldg(g.tabV + 2 * cls[k]), cb = __ldg(g.tabV + 2 * cls[k] + 1);
+        const float i1z = k ? f4(i1, k - 1) : i1m, i0z = k ? f4(i0, k - 1) : i0m;
+        const float c0 = fadd(fsub(fsub(f4(i2, k), f4(i2y, k)), f4(i1, k)), i1z);
+        const float c1 = fadd(fsub(fsub(f4(i0, k), i0z), f4(i2, k)), f4(i2x, k));
+        const float c2 = fadd(fsub(fsub(f4(i1, k), f4(i1x, k)), f4(i0, k)), f4(i0y, k));
+        set4(n0, k, fadd(fmul(f4(n0, k), ca.x), fmul(ca.w, c0)));
+        set4(n1, k, fadd(fmul(f4(n1, k), ca.y), fmul(cb.x, c1)));
+        set4(n2, k, fadd(fmul(f4(n2, k), ca.z), fmul(cb.y, c2)));
+    }
+    *reinterpret_cast<float4*>(V + o) = n0;
+    *reinterpret_cast<float4*>(V + (S + o)) = n1;
+    *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
+}
+
 template <bool COMPRESSED, bool UPML, typename IX = unsigned long long>
 __global__ void __launch_bounds__(256) k_update_i(GridDev g)
 {
