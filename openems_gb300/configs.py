@@ -351,6 +351,42 @@ def td_dumps(n=(16, 14, 12), steps=120, bc=(2, 2, 3, 3, 0, 0), seed=5):
     return op.build(steps)
 
 
+def conducting_sheet(n=(24, 20, 22), steps=400, bc=(2,) * 6, sigma=5.8e7, thickness=35e-6, pec=False, seed=9,
+                     dispersive=False):
+    """Conducting sheets (Operator_Ext_ConductingSheet): a z-normal sheet across most of the cross
+    section between a point source and a probe, a small x-normal sheet, a three-dimensional box of
+    the sheet material (PEC fallback) and a sheet reaching the boundary layer (PEC fallback there),
+    on a graded mesh.  pec=True puts a metal plate where the main sheet is (for comparisons)."""
+    rng = np.random.default_rng(seed)
+    lines = [np.cumsum(np.concatenate([[0.0], rng.uniform(0.8, 1.2, k - 1)])) for k in n]
+    g = Grid(lines, unit=1e-3)
+    gl = g.lines
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(5e9, 4e9)
+    c = [k // 2 for k in n]
+
+    def P(i, j, k):
+        return [gl[0][i], gl[1][j], gl[2][k]]
+    if pec:
+        csx.AddMetal("plate").AddBox(P(3, 3, c[2]), P(n[0] - 4, n[1] - 4, c[2]), priority=10)
+    else:
+        sheet = csx.AddConductingSheet("sheet", sigma, thickness)
+        sheet.AddBox(P(3, 3, c[2]), P(n[0] - 4, n[1] - 4, c[2]), priority=10)
+        sheet.AddBox(P(4, 4, 4), P(6, 7, 6), priority=10)                      # a volume: PEC fallback
+        csx.AddConductingSheet("small", 1e5, 2e-6).AddBox(P(c[0] + 4, 3, 4), P(c[0] + 4, 8, 8), priority=11)
+        csx.AddConductingSheet("edge", 3e6, 10e-6).AddBox(P(0, c[1], 2), P(5, c[1], 6), priority=11)
+    if dispersive:
+        csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[6e9], eps_relax_time=[1e-9]).AddBox(
+            P(3, 3, c[2] + 2), P(9, 9, c[2] + 5), priority=2)
+    csx.AddMaterial("diel", epsilon=2.5).AddBox(P(2, 2, c[2] - 4), P(n[0] - 3, n[1] - 3, c[2] - 1))
+    csx.AddExcitation("src", 0, [1.0, 0, 0]).AddBox(P(c[0], c[1], c[2] - 3), P(c[0] + 1, c[1], c[2] - 3))
+    csx.AddProbe("u_below", 0, interval=1).AddBox(P(c[0], c[1], c[2] - 2), P(c[0] + 1, c[1], c[2] - 2))
+    csx.AddProbe("u_above", 0, interval=1).AddBox(P(c[0], c[1], c[2] + 3), P(c[0] + 1, c[1], c[2] + 3))
+    op = Operator(csx, g, exc, bc=bc, pml_size=(4,) * 6)
+    return op.build(steps)
+
+
 def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
     """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""
     nx, ny, nz = shape

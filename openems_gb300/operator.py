@@ -48,8 +48,9 @@ C0 = 299792458.0            # tools/constants.h:25
 Z0 = 376.730313461          # tools/constants.h:26
 PI = 3.141592653589793238462643383279
 
-# property kinds (bit flags, like CSProperties::PropertyType)
-MATERIAL, METAL, EXCITATION, LUMPED, PROBE, DUMP = 1, 2, 4, 8, 16, 32
+# property kinds (bit flags, like CSProperties::PropertyType); a conducting sheet is a metal
+# property of its own type (METAL | CONDSHEET), so the PEC pass does not take it for metal
+MATERIAL, METAL, EXCITATION, LUMPED, PROBE, DUMP, CONDSHEET = 1, 2, 4, 8, 16, 32, 64
 
 
 # =========================================================================================
@@ -129,6 +130,11 @@ class Structure:
 
     def AddMetal(self, name):
         return self._add(METAL, name)
+
+    def AddConductingSheet(self, name, conductivity, thickness):
+        """Thin conducting sheet (CSPropConductingSheet): conductivity in S/m, thickness in metres,
+        on two-dimensional boxes; modelled by Operator_Ext_ConductingSheet."""
+        return self._add(METAL | CONDSHEET, name, conductivity=float(conductivity), thickness=float(thickness))
 
     def AddLumpedElement(self, name, ny, R=float('nan'), C=float('nan'), caps=True, L=float('nan'), LEtype=0):
         """Lumped element (CSPropLumpedElement): LEtype 0 = parallel, 1 = series, -1 = invalid.
@@ -953,6 +959,9 @@ class Operator:
         mur = self._build_mur(exc)
         upml = self._build_upml()
         lorentz = self._build_lorentz()
+        # Operator_Ext_ConductingSheet follows Operator_Ext_LorentzMaterial (openems.cpp:1236-1239)
+        # and hands its tables to the same engine extension
+        lorentz = lorentz + self._build_conducting_sheet()
         # Operator_Ext_LumpedRLC is added after the dispersive extensions (openems.cpp:1236-1241)
         rlc = self._build_lumped_rlc()
         vprobes, iprobes, dumps = self._build_processing()
@@ -1705,6 +1714,124 @@ class Operator:
         with np.errstate(over="ignore", invalid="ignore"):
             arr = {k: np.array(v, np.float64).astype(ft) for k, v in cols.items()}
         return LumpedRLCTable(np.array(P, np.uint32).T.copy(), np.array(D, np.int32), **arr)
+
+    def _build_conducting_sheet(self):
+        """Operator_Ext_ConductingSheet::BuildExtension (operator_ext_conductingsheet.cpp:42-263):
+        two voltage ADE orders on the edges of two-dimensional conducting-sheet boxes, with the
+        sheet's EC_G/EC_C rewritten from the fitted model (condsheet_table).  Edges of sheets that
+        are not two-dimensional, lie in a boundary layer or have no conductance fall back to PEC."""
+        from . import condsheet_table as T
+        if not any(p.kind & CONDSHEET for p in self.csx.props):
+            return []
+        ft = self.ft
+        N = [int(v) for v in self.N]
+        dT = self.dT
+        u = self.unit
+        # GetBCSize: 0 for PEC/PMC, 1 for Mur, the PML size for UPML (openems.cpp:388-403)
+        bcs = [0 if b in (0, 1) else (1 if b == 2 else int(self.pml_size[w])) for w, b in enumerate(self.bc)]
+        recs = self._matmetal.recs
+        tan = np.full((3,) + tuple(N), -1, np.int64)
+        cond = np.zeros((3,) + tuple(N), ft)
+        thick = np.zeros((3,) + tuple(N), ft)
+        on = np.zeros(tuple(N), bool)
+        ax = [np.arange(k) for k in N]
+        disable = np.zeros(tuple(N), bool)
+        for m in range(3):
+            bad = (ax[m] <= bcs[2 * m]) | (ax[m] >= N[m] - bcs[2 * m + 1] - 1)
+            sh = [1, 1, 1]
+            sh[m] = N[m]
+            disable |= bad.reshape(sh)
+        for n in range(3):
+            nP, nPP = (n + 1) % 3, (n + 2) % 3
+            cs = [self.L[0], self.L[1], self.L[2]]
+            cs[n] = self.dl[n]
+            # the winning record at every Yee point (GetPropertyByCoordPriority with its primitive)
+            win = np.full(tuple(N), -1, np.int64)
+            for ri, (lo, hi, *_r) in enumerate(recs):
+                rx = np.nonzero((cs[0] >= lo[0]) & (cs[0] <= hi[0]))[0]
+                ry = np.nonzero((cs[1] >= lo[1]) & (cs[1] <= hi[1]))[0]
+                rz = np.nonzero((cs[2] >= lo[2]) & (cs[2] <= hi[2]))[0]
+                if rx.size and ry.size and rz.size:
+                    win[np.ix_(rx, ry, rz)] = ri
+            valid = np.ones(tuple(N), bool)
+            sl = [slice(None)] * 3
+            sl[n] = slice(N[n] - 1, None)
+            valid[tuple(sl)] = False          # GetYeeCoords is false for pos[n] >= N-1
+            for x, y, z in zip(*np.nonzero((win >= 0) & valid)):
+                lo, hi, _pr, _sq, prop = recs[win[x, y, z]][:5]
+                if not (prop.kind & CONDSHEET):
+                    continue
+                dim = int(sum(lo[k] != hi[k] for k in range(3)))
+                if dim != 2 or disable[x, y, z] or not (ft(prop.params["conductivity"]) > 0) or \
+                        not (ft(prop.params["thickness"]) > 0):
+                    self.vv[n, x, y, z] = 0      # fallback to PEC
+                    self.vi[n, x, y, z] = 0
+                    continue
+                cond[n, x, y, z] = prop.params["conductivity"]
+                thick[n, x, y, z] = prop.params["thickness"]
+                if lo[nP] != hi[nP]:
+                    tan[n, x, y, z] = nP
+                if lo[nPP] != hi[nPP]:
+                    tan[n, x, y, z] = nPP
+                on[x, y, z] = True
+        pos = np.array(np.nonzero(on), np.int64)       # x-major scan order
+        M = pos.shape[1]
+        if M == 0:
+            return []
+        vint = [np.zeros((3, M), ft), np.zeros((3, M), ft)]
+        vext = [np.zeros((3, M), ft), np.zeros((3, M), ft)]
+        w_stop = ft(self.exc.f_max * 2 * PI)
+        for i in range(M):
+            p = [int(pos[0, i]), int(pos[1, i]), int(pos[2, i])]
+            for n in range(3):
+                t_dir = int(tan[n, p[0], p[1], p[2]])
+                G0 = ft(cond[n, p[0], p[1], p[2]] * thick[n, p[0], p[1], p[2]])
+                tk = thick[n, p[0], p[1], p[2]]
+                with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+                    w0 = ft(np.float64(8.0) / np.float64(G0) / np.float64(tk) / MUE0)
+                    omega_max = ft(w_stop / w0)
+                k = 0
+                while k < len(T.OMEGA_STOP) and not (T.OMEGA_STOP[k] > float(omega_max)):
+                    k += 1
+                if k >= len(T.OMEGA_STOP):
+                    k = len(T.OMEGA_STOP) - 1
+                if t_dir < 0:
+                    continue
+                wtl = ft((self.md[n][p[n]] * u) / (self.dd[t_dir][p[t_dir]] * u))
+                factor = ft(1)
+                if tan[t_dir, p[0], p[1], p[2]] < 0:
+                    factor = ft(2)
+                q = list(p)
+                q[t_dir] -= 1
+                if tan[t_dir, q[0], q[1], q[2]] < 0:
+                    factor = ft(2)
+                L1 = ft(T.L1[k] / float(G0) / float(w0) * float(factor))
+                L2 = ft(T.L2[k] / float(G0) / float(w0) * float(factor))
+                R1 = ft(T.R1[k] / float(G0) * float(factor))
+                R2 = ft(T.R2[k] / float(G0) * float(factor))
+                G = ft(float(G0) * T.G[k] / float(factor))
+                L1 = ft(L1 * wtl)
+                L2 = ft(L2 * wtl)
+                R1 = ft(R1 * wtl)
+                R2 = ft(R2 * wtl)
+                G = ft(G / wtl)
+                Lmin = L2 if L2 < L1 else L1
+                x, y, z = p
+                self.EC_G[n, x, y, z] = G
+                self.EC_C[n, x, y, z] = ft(dT * dT / 4.0 * (16.0 / float(Lmin) + float(ft(1) / L1) + float(ft(1) / L2)))
+                a_, b_, c_, d_ = self._ec_op(self.EC_C[n, x, y, z], self.EC_G[n, x, y, z],
+                                             self.EC_L[n, x, y, z], self.EC_R[n, x, y, z], dT)
+                self.vv[n, x, y, z], self.vi[n, x, y, z] = a_, b_
+                self.ii[n, x, y, z], self.iv[n, x, y, z] = c_, d_
+                vi_ = float(self.vi[n, x, y, z])
+                for o, (Lk, Rk) in enumerate(((L1, R1), (L2, R2))):
+                    Lf, Rf = float(Lk), float(Rk)
+                    vint[o][n, i] = ft((2.0 * Lf - dT * Rf) / (2.0 * Lf + dT * Rf))
+                    vext[o][n, i] = ft(dT / (Lf + dT * Rf / 2.0) * vi_)
+        pos32 = pos.astype(np.uint32)
+        z = np.zeros((3, M), ft)
+        return [LorentzOrder(pos32.copy(), True, False, False, False, vint[o], vext[o], z.copy(), z.copy(), z.copy(),
+                             z.copy()) for o in range(2)]
 
     def _build_lorentz(self):
         """Operator_Ext_LorentzMaterial::BuildExtension, evaluated in parallel x-slabs; positions

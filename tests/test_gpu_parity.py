@@ -55,6 +55,9 @@ CASES = [
                                                    steps=200), 200),
     ("lumped_rlc_mur", lambda: configs.lumped_rlc(steps=300), 300),
     ("lumped_rlc_upml_dispersive", lambda: configs.lumped_rlc(bc=(3,) * 6, dispersive=True, steps=240), 240),
+    ("conducting_sheet_mur", lambda: configs.conducting_sheet(steps=240), 240),
+    ("conducting_sheet_upml_dispersive", lambda: configs.conducting_sheet(bc=(3,) * 6, dispersive=True, steps=200),
+     200),
 ]
 
 
