@@ -387,6 +387,32 @@ def conducting_sheet(n=(24, 20, 22), steps=400, bc=(2,) * 6, sigma=5.8e7, thickn
     return op.build(steps)
 
 
+def coax(steps=5000, length=1000.0, res=5.0):
+    """The reference's coax test (TESTSUITE/combinedtests/Coax.m:24-90): a PEC coaxial line of
+    inner radius 100 and outer radii 230/240 (drawing units, mm) on a 5 mm mesh, PEC on every wall
+    but a PML_8 at the far end, a radially weighted soft excitation at z = 0 and, half way down,
+    a voltage probe across the gap and a current probe around the inner conductor."""
+    r_i, r_ai, r_aa = 100.0, 230.0, 240.0
+    xs = np.arange(-2.5 * res - r_aa, r_aa + 2.5 * res + 1e-9, res)
+    nz = int(round(length / res)) + 1
+    zs = np.linspace(0.0, length, nz)
+    g = Grid([xs, xs.copy(), zs], unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(0.0, 1e9)
+    pec = csx.AddMetal("PEC")
+    pec.AddCylinder([0, 0, 0], [0, 0, length], r_i, priority=1)
+    pec.AddCylindricalShell([0, 0, 0], [0, 0, length], 0.5 * (r_aa + r_ai), r_aa - r_ai, priority=0)
+    weight = (lambda x, y, z: x / (x * x + y * y), lambda x, y, z: y / (x * x + y * y), lambda x, y, z: 0.0)
+    csx.AddExcitation("excite", 0, [1, 1, 0], weight=weight).AddCylindricalShell(
+        [0, 0, 0], [0, 0, res / 2], 0.5 * (r_i + r_ai), r_ai - r_i)
+    csx.AddProbe("ut1", 0, interval=1).AddBox([r_i, 0, length / 2], [r_ai, 0, length / 2])
+    mid = r_i + 3 * res
+    csx.AddProbe("it1", 1, interval=1).AddBox([-mid, -mid, length / 2], [mid, mid, length / 2])
+    op = Operator(csx, g, exc, bc=(0, 0, 0, 0, 0, 3), pml_size=(8,) * 6)
+    return op.build(steps)
+
+
 def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
     """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""
     nx, ny, nz = shape

@@ -68,6 +68,18 @@ class Property:
         self.structure._add_box(self, np.asarray(start, float), np.asarray(stop, float), priority)
         return self
 
+    def AddCylinder(self, start, stop, radius, priority=0):
+        """Solid cylinder (CSPrimCylinder) whose axis runs from start to stop along one mesh axis:
+        the points within `radius` of the axis, ends included."""
+        self.structure._add_cylinder(self, start, stop, float(radius), None, priority)
+        return self
+
+    def AddCylindricalShell(self, start, stop, radius, shell_width, priority=0):
+        """Cylindrical shell (CSPrimCylindricalShell) along one mesh axis: the points whose
+        distance to the axis is within shell_width/2 of `radius`."""
+        self.structure._add_cylinder(self, start, stop, float(radius), float(shell_width), priority)
+        return self
+
     # plane-wave excitation (exc_type 10) parameters, named like CSPropExcitation's setters
     def SetPropagationDir(self, val):
         self.params["prop_dir"] = np.asarray(val, float)
@@ -86,13 +98,34 @@ class Structure:
         self.boxes = []          # (start, stop, priority, seq, prop)
         self._seq = 0
 
-    def _add_box(self, prop, start, stop, priority):
+    def _add_box(self, prop, start, stop, priority, shape=None):
         lo = np.minimum(start, stop)
         hi = np.maximum(start, stop)
-        rec = (lo, hi, int(priority), self._seq, prop, start.copy(), stop.copy())
+        rec = (lo, hi, int(priority), self._seq, prop, start.copy(), stop.copy(), shape)
         self._seq += 1
         prop.boxes.append(rec)
         self.boxes.append(rec)
+
+    def _add_cylinder(self, prop, start, stop, radius, width, priority):
+        """A cylinder or shell along one axis; the record carries its bounding box and the shape
+        (axis, centre in the two other axes, radius, shell width or None)."""
+        start = np.asarray(start, float)
+        stop = np.asarray(stop, float)
+        d = np.nonzero(start != stop)[0]
+        if d.size != 1:
+            raise ValueError("cylinders must run along one mesh axis")
+        a = int(d[0])
+        b, c = (a + 1) % 3, (a + 2) % 3
+        r_out = radius + (0.5 * width if width is not None else 0.0)
+        lo = start.copy()
+        hi = stop.copy()
+        lo[a], hi[a] = min(start[a], stop[a]), max(start[a], stop[a])
+        for k in (b, c):
+            lo[k], hi[k] = start[k] - r_out, start[k] + r_out
+        shape = (a, float(start[b]), float(start[c]), radius, width)
+        self._add_box(prop, lo, hi, priority, shape)
+        prop.boxes[-1] = prop.boxes[-1][:5] + (start.copy(), stop.copy(), shape)
+        self.boxes[-1] = prop.boxes[-1]
 
     def _add(self, kind, name, **params):
         p = Property(self, kind, name, **params)
@@ -144,9 +177,11 @@ class Structure:
         return self._add(LUMPED, name, ny=int(ny), R=float(R), C=float(C), caps=bool(caps), L=float(L),
                          LEtype=int(LEtype))
 
-    def AddExcitation(self, name, exc_type, exc_val, delay=0.0):
+    def AddExcitation(self, name, exc_type, exc_val, delay=0.0, weight=None):
+        """Excitation property; `weight` = three functions f(x, y, z) of the drawing-unit
+        coordinates that scale the components (CSPropExcitation's weight functions)."""
         return self._add(EXCITATION, name, exc_type=int(exc_type),
-                         exc_val=np.asarray(exc_val, float), delay=float(delay))
+                         exc_val=np.asarray(exc_val, float), delay=float(delay), weight=weight)
 
     def AddProbe(self, name, p_type, weight=1.0, norm_dir=-1, frequency=(), start_time=0.0, stop_time=0.0,
                  interval=0):
@@ -465,16 +500,50 @@ class _Painter:
             return slice(int(m[0]), int(m[-1]) + 1)
         return m
 
+    @staticmethod
+    def rec_cells(rec, cx, cy, cz):
+        """Index arrays (ix, iy, iz) of the sample grid and a boolean mask over them (None = all)
+        of the points inside primitive `rec`; None when its bounding box holds no point."""
+        lo, hi = rec[0], rec[1]
+        cs = (cx, cy, cz)
+        idx = [np.nonzero((cs[k] >= lo[k]) & (cs[k] <= hi[k]))[0] for k in range(3)]
+        if any(i.size == 0 for i in idx):
+            return None
+        shape = rec[7] if len(rec) > 7 else None
+        if shape is None:
+            return idx, None
+        a, pb, pc, radius, width = shape
+        b, c = (a + 1) % 3, (a + 2) % 3
+        db = np.asarray(cs[b], np.float64)[idx[b]] - pb
+        dc = np.asarray(cs[c], np.float64)[idx[c]] - pc
+        dist = np.sqrt(db[:, None] ** 2 + dc[None, :] ** 2)       # [b][c]
+        inside = dist <= radius if width is None else np.abs(dist - radius) <= 0.5 * width
+        # broadcast [b][c] to the index order (x, y, z)
+        m = inside.T if b > c else inside
+        m = np.expand_dims(m, a)
+        m = np.broadcast_to(m, tuple(i.size for i in idx))
+        return idx, m
+
     def paint(self, cx, cy, cz):
         """Return int32 array [len(cx),len(cy),len(cz)] of property indices (-1 = background)."""
         out = np.full((len(cx), len(cy), len(cz)), -1, np.int32)
-        for lo, hi, _prio, _seq, prop, *_ in self.recs:
+        for rec in self.recs:
+            lo, hi, _prio, _seq, prop = rec[:5]
+            pid = self.prop_index[id(prop)]
+            if len(rec) > 7 and rec[7] is not None:
+                hit = self.rec_cells(rec, cx, cy, cz)
+                if hit is None:
+                    continue
+                (ax, ay, az), m = hit
+                sub = out[np.ix_(ax, ay, az)]
+                sub[m] = pid
+                out[np.ix_(ax, ay, az)] = sub
+                continue
             rx = self._range(cx, lo[0], hi[0])
             ry = self._range(cy, lo[1], hi[1])
             rz = self._range(cz, lo[2], hi[2])
             if rx is None or ry is None or rz is None:
                 continue
-            pid = self.prop_index[id(prop)]
             if isinstance(rx, slice) and isinstance(ry, slice) and isinstance(rz, slice):
                 out[rx, ry, rz] = pid
             else:
@@ -561,7 +630,11 @@ class Operator:
         self.grid = grid
         self.exc = excitation
         self.bc = [int(b) for b in bc]
-        self.pml_size = [int(s) if b == 3 else 0 for s, b in zip(pml_size, bc)]
+        # every wall keeps its configured PML size (openEMS defaults all six to 8,
+        # openems.cpp:129), PML or not: Operator_Ext_UPML grades an upper PML with the lower
+        # wall's size (operator_ext_upml.cpp:315, width/m_Size[2*n]), so a PML on the upper wall
+        # alone depends on the size of the wall below
+        self.pml_size = [int(s) for s in pml_size]
         self.forced_dt = float(timestep)
         self.ts_factor = float(timestep_factor)
         self.over_sampling = int(over_sampling)
@@ -762,6 +835,8 @@ class Operator:
         if np.dtype(self.ft) != np.float32:
             raise ValueError("Operator.build(device='cuda'): float32 operators only")
         recs = self._mat.recs
+        if any(len(r) > 7 and r[7] is not None for r in recs):
+            raise ValueError("Operator.build(device='cuda'): cylinder materials are built on the host")
         if any(r[4].params.get("voxel") for r in recs):
             raise ValueError("Operator.build(device='cuda'): voxel materials are built on the host")
         keys = ("epsilon", "kappa", "mue", "sigma")
@@ -1116,7 +1191,11 @@ class Operator:
                     et = prop.params["exc_type"]
                     if et not in (0, 1):
                         continue
-                    amp = prop.params["exc_val"][n] * (self.md[n][(x, y, z)[n]] * u)
+                    ex = prop.params["exc_val"][n]
+                    wf = prop.params.get("weight")
+                    if wf is not None:       # GetWeightedExcitation at the Yee point (drawing units)
+                        ex = ex * float(wf[n](float(cs[0][x]), float(cs[1][y]), float(cs[2][z])))
+                    amp = ex * (self.md[n][(x, y, z)[n]] * u)
                     if amp != 0:
                         vrec.append((z, y, x, n, amp, int(prop.params["delay"] / self.dT)))
                     if et == 1:
@@ -1501,7 +1580,7 @@ class Operator:
                 depth = width - (L[N - 1] - L[pos]) * u
                 if n == ny:
                     depth = depth + el / 2
-                dl = width / sz[2 * n] if sz[2 * n] else float("inf")
+                dl = width / sz[2 * n] if sz[2 * n] else float("inf")    # the lower wall's size, as the reference
                 with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
                     g = self._grading(depth, dl, width, Z0, float(sz[2 * n]))
                 kvn = np.where(up & (depth > 0), g, kvn)
@@ -1747,12 +1826,17 @@ class Operator:
             cs[n] = self.dl[n]
             # the winning record at every Yee point (GetPropertyByCoordPriority with its primitive)
             win = np.full(tuple(N), -1, np.int64)
-            for ri, (lo, hi, *_r) in enumerate(recs):
-                rx = np.nonzero((cs[0] >= lo[0]) & (cs[0] <= hi[0]))[0]
-                ry = np.nonzero((cs[1] >= lo[1]) & (cs[1] <= hi[1]))[0]
-                rz = np.nonzero((cs[2] >= lo[2]) & (cs[2] <= hi[2]))[0]
-                if rx.size and ry.size and rz.size:
+            for ri, rec in enumerate(recs):
+                hit = _Painter.rec_cells(rec, cs[0], cs[1], cs[2])
+                if hit is None:
+                    continue
+                (rx, ry, rz), msk = hit
+                if msk is None:
                     win[np.ix_(rx, ry, rz)] = ri
+                else:
+                    sub = win[np.ix_(rx, ry, rz)]
+                    sub[msk] = ri
+                    win[np.ix_(rx, ry, rz)] = sub
             valid = np.ones(tuple(N), bool)
             sl = [slice(None)] * 3
             sl[n] = slice(N[n] - 1, None)
@@ -1962,7 +2046,7 @@ class Operator:
                     start_ts = int(math.floor(prop.params["start_time"] / self.dT))
                 if prop.params["stop_time"] > 0:
                     stop_ts = int(math.ceil(prop.params["stop_time"] / self.dT))
-                for lo, hi, _pr, _sq, _p, b_start, b_stop in prop.boxes:
+                for lo, hi, _pr, _sq, _p, b_start, b_stop, *_ in prop.boxes:
                     if pt == 0:
                         s = np.array([self.snap_line(n, b_start[n], False)[0] for n in range(3)])
                         e = np.array([self.snap_line(n, b_stop[n], False)[0] for n in range(3)])

@@ -55,6 +55,7 @@ CASES = [
                                                    steps=200), 200),
     ("lumped_rlc_mur", lambda: configs.lumped_rlc(steps=300), 300),
     ("lumped_rlc_upml_dispersive", lambda: configs.lumped_rlc(bc=(3,) * 6, dispersive=True, steps=240), 240),
+    ("coax_cylinders", lambda: configs.coax(steps=150, length=200.0), 150),
     ("conducting_sheet_mur", lambda: configs.conducting_sheet(steps=240), 240),
     ("conducting_sheet_upml_dispersive", lambda: configs.conducting_sheet(bc=(3,) * 6, dispersive=True, steps=200),
      200),
@@ -181,6 +182,20 @@ def test_cavity_reference_contract_on_gpu(cuda_lib):
     r = OracleEngine(op, c["steps"])
     r.IterateTS(c["steps"])
     assert bits_equal(uy, r.probe_series(r.vprobe_ids[1]))
+
+
+def test_coax_reference_contract_on_gpu(cuda_lib):
+    """TESTSUITE/combinedtests/Coax.m on the CUDA engine: |U/I| within +3 % / -1 % of the
+    analytic Z0 from 0 to 1 GHz."""
+    from test_contracts_host import coax_impedance, coax_z0
+    op = configs.coax(steps=5000)
+    g = Engine_CUDA(op, 5000)
+    g.IterateTS(5000)
+    g.sync()
+    f, Z = coax_impedance(g, op)
+    Z0 = coax_z0()
+    assert f.size > 50
+    assert (Z <= Z0 * 1.03).all() and (Z >= Z0 * 0.99).all(), (Z.min() / Z0, Z.max() / Z0)
 
 
 def test_against_committed_fixtures(cuda_lib):
