@@ -163,6 +163,15 @@ int oems_cuda_add_current_probe(oems_cuda_engine* eng, const unsigned int start[
                                 double weight, unsigned int interval, unsigned int start_ts,
                                 unsigned int stop_ts, int* id);
 
+/* ProcessFieldProbe (Common/processfieldprobe.cpp:77-92), probe types 2/3 of openems.cpp:541-544:
+ * the E (field 0) or H (field 1) field at one Yee position without interpolation, i.e.
+ * GetRawField / GetRawDualField (FDTD/engine_interface_fdtd.cpp:263-268, 136-142) = value /
+ * el[n] (0 where el[n] == 0), el = GetEdgeLength(n, pos) of the main (E) or dual (H) mesh.
+ * Three values per sample (series [slot][3], DFT [nf][3][re,im]); H uses the dual time. */
+int oems_cuda_add_field_probe(oems_cuda_engine* eng, int field, const unsigned int pos[3], const double el[3],
+                              double weight, unsigned int interval, unsigned int start_ts,
+                              unsigned int stop_ts, int* id);
+
 /* ProcessIntegral FD part (Common/processintegral.cpp:156-167): complex<double> DFT at
  * num_freqs frequencies, accumulated every fd_interval steps. */
 int oems_cuda_set_probe_dft(oems_cuda_engine* eng, int probe_id, unsigned int fd_interval,

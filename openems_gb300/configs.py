@@ -413,6 +413,42 @@ def coax(steps=5000, length=1000.0, res=5.0):
     return op.build(steps)
 
 
+def fieldprobes(half=8, steps=600, freqs=(5e8,), interval=0):
+    """The reference's field probe test (TESTSUITE/probes/fieldprobes.m:36-116) at a smaller
+    extent: an infinitesimal dipole (hard Ez over lambda/50, lambda at 1 GHz, drawing unit 1 um)
+    on a uniform lambda/100 mesh of +-half dipole lengths, Mur on every wall, a Gaussian pulse
+    (f0 0, fc 1 GHz), OverSampling 10; six E and six H time-domain dumps without interpolation on
+    the faces of the cube +-2.25 dipole lengths, and E (type 2) and H (type 3) point probes at the
+    face centres (the given frequencies add a DFT to the probes; ``interval`` overrides the
+    probes' sampling interval)."""
+    c0 = 299792458.0
+    unit = 1e-6
+    dl = c0 / 1e9 / unit / 50
+    m = np.arange(-2 * half, 2 * half + 1) * (dl / 2)
+    g = Grid([m, m.copy(), m.copy()], unit=unit)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(0.0, 1e9)
+    csx.AddExcitation("infDipole", 1, [0, 0, 1.0]).AddBox([0, 0, -dl / 2], [0, 0, dl / 2])
+    s1 = [-4.5 * dl / 2] * 3
+    s2 = [4.5 * dl / 2] * 3
+    faces = {"xn": (s1, [s1[0], s2[1], s2[2]]), "xp": ([s2[0], s1[1], s1[2]], s2),
+             "yn": (s1, [s2[0], s1[1], s2[2]]), "yp": ([s1[0], s2[1], s1[2]], s2),
+             "zn": (s1, [s2[0], s2[1], s1[2]]), "zp": ([s1[0], s1[1], s2[2]], s2)}
+    for f, (a, b) in faces.items():
+        csx.AddDump("Et_" + f, dump_type=0, dump_mode=0).AddBox(a, b)
+        csx.AddDump("Ht_" + f, dump_type=1, dump_mode=0).AddBox(a, b)
+    coords = [[s1[0], 0, 0], [s2[0], 0, 0], [0, s1[1], 0], [0, s2[1], 0], [0, 0, s1[2]], [0, 0, s2[2]]]
+    for k, c in enumerate(coords):
+        csx.AddProbe("et%d" % (k + 1), 2, frequency=freqs, interval=interval).AddBox(c, c)
+    for k, c in enumerate(coords):
+        csx.AddProbe("ht%d" % (k + 1), 3, frequency=freqs, interval=interval).AddBox(c, c)
+    op = Operator(csx, g, exc, bc=(2,) * 6, over_sampling=10)
+    data = op.build(steps)
+    data.fieldprobe_coords = coords
+    return data
+
+
 def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
     """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""
     nx, ny, nz = shape

@@ -586,8 +586,11 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     oems_adjoint_state* s = e->adj;
     if (!s->steps) return afail(e, OEMS_ERR_STATE, "adjoint backward before forward");
     if (!gvv || !gvi || (nprobe && (!probe_ids || !sources))) return OEMS_ERR_ARG;
-    for (unsigned k = 0; k < nprobe; ++k)
+    for (unsigned k = 0; k < nprobe; ++k) {
         if (probe_ids[k] < 0 || probe_ids[k] >= (int)e->probe_dev.size()) return afail(e, OEMS_ERR_ARG, "bad probe id");
+        if (e->probe_dev[probe_ids[k]].type >= 2)
+            return afail(e, OEMS_ERR_ARG, "field probes are not objectives (voltage/current probes only)");
+    }
     AdjDev& d = s->dev;
     cudaStream_t st = e->stream;
     const unsigned N = s->steps;

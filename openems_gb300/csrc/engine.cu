@@ -527,6 +527,16 @@ static int add_probe(oems_cuda_engine* e, int type, const unsigned* start, const
     return OEMS_OK;
 }
 
+int oems_cuda_add_field_probe(oems_cuda_engine* e, int field, const unsigned int pos[3], const double el[3],
+                              double weight, unsigned int interval, unsigned int start_ts, unsigned int stop_ts,
+                              int* id)
+{
+    if (!e || !el || (field != 0 && field != 1)) return OEMS_ERR_ARG;
+    const int rc = add_probe(e, 2 + field, pos, pos, -1, nullptr, nullptr, weight, interval, start_ts, stop_ts, id);
+    if (rc == OEMS_OK) memcpy(e->probes[*id].el, el, sizeof(double) * 3);
+    return rc;
+}
+
 int oems_cuda_add_voltage_probe(oems_cuda_engine* e, const unsigned int start[3], const unsigned int stop[3],
                                 double weight, unsigned int interval, unsigned int start_ts, unsigned int stop_ts,
                                 int* id)
@@ -1154,7 +1164,12 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
             term.push_back(cell_off(e, comp, x, y, z));
             sign.push_back((signed char)sg);
         };
-        if (p.type == 0) {  // Engine_Interface_FDTD::CalcVoltageIntegral
+        if (p.type >= 2) {  // ProcessFieldProbe: one term per component, divided by its edge length
+            for (int n = 0; n < 3; ++n) {
+                add(n, p.start[0], p.start[1], p.start[2], +1);
+                d.el[n] = p.el[n];
+            }
+        } else if (p.type == 0) {  // Engine_Interface_FDTD::CalcVoltageIntegral
             for (int n = 0; n < 3; ++n) {
                 if (p.start[n] < p.stop[n]) {
                     unsigned pos[3] = {p.start[0], p.start[1], p.start[2]};
@@ -1196,8 +1211,9 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         d.weight = p.weight;
         d.interval = p.interval; d.start_ts = p.start_ts; d.stop_ts = p.stop_ts;
         d.nslots = max_ts / p.interval + 1;
+        d.ncomp = p.type >= 2 ? 3u : 1u;
         {
-            std::vector<double> nan(d.nslots, std::nan(""));
+            std::vector<double> nan((size_t)d.nslots * d.ncomp, std::nan(""));
             double* ser;
             if ((rc = dupload(e, &ser, nan.data(), nan.size()))) return rc;
             e->state.push_back({ser, nan.size() * sizeof(double)});
@@ -1211,7 +1227,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
             std::vector<double2> ph((size_t)d.nsamp * d.nf);
             for (unsigned k = 0; k < d.nsamp; ++k) {
                 const double ts = (double)k * d.fd_interval;
-                const double time = (ts + (double)(p.type == 1) * 0.5) * e->dt;
+                const double time = (ts + (double)(p.type == 1 || p.type == 3) * 0.5) * e->dt;
                 for (unsigned f = 0; f < d.nf; ++f) {
                     const std::complex<double> ex = std::exp(std::complex<double>(-0.0, ((-2.0 * kPI) * p.freqs[f]) * time));
                     ph[(size_t)k * d.nf + f] = make_double2(ex.real(), ex.imag());
@@ -1221,7 +1237,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
             if ((rc = dupload(e, &dph, ph.data(), ph.size()))) return rc;
             d.phasor = dph;
             double* dd;
-            if ((rc = dalloc(e, &dd, 2 * (size_t)d.nf, true, true))) return rc;
+            if ((rc = dalloc(e, &dd, 2 * (size_t)d.nf * d.ncomp, true, true))) return rc;
             d.dft = dd;
         } else {
             d.fd_interval = 0;
@@ -1470,7 +1486,7 @@ int oems_cuda_read_probe(oems_cuda_engine* e, int id, double* out, size_t cap, s
     if (!e || !out || !count || id < 0 || id >= (int)e->probe_dev.size()) return OEMS_ERR_ARG;
     if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
     const ProbeDev& d = e->probe_dev[id];
-    const size_t n = std::min<size_t>(cap, d.nslots);
+    const size_t n = std::min<size_t>(cap, (size_t)d.nslots * d.ncomp);
     CK(cudaMemcpyAsync(out, d.series, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     *count = n;
@@ -1484,7 +1500,8 @@ int oems_cuda_read_probe_range(oems_cuda_engine* e, int id, size_t first, size_t
     const ProbeDev& d = e->probe_dev[id];
     if (first + count > d.nslots) return fail(e, OEMS_ERR_ARG, "probe slot range out of bounds");
     if (count) {
-        CK(cudaMemcpyAsync(out, d.series + first, count * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpyAsync(out, d.series + first * d.ncomp, count * d.ncomp * sizeof(double),
+                           cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
     }
     return OEMS_OK;
@@ -1496,7 +1513,7 @@ int oems_cuda_read_probe_dft(oems_cuda_engine* e, int id, double* out)
     if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
     const ProbeDev& d = e->probe_dev[id];
     if (d.nf) {
-        CK(cudaMemcpyAsync(out, d.dft, 2 * d.nf * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpyAsync(out, d.dft, 2 * d.nf * d.ncomp * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
     }
     return OEMS_OK;

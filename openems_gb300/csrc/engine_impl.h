@@ -32,8 +32,9 @@ struct LorHost {
     std::vector<float> vint, vext, vlor, iint, iext, ilor;
 };
 struct ProbeHost {
-    int type;
+    int type;                      // 0 voltage, 1 current, 2 E field, 3 H field
     unsigned start[3], stop[3];
+    double el[3] = {0, 0, 0};      // field probes: edge lengths at start
     int nd, si[3], ei[3];
     double weight;
     unsigned interval, start_ts, stop_ts;

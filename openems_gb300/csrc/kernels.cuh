@@ -818,16 +818,18 @@ static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long
 // Common/processintegral.cpp:134-171), FD field dumps (ProcessFieldsFD::Process,
 // Common/processfields_fd.cpp:72-107) and the numTS increment.
 struct ProbeDev {
-    int type;                        // 0 voltage (double sum), 1 current (float sum)
+    int type;                        // 0 voltage (double sum), 1 current (float sum), 2/3 E/H field
+    unsigned ncomp;                  // values per sample: 1, or 3 (field probes)
+    double el[3];                    // field probes: edge length of each component
     unsigned nterm;
     const unsigned long long* term;  // field offsets in reference summation order
     const signed char* sign;         // +1 / -1
     double weight;
     unsigned interval, start_ts, stop_ts, nslots;
-    double* series;
+    double* series;                  // [nslots][ncomp]
     unsigned fd_interval, nf, nsamp;
     const double2* phasor;           // [nsamp][nf] = exp(-2j*pi*f*t)
-    double* dft;                     // [nf][2]
+    double* dft;                     // [nf][ncomp][2]
     double dt;
 };
 
@@ -856,13 +858,46 @@ struct StepEndDev {
     unsigned* blocks_done;
 };
 
+// Record value*weight `a` of component c: the time series slot and the DFT accumulation
+// (ProcessIntegral::Process, Common/processintegral.cpp:144-167), double arithmetic in its order.
+static __device__ void probe_record(const ProbeDev& p, unsigned ts, unsigned c, double a, bool do_td, bool do_fd)
+{
+    if (do_td) {
+        const unsigned slot = ts / p.interval;
+        if (slot < p.nslots) p.series[(unsigned long long)slot * p.ncomp + c] = a;
+    }
+    if (do_fd) {
+        const unsigned smp = ts / p.fd_interval;
+        if (smp < p.nsamp) {
+            for (unsigned f = 0; f < p.nf; ++f) {
+                const double2 e = p.phasor[(unsigned long long)smp * p.nf + f];
+                double re = __dmul_rn(e.x, a), im = __dmul_rn(e.y, a);
+                re = __dmul_rn(re, 2.0); im = __dmul_rn(im, 2.0);
+                re = __dmul_rn(re, p.dt); im = __dmul_rn(im, p.dt);
+                re = __dmul_rn(re, (double)p.fd_interval); im = __dmul_rn(im, (double)p.fd_interval);
+                double* acc = p.dft + 2 * ((unsigned long long)f * p.ncomp + c);
+                acc[0] = __dadd_rn(acc[0], re);
+                acc[1] = __dadd_rn(acc[1], im);
+            }
+        }
+    }
+}
+
 static __device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned ts, int lane)
 {
     if (ts < p.start_ts || ts > p.stop_ts) return;
     const bool do_td = (ts % p.interval) == 0;
     const bool do_fd = p.fd_interval && (ts % p.fd_interval) == 0;
     if (!do_td && !do_fd) return;
-    const float* F = p.type == 0 ? g.V : g.I;
+    const float* F = (p.type == 0 || p.type == 2) ? g.V : g.I;
+    if (p.type >= 2) {
+        // ProcessFieldProbe: lane n evaluates component n (GetRawField / GetRawDualField)
+        if (lane >= 3) return;
+        const double value = (double)__ldcg(F + p.term[lane]);
+        const double delta = p.el[lane];
+        probe_record(p, ts, lane, __dmul_rn(delta != 0.0 ? __ddiv_rn(value, delta) : 0.0, p.weight), do_td, do_fd);
+        return;
+    }
     // lanes fetch terms in parallel, lane 0 accumulates them in the reference's order
     double accd = 0.0;
     float accf = 0.0f;
@@ -883,25 +918,7 @@ static __device__ void probe_eval(const GridDev& g, const ProbeDev& p, unsigned 
     }
     if (lane != 0) return;
     const double val = p.type == 0 ? accd : (double)accf;
-    const double a = __dmul_rn(val, p.weight);
-    if (do_td) {
-        const unsigned slot = ts / p.interval;
-        if (slot < p.nslots) p.series[slot] = a;
-    }
-    if (do_fd) {
-        const unsigned smp = ts / p.fd_interval;
-        if (smp < p.nsamp) {
-            for (unsigned f = 0; f < p.nf; ++f) {
-                const double2 e = p.phasor[(unsigned long long)smp * p.nf + f];
-                double re = __dmul_rn(e.x, a), im = __dmul_rn(e.y, a);
-                re = __dmul_rn(re, 2.0); im = __dmul_rn(im, 2.0);
-                re = __dmul_rn(re, p.dt); im = __dmul_rn(im, p.dt);
-                re = __dmul_rn(re, (double)p.fd_interval); im = __dmul_rn(im, (double)p.fd_interval);
-                p.dft[2 * f] = __dadd_rn(p.dft[2 * f], re);
-                p.dft[2 * f + 1] = __dadd_rn(p.dft[2 * f + 1], im);
-            }
-        }
-    }
+    probe_record(p, ts, 0, __dmul_rn(val, p.weight), do_td, do_fd);
 }
 
 // E (Engine_Interface_FDTD::GetRawInterpolatedField, FDTD/engine_interface_fdtd.cpp:63-123) or

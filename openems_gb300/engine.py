@@ -40,6 +40,7 @@ class EngineBase:
         self.max_ts = int(max_timesteps)
         self._keep = []
         self.vprobe_ids, self.iprobe_ids, self.dump_ids = [], [], []
+        self.fprobe_ids = []
         self.td_dump_ids = []
         # time-domain dump files go to <dump_path>/<dump name>_<numTS>.vtr, as the reference
         # writes them into the simulation path
@@ -140,6 +141,22 @@ class EngineBase:
                      "add_current_probe")
             self._probe_dft(pid.value, p)
             self.iprobe_ids.append(pid.value)
+        fps = list(getattr(op, "fprobes", []) or [])
+        if fps:
+            from .operator import _main_delta, _dual_delta
+            g = op.grid
+            for p in fps:
+                pid = C.c_int(-1)
+                pos = self._a(p.pos, np.uint32)
+                # GetEdgeLength(n, pos) of the main mesh (E) or the dual mesh (H)
+                delta = _main_delta if p.field == 0 else _dual_delta
+                el = self._a([float(delta(np.asarray(g.lines[n], np.float64))[int(p.pos[n])] * g.unit)
+                              for n in range(3)], np.float64)
+                self._ck(L.add_field_probe(self.h, int(p.field), _p(pos, C.c_uint), _p(el, C.c_double),
+                                           float(p.weight), int(p.interval), int(p.start_ts),
+                                           int(min(p.stop_ts, 0xFFFFFFFF)), C.byref(pid)), "add_field_probe")
+                self._probe_dft(pid.value, p)
+                self.fprobe_ids.append(pid.value)
         td = list(getattr(op, "td_dumps", []) or [])
         if op.dumps or td:
             g = op.grid
@@ -215,17 +232,27 @@ class EngineBase:
     def SetCurr(self, n, x, y, z, value):
         self._ck(self.lib.set_value(self.h, CURR, n, x, y, z, float(value)), "set_value")
 
+    def _ncomp(self, pid: int) -> int:
+        return 3 if pid in self.fprobe_ids else 1
+
     def probe_series(self, pid: int) -> np.ndarray:
-        cap = self.max_ts + 1
+        """Samples of probe `pid` (NaN where no sample was taken); a field probe gives [n][3]."""
+        nc = self._ncomp(pid)
+        cap = (self.max_ts + 1) * nc
         out = np.empty(cap, np.float64)
         cnt = C.c_size_t(0)
         self._ck(self.lib.read_probe(self.h, pid, _p(out, C.c_double), cap, C.byref(cnt)), "read_probe")
-        return out[:cnt.value]
+        out = out[:cnt.value]
+        return out.reshape(-1, 3) if nc == 3 else out
 
     def probe_dft(self, pid: int, nf: int) -> np.ndarray:
-        out = np.zeros(2 * max(nf, 1), np.float64)
+        """Accumulated DFT of probe `pid` at its nf frequencies; a field probe gives [nf][3]."""
+        nc = self._ncomp(pid)
+        n = nf * nc
+        out = np.zeros(2 * max(n, 1), np.float64)
         self._ck(self.lib.read_probe_dft(self.h, pid, _p(out, C.c_double)), "read_probe_dft")
-        return out[0:2 * nf:2] + 1j * out[1:2 * nf:2]
+        z = out[0:2 * n:2] + 1j * out[1:2 * n:2]
+        return z.reshape(nf, 3) if nc == 3 else z
 
     def fd_dump(self, did: int) -> np.ndarray:
         d = self.op.dumps[self.dump_ids.index(did)]
@@ -294,10 +321,13 @@ class Engine_CUDA(EngineBase):
         return list(ms), list(cnt)
 
     def probe_range(self, pid: int, first: int, count: int) -> np.ndarray:
-        out = np.empty(max(count, 1), np.float64)
+        """Sample slots [first, first+count) of probe `pid` ([count][3] for a field probe)."""
+        nc = self._ncomp(pid)
+        out = np.empty(max(count * nc, 1), np.float64)
         self._ck(self.lib.read_probe_range(self.h, pid, int(first), int(count), _p(out, C.c_double)),
                  "read_probe_range")
-        return out[:count]
+        out = out[:count * nc]
+        return out.reshape(-1, 3) if nc == 3 else out
 
     def snapshot(self) -> bytes:
         sz = C.c_size_t()

@@ -185,8 +185,8 @@ class Structure:
 
     def AddProbe(self, name, p_type, weight=1.0, norm_dir=-1, frequency=(), start_time=0.0, stop_time=0.0,
                  interval=0):
-        """Voltage (p_type 0) or current (p_type 1) probe; ``interval`` overrides the default
-        sampling interval Nyquist/OverSampling (openems.cpp:568)."""
+        """Voltage (p_type 0), current (1), E-field (2) or H-field (3) probe; ``interval``
+        overrides the default sampling interval Nyquist/OverSampling (openems.cpp:568)."""
         return self._add(PROBE, name, p_type=int(p_type), weight=float(weight), norm_dir=int(norm_dir),
                          frequency=list(frequency), start_time=float(start_time), stop_time=float(stop_time),
                          interval=int(interval))
@@ -349,6 +349,22 @@ class CurrentProbe:
 
 
 @dataclass
+class FieldProbe:
+    """E (field 0, probe type 2) or H (field 1, probe type 3) point probe: the three Yee values at
+    ``pos`` (main mesh for E, dual mesh for H) over their edge lengths, no interpolation
+    (ProcessFieldProbe, Common/processfieldprobe.cpp:77-92); H samples carry the dual time."""
+    name: str
+    field: int
+    pos: np.ndarray
+    weight: float
+    interval: int
+    fd_interval: int
+    freqs: list
+    start_ts: int = 0
+    stop_ts: int = 0xFFFFFFFF
+
+
+@dataclass
 class FieldDumpFD:
     """FD dump box (Common/processfields_fd.cpp): E (field=0) or H (field=1); interp = the dump
     mode (0 none, 1 node, 2 cell interpolation); dual = the box was snapped to the dual mesh."""
@@ -399,6 +415,7 @@ class OperatorData:
     tfsf: Optional[TFSFTable] = None
     rlc: Optional[LumpedRLCTable] = None
     td_dumps: list = field(default_factory=list)
+    fprobes: list = field(default_factory=list)
 
 
 # lumped element types (CSPropLumpedElement::LEtype)
@@ -1043,7 +1060,8 @@ class Operator:
         data = OperatorData(num_lines=self.N.astype(np.uint32), dt=dT, vv=self.vv, vi=self.vi, ii=self.ii,
                             iv=self.iv, exc=exc, upml=upml, mur=mur, lorentz=lorentz, vprobes=vprobes,
                             iprobes=iprobes, dumps=dumps, nyquist=self.exc.GetNyquistNum(),
-                            excitation=self.exc, grid=self.grid, tfsf=tfsf, rlc=rlc, td_dumps=self.td_dumps)
+                            excitation=self.exc, grid=self.grid, tfsf=tfsf, rlc=rlc, td_dumps=self.td_dumps,
+                            fprobes=self.fprobes)
         return data
 
     # ---- boundary conditions ---------------------------------------------------------------
@@ -2023,6 +2041,7 @@ class Operator:
     def _build_processing(self):
         vprobes, iprobes, dumps = [], [], []
         td_dumps = self.td_dumps = []
+        fprobes = self.fprobes = []
         nyq = self.exc.GetNyquistNum()
         for prop in self.csx.props:
             if prop.kind == PROBE:
@@ -2077,6 +2096,14 @@ class Operator:
                             continue
                         iprobes.append(CurrentProbe(prop.name, s, e, nd, si, ei, prop.params["weight"], interval,
                                                     fd_interval, freqs, start_ts, stop_ts))
+                    elif pt in (2, 3):
+                        # field probes snap to the main (E) or dual (H) mesh, SnapMethod 0
+                        # (openems.cpp:559-577, Processing::DefineStartStopCoord)
+                        dim, s, e, _, _ = self.snap_box(lo, hi, dual=pt == 3, method=0)
+                        if dim < 0:
+                            continue
+                        fprobes.append(FieldProbe(prop.name, pt - 2, s, prop.params["weight"], interval,
+                                                  fd_interval, freqs, start_ts, stop_ts))
             elif prop.kind == DUMP and prop.params["dump_type"] in (0, 1):
                 # ProcessFieldsTD (openems.cpp:611-690): interval Nyquist/OverSampling
                 field_ = prop.params["dump_type"]

@@ -74,8 +74,10 @@ typedef struct {
 } lor_t;
 
 typedef struct {
-    int type; /* 0 voltage, 1 current */
+    int type; /* 0 voltage, 1 current, 2 E field, 3 H field */
     unsigned start[3], stop[3];
+    double el[3]; /* field probes: edge length of each component at start (E main, H dual mesh) */
+    unsigned ncomp; /* values per sample: 1, or 3 for a field probe */
     int nd, si[3], ei[3];
     double weight;
     unsigned interval, start_ts, stop_ts;
@@ -591,11 +593,12 @@ static int add_probe(eng_t *e, int type, const unsigned start[3], const unsigned
         int diff = (start[0] != stop[0]) + (start[1] != stop[1]) + (start[2] != stop[2]);
         if (diff != 1)
             return ERR_ARG;
-    } else if (nd < 0 || nd > 2)
+    } else if (type == 1 && (nd < 0 || nd > 2))
         return ERR_ARG;
     probe_t *p = &e->probes[e->nprobes];
     memset(p, 0, sizeof(*p));
     p->type = type;
+    p->ncomp = type >= 2 ? 3 : 1;
     memcpy(p->start, start, 12);
     memcpy(p->stop, stop, 12);
     p->nd = nd;
@@ -624,6 +627,19 @@ int oems_ref_add_current_probe(eng_t *e, const unsigned start[3], const unsigned
     return add_probe(e, 1, start, stop, nd, si, ei, weight, interval, start_ts, stop_ts, id);
 }
 
+/* ProcessFieldProbe (Common/processfieldprobe.cpp:77-92): the E (field 0) or H (field 1) field
+ * at one Yee position without interpolation; el = the three edge lengths there */
+int oems_ref_add_field_probe(eng_t *e, int field, const unsigned pos[3], const double el[3], double weight,
+                             unsigned interval, unsigned start_ts, unsigned stop_ts, int *id)
+{
+    if (!e || !el || (field != 0 && field != 1))
+        return ERR_ARG;
+    int rc = add_probe(e, 2 + field, pos, pos, -1, NULL, NULL, weight, interval, start_ts, stop_ts, id);
+    if (rc == OK)
+        memcpy(e->probes[*id].el, el, sizeof(double) * 3);
+    return rc;
+}
+
 int oems_ref_set_probe_dft(eng_t *e, int id, unsigned fd_interval, unsigned nf, const double *freqs)
 {
     if (!e || id < 0 || id >= e->nprobes || (nf && !freqs))
@@ -634,7 +650,7 @@ int oems_ref_set_probe_dft(eng_t *e, int id, unsigned fd_interval, unsigned nf, 
     free(p->freqs); free(p->dft);
     p->freqs = (double *)xcalloc(nf, 8);
     if (nf) memcpy(p->freqs, freqs, 8 * (size_t)nf);
-    p->dft = (double *)xcalloc(2 * (size_t)nf, 8);
+    p->dft = (double *)xcalloc(2 * (size_t)nf * p->ncomp, 8);
     return OK;
 }
 
@@ -1194,6 +1210,35 @@ static void process_probes(eng_t *e)
         int do_fd = p->fd_interval && (ts % p->fd_interval) == 0;
         if (!do_td && !do_fd)
             continue;
+        if (p->type >= 2) {
+            /* Engine_Interface_FDTD::GetRawField (FDTD/engine_interface_fdtd.cpp:263-276) / GetRawDualField (:136-148):
+             * value / edge length, 0 on a zero length; rows of ProcessIntegral::Process per component */
+            const unsigned *q = p->start;
+            double time = ((double)ts + (double)(p->type == 3) * 0.5) * e->dt;
+            for (unsigned c = 0; c < 3; ++c) {
+                double value = p->type == 2 ? (double)GETV(e, c, q[0], q[1], q[2]) : (double)GETI(e, c, q[0], q[1], q[2]);
+                double v = p->el[c] != 0.0 ? value / p->el[c] : 0.0;
+                double a = v * p->weight;
+                if (do_td) {
+                    size_t slot = ts / p->interval;
+                    if (slot < p->nslots)
+                        p->series[3 * slot + c] = a;
+                }
+                if (do_fd) {
+                    for (unsigned f = 0; f < p->nf; ++f) {
+                        double th = ((-2.0 * M_PI_REF) * p->freqs[f]) * time;
+                        double complex ex = cexp(CMPLX(-0.0, th));
+                        double re = creal(ex) * a, im = cimag(ex) * a;
+                        re = re * 2.0; im = im * 2.0;
+                        re = re * e->dt; im = im * e->dt;
+                        re = re * (double)p->fd_interval; im = im * (double)p->fd_interval;
+                        p->dft[2 * (3 * f + c)] += re;
+                        p->dft[2 * (3 * f + c) + 1] += im;
+                    }
+                }
+            }
+            continue;
+        }
         double val = p->type == 0 ? voltage_integral(e, p) : current_integral(e, p);
         double time = ((double)ts + (double)(p->type == 1) * 0.5) * e->dt;
         if (do_td) {
@@ -1575,8 +1620,8 @@ int oems_ref_init(eng_t *e, unsigned max_ts)
     for (int k = 0; k < e->nprobes; ++k) {
         probe_t *p = &e->probes[k];
         p->nslots = max_ts / p->interval + 1;
-        p->series = (double *)malloc(p->nslots * sizeof(double));
-        for (size_t s = 0; s < p->nslots; ++s)
+        p->series = (double *)malloc(p->nslots * p->ncomp * sizeof(double));
+        for (size_t s = 0; s < p->nslots * p->ncomp; ++s)
             p->series[s] = NAN;
     }
     e->inited = 1;
@@ -1665,7 +1710,8 @@ int oems_ref_read_probe(eng_t *e, int id, double *out, size_t cap, size_t *count
     if (!e || id < 0 || id >= e->nprobes || !out || !count)
         return ERR_ARG;
     probe_t *p = &e->probes[id];
-    size_t n = p->nslots < cap ? p->nslots : cap;
+    size_t tot = p->nslots * p->ncomp;
+    size_t n = tot < cap ? tot : cap;
     memcpy(out, p->series, n * sizeof(double));
     *count = n;
     return OK;
@@ -1676,7 +1722,7 @@ int oems_ref_read_probe_dft(eng_t *e, int id, double *out)
     if (!e || id < 0 || id >= e->nprobes || !out)
         return ERR_ARG;
     probe_t *p = &e->probes[id];
-    memcpy(out, p->dft, 2 * p->nf * sizeof(double));
+    memcpy(out, p->dft, 2 * p->nf * p->ncomp * sizeof(double));
     return OK;
 }
 

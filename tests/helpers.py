@@ -35,11 +35,13 @@ def compare_engines(ga, gb, check_dumps=True):
     for w in (0, 1):
         fa, fb = ga.read_field(w), gb.read_field(w)
         out[f"field{w}"] = bits_equal(fa, fb)
-    for pid in ga.vprobe_ids + ga.iprobe_ids:
+    fids = list(getattr(ga, "fprobe_ids", []))
+    fps = list(getattr(ga.op, "fprobes", []) or [])
+    for pid in ga.vprobe_ids + ga.iprobe_ids + fids:
         sa, sb = ga.probe_series(pid), gb.probe_series(pid)
         out[f"probe{pid}"] = np.array_equal(np.isnan(sa), np.isnan(sb)) and bits_equal(
             np.nan_to_num(sa), np.nan_to_num(sb))
-    for pid, p in zip(ga.vprobe_ids + ga.iprobe_ids, ga.op.vprobes + ga.op.iprobes):
+    for pid, p in zip(ga.vprobe_ids + ga.iprobe_ids + fids, ga.op.vprobes + ga.op.iprobes + fps):
         if p.fd_interval and p.freqs:
             out[f"dft{pid}"] = bits_equal(ga.probe_dft(pid, len(p.freqs)), gb.probe_dft(pid, len(p.freqs)))
     if check_dumps:
