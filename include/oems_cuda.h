@@ -132,6 +132,19 @@ int oems_cuda_set_tfsf(oems_cuda_engine* eng, unsigned int volt_count, const uns
                        const float* curr_amp, const float* sig_volt, const float* sig_curr, unsigned int length,
                        unsigned int period, unsigned int max_delay);
 
+/* Engine_Ext_Cylinder (FDTD/extensions/engine_ext_cylinder.cpp:45-101) with Operator_Ext_Cylinder's
+ * tables (FDTD/extensions/operator_ext_cylinder.cpp:44-112), for a mesh in cylindrical coordinates
+ * (x = rho, y = alpha, z) whose operator Operator_Cylinder built. closed_alpha: the alpha lines
+ * span 2*pi and line Ny-2 repeats line 0; after each voltage update the rho and z voltages of
+ * line Ny-2 are copied onto line 0, after each current update the rho and z currents of line 0
+ * onto line Ny-2. r0_included (closed meshes only): rho = 0 is the first line and the axis z
+ * voltage becomes V*vv_r0[z] + sum over alpha lines 0..Ny-2 of vi_r0[z]*I_alpha (float, in that
+ * order), written to every alpha line, with the alpha voltages on the axis set to zero; vv_r0 and
+ * vi_r0 hold Nz floats. The post-voltage hook runs before the TFSF and Mur post hooks (priority
+ * 1e5). Batched and adjoint runs reject it. */
+int oems_cuda_set_cylinder(oems_cuda_engine* eng, int closed_alpha, int r0_included, const float* vv_r0,
+                           const float* vi_r0);
+
 /* Engine_Ext_LumpedRLC (FDTD/extensions/engine_ext_lumpedRLC.cpp:80-147) fed with
  * Operator_Ext_LumpedRLC's tables (FDTD/extensions/operator_ext_lumpedRLC.h:58-82): count lumped
  * edges, pos unsigned [3][count] (v_RLC_pos), dir int [count] (v_RLC_dir) and the float [count]
@@ -382,7 +395,7 @@ int oems_cuda_timed_iterate(oems_cuda_engine* eng, unsigned int n_steps, float* 
 /* Kernel classes reported by oems_cuda_profile_steps. */
 #define OEMS_KC_UPDATE_V  0
 #define OEMS_KC_UPDATE_I  1
-#define OEMS_KC_MUR       2
+#define OEMS_KC_MUR       2   /* boundary hooks: Mur walls and the cylinder's alpha seam / axis */
 #define OEMS_KC_LORENTZ   3   /* auxiliary-equation kernels: Drude/Lorentz and lumped RLC */
 #define OEMS_KC_EXCITE    4
 #define OEMS_KC_STEP_END  5

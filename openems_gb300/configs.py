@@ -449,6 +449,55 @@ def fieldprobes(half=8, steps=600, freqs=(5e8,), interval=0):
     return data
 
 
+def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71):
+    """The reference's coax example in cylindrical coordinates
+    (matlab/examples/waveguide/Coax_CylinderCoords.m:25-123): rho from the inner radius 100 to the
+    outer radius 230 on a 10 mm mesh, 71 alpha lines over 2*pi (a closed mesh), z over 1000 mm; PEC
+    on every wall but Mur at the far end; a radial soft excitation weighted 1/rho on the z = 0 plane
+    (f0 = fc = 0.5 GHz); half way down, a voltage probe across the gap at alpha = 0 and a current
+    loop around the inner conductor on the dual mesh (one full turn of alpha)."""
+    from .operator_cyl import OperatorCylinder
+    r_i, r_a = 100.0, 230.0
+    rs = np.arange(r_i, r_a + 0.5 * res, res)
+    al = np.linspace(0.0, 2 * np.pi, n_alpha)
+    zs = np.arange(0.0, length + 0.5 * res, res)
+    g = Grid([rs, al, zs], unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(0.5e9, 0.5e9)
+    weight = (lambda r, a, z: 1.0 / r, lambda r, a, z: 0.0, lambda r, a, z: 0.0)
+    csx.AddExcitation("excite", 0, [1.0, 0, 0], weight=weight).AddBox([r_i, al[0], 0.0], [r_a, al[-1], 0.0])
+    zm = zs[len(zs) // 2]
+    csx.AddProbe("ut1", 0, interval=1).AddBox([r_i, 0.0, zm], [r_a, 0.0, zm])
+    mid = 0.5 * (r_i + r_a)
+    a1 = al[1]
+    # the loop starts below the mesh (no inner side) and runs over dual alpha lines 0 .. N-2
+    csx.AddProbe("it1", 1, norm_dir=2, interval=1).AddBox([0.0, 0.5 * a1, zm], [mid, 2 * np.pi + 0.5 * a1, zm])
+    op = OperatorCylinder(csx, g, exc, bc=(0, 0, 0, 0, 0, 2))
+    return op.build(steps)
+
+
+def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe_r=0.0):
+    """A pillbox cavity in cylindrical coordinates with rho = 0 on the mesh: radius 50 mm, height
+    20 mm, PEC walls, a 2.5 mm rho/z mesh and 10 degree alpha steps (a closed mesh), a soft Ez
+    point source off the axis (f0 3 GHz, fc 2 GHz) and an Ez voltage probe at ``probe_r`` (on the
+    axis by default, where the TM010 field is largest and the axis hook computes it)."""
+    from .operator_cyl import OperatorCylinder
+    rs = np.arange(0.0, radius + 0.5 * res, res)
+    al = np.linspace(0.0, 2 * np.pi, n_alpha)
+    zs = np.arange(0.0, height + 0.5 * res, res)
+    g = Grid([rs, al, zs], unit=1e-3)
+    csx = Structure()
+    exc = Excitation()
+    exc.SetupGaussianPulse(3e9, 2e9)
+    k = len(zs) // 2
+    rs_src = rs[len(rs) // 3]
+    csx.AddExcitation("src", 0, [0, 0, 1.0]).AddBox([rs_src, al[3], zs[k]], [rs_src, al[3], zs[k + 1]])
+    csx.AddProbe("uz", 0, interval=1).AddBox([probe_r, 0.0, zs[1]], [probe_r, 0.0, zs[-2]])
+    op = OperatorCylinder(csx, g, exc, bc=(0,) * 6)
+    return op.build(steps)
+
+
 def patch(shape=(160, 160, 80), steps=20000, with_nf2ff=True):
     """Microstrip patch antenna on a graded mesh with UPML, lumped port and NF2FF box."""
     nx, ny, nz = shape

@@ -477,9 +477,9 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     if (!e || !box_start || !box_stop) return OEMS_ERR_ARG;
     if (!e->inited) return afail(e, OEMS_ERR_STATE, "engine not initialised");
     if (e->adj) return afail(e, OEMS_ERR_STATE, "adjoint already set up");
-    if (!e->mur.empty() || !e->lor.empty() || e->has_tfsf || e->rlc.count || e->has_td)
+    if (!e->mur.empty() || !e->lor.empty() || e->has_tfsf || e->rlc.count || e->has_td || e->cyl_closed)
         return afail(e, OEMS_ERR_UNSUPPORTED,
-                     "adjoint: Mur walls, dispersive materials, TFSF and lumped RLC loads are not supported");
+                     "adjoint: Mur walls, dispersive materials, TFSF, lumped RLC loads and cylinder meshes are not supported");
     for (int a = 0; a < 3; ++a)
         if (box_start[a] >= box_stop[a] || box_stop[a] > e->N[a]) return afail(e, OEMS_ERR_ARG, "adjoint: design box outside the mesh");
     for (const auto& u : e->upml) {

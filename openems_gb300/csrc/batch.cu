@@ -488,7 +488,7 @@ int oems_cuda_batch_create(oems_cuda_engine* const* engines, unsigned int count,
         if (k == 0) b->device = e->device;
         if (e->device != b->device) return OEMS_ERR_ARG;
         // the fused batch step covers the excitation, UPML and probe paths
-        if (!e->mur.empty() || !e->lor.empty() || !e->dumps.empty() || e->has_tfsf || e->rlc.count)
+        if (!e->mur.empty() || !e->lor.empty() || !e->dumps.empty() || e->has_tfsf || e->rlc.count || e->cyl_closed)
             return OEMS_ERR_UNSUPPORTED;
         if (e->excV.count > kMaxFusedSources || e->excI.count > kMaxFusedSources) return OEMS_ERR_UNSUPPORTED;
         b->eng.push_back(e);

@@ -412,6 +412,21 @@ int oems_cuda_set_tfsf(oems_cuda_engine* e, unsigned int volt_count, const unsig
     return OEMS_OK;
 }
 
+int oems_cuda_set_cylinder(oems_cuda_engine* e, int closed_alpha, int r0_included, const float* vv_r0,
+                           const float* vi_r0)
+{
+    if (!e) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if (r0_included && (!closed_alpha || !vv_r0 || !vi_r0))
+        return fail(e, OEMS_ERR_ARG, "rho = 0 needs a closed alpha mesh and its axis coefficients");
+    if (e->N[1] < 3) return fail(e, OEMS_ERR_ARG, "a closed alpha mesh needs at least 3 alpha lines");
+    e->cyl_closed = closed_alpha != 0;
+    e->cyl_r0 = e->cyl_closed && r0_included != 0;
+    e->cyl_vv_r0.assign(e->cyl_r0 ? vv_r0 : nullptr, e->cyl_r0 ? vv_r0 + e->N[2] : nullptr);
+    e->cyl_vi_r0.assign(e->cyl_r0 ? vi_r0 : nullptr, e->cyl_r0 ? vi_r0 + e->N[2] : nullptr);
+    return OEMS_OK;
+}
+
 int oems_cuda_set_lumped_rlc(oems_cuda_engine* e, unsigned int count, const unsigned int* pos, const int* dir,
                              const float* ilv, const float* i2v, const float* vv2, const float* vj1, const float* vj2,
                              const float* vvd, const float* ib0, const float* b1, const float* b2)
@@ -801,6 +816,12 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     launch_update(e, false, s);
     post();
     ++L;
+    const unsigned cyl_v = g.Nx * g.Nz, cyl_i = (g.Nx - 1) * (g.Nz - 1);
+    if (e->cyl.closed) {   // post-voltage hook, priority 1e5: before TFSF and Mur
+        pre(OEMS_KC_MUR);
+        k_cyl_post_v<<<(cyl_v + 255) / 256, blk, 0, s>>>(g, e->cyl);
+        post(); ++L;
+    }
     if (e->tfsfV.ntarget) {
         pre(OEMS_KC_EXCITE);
         k_tfsf<<<(e->tfsfV.ntarget + 255) / 256, blk, 0, s>>>(e->dV, e->tfsfV, e->d_numTS);
@@ -822,6 +843,11 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     launch_update(e, true, s);
     post();
     ++L;
+    if (e->cyl.closed) {
+        pre(OEMS_KC_MUR);
+        k_cyl_post_i<<<(cyl_i + 255) / 256, blk, 0, s>>>(g);
+        post(); ++L;
+    }
     if (e->tfsfI.ntarget) {
         pre(OEMS_KC_EXCITE);
         k_tfsf<<<(e->tfsfI.ntarget + 255) / 256, blk, 0, s>>>(e->dI, e->tfsfI, e->d_numTS);
@@ -1043,11 +1069,26 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         // lumped RLC loads: their apply reads the raw updated value of an edge that may be a
         // Mur line, which the form inside the voltage update does not keep.
         const char* ms = getenv("OEMS_CUDA_MUR_SEPARATE");
-        e->mur_separate = (ms && ms[0] == '1') || e->has_tfsf || !e->rlc_host.off.empty();
+        // The cylinder's post-voltage hook (priority 1e5) rewrites the alpha seam and the axis
+        // before the Mur post hook reads its lines, so it needs them too.
+        e->mur_separate = (ms && ms[0] == '1') || e->has_tfsf || !e->rlc_host.off.empty() || e->cyl_closed;
         // the lane-parallel form: no UPML (plain update kernel), every wall active from step 0
         bool always = true;
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
         md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
+    }
+
+    // cylinder extension
+    if (e->cyl_closed) {
+        e->cyl.closed = 1;
+        e->cyl.r0 = e->cyl_r0;
+        if (e->cyl_r0) {
+            float *a, *b;
+            if ((rc = dupload(e, &a, e->cyl_vv_r0.data(), e->cyl_vv_r0.size()))) return rc;
+            if ((rc = dupload(e, &b, e->cyl_vi_r0.data(), e->cyl_vi_r0.size()))) return rc;
+            e->cyl.vv_r0 = a;
+            e->cyl.vi_r0 = b;
+        }
     }
 
     // TFSF: group the terms by target cell (stable, so each cell keeps the reference's order)
@@ -1340,6 +1381,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     {
         const char* env = getenv("OEMS_CUDA_FUSED");
         e->use_fused = env && env[0] == '1' && e->mur.empty() && e->lor.empty() && !e->has_tfsf && !e->rlc.count &&
+                       !e->cyl_closed &&
                        e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC && e->K % 2 == 0 &&
                        3ull * e->S < (1ull << 32);        // the staged-plane offsets are 32-bit
         if (e->use_fused && (rc = setup_fused(e))) return rc;

@@ -122,6 +122,9 @@ struct oems_cuda_engine {
     unsigned tfsf_len = 0, tfsf_period = 0;
     // lumped RLC loads
     RlcHost rlc_host;
+    // cylinder extension: closed alpha mesh, rho = 0 on it, axis coefficients [Nz]
+    int cyl_closed = 0, cyl_r0 = 0;
+    std::vector<float> cyl_vv_r0, cyl_vi_r0;
 
     // device state after init
     bool inited = false;
@@ -133,6 +136,7 @@ struct oems_cuda_engine {
     ExcDev excV{}, excI{};
     TfsfDev tfsfV{}, tfsfI{};
     RlcDev rlc{};
+    CylDev cyl{};
     MurDev murdev{};
     std::vector<LorDev> lorV, lorI;
     StepEndDev stepend{};

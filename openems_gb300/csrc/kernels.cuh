@@ -683,6 +683,55 @@ struct RlcDev {
     float* j;                        // [3][count] auxiliary currents
 };
 
+// Engine_Ext_Cylinder (FDTD/extensions/engine_ext_cylinder.cpp:45-101) on a closed alpha mesh
+// (y = alpha, line Ny-2 is line 0 once more); with rho = 0 on the mesh the axis z voltage is
+// rebuilt from the alpha currents around it.
+struct CylDev {
+    int closed, r0;
+    const float* vv_r0;   // [Nz]
+    const float* vi_r0;   // [Nz]
+};
+
+// DoPostVoltageUpdates: one thread per (rho, z).  Thread (0, z) first sums the axis voltage in
+// the reference's order and writes it to every alpha line (alpha voltages there are zero); every
+// thread then copies the rho and z voltages of alpha line Ny-2 onto line 0.  A thread writes only
+// its own (rho, z) lines, so the threads are independent.
+static __global__ void __launch_bounds__(256) k_cyl_post_v(GridDev g, CylDev c)
+{
+    const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (unsigned long long)g.Nx * g.Nz) return;
+    const unsigned r = (unsigned)(t / g.Nz), z = (unsigned)(t % g.Nz), last = g.Ny - 2;
+    auto off = [&](unsigned n, unsigned x, unsigned a) {
+        return (unsigned long long)n * g.S + ((unsigned long long)x * g.Ny + a) * g.Pz + z;
+    };
+    float* V = g.V;
+    if (c.r0 && r == 0) {
+        float volt = fmul(V[off(2, 0, 0)], c.vv_r0[z]);
+        for (unsigned a = 0; a + 1 < g.Ny; ++a) volt = fadd(volt, fmul(c.vi_r0[z], g.I[off(1, 0, a)]));
+        for (unsigned a = 0; a < g.Ny; ++a) {
+            V[off(1, 0, a)] = 0.0f;
+            V[off(2, 0, a)] = volt;
+        }
+    }
+    V[off(0, r, 0)] = V[off(0, r, last)];
+    V[off(2, r, 0)] = V[off(2, r, last)];
+}
+
+// DoPostCurrentUpdates: the rho and z currents of alpha line 0 onto line Ny-2, one thread per
+// (rho, z) with rho < Nx-1 and z < Nz-1.
+static __global__ void __launch_bounds__(256) k_cyl_post_i(GridDev g)
+{
+    const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nz = g.Nz - 1;
+    if (t >= (unsigned long long)(g.Nx - 1) * nz) return;
+    const unsigned r = (unsigned)(t / nz), z = (unsigned)(t % nz), last = g.Ny - 2;
+    auto off = [&](unsigned n, unsigned a) {
+        return (unsigned long long)n * g.S + ((unsigned long long)r * g.Ny + a) * g.Pz + z;
+    };
+    g.I[off(0, last)] = g.I[off(0, 0)];
+    g.I[off(2, last)] = g.I[off(2, 0)];
+}
+
 static __global__ void k_lumped_rlc(float* __restrict__ V, RlcDev r, const unsigned* __restrict__ numTS)
 {
     const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;

@@ -113,6 +113,13 @@ class EngineBase:
                                 b[4].size, *[_p(x, ct) for x, ct in zip(b, ctypes_of)],
                                 _p(sv, C.c_float), _p(sc, C.c_float), sv.size, int(t.period), int(t.max_delay)),
                      "set_tfsf")
+        cyl = getattr(op, "cylinder", None)
+        if cyl is not None:
+            vv0 = self._a(cyl.vv_r0, np.float32)
+            vi0 = self._a(cyl.vi_r0, np.float32)
+            self._ck(L.set_cylinder(self.h, int(cyl.closed_alpha), int(cyl.r0_included),
+                                    _p(vv0, C.c_float) if vv0.size else None,
+                                    _p(vi0, C.c_float) if vi0.size else None), "set_cylinder")
         r = getattr(op, "rlc", None)
         if r is not None:
             pos = self._a(r.pos, np.uint32)
@@ -141,22 +148,15 @@ class EngineBase:
                      "add_current_probe")
             self._probe_dft(pid.value, p)
             self.iprobe_ids.append(pid.value)
-        fps = list(getattr(op, "fprobes", []) or [])
-        if fps:
-            from .operator import _main_delta, _dual_delta
-            g = op.grid
-            for p in fps:
-                pid = C.c_int(-1)
-                pos = self._a(p.pos, np.uint32)
-                # GetEdgeLength(n, pos) of the main mesh (E) or the dual mesh (H)
-                delta = _main_delta if p.field == 0 else _dual_delta
-                el = self._a([float(delta(np.asarray(g.lines[n], np.float64))[int(p.pos[n])] * g.unit)
-                              for n in range(3)], np.float64)
-                self._ck(L.add_field_probe(self.h, int(p.field), _p(pos, C.c_uint), _p(el, C.c_double),
-                                           float(p.weight), int(p.interval), int(p.start_ts),
-                                           int(min(p.stop_ts, 0xFFFFFFFF)), C.byref(pid)), "add_field_probe")
-                self._probe_dft(pid.value, p)
-                self.fprobe_ids.append(pid.value)
+        for p in list(getattr(op, "fprobes", []) or []):
+            pid = C.c_int(-1)
+            pos = self._a(p.pos, np.uint32)
+            el = self._a(p.el, np.float64)     # GetEdgeLength(n, pos) of the main (E) or dual (H) mesh
+            self._ck(L.add_field_probe(self.h, int(p.field), _p(pos, C.c_uint), _p(el, C.c_double),
+                                       float(p.weight), int(p.interval), int(p.start_ts),
+                                       int(min(p.stop_ts, 0xFFFFFFFF)), C.byref(pid)), "add_field_probe")
+            self._probe_dft(pid.value, p)
+            self.fprobe_ids.append(pid.value)
         td = list(getattr(op, "td_dumps", []) or [])
         if op.dumps or td:
             g = op.grid

@@ -362,6 +362,7 @@ class FieldProbe:
     freqs: list
     start_ts: int = 0
     stop_ts: int = 0xFFFFFFFF
+    el: tuple = ()                # GetEdgeLength(n, pos) of each component (E main, H dual mesh)
 
 
 @dataclass
@@ -416,6 +417,7 @@ class OperatorData:
     rlc: Optional[LumpedRLCTable] = None
     td_dumps: list = field(default_factory=list)
     fprobes: list = field(default_factory=list)
+    cylinder: Optional["CylinderTable"] = None
 
 
 # lumped element types (CSPropLumpedElement::LEtype)
@@ -868,6 +870,10 @@ class Operator:
         return b, dt
 
     # ---- timestep (FDTD/operator.cpp:1956-2030) --------------------------------------------
+    def calc_timestep(self):
+        """Operator::CalcTimestep (FDTD/operator.cpp:1880-1889): the Rennings Var3 timestep."""
+        return self.calc_timestep_var3()
+
     def calc_timestep_var3(self):
         def work(x0, x1):
             h0, h1 = max(x0 - 1, 0), min(x1 + 1, int(self.N[0]))
@@ -1012,7 +1018,7 @@ class Operator:
                 gpu[0].close()
                 raise ValueError("Operator: timestep is zero")
         else:
-            dT = self.calc_timestep_var3()
+            dT = self.calc_timestep()
         dT *= self.ts_factor
         if self.exc.period > 0:
             TS = math.ceil(self.exc.period / dT)
@@ -1043,6 +1049,9 @@ class Operator:
         self._calc_pec()
         self._calc_lumped()
         self._apply_magnetic_bc([b == 1 for b in self.bc])
+        # the cylinder extension is added with the grid (Operator_Cylinder::SetupCSXGrid), before
+        # every other extension, so it is built first
+        cyl = self._build_cylinder()
 
         exc = self._build_excitation()
         # Operator_Ext_TFSF is added right after the excitation extension (openems.cpp:1186-1188)
@@ -1061,8 +1070,20 @@ class Operator:
                             iv=self.iv, exc=exc, upml=upml, mur=mur, lorentz=lorentz, vprobes=vprobes,
                             iprobes=iprobes, dumps=dumps, nyquist=self.exc.GetNyquistNum(),
                             excitation=self.exc, grid=self.grid, tfsf=tfsf, rlc=rlc, td_dumps=self.td_dumps,
-                            fprobes=self.fprobes)
+                            fprobes=self.fprobes, cylinder=cyl)
         return data
+
+    def _build_cylinder(self):
+        """Cartesian meshes have no cylinder extension."""
+        return None
+
+    def _yee_painter(self, kinds):
+        """Property lookup at Yee coordinates (GetYeeCoords + GetPropertyByCoordPriority)."""
+        return _Painter(self.csx, kinds)
+
+    def _mur_painter(self):
+        """Material lookup at the Mur wall's mesh coordinates (operator_ext_mur_abc.cpp:125-160)."""
+        return self._mat
 
     # ---- boundary conditions ---------------------------------------------------------------
     def _apply_electric_bc(self, dirs):
@@ -1192,7 +1213,7 @@ class Operator:
         List order follows the reference's loops: z outer, then y, then x, then the component.
         """
         u = self.unit
-        painter = _Painter(self.csx, EXCITATION)
+        painter = self._yee_painter(EXCITATION)
         vrec, crec = [], []
         if painter.props:
             for n in range(3):
@@ -1213,7 +1234,7 @@ class Operator:
                     wf = prop.params.get("weight")
                     if wf is not None:       # GetWeightedExcitation at the Yee point (drawing units)
                         ex = ex * float(wf[n](float(cs[0][x]), float(cs[1][y]), float(cs[2][z])))
-                    amp = ex * (self.md[n][(x, y, z)[n]] * u)
+                    amp = ex * self._edge_length(n, (x, y, z))
                     if amp != 0:
                         vrec.append((z, y, x, n, amp, int(prop.params["delay"] / self.dT)))
                     if et == 1:
@@ -1230,7 +1251,7 @@ class Operator:
                     et = prop.params["exc_type"]
                     if et not in (2, 3):
                         continue
-                    amp = prop.params["exc_val"][n] * (self.dd[n][(x, y, z)[n]] * u)
+                    amp = prop.params["exc_val"][n] * self._edge_length(n, (x, y, z), dual=True)
                     if amp != 0:
                         crec.append((z, y, x, n, amp, int(prop.params["delay"] / self.dT)))
                     if et == 3:
@@ -1503,7 +1524,7 @@ class Operator:
             cs[ny] = np.array([c_ny])
             cs[nyP] = self.L[nyP]
             cs[nyPP] = self.L[nyPP]
-            m = self._mat.paint(*cs)
+            m = self._mur_painter().paint(*cs)
             m2 = np.moveaxis(m, ny, 0)[0]            # axes now (nyP? ...) -> reorder below
             # moveaxis leaves the remaining axes in increasing order; we need [nyP][nyPP]
             if nyP > nyPP:
@@ -2102,8 +2123,9 @@ class Operator:
                         dim, s, e, _, _ = self.snap_box(lo, hi, dual=pt == 3, method=0)
                         if dim < 0:
                             continue
+                        el = tuple(self._edge_length(n, tuple(int(v) for v in s), dual=pt == 3) for n in range(3))
                         fprobes.append(FieldProbe(prop.name, pt - 2, s, prop.params["weight"], interval,
-                                                  fd_interval, freqs, start_ts, stop_ts))
+                                                  fd_interval, freqs, start_ts, stop_ts, el))
             elif prop.kind == DUMP and prop.params["dump_type"] in (0, 1):
                 # ProcessFieldsTD (openems.cpp:611-690): interval Nyquist/OverSampling
                 field_ = prop.params["dump_type"]

@@ -140,6 +140,9 @@ typedef struct oems_ref_engine {
     int *rlc_dir;
     float *rlc_c; /* [9][n]: ilv, i2v, vv2, vj1, vj2, vvd, ib0, b1, b2 */
     float *rlc_il, *rlc_vd[3], *rlc_j[3];
+    /* Engine_Ext_Cylinder: closed alpha mesh, rho = 0 on it, the axis coefficients [Nz] */
+    int cyl_closed, cyl_r0;
+    float *cyl_vv_r0, *cyl_vi_r0;
     /* extensions */
     upml_t upml[MAX_UPML];
     int nupml;
@@ -260,6 +263,7 @@ void oems_ref_destroy(eng_t *e)
     free(e->tf_v_idx); free(e->tf_i_idx); free(e->tf_v_delay); free(e->tf_i_delay); free(e->tf_lut);
     free(e->tf_v_dir); free(e->tf_i_dir); free(e->tf_v_delta); free(e->tf_i_delta);
     free(e->tf_v_amp); free(e->tf_i_amp); free(e->tf_sig_v); free(e->tf_sig_i);
+    free(e->cyl_vv_r0); free(e->cyl_vi_r0);
     free(e->rlc_pos); free(e->rlc_dir); free(e->rlc_c); free(e->rlc_il);
     for (int q = 0; q < 3; ++q) { free(e->rlc_vd[q]); free(e->rlc_j[q]); }
     for (int r = 0; r < e->nupml; ++r) {
@@ -451,6 +455,23 @@ static void *dupmem(const void *src, size_t bytes)
     if (bytes)
         memcpy(p, src, bytes);
     return p;
+}
+
+/* Operator_Ext_Cylinder's tables (FDTD/extensions/operator_ext_cylinder.cpp:44-112): a closed
+ * alpha mesh and, with rho = 0 on it, vv_r0/vi_r0 for every z line */
+int oems_ref_set_cylinder(eng_t *e, int closed_alpha, int r0_included, const float *vv_r0, const float *vi_r0)
+{
+    if (!e || (r0_included && (!closed_alpha || !vv_r0 || !vi_r0)) || e->N[1] < 3)
+        return ERR_ARG;
+    e->cyl_closed = closed_alpha != 0;
+    e->cyl_r0 = r0_included != 0;
+    free(e->cyl_vv_r0); free(e->cyl_vi_r0);
+    e->cyl_vv_r0 = e->cyl_vi_r0 = NULL;
+    if (e->cyl_r0) {
+        e->cyl_vv_r0 = (float *)dupmem(vv_r0, 4 * (size_t)e->N[2]);
+        e->cyl_vi_r0 = (float *)dupmem(vi_r0, 4 * (size_t)e->N[2]);
+    }
+    return OK;
 }
 
 int oems_ref_set_tfsf(eng_t *e, unsigned nV, const unsigned *v_idx, const unsigned short *v_dir,
@@ -1429,6 +1450,47 @@ static void process_all(eng_t *e)
 /* ------------------------------------------------------------------------------------------ */
 /* stepping */
 
+/* Engine_Ext_Cylinder::DoPostVoltageUpdates (FDTD/extensions/engine_ext_cylinder.cpp:45-84):
+ * the axis z voltage from the alpha currents around it, then the closed alpha seam */
+static void cyl_post_volt(eng_t *e)
+{
+    if (!e->cyl_closed)
+        return;
+    const unsigned Nr = e->N[0], Na = e->N[1], Nz = e->N[2], last = Na - 2;
+    if (e->cyl_r0) {
+        for (unsigned z = 0; z < Nz; ++z) {
+            float volt = GETV(e, 2, 0, 0, z) * e->cyl_vv_r0[z];
+            for (unsigned a = 0; a < Na - 1; ++a)
+                volt += e->cyl_vi_r0[z] * GETI(e, 1, 0, a, z);
+            *fptr(e, 0, 2, 0, 0, z) = volt;
+        }
+        for (unsigned a = 0; a < Na; ++a)
+            for (unsigned z = 0; z < Nz; ++z) {
+                *fptr(e, 0, 1, 0, a, z) = 0;   /* no alpha voltage on the axis */
+                *fptr(e, 0, 2, 0, a, z) = GETV(e, 2, 0, 0, z);
+            }
+    }
+    for (unsigned r = 0; r < Nr; ++r)
+        for (unsigned z = 0; z < Nz; ++z) {
+            *fptr(e, 0, 0, r, 0, z) = GETV(e, 0, r, last, z);
+            *fptr(e, 0, 2, r, 0, z) = GETV(e, 2, r, last, z);
+        }
+}
+
+/* Engine_Ext_Cylinder::DoPostCurrentUpdates (:86-101): the tangential currents of alpha line 0
+ * onto line N-2 */
+static void cyl_post_curr(eng_t *e)
+{
+    if (!e->cyl_closed)
+        return;
+    const unsigned Nr = e->N[0], Na = e->N[1], Nz = e->N[2], last = Na - 2;
+    for (unsigned r = 0; r + 1 < Nr; ++r)
+        for (unsigned z = 0; z + 1 < Nz; ++z) {
+            *fptr(e, 1, 0, r, last, z) = GETI(e, 0, r, 0, z);
+            *fptr(e, 1, 2, r, last, z) = GETI(e, 2, r, 0, z);
+        }
+}
+
 /* extension phases in reference order; thread 0 runs the non-threaded extensions */
 static void pre_volt(eng_t *e)
 {
@@ -1442,7 +1504,8 @@ static void pre_volt(eng_t *e)
 
 static void post_volt_apply(eng_t *e)
 {
-    /* post hooks in priority order: UPML (run by the caller), TFSF (5e4), Mur (0) */
+    /* post hooks in priority order: UPML (run by the caller), cylinder (1e5), TFSF (5e4), Mur (0) */
+    cyl_post_volt(e);
     tfsf_apply(e, 0);
     for (int w = e->nmur - 1; w >= 0; --w)
         mur_post(e, &e->mur[w]);
@@ -1464,6 +1527,7 @@ static void pre_curr(eng_t *e)
 
 static void post_curr_apply(eng_t *e)
 {
+    cyl_post_curr(e);
     tfsf_apply(e, 1);
     for (int o = 0; o < e->nlor; ++o)
         lorentz_apply(e, &e->lor[o], 1);

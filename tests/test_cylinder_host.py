@@ -1,0 +1,149 @@
+"""CPU tests of the cylindrical-coordinate operator (Operator_Cylinder + Operator_Ext_Cylinder) and
+of the cylinder engine hooks (Engine_Ext_Cylinder) in the oracle.
+
+The reference has no test of its cylindrical engine; it is pinned here by
+* known answers of the equivalent circuit in vacuum: the capacitance of rho, alpha and z edges
+  from the cylindrical edge lengths and areas (alpha edges rho*dalpha, z faces annular sectors),
+  and the closed alpha mesh (line a1 + 2*pi appended, the last angle set to a0 + 2*pi);
+* the structural invariants the hooks keep: the alpha seam (voltages of line 0 equal line N-2,
+  currents of line N-2 equal line 0) and the axis (no alpha voltage, one z voltage per height);
+* two physics contracts: the coax example of the reference in cylindrical coordinates
+  (matlab/examples/waveguide/Coax_CylinderCoords.m) must give Z0 = eta0/(2 pi) ln(230/100) within
+  the +3/-1 % of the reference's Cartesian coax test, and a pillbox cavity with rho = 0 on the
+  mesh must ring at the TM010 frequency 2.4048 c/(2 pi a) within the -0.25/+0 % the reference's
+  cavity test allows for TM modes;
+* basic vs multithreaded oracle equality, bit for bit.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from openems_gb300 import configs
+from openems_gb300.excitation import Excitation
+from openems_gb300.operator import EPS0, MUE0, Grid, Structure
+from openems_gb300.operator_cyl import OperatorCylinder
+from oracle.oracle import OracleEngine
+
+from helpers import bits_equal
+
+C0 = 299792458.0
+THREADS = 4
+
+
+def _vacuum(lines, bc=(0,) * 6):
+    exc = Excitation()
+    exc.SetupGaussianPulse(3e9, 2e9)
+    return OperatorCylinder(Structure(), Grid(lines, unit=1e-3), exc, bc=bc)
+
+
+def test_closed_alpha_mesh_and_flags():
+    al = np.linspace(0.0, 2 * np.pi, 13)
+    op = _vacuum([np.arange(0.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)])
+    a = op.L[1]
+    assert a.size == 14 and a[-2] == 2 * np.pi + al[0] and a[-1] == 2 * np.pi + al[1]
+    assert op.closed_alpha and op.r0_included
+    op2 = _vacuum([np.arange(5.0, 20.1, 2.0), np.linspace(0.0, 1.0, 6), np.arange(0.0, 10.1, 2.0)])
+    assert not op2.closed_alpha and not op2.r0_included and op2.L[1].size == 6
+    with pytest.raises(ValueError):
+        _vacuum([np.arange(5.0, 20.1, 2.0), np.linspace(0.0, 7.0, 6), np.arange(0.0, 10.1, 2.0)])
+    # Mur walls the reference rejects in cylindrical coordinates are dropped: rho_min on a closed
+    # mesh and both alpha walls; rho_max and z walls stay
+    op3 = _vacuum([np.arange(5.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(2,) * 6)
+    assert op3.dropped_mur == [0, 2, 3] and op3.bc == [0, 2, 0, 0, 2, 2]
+    with pytest.raises(ValueError):
+        _vacuum([np.arange(5.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(0, 0, 0, 0, 3, 3))
+
+
+def test_equivalent_circuit_known_answers():
+    rs = np.array([4.0, 5.0, 6.5, 8.0, 10.0, 12.0])
+    al = np.linspace(0.0, 2 * np.pi, 17)
+    zs = np.array([0.0, 1.5, 3.0, 5.0, 6.0])
+    op = _vacuum([rs, al, zs])
+    op.calc_ec()
+    u = 1e-3
+    a = op.L[1]
+    dl_r = 0.5 * (rs[:-1] + rs[1:])
+    for (i, j, k) in [(2, 3, 2), (1, 7, 1), (3, 12, 2)]:
+        dr, dz, da = rs[i + 1] - rs[i], zs[k + 1] - zs[k], a[j + 1] - a[j]
+        # dual deltas: distances between neighbouring dual lines
+        dr_d = dl_r[i] - dl_r[i - 1]
+        dz_d = 0.5 * (zs[k + 1] - zs[k - 1])
+        da_d = 0.5 * (a[j + 1] - a[j - 1])
+        # rho edge: area = (rho_dual * dalpha_dual) * dz_dual, length = drho
+        want = EPS0 * (da_d * u * dl_r[i]) * (dz_d * u) / (dr * u)
+        assert op.EC_C[0, i, j, k] == pytest.approx(want, rel=2e-6)
+        # alpha edge: length = rho * dalpha, area = drho_dual * dz_dual
+        want = EPS0 * (dr_d * u) * (dz_d * u) / (da * u * rs[i])
+        assert op.EC_C[1, i, j, k] == pytest.approx(want, rel=2e-6)
+        # z edge: the annular sector between the dual radii r1..r2 over the main dalpha
+        r2, r1 = dl_r[i] * u, dl_r[i] * u - dr_d * u
+        want = EPS0 * (da / 2 * (r2 ** 2 - r1 ** 2)) / (dz * u)
+        assert op.EC_C[2, i, j, k] == pytest.approx(want, rel=2e-6)
+        # inductance of an alpha edge: mu0 * (drho * dz) / (rho_dual * dalpha_dual)
+        want = MUE0 * (dr * u) * (dz * u) / (da_d * u * dl_r[i])
+        assert op.EC_L[1, i, j, k] == pytest.approx(want, rel=2e-6)
+
+
+def _invariants(e, op):
+    V, I = e.read_field(0), e.read_field(1)
+    assert bits_equal(V[0][:, 0, :], V[0][:, -2, :]) and bits_equal(V[2][:, 0, :], V[2][:, -2, :])
+    assert bits_equal(I[0][:-1, -2, :-1], I[0][:-1, 0, :-1]) and bits_equal(I[2][:-1, -2, :-1], I[2][:-1, 0, :-1])
+    if op.cylinder.r0_included:
+        assert not V[1][0].any()
+        assert bits_equal(V[2][0], np.broadcast_to(V[2][0][:1], V[2][0].shape))
+
+
+def test_coax_impedance_in_cylindrical_coordinates():
+    steps = 5000
+    op = configs.coax_cyl(steps=steps)
+    assert op.cylinder.closed_alpha and not op.cylinder.r0_included
+    e = OracleEngine(op, steps, threads=THREADS)
+    e.IterateTS(steps)
+    _invariants(e, op)
+    u = e.probe_series(e.vprobe_ids[0])
+    i = e.probe_series(e.iprobe_ids[0])
+    nfft = 1 << int(math.ceil(math.log2(len(u))))
+    f = np.fft.rfftfreq(nfft, op.dt)
+    sel = f <= 1e9
+    Z = np.abs(np.fft.rfft(u, nfft)[sel] / np.fft.rfft(i, nfft)[sel])
+    Z0 = math.sqrt(MUE0 / EPS0) * math.log(230 / 100) / (2 * math.pi)
+    assert sel.sum() > 50
+    assert (Z <= Z0 * 1.03).all() and (Z >= Z0 * 0.99).all(), (Z.min() / Z0, Z.max() / Z0)
+
+
+def test_pillbox_tm010_resonance_with_the_axis():
+    steps = 20000
+    op = configs.cavity_cyl(steps=steps)
+    assert op.cylinder.r0_included
+    e = OracleEngine(op, steps, threads=THREADS)
+    e.IterateTS(steps)
+    _invariants(e, op)
+    u = e.probe_series(e.vprobe_ids[0])[3000:]
+    u = u - u.mean()
+    nf = 1 << 22
+    spec = np.abs(np.fft.rfft(u * np.hanning(len(u)), nf))
+    f = np.fft.rfftfreq(nf, op.dt)
+    sel = (f > 1e9) & (f < 6e9)
+    fp = f[sel][np.argmax(spec[sel])]
+    f010 = 2.404825557695773 * C0 / (2 * math.pi * 0.05)
+    assert -2.5e-3 <= fp / f010 - 1 <= 0.0, fp / f010 - 1
+
+
+@pytest.mark.parametrize("name,fn,steps", [
+    ("coax", lambda: configs.coax_cyl(steps=300, length=400.0), 300),
+    ("cavity", lambda: configs.cavity_cyl(steps=600), 600),
+    ("cavity_off_axis_probe", lambda: configs.cavity_cyl(steps=400, n_alpha=25, probe_r=10.0), 400),
+])
+def test_basic_equals_multithreaded(name, fn, steps):
+    op = fn()
+    a = OracleEngine(op, steps)
+    b = OracleEngine(op, steps, threads=3)
+    for n in (steps // 3, steps - steps // 3):
+        a.IterateTS(n)
+        b.IterateTS(n)
+    for w in (0, 1):
+        assert bits_equal(a.read_field(w), b.read_field(w)), (name, w)
+    for pid in a.vprobe_ids + a.iprobe_ids:
+        assert np.array_equal(a.probe_series(pid), b.probe_series(pid), equal_nan=True)
+    _invariants(a, op)

@@ -59,6 +59,9 @@ CASES = [
     ("conducting_sheet_mur", lambda: configs.conducting_sheet(steps=240), 240),
     ("conducting_sheet_upml_dispersive", lambda: configs.conducting_sheet(bc=(3,) * 6, dispersive=True, steps=200),
      200),
+    ("coax_cyl_closed_alpha_mur", lambda: configs.coax_cyl(steps=200, length=400.0), 200),
+    ("cavity_cyl_axis", lambda: configs.cavity_cyl(steps=400), 400),
+    ("cavity_cyl_off_axis", lambda: configs.cavity_cyl(steps=300, n_alpha=25, probe_r=10.0), 300),
 ]
 
 
@@ -196,6 +199,40 @@ def test_coax_reference_contract_on_gpu(cuda_lib):
     Z0 = coax_z0()
     assert f.size > 50
     assert (Z <= Z0 * 1.03).all() and (Z >= Z0 * 0.99).all(), (Z.min() / Z0, Z.max() / Z0)
+
+
+def test_cylinder_contracts_on_gpu(cuda_lib):
+    """The cylindrical-coordinate contracts on the CUDA engine: the coax example's |U/I| within
+    +3/-1 % of Z0, and the pillbox TM010 resonance within -0.25/+0 %, both with probe series
+    bit-identical to the multithreaded oracle's."""
+    import math
+    from openems_gb300.operator import EPS0, MUE0
+    for fn, steps in ((configs.coax_cyl, 5000), (configs.cavity_cyl, 20000)):
+        op = fn(steps=steps)
+        g = Engine_CUDA(op, steps)
+        g.IterateTS(steps)
+        g.sync()
+        r = OracleEngine(op, steps, threads=4)
+        r.IterateTS(steps)
+        for pid in g.vprobe_ids + g.iprobe_ids:
+            assert bits_equal(g.probe_series(pid), r.probe_series(pid)), (fn.__name__, pid)
+        u = g.probe_series(g.vprobe_ids[0])
+        if fn is configs.coax_cyl:
+            i = g.probe_series(g.iprobe_ids[0])
+            nfft = 1 << int(math.ceil(math.log2(len(u))))
+            f = np.fft.rfftfreq(nfft, op.dt)
+            sel = f <= 1e9
+            Z = np.abs(np.fft.rfft(u, nfft)[sel] / np.fft.rfft(i, nfft)[sel])
+            Z0 = math.sqrt(MUE0 / EPS0) * math.log(230 / 100) / (2 * math.pi)
+            assert (Z <= Z0 * 1.03).all() and (Z >= Z0 * 0.99).all()
+        else:
+            u = u[3000:] - u[3000:].mean()
+            nf = 1 << 22
+            spec = np.abs(np.fft.rfft(u * np.hanning(len(u)), nf))
+            f = np.fft.rfftfreq(nf, op.dt)
+            sel = (f > 1e9) & (f < 6e9)
+            f010 = 2.404825557695773 * 299792458.0 / (2 * math.pi * 0.05)
+            assert -2.5e-3 <= f[sel][np.argmax(spec[sel])] / f010 - 1 <= 0.0
 
 
 def test_against_committed_fixtures(cuda_lib):
