@@ -1077,6 +1077,15 @@ class Operator:
         """Cartesian meshes have no cylinder extension."""
         return None
 
+    def _edge_geometry(self, n, pos_axes):
+        """GetEdgeLength(n, pos), GetEdgeArea(n, pos) and their dual versions over the box of
+        positions pos_axes (broadcastable arrays, metres)."""
+        a, p, pp = _axes(n)
+        u = self.unit
+        De, Ap, App = _bcast(n, self.md[a][pos_axes[a]] * u, self.dd[p][pos_axes[p]] * u, self.dd[pp][pos_axes[pp]] * u)
+        Dh, Bp, Bpp = _bcast(n, self.dd[a][pos_axes[a]] * u, self.md[p][pos_axes[p]] * u, self.md[pp][pos_axes[pp]] * u)
+        return De, Ap * App, Dh, Bp * Bpp
+
     def _yee_painter(self, kinds):
         """Property lookup at Yee coordinates (GetYeeCoords + GetPropertyByCoordPriority)."""
         return _Painter(self.csx, kinds)
@@ -1660,8 +1669,7 @@ class Operator:
                 op_ii = self.ii[n][sl]
                 op_iv = self.iv[n][sl]
                 # GetEdgeLength(n,pos)/GetEdgeArea(n,pos) and their dual versions
-                De, Ap, App = _bcast(n, self.md[a][pos_axes[a]] * u, self.dd[p][pos_axes[p]] * u, self.dd[pp][pos_axes[pp]] * u)
-                Dh, Bp, Bpp = _bcast(n, self.dd[a][pos_axes[a]] * u, self.md[p][pos_axes[p]] * u, self.md[pp][pos_axes[pp]] * u)
+                De, Ae, Dh, Ah = self._edge_geometry(n, pos_axes)
                 kvp = np.broadcast_to(KV[p], shape)
                 kvpp = np.broadcast_to(KV[pp], shape)
                 kvn = np.broadcast_to(KV[a], shape)
@@ -1673,7 +1681,7 @@ class Operator:
                 not_pec = (op_vv + op_vi) != 0
                 mod = act_v & not_pec
                 new_vv = ((2 * EPS0 - kvp * dT) / (2 * EPS0 + kvp * dT)).astype(self.ft)
-                new_vi = ((2 * EPS0 * dT) / (2 * EPS0 + kvp * dT) * De / (Ap * App)).astype(self.ft)
+                new_vi = ((2 * EPS0 * dT) / (2 * EPS0 + kvp * dT) * De / Ae).astype(self.ft)
                 e_vv = ((2 * EPS0 - kvpp * dT) / (2 * EPS0 + kvpp * dT)).astype(self.ft)
                 e_vvfn = ((2 * EPS0 + kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(self.ft)
                 e_vvfo = ((2 * EPS0 - kvn * dT) / (2 * EPS0 + kvpp * dT) / eff_eps).astype(self.ft)
@@ -1687,7 +1695,7 @@ class Operator:
                 not_pmc = (op_ii + op_iv) != 0
                 mod = act_i & not_pmc
                 new_ii = ((2 * EPS0 - kip * dT) / (2 * EPS0 + kip * dT)).astype(self.ft)
-                new_iv = ((2 * EPS0 * dT) / (2 * EPS0 + kip * dT) * Dh / (Bp * Bpp)).astype(self.ft)
+                new_iv = ((2 * EPS0 * dT) / (2 * EPS0 + kip * dT) * Dh / Ah).astype(self.ft)
                 e_ii = ((2 * EPS0 - kipp * dT) / (2 * EPS0 + kipp * dT)).astype(self.ft)
                 e_iifn = ((2 * EPS0 + kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(self.ft)
                 e_iifo = ((2 * EPS0 - kin * dT) / (2 * EPS0 + kipp * dT) / eff_mue).astype(self.ft)

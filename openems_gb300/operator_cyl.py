@@ -18,9 +18,10 @@ alpha edges are rho times their angle (GetEdgeLength, :204-210), z faces are ann
 
 Built here: materials (eps, kappa, mue, sigma), metal (PEC), soft/hard and weighted excitations,
 Mur walls that the reference accepts in cylindrical coordinates (operator_ext_mur_abc.cpp:47-54;
-the others are dropped as there, leaving PEC), voltage, current and field probes.  Not built for
-this mesh: UPML, TFSF (rejected by the reference too), lumped elements, dispersive materials and
-conducting sheets, field dumps, and alpha fitting of coordinates outside the mesh's alpha range.
+the others are dropped as there, leaving PEC), UPML on the rho and z walls, voltage, current and
+field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the reference too),
+lumped elements, dispersive materials and conducting sheets, field dumps, and alpha fitting of
+coordinates outside the mesh's alpha range.
 """
 from __future__ import annotations
 
@@ -83,8 +84,12 @@ class OperatorCylinder(Operator):
         # on an open mesh rho = 0 needs no special treatment (E_alpha/E_z there are PEC anyway)
         self.r0_included = bool(lines[0][0] == 0.0 and closed)
         bc = [int(b) for b in bc]
-        if 3 in bc:
-            raise ValueError("OperatorCylinder: UPML in cylindrical coordinates is not built")
+        # UPML on the rho and z walls; an alpha PML would grade with rho (operator_ext_upml.cpp:
+        # 280-284) and is not built, nor is a PML at rho = 0
+        if bc[2] == 3 or bc[3] == 3:
+            raise ValueError("OperatorCylinder: a UPML on the alpha walls is not built")
+        if bc[0] == 3 and lines[0][0] == 0.0:
+            raise ValueError("OperatorCylinder: no UPML at rho = 0")
         # Mur walls the reference rejects in cylindrical coordinates are dropped (PEC remains)
         self.dropped_mur = []
         for w in range(6):
@@ -257,14 +262,28 @@ class OperatorCylinder(Operator):
     def _ec_double(self):
         P = self._grid_pos()
         out = []
+        self._eff = {}
         for n in range(3):
-            e0, e1, e2, e3 = self.eff_mat(n)
+            e0, e1, e2, e3 = self._eff[n] = self.eff_mat(n)
             D, A = self._cyl_len(n, P, False), self._edge_area(n, P, False)
             Dh, Ah = self._cyl_len(n, P, True), self._edge_area(n, P, True)
             with np.errstate(divide="ignore", invalid="ignore"):
                 out.append((np.where(D != 0, e0 * A / D, 0.0), np.where(D != 0, e1 * A / D, 0.0),
                             np.where(Dh != 0, e2 * Ah / Dh, 0.0), np.where(Dh != 0, e3 * Ah / Dh, 0.0)))
         return out
+
+    def eff_region(self, n, start, nl):
+        """The effective material of direction n on the box start..start+nl (from the full mesh)."""
+        if not hasattr(self, "_eff"):
+            self._eff = {k: self.eff_mat(k) for k in range(3)}
+        sl = tuple(slice(int(start[a]), int(start[a] + nl[a])) for a in range(3))
+        return [x[sl] for x in self._eff[n]]
+
+    def _edge_geometry(self, n, pos_axes):
+        P = [np.asarray(pos_axes[0]).reshape(-1, 1, 1), np.asarray(pos_axes[1]).reshape(1, -1, 1),
+             np.asarray(pos_axes[2]).reshape(1, 1, -1)]
+        return (self._cyl_len(n, P, False), self._edge_area(n, P, False),
+                self._cyl_len(n, P, True), self._edge_area(n, P, True))
 
     def calc_ec(self):
         ec = self._ec_double()

@@ -8,8 +8,8 @@ The reference has no test of its cylindrical engine; it is pinned here by
 * the structural invariants the hooks keep: the alpha seam (voltages of line 0 equal line N-2,
   currents of line N-2 equal line 0) and the axis (no alpha voltage, one z voltage per height);
 * two physics contracts: the coax example of the reference in cylindrical coordinates
-  (matlab/examples/waveguide/Coax_CylinderCoords.m) must give Z0 = eta0/(2 pi) ln(230/100) within
-  the +3/-1 % of the reference's Cartesian coax test, and a pillbox cavity with rho = 0 on the
+  (matlab/examples/waveguide/Coax_CylinderCoords.m, with its Mur or its PML_8 far end) must give
+  Z0 = eta0/(2 pi) ln(230/100) within the +3/-1 % of the reference's Cartesian coax test, and a pillbox cavity with rho = 0 on the
   mesh must ring at the TM010 frequency 2.4048 c/(2 pi a) within the -0.25/+0 % the reference's
   cavity test allows for TM modes;
 * basic vs multithreaded oracle equality, bit for bit.
@@ -51,8 +51,12 @@ def test_closed_alpha_mesh_and_flags():
     # mesh and both alpha walls; rho_max and z walls stay
     op3 = _vacuum([np.arange(5.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(2,) * 6)
     assert op3.dropped_mur == [0, 2, 3] and op3.bc == [0, 2, 0, 0, 2, 2]
+    # UPML on the rho and z walls is built; on the alpha walls or at rho = 0 it is not
+    for bc in ((0, 0, 3, 0, 0, 0), (0, 0, 0, 3, 0, 0)):
+        with pytest.raises(ValueError):
+            _vacuum([np.arange(5.0, 20.1, 2.0), np.linspace(0.0, 1.0, 12), np.arange(0.0, 10.1, 2.0)], bc=bc)
     with pytest.raises(ValueError):
-        _vacuum([np.arange(5.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(0, 0, 0, 0, 3, 3))
+        _vacuum([np.arange(0.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(3, 0, 0, 0, 0, 0))
 
 
 def test_equivalent_circuit_known_answers():
@@ -94,9 +98,11 @@ def _invariants(e, op):
         assert bits_equal(V[2][0], np.broadcast_to(V[2][0][:1], V[2][0].shape))
 
 
-def test_coax_impedance_in_cylindrical_coordinates():
+@pytest.mark.parametrize("pml", [False, True])
+def test_coax_impedance_in_cylindrical_coordinates(pml):
     steps = 5000
-    op = configs.coax_cyl(steps=steps)
+    op = configs.coax_cyl(steps=steps, pml=pml)
+    assert len(op.upml) == int(pml) and len(op.mur) == 1 - int(pml)
     assert op.cylinder.closed_alpha and not op.cylinder.r0_included
     e = OracleEngine(op, steps, threads=THREADS)
     e.IterateTS(steps)
@@ -132,6 +138,7 @@ def test_pillbox_tm010_resonance_with_the_axis():
 
 @pytest.mark.parametrize("name,fn,steps", [
     ("coax", lambda: configs.coax_cyl(steps=300, length=400.0), 300),
+    ("coax_upml", lambda: configs.coax_cyl(steps=300, length=400.0, pml=True), 300),
     ("cavity", lambda: configs.cavity_cyl(steps=600), 600),
     ("cavity_off_axis_probe", lambda: configs.cavity_cyl(steps=400, n_alpha=25, probe_r=10.0), 400),
 ])
