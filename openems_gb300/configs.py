@@ -478,11 +478,12 @@ def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False):
     return op.build(steps)
 
 
-def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe_r=0.0):
+def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe_r=0.0, dispersive=False):
     """A pillbox cavity in cylindrical coordinates with rho = 0 on the mesh: radius 50 mm, height
     20 mm, PEC walls, a 2.5 mm rho/z mesh and 10 degree alpha steps (a closed mesh), a soft Ez
     point source off the axis (f0 3 GHz, fc 2 GHz) and an Ez voltage probe at ``probe_r`` (on the
-    axis by default, where the TM010 field is largest and the axis hook computes it)."""
+    axis by default, where the TM010 field is largest and the axis hook computes it).
+    ``dispersive``: a Drude rod on the axis and a Lorentz sector across the alpha seam."""
     from .operator_cyl import OperatorCylinder
     rs = np.arange(0.0, radius + 0.5 * res, res)
     al = np.linspace(0.0, 2 * np.pi, n_alpha)
@@ -495,6 +496,13 @@ def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe
     rs_src = rs[len(rs) // 3]
     csx.AddExcitation("src", 0, [0, 0, 1.0]).AddBox([rs_src, al[3], zs[k]], [rs_src, al[3], zs[k + 1]])
     csx.AddProbe("uz", 0, interval=1).AddBox([probe_r, 0.0, zs[1]], [probe_r, 0.0, zs[-2]])
+    if dispersive:
+        csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[4e9], eps_relax_time=[1e-9]).AddBox(
+            [0.0, 0.0, zs[2]], [3 * res, 2 * np.pi, zs[-3]])
+        csx.AddLorentzMaterial("lor", epsilon=2.0, eps_plasma_freq=[6e9], eps_relax_time=[2e-9],
+                               eps_lor_pole_freq=[3e9]).AddBox([0.5 * radius, al[-4], zs[1]], [0.8 * radius, 2 * np.pi, zs[-2]])
+        csx.AddLorentzMaterial("lor2", epsilon=2.0, eps_plasma_freq=[6e9], eps_relax_time=[2e-9],
+                               eps_lor_pole_freq=[3e9]).AddBox([0.5 * radius, 0.0, zs[1]], [0.8 * radius, al[3], zs[-2]])
     op = OperatorCylinder(csx, g, exc, bc=(0,) * 6)
     return op.build(steps)
 

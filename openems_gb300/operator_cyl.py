@@ -18,9 +18,10 @@ alpha edges are rho times their angle (GetEdgeLength, :204-210), z faces are ann
 
 Built here: materials (eps, kappa, mue, sigma), metal (PEC), soft/hard and weighted excitations,
 Mur walls that the reference accepts in cylindrical coordinates (operator_ext_mur_abc.cpp:47-54;
-the others are dropped as there, leaving PEC), UPML on the rho and z walls, voltage, current and
-field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the reference too),
-lumped elements, dispersive materials and conducting sheets, field dumps, and alpha fitting of
+the others are dropped as there, leaving PEC), UPML on the rho and z walls, Drude/Lorentz
+materials (their tables read only the equivalent circuit, which carries the geometry), voltage,
+current and field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the
+reference too), lumped elements and conducting sheets, field dumps, and alpha fitting of
 coordinates outside the mesh's alpha range.
 """
 from __future__ import annotations
@@ -381,8 +382,6 @@ class OperatorCylinder(Operator):
         if device not in (None, "cpu"):
             raise ValueError("OperatorCylinder: the operator is built on the host")
         data = super().build(num_ts, device="cpu")
-        if data.lorentz:
-            raise ValueError("OperatorCylinder: dispersive materials are not built in cylindrical coordinates")
         data.closed_alpha = self.closed_alpha
         data.r0_included = self.r0_included
         return data

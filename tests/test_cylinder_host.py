@@ -91,7 +91,11 @@ def test_equivalent_circuit_known_answers():
 
 def _invariants(e, op):
     V, I = e.read_field(0), e.read_field(1)
-    assert bits_equal(V[0][:, 0, :], V[0][:, -2, :]) and bits_equal(V[2][:, 0, :], V[2][:, -2, :])
+    # the voltage seam holds after the cylinder's post hook; an apply hook that runs after it
+    # (a dispersive material on line N-2; line 0 has no ADE, its vi being zero there) breaks it
+    # until the next step's copy, in the reference's order as here
+    if not op.lorentz:
+        assert bits_equal(V[0][:, 0, :], V[0][:, -2, :]) and bits_equal(V[2][:, 0, :], V[2][:, -2, :])
     assert bits_equal(I[0][:-1, -2, :-1], I[0][:-1, 0, :-1]) and bits_equal(I[2][:-1, -2, :-1], I[2][:-1, 0, :-1])
     if op.cylinder.r0_included:
         assert not V[1][0].any()
@@ -141,6 +145,7 @@ def test_pillbox_tm010_resonance_with_the_axis():
     ("coax_upml", lambda: configs.coax_cyl(steps=300, length=400.0, pml=True), 300),
     ("cavity", lambda: configs.cavity_cyl(steps=600), 600),
     ("cavity_off_axis_probe", lambda: configs.cavity_cyl(steps=400, n_alpha=25, probe_r=10.0), 400),
+    ("cavity_dispersive", lambda: configs.cavity_cyl(steps=400, dispersive=True), 400),
 ])
 def test_basic_equals_multithreaded(name, fn, steps):
     op = fn()
