@@ -449,14 +449,15 @@ def fieldprobes(half=8, steps=600, freqs=(5e8,), interval=0):
     return data
 
 
-def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False):
+def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=None):
     """The reference's coax example in cylindrical coordinates
     (matlab/examples/waveguide/Coax_CylinderCoords.m:25-123): rho from the inner radius 100 to the
     outer radius 230 on a 10 mm mesh, 71 alpha lines over 2*pi (a closed mesh), z over 1000 mm; PEC
     on every wall but Mur at the far end; a radial soft excitation weighted 1/rho on the z = 0 plane
     (f0 = fc = 0.5 GHz); half way down, a voltage probe across the gap at alpha = 0 and a current
     loop around the inner conductor on the dual mesh (one full turn of alpha).  ``pml``: a PML_8 at
-    the far end instead of Mur (the example's use_pml option)."""
+    the far end instead of Mur (the example's use_pml option).  ``load``: a radial lumped resistor
+    of that many ohms over the whole far-end wall (one parallel RC element), PEC behind it."""
     from .operator_cyl import OperatorCylinder
     r_i, r_a = 100.0, 230.0
     rs = np.arange(r_i, r_a + 0.5 * res, res)
@@ -474,7 +475,10 @@ def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False):
     a1 = al[1]
     # the loop starts below the mesh (no inner side) and runs over dual alpha lines 0 .. N-2
     csx.AddProbe("it1", 1, norm_dir=2, interval=1).AddBox([0.0, 0.5 * a1, zm], [mid, 2 * np.pi + 0.5 * a1, zm])
-    op = OperatorCylinder(csx, g, exc, bc=(0, 0, 0, 0, 0, 3 if pml else 2), pml_size=(8,) * 6)
+    if load is not None:
+        csx.AddLumpedElement("load", ny=0, R=float(load), caps=False).AddBox([r_i, al[0], zs[-1]], [r_a, al[-1], zs[-1]])
+    far = 0 if load is not None else (3 if pml else 2)
+    op = OperatorCylinder(csx, g, exc, bc=(0, 0, 0, 0, 0, far), pml_size=(8,) * 6)
     return op.build(steps)
 
 

@@ -1077,6 +1077,14 @@ class Operator:
         """Cartesian meshes have no cylinder extension."""
         return None
 
+    def _area_over_length(self, ny, pos):
+        """GetEdgeArea(ny, pos) / GetEdgeLength(ny, pos) of one edge; the area is the product of
+        the two node widths (GetNodeArea, FDTD/operator.cpp:235-240)."""
+        u = self.unit
+        nyP, nyPP = (ny + 1) % 3, (ny + 2) % 3
+        area = (self.dd[nyP][pos[nyP]] * u) * (self.dd[nyPP][pos[nyPP]] * u)
+        return area / (self.md[ny][pos[ny]] * u)
+
     def _edge_geometry(self, n, pos_axes):
         """GetEdgeLength(n, pos), GetEdgeArea(n, pos) and their dual versions over the box of
         positions pos_axes (broadcastable arrays, metres)."""
@@ -1168,10 +1176,8 @@ class Operator:
                 dim, s, e, _, _ = self.snap_box(lo, hi, dual=False, method=0)
                 if dim <= 0 or s[ny] == e[ny]:
                     continue
-                # edge area / edge length per edge (GetEdgeArea(ny,pos)/GetEdgeLength(ny,pos))
                 def gc(pos):
-                    area = self.dd[nyP][pos[nyP]] * u * self.dd[nyPP][pos[nyPP]] * u
-                    return area / (self.md[ny][pos[ny]] * u)
+                    return self._area_over_length(ny, pos)
                 unitGC = 0.0
                 pos = [0, 0, 0]
                 for pos[ny] in range(s[ny], e[ny]):

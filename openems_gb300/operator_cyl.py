@@ -19,10 +19,11 @@ alpha edges are rho times their angle (GetEdgeLength, :204-210), z faces are ann
 Built here: materials (eps, kappa, mue, sigma), metal (PEC), soft/hard and weighted excitations,
 Mur walls that the reference accepts in cylindrical coordinates (operator_ext_mur_abc.cpp:47-54;
 the others are dropped as there, leaving PEC), UPML on the rho and z walls, Drude/Lorentz
-materials (their tables read only the equivalent circuit, which carries the geometry), voltage,
+materials (their tables read only the equivalent circuit, which carries the geometry), parallel
+RC lumped elements (Calc_LumpedElements with the cylindrical edge area over length), voltage,
 current and field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the
-reference too), lumped elements and conducting sheets, field dumps, and alpha fitting of
-coordinates outside the mesh's alpha range.
+reference too), series or inductive lumped elements and conducting sheets, field dumps, and
+alpha fitting of coordinates outside the mesh's alpha range.
 """
 from __future__ import annotations
 
@@ -31,7 +32,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .operator import (CONDSHEET, DUMP, EPS0, LUMPED, METAL, MUE0, Grid, Operator, _axes, _coords_xyz)
+from .operator import (CONDSHEET, DUMP, EPS0, LUMPED, METAL, MUE0, Grid, Operator, _axes, _is_lumped_rlc)
 
 CLOSED_ALPHA_THRESHOLD = 1e-6     # OPERATOR_CYLINDER_CLOSED_ALPHA_THRESHOLD (operator_cylinder.h:21)
 TWO_PI = 2.0 * math.pi
@@ -107,9 +108,12 @@ class OperatorCylinder(Operator):
             # PEC (CalcPEC_Range) looks the metal up at Yee coordinates
             self._matmetal = _AlphaWrapPainter(self._matmetal, self.L[1][0], inclusive=True)
         for prop in structure.props:
-            if prop.kind & (LUMPED | CONDSHEET):
-                raise ValueError(f"OperatorCylinder: {prop.name}: lumped elements and conducting sheets "
-                                 "are not built in cylindrical coordinates")
+            if prop.kind == LUMPED and _is_lumped_rlc(prop):
+                raise ValueError(f"OperatorCylinder: {prop.name}: series / inductive lumped elements are not "
+                                 "built in cylindrical coordinates (parallel RC elements are)")
+            if prop.kind & CONDSHEET:
+                raise ValueError(f"OperatorCylinder: {prop.name}: conducting sheets are not built in "
+                                 "cylindrical coordinates")
             if prop.kind == DUMP:
                 raise ValueError(f"OperatorCylinder: {prop.name}: field dumps are not built in cylindrical coordinates")
             if prop.params.get("exc_type") == 10:
@@ -279,6 +283,10 @@ class OperatorCylinder(Operator):
             self._eff = {k: self.eff_mat(k) for k in range(3)}
         sl = tuple(slice(int(start[a]), int(start[a] + nl[a])) for a in range(3))
         return [x[sl] for x in self._eff[n]]
+
+    def _area_over_length(self, ny, pos):
+        P = [np.asarray(int(v)) for v in pos]
+        return float(self._edge_area(ny, P, False)) / float(self._cyl_len(ny, P, False))
 
     def _edge_geometry(self, n, pos_axes):
         P = [np.asarray(pos_axes[0]).reshape(-1, 1, 1), np.asarray(pos_axes[1]).reshape(1, -1, 1),

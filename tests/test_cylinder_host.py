@@ -122,6 +122,24 @@ def test_coax_impedance_in_cylindrical_coordinates(pml):
     assert (Z <= Z0 * 1.03).all() and (Z >= Z0 * 0.99).all(), (Z.min() / Z0, Z.max() / Z0)
 
 
+def test_coax_with_a_lumped_load_sweeps_between_r_and_z0_squared_over_r():
+    """A parallel-RC lumped element of R = Z0/2 across the far-end wall of the cylindrical coax
+    (a ring of radial edges, Calc_LumpedElements with cylindrical areas): on a lossless line the
+    input impedance magnitude runs between R and Z0^2/R over the band (VSWR 2); within 3 %."""
+    steps = 5000
+    Z0 = math.sqrt(MUE0 / EPS0) * math.log(230 / 100) / (2 * math.pi)
+    op = configs.coax_cyl(steps=steps, load=Z0 / 2)
+    e = OracleEngine(op, steps, threads=THREADS)
+    e.IterateTS(steps)
+    u = e.probe_series(e.vprobe_ids[0])
+    i = e.probe_series(e.iprobe_ids[0])
+    nfft = 1 << int(math.ceil(math.log2(len(u))))
+    f = np.fft.rfftfreq(nfft, op.dt)
+    sel = f <= 1e9
+    Z = np.abs(np.fft.rfft(u, nfft)[sel] / np.fft.rfft(i, nfft)[sel]) / Z0
+    assert abs(Z.min() / 0.5 - 1) < 0.03 and abs(Z.max() / 2.0 - 1) < 0.03, (Z.min(), Z.max())
+
+
 def test_pillbox_tm010_resonance_with_the_axis():
     steps = 20000
     op = configs.cavity_cyl(steps=steps)
@@ -143,6 +161,7 @@ def test_pillbox_tm010_resonance_with_the_axis():
 @pytest.mark.parametrize("name,fn,steps", [
     ("coax", lambda: configs.coax_cyl(steps=300, length=400.0), 300),
     ("coax_upml", lambda: configs.coax_cyl(steps=300, length=400.0, pml=True), 300),
+    ("coax_load", lambda: configs.coax_cyl(steps=300, length=400.0, load=30.0), 300),
     ("cavity", lambda: configs.cavity_cyl(steps=600), 600),
     ("cavity_off_axis_probe", lambda: configs.cavity_cyl(steps=400, n_alpha=25, probe_r=10.0), 400),
     ("cavity_dispersive", lambda: configs.cavity_cyl(steps=400, dispersive=True), 400),
