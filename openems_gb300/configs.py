@@ -450,6 +450,11 @@ def fieldprobes(half=8, steps=600, freqs=(5e8,), interval=0):
 
 
 def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=None):
+    """``coax_cyl_operator`` built for ``steps`` timesteps."""
+    return coax_cyl_operator(length, res, n_alpha, pml, load).build(steps)
+
+
+def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None):
     """The reference's coax example in cylindrical coordinates
     (matlab/examples/waveguide/Coax_CylinderCoords.m:25-123): rho from the inner radius 100 to the
     outer radius 230 on a 10 mm mesh, 71 alpha lines over 2*pi (a closed mesh), z over 1000 mm; PEC
@@ -457,7 +462,7 @@ def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=No
     (f0 = fc = 0.5 GHz); half way down, a voltage probe across the gap at alpha = 0 and a current
     loop around the inner conductor on the dual mesh (one full turn of alpha).  ``pml``: a PML_8 at
     the far end instead of Mur (the example's use_pml option).  ``load``: a radial lumped resistor
-    of that many ohms over the whole far-end wall (one parallel RC element), PEC behind it."""
+    of that many ohms over the far-end wall (one parallel RC element), with no BC on that wall."""
     from .operator_cyl import OperatorCylinder
     r_i, r_a = 100.0, 230.0
     rs = np.arange(r_i, r_a + 0.5 * res, res)
@@ -476,10 +481,13 @@ def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=No
     # the loop starts below the mesh (no inner side) and runs over dual alpha lines 0 .. N-2
     csx.AddProbe("it1", 1, norm_dir=2, interval=1).AddBox([0.0, 0.5 * a1, zm], [mid, 2 * np.pi + 0.5 * a1, zm])
     if load is not None:
-        csx.AddLumpedElement("load", ny=0, R=float(load), caps=False).AddBox([r_i, al[0], zs[-1]], [r_a, al[-1], zs[-1]])
-    far = 0 if load is not None else (3 if pml else 2)
-    op = OperatorCylinder(csx, g, exc, bc=(0, 0, 0, 0, 0, far), pml_size=(8,) * 6)
-    return op.build(steps)
+        # up to the last distinct angle: snapping folds alpha = 2*pi back to 0 on a closed mesh
+        # (SnapToMeshLine + FitToAlphaRange), which would leave a single radial edge chain
+        csx.AddLumpedElement("load", ny=0, R=float(load), caps=False).AddBox([r_i, al[0], zs[-1]], [r_a, al[-2], zs[-1]])
+    # a load sits on the far wall without a BC (-1): on a PEC wall the line N-2, which the snapped
+    # element does not reach, would stay PEC and the seam copy would short line 0
+    far = -1 if load is not None else (3 if pml else 2)
+    return OperatorCylinder(csx, g, exc, bc=(0, 0, 0, 0, 0, far), pml_size=(8,) * 6)
 
 
 def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe_r=0.0, dispersive=False):

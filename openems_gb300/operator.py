@@ -947,35 +947,42 @@ class Operator:
         return vv.astype(self.ft), vi.astype(self.ft), ii.astype(self.ft), iv.astype(self.ft)
 
     # ---- snapping (FDTD/operator.cpp:252-372) ----------------------------------------------
-    def snap_line(self, ny, coord, dual=False):
+    def _num_lines(self, ny, full):
+        """GetNumberOfLines(ny, fullMesh): every line on a Cartesian mesh."""
+        return int(self.N[ny])
+
+    def snap_line(self, ny, coord, dual=False, full=False):
+        """SnapToMeshLine (FDTD/operator.cpp:252-280) over GetNumberOfLines(ny, full) lines."""
         L = self.L[ny]
+        nl = self._num_lines(ny, full)
         if coord < L[0]:
             return 0, False
-        if coord > L[-1]:
-            return len(L) - 1, False
+        if coord > L[nl - 1]:
+            return nl - 1, False
         if not dual:
             dl = self.dl[ny]
-            for n in range(len(L)):
+            for n in range(nl):
                 if coord <= dl[n]:
                     return n, True
         else:
-            for n in range(1, len(L)):
+            for n in range(1, nl):
                 if coord <= L[n]:
                     return n - 1, True
         return 0, True
 
-    def snap_box(self, start, stop, dual=False, method=0):
+    def snap_box(self, start, stop, dual=False, method=0, full=False):
         """SnapBox2Mesh; returns (dim, uiStart, uiStop, startIn, stopIn) or dim=-2 if outside."""
         lstart = np.minimum(start, stop)
         lstop = np.maximum(start, stop)
+        nl = [self._num_lines(n, full) for n in range(3)]
         for n in range(3):
-            mn, mx = self.L[n][0], self.L[n][-1]
+            mn, mx = self.L[n][0], self.L[n][nl[n] - 1]
             if (lstart[n] < mn and lstop[n] < mn) or (lstart[n] > mx and lstop[n] > mx):
                 return -2, None, None, None, None
         s, si, e, ei = [0] * 3, [False] * 3, [0] * 3, [False] * 3
         for n in range(3):
-            s[n], si[n] = self.snap_line(n, lstart[n], dual)
-            e[n], ei[n] = self.snap_line(n, lstop[n], dual)
+            s[n], si[n] = self.snap_line(n, lstart[n], dual, full)
+            e[n], ei[n] = self.snap_line(n, lstop[n], dual, full)
         dim = 0
 
         def line(n, i):
@@ -984,10 +991,10 @@ class Operator:
             if method == 1 and e[n] > s[n]:
                 if line(n, s[n]) > lstart[n] and s[n] > 0:
                     s[n] -= 1
-                if line(n, e[n]) < lstop[n] and e[n] < self.N[n] - 1:
+                if line(n, e[n]) < lstop[n] and e[n] < nl[n] - 1:
                     e[n] += 1
             elif method == 2 and e[n] > s[n]:
-                if line(n, s[n]) < lstart[n] and s[n] < self.N[n] - 1:
+                if line(n, s[n]) < lstart[n] and s[n] < nl[n] - 1:
                     s[n] += 1
                 if line(n, e[n]) > lstop[n] and e[n] > 0:
                     e[n] -= 1
@@ -1173,7 +1180,8 @@ class Operator:
             ny = prop.params["ny"]
             nyP, nyPP = (ny + 1) % 3, (ny + 2) % 3
             for lo, hi, _pr, _sq, _p, *_ in prop.boxes:
-                dim, s, e, _, _ = self.snap_box(lo, hi, dual=False, method=0)
+                # the base SnapBox2Mesh on the full mesh (Operator::SnapBox2Mesh, qualified)
+                dim, s, e, _, _ = Operator.snap_box(self, lo, hi, dual=False, method=0, full=True)
                 if dim <= 0 or s[ny] == e[ny]:
                     continue
                 def gc(pos):

@@ -304,6 +304,53 @@ class OperatorCylinder(Operator):
         # Calc_ECPos of the z edges on the axis, in double, for the rho = 0 extension
         self._r0_CG = (ec[2][0][0], ec[2][1][0])
 
+    # ---- snapping (operator_cylinder.cpp:100-108, 227-296) ---------------------------------
+    def _num_lines(self, ny, full):
+        """GetNumberOfLines: a closed mesh hides its last two alpha lines from processing."""
+        if not full and ny == 1 and self.closed_alpha:
+            return int(self.N[1]) - 2
+        return int(self.N[ny])
+
+    def fit_to_alpha_range(self, a, full=False):
+        """FitToAlphaRange (:227-249): a coordinate shifted by 2*pi into the alpha lines' range."""
+        lo = float(self.L[1][0])
+        hi = float(self.L[1][self._num_lines(1, full) - 1])
+        if lo <= a <= hi:
+            return a
+        while a < lo:
+            a += TWO_PI
+            if a > hi:
+                return a - TWO_PI
+            if a > lo:
+                return a
+        while a > hi:
+            a -= TWO_PI
+            if a < lo:
+                return a + TWO_PI
+            if a < hi:
+                return a
+        return a
+
+    def snap_line(self, ny, coord, dual=False, full=False):
+        if ny == 1:
+            coord = self.fit_to_alpha_range(float(coord))
+        return super().snap_line(ny, coord, dual, full)
+
+    def snap_box(self, start, stop, dual=False, method=0, full=False):
+        """SnapBox2Mesh (:270-290): the alpha span is centred by FitToAlphaRange and clamped to
+        the alpha lines before the Cartesian snapping."""
+        a_min = float(self.L[1][0])
+        a_max = float(self.L[1][self._num_lines(1, full) - 1])
+        a_size = float(stop[1]) - float(start[1])
+        a_center = self.fit_to_alpha_range(0.5 * (float(stop[1]) + float(start[1])))
+        a_start = a_center - a_size / 2
+        a_stop = a_start + a_size
+        a_stop = min(max(a_stop, a_min), a_max)
+        a_start = min(max(a_start, a_min), a_max)
+        l_start = np.array([start[0], a_start, start[2]], np.float64)
+        l_stop = np.array([stop[0], a_stop, stop[2]], np.float64)
+        return super().snap_box(l_start, l_stop, dual, method, full)
+
     def _yee_painter(self, kinds):
         p = super()._yee_painter(kinds)
         return _AlphaWrapPainter(p, self.L[1][0], inclusive=True) if self.closed_alpha else p
