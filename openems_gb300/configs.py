@@ -449,12 +449,12 @@ def fieldprobes(half=8, steps=600, freqs=(5e8,), interval=0):
     return data
 
 
-def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=None):
+def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=None, rlc=False):
     """``coax_cyl_operator`` built for ``steps`` timesteps."""
-    return coax_cyl_operator(length, res, n_alpha, pml, load).build(steps)
+    return coax_cyl_operator(length, res, n_alpha, pml, load, rlc).build(steps)
 
 
-def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None):
+def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None, rlc=False):
     """The reference's coax example in cylindrical coordinates
     (matlab/examples/waveguide/Coax_CylinderCoords.m:25-123): rho from the inner radius 100 to the
     outer radius 230 on a 10 mm mesh, 71 alpha lines over 2*pi (a closed mesh), z over 1000 mm; PEC
@@ -462,7 +462,9 @@ def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None)
     (f0 = fc = 0.5 GHz); half way down, a voltage probe across the gap at alpha = 0 and a current
     loop around the inner conductor on the dual mesh (one full turn of alpha).  ``pml``: a PML_8 at
     the far end instead of Mur (the example's use_pml option).  ``load``: a radial lumped resistor
-    of that many ohms over the far-end wall (one parallel RC element), with no BC on that wall."""
+    of that many ohms across the gap one line in front of the far end (one parallel RC element, or
+    with ``rlc`` a parallel R || 1 uH element of the lumped RLC extension), so the line sees it
+    in parallel with the matched remainder."""
     from .operator_cyl import OperatorCylinder
     r_i, r_a = 100.0, 230.0
     rs = np.arange(r_i, r_a + 0.5 * res, res)
@@ -483,10 +485,10 @@ def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None)
     if load is not None:
         # up to the last distinct angle: snapping folds alpha = 2*pi back to 0 on a closed mesh
         # (SnapToMeshLine + FitToAlphaRange), which would leave a single radial edge chain
-        csx.AddLumpedElement("load", ny=0, R=float(load), caps=False).AddBox([r_i, al[0], zs[-1]], [r_a, al[-2], zs[-1]])
-    # a load sits on the far wall without a BC (-1): on a PEC wall the line N-2, which the snapped
-    # element does not reach, would stay PEC and the seam copy would short line 0
-    far = -1 if load is not None else (3 if pml else 2)
+        # rlc: a parallel R || 1 uH element, which the lumped RLC extension builds
+        csx.AddLumpedElement("load", ny=0, R=float(load), caps=False, L=1e-6 if rlc else float("nan")).AddBox(
+            [r_i, al[0], zs[-2]], [r_a, al[-2], zs[-2]])
+    far = 3 if pml else 2
     return OperatorCylinder(csx, g, exc, bc=(0, 0, 0, 0, 0, far), pml_size=(8,) * 6)
 
 

@@ -1759,7 +1759,7 @@ class Operator:
                 continue
             d1, d2 = (d + 1) % 3, (d + 2) % 3
             for lo, hi, *_ in prop.boxes:
-                dim, s0, e0, _, _ = self.snap_box(lo, hi, dual=False, method=0)
+                dim, s0, e0, _, _ = self.snap_box(lo, hi, dual=False, method=0, full=True)
                 if dim <= 0:
                     continue
                 s0 = [int(v) for v in s0]

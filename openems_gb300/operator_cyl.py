@@ -20,10 +20,10 @@ Built here: materials (eps, kappa, mue, sigma), metal (PEC), soft/hard and weigh
 Mur walls that the reference accepts in cylindrical coordinates (operator_ext_mur_abc.cpp:47-54;
 the others are dropped as there, leaving PEC), UPML on the rho and z walls, Drude/Lorentz
 materials (their tables read only the equivalent circuit, which carries the geometry), parallel
-RC lumped elements (Calc_LumpedElements with the cylindrical edge area over length), voltage,
-current and field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the
-reference too), series or inductive lumped elements and conducting sheets, field dumps, and
-alpha fitting of coordinates outside the mesh's alpha range.
+RC lumped elements (Calc_LumpedElements with the cylindrical edge area over length), lumped RLC
+elements (Operator_Ext_LumpedRLC reads the equivalent circuit and snaps on the full mesh),
+voltage, current and field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the
+reference too), conducting sheets, and field dumps.
 """
 from __future__ import annotations
 
@@ -32,7 +32,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .operator import (CONDSHEET, DUMP, EPS0, LUMPED, METAL, MUE0, Grid, Operator, _axes, _is_lumped_rlc)
+from .operator import CONDSHEET, DUMP, EPS0, METAL, MUE0, Grid, Operator, _axes
 
 CLOSED_ALPHA_THRESHOLD = 1e-6     # OPERATOR_CYLINDER_CLOSED_ALPHA_THRESHOLD (operator_cylinder.h:21)
 TWO_PI = 2.0 * math.pi
@@ -108,9 +108,6 @@ class OperatorCylinder(Operator):
             # PEC (CalcPEC_Range) looks the metal up at Yee coordinates
             self._matmetal = _AlphaWrapPainter(self._matmetal, self.L[1][0], inclusive=True)
         for prop in structure.props:
-            if prop.kind == LUMPED and _is_lumped_rlc(prop):
-                raise ValueError(f"OperatorCylinder: {prop.name}: series / inductive lumped elements are not "
-                                 "built in cylindrical coordinates (parallel RC elements are)")
             if prop.kind & CONDSHEET:
                 raise ValueError(f"OperatorCylinder: {prop.name}: conducting sheets are not built in "
                                  "cylindrical coordinates")
