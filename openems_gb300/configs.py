@@ -98,6 +98,10 @@ def small_mixed(n=(18, 16, 14), steps=200, bc=(3, 3, 2, 2, 0, 3), pml=4, seed=1,
     exc.SetupGaussianPulse(6e9, 5e9)
     L = [l[-1] for l in g.lines]
     csx.AddMaterial("diel", epsilon=4.0, kappa=0.05).AddBox([0.3 * L[0], 0.2 * L[1], 0.2 * L[2]], [0.6 * L[0], 0.7 * L[1], 0.5 * L[2]])
+    if field_probes:
+        pt = [0.4 * radius, al[5], zs[k]]
+        csx.AddProbe("et", 2, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
+        csx.AddProbe("ht", 3, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
     if dispersive:
         csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[5e9], eps_relax_time=[2e-9]).AddBox(
             [0.55 * L[0], 0.4 * L[1], 0.4 * L[2]], [0.8 * L[0], 0.8 * L[1], 0.8 * L[2]], priority=5)
@@ -492,12 +496,14 @@ def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None,
     return OperatorCylinder(csx, g, exc, bc=(0, 0, 0, 0, 0, far), pml_size=(8,) * 6)
 
 
-def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe_r=0.0, dispersive=False):
+def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe_r=0.0, dispersive=False,
+               field_probes=False):
     """A pillbox cavity in cylindrical coordinates with rho = 0 on the mesh: radius 50 mm, height
     20 mm, PEC walls, a 2.5 mm rho/z mesh and 10 degree alpha steps (a closed mesh), a soft Ez
     point source off the axis (f0 3 GHz, fc 2 GHz) and an Ez voltage probe at ``probe_r`` (on the
     axis by default, where the TM010 field is largest and the axis hook computes it).
-    ``dispersive``: a Drude rod on the axis and a Lorentz sector across the alpha seam."""
+    ``dispersive``: a Drude rod on the axis and a Lorentz sector across the alpha seam.
+    ``field_probes``: E and H point probes off the axis (probe types 2 and 3), sampled every step."""
     from .operator_cyl import OperatorCylinder
     rs = np.arange(0.0, radius + 0.5 * res, res)
     al = np.linspace(0.0, 2 * np.pi, n_alpha)

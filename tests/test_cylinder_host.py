@@ -189,6 +189,30 @@ def test_pillbox_tm010_resonance_with_the_axis():
     assert -2.5e-3 <= fp / f010 - 1 <= 0.0, fp / f010 - 1
 
 
+def test_field_probes_on_the_cylindrical_mesh():
+    """E/H point probes (ProcessFieldProbe) divide by the cylindrical GetEdgeLength: the alpha
+    component by rho * dalpha (main mesh for E, dual for H)."""
+    steps = 300
+    op = configs.cavity_cyl(steps=steps, field_probes=True)
+    e = OracleEngine(op, steps)
+    e.IterateTS(steps)
+    V, I = e.read_field(0), e.read_field(1)
+    u = op.grid.unit
+    for pid, p in zip(e.fprobe_ids, op.fprobes):
+        x, y, z = (int(v) for v in p.pos)
+        lines = op.grid.lines
+        dual = p.field == 1
+        from openems_gb300.operator import _dual_delta, _dual_line, _main_delta
+        d = (_dual_delta if dual else _main_delta)
+        rho = (_dual_line(lines[0]) if dual else np.asarray(lines[0]))[x]
+        want_el = [d(lines[0])[x] * u, d(lines[1])[y] * u * rho, d(lines[2])[z] * u]
+        assert np.allclose(p.el, want_el, rtol=1e-15)
+        F = I if dual else V
+        last = e.probe_series(pid)[steps]
+        want = np.array([float(F[c, x, y, z]) / want_el[c] for c in range(3)])
+        assert np.array_equal(last, want), (p.name, last, want)
+
+
 @pytest.mark.parametrize("name,fn,steps", [
     ("coax", lambda: configs.coax_cyl(steps=300, length=400.0), 300),
     ("coax_upml", lambda: configs.coax_cyl(steps=300, length=400.0, pml=True), 300),
