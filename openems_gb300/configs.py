@@ -98,10 +98,6 @@ def small_mixed(n=(18, 16, 14), steps=200, bc=(3, 3, 2, 2, 0, 3), pml=4, seed=1,
     exc.SetupGaussianPulse(6e9, 5e9)
     L = [l[-1] for l in g.lines]
     csx.AddMaterial("diel", epsilon=4.0, kappa=0.05).AddBox([0.3 * L[0], 0.2 * L[1], 0.2 * L[2]], [0.6 * L[0], 0.7 * L[1], 0.5 * L[2]])
-    if field_probes:
-        pt = [0.4 * radius, al[5], zs[k]]
-        csx.AddProbe("et", 2, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
-        csx.AddProbe("ht", 3, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
     if dispersive:
         csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[5e9], eps_relax_time=[2e-9]).AddBox(
             [0.55 * L[0], 0.4 * L[1], 0.4 * L[2]], [0.8 * L[0], 0.8 * L[1], 0.8 * L[2]], priority=5)
@@ -453,12 +449,12 @@ def fieldprobes(half=8, steps=600, freqs=(5e8,), interval=0):
     return data
 
 
-def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=None, rlc=False):
+def coax_cyl(steps=5000, length=1000.0, res=10.0, n_alpha=71, pml=False, load=None, rlc=False, shield=None):
     """``coax_cyl_operator`` built for ``steps`` timesteps."""
-    return coax_cyl_operator(length, res, n_alpha, pml, load, rlc).build(steps)
+    return coax_cyl_operator(length, res, n_alpha, pml, load, rlc, shield).build(steps)
 
 
-def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None, rlc=False):
+def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None, rlc=False, shield=None):
     """The reference's coax example in cylindrical coordinates
     (matlab/examples/waveguide/Coax_CylinderCoords.m:25-123): rho from the inner radius 100 to the
     outer radius 230 on a 10 mm mesh, 71 alpha lines over 2*pi (a closed mesh), z over 1000 mm; PEC
@@ -468,7 +464,8 @@ def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None,
     the far end instead of Mur (the example's use_pml option).  ``load``: a radial lumped resistor
     of that many ohms across the gap one line in front of the far end (one parallel RC element, or
     with ``rlc`` a parallel R || 1 uH element of the lumped RLC extension), so the line sees it
-    in parallel with the matched remainder."""
+    in parallel with the matched remainder.  ``shield``: "sheet" (a 35 um copper conducting sheet)
+    or "metal" (PEC) across the gap a quarter of the way down, between source and probes."""
     from .operator_cyl import OperatorCylinder
     r_i, r_a = 100.0, 230.0
     rs = np.arange(r_i, r_a + 0.5 * res, res)
@@ -486,6 +483,13 @@ def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None,
     a1 = al[1]
     # the loop starts below the mesh (no inner side) and runs over dual alpha lines 0 .. N-2
     csx.AddProbe("it1", 1, norm_dir=2, interval=1).AddBox([0.0, 0.5 * a1, zm], [mid, 2 * np.pi + 0.5 * a1, zm])
+    if shield is not None:
+        zq = zs[len(zs) // 4]
+        box = ([r_i, al[0], zq], [r_a, al[-1], zq])
+        if shield == "sheet":
+            csx.AddConductingSheet("shield", conductivity=5.8e7, thickness=35e-6).AddBox(*box)
+        else:
+            csx.AddMetal("shield").AddBox(*box)
     if load is not None:
         # up to the last distinct angle: snapping folds alpha = 2*pi back to 0 on a closed mesh
         # (SnapToMeshLine + FitToAlphaRange), which would leave a single radial edge chain
@@ -516,6 +520,10 @@ def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe
     rs_src = rs[len(rs) // 3]
     csx.AddExcitation("src", 0, [0, 0, 1.0]).AddBox([rs_src, al[3], zs[k]], [rs_src, al[3], zs[k + 1]])
     csx.AddProbe("uz", 0, interval=1).AddBox([probe_r, 0.0, zs[1]], [probe_r, 0.0, zs[-2]])
+    if field_probes:
+        pt = [0.4 * radius, al[5], zs[k]]
+        csx.AddProbe("et", 2, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
+        csx.AddProbe("ht", 3, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
     if dispersive:
         csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[4e9], eps_relax_time=[1e-9]).AddBox(
             [0.0, 0.0, zs[2]], [3 * res, 2 * np.pi, zs[-3]])

@@ -1084,6 +1084,10 @@ class Operator:
         """Cartesian meshes have no cylinder extension."""
         return None
 
+    def _node_width_at(self, ny, pos, dual=False):
+        """GetNodeWidth(ny, pos, dual) = GetEdgeLength(ny, pos, !dual) for one position."""
+        return self._edge_length(ny, pos, not dual)
+
     def _area_over_length(self, ny, pos):
         """GetEdgeArea(ny, pos) / GetEdgeLength(ny, pos) of one edge; the area is the product of
         the two node widths (GetNodeArea, FDTD/operator.cpp:235-240)."""
@@ -1942,7 +1946,8 @@ class Operator:
                     k = len(T.OMEGA_STOP) - 1
                 if t_dir < 0:
                     continue
-                wtl = ft((self.md[n][p[n]] * u) / (self.dd[t_dir][p[t_dir]] * u))
+                # GetEdgeLength(n, pos) / GetNodeWidth(t_dir, pos)
+                wtl = ft(self._edge_length(n, p) / self._node_width_at(t_dir, p))
                 factor = ft(1)
                 if tan[t_dir, p[0], p[1], p[2]] < 0:
                     factor = ft(2)

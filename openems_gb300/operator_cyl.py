@@ -22,8 +22,9 @@ the others are dropped as there, leaving PEC), UPML on the rho and z walls, Drud
 materials (their tables read only the equivalent circuit, which carries the geometry), parallel
 RC lumped elements (Calc_LumpedElements with the cylindrical edge area over length), lumped RLC
 elements (Operator_Ext_LumpedRLC reads the equivalent circuit and snaps on the full mesh),
-voltage, current and field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the
-reference too), conducting sheets, and field dumps.
+conducting sheets (their edge length over node width taken cylindrically), voltage, current and
+field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the reference too), and
+field dumps.
 """
 from __future__ import annotations
 
@@ -32,7 +33,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .operator import CONDSHEET, DUMP, EPS0, METAL, MUE0, Grid, Operator, _axes
+from .operator import DUMP, EPS0, METAL, MUE0, Grid, Operator, _axes
 
 CLOSED_ALPHA_THRESHOLD = 1e-6     # OPERATOR_CYLINDER_CLOSED_ALPHA_THRESHOLD (operator_cylinder.h:21)
 TWO_PI = 2.0 * math.pi
@@ -108,9 +109,6 @@ class OperatorCylinder(Operator):
             # PEC (CalcPEC_Range) looks the metal up at Yee coordinates
             self._matmetal = _AlphaWrapPainter(self._matmetal, self.L[1][0], inclusive=True)
         for prop in structure.props:
-            if prop.kind & CONDSHEET:
-                raise ValueError(f"OperatorCylinder: {prop.name}: conducting sheets are not built in "
-                                 "cylindrical coordinates")
             if prop.kind == DUMP:
                 raise ValueError(f"OperatorCylinder: {prop.name}: field dumps are not built in cylindrical coordinates")
             if prop.params.get("exc_type") == 10:
@@ -280,6 +278,10 @@ class OperatorCylinder(Operator):
             self._eff = {k: self.eff_mat(k) for k in range(3)}
         sl = tuple(slice(int(start[a]), int(start[a] + nl[a])) for a in range(3))
         return [x[sl] for x in self._eff[n]]
+
+    def _node_width_at(self, ny, pos, dual=False):
+        """Operator_Cylinder::GetNodeWidth (:134-143) for one position (metres)."""
+        return float(self._node_width(ny, [np.asarray(int(v)) for v in pos], dual))
 
     def _area_over_length(self, ny, pos):
         P = [np.asarray(int(v)) for v in pos]

@@ -189,6 +189,23 @@ def test_pillbox_tm010_resonance_with_the_axis():
     assert -2.5e-3 <= fp / f010 - 1 <= 0.0, fp / f010 - 1
 
 
+def test_conducting_sheet_shields_the_coax():
+    """A 35 um copper conducting sheet (Operator_Ext_ConductingSheet, edge length over node width
+    taken cylindrically) across the coax between the source and the probe lets through less than
+    1e-3 of the unshielded voltage, as the Cartesian sheet test requires; a PEC annulus none."""
+    steps = 3000
+    peak = {}
+    for sh in (None, "sheet", "metal"):
+        op = configs.coax_cyl(steps=steps, length=600.0, shield=sh)
+        assert (len(op.lorentz) == 2) == (sh == "sheet")
+        e = OracleEngine(op, steps, threads=THREADS)
+        e.IterateTS(steps)
+        peak[sh] = np.abs(e.probe_series(e.vprobe_ids[0])).max()
+    assert peak[None] > 0
+    assert peak["sheet"] < 1e-3 * peak[None]
+    assert peak["metal"] <= peak["sheet"]
+
+
 def test_field_probes_on_the_cylindrical_mesh():
     """E/H point probes (ProcessFieldProbe) divide by the cylindrical GetEdgeLength: the alpha
     component by rho * dalpha (main mesh for E, dual for H)."""
@@ -198,6 +215,7 @@ def test_field_probes_on_the_cylindrical_mesh():
     e.IterateTS(steps)
     V, I = e.read_field(0), e.read_field(1)
     u = op.grid.unit
+    assert len(e.fprobe_ids) == 2 and [p.field for p in op.fprobes] == [0, 1]
     for pid, p in zip(e.fprobe_ids, op.fprobes):
         x, y, z = (int(v) for v in p.pos)
         lines = op.grid.lines
@@ -218,6 +236,7 @@ def test_field_probes_on_the_cylindrical_mesh():
     ("coax_upml", lambda: configs.coax_cyl(steps=300, length=400.0, pml=True), 300),
     ("coax_load", lambda: configs.coax_cyl(steps=300, length=400.0, load=30.0), 300),
     ("coax_rlc_load", lambda: configs.coax_cyl(steps=300, length=400.0, load=30.0, rlc=True), 300),
+    ("coax_sheet", lambda: configs.coax_cyl(steps=300, length=400.0, shield="sheet"), 300),
     ("cavity", lambda: configs.cavity_cyl(steps=600), 600),
     ("cavity_off_axis_probe", lambda: configs.cavity_cyl(steps=400, n_alpha=25, probe_r=10.0), 400),
     ("cavity_dispersive", lambda: configs.cavity_cyl(steps=400, dispersive=True), 400),

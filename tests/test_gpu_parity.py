@@ -63,6 +63,7 @@ CASES = [
     ("coax_cyl_closed_alpha_upml", lambda: configs.coax_cyl(steps=200, length=400.0, pml=True), 200),
     ("coax_cyl_lumped_load", lambda: configs.coax_cyl(steps=200, length=400.0, load=30.0), 200),
     ("coax_cyl_rlc_load", lambda: configs.coax_cyl(steps=200, length=400.0, load=30.0, rlc=True), 200),
+    ("coax_cyl_conducting_sheet", lambda: configs.coax_cyl(steps=200, length=400.0, shield="sheet"), 200),
     ("cavity_cyl_axis", lambda: configs.cavity_cyl(steps=400), 400),
     ("cavity_cyl_off_axis", lambda: configs.cavity_cyl(steps=300, n_alpha=25, probe_r=10.0), 300),
     ("cavity_cyl_dispersive", lambda: configs.cavity_cyl(steps=300, dispersive=True), 300),
