@@ -1677,8 +1677,11 @@ class Operator:
             for n in range(3):
                 a, p, pp = _axes(n)
                 kv1, ki1 = self._grading_kappa(n, pos_axes)
-                KV = [kv1[k].reshape([-1 if j == k else 1 for j in range(3)]) for k in range(3)]
-                KI = [ki1[k].reshape([-1 if j == k else 1 for j in range(3)]) for k in range(3)]
+                # 1-D gradings along their axis, or arrays that already broadcast over the region
+                KV = [kv1[k] if kv1[k].ndim == 3 else kv1[k].reshape([-1 if j == k else 1 for j in range(3)])
+                      for k in range(3)]
+                KI = [ki1[k] if ki1[k].ndim == 3 else ki1[k].reshape([-1 if j == k else 1 for j in range(3)])
+                      for k in range(3)]
                 ksum_v = np.broadcast_to(KV[0] + KV[1] + KV[2], shape)
                 ksum_i = np.broadcast_to(KI[0] + KI[1] + KI[2], shape)
                 eff_eps, eff_kap, eff_mue, _ = self.eff_region(n, start, nl)

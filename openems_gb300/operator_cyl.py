@@ -18,13 +18,13 @@ alpha edges are rho times their angle (GetEdgeLength, :204-210), z faces are ann
 
 Built here: materials (eps, kappa, mue, sigma), metal (PEC), soft/hard and weighted excitations,
 Mur walls that the reference accepts in cylindrical coordinates (operator_ext_mur_abc.cpp:47-54;
-the others are dropped as there, leaving PEC), UPML on the rho and z walls, Drude/Lorentz
+the others are dropped as there, leaving PEC), UPML on the rho and z walls and on the alpha
+walls of an open mesh (graded with rho along alpha), Drude/Lorentz
 materials (their tables read only the equivalent circuit, which carries the geometry), parallel
 RC lumped elements (Calc_LumpedElements with the cylindrical edge area over length), lumped RLC
 elements (Operator_Ext_LumpedRLC reads the equivalent circuit and snaps on the full mesh),
 conducting sheets (their edge length over node width taken cylindrically), voltage, current and
-field probes.  Not built for this mesh: an alpha UPML, TFSF (rejected by the reference too), and
-field dumps.
+field probes.  Not built for this mesh: TFSF (rejected by the reference too) and field dumps.
 """
 from __future__ import annotations
 
@@ -33,7 +33,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .operator import DUMP, EPS0, METAL, MUE0, Grid, Operator, _axes
+from .operator import DUMP, EPS0, METAL, MUE0, Z0, Grid, Operator, _axes
 
 CLOSED_ALPHA_THRESHOLD = 1e-6     # OPERATOR_CYLINDER_CLOSED_ALPHA_THRESHOLD (operator_cylinder.h:21)
 TWO_PI = 2.0 * math.pi
@@ -87,10 +87,9 @@ class OperatorCylinder(Operator):
         # on an open mesh rho = 0 needs no special treatment (E_alpha/E_z there are PEC anyway)
         self.r0_included = bool(lines[0][0] == 0.0 and closed)
         bc = [int(b) for b in bc]
-        # UPML on the rho and z walls; an alpha PML would grade with rho (operator_ext_upml.cpp:
-        # 280-284) and is not built, nor is a PML at rho = 0
-        if bc[2] == 3 or bc[3] == 3:
-            raise ValueError("OperatorCylinder: a UPML on the alpha walls is not built")
+        # UPML: on the alpha walls of an open mesh only (a closed mesh has none), and not at rho = 0
+        if closed and (bc[2] == 3 or bc[3] == 3):
+            raise ValueError("OperatorCylinder: a closed alpha mesh has no alpha walls for a UPML")
         if bc[0] == 3 and lines[0][0] == 0.0:
             raise ValueError("OperatorCylinder: no UPML at rho = 0")
         # Mur walls the reference rejects in cylindrical coordinates are dropped (PEC remains)
@@ -286,6 +285,70 @@ class OperatorCylinder(Operator):
     def _area_over_length(self, ny, pos):
         P = [np.asarray(int(v)) for v in pos]
         return float(self._edge_area(ny, P, False)) / float(self._cyl_len(ny, P, False))
+
+    def _grading_kappa(self, ny, pos_axes):
+        """CalcGradingKappa (operator_ext_upml.cpp:269-343) on this mesh: along rho and z as on a
+        Cartesian mesh; along alpha the width, the depth and the edge length are scaled by the
+        main rho line of the position (:280-284, :313-317), so that grading is returned as a
+        [rho][alpha][1] array over the region."""
+        kv, ki = super()._grading_kappa(ny, pos_axes)
+        BC, sz = self._pml_bc, self._pml_sz
+        n = 1
+        if not (BC[2] == 3 or BC[3] == 3):
+            return kv, ki
+        u = self.unit
+        L = self.L[n]
+        N = int(self.N[n])
+        pos = np.asarray(pos_axes[1])[None, :]
+        rho = self.L[0][np.asarray(pos_axes[0])][:, None]
+        el = (self.md[n][pos] * u) * rho                     # Operator_Cylinder::GetEdgeLength(1, pos)
+        shape = (rho.shape[0], pos.shape[1])
+        kvn = np.zeros(shape)
+        kin = np.zeros(shape)
+        low = np.broadcast_to((pos <= sz[2]) & (BC[2] == 3), shape)
+        up = np.broadcast_to((pos >= N - 1 - sz[3]) & (BC[3] == 3), shape) & ~low
+        err = dict(divide="ignore", invalid="ignore", over="ignore")
+        if low.any():
+            width = (L[sz[2]] - L[0]) * u
+            depth = width - (L[pos] - L[0]) * u
+            width = width * rho
+            depth = depth * rho
+            if n == ny:
+                depth = depth - el / 2
+            dl = width / sz[2]
+            with np.errstate(**err):
+                g = self._grading(depth, dl, width, Z0, float(sz[2]))
+            kvn = np.where(low & (depth > 0), g, kvn)
+            if n == ny:
+                depth = depth + el / 2
+            if n != ny:
+                depth = depth - el / 2
+            depth = np.where(depth < 0, 0.0, depth)
+            with np.errstate(**err):
+                g = self._grading(depth, dl, width, Z0, float(sz[2]))
+            kin = np.where(low & (depth > 0), g, kin)
+        if up.any():
+            width = (L[N - 1] - L[N - sz[3] - 1]) * u
+            depth = width - (L[N - 1] - L[pos]) * u
+            width = width * rho
+            depth = depth * rho
+            if n == ny:
+                depth = depth + el / 2
+            with np.errstate(**err):
+                dl = width / sz[2] if sz[2] else np.full(shape, np.inf)   # the lower wall's size
+                g = self._grading(depth, dl, width, Z0, float(sz[2]))
+            kvn = np.where(up & (depth > 0), g, kvn)
+            if n == ny:
+                depth = depth - el / 2
+            if n != ny:
+                depth = depth + el / 2
+            depth = np.where(depth > width, 0.0, depth)
+            with np.errstate(**err):
+                g = self._grading(depth, dl, width, Z0, float(sz[2]))
+            kin = np.where(up & (depth > 0), g, kin)
+        kv[1] = np.nan_to_num(kvn)[:, :, None]
+        ki[1] = np.nan_to_num(kin)[:, :, None]
+        return kv, ki
 
     def _edge_geometry(self, n, pos_axes):
         P = [np.asarray(pos_axes[0]).reshape(-1, 1, 1), np.asarray(pos_axes[1]).reshape(1, -1, 1),

@@ -51,10 +51,11 @@ def test_closed_alpha_mesh_and_flags():
     # mesh and both alpha walls; rho_max and z walls stay
     op3 = _vacuum([np.arange(5.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(2,) * 6)
     assert op3.dropped_mur == [0, 2, 3] and op3.bc == [0, 2, 0, 0, 2, 2]
-    # UPML on the rho and z walls is built; on the alpha walls or at rho = 0 it is not
+    # UPML on the rho and z walls and on the alpha walls of an open mesh is built; a closed mesh
+    # has no alpha walls, and there is none at rho = 0
     for bc in ((0, 0, 3, 0, 0, 0), (0, 0, 0, 3, 0, 0)):
         with pytest.raises(ValueError):
-            _vacuum([np.arange(5.0, 20.1, 2.0), np.linspace(0.0, 1.0, 12), np.arange(0.0, 10.1, 2.0)], bc=bc)
+            _vacuum([np.arange(5.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=bc)
     with pytest.raises(ValueError):
         _vacuum([np.arange(0.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(3, 0, 0, 0, 0, 0))
 
@@ -90,6 +91,8 @@ def test_equivalent_circuit_known_answers():
 
 
 def _invariants(e, op):
+    if op.cylinder is None:          # an open alpha mesh has no seam and no axis hook
+        return
     V, I = e.read_field(0), e.read_field(1)
     # the voltage seam holds after the cylinder's post hook; an apply hook that runs after it (a
     # dispersive material on line N-2, where line 0 has no ADE, its vi being zero there, or a
@@ -206,6 +209,44 @@ def test_conducting_sheet_shields_the_coax():
     assert peak["metal"] <= peak["sheet"]
 
 
+def test_alpha_upml_grading_scales_with_rho():
+    """CalcGradingKappa along alpha on an open mesh: width, depth and the edge length are scaled by
+    the main rho line, so the grading (inversely proportional to its cell size) times rho is the
+    same on every rho line, and zero outside the PML."""
+    exc = Excitation()
+    exc.SetupGaussianPulse(8e9, 3e9)
+    o = OperatorCylinder(Structure(), Grid([np.arange(20.0, 60.1, 2.0), np.linspace(0, np.pi / 2, 61),
+                                            np.arange(0.0, 6.1, 2.0)], unit=1e-3), exc,
+                         bc=(0, 0, 3, 3, 0, 0), pml_size=(8,) * 6)
+    o.calc_ec()
+    o.dT = o.calc_timestep()
+    o._upml_regions()
+    pos_axes = [np.arange(21), np.arange(61), np.arange(4)]
+    rho = o.L[0][:, None]
+    for ny in range(3):
+        kv, ki = o._grading_kappa(ny, pos_axes)
+        for k in (kv[1][:, :, 0], ki[1][:, :, 0]):
+            # on the wall lines themselves depth == width, and whether `depth > width` holds after
+            # adding and removing half an edge length is decided by rounding, as in the reference
+            scaled = (k * rho)[:, 1:-1]
+            assert np.allclose(scaled, scaled[:1], rtol=1e-12, atol=0)
+            assert (k[:, 9:52] == 0).all() and (k[:, 1:8] > 0).all()
+
+
+def test_alpha_upml_drains_the_open_sector():
+    """A sector between PEC plates and PEC rho walls leaves only its alpha walls as a way out: with
+    a UPML there, 3000 steps after a pulse above the guide's cutoff the stored energy is below
+    1e-2 of the same sector with PEC alpha walls."""
+    steps = 3000
+    energy = {}
+    for bc in (0, 3):
+        op = configs.sector_cyl(steps=steps, alpha_bc=bc)
+        e = OracleEngine(op, steps, threads=THREADS)
+        e.IterateTS(steps)
+        energy[bc] = e.CalcFastEnergy()
+    assert energy[0] > 0 and energy[3] < 1e-2 * energy[0], energy
+
+
 def test_field_probes_on_the_cylindrical_mesh():
     """E/H point probes (ProcessFieldProbe) divide by the cylindrical GetEdgeLength: the alpha
     component by rho * dalpha (main mesh for E, dual for H)."""
@@ -237,6 +278,7 @@ def test_field_probes_on_the_cylindrical_mesh():
     ("coax_load", lambda: configs.coax_cyl(steps=300, length=400.0, load=30.0), 300),
     ("coax_rlc_load", lambda: configs.coax_cyl(steps=300, length=400.0, load=30.0, rlc=True), 300),
     ("coax_sheet", lambda: configs.coax_cyl(steps=300, length=400.0, shield="sheet"), 300),
+    ("sector_alpha_upml", lambda: configs.sector_cyl(steps=300), 300),
     ("cavity", lambda: configs.cavity_cyl(steps=600), 600),
     ("cavity_off_axis_probe", lambda: configs.cavity_cyl(steps=400, n_alpha=25, probe_r=10.0), 400),
     ("cavity_dispersive", lambda: configs.cavity_cyl(steps=400, dispersive=True), 400),
