@@ -90,6 +90,37 @@ def test_equivalent_circuit_known_answers():
         assert op.EC_L[1, i, j, k] == pytest.approx(want, rel=2e-6)
 
 
+def test_quarter_cell_average_on_a_dielectric_core():
+    """AverageMatQuarterCell with Operator_Cylinder's node areas: a z edge on the surface of a
+    dielectric core (rho < rho_i, eps_r 4) averages eps over its four neighbouring cells weighted
+    by GetNodeArea(2, pos, dual) -- annular sectors over the main rho lines and the dual alpha
+    step -- and an alpha edge there by the rho widths times the z widths."""
+    rs = np.array([4.0, 5.0, 6.5, 8.0, 10.0, 12.0])
+    al = np.linspace(0.0, 2 * np.pi, 17)
+    zs = np.array([0.0, 1.5, 3.0, 5.0, 6.0])
+    exc = Excitation()
+    exc.SetupGaussianPulse(3e9, 2e9)
+    csx = Structure()
+    i, j, k = 2, 5, 2
+    csx.AddMaterial("core", epsilon=4.0).AddBox([0.0, -1.0, -1.0], [rs[i], 7.0, 7.0])
+    op = OperatorCylinder(csx, Grid([rs, al, zs], unit=1e-3), exc)
+    e0, _, _, _ = op.eff_mat(2)
+    u = 1e-3
+    da = op.dd[1]                                   # dual alpha steps
+    a_out = lambda jj: da[jj] / 2 * ((rs[i + 1] * u) ** 2 - (rs[i] * u) ** 2)
+    a_in = lambda jj: da[jj] / 2 * ((rs[i] * u) ** 2 - (rs[i - 1] * u) ** 2)
+    want = EPS0 * (a_out(j) + 4.0 * a_in(j) + a_out(j - 1) + 4.0 * a_in(j - 1)) / (
+        a_out(j) + a_in(j) + a_out(j - 1) + a_in(j - 1))
+    assert e0[i, j, k] == pytest.approx(want, rel=1e-12)
+    # alpha edge (n = 1): quarter areas NodeWidth(z) * NodeWidth(rho) over main deltas
+    e1, _, _, _ = op.eff_mat(1)
+    dz_up, dz_dn = zs[k + 1] - zs[k], zs[k] - zs[k - 1]
+    dr_up, dr_dn = rs[i + 1] - rs[i], rs[i] - rs[i - 1]
+    want = EPS0 * (dz_up * dr_up + dz_dn * dr_up + dz_up * 4.0 * dr_dn + dz_dn * 4.0 * dr_dn) / (
+        (dz_up + dz_dn) * (dr_up + dr_dn))
+    assert e1[i, j, k] == pytest.approx(want, rel=1e-12)
+
+
 def _invariants(e, op):
     if op.cylinder is None:          # an open alpha mesh has no seam and no axis hook
         return
