@@ -537,20 +537,20 @@ def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe
 
 def sector_cyl(steps=1500, alpha_bc=3, pml=8, rho_bc=0):
     """An open quarter-circle sector in cylindrical coordinates: rho 20-60 mm (2 mm), alpha over
-    pi/2 in 61 lines, z 0-6 mm between PEC plates, ``rho_bc`` on both rho walls (PEC: the alpha
+    pi/2 in 61 lines, z 0-16 mm between PEC plates, ``rho_bc`` on both rho walls (PEC: the alpha
     walls are the only way out) and ``alpha_bc`` (3 = a UPML of ``pml`` cells) on both alpha walls;
     a soft Ez source in the middle of the sector (f0 8 GHz, fc 3 GHz: above the 3.75 GHz cutoff of
     the curved guide between the rho walls) and an Ez probe near one alpha wall."""
     from .operator_cyl import OperatorCylinder
     rs = np.arange(20.0, 60.0 + 1e-9, 2.0)
     al = np.linspace(0.0, 0.5 * np.pi, 61)
-    zs = np.arange(0.0, 6.0 + 1e-9, 2.0)
+    zs = np.arange(0.0, 16.0 + 1e-9, 2.0)
     g = Grid([rs, al, zs], unit=1e-3)
     csx = Structure()
     exc = Excitation()
     exc.SetupGaussianPulse(8e9, 3e9)
-    csx.AddExcitation("src", 0, [0, 0, 1.0]).AddBox([rs[10], al[30], zs[1]], [rs[10], al[30], zs[2]])
-    csx.AddProbe("uz", 0, interval=1).AddBox([rs[10], al[12], zs[1]], [rs[10], al[12], zs[2]])
+    csx.AddExcitation("src", 0, [0, 0, 1.0]).AddBox([rs[10], al[30], zs[4]], [rs[10], al[30], zs[5]])
+    csx.AddProbe("uz", 0, interval=1).AddBox([rs[10], al[12], zs[4]], [rs[10], al[12], zs[5]])
     op = OperatorCylinder(csx, g, exc, bc=(rho_bc, rho_bc, alpha_bc, alpha_bc, 0, 0), pml_size=(pml,) * 6)
     return op.build(steps)
 

@@ -247,12 +247,12 @@ def test_alpha_upml_grading_scales_with_rho():
     exc = Excitation()
     exc.SetupGaussianPulse(8e9, 3e9)
     o = OperatorCylinder(Structure(), Grid([np.arange(20.0, 60.1, 2.0), np.linspace(0, np.pi / 2, 61),
-                                            np.arange(0.0, 6.1, 2.0)], unit=1e-3), exc,
+                                            np.arange(0.0, 16.1, 2.0)], unit=1e-3), exc,
                          bc=(0, 0, 3, 3, 0, 0), pml_size=(8,) * 6)
     o.calc_ec()
     o.dT = o.calc_timestep()
     o._upml_regions()
-    pos_axes = [np.arange(21), np.arange(61), np.arange(4)]
+    pos_axes = [np.arange(21), np.arange(61), np.arange(9)]
     rho = o.L[0][:, None]
     for ny in range(3):
         kv, ki = o._grading_kappa(ny, pos_axes)
