@@ -218,6 +218,13 @@ int oems_cuda_add_td_dump(oems_cuda_engine* eng, int field, int interp, const un
                           unsigned int stop_ts, const double* edge_len, const double* dual_edge_len,
                           const double* coords, const char* file_prefix, int* id);
 
+/* A dump (FD or time-domain) on a cylindrical mesh (x = rho, y = alpha), without interpolation
+ * only: rho[N0] holds GetDiscLine(0, x) of the dump's mesh (main for E, dual for H) in drawing
+ * units; the raw alpha value is divided by its edge length times rho, as
+ * Operator_Cylinder::GetEdgeLength (FDTD/operator_cylinder.cpp:204-210) has it. Call before
+ * oems_cuda_init. */
+int oems_cuda_set_dump_rho(oems_cuda_engine* eng, int id, const double* rho);
+
 /* Wait until every time-domain dump sample of the steps issued so far is written to its file;
  * OEMS_ERR_IO (with oems_cuda_last_error) if a file could not be written. oems_cuda_destroy
  * also finishes the pending files. */

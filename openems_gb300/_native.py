@@ -45,6 +45,7 @@ SIGNATURES = {
     "add_current_probe": (I, [P, PU, PU, I, PI_, PI_, D, U, U, U, PI_]),
     "add_field_probe": (I, [P, I, PU, PD, D, U, U, U, PI_]),
     "set_cylinder": (I, [P, I, I, PF, PF]),
+    "set_dump_rho": (I, [P, I, PD]),
     "set_probe_dft": (I, [P, I, U, U, PD]),
     "add_fd_dump": (I, [P, I, I, PU, PU, U, U, PD, PD, PD, PI_]),
     "add_td_dump": (I, [P, I, I, PU, PU, U, U, U, PD, PD, PD, C.c_char_p, PI_]),

@@ -501,13 +501,15 @@ def coax_cyl_operator(length=1000.0, res=10.0, n_alpha=71, pml=False, load=None,
 
 
 def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe_r=0.0, dispersive=False,
-               field_probes=False):
+               field_probes=False, fd_dumps=False):
     """A pillbox cavity in cylindrical coordinates with rho = 0 on the mesh: radius 50 mm, height
     20 mm, PEC walls, a 2.5 mm rho/z mesh and 10 degree alpha steps (a closed mesh), a soft Ez
     point source off the axis (f0 3 GHz, fc 2 GHz) and an Ez voltage probe at ``probe_r`` (on the
     axis by default, where the TM010 field is largest and the axis hook computes it).
     ``dispersive``: a Drude rod on the axis and a Lorentz sector across the alpha seam.
-    ``field_probes``: E and H point probes off the axis (probe types 2 and 3), sampled every step."""
+    ``field_probes``: E and H point probes off the axis (probe types 2 and 3), sampled every step.
+    ``fd_dumps``: E and H frequency-domain dumps without interpolation at 2.3 GHz over a box
+    around the field probes' node."""
     from .operator_cyl import OperatorCylinder
     rs = np.arange(0.0, radius + 0.5 * res, res)
     al = np.linspace(0.0, 2 * np.pi, n_alpha)
@@ -524,6 +526,10 @@ def cavity_cyl(steps=20000, radius=50.0, height=20.0, res=2.5, n_alpha=37, probe
         pt = [0.4 * radius, al[5], zs[k]]
         csx.AddProbe("et", 2, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
         csx.AddProbe("ht", 3, interval=1, frequency=[2.3e9]).AddBox(pt, pt)
+    if fd_dumps:
+        lo, hi = [0.3 * radius, al[3], zs[k - 1]], [0.5 * radius, al[7], zs[k + 1]]
+        csx.AddDump("Ef", dump_type=10, dump_mode=0, frequency=[2.3e9]).AddBox(lo, hi)
+        csx.AddDump("Hf", dump_type=11, dump_mode=0, frequency=[2.3e9]).AddBox(lo, hi)
     if dispersive:
         csx.AddLorentzMaterial("drude", epsilon=1.5, eps_plasma_freq=[4e9], eps_relax_time=[1e-9]).AddBox(
             [0.0, 0.0, zs[2]], [3 * res, 2 * np.pi, zs[-3]])

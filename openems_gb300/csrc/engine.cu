@@ -576,6 +576,15 @@ int oems_cuda_set_probe_dft(oems_cuda_engine* e, int id, unsigned int fd_interva
     return OEMS_OK;
 }
 
+int oems_cuda_set_dump_rho(oems_cuda_engine* e, int id, const double* rho)
+{
+    if (!e || !rho || id < 0 || id >= (int)e->dumps.size()) return OEMS_ERR_ARG;
+    if (e->inited) return fail(e, OEMS_ERR_STATE, "engine already initialised");
+    if (e->dumps[id].interp != 0) return fail(e, OEMS_ERR_ARG, "cylindrical dumps without interpolation only");
+    e->dumps[id].rho.assign(rho, rho + e->N[0]);
+    return OEMS_OK;
+}
+
 int oems_cuda_add_fd_dump(oems_cuda_engine* e, int field, int interp, const unsigned int start[3],
                           const unsigned int stop[3], unsigned int fd_interval, unsigned int nf, const double* freqs,
                           const double* el, const double* del, int* id)
@@ -1340,6 +1349,11 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         double* del;
         if ((rc = dupload(e, &del, p.el.data(), p.el.size()))) return rc;
         d.el = del;
+        if (!p.rho.empty()) {
+            double* dr;
+            if ((rc = dupload(e, &dr, p.rho.data(), p.rho.size()))) return rc;
+            d.rho = dr;
+        }
         float2* acc;
         if ((rc = dalloc(e, &acc, std::max<size_t>(1, (size_t)d.nf * 3 * d.npos), true, true))) return rc;
         d.acc = acc;

@@ -63,6 +63,7 @@ struct DumpHost {
     unsigned fd_interval;
     std::vector<double> freqs;
     std::vector<double> el;  // edge lengths used by this field type, concatenated x,y,z
+    std::vector<double> rho; // cylindrical mesh: rho per x line of the dump's mesh (empty otherwise)
 };
 
 }  // namespace oems_host

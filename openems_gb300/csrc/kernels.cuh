@@ -890,6 +890,7 @@ struct DumpDev {
     unsigned fd_interval, nf, nsamp;
     const float2* phasor;            // [nsamp][nf], includes *2 and *dt*fd_interval
     const double* el;                // GetEdgeLength per line, concatenated x,y,z (E: main, H: dual)
+    const double* rho;               // cylindrical mesh (no interpolation): rho per x line, else null
     float2* acc;                     // [nf][3][npos]
     // time-domain dump (ProcessFieldsTD): td = 1; sample ts (ts % td_interval == 0 within
     // [td_start, td_stop]) goes to ring slot (ts / td_interval) % nslot as float [3][npos]
@@ -981,7 +982,8 @@ static __device__ void dump_field(const GridDev& g, const DumpDev& d, const unsi
     const float* F = d.field == 0 ? g.V : g.I;
     // GetRawField / GetRawDualField: value / edge length (0 for a zero length)
     auto raw = [&](int n, const unsigned* p) -> double {
-        const double delta = d.el[eoff[n] + p[n]];
+        double delta = d.el[eoff[n] + p[n]];
+        if (n == 1 && d.rho) delta = __dmul_rn(delta, d.rho[p[0]]);   // Operator_Cylinder::GetEdgeLength
         const float v = F[(unsigned long long)n * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2]];
         return delta != 0.0 ? __ddiv_rn((double)v, delta) : 0.0;
     };

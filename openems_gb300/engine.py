@@ -172,6 +172,10 @@ class EngineBase:
                                        _p(e, C.c_uint), int(d.fd_interval),
                                        fr.size, _p(fr, C.c_double), _p(el, C.c_double), _p(dl, C.c_double),
                                        C.byref(did)), "add_fd_dump")
+                rl = getattr(op, "rho_lines", None)
+                if rl is not None:         # cylindrical mesh: alpha edges scale with rho
+                    rho = self._a(rl[1] if d.dual else rl[0], np.float64)
+                    self._ck(L.set_dump_rho(self.h, did.value, _p(rho, C.c_double)), "set_dump_rho")
                 self.dump_ids.append(did.value)
             for d in td:
                 did = C.c_int(-1)

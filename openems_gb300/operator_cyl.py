@@ -108,8 +108,9 @@ class OperatorCylinder(Operator):
             # PEC (CalcPEC_Range) looks the metal up at Yee coordinates
             self._matmetal = _AlphaWrapPainter(self._matmetal, self.L[1][0], inclusive=True)
         for prop in structure.props:
-            if prop.kind == DUMP:
-                raise ValueError(f"OperatorCylinder: {prop.name}: field dumps are not built in cylindrical coordinates")
+            if prop.kind == DUMP and (prop.params["dump_type"] not in (10, 11) or prop.params["dump_mode"] != 0):
+                raise ValueError(f"OperatorCylinder: {prop.name}: on a cylindrical mesh only frequency-domain "
+                                 "dumps without interpolation are built")
             if prop.params.get("exc_type") == 10:
                 raise ValueError("OperatorCylinder: TFSF is not cylinder-safe (operator_ext_tfsf.h:40)")
         if any(len(r) > 7 and r[7] is not None for r in structure.boxes):
@@ -499,6 +500,7 @@ class OperatorCylinder(Operator):
         if device not in (None, "cpu"):
             raise ValueError("OperatorCylinder: the operator is built on the host")
         data = super().build(num_ts, device="cpu")
+        data.rho_lines = (np.array(self.L[0], np.float64), np.array(self.dl[0], np.float64))   # main, dual
         data.closed_alpha = self.closed_alpha
         data.r0_included = self.r0_included
         return data

@@ -100,6 +100,7 @@ typedef struct {
     unsigned fd_interval, nf;
     double *freqs;
     double *el[3], *del[3];
+    double *rho; /* cylindrical mesh: rho of each x line of the dump's mesh, else NULL */
     float *acc; /* [nf][3][sx][sy][sz][2] */
 } dump_t;
 
@@ -285,7 +286,7 @@ void oems_ref_destroy(eng_t *e)
     }
     for (int d = 0; d < e->ndumps; ++d) {
         dump_t *q = &e->dumps[d];
-        free(q->freqs); free(q->acc); free(q->samp_ts); free(q->samples);
+        free(q->freqs); free(q->acc); free(q->samp_ts); free(q->samples); free(q->rho);
         for (int n = 0; n < 3; ++n) { free(q->el[n]); free(q->del[n]); }
     }
     free(e);
@@ -672,6 +673,17 @@ int oems_ref_set_probe_dft(eng_t *e, int id, unsigned fd_interval, unsigned nf, 
     p->freqs = (double *)xcalloc(nf, 8);
     if (nf) memcpy(p->freqs, freqs, 8 * (size_t)nf);
     p->dft = (double *)xcalloc(2 * (size_t)nf * p->ncomp, 8);
+    return OK;
+}
+
+/* A dump on a cylindrical mesh (no interpolation only): rho of every x line of the dump's mesh
+ * (main for E, dual for H), which scales the alpha edge lengths */
+int oems_ref_set_dump_rho(eng_t *e, int id, const double *rho)
+{
+    if (!e || id < 0 || id >= e->ndumps || !rho || e->dumps[id].interp != 0)
+        return ERR_ARG;
+    free(e->dumps[id].rho);
+    e->dumps[id].rho = (double *)dupmem(rho, 8 * (size_t)e->N[0]);
     return OK;
 }
 
@@ -1293,6 +1305,16 @@ static void dump_field(eng_t *e, const dump_t *d, const unsigned pos[3], double 
     for (int n = 0; n < 3; ++n) {
         int nP = (n + 1) % 3, nPP = (n + 2) % 3;
         unsigned ip[3] = {pos[0], pos[1], pos[2]};
+        if (d->rho && d->interp == 0) {
+            /* Operator_Cylinder::GetEdgeLength (FDTD/operator_cylinder.cpp:204-210): alpha edges
+             * carry the rho of their line */
+            double delta = (d->field == 0 ? d->el[n] : d->del[n])[ip[n]];
+            if (n == 1)
+                delta = delta * d->rho[ip[0]];
+            double v = d->field == 0 ? (double)GETV(e, n, ip[0], ip[1], ip[2]) : (double)GETI(e, n, ip[0], ip[1], ip[2]);
+            out[n] = delta != 0.0 ? v / delta : 0.0;
+            continue;
+        }
         if (d->field == 0) {
 #define RAWE(p) (d->el[n][(p)[n]] ? (double)GETV(e, n, (p)[0], (p)[1], (p)[2]) / d->el[n][(p)[n]] : 0.0)
             if (d->interp == 0) {

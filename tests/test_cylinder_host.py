@@ -121,6 +121,27 @@ def test_quarter_cell_average_on_a_dielectric_core():
     assert e1[i, j, k] == pytest.approx(want, rel=1e-12)
 
 
+def test_fd_dumps_equal_field_probe_dfts_on_the_cylindrical_mesh():
+    """Frequency-domain E and H dumps without interpolation on the cylindrical mesh divide the
+    alpha component by rho times its angle, as the field probes do: at the probes' node the
+    dumps' complex<float> DFT equals the probes' double DFT within 1e-5 per component (the alpha
+    component is of the same order as the others, and off by rho without the factor)."""
+    steps = 3000
+    op = configs.cavity_cyl(steps=steps, field_probes=True, fd_dumps=True)
+    e = OracleEngine(op, steps)
+    e.IterateTS(steps)
+    assert len(e.dump_ids) == 2
+    for did, d in zip(e.dump_ids, op.dumps):
+        pid, p = next((i, q) for i, q in zip(e.fprobe_ids, op.fprobes) if q.field == d.field)
+        assert d.fd_interval == p.fd_interval and list(d.freqs) == list(p.freqs)
+        idx = [int(p.pos[a]) - int(d.start[a]) for a in range(3)]
+        dump = e.fd_dump(did)[0, :, idx[0], idx[1], idx[2]]
+        probe = e.probe_dft(pid, 1)[0]
+        big = np.abs(probe) > 1e-3 * np.abs(probe).max()
+        assert big[1], d.name                       # the alpha component carries the rho factor
+        assert (np.abs(dump - probe)[big] <= 1e-5 * np.abs(probe)[big]).all(), (d.name, dump, probe)
+
+
 def _invariants(e, op):
     if op.cylinder is None:          # an open alpha mesh has no seam and no axis hook
         return

@@ -67,7 +67,7 @@ CASES = [
     ("cavity_cyl_axis", lambda: configs.cavity_cyl(steps=400), 400),
     ("cavity_cyl_off_axis", lambda: configs.cavity_cyl(steps=300, n_alpha=25, probe_r=10.0), 300),
     ("cavity_cyl_dispersive", lambda: configs.cavity_cyl(steps=300, dispersive=True), 300),
-    ("cavity_cyl_field_probes", lambda: configs.cavity_cyl(steps=300, field_probes=True), 300),
+    ("cavity_cyl_field_probes_fd_dumps", lambda: configs.cavity_cyl(steps=300, field_probes=True, fd_dumps=True), 300),
     ("sector_cyl_alpha_upml", lambda: configs.sector_cyl(steps=300), 300),
 ]
 
