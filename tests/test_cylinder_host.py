@@ -60,6 +60,29 @@ def test_closed_alpha_mesh_and_flags():
         _vacuum([np.arange(0.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)], bc=(3, 0, 0, 0, 0, 0))
 
 
+def test_alpha_fitting_and_snapping_known_answers():
+    """FitToAlphaRange / SnapToMeshLine / SnapBox2Mesh (operator_cylinder.cpp:227-296) on a closed
+    mesh of 12 alpha steps: processing sees the distinct lines 0..N-3 only."""
+    al = np.linspace(0.0, 2 * np.pi, 13)
+    op = _vacuum([np.arange(5.0, 20.1, 2.0), al, np.arange(0.0, 10.1, 2.0)])
+    da = al[1]
+    hi = op.L[1][op._num_lines(1, False) - 1]
+    assert op._num_lines(1, False) == 12 and op._num_lines(1, True) == 14 and hi == al[11]
+    assert op.fit_to_alpha_range(1.0) == 1.0
+    assert op.fit_to_alpha_range(2 * np.pi) == pytest.approx(0.0, abs=1e-15)       # folds to 0
+    assert op.fit_to_alpha_range(3 * da + 4 * np.pi) == pytest.approx(3 * da)
+    # just below a0 moves up by 2 pi, lands above the last distinct line and is moved back
+    assert op.fit_to_alpha_range(-0.5 * da) == pytest.approx(-0.5 * da)
+    assert op.snap_line(1, 2 * np.pi)[0] == 0
+    assert op.snap_line(1, 2 * np.pi, full=True)[0] == 0                             # the fold applies
+    # the reference example's current-probe box: alpha 0..1000 clamps to the distinct lines
+    dim, s, e, _, _ = op.snap_box(np.array([0.0, 0.0, 2.0]), np.array([9.0, 1000.0, 2.0]), dual=False)
+    assert (s[1], e[1]) == (0, 11)
+    # on the full mesh (lumped elements) the span may reach the repeated lines, the fold still not
+    dim, s, e, _, _ = op.snap_box(np.array([5.0, 0.0, 2.0]), np.array([9.0, al[-2], 2.0]), full=True)
+    assert (s[1], e[1]) == (0, 11)
+
+
 def test_equivalent_circuit_known_answers():
     rs = np.array([4.0, 5.0, 6.5, 8.0, 10.0, 12.0])
     al = np.linspace(0.0, 2 * np.pi, 17)
