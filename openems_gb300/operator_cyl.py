@@ -216,20 +216,21 @@ class OperatorCylinder(Operator):
         deltaPP_M = self._raw_delta_c(pp, i_pp - 1)
         L, Lp, Lpp = self.L[a], self.L[p], self.L[pp]
 
-        def shifted(**d):
+        def shifted(offsets):
+            """The position grid moved by {axis: offset}."""
             q = list(P)
-            for ax, s in d.items():
-                q[int(ax[1])] = q[int(ax[1])] + s
+            for ax, off in offsets.items():
+                q[ax] = q[ax] + off
             return q
         cn = L + delta * 0.5
         cp_up, cp_dn = Lp + deltaP * 0.25, Lp - deltaP_M * 0.25
         cpp_up, cpp_dn = Lpp + deltaPP * 0.25, Lpp - deltaPP_M * 0.25
-        samples = [(cp_up, cpp_up, {}), (cp_dn, cpp_up, {f"a{p}": -1}),
-                   (cp_up, cpp_dn, {f"a{pp}": -1}), (cp_dn, cpp_dn, {f"a{p}": -1, f"a{pp}": -1})]
+        samples = [(cp_up, cpp_up, {}), (cp_dn, cpp_up, {p: -1}),
+                   (cp_up, cpp_dn, {pp: -1}), (cp_dn, cpp_dn, {p: -1, pp: -1})]
         eps_acc = kap_acc = area = None
         for cpv, cppv, sh in samples:
             e, k = self._lookup(n, cn, cpv, cppv, ("epsilon", "kappa"))
-            A = np.broadcast_to(self._node_area_i(n, shifted(**sh), True), e.shape)
+            A = np.broadcast_to(self._node_area_i(n, shifted(sh), True), e.shape)
             if eps_acc is None:
                 eps_acc, kap_acc, area = e * A, k * A, A.copy()
             else:
@@ -242,7 +243,7 @@ class OperatorCylinder(Operator):
         cppm = Lpp + deltaPP * 0.5
         with np.errstate(divide="ignore", invalid="ignore"):
             mu_dn, sg_dn = self._lookup(n, L - delta_M * 0.25, cpm, cppm, ("mue", "sigma"))
-            Ddn = np.broadcast_to(self._node_width_i(n, shifted(**{f"a{a}": -1}), True), mu_dn.shape)
+            Ddn = np.broadcast_to(self._node_width_i(n, shifted({a: -1}), True), mu_dn.shape)
             eff2 = Ddn / mu_dn
             eff3 = np.where(sg_dn != 0, Ddn / np.where(sg_dn != 0, sg_dn, 1.0), 0.0)
             length = Ddn
