@@ -16,7 +16,8 @@ alpha edges are rho times their angle (GetEdgeLength, :204-210), z faces are ann
   the summed capacitance and conductance of every z edge on the axis; metal on the axis zeroes
   them.  A mesh that includes rho = 0 uses the conservative Var1 timestep (CalcTimestep, :88-95).
 
-Built here: materials (eps, kappa, mue, sigma), metal (PEC), soft/hard and weighted excitations,
+Built here: materials (eps, kappa, mue, sigma) and metal (PEC) on boxes and on cylinder primitives
+whose axis is the z axis, soft/hard and weighted excitations,
 Mur walls that the reference accepts in cylindrical coordinates (operator_ext_mur_abc.cpp:47-54;
 the others are dropped as there, leaving PEC), UPML on the rho and z walls and on the alpha
 walls of an open mesh (graded with rho along alpha), Drude/Lorentz
@@ -28,6 +29,7 @@ field probes.  Not built for this mesh: TFSF (rejected by the reference too) and
 """
 from __future__ import annotations
 
+import copy
 import math
 from dataclasses import dataclass
 
@@ -101,6 +103,7 @@ class OperatorCylinder(Operator):
             if (ny == 0 and not top and (self.r0_included or self.closed_alpha)) or (ny == 1 and self.closed_alpha):
                 bc[w] = 0
                 self.dropped_mur.append(w)
+        structure = self._axial_boxes(structure)
         super().__init__(structure, Grid(lines, unit=grid.unit), excitation, bc=bc, **kw)
         self._mat_raw, self._matmetal_raw = self._mat, self._matmetal
         if self.closed_alpha:
@@ -113,8 +116,30 @@ class OperatorCylinder(Operator):
                                  "dumps without interpolation are built")
             if prop.params.get("exc_type") == 10:
                 raise ValueError("OperatorCylinder: TFSF is not cylinder-safe (operator_ext_tfsf.h:40)")
-        if any(len(r) > 7 and r[7] is not None for r in structure.boxes):
-            raise ValueError("OperatorCylinder: cylinder primitives are Cartesian; use boxes in (rho, alpha, z)")
+
+
+    @staticmethod
+    def _axial_boxes(structure):
+        """CSXCAD's cylinder primitives are Cartesian. A cylinder (or shell) whose axis is the z
+        axis is the box rho <= R (|rho - R| <= width/2) over every alpha in (rho, alpha, z), and is
+        painted as that box; others are rejected.  Works on a shallow copy of the structure."""
+        recs = []
+        for r in structure.boxes:
+            shape = r[7] if len(r) > 7 else None
+            if shape is None:
+                recs.append(r)
+                continue
+            a, pb, pc, radius, width = shape
+            if a != 2 or pb != 0.0 or pc != 0.0:
+                raise ValueError("OperatorCylinder: only cylinder primitives on the z axis are built; "
+                                 "use boxes in (rho, alpha, z)")
+            r_lo, r_hi = (0.0, radius) if width is None else (radius - 0.5 * width, radius + 0.5 * width)
+            lo = np.array([max(r_lo, 0.0), -1e30, r[0][2]])
+            hi = np.array([r_hi, 1e30, r[1][2]])
+            recs.append((lo, hi) + tuple(r[2:7]) + (None,))
+        out = copy.copy(structure)
+        out.boxes = recs
+        return out
 
     # ---- geometry on index arrays (all lengths in metres) -------------------------------------
     def _line(self, k, idx, dual):

@@ -83,6 +83,37 @@ def test_alpha_fitting_and_snapping_known_answers():
     assert (s[1], e[1]) == (0, 11)
 
 
+def test_z_axis_cylinder_primitives_paint_as_rho_boxes():
+    """A Cartesian cylinder (and shell) on the z axis is the rho range over every alpha: the
+    operator equals the one built from the equivalent (rho, alpha, z) boxes, bit for bit; an
+    off-axis cylinder is rejected."""
+    al = np.linspace(0.0, 2 * np.pi, 25)
+    lines = [np.arange(0.0, 20.1, 1.0), al, np.arange(0.0, 10.1, 1.0)]
+
+    def build(use_cyl):
+        exc = Excitation()
+        exc.SetupGaussianPulse(3e9, 2e9)
+        csx = Structure()
+        rod = csx.AddMaterial("rod", epsilon=3.0, kappa=0.01)
+        shell = csx.AddMetal("shell")
+        if use_cyl:
+            rod.AddCylinder([0, 0, 2.0], [0, 0, 8.0], 6.5, priority=1)
+            shell.AddCylindricalShell([0, 0, 0.0], [0, 0, 10.0], 15.0, 2.0, priority=2)
+        else:
+            rod.AddBox([0, -1e30, 2.0], [6.5, 1e30, 8.0], priority=1)
+            shell.AddBox([14.0, -1e30, 0.0], [16.0, 1e30, 10.0], priority=2)
+        return OperatorCylinder(csx, Grid(lines, unit=1e-3), exc).build(20)
+    a, b = build(True), build(False)
+    for k in ("vv", "vi", "ii", "iv"):
+        assert bits_equal(getattr(a, k), getattr(b, k)), k
+    exc = Excitation()
+    exc.SetupGaussianPulse(3e9, 2e9)
+    csx = Structure()
+    csx.AddMaterial("off", epsilon=2.0).AddCylinder([3.0, 0, 2.0], [3.0, 0, 8.0], 1.0)
+    with pytest.raises(ValueError):
+        OperatorCylinder(csx, Grid(lines, unit=1e-3), exc)
+
+
 def test_equivalent_circuit_known_answers():
     rs = np.array([4.0, 5.0, 6.5, 8.0, 10.0, 12.0])
     al = np.linspace(0.0, 2 * np.pi, 17)
