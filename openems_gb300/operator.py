@@ -1105,6 +1105,10 @@ class Operator:
         Dh, Bp, Bpp = _bcast(n, self.dd[a][pos_axes[a]] * u, self.md[p][pos_axes[p]] * u, self.md[pp][pos_axes[pp]] * u)
         return De, Ap * App, Dh, Bp * Bpp
 
+    def _weight_coords(self, cs, x, y, z):
+        """The Yee coordinates (drawing units) an excitation weight function is evaluated at."""
+        return float(cs[0][x]), float(cs[1][y]), float(cs[2][z])
+
     def _yee_painter(self, kinds):
         """Property lookup at Yee coordinates (GetYeeCoords + GetPropertyByCoordPriority)."""
         return _Painter(self.csx, kinds)
@@ -1260,7 +1264,7 @@ class Operator:
                     ex = prop.params["exc_val"][n]
                     wf = prop.params.get("weight")
                     if wf is not None:       # GetWeightedExcitation at the Yee point (drawing units)
-                        ex = ex * float(wf[n](float(cs[0][x]), float(cs[1][y]), float(cs[2][z])))
+                        ex = ex * float(wf[n](*self._weight_coords(cs, x, y, z)))
                     amp = ex * self._edge_length(n, (x, y, z))
                     if amp != 0:
                         vrec.append((z, y, x, n, amp, int(prop.params["delay"] / self.dT)))

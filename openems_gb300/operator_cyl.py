@@ -440,6 +440,17 @@ class OperatorCylinder(Operator):
         l_stop = np.array([stop[0], a_stop, stop[2]], np.float64)
         return super().snap_box(l_start, l_stop, dual, method, full)
 
+    def _weight_coords(self, cs, x, y, z):
+        """GetYeeCoords folds alpha from a0 + 2*pi on back by 2*pi on a closed mesh (:119-129)."""
+        r, a, zz = super()._weight_coords(cs, x, y, z)
+        if self.closed_alpha:
+            a0 = float(self.L[1][0])
+            if a >= a0 + TWO_PI:
+                a -= TWO_PI
+            elif a < a0:
+                a += TWO_PI
+        return r, a, zz
+
     def _yee_painter(self, kinds):
         p = super()._yee_painter(kinds)
         return _AlphaWrapPainter(p, self.L[1][0], inclusive=True) if self.closed_alpha else p

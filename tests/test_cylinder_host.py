@@ -114,6 +114,25 @@ def test_z_axis_cylinder_primitives_paint_as_rho_boxes():
         OperatorCylinder(csx, Grid(lines, unit=1e-3), exc)
 
 
+def test_excitation_weights_see_folded_alpha():
+    """An excitation weight is evaluated at GetYeeCoords, which folds alpha from a0 + 2 pi on:
+    with a weight linear in alpha, the source on line N-2 (a0 + 2 pi) gets the weight of line 0."""
+    al = np.linspace(0.0, 2 * np.pi, 13)
+    exc = Excitation()
+    exc.SetupGaussianPulse(3e9, 2e9)
+    csx = Structure()
+    w = (lambda r, a, z: 0.0, lambda r, a, z: 0.0, lambda r, a, z: 1.0 + a)
+    csx.AddExcitation("src", 0, [0, 0, 1.0], weight=w).AddBox([10.0, 0.0, 4.0], [10.0, 2 * np.pi, 6.0])
+    op = OperatorCylinder(csx, Grid([np.arange(5.0, 20.1, 1.0), al, np.arange(0.0, 10.1, 1.0)], unit=1e-3),
+                          exc).build(10)
+    t = op.exc
+    amp = {(int(t.volt_index[1, i]), int(t.volt_index[2, i])): float(t.volt_amp[i]) for i in range(t.volt_amp.size)}
+    N = len(al) + 1
+    for z in (4, 5):
+        assert amp[(N - 2, z)] == amp[(0, z)]
+        assert amp[(3, z)] == pytest.approx(amp[(0, z)] * (1.0 + al[3]))
+
+
 def test_equivalent_circuit_known_answers():
     rs = np.array([4.0, 5.0, 6.5, 8.0, 10.0, 12.0])
     al = np.linspace(0.0, 2 * np.pi, 17)
