@@ -133,6 +133,24 @@ def test_excitation_weights_see_folded_alpha():
         assert amp[(3, z)] == pytest.approx(amp[(0, z)] * (1.0 + al[3]))
 
 
+@pytest.mark.parametrize("dump_type,dump_mode,ok", [(10, 0, True), (11, 0, True), (10, 1, False),
+                                                    (11, 2, False), (0, 0, False), (1, 1, False)])
+def test_which_field_dumps_a_cylindrical_mesh_builds(dump_type, dump_mode, ok):
+    """Frequency-domain dumps without interpolation are built; interpolated ones and time-domain
+    dumps (whose reference files are Cartesian structured grids) are rejected."""
+    exc = Excitation()
+    exc.SetupGaussianPulse(3e9, 2e9)
+    csx = Structure()
+    csx.AddDump("d", dump_type=dump_type, dump_mode=dump_mode, frequency=[1e9]).AddBox([6.0, 0.0, 1.0], [9.0, 1.0, 5.0])
+    g = Grid([np.arange(5.0, 20.1, 1.0), np.linspace(0.0, 2 * np.pi, 13), np.arange(0.0, 10.1, 1.0)], unit=1e-3)
+    if ok:
+        op = OperatorCylinder(csx, g, exc).build(10)
+        assert len(op.dumps) == 1 and op.dumps[0].interp == 0 and op.rho_lines[0][0] == 5.0
+    else:
+        with pytest.raises(ValueError):
+            OperatorCylinder(csx, g, exc)
+
+
 def test_equivalent_circuit_known_answers():
     rs = np.array([4.0, 5.0, 6.5, 8.0, 10.0, 12.0])
     al = np.linspace(0.0, 2 * np.pi, 17)
