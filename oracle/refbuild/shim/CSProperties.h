@@ -1,0 +1,2 @@
+/* ORACLE BUILD SHIM (test infrastructure only): see ContinuousStructure.h. */
+#include "ContinuousStructure.h"
