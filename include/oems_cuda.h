@@ -278,7 +278,8 @@ int oems_cuda_energy(oems_cuda_engine* eng, double* energy);
 
 /* Allocation-free variant of the energy reduction, with no counterpart in the reference. It
  * serves callers that must not call cudaMalloc: their device memory is owned by a host
- * framework's pool or arena, or they run inside CUDA stream capture. The caller passes its own
+ * framework's pool or arena (a raw allocation would bypass its accounting), or their deployment
+ * forbids device allocation after start-up. The caller passes its own
  * device fields volt_dev/curr_dev, float [3][Nx][Ny][z_stride] with z_stride >= Nz, and a host
  * `energy`. The reduction uses a fixed 128 KB scratch array that is part of the library image,
  * so the entry point allocates nothing. Limit: Nx-1 <= OEMS_NOALLOC_MAX_PLANES x-planes; larger

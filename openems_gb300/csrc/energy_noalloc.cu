@@ -3,8 +3,8 @@
 // Who this is for: callers whose device memory is owned by someone else and who therefore must
 // not call cudaMalloc themselves. Examples are a host framework that hands out all device
 // memory from its own caching pool or arena (a raw cudaMalloc would bypass its accounting and
-// can fail once the pool has reserved the card), code running inside CUDA stream capture (where
-// cudaMalloc is not allowed), and deployments that forbid runtime allocation after start-up.
+// can fail once the pool has reserved the card), and deployments that forbid runtime allocation
+// after start-up.  The call reads the result back and synchronizes the caller's stream.
 // Such a caller already holds the voltage and current fields in device memory; this entry point
 // reduces them with scratch that is part of the library image instead of allocated memory.
 //
@@ -117,9 +117,13 @@ extern "C" int oems_cuda_energy_noalloc(const float* volt_dev, const float* curr
     if (rc != OEMS_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     k_plane_energy<<<Nx - 1, 256, 0, s>>>(volt_dev, curr_dev, Nx, Ny, Nz, z_stride, scratch);
+    cudaError_t c = cudaGetLastError();
+    if (c != cudaSuccess) return OEMS_ERR_CUDA;   // nothing launched: do not read stale scratch
     k_sum_planes<<<1, 32, 0, s>>>(Nx - 1, scratch);
+    c = cudaGetLastError();
+    if (c != cudaSuccess) return OEMS_ERR_CUDA;
     double eh[2] = {0.0, 0.0};
-    cudaError_t c = cudaMemcpyAsync(eh, scratch + 2 * kMaxPlanes, sizeof(eh), cudaMemcpyDeviceToHost, s);
+    c = cudaMemcpyAsync(eh, scratch + 2 * kMaxPlanes, sizeof(eh), cudaMemcpyDeviceToHost, s);
     if (c == cudaSuccess) c = cudaStreamSynchronize(s);
     if (c != cudaSuccess) { cudaGetLastError(); return OEMS_ERR_CUDA; }
     *energy = 8.85418781762e-12 * eh[0] + 1.256637062e-6 * eh[1];

@@ -35,7 +35,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .operator import DUMP, EPS0, METAL, MUE0, Z0, Grid, Operator, _axes
+from .operator import DUMP, EPS0, MATERIAL, METAL, MUE0, Z0, Grid, Operator, _axes
 
 CLOSED_ALPHA_THRESHOLD = 1e-6     # OPERATOR_CYLINDER_CLOSED_ALPHA_THRESHOLD (operator_cylinder.h:21)
 TWO_PI = 2.0 * math.pi
@@ -130,6 +130,11 @@ class OperatorCylinder(Operator):
                 recs.append(r)
                 continue
             a, pb, pc, radius, width = shape
+            if r[4].kind not in (MATERIAL, METAL):
+                # excitations, probes, dumps, lumped elements and sheets snap their property's own
+                # box list, which keeps the Cartesian bounding box of the primitive
+                raise ValueError(f"OperatorCylinder: {r[4].name}: cylinder primitives are built for "
+                                 "materials and metal only; give this property boxes in (rho, alpha, z)")
             if a != 2 or pb != 0.0 or pc != 0.0:
                 raise ValueError("OperatorCylinder: only cylinder primitives on the z axis are built; "
                                  "use boxes in (rho, alpha, z)")
@@ -445,9 +450,11 @@ class OperatorCylinder(Operator):
         r, a, zz = super()._weight_coords(cs, x, y, z)
         if self.closed_alpha:
             a0 = float(self.L[1][0])
+            # two independent tests in the reference's order: a value that rounding leaves below
+            # a0 after the first fold is folded back up by the second
             if a >= a0 + TWO_PI:
                 a -= TWO_PI
-            elif a < a0:
+            if a < a0:
                 a += TWO_PI
         return r, a, zz
 
