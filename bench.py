@@ -13,8 +13,15 @@ e2e     = the same metric through the C ABI with host buffers: per step one oems
 roofline= algorithmic bytes of the dominant kernel (36 B per cell per half-step update: read the
           updated field, read the other field, write the updated field) over its average
           CUDA-event duration, against the measured HBM copy bandwidth
-cpu_baseline = the multithreaded SSE-compressed engine restated on the host cores
-          (oracle port, all cores) on a bounded number of steps of the same workload
+cpu_baseline = openEMS's multithreaded SSE-compressed engine on the host cores (all cores) on a
+          bounded number of steps of the same workload: the reference's own engine compiled from
+          its sources (oracle/_ref) where that build exists on the host, else the C restatement
+          of it (oracle port); ``kind`` says which.  cpu_thread_sweep repeats it at 1, 2, 4, ...
+          threads.
+configs = the 100^3 vacuum cube and the 160x160x80 patch (UPML, lumped port, NF2FF boxes) on the
+          GPU: both largely L2-resident, so they report MCells/s only
+e2e_job = the whole stress job as a user runs it: operator build, engine setup, the
+          configuration's 2000 steps with every probe sample read back, teardown
 
 Multi-GPU: replicas only (one independent simulation per rank, no collective on the data path);
 ``value`` is the sum over ranks.
@@ -130,10 +137,27 @@ def build_workload(name, shape=None):
     raise SystemExit(f"unknown workload {name}")
 
 
-def cpu_baseline(op, steps_cap, budget_s, threads):
-    """Multithreaded SSE-compressed restatement (oracle port) on the host cores."""
+def cpu_engine(op, max_ts, threads):
+    """The CPU engine timed as the reference: openEMS's own multithreaded engine compiled from
+    its sources (oracle/_ref) where it was built on this host, else the C restatement of it
+    (the oracle port; the reference sources are not on every host).  Returns (engine, kind)."""
+    try:
+        from oracle import refengine
+        if refengine.available():
+            return refengine.RefEngine(op, max_ts, kind="multithread", threads=threads), "reference"
+    except Exception:
+        pass
     from oracle.oracle import OracleEngine
-    eng = OracleEngine(op, steps_cap + 2, threads=threads)
+    return OracleEngine(op, max_ts, threads=threads), "port"
+
+
+def cpu_baseline(op, steps_cap, budget_s, threads, engine=None):
+    """openEMS's multithreaded SSE-compressed engine on the host cores, stepping like its
+    processing loop (one step, then the probes)."""
+    if engine is None:
+        eng, kind = cpu_engine(op, steps_cap + 2, threads)
+    else:
+        eng, kind = engine
     eng.IterateTS(1)                        # warm-up step (threads started, pages touched)
     n = 0
     t0 = time.perf_counter()
@@ -145,7 +169,56 @@ def cpu_baseline(op, steps_cap, budget_s, threads):
     dt = time.perf_counter() - t0
     eng.close()
     cells = float(np.prod(op.num_lines.astype(np.float64)))
-    return cells * n / dt / 1e6, n, dt
+    return cells * n / dt / 1e6, n, dt, kind
+
+
+def cpu_thread_sweep(op, budget_s, nproc):
+    """The CPU engine at 1, 2, 4, ... threads up to nproc (a bounded sample of steps each)."""
+    out = {}
+    t = 1
+    counts = []
+    while t < nproc:
+        counts.append(t)
+        t *= 2
+    counts.append(nproc)
+    for t in counts:
+        v, n, sec, kind = cpu_baseline(op, 50, budget_s, t)
+        out[str(t)] = {"mcells_s": round(v, 1), "steps": n, "seconds": round(sec, 2), "kind": kind}
+    return out
+
+
+def measure_config(name, steps, e2e_steps=200):
+    """One more configuration on the GPU: device-timed MCells/s over `steps` replayed steps, and
+    MCells/s end to end through the C ABI (iterate(1) + a synchronous read of every probe's new
+    sample per step, openEMS's processing loop)."""
+    from openems_gb300.engine import Engine_CUDA
+    from openems_gb300.operator import build_device
+    t0 = time.perf_counter()
+    with build_device("cuda" if name != "design" else "cpu"):
+        op, desc = build_workload(name)
+    t_build = time.perf_counter() - t0
+    cells = float(np.prod(op.num_lines.astype(np.float64)))
+    eng = Engine_CUDA(op, steps + e2e_steps + 16)
+    eng.IterateTS(5)
+    eng.sync()
+    ms = eng.timed_iterate(steps)
+    pids = eng.vprobe_ids + eng.iprobe_ids
+    slot = eng.GetNumberOfTimesteps()
+    t1 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eng.IterateTS(1)
+        slot += 1
+        for pid in pids:
+            eng.probe_range(pid, slot, 1)
+    e2e_s = time.perf_counter() - t1
+    state_mb = 24 * cells / 1e6
+    out = {"workload": desc, "cells": cells, "steps": steps, "mcells_s": cells * steps / (ms / 1e3) / 1e6,
+           "ms_per_step": ms / steps, "e2e_mcells_s": cells * e2e_steps / e2e_s / 1e6, "e2e_steps": e2e_steps,
+           "build_s": round(t_build, 2), "launches_per_step": eng.launches_per_step(),
+           "l2": "field state %.0f MB against a 129 MB L2: largely L2-resident, so no HBM fraction is claimed"
+                 % state_mb}
+    eng.close()
+    return out
 
 
 def measure_batched(count):
@@ -310,9 +383,8 @@ def run_reference(args, op, desc, rank):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    from oracle.oracle import OracleEngine
     cells = float(np.prod(op.num_lines.astype(np.float64)))
-    eng = OracleEngine(op, args.steps + args.warmup + 2, threads=threads)
+    eng, kind = cpu_engine(op, args.steps + args.warmup + 2, threads)
     eng.IterateTS(max(args.warmup, 1))
     t0 = time.perf_counter()
     done = 0
@@ -330,8 +402,9 @@ def run_reference(args, op, desc, rank):
         "steps": done, "warmup": args.warmup, "ms_per_step": dt / done * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "cells": cells},
-        "cpu_baseline": {"value": v, "unit": "MCells/s", "cores": threads, "kind": "port",
-                         "sample": f"{done} timesteps of the full workload (bounded to {budget:.0f} s)"},
+        "cpu_baseline": {"value": v, "unit": "MCells/s", "cores": threads, "kind": kind,
+                         "sample": f"{done} timesteps of the full workload (bounded to {budget:.0f} s), "
+                                   "one step then the probes, as openEMS's processing loop runs"},
         "e2e": {"value": v, "unit": "MCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -353,6 +426,11 @@ def main():
     ap.add_argument("--no-nf2ff", action="store_true", help="skip the NF2FF far-field measurement")
     ap.add_argument("--adjoint-steps", type=int, default=8000,
                     help="timesteps of the differentiable-form measurement (8000 = its configuration)")
+    ap.add_argument("--no-configs", action="store_true", help="skip the 100^3 cube and patch measurements")
+    ap.add_argument("--no-cpu-sweep", action="store_true", help="skip the CPU thread sweep")
+    ap.add_argument("--sweep-budget", type=float, default=3.0, help="seconds per thread count of the CPU sweep")
+    ap.add_argument("--job-steps", type=int, default=2000,
+                    help="steps of the whole-job measurement (2000 = the stress configuration's)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -440,6 +518,32 @@ def main():
     launches = eng.launches_per_step()
     eng.close()
 
+    # ---- the whole job as a user runs it: operator build, engine setup, the configuration's
+    # steps in openEMS's processing style (probe samples read back every step), teardown --------
+    e2e_job = None
+    if rank == 0 and args.workload == "stress" and args.job_steps > 0:
+        t0 = time.perf_counter()
+        with build_device(dev):
+            jop, _ = build_workload(args.workload, shape)
+        t1 = time.perf_counter()
+        jeng = Engine_CUDA(jop, args.job_steps + 2)
+        t2 = time.perf_counter()
+        jp = jeng.vprobe_ids + jeng.iprobe_ids
+        jslot = 0
+        for _ in range(args.job_steps):
+            jeng.IterateTS(1)
+            jslot += 1
+            for pid in jp:
+                jeng.probe_range(pid, jslot, 1)
+        t3 = time.perf_counter()
+        jeng.close()
+        t4 = time.perf_counter()
+        e2e_job = {"value": cells * args.job_steps / (t4 - t0) / 1e6, "unit": "MCells/s",
+                   "steps": args.job_steps, "seconds": round(t4 - t0, 3), "build_s": round(t1 - t0, 3),
+                   "engine_setup_s": round(t2 - t1, 3), "steps_s": round(t3 - t2, 3),
+                   "teardown_s": round(t4 - t3, 3),
+                   "note": "operator build + engine setup + every step with its probe samples read back + teardown"}
+
     batched = None
     if rank == 0 and not args.no_batch:
         batched = measure_batched(args.batch_count)
@@ -452,12 +556,19 @@ def main():
     if rank == 0 and not args.no_nf2ff:
         nf2ff = measure_nf2ff()
 
+    others = None
+    if rank == 0 and not args.no_configs:
+        others = {"plain_100": measure_config("plain", 2000), "patch_160x160x80": measure_config("patch", 1000)}
+
     base = None
+    sweep = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, n, sec = cpu_baseline(op, 50, args.cpu_budget, threads)
-        base = {"value": v, "unit": "MCells/s", "cores": threads, "kind": "port",
+        v, n, sec, kind = cpu_baseline(op, 50, args.cpu_budget, threads)
+        base = {"value": v, "unit": "MCells/s", "cores": threads, "kind": kind,
                 "sample": f"{n} timesteps of the full {desc} workload ({sec:.1f} s, setup excluded)"}
+        if not args.no_cpu_sweep:
+            sweep = cpu_thread_sweep(op, args.sweep_budget, threads)
 
     if rank == 0:
         line = {
@@ -471,7 +582,10 @@ def main():
                 "engine_setup_s": round(t_setup, 1)},
             "roofline": roofline,
             "cpu_baseline": base,
+            "cpu_thread_sweep": sweep,
             "e2e": e2e,
+            "e2e_job": e2e_job,
+            "configs": others,
             "clocks": clocks,
             "gpu_launches": launches * args.steps,
             "launches_per_step": launches,

@@ -272,6 +272,13 @@ int oems_cuda_read_probe_dft(oems_cuda_engine* eng, int probe_id, double* out);
 /* FD dump: complex<float> [num_freqs][3][sx][sy][sz] as interleaved re/im floats. */
 int oems_cuda_read_fd_dump(oems_cuda_engine* eng, int dump_id, float* out, size_t cap_floats);
 
+/* ProcessFieldsFD::DumpFDData with the VTK file type (Common/processfields_fd.cpp:114-215): writes
+ * the accumulated FD dump as VTK XML rectilinear-grid files, per frequency 21 phase snapshots
+ * <prefix>_f=<freq>_p=<degrees>.vtr plus <prefix>_f=<freq>_abs.vtr and _arg.vtr, with the
+ * reference's names and complex<float> arithmetic.  coords: the sample coordinates in metres,
+ * x then y then z (sx + sy + sz values).  Errors writing a file give OEMS_ERR_IO. */
+int oems_cuda_write_fd_dump(oems_cuda_engine* eng, int dump_id, const char* prefix, const double* coords);
+
 /* Engine_Interface_FDTD::CalcFastEnergy (FDTD/engine_interface_fdtd.cpp:302-347):
  * eps0*sum(V^2) + mu0*sum(I^2) over [0,N-1)^3, device reduction in double. */
 int oems_cuda_energy(oems_cuda_engine* eng, double* energy);

@@ -73,6 +73,7 @@ CUDA_ONLY = {
     "profile_steps": (I, [P, U, PF, PU]),
     "read_probe_range": (I, [P, I, SZ, SZ, PD]),
     "flush_dumps": (I, [P]),
+    "write_fd_dump": (I, [P, I, C.c_char_p, PD]),
     "energy_noalloc": (I, [P, P, PU, U, P, PD]),
     "batch_create": (I, [C.POINTER(P), U, C.POINTER(P)]),
     "batch_run": (I, [P, PU, U, U]),

@@ -249,6 +249,9 @@ int oems_cuda_create(const unsigned int num_lines[3], double dt, int device, oem
     e->dt = dt;
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&e->stream_r, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
     int rc;
     if ((rc = dalloc(e, &e->dV, 3 * (size_t)e->S, true, true))) return rc;
     if ((rc = dalloc(e, &e->dI, 3 * (size_t)e->S, true, true))) return rc;
@@ -268,6 +271,9 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     if (e->graphK) cudaGraphExecDestroy(e->graphK);
     oems_adjoint_free(e->adj);
     for (void* p : e->allocs) cudaFree(p);
+    if (e->stream_r) { cudaStreamSynchronize(e->stream_r); cudaStreamDestroy(e->stream_r); }
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -708,6 +714,12 @@ void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp)
     }
     sp.main_cells = rest ? sp.n[0] * sp.n[1] * sp.n[2] : 0;
     sp.main_blocks = (sp.main_cells + 255) / 256;
+    // four z cells per thread in the main box of the compressed forward kernels: the box's z range
+    // on multiples of four, 32-bit offsets (the adjoint kernels keep one cell per thread)
+    sp.v4 = (!sp.full && sp.main_cells && e->compressed && e->vec4 && 3ull * e->S < (1ull << 32) &&
+             sp.lo[2] % 4 == 0 && sp.n[2] % 4 == 0) ? 1 : 0;
+    sp.main_cells4 = sp.v4 ? sp.main_cells / 4 : 0;
+    sp.main_blocks4 = (sp.main_cells4 + 255) / 256;
     sp.first_block[0] = 0;
     for (int r = 0; r < g.nupml; ++r) sp.first_block[r + 1] = sp.first_block[r] + (g.upml[r].n + 255) / 256;
 }
@@ -727,6 +739,23 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
     const bool mur = !curr && !e->mur.empty() && !e->mur_separate;
     if (e->use_split) {
         const SplitDev& sp = curr ? e->splitI : e->splitV;
+        if (sp.v4 && !mur && e->stream_r) {
+            // region blocks on a branch stream, the main box four cells per thread on this one
+            const unsigned rb = sp.first_block[sp.nreg];
+            cudaEventRecord(e->ev_fork, s);
+            cudaStreamWaitEvent(e->stream_r, e->ev_fork, 0);
+            if (rb) {
+                if (curr) k_update_split<true, true><<<rb, 256, 0, e->stream_r>>>(g, sp, m, ts);
+                else k_update_split<true, false><<<rb, 256, 0, e->stream_r>>>(g, sp, m, ts);
+            }
+            if (sp.main_blocks4) {
+                if (curr) k_update_box4<true><<<sp.main_blocks4, 256, 0, s>>>(g, sp);
+                else k_update_box4<false><<<sp.main_blocks4, 256, 0, s>>>(g, sp);
+            }
+            cudaEventRecord(e->ev_join, e->stream_r);
+            cudaStreamWaitEvent(s, e->ev_join, 0);
+            return;
+        }
         const unsigned blocks = sp.main_blocks + sp.first_block[sp.nreg];
         if (!blocks) return;
         if (e->compressed) {
@@ -754,6 +783,9 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
             if (o32 && e->vec4 && mode == 0) {
                 const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
                 k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
+            } else if (o32 && e->vec4 && mode == 2 && e->mur_v4) {
+                const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
+                k_update_v4m<unsigned><<<gv4, 256, 0, s>>>(g, m, ts);
             } else if (o32) {
                 if (mode == 2) launch_v<true, false, 2, unsigned>(gv, s, g, m, ts);
                 else if (mode == 1) launch_v<true, false, 1, unsigned>(gv, s, g, m, ts);
@@ -1085,6 +1117,10 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         bool always = true;
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
         md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
+        // the float4 form needs each z wall's line and shift in one aligned group of four z
+        e->mur_v4 = md.lanes != 0;
+        for (int q = 0; q < md.nz && q < 2; ++q)
+            e->mur_v4 = e->mur_v4 && (md.z[q].line & ~3u) == (md.z[q].shift & ~3u);
     }
 
     // cylinder extension

@@ -86,6 +86,10 @@ void td_free(oems_cuda_engine* e);
 struct oems_cuda_engine {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // branch stream of the UPML split (region blocks beside the float4 main box) and its fork
+    // and join events
+    cudaStream_t stream_r = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     unsigned N[3] = {0, 0, 0};
     unsigned Pz = 0;
     unsigned long long S = 0;
@@ -164,6 +168,9 @@ struct oems_cuda_engine {
     bool mur_separate = false;
     // float4 forms of the update kernels (4 z cells per thread) where they exist
     bool vec4 = true;
+    // the float4 voltage update carries the lane-parallel Mur hooks (k_update_v4m): every z
+    // wall's line and shift lie in one float4
+    bool mur_v4 = false;
     // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
     // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
     // whenever the host sees it

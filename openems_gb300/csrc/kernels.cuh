@@ -440,14 +440,10 @@ __device__ __forceinline__ void set4(float4& v, int k, float a)
     if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
 }
 
+// four current cells (x, y, z0..z0+3) of the compressed operator without UPML
 template <typename IX = unsigned>
-__global__ void __launch_bounds__(256) k_update_i4(GridDev g)
+__device__ __forceinline__ void update_i4_cells(const GridDev& g, unsigned x, unsigned y, unsigned z0)
 {
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned pz4 = g.Pz >> 2;
-    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
-    if (y + 1 >= g.Ny || z0 + 1 >= g.Nz) return;
     const IX S = (IX)g.S;
     const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
     const IX sx = (IX)g.Ny * g.Pz;
@@ -478,20 +474,27 @@ __global__ void __launch_bounds__(256) k_update_i4(GridDev g)
     *reinterpret_cast<float4*>(I + (2 * S + o)) = a2;
 }
 
+template <typename IX = unsigned>
+__global__ void __launch_bounds__(256) k_update_i4(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned pz4 = g.Pz >> 2;
+    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
+    if (y + 1 >= g.Ny || z0 + 1 >= g.Nz) return;
+    update_i4_cells<IX>(g, x, y, z0);
+}
+
 // Vectorised voltage update of the compressed operator without UPML and without Mur walls, four
 // consecutive z cells per thread (see k_update_i4).  The -z neighbour of lane k is lane k-1, of
 // lane 0 the float before the vector (the cell itself at z = 0, the reference's "same cell"
 // read).  Lanes past z = Nz-1 are padding and keep their zero.  (With Mur walls the hooks make a
 // float4 form no faster than the one-cell form on GB300: the wall lanes of every row serialise
 // their warps, and a separate pass over the scattered row ends costs as much.)
+// four voltage cells (x, y, z0..z0+3) of the compressed operator without UPML and Mur hooks
 template <typename IX = unsigned>
-__global__ void __launch_bounds__(256) k_update_v4(GridDev g)
+__device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, unsigned y, unsigned z0)
 {
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned pz4 = g.Pz >> 2;
-    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
-    if (y >= g.Ny || z0 >= g.Nz) return;
     const IX S = (IX)g.S;
     const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
     const IX sx = x ? (IX)g.Ny * g.Pz : (IX)0;
@@ -523,6 +526,136 @@ __global__ void __launch_bounds__(256) k_update_v4(GridDev g)
     *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
 }
 
+template <typename IX = unsigned>
+__global__ void __launch_bounds__(256) k_update_v4(GridDev g)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned pz4 = g.Pz >> 2;
+    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
+    if (y >= g.Ny || z0 >= g.Nz) return;
+    update_v4_cells<IX>(g, x, y, z0);
+}
+
+// k_update_v4 with the Mur pre/post voltage hooks of the lane-parallel wall form (MurDev::lanes:
+// every wall active from step 0, at most two z walls).  The host chooses it only when each z
+// wall's line and shift lie in one float4, so the thread owning them holds V_old(line),
+// V_old(shift) and V_new(shift) itself and forms the wall value
+//   b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift)
+// (FDTD/extensions/engine_ext_mur_abc.cpp:83-149) in registers: in a direct column it becomes the
+// line's final value in the same float4 store, elsewhere it goes to the wall buffer for k_mur's
+// apply and the line lanes of components 0 and 1 stay unwritten.  x/y walls use mur_cell per lane
+// (their shift cells read V_old(line) of another thread's cell, which therefore keeps its
+// tangential components unwritten).  Only the threads of wall cells do extra work; their old
+// values are read again from memory, which still holds them until the thread's own store.
+// the x/y wall hooks of the four lanes of a float4 voltage update (kept out of line: only the
+// threads of cells next to x/y walls run it, and it needs many registers)
+static __device__ __noinline__ void mur_xy_lanes(const GridDev& g, const MurDev& m, unsigned ts, unsigned x, unsigned y,
+                                          unsigned z0, unsigned long long o, const float4 n0, const float4 n1,
+                                          const float4 n2, unsigned& km0, unsigned& km1, unsigned& km2)
+{
+    const float* V = g.V;
+    const float4 a0 = ld4(V + o), a1 = ld4(V + (g.S + o)), a2 = ld4(V + (2 * g.S + o));   // still V_old
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (z0 + k >= g.Nz) break;
+        const unsigned keep = mur_cell<2>(g, m, ts, x, y, z0 + k, o + k, f4(a0, k), f4(a1, k), f4(a2, k), f4(n0, k),
+                                          f4(n1, k), f4(n2, k));
+        if (!(keep & 1u)) km0 &= ~(1u << k);
+        if (!(keep & 2u)) km1 &= ~(1u << k);
+        if (!(keep & 4u)) km2 &= ~(1u << k);
+    }
+}
+
+template <typename IX = unsigned>
+__global__ void __launch_bounds__(256, 4) k_update_v4m(GridDev g, MurDev m, const unsigned* __restrict__ numTS)
+{
+    const unsigned x = blockIdx.y;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned pz4 = g.Pz >> 2;
+    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
+    if (y >= g.Ny || z0 >= g.Nz) return;
+    const IX S = (IX)g.S;
+    const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
+    const IX sx = x ? (IX)g.Ny * g.Pz : (IX)0;
+    const IX sy = y ? (IX)g.Pz : (IX)0;
+    const float* __restrict__ I = g.I;
+    float* __restrict__ V = g.V;
+    // z walls whose line and shift are lanes of this float4 (bit q = wall m.z[q])
+    unsigned zw = 0;
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+        if (q < m.nz && (m.z[q].line & ~3u) == z0) zw |= 1u << q;
+    const bool xyw = mur_wall_cell<2>(m, x, y, 0u);
+    const unsigned kc = x * g.Ny + y;
+    // start the wall coefficients on their way to L1 (a prefetch holds no register)
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+        if (zw & (1u << q)) {
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(m.z[q].cP + kc));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(m.z[q].cPP + kc));
+        }
+    const float4 i0 = ldg4(I + o), i1 = ldg4(I + (S + o)), i2 = ldg4(I + (2 * S + o));
+    const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
+    const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
+    const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (z0 + k >= g.Nz) break;
+        const float4 ca = __ldg(g.tabV + 2 * cls[k]), cb = __ldg(g.tabV + 2 * cls[k] + 1);
+        const float i1z = k ? f4(i1, k - 1) : i1m, i0z = k ? f4(i0, k - 1) : i0m;
+        const float c0 = fadd(fsub(fsub(f4(i2, k), f4(i2y, k)), f4(i1, k)), i1z);
+        const float c1 = fadd(fsub(fsub(f4(i0, k), i0z), f4(i2, k)), f4(i2x, k));
+        const float c2 = fadd(fsub(fsub(f4(i1, k), f4(i1x, k)), f4(i0, k)), f4(i0y, k));
+        set4(n0, k, fadd(fmul(f4(n0, k), ca.x), fmul(ca.w, c0)));
+        set4(n1, k, fadd(fmul(f4(n1, k), ca.y), fmul(cb.x, c1)));
+        set4(n2, k, fadd(fmul(f4(n2, k), ca.z), fmul(cb.y, c2)));
+    }
+    // store masks: bit k of km[c] = lane k of component c is written
+    unsigned km0 = 15u, km1 = 15u, km2 = 15u;
+    if (xyw) mur_xy_lanes(g, m, __ldg(numTS), x, y, z0, (unsigned long long)o, n0, n1, n2, km0, km1, km2);
+    if (zw) {
+        const float4 a0 = ld4(V + o), a1 = ld4(V + (S + o));   // still V_old
+        const bool direct = mur_z_direct(m, x, y);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!(zw & (1u << q))) continue;
+            const int kl = (int)(m.z[q].line - z0), ks = (int)(m.z[q].shift - z0);
+            const float cP = __ldg(m.z[q].cP + kc), cPP = __ldg(m.z[q].cPP + kc);
+            const float b0 = fadd(fsub(f4(a0, ks), fmul(cP, f4(a0, kl))), fmul(cP, f4(n0, ks)));
+            const float b1 = fadd(fsub(f4(a1, ks), fmul(cPP, f4(a1, kl))), fmul(cPP, f4(n1, ks)));
+            if (direct) {
+                set4(n0, kl, b0);
+                set4(n1, kl, b1);
+            } else {
+                m.z[q].bP[kc] = b0;
+                m.z[q].bPP[kc] = b1;
+                km0 &= ~(1u << kl);
+                km1 &= ~(1u << kl);
+            }
+        }
+    }
+    // lanes past Nz-1 are padding: they keep their zero either way
+    if (km0 == 15u) *reinterpret_cast<float4*>(V + o) = n0;
+    else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) if (km0 & (1u << k)) V[o + k] = f4(n0, k);
+    }
+    if (km1 == 15u) *reinterpret_cast<float4*>(V + (S + o)) = n1;
+    else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) if (km1 & (1u << k)) V[S + o + k] = f4(n1, k);
+    }
+    if (km2 == 15u) *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
+    else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) if (km2 & (1u << k)) V[2 * S + o + k] = f4(n2, k);
+    }
+}
+
 template <bool COMPRESSED, bool UPML, typename IX = unsigned long long>
 __global__ void __launch_bounds__(256) k_update_i(GridDev g)
 {
@@ -533,16 +666,24 @@ __global__ void __launch_bounds__(256) k_update_i(GridDev g)
     update_i_cell<COMPRESSED, UPML, false, IX>(g, x, y, z);
 }
 
-// Work split for meshes with UPML regions: blocks [0, main_blocks) map the cells outside every
-// region (a box when the regions are boundary slabs, else the whole range with UPML cells
-// skipped), the following blocks map the cells of each region in region order.  Every warp then
-// runs one code path, and region cells read their fluxes with region-local coalesced offsets.
+// Work split for meshes with UPML regions: the first blocks map the cells of each region in
+// region order, the following blocks the cells outside every region (a box when the regions are
+// boundary slabs, else the whole range with UPML cells skipped).  Every warp then runs one code
+// path, and region cells read their fluxes with region-local coalesced offsets.  The region blocks
+// come first because they carry the longer dependent load chains (class index, then the class
+// table, then the fluxes): started first, they overlap with the streaming main blocks instead of
+// forming the launch's tail.  With v4 the host launches only the region blocks of this kernel and
+// walks the main box with k_update_box4 on a parallel branch, four z cells per thread (the float4
+// bodies of the plain kernels; the box's z range starts and ends on multiples of four): the two
+// kernels need different register budgets, and as separate launches they run side by side.
 struct SplitDev {
     unsigned lo[3], n[3];                      // main part: this box of cells
     unsigned main_cells, main_blocks;
     int full;                                  // 1: the box is the whole update range, skip UPML cells
+    int v4;                                    // 1: main box four z cells per thread (k_update_box4)
+    unsigned main_cells4, main_blocks4;        // groups of four and their blocks when v4
     unsigned nreg;
-    unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1]) after main
+    unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1])
 };
 
 // The compressed-operator form without Mur hooks fits 32 registers (a few bytes spill to L1), so
@@ -551,9 +692,10 @@ template <bool COMPRESSED, bool CURR, bool MUR = false>
 __global__ void __launch_bounds__(256, (COMPRESSED && !MUR) ? 8 : 1)
     k_update_split(GridDev g, SplitDev sp, MurDev m, const unsigned* __restrict__ numTS)
 {
-
     unsigned b = blockIdx.x;
-    if (b < sp.main_blocks) {
+    const unsigned rblocks = sp.first_block[sp.nreg];
+    if (b >= rblocks) {
+        b -= rblocks;
         unsigned t = b * 256u + threadIdx.x;
         if (t >= sp.main_cells) return;
         const unsigned z = sp.lo[2] + t % sp.n[2];
@@ -569,7 +711,6 @@ __global__ void __launch_bounds__(256, (COMPRESSED && !MUR) ? 8 : 1)
         else update_v_cell<COMPRESSED, false>(g, x, y, z);
         return;
     }
-    b -= sp.main_blocks;
     int r = 0;
     while (r + 1 < (int)sp.nreg && b >= sp.first_block[r + 1]) ++r;
     const UpmlDev& u = g.upml[r];
@@ -584,6 +725,21 @@ __global__ void __launch_bounds__(256, (COMPRESSED && !MUR) ? 8 : 1)
         if (MUR && mur_wall_cell(m, x, y, z)) update_v_cell<COMPRESSED, true, false, 1>(g, x, y, z, r, loc, &m, __ldg(numTS));
         else update_v_cell<COMPRESSED, true>(g, x, y, z, r, loc);
     }
+}
+
+// The main box of a UPML split, four z cells per thread (compressed operator, no Mur hooks).
+template <bool CURR>
+__global__ void __launch_bounds__(256) k_update_box4(GridDev g, SplitDev sp)
+{
+    unsigned t = blockIdx.x * 256u + threadIdx.x;
+    if (t >= sp.main_cells4) return;
+    const unsigned n4 = sp.n[2] >> 2;
+    const unsigned z = sp.lo[2] + ((t % n4) << 2);
+    t /= n4;
+    const unsigned y = sp.lo[1] + t % sp.n[1];
+    const unsigned x = sp.lo[0] + t / sp.n[1];
+    if (CURR) update_i4_cells<unsigned>(g, x, y, z);
+    else update_v4_cells<unsigned>(g, x, y, z);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -27,6 +27,8 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <cmath>
+#include <complex>
 #include <vector>
 
 #include "engine_impl.h"
@@ -86,15 +88,13 @@ struct oems_td_pipeline {
 
 namespace {
 
-// one sample as a VTK XML RectilinearGrid file (raw appended data, UInt64 block headers)
-int write_vtr(const TdDump& d, unsigned ts, const float* data, std::string& err)
+// a vector field float [3][sx][sy][sz] (z fastest) on a rectilinear grid as a VTK XML
+// RectilinearGrid file (raw appended data, UInt64 block headers); coords = x, y, z lines
+int write_vtr_file(const std::string& path, const char* name, const unsigned dims[3], const double* coords,
+                   const float* data, std::string& err)
 {
-    char tsbuf[32];
-    std::snprintf(tsbuf, sizeof(tsbuf), "%08u", ts);
-    const std::string path = d.prefix + "_" + tsbuf + ".vtr";
-    const unsigned sx = d.sz[0], sy = d.sz[1], sz = d.sz[2];
-    const size_t npos = d.npos;
-    const char* name = d.field == 0 ? "E-Field" : "H-Field";
+    const unsigned sx = dims[0], sy = dims[1], sz = dims[2];
+    const size_t npos = (size_t)sx * sy * sz;
     const uint16_t probe = 1;
     unsigned char lo;
     std::memcpy(&lo, &probe, 1);
@@ -150,9 +150,9 @@ int write_vtr(const TdDump& d, unsigned ts, const float* data, std::string& err)
         ok = ok && (n == 0 || std::fwrite(p, 1, (size_t)n, f) == (size_t)n);
     };
     block(pts.data(), nf);
-    block(d.coords.data(), nx);
-    block(d.coords.data() + sx, ny);
-    block(d.coords.data() + sx + sy, nz);
+    block(coords, nx);
+    block(coords + sx, ny);
+    block(coords + sx + sy, nz);
     const char* tail = "\n  </AppendedData>\n</VTKFile>\n";
     ok = ok && std::fwrite(tail, 1, std::strlen(tail), f) == std::strlen(tail);
     ok = (std::fclose(f) == 0) && ok;
@@ -161,6 +161,15 @@ int write_vtr(const TdDump& d, unsigned ts, const float* data, std::string& err)
         return OEMS_ERR_IO;
     }
     return OEMS_OK;
+}
+
+// one time-domain sample: <prefix>_<numTS, 8 digits>.vtr
+int write_vtr(const TdDump& d, unsigned ts, const float* data, std::string& err)
+{
+    char tsbuf[32];
+    std::snprintf(tsbuf, sizeof(tsbuf), "%08u", ts);
+    return write_vtr_file(d.prefix + "_" + tsbuf + ".vtr", d.field == 0 ? "E-Field" : "H-Field", d.sz,
+                          d.coords.data(), data, err);
 }
 
 void writer_loop(oems_td_pipeline* p)
@@ -352,4 +361,52 @@ void td_free(oems_cuda_engine* e)
         }
     delete p;
     e->td = nullptr;
+}
+
+// ProcessFieldsFD::DumpFDData for the VTK file type (Common/processfields_fd.cpp:114-215): per
+// frequency, 21 phase snapshots real(F * exp(j * 2 pi p / 21)), the magnitude |F| and the phase
+// arg(F) of every component, as <prefix>_f=<freq>_p=<degrees, 3 digits>.vtr, ..._abs.vtr and
+// ..._arg.vtr.  The frequency is written as an integer when it is one, else with six decimals
+// (std::to_string), and the arithmetic is the reference's complex<float> arithmetic.
+extern "C" int oems_cuda_write_fd_dump(oems_cuda_engine* e, int id, const char* prefix, const double* coords)
+{
+    if (!e || !prefix || !prefix[0] || !coords || id < 0 || id >= (int)e->dumps.size()) return OEMS_ERR_ARG;
+    if (!e->inited) return OEMS_ERR_STATE;
+    const DumpHost& h = e->dumps[id];
+    if (h.td) return OEMS_ERR_ARG;
+    unsigned dims[3];
+    size_t npos = 1;
+    for (int a = 0; a < 3; ++a) {
+        dims[a] = h.stop[a] - h.start[a] + 1;
+        npos *= dims[a];
+    }
+    const size_t nf = h.freqs.size();
+    std::vector<float> acc(nf * 3 * npos * 2);
+    int rc = oems_cuda_read_fd_dump(e, id, acc.data(), acc.size());
+    if (rc != OEMS_OK) return rc;
+    const char* name = h.field == 0 ? "E-Field" : "H-Field";
+    std::vector<float> out(3 * npos);
+    std::string err;
+    const int Nr_Ph = 21;
+    for (size_t f = 0; f < nf; ++f) {
+        const double freq = h.freqs[f];
+        const std::string sf = (freq - (long)freq) == 0 ? std::to_string((long)freq) : std::to_string(freq);
+        const std::complex<float>* F = reinterpret_cast<const std::complex<float>*>(acc.data()) + f * 3 * npos;
+        for (int p = 0; p < Nr_Ph; ++p) {
+            const double angle = 2.0 * M_PI * p / Nr_Ph;
+            const std::complex<float> ejw = std::exp((std::complex<float>)(std::complex<double>(0.0, 1.0) * angle));
+            for (size_t q = 0; q < 3 * npos; ++q) out[q] = std::real(F[q] * ejw);
+            char deg[16];
+            std::snprintf(deg, sizeof(deg), "%03d", (int)(angle * 180 / M_PI));
+            rc = write_vtr_file(std::string(prefix) + "_f=" + sf + "_p=" + deg + ".vtr", name, dims, coords, out.data(), err);
+            if (rc != OEMS_OK) { e->err = err; return rc; }
+        }
+        for (size_t q = 0; q < 3 * npos; ++q) out[q] = std::abs(F[q]);
+        rc = write_vtr_file(std::string(prefix) + "_f=" + sf + "_abs.vtr", name, dims, coords, out.data(), err);
+        if (rc != OEMS_OK) { e->err = err; return rc; }
+        for (size_t q = 0; q < 3 * npos; ++q) out[q] = std::arg(F[q]);
+        rc = write_vtr_file(std::string(prefix) + "_f=" + sf + "_arg.vtr", name, dims, coords, out.data(), err);
+        if (rc != OEMS_OK) { e->err = err; return rc; }
+    }
+    return OEMS_OK;
 }

@@ -303,6 +303,20 @@ class Engine_CUDA(EngineBase):
             raise EngineError(f"oems_cuda_create failed: {_native.ERRORS.get(rc, rc)} {msg!r}")
         super().__init__(lib, h, op, max_timesteps, max_classes, dump_path)
 
+    def write_fd_dump(self, did: int, prefix: Optional[str] = None):
+        """Write FD dump `did` as the reference's VTK files (<prefix>_f=<freq>_p=<deg>.vtr,
+        _abs, _arg); the prefix defaults to <dump_path>/<dump name>."""
+        d = self.op.dumps[self.dump_ids.index(did)]
+        g = self.op.grid
+        from .operator import _dual_line
+        lines = [(_dual_line(np.asarray(l, np.float64)) if d.dual else np.asarray(l, np.float64)) * g.unit
+                 for l in g.lines]
+        xyz = np.ascontiguousarray(np.concatenate([lines[a][int(d.start[a]):int(d.stop[a]) + 1] for a in range(3)]),
+                                   np.float64)
+        if prefix is None:
+            prefix = os.path.join(self.dump_path, d.name)
+        self._ck(self.lib.write_fd_dump(self.h, int(did), prefix.encode(), _p(xyz, C.c_double)), "write_fd_dump")
+
     def flush_dumps(self):
         """Wait until every time-domain dump file of the steps issued so far is written."""
         self._ck(self.lib.flush_dumps(self.h), "flush_dumps")
