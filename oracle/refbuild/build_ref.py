@@ -111,5 +111,31 @@ def build(force: bool = False) -> list:
     return out
 
 
+BINDING_SRC = os.path.join(os.path.dirname(ORACLE), "openems_gb300", "binding", "engine_cuda.cpp")
+CUDA_LIB_DIR = os.path.join(os.path.dirname(ORACLE), "openems_gb300", "_build")
+INCLUDE = os.path.join(os.path.dirname(ORACLE), "include")
+
+
+def build_binding() -> str:
+    """Compile the openEMS-side binding (openems_gb300/binding/engine_cuda.cpp) against the
+    reference's headers and link it with the reference's engine objects and the CUDA engine
+    library, every symbol resolved (-z defs): the proof that the drop-in boundary builds inside
+    openEMS.  Returns the library path ('' when the reference tree is absent)."""
+    if not available():
+        return ""
+    libs = build()
+    odir = os.path.join(OUT, "obj_" + os.path.basename(libs[1]).split(".")[0])
+    objs = [os.path.join(odir, f) for f in sorted(os.listdir(odir)) if f.endswith(".o") and not f.startswith("harness")]
+    path = os.path.join(OUT, "liboems_engine_cuda_binding.so")
+    bobj = os.path.join(OUT, "engine_cuda_binding.o")
+    _compile(BINDING_SRC, bobj, ["-I", INCLUDE, "-DOEMS_SHIM_ARCH_NOT_X86"])
+    cmd = (["g++", "-shared", "-pthread", "-Wl,-z,defs", "-o", path, bobj] + objs +
+           ["-L", CUDA_LIB_DIR, "-loems_cuda", "-Wl,-rpath," + CUDA_LIB_DIR])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"linking the binding failed:\n{r.stderr[-4000:]}")
+    return path
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv) or "reference tree not found: nothing built")
