@@ -239,14 +239,17 @@ __global__ void __launch_bounds__(256) k_adj_w(AdjDev a)
     adj_w_cell(a, blockIdx.y, y, z, -2, 0);
 }
 
-// the engine's UPML work split (k_update_split): interior blocks, then the region blocks
+// the engine's UPML work split (k_update_split): the region blocks first, then the blocks of the
+// cells outside every region (a launch of the first first_block[nreg] blocks covers the regions
+// alone, while k_adj_box4_* walk the main box on a parallel branch)
 template <bool CURR>
 __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
 {
     const GridDev& g = a.g;
     unsigned b = blockIdx.x;
-    if (b < sp.main_blocks) {
-        unsigned t = b * 256u + threadIdx.x;
+    const unsigned rblocks = sp.first_block[sp.nreg];
+    if (b >= rblocks) {
+        unsigned t = (b - rblocks) * 256u + threadIdx.x;
         if (t >= sp.main_cells) return;
         const unsigned z = sp.lo[2] + t % sp.n[2];
         t /= sp.n[2];
@@ -260,7 +263,6 @@ __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
         else adj_w_cell(a, x, y, z, -1, 0);
         return;
     }
-    b -= sp.main_blocks;
     int r = 0;
     while (r + 1 < (int)sp.nreg && b >= sp.first_block[r + 1]) ++r;
     const UpmlDev& u = g.upml[r];
@@ -274,6 +276,111 @@ __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
     } else {
         adj_w_cell(a, x, y, z, r, loc);
     }
+}
+
+// The main box of the split (compressed operator, no UPML cell in it), four z cells per thread:
+// adj_u_cell / adj_w_cell's arithmetic per lane, with the float4 loads of the forward's
+// update_*4_cells.  Lane k is cell z0 + k; the box's z range is a multiple of four from a
+// multiple of four, and its cells are interior to the update range of each half-step.
+__global__ void __launch_bounds__(256, 4) k_adj_box4_u(AdjDev a, SplitDev sp)
+{
+    unsigned t = blockIdx.x * 256u + threadIdx.x;
+    if (t >= sp.main_cells4) return;
+    const unsigned n4 = sp.n[2] >> 2;
+    const unsigned z0 = sp.lo[2] + ((t % n4) << 2);
+    t /= n4;
+    const unsigned y = sp.lo[1] + t % sp.n[1];
+    const unsigned x = sp.lo[0] + t / sp.n[1];
+    const GridDev& g = a.g;
+    const unsigned S = (unsigned)g.S;
+    const unsigned o = (x * g.Ny + y) * g.Pz + z0;
+    const unsigned sx = g.Ny * g.Pz, sy = g.Pz;
+    const float* __restrict__ W = a.W;
+    const float4 w0 = ldg4(W + o), w1 = ldg4(W + (S + o)), w2 = ldg4(W + (2 * S + o));
+    const float w1z4 = __ldg(W + (S + o + 4)), w0z4 = __ldg(W + (o + 4));
+    const float4 w2y = ldg4(W + (2 * S + o + sy)), w0y = ldg4(W + (o + sy));
+    const float4 w2x = ldg4(W + (2 * S + o + sx)), w1x = ldg4(W + (S + o + sx));
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    float4 u0 = ld4(a.U + o), u1 = ld4(a.U + (S + o)), u2 = ld4(a.U + (2 * S + o));
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    const bool src = a.injI.count && (unsigned long long)o + 3 >= a.injI.lo && (unsigned long long)o <= a.injI.hi;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const unsigned z = z0 + k;
+        const float4 ca = __ldg(g.tabI + 2 * cls[k]), cb = __ldg(g.tabI + 2 * cls[k] + 1);
+        const float a1z = k < 3 ? f4(w1, k + 1) : w1z4, a0z = k < 3 ? f4(w0, k + 1) : w0z4;
+        float d[3] = {
+            fadd(fsub(fsub(z > 0 ? f4(w1, k) : 0.f, a1z), y > 0 ? f4(w2, k) : 0.f), f4(w2y, k)),
+            fadd(fsub(fsub(x > 0 ? f4(w2, k) : 0.f, f4(w2x, k)), z > 0 ? f4(w0, k) : 0.f), a0z),
+            fadd(fsub(fsub(y > 0 ? f4(w0, k) : 0.f, f4(w0y, k)), x > 0 ? f4(w1, k) : 0.f), f4(w1x, k))};
+        if (src) add_sources(a, a.injI, (unsigned long long)o + k, d);
+        set4(u0, k, fadd(fmul(ca.x, f4(u0, k)), fmul(ca.w, d[0])));
+        set4(u1, k, fadd(fmul(ca.y, f4(u1, k)), fmul(cb.x, d[1])));
+        set4(u2, k, fadd(fmul(ca.z, f4(u2, k)), fmul(cb.y, d[2])));
+    }
+    *reinterpret_cast<float4*>(a.U + o) = u0;
+    *reinterpret_cast<float4*>(a.U + (S + o)) = u1;
+    *reinterpret_cast<float4*>(a.U + (2 * S + o)) = u2;
+}
+
+__global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
+{
+    unsigned t = blockIdx.x * 256u + threadIdx.x;
+    if (t >= sp.main_cells4) return;
+    const unsigned n4 = sp.n[2] >> 2;
+    const unsigned z0 = sp.lo[2] + ((t % n4) << 2);
+    t /= n4;
+    const unsigned y = sp.lo[1] + t % sp.n[1];
+    const unsigned x = sp.lo[0] + t / sp.n[1];
+    const GridDev& g = a.g;
+    const unsigned S = (unsigned)g.S;
+    const unsigned o = (x * g.Ny + y) * g.Pz + z0;
+    const unsigned sx = x ? g.Ny * g.Pz : 0u, sy = y ? g.Pz : 0u;
+    const float* __restrict__ U = a.U;
+    const float4 u0 = ldg4(U + o), u1 = ldg4(U + (S + o)), u2 = ldg4(U + (2 * S + o));
+    const float u1m = z0 ? __ldg(U + (S + o - 1)) : 0.f, u0m = z0 ? __ldg(U + (o - 1)) : 0.f;
+    const float4 u2y = ldg4(U + (2 * S + o - sy)), u0y = ldg4(U + (o - sy));
+    const float4 u2x = ldg4(U + (2 * S + o - sx)), u1x = ldg4(U + (S + o - sx));
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    float4 n0 = ld4(a.W + o), n1 = ld4(a.W + (S + o)), n2 = ld4(a.W + (2 * S + o));
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    const bool src = a.injV.count && (unsigned long long)o + 3 >= a.injV.lo && (unsigned long long)o <= a.injV.hi;
+    const unsigned bx = x - a.b0[0], by = y - a.b0[1];
+    const bool inbox = bx < a.bn[0] && by < a.bn[1];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const unsigned z = z0 + k;
+        const float4 ca = __ldg(g.tabV + 2 * cls[k]), cb = __ldg(g.tabV + 2 * cls[k] + 1);
+        // -z neighbours: lane k-1, for lane 0 the float before the vector (none at z = 0)
+        const float b1z = k ? f4(u1, k - 1) : u1m, b0z = k ? f4(u0, k - 1) : u0m;
+        float gs[3] = {
+            fadd(fsub(fsub(f4(u1, k), z ? b1z : 0.f), f4(u2, k)), y ? f4(u2y, k) : 0.f),
+            fsub(fadd(fsub(f4(u2, k), x ? f4(u2x, k) : 0.f), z ? b0z : 0.f), f4(u0, k)),
+            fadd(fsub(fsub(f4(u0, k), y ? f4(u0y, k) : 0.f), f4(u1, k)), x ? f4(u1x, k) : 0.f)};
+        if (src) add_sources(a, a.injV, (unsigned long long)o + k, gs);
+        const float vv[3] = {ca.x, ca.y, ca.z}, vi[3] = {ca.w, cb.x, cb.y};
+        const float wn[3] = {fadd(fmul(vv[0], f4(n0, k)), fmul(vi[0], gs[0])),
+                             fadd(fmul(vv[1], f4(n1, k)), fmul(vi[1], gs[1])),
+                             fadd(fmul(vv[2], f4(n2, k)), fmul(vi[2], gs[2]))};
+        set4(n0, k, wn[0]);
+        set4(n1, k, wn[1]);
+        set4(n2, k, wn[2]);
+        const unsigned bz = z - a.b0[2];
+        if (inbox && bz < a.bn[2]) {
+            const unsigned kb = (bx * a.bn[1] + by) * a.bn[2] + bz;
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                if (vi[m] == 0.f) continue;                     // PEC edge: no dependence
+                const float b = fmul(wn[m], __frcp_rn(vi[m]));
+                const unsigned kk = m * a.B + kb;
+                a.gvv[kk] += (double)fmul(b, __ldg(a.fv + kk));
+                a.gvi[kk] += (double)fmul(b, __ldg(a.fc + kk));
+            }
+        }
+    }
+    *reinterpret_cast<float4*>(a.W + o) = n0;
+    *reinterpret_cast<float4*>(a.W + (S + o)) = n1;
+    *reinterpret_cast<float4*>(a.W + (2 * S + o)) = n2;
 }
 
 // V^n and K_V I^n (the arithmetic of update_v_cell) in the design box, into slot
@@ -327,6 +434,10 @@ struct oems_adjoint_state {
     cudaStream_t rs = nullptr;
     cudaEvent_t ev_recomputed[2] = {nullptr, nullptr};
     cudaEvent_t ev_reversed[2] = {nullptr, nullptr};
+    // UPML split with a float4 main box: the region blocks of each reverse half-step run on
+    // `rb` beside the main box, forked from and joined back to the sweep's stream
+    cudaStream_t rb = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     float fwd_ms = 0.f, bwd_ms = 0.f;
     unsigned launches_per_reverse_step = 0;
 };
@@ -531,6 +642,12 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     if ((rc = aalloc(e, s, &s->rec_numTS, 1))) return rc;
     if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess)
         return afail(e, OEMS_ERR_CUDA, "adjoint events");
+    if (e->use_split && e->compressed && e->splitI.v4 && e->splitV.v4) {
+        if (cudaStreamCreateWithFlags(&s->rb, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return afail(e, OEMS_ERR_CUDA, "adjoint branch stream");
+    }
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) return afail(e, OEMS_ERR_CUDA, "adjoint setup sync");
     return OEMS_OK;
 }
@@ -640,7 +757,26 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         d.n = n;
         d.fv = slot;
         d.fc = slot + 3 * d.B;
-        if (e->use_split) {
+        if (e->use_split && s->rb) {
+            // per half-step: region blocks on the branch stream, the main box four cells per
+            // thread on the sweep's stream, joined before the next half-step reads the result
+            const SplitDev* sp[2] = {&e->splitI, &e->splitV};
+            for (int h = 0; h < 2; ++h) {
+                const unsigned rblk = sp[h]->first_block[sp[h]->nreg];
+                cudaEventRecord(s->ev_fork, rst);
+                cudaStreamWaitEvent(s->rb, s->ev_fork, 0);
+                if (rblk) {
+                    if (h == 0) k_adj_split<true><<<rblk, 256, 0, s->rb>>>(d, *sp[h]);
+                    else k_adj_split<false><<<rblk, 256, 0, s->rb>>>(d, *sp[h]);
+                }
+                if (sp[h]->main_blocks4) {
+                    if (h == 0) k_adj_box4_u<<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
+                    else k_adj_box4_w<<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
+                }
+                cudaEventRecord(s->ev_join, s->rb);
+                cudaStreamWaitEvent(rst, s->ev_join, 0);
+            }
+        } else if (e->use_split) {
             if (bu) k_adj_split<true><<<bu, 256, 0, rst>>>(d, e->splitI);
             if (bw) k_adj_split<false><<<bw, 256, 0, rst>>>(d, e->splitV);
         } else {
@@ -704,6 +840,7 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         cudaStreamSynchronize(st);
     }
     if (s->rs) cudaStreamSynchronize(s->rs);
+    if (s->rb) cudaStreamSynchronize(s->rb);
     release();
     d.src = nullptr;
     d.injV = InjList{};
@@ -735,5 +872,8 @@ void oems_adjoint_free(oems_adjoint_state* s)
         if (s->ev_reversed[b]) cudaEventDestroy(s->ev_reversed[b]);
     }
     if (s->rs) cudaStreamDestroy(s->rs);
+    if (s->rb) cudaStreamDestroy(s->rb);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     delete s;
 }

@@ -537,38 +537,20 @@ __global__ void __launch_bounds__(256) k_update_v4(GridDev g)
     update_v4_cells<IX>(g, x, y, z0);
 }
 
-// k_update_v4 with the Mur pre/post voltage hooks of the lane-parallel wall form (MurDev::lanes:
-// every wall active from step 0, at most two z walls).  The host chooses it only when each z
-// wall's line and shift lie in one float4, so the thread owning them holds V_old(line),
-// V_old(shift) and V_new(shift) itself and forms the wall value
-//   b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift)
-// (FDTD/extensions/engine_ext_mur_abc.cpp:83-149) in registers: in a direct column it becomes the
-// line's final value in the same float4 store, elsewhere it goes to the wall buffer for k_mur's
-// apply and the line lanes of components 0 and 1 stay unwritten.  x/y walls use mur_cell per lane
-// (their shift cells read V_old(line) of another thread's cell, which therefore keeps its
-// tangential components unwritten).  Only the threads of wall cells do extra work; their old
-// values are read again from memory, which still holds them until the thread's own store.
-// the x/y wall hooks of the four lanes of a float4 voltage update (kept out of line: only the
-// threads of cells next to x/y walls run it, and it needs many registers)
-static __device__ __noinline__ void mur_xy_lanes(const GridDev& g, const MurDev& m, unsigned ts, unsigned x, unsigned y,
-                                          unsigned z0, unsigned long long o, const float4 n0, const float4 n1,
-                                          const float4 n2, unsigned& km0, unsigned& km1, unsigned& km2)
-{
-    const float* V = g.V;
-    const float4 a0 = ld4(V + o), a1 = ld4(V + (g.S + o)), a2 = ld4(V + (2 * g.S + o));   // still V_old
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        if (z0 + k >= g.Nz) break;
-        const unsigned keep = mur_cell<2>(g, m, ts, x, y, z0 + k, o + k, f4(a0, k), f4(a1, k), f4(a2, k), f4(n0, k),
-                                          f4(n1, k), f4(n2, k));
-        if (!(keep & 1u)) km0 &= ~(1u << k);
-        if (!(keep & 2u)) km1 &= ~(1u << k);
-        if (!(keep & 4u)) km2 &= ~(1u << k);
-    }
-}
-
+// k_update_v4 with the Mur pre/post voltage hooks of the z walls (FDTD/extensions/
+// engine_ext_mur_abc.cpp:83-149) in the lane-parallel wall form (MurDev::lanes: every wall
+// active from step 0).  The host chooses it when each z wall's line and shift lie in one float4
+// (at most one z wall per float4), so the thread owning them holds V_old(line), V_old(shift) and
+// V_new(shift) itself:
+//   b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift),
+// its pre-voltage part formed before the update overwrites the old values.  In a direct column
+// (no x/y wall line or shift there) b becomes the line's final value in the same float4 store;
+// elsewhere it goes to the wall buffer for k_mur's apply, and the line keeps its raw updated
+// value, which is what the x/y walls' post hooks must read at their shift cells.  The x/y walls'
+// pre and post hooks run as k_mur phases 0 and 1 around this launch (their line and shift planes
+// are contiguous in memory), so every thread stores whole float4s.
 template <typename IX = unsigned>
-__global__ void __launch_bounds__(256, 4) k_update_v4m(GridDev g, MurDev m, const unsigned* __restrict__ numTS)
+__global__ void __launch_bounds__(256, 4) k_update_v4m(GridDev g, MurDev m)
 {
     const unsigned x = blockIdx.y;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -581,26 +563,25 @@ __global__ void __launch_bounds__(256, 4) k_update_v4m(GridDev g, MurDev m, cons
     const IX sy = y ? (IX)g.Pz : (IX)0;
     const float* __restrict__ I = g.I;
     float* __restrict__ V = g.V;
-    // z walls whose line and shift are lanes of this float4 (bit q = wall m.z[q])
-    unsigned zw = 0;
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-        if (q < m.nz && (m.z[q].line & ~3u) == z0) zw |= 1u << q;
-    const bool xyw = mur_wall_cell<2>(m, x, y, 0u);
+    int q = -1;
+    if (m.nz > 0 && (m.z[0].line & ~3u) == z0) q = 0;
+    else if (m.nz > 1 && (m.z[1].line & ~3u) == z0) q = 1;
     const unsigned kc = x * g.Ny + y;
-    // start the wall coefficients on their way to L1 (a prefetch holds no register)
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-        if (zw & (1u << q)) {
-            asm volatile("prefetch.global.L1 [%0];" ::"l"(m.z[q].cP + kc));
-            asm volatile("prefetch.global.L1 [%0];" ::"l"(m.z[q].cPP + kc));
-        }
     const float4 i0 = ldg4(I + o), i1 = ldg4(I + (S + o)), i2 = ldg4(I + (2 * S + o));
     const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
     const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
     const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
+    int kl = 0, ks = 0;
+    float pre0 = 0.f, pre1 = 0.f;
+    if (q >= 0) {
+        kl = (int)(m.z[q].line - z0);
+        ks = (int)(m.z[q].shift - z0);
+        const float cP = __ldg(m.z[q].cP + kc), cPP = __ldg(m.z[q].cPP + kc);
+        pre0 = fsub(f4(n0, ks), fmul(cP, f4(n0, kl)));
+        pre1 = fsub(f4(n1, ks), fmul(cPP, f4(n1, kl)));
+    }
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -614,46 +595,22 @@ __global__ void __launch_bounds__(256, 4) k_update_v4m(GridDev g, MurDev m, cons
         set4(n1, k, fadd(fmul(f4(n1, k), ca.y), fmul(cb.x, c1)));
         set4(n2, k, fadd(fmul(f4(n2, k), ca.z), fmul(cb.y, c2)));
     }
-    // store masks: bit k of km[c] = lane k of component c is written
-    unsigned km0 = 15u, km1 = 15u, km2 = 15u;
-    if (xyw) mur_xy_lanes(g, m, __ldg(numTS), x, y, z0, (unsigned long long)o, n0, n1, n2, km0, km1, km2);
-    if (zw) {
-        const float4 a0 = ld4(V + o), a1 = ld4(V + (S + o));   // still V_old
-        const bool direct = mur_z_direct(m, x, y);
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            if (!(zw & (1u << q))) continue;
-            const int kl = (int)(m.z[q].line - z0), ks = (int)(m.z[q].shift - z0);
-            const float cP = __ldg(m.z[q].cP + kc), cPP = __ldg(m.z[q].cPP + kc);
-            const float b0 = fadd(fsub(f4(a0, ks), fmul(cP, f4(a0, kl))), fmul(cP, f4(n0, ks)));
-            const float b1 = fadd(fsub(f4(a1, ks), fmul(cPP, f4(a1, kl))), fmul(cPP, f4(n1, ks)));
-            if (direct) {
-                set4(n0, kl, b0);
-                set4(n1, kl, b1);
-            } else {
-                m.z[q].bP[kc] = b0;
-                m.z[q].bPP[kc] = b1;
-                km0 &= ~(1u << kl);
-                km1 &= ~(1u << kl);
-            }
+    if (q >= 0) {
+        // post: + cP * V_new(shift); the coefficients are in L1 from the loads above
+        const float b0 = fadd(pre0, fmul(__ldg(m.z[q].cP + kc), f4(n0, ks)));
+        const float b1 = fadd(pre1, fmul(__ldg(m.z[q].cPP + kc), f4(n1, ks)));
+        if (mur_z_direct(m, x, y)) {
+            set4(n0, kl, b0);
+            set4(n1, kl, b1);
+        } else {
+            m.z[q].bP[kc] = b0;
+            m.z[q].bPP[kc] = b1;
         }
     }
-    // lanes past Nz-1 are padding: they keep their zero either way
-    if (km0 == 15u) *reinterpret_cast<float4*>(V + o) = n0;
-    else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) if (km0 & (1u << k)) V[o + k] = f4(n0, k);
-    }
-    if (km1 == 15u) *reinterpret_cast<float4*>(V + (S + o)) = n1;
-    else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) if (km1 & (1u << k)) V[S + o + k] = f4(n1, k);
-    }
-    if (km2 == 15u) *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
-    else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) if (km2 & (1u << k)) V[2 * S + o + k] = f4(n2, k);
-    }
+    // lanes past Nz-1 are padding: they keep their zero
+    *reinterpret_cast<float4*>(V + o) = n0;
+    *reinterpret_cast<float4*>(V + (S + o)) = n1;
+    *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
 }
 
 template <bool COMPRESSED, bool UPML, typename IX = unsigned long long>
