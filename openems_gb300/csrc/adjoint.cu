@@ -280,17 +280,19 @@ __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
 
 // The main box of the split (compressed operator, no UPML cell in it), four z cells per thread:
 // adj_u_cell / adj_w_cell's arithmetic per lane, with the float4 loads of the forward's
-// update_*4_cells.  Lane k is cell z0 + k; the box's z range is a multiple of four from a
-// multiple of four, and its cells are interior to the update range of each half-step.
+// update_*4_cells.  Lane k is cell z0 + k; groups start on multiples of four, and lanes outside
+// the box's z range are computed but not stored (their cells belong to the region blocks).
 __global__ void __launch_bounds__(256, 4) k_adj_box4_u(AdjDev a, SplitDev sp)
 {
     unsigned t = blockIdx.x * 256u + threadIdx.x;
     if (t >= sp.main_cells4) return;
-    const unsigned n4 = sp.n[2] >> 2;
-    const unsigned z0 = sp.lo[2] + ((t % n4) << 2);
-    t /= n4;
+    const unsigned z0 = sp.z4 + ((t % sp.n4) << 2);
+    t /= sp.n4;
     const unsigned y = sp.lo[1] + t % sp.n[1];
     const unsigned x = sp.lo[0] + t / sp.n[1];
+    unsigned mask = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) mask |= (z0 + k >= sp.lo[2] && z0 + k < sp.lo[2] + sp.n[2]) ? (1u << k) : 0u;
     const GridDev& g = a.g;
     const unsigned S = (unsigned)g.S;
     const unsigned o = (x * g.Ny + y) * g.Pz + z0;
@@ -318,20 +320,22 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_u(AdjDev a, SplitDev sp)
         set4(u1, k, fadd(fmul(ca.y, f4(u1, k)), fmul(cb.x, d[1])));
         set4(u2, k, fadd(fmul(ca.z, f4(u2, k)), fmul(cb.y, d[2])));
     }
-    *reinterpret_cast<float4*>(a.U + o) = u0;
-    *reinterpret_cast<float4*>(a.U + (S + o)) = u1;
-    *reinterpret_cast<float4*>(a.U + (2 * S + o)) = u2;
+    st4_masked(a.U + o, u0, mask);
+    st4_masked(a.U + (S + o), u1, mask);
+    st4_masked(a.U + (2 * S + o), u2, mask);
 }
 
 __global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
 {
     unsigned t = blockIdx.x * 256u + threadIdx.x;
     if (t >= sp.main_cells4) return;
-    const unsigned n4 = sp.n[2] >> 2;
-    const unsigned z0 = sp.lo[2] + ((t % n4) << 2);
-    t /= n4;
+    const unsigned z0 = sp.z4 + ((t % sp.n4) << 2);
+    t /= sp.n4;
     const unsigned y = sp.lo[1] + t % sp.n[1];
     const unsigned x = sp.lo[0] + t / sp.n[1];
+    unsigned mask = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) mask |= (z0 + k >= sp.lo[2] && z0 + k < sp.lo[2] + sp.n[2]) ? (1u << k) : 0u;
     const GridDev& g = a.g;
     const unsigned S = (unsigned)g.S;
     const unsigned o = (x * g.Ny + y) * g.Pz + z0;
@@ -366,7 +370,7 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
         set4(n1, k, wn[1]);
         set4(n2, k, wn[2]);
         const unsigned bz = z - a.b0[2];
-        if (inbox && bz < a.bn[2]) {
+        if (inbox && bz < a.bn[2] && (mask & (1u << k))) {
             const unsigned kb = (bx * a.bn[1] + by) * a.bn[2] + bz;
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
@@ -378,9 +382,9 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
             }
         }
     }
-    *reinterpret_cast<float4*>(a.W + o) = n0;
-    *reinterpret_cast<float4*>(a.W + (S + o)) = n1;
-    *reinterpret_cast<float4*>(a.W + (2 * S + o)) = n2;
+    st4_masked(a.W + o, n0, mask);
+    st4_masked(a.W + (S + o), n1, mask);
+    st4_masked(a.W + (2 * S + o), n2, mask);
 }
 
 // V^n and K_V I^n (the arithmetic of update_v_cell) in the design box, into slot

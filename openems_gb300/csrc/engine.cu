@@ -716,9 +716,10 @@ void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp)
     sp.main_blocks = (sp.main_cells + 255) / 256;
     // four z cells per thread in the main box of the compressed forward kernels: the box's z range
     // on multiples of four, 32-bit offsets (the adjoint kernels keep one cell per thread)
-    sp.v4 = (!sp.full && sp.main_cells && e->compressed && e->vec4 && 3ull * e->S < (1ull << 32) &&
-             sp.lo[2] % 4 == 0 && sp.n[2] % 4 == 0) ? 1 : 0;
-    sp.main_cells4 = sp.v4 ? sp.main_cells / 4 : 0;
+    sp.v4 = (!sp.full && sp.main_cells && e->compressed && e->vec4 && 3ull * e->S < (1ull << 32)) ? 1 : 0;
+    sp.z4 = sp.lo[2] & ~3u;
+    sp.n4 = sp.v4 ? (((sp.lo[2] + sp.n[2] + 3u) & ~3u) - sp.z4) / 4u : 0u;
+    sp.main_cells4 = sp.v4 ? sp.n[0] * sp.n[1] * sp.n4 : 0;
     sp.main_blocks4 = (sp.main_cells4 + 255) / 256;
     sp.first_block[0] = 0;
     for (int r = 0; r < g.nupml; ++r) sp.first_block[r + 1] = sp.first_block[r] + (g.upml[r].n + 255) / 256;
@@ -1124,7 +1125,9 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
         md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
         // the float4 form needs each z wall's line and shift in one aligned group of four z
-        e->mur_v4 = md.lanes != 0 && e->N[2] >= 8 && e->compressed && e->vec4 && 3ull * e->S < (1ull << 32);
+        const char* mv = getenv("OEMS_CUDA_MUR_V4");   // 0: keep the one-cell form with the hooks inside
+        e->mur_v4 = md.lanes != 0 && e->N[2] >= 8 && e->compressed && e->vec4 && 3ull * e->S < (1ull << 32) &&
+                    !(mv && mv[0] == '0');
         for (int q = 0; q < md.nz && q < 2; ++q)
             e->mur_v4 = e->mur_v4 && (md.z[q].line & ~3u) == (md.z[q].shift & ~3u);
         if (e->mur_v4) {

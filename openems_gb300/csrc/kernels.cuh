@@ -440,9 +440,23 @@ __device__ __forceinline__ void set4(float4& v, int k, float a)
     if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
 }
 
-// four current cells (x, y, z0..z0+3) of the compressed operator without UPML
+// store the lanes of `mask` (bit k = lane k) of a float4: one vector store when all four are set
+__device__ __forceinline__ void st4_masked(float* p, const float4 v, unsigned mask)
+{
+    if (mask == 15u) {
+        *reinterpret_cast<float4*>(p) = v;
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (mask & (1u << k)) p[k] = f4(v, k);
+}
+
+// four current cells (x, y, z0..z0+3) of the compressed operator without UPML; only the lanes of
+// `mask` are stored (the others belong to another kernel's cells)
 template <typename IX = unsigned>
-__device__ __forceinline__ void update_i4_cells(const GridDev& g, unsigned x, unsigned y, unsigned z0)
+__device__ __forceinline__ void update_i4_cells(const GridDev& g, unsigned x, unsigned y, unsigned z0,
+                                                unsigned mask = 15u)
 {
     const IX S = (IX)g.S;
     const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
@@ -469,9 +483,9 @@ __device__ __forceinline__ void update_i4_cells(const GridDev& g, unsigned x, un
         set4(a1, k, fadd(fmul(f4(a1, k), ca.y), fmul(cb.x, c1)));
         set4(a2, k, fadd(fmul(f4(a2, k), ca.z), fmul(cb.y, c2)));
     }
-    *reinterpret_cast<float4*>(I + o) = a0;
-    *reinterpret_cast<float4*>(I + (S + o)) = a1;
-    *reinterpret_cast<float4*>(I + (2 * S + o)) = a2;
+    st4_masked(I + o, a0, mask);
+    st4_masked(I + (S + o), a1, mask);
+    st4_masked(I + (2 * S + o), a2, mask);
 }
 
 template <typename IX = unsigned>
@@ -491,9 +505,11 @@ __global__ void __launch_bounds__(256) k_update_i4(GridDev g)
 // read).  Lanes past z = Nz-1 are padding and keep their zero.  (With Mur walls the hooks make a
 // float4 form no faster than the one-cell form on GB300: the wall lanes of every row serialise
 // their warps, and a separate pass over the scattered row ends costs as much.)
-// four voltage cells (x, y, z0..z0+3) of the compressed operator without UPML and Mur hooks
+// four voltage cells (x, y, z0..z0+3) of the compressed operator without UPML and Mur hooks;
+// only the lanes of `mask` are stored
 template <typename IX = unsigned>
-__device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, unsigned y, unsigned z0)
+__device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, unsigned y, unsigned z0,
+                                                unsigned mask = 15u)
 {
     const IX S = (IX)g.S;
     const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
@@ -521,9 +537,9 @@ __device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, un
         set4(n1, k, fadd(fmul(f4(n1, k), ca.y), fmul(cb.x, c1)));
         set4(n2, k, fadd(fmul(f4(n2, k), ca.z), fmul(cb.y, c2)));
     }
-    *reinterpret_cast<float4*>(V + o) = n0;
-    *reinterpret_cast<float4*>(V + (S + o)) = n1;
-    *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
+    st4_masked(V + o, n0, mask);
+    st4_masked(V + (S + o), n1, mask);
+    st4_masked(V + (2 * S + o), n2, mask);
 }
 
 template <typename IX = unsigned>
@@ -631,13 +647,14 @@ __global__ void __launch_bounds__(256) k_update_i(GridDev g)
 // table, then the fluxes): started first, they overlap with the streaming main blocks instead of
 // forming the launch's tail.  With v4 the host launches only the region blocks of this kernel and
 // walks the main box with k_update_box4 on a parallel branch, four z cells per thread (the float4
-// bodies of the plain kernels; the box's z range starts and ends on multiples of four): the two
-// kernels need different register budgets, and as separate launches they run side by side.
+// bodies of the plain kernels, in groups aligned to four z): the two kernels need different
+// register budgets, and as separate launches they run side by side.
 struct SplitDev {
     unsigned lo[3], n[3];                      // main part: this box of cells
     unsigned main_cells, main_blocks;
     int full;                                  // 1: the box is the whole update range, skip UPML cells
     int v4;                                    // 1: main box four z cells per thread (k_update_box4)
+    unsigned z4, n4;                           // first z of the groups of four, groups per row
     unsigned main_cells4, main_blocks4;        // groups of four and their blocks when v4
     unsigned nreg;
     unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1])
@@ -685,18 +702,23 @@ __global__ void __launch_bounds__(256, (COMPRESSED && !MUR) ? 8 : 1)
 }
 
 // The main box of a UPML split, four z cells per thread (compressed operator, no Mur hooks).
+// Groups of four start on multiples of four (z4 = lo[2] rounded down); lanes outside the box's
+// z range are computed but not stored (their cells belong to the region blocks).
 template <bool CURR>
 __global__ void __launch_bounds__(256) k_update_box4(GridDev g, SplitDev sp)
 {
     unsigned t = blockIdx.x * 256u + threadIdx.x;
     if (t >= sp.main_cells4) return;
-    const unsigned n4 = sp.n[2] >> 2;
-    const unsigned z = sp.lo[2] + ((t % n4) << 2);
-    t /= n4;
+    const unsigned z = sp.z4 + ((t % sp.n4) << 2);
+    t /= sp.n4;
     const unsigned y = sp.lo[1] + t % sp.n[1];
     const unsigned x = sp.lo[0] + t / sp.n[1];
-    if (CURR) update_i4_cells<unsigned>(g, x, y, z);
-    else update_v4_cells<unsigned>(g, x, y, z);
+    const unsigned zlo = sp.lo[2], zhi = sp.lo[2] + sp.n[2];
+    unsigned mask = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) mask |= (z + k >= zlo && z + k < zhi) ? (1u << k) : 0u;
+    if (CURR) update_i4_cells<unsigned>(g, x, y, z, mask);
+    else update_v4_cells<unsigned>(g, x, y, z, mask);
 }
 
 // ---------------------------------------------------------------------------------------------
