@@ -10,7 +10,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC_DIR = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboems_cuda.so")
-SOURCES = ["engine.cu", "batch.cu", "energy_noalloc.cu", "adjoint.cu", "nf2ff.cu", "opbuild.cu", "tddump.cu"]
+SOURCES = ["engine.cu", "batch.cu", "energy_noalloc.cu", "adjoint.cu", "nf2ff.cu", "opbuild.cu", "tddump.cu",
+           "compress.cu"]
 HEADERS = ["kernels.cuh", "engine_impl.h", "fused.cuh"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",

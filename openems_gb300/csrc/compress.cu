@@ -115,6 +115,25 @@ __global__ void k_tables(const float* vv, const float* vi, const float* ii, cons
     tabI[2 * k + 1] = make_float4(iv[cells + c], iv[2 * cells + c], 0.f, 0.f);
 }
 
+// a CUDA failure: the error text on the engine, the OEMS code returned
+int cfail(oems_cuda_engine* e, cudaError_t c, const char* what)
+{
+    cudaGetLastError();
+    e->err = std::string("operator compression: ") + what + ": " + cudaGetErrorString(c);
+    return c == cudaErrorMemoryAllocation ? OEMS_ERR_NOMEM : OEMS_ERR_CUDA;
+}
+
+// a device allocation owned by the engine (freed with it)
+template <class T>
+cudaError_t keep(oems_cuda_engine* e, T** out, size_t n)
+{
+    void* q = nullptr;
+    cudaError_t c = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+    if (c == cudaSuccess) e->allocs.push_back(q);
+    *out = (T*)q;
+    return c;
+}
+
 struct Scratch {
     std::vector<void*> p;
     ~Scratch()
@@ -149,7 +168,7 @@ int compress_dense_device(oems_cuda_engine* e, const float* vv, const float* vi,
 #define CKS(x)                                                   \
     do {                                                         \
         cudaError_t c_ = (x);                                    \
-        if (c_ != cudaSuccess) return cuda_fail(e, c_, #x);      \
+        if (c_ != cudaSuccess) return cfail(e, c_, #x);          \
     } while (0)
     CKS(t.get(&dvv, 3 * cells));
     CKS(t.get(&dvi, 3 * cells));
@@ -196,10 +215,11 @@ int compress_dense_device(oems_cuda_engine* e, const float* vv, const float* vi,
     CKS(cub::DeviceRadixSort::SortPairs(tmp3, tb3, first, first2, ids, ids2, (int)U, 0, 32, s));
     const unsigned ublocks = (U + 255) / 256;
     k_rank<<<ublocks, 256, 0, s>>>(ids2, U, cls_of_run);
-    int rc;
-    if ((rc = dalloc(e, &e->didx, (size_t)e->N[0] * e->N[1] * e->Pz, true))) return rc;
-    if ((rc = dalloc(e, &e->dtabV, 2 * (size_t)U))) return rc;
-    if ((rc = dalloc(e, &e->dtabI, 2 * (size_t)U))) return rc;
+    const size_t nidx = (size_t)e->N[0] * e->N[1] * e->Pz;
+    CKS(keep(e, &e->didx, nidx));
+    CKS(cudaMemsetAsync(e->didx, 0, nidx * sizeof(unsigned), s));   // padding lanes: class 0
+    CKS(keep(e, &e->dtabV, 2 * (size_t)U));
+    CKS(keep(e, &e->dtabI, 2 * (size_t)U));
     k_scatter_index<<<blocks, 256, 0, s>>>(run, cell2, cls_of_run, cells, e->N[2], e->Pz, e->didx);
     k_tables<<<ublocks, 256, 0, s>>>(dvv, dvi, dii, div, cells, first2, U, e->dtabV, e->dtabI);
     CKS(cudaGetLastError());

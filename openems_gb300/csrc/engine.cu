@@ -74,69 +74,6 @@ inline unsigned long long cell_off(const oems_cuda_engine* e, unsigned n, unsign
     return (unsigned long long)n * e->S + ((unsigned long long)x * e->N[1] + y) * e->Pz + z;
 }
 
-// ---- operator compression (Operator_SSE_Compressed::CompressOperator restated per cell) ------
-struct Key12 {
-    uint32_t w[12];
-};
-
-uint64_t hash12(const Key12& k)
-{
-    uint64_t h = 1469598103934665603ULL;
-    for (int i = 0; i < 12; ++i) {
-        h ^= k.w[i];
-        h *= 1099511628211ULL;
-        h ^= h >> 31;
-    }
-    return h;
-}
-
-// classes numbered in order of first appearance (x, y, z loops), like the reference
-int compress_dense(oems_cuda_engine* e, const float* vv, const float* vi, const float* ii, const float* iv,
-                   unsigned max_classes, std::vector<unsigned>& index, std::vector<Key12>& keys)
-{
-    const unsigned Nx = e->N[0], Ny = e->N[1], Nz = e->N[2];
-    const size_t cells = (size_t)Nx * Ny * Nz;
-    index.assign((size_t)Nx * Ny * e->Pz, 0u);
-    keys.clear();
-    size_t hcap = 1u << 16;
-    std::vector<int64_t> htab(hcap, -1);
-    Key12 k;
-    for (unsigned x = 0; x < Nx; ++x)
-        for (unsigned y = 0; y < Ny; ++y)
-            for (unsigned z = 0; z < Nz; ++z) {
-                const size_t c = ((size_t)x * Ny + y) * Nz + z;
-                for (int n = 0; n < 3; ++n) {
-                    memcpy(&k.w[n], vv + n * cells + c, 4);
-                    memcpy(&k.w[3 + n], vi + n * cells + c, 4);
-                    memcpy(&k.w[6 + n], ii + n * cells + c, 4);
-                    memcpy(&k.w[9 + n], iv + n * cells + c, 4);
-                }
-                size_t slot = hash12(k) & (hcap - 1);
-                int64_t found = -1;
-                while (htab[slot] >= 0) {
-                    if (memcmp(&keys[htab[slot]], &k, sizeof(Key12)) == 0) { found = htab[slot]; break; }
-                    slot = (slot + 1) & (hcap - 1);
-                }
-                if (found < 0) {
-                    if (max_classes && keys.size() >= max_classes) return 1;  // too many: use dense
-                    found = (int64_t)keys.size();
-                    keys.push_back(k);
-                    htab[slot] = found;
-                    if (keys.size() * 2 > hcap) {
-                        hcap *= 4;
-                        htab.assign(hcap, -1);
-                        for (size_t j = 0; j < keys.size(); ++j) {
-                            size_t s2 = hash12(keys[j]) & (hcap - 1);
-                            while (htab[s2] >= 0) s2 = (s2 + 1) & (hcap - 1);
-                            htab[s2] = (int64_t)j;
-                        }
-                    }
-                }
-                index[((size_t)x * Ny + y) * e->Pz + z] = (unsigned)found;
-            }
-    return 0;
-}
-
 // UPML coefficient classes of one region: the 18 values (vv, vvfo, vvfn, ii, iifo, iifn of the
 // three components) of each cell, deduplicated; false when there are more than 65535 classes.
 bool compress_upml(const UpmlHost& u, std::vector<unsigned short>& cls, std::vector<float4>& tab)
@@ -191,29 +128,6 @@ bool compress_upml(const UpmlHost& u, std::vector<unsigned short>& cls, std::vec
             t[2] = make_float4(v[8], v[9], v[10], v[11]);
         }
     return true;
-}
-
-int upload_compressed(oems_cuda_engine* e, const std::vector<unsigned>& index, const std::vector<Key12>& keys)
-{
-    const size_t U = keys.size();
-    std::vector<float4> tv(2 * U), ti(2 * U);
-    for (size_t j = 0; j < U; ++j) {
-        float f[12];
-        memcpy(f, keys[j].w, 48);
-        tv[2 * j] = make_float4(f[0], f[1], f[2], f[3]);
-        tv[2 * j + 1] = make_float4(f[4], f[5], 0.f, 0.f);
-        ti[2 * j] = make_float4(f[6], f[7], f[8], f[9]);
-        ti[2 * j + 1] = make_float4(f[10], f[11], 0.f, 0.f);
-    }
-    int rc;
-    if ((rc = dupload(e, &e->didx, index.data(), index.size()))) return rc;
-    if ((rc = dupload(e, &e->dtabV, tv.data(), tv.size()))) return rc;
-    if ((rc = dupload(e, &e->dtabI, ti.data(), ti.size()))) return rc;
-    CK(cudaStreamSynchronize(e->stream));
-    e->compressed = true;
-    e->nclasses = (unsigned)U;
-    e->op_set = true;
-    return OEMS_OK;
 }
 
 int upload_dense(oems_cuda_engine* e, const float* src, float** dst)
@@ -289,13 +203,11 @@ int oems_cuda_set_operator(oems_cuda_engine* e, const float* vv, const float* vi
     if (!e || !vv || !vi || !ii || !iv) return OEMS_ERR_ARG;
     if (e->inited || e->op_set) return fail(e, OEMS_ERR_STATE, "operator already set");
     CK(cudaSetDevice(e->device));
-    std::vector<unsigned> index;
-    std::vector<Key12> keys;
+    // per-cell coefficient classes, found on the device (compress.cu); too many classes keep
+    // the dense arrays
     const unsigned cap = max_classes ? max_classes : (1u << 22);
-    if (compress_dense(e, vv, vi, ii, iv, cap, index, keys) == 0) return upload_compressed(e, index, keys);
-    index.clear();
-    keys.clear();
-    int rc;
+    int rc = compress_dense_device(e, vv, vi, ii, iv, cap);
+    if (rc != 1) return rc;
     if ((rc = upload_dense(e, vv, &e->dvv))) return rc;
     if ((rc = upload_dense(e, vi, &e->dvi))) return rc;
     if ((rc = upload_dense(e, ii, &e->dii))) return rc;
@@ -786,7 +698,8 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
                 k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
             } else if (mode == 2 && e->mur_v4) {
                 const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
-                k_update_v4m<unsigned><<<gv4, 256, 0, s>>>(g, m);
+                if (e->v4m_minb == 3) k_update_v4m<unsigned, 3><<<gv4, 256, 0, s>>>(g, m);
+                else k_update_v4m<unsigned, 4><<<gv4, 256, 0, s>>>(g, m);
             } else if (o32) {
                 if (mode == 2) launch_v<true, false, 2, unsigned>(gv, s, g, m, ts);
                 else if (mode == 1) launch_v<true, false, 1, unsigned>(gv, s, g, m, ts);
@@ -1125,6 +1038,8 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
         md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
         // the float4 form needs each z wall's line and shift in one aligned group of four z
+        const char* mb = getenv("OEMS_CUDA_V4M_MINB");
+        e->v4m_minb = (mb && mb[0] == '3') ? 3 : 4;
         const char* mv = getenv("OEMS_CUDA_MUR_V4");   // 0: keep the one-cell form with the hooks inside
         e->mur_v4 = md.lanes != 0 && e->N[2] >= 8 && e->compressed && e->vec4 && 3ull * e->S < (1ull << 32) &&
                     !(mv && mv[0] == '0');

@@ -173,6 +173,7 @@ struct oems_cuda_engine {
     // x/y walls' pre/post hooks then run as k_mur phases 0/1 over murdev_xy (those walls only)
     bool mur_v4 = false;
     MurDev murdev_xy{};
+    int v4m_minb = 4;
     unsigned mur_xy_pts = 0;
     // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
     // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
@@ -192,6 +193,10 @@ int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch);
 void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp);
 // one update launch (V or I) of the engine's kernel configuration on stream s
 void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s);
+// per-cell coefficient classes of dense N-I-J-K arrays on the device (compress.cu): 0 = built,
+// 1 = more than `cap` classes, else an OEMS error code
+int compress_dense_device(oems_cuda_engine* e, const float* vv, const float* vi, const float* ii, const float* iv,
+                          unsigned cap);
 
 
 // per-launch events for oems_cuda_profile_steps (never used inside a captured graph)

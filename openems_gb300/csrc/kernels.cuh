@@ -565,8 +565,8 @@ __global__ void __launch_bounds__(256) k_update_v4(GridDev g)
 // value, which is what the x/y walls' post hooks must read at their shift cells.  The x/y walls'
 // pre and post hooks run as k_mur phases 0 and 1 around this launch (their line and shift planes
 // are contiguous in memory), so every thread stores whole float4s.
-template <typename IX = unsigned>
-__global__ void __launch_bounds__(256, 4) k_update_v4m(GridDev g, MurDev m)
+template <typename IX = unsigned, int MINB = 4>
+__global__ void __launch_bounds__(256, MINB) k_update_v4m(GridDev g, MurDev m)
 {
     const unsigned x = blockIdx.y;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
