@@ -696,10 +696,6 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
             if (o32 && e->vec4 && mode == 0) {
                 const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
                 k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
-            } else if (mode == 2 && e->mur_v4) {
-                const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
-                if (e->v4m_minb == 3) k_update_v4m<unsigned, 3><<<gv4, 256, 0, s>>>(g, m);
-                else k_update_v4m<unsigned, 4><<<gv4, 256, 0, s>>>(g, m);
             } else if (o32) {
                 if (mode == 2) launch_v<true, false, 2, unsigned>(gv, s, g, m, ts);
                 else if (mode == 1) launch_v<true, false, 1, unsigned>(gv, s, g, m, ts);
@@ -767,16 +763,10 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     // the Mur pre/post hooks run inside the voltage update unless mur_separate
     const bool mur_sep = !e->mur.empty() && e->mur_separate;
     if (mur_sep) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 0, e->d_numTS); post(); ++L; }
-    // the float4 voltage update with the z walls' hooks: the x/y walls' pre hooks before it,
-    // their post hooks after it
-    const bool xy_sep = e->mur_v4 && e->murdev.lanes && !e->mur_separate && e->murdev_xy.nwall > 0;
-    const dim3 xy_grid((e->mur_xy_pts + 255) / 256, (unsigned)e->murdev_xy.nwall);
-    if (xy_sep) { pre(OEMS_KC_MUR); k_mur<<<xy_grid, blk, 0, s>>>(g, e->murdev_xy, 0, e->d_numTS); post(); ++L; }
     pre(OEMS_KC_UPDATE_V);
     launch_update(e, false, s);
     post();
     ++L;
-    if (xy_sep) { pre(OEMS_KC_MUR); k_mur<<<xy_grid, blk, 0, s>>>(g, e->murdev_xy, 1, e->d_numTS); post(); ++L; }
     const unsigned cyl_v = g.Nx * g.Nz, cyl_i = (g.Nx - 1) * (g.Nz - 1);
     if (e->cyl.closed) {   // post-voltage hook, priority 1e5: before TFSF and Mur
         pre(OEMS_KC_MUR);
@@ -1037,25 +1027,6 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         bool always = true;
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
         md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
-        // the float4 form needs each z wall's line and shift in one aligned group of four z
-        const char* mb = getenv("OEMS_CUDA_V4M_MINB");
-        e->v4m_minb = (mb && mb[0] == '3') ? 3 : 4;
-        const char* mv = getenv("OEMS_CUDA_MUR_V4");   // 0: keep the one-cell form with the hooks inside
-        e->mur_v4 = md.lanes != 0 && e->N[2] >= 8 && e->compressed && e->vec4 && 3ull * e->S < (1ull << 32) &&
-                    !(mv && mv[0] == '0');
-        for (int q = 0; q < md.nz && q < 2; ++q)
-            e->mur_v4 = e->mur_v4 && (md.z[q].line & ~3u) == (md.z[q].shift & ~3u);
-        if (e->mur_v4) {
-            MurDev& xy = e->murdev_xy;
-            xy = md;
-            xy.nwall = 0;
-            e->mur_xy_pts = 0;
-            for (int w = 0; w < md.nwall; ++w)
-                if (md.w[w].ny != 2) {
-                    xy.w[xy.nwall++] = md.w[w];
-                    e->mur_xy_pts = std::max(e->mur_xy_pts, md.w[w].n1 * md.w[w].n2);
-                }
-        }
     }
 
     // cylinder extension

@@ -168,13 +168,7 @@ struct oems_cuda_engine {
     bool mur_separate = false;
     // float4 forms of the update kernels (4 z cells per thread) where they exist
     bool vec4 = true;
-    // the float4 voltage update carries the z walls' Mur hooks (k_update_v4m): lane-parallel
-    // walls, every z wall's line and shift in one float4, compressed operator without UPML; the
-    // x/y walls' pre/post hooks then run as k_mur phases 0/1 over murdev_xy (those walls only)
-    bool mur_v4 = false;
-    MurDev murdev_xy{};
-    int v4m_minb = 4;
-    unsigned mur_xy_pts = 0;
+
     // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
     // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
     // whenever the host sees it

@@ -502,9 +502,10 @@ __global__ void __launch_bounds__(256) k_update_i4(GridDev g)
 // Vectorised voltage update of the compressed operator without UPML and without Mur walls, four
 // consecutive z cells per thread (see k_update_i4).  The -z neighbour of lane k is lane k-1, of
 // lane 0 the float before the vector (the cell itself at z = 0, the reference's "same cell"
-// read).  Lanes past z = Nz-1 are padding and keep their zero.  (With Mur walls the hooks make a
-// float4 form no faster than the one-cell form on GB300: the wall lanes of every row serialise
-// their warps, and a separate pass over the scattered row ends costs as much.)
+// read).  Lanes past z = Nz-1 are padding and keep their zero.  (With Mur walls the one-cell form
+// carrying the hooks stays the faster choice on GB300: a float4 update with the z walls' hooks in
+// the registers of the wall thread measured 94 us against 78 us without walls on 256x256x192,
+// every warp holding one wall thread, and a register spill or an exposed coefficient load with it.)
 // four voltage cells (x, y, z0..z0+3) of the compressed operator without UPML and Mur hooks;
 // only the lanes of `mask` are stored
 template <typename IX = unsigned>
@@ -551,82 +552,6 @@ __global__ void __launch_bounds__(256) k_update_v4(GridDev g)
     const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
     if (y >= g.Ny || z0 >= g.Nz) return;
     update_v4_cells<IX>(g, x, y, z0);
-}
-
-// k_update_v4 with the Mur pre/post voltage hooks of the z walls (FDTD/extensions/
-// engine_ext_mur_abc.cpp:83-149) in the lane-parallel wall form (MurDev::lanes: every wall
-// active from step 0).  The host chooses it when each z wall's line and shift lie in one float4
-// (at most one z wall per float4), so the thread owning them holds V_old(line), V_old(shift) and
-// V_new(shift) itself:
-//   b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift),
-// its pre-voltage part formed before the update overwrites the old values.  In a direct column
-// (no x/y wall line or shift there) b becomes the line's final value in the same float4 store;
-// elsewhere it goes to the wall buffer for k_mur's apply, and the line keeps its raw updated
-// value, which is what the x/y walls' post hooks must read at their shift cells.  The x/y walls'
-// pre and post hooks run as k_mur phases 0 and 1 around this launch (their line and shift planes
-// are contiguous in memory), so every thread stores whole float4s.
-template <typename IX = unsigned, int MINB = 4>
-__global__ void __launch_bounds__(256, MINB) k_update_v4m(GridDev g, MurDev m)
-{
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned pz4 = g.Pz >> 2;
-    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
-    if (y >= g.Ny || z0 >= g.Nz) return;
-    const IX S = (IX)g.S;
-    const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
-    const IX sx = x ? (IX)g.Ny * g.Pz : (IX)0;
-    const IX sy = y ? (IX)g.Pz : (IX)0;
-    const float* __restrict__ I = g.I;
-    float* __restrict__ V = g.V;
-    int q = -1;
-    if (m.nz > 0 && (m.z[0].line & ~3u) == z0) q = 0;
-    else if (m.nz > 1 && (m.z[1].line & ~3u) == z0) q = 1;
-    const unsigned kc = x * g.Ny + y;
-    const float4 i0 = ldg4(I + o), i1 = ldg4(I + (S + o)), i2 = ldg4(I + (2 * S + o));
-    const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
-    const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
-    const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
-    float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
-    int kl = 0, ks = 0;
-    float pre0 = 0.f, pre1 = 0.f;
-    if (q >= 0) {
-        kl = (int)(m.z[q].line - z0);
-        ks = (int)(m.z[q].shift - z0);
-        const float cP = __ldg(m.z[q].cP + kc), cPP = __ldg(m.z[q].cPP + kc);
-        pre0 = fsub(f4(n0, ks), fmul(cP, f4(n0, kl)));
-        pre1 = fsub(f4(n1, ks), fmul(cPP, f4(n1, kl)));
-    }
-    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        if (z0 + k >= g.Nz) break;
-        const float4 ca = __ldg(g.tabV + 2 * cls[k]), cb = __ldg(g.tabV + 2 * cls[k] + 1);
-        const float i1z = k ? f4(i1, k - 1) : i1m, i0z = k ? f4(i0, k - 1) : i0m;
-        const float c0 = fadd(fsub(fsub(f4(i2, k), f4(i2y, k)), f4(i1, k)), i1z);
-        const float c1 = fadd(fsub(fsub(f4(i0, k), i0z), f4(i2, k)), f4(i2x, k));
-        const float c2 = fadd(fsub(fsub(f4(i1, k), f4(i1x, k)), f4(i0, k)), f4(i0y, k));
-        set4(n0, k, fadd(fmul(f4(n0, k), ca.x), fmul(ca.w, c0)));
-        set4(n1, k, fadd(fmul(f4(n1, k), ca.y), fmul(cb.x, c1)));
-        set4(n2, k, fadd(fmul(f4(n2, k), ca.z), fmul(cb.y, c2)));
-    }
-    if (q >= 0) {
-        // post: + cP * V_new(shift); the coefficients are in L1 from the loads above
-        const float b0 = fadd(pre0, fmul(__ldg(m.z[q].cP + kc), f4(n0, ks)));
-        const float b1 = fadd(pre1, fmul(__ldg(m.z[q].cPP + kc), f4(n1, ks)));
-        if (mur_z_direct(m, x, y)) {
-            set4(n0, kl, b0);
-            set4(n1, kl, b1);
-        } else {
-            m.z[q].bP[kc] = b0;
-            m.z[q].bPP[kc] = b1;
-        }
-    }
-    // lanes past Nz-1 are padding: they keep their zero
-    *reinterpret_cast<float4*>(V + o) = n0;
-    *reinterpret_cast<float4*>(V + (S + o)) = n1;
-    *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
 }
 
 template <bool COMPRESSED, bool UPML, typename IX = unsigned long long>
