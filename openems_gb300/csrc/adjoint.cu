@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256) k_adj_w(AdjDev a)
 
 // the engine's UPML work split (k_update_split): the region blocks first, then the blocks of the
 // cells outside every region (a launch of the first first_block[nreg] blocks covers the regions
-// alone, while k_adj_box4_* walk the main box on a parallel branch)
+// alone, followed by k_adj_box4_* over the main box)
 template <bool CURR>
 __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
 {
@@ -438,10 +438,8 @@ struct oems_adjoint_state {
     cudaStream_t rs = nullptr;
     cudaEvent_t ev_recomputed[2] = {nullptr, nullptr};
     cudaEvent_t ev_reversed[2] = {nullptr, nullptr};
-    // UPML split with a float4 main box: the region blocks of each reverse half-step run on
-    // `rb` beside the main box, forked from and joined back to the sweep's stream
-    cudaStream_t rb = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // UPML split with a float4 main box (k_adj_box4_*)
+    bool box4 = false;
     float fwd_ms = 0.f, bwd_ms = 0.f;
     unsigned launches_per_reverse_step = 0;
 };
@@ -646,12 +644,7 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     if ((rc = aalloc(e, s, &s->rec_numTS, 1))) return rc;
     if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess)
         return afail(e, OEMS_ERR_CUDA, "adjoint events");
-    if (e->use_split && e->compressed && e->splitI.v4 && e->splitV.v4) {
-        if (cudaStreamCreateWithFlags(&s->rb, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) != cudaSuccess)
-            return afail(e, OEMS_ERR_CUDA, "adjoint branch stream");
-    }
+    s->box4 = e->use_split && e->compressed && e->splitI.v4 && e->splitV.v4;
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) return afail(e, OEMS_ERR_CUDA, "adjoint setup sync");
     return OEMS_OK;
 }
@@ -761,24 +754,19 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         d.n = n;
         d.fv = slot;
         d.fc = slot + 3 * d.B;
-        if (e->use_split && s->rb) {
-            // per half-step: region blocks on the branch stream, the main box four cells per
-            // thread on the sweep's stream, joined before the next half-step reads the result
+        if (e->use_split && s->box4) {
+            // per half-step: the region blocks, then the main box four cells per thread
             const SplitDev* sp[2] = {&e->splitI, &e->splitV};
             for (int h = 0; h < 2; ++h) {
                 const unsigned rblk = sp[h]->first_block[sp[h]->nreg];
-                cudaEventRecord(s->ev_fork, rst);
-                cudaStreamWaitEvent(s->rb, s->ev_fork, 0);
                 if (rblk) {
-                    if (h == 0) k_adj_split<true><<<rblk, 256, 0, s->rb>>>(d, *sp[h]);
-                    else k_adj_split<false><<<rblk, 256, 0, s->rb>>>(d, *sp[h]);
+                    if (h == 0) k_adj_split<true><<<rblk, 256, 0, rst>>>(d, *sp[h]);
+                    else k_adj_split<false><<<rblk, 256, 0, rst>>>(d, *sp[h]);
                 }
                 if (sp[h]->main_blocks4) {
                     if (h == 0) k_adj_box4_u<<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
                     else k_adj_box4_w<<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
                 }
-                cudaEventRecord(s->ev_join, s->rb);
-                cudaStreamWaitEvent(rst, s->ev_join, 0);
             }
         } else if (e->use_split) {
             if (bu) k_adj_split<true><<<bu, 256, 0, rst>>>(d, e->splitI);
@@ -844,7 +832,6 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         cudaStreamSynchronize(st);
     }
     if (s->rs) cudaStreamSynchronize(s->rs);
-    if (s->rb) cudaStreamSynchronize(s->rb);
     release();
     d.src = nullptr;
     d.injV = InjList{};
@@ -876,8 +863,5 @@ void oems_adjoint_free(oems_adjoint_state* s)
         if (s->ev_reversed[b]) cudaEventDestroy(s->ev_reversed[b]);
     }
     if (s->rs) cudaStreamDestroy(s->rs);
-    if (s->rb) cudaStreamDestroy(s->rb);
-    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
-    if (s->ev_join) cudaEventDestroy(s->ev_join);
     delete s;
 }

@@ -163,9 +163,6 @@ int oems_cuda_create(const unsigned int num_lines[3], double dt, int device, oem
     e->dt = dt;
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&e->stream_r, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
     int rc;
     if ((rc = dalloc(e, &e->dV, 3 * (size_t)e->S, true, true))) return rc;
     if ((rc = dalloc(e, &e->dI, 3 * (size_t)e->S, true, true))) return rc;
@@ -185,9 +182,6 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     if (e->graphK) cudaGraphExecDestroy(e->graphK);
     oems_adjoint_free(e->adj);
     for (void* p : e->allocs) cudaFree(p);
-    if (e->stream_r) { cudaStreamSynchronize(e->stream_r); cudaStreamDestroy(e->stream_r); }
-    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
-    if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -652,21 +646,18 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
     const bool mur = !curr && !e->mur.empty() && !e->mur_separate;
     if (e->use_split) {
         const SplitDev& sp = curr ? e->splitI : e->splitV;
-        if (sp.v4 && !mur && e->stream_r) {
-            // region blocks on a branch stream, the main box four cells per thread on this one
+        if (sp.v4 && !mur) {
+            // the region blocks, then the main box four cells per thread (the two write disjoint
+            // cells; as separate launches each gets its own register budget)
             const unsigned rb = sp.first_block[sp.nreg];
-            cudaEventRecord(e->ev_fork, s);
-            cudaStreamWaitEvent(e->stream_r, e->ev_fork, 0);
             if (rb) {
-                if (curr) k_update_split<true, true><<<rb, 256, 0, e->stream_r>>>(g, sp, m, ts);
-                else k_update_split<true, false><<<rb, 256, 0, e->stream_r>>>(g, sp, m, ts);
+                if (curr) k_update_split<true, true><<<rb, 256, 0, s>>>(g, sp, m, ts);
+                else k_update_split<true, false><<<rb, 256, 0, s>>>(g, sp, m, ts);
             }
             if (sp.main_blocks4) {
                 if (curr) k_update_box4<true><<<sp.main_blocks4, 256, 0, s>>>(g, sp);
                 else k_update_box4<false><<<sp.main_blocks4, 256, 0, s>>>(g, sp);
             }
-            cudaEventRecord(e->ev_join, e->stream_r);
-            cudaStreamWaitEvent(s, e->ev_join, 0);
             return;
         }
         const unsigned blocks = sp.main_blocks + sp.first_block[sp.nreg];

@@ -86,10 +86,6 @@ void td_free(oems_cuda_engine* e);
 struct oems_cuda_engine {
     int device = 0;
     cudaStream_t stream = nullptr;
-    // branch stream of the UPML split (region blocks beside the float4 main box) and its fork
-    // and join events
-    cudaStream_t stream_r = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     unsigned N[3] = {0, 0, 0};
     unsigned Pz = 0;
     unsigned long long S = 0;

@@ -571,9 +571,8 @@ __global__ void __launch_bounds__(256) k_update_i(GridDev g)
 // come first because they carry the longer dependent load chains (class index, then the class
 // table, then the fluxes): started first, they overlap with the streaming main blocks instead of
 // forming the launch's tail.  With v4 the host launches only the region blocks of this kernel and
-// walks the main box with k_update_box4 on a parallel branch, four z cells per thread (the float4
-// bodies of the plain kernels, in groups aligned to four z): the two kernels need different
-// register budgets, and as separate launches they run side by side.
+// then walks the main box with k_update_box4, four z cells per thread (the float4 bodies of the
+// plain kernels, in groups aligned to four z): the two need different register budgets.
 struct SplitDev {
     unsigned lo[3], n[3];                      // main part: this box of cells
     unsigned main_cells, main_blocks;
