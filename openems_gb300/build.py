@@ -12,7 +12,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboems_cuda.so")
 SOURCES = ["engine.cu", "batch.cu", "energy_noalloc.cu", "adjoint.cu", "nf2ff.cu", "opbuild.cu", "tddump.cu",
            "compress.cu"]
-HEADERS = ["kernels.cuh", "engine_impl.h", "fused.cuh"]
+HEADERS = ["kernels.cuh", "engine_impl.h", "fused.cuh", "march.cuh", "march_dev.h"]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-pthread", "-shared", "-lpthread"]

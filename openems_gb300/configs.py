@@ -133,8 +133,10 @@ def small_mixed(n=(18, 16, 14), steps=200, bc=(3, 3, 2, 2, 0, 3), pml=4, seed=1,
 
 
 # ------------------------------------------------------------------------------------------
-def stress(shape=(512, 512, 256), steps=2000, nblocks=64, seed=20261204, pitch_mm=1.0):
-    """Bandwidth-stress mesh: random dielectric/lossy blocks, 10 % dispersive, Mur walls."""
+def stress(shape=(512, 512, 256), steps=2000, nblocks=64, seed=20261204, pitch_mm=1.0, bc=(2,) * 6,
+           dispersive=True):
+    """Bandwidth-stress mesh: random dielectric/lossy blocks, 10 % dispersive, Mur walls (``bc``
+    and ``dispersive`` give the PEC / non-dispersive variants of the same blocks)."""
     rng = np.random.default_rng(seed)
     g = Grid([_uniform(k, pitch_mm) for k in shape], unit=1e-3)
     csx = Structure()
@@ -152,7 +154,7 @@ def stress(shape=(512, 512, 256), steps=2000, nblocks=64, seed=20261204, pitch_m
         kap = rng.uniform(0.0, 0.1)
         start = lo * pitch_mm
         stop = hi * pitch_mm
-        if b in disp:
+        if b in disp and dispersive:
             fp = rng.uniform(1e9, 10e9)
             tr = 1.0 / rng.uniform(1e8, 1e9)
             if b % 2:
@@ -178,7 +180,7 @@ def stress(shape=(512, 512, 256), steps=2000, nblocks=64, seed=20261204, pitch_m
         a[d] -= 1
         b[d] += 2
         csx.AddProbe(f"mon{s}", 0, interval=1).AddBox(a * pitch_mm, b * pitch_mm)
-    op = Operator(csx, g, exc, bc=(2,) * 6)
+    op = Operator(csx, g, exc, bc=bc)
     return op.build(steps)
 
 

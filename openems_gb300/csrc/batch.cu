@@ -456,7 +456,8 @@ int capture_concurrent(oems_cuda_batch* b, const std::vector<int>& act, unsigned
     return rc;
 }
 
-int run_concurrent(oems_cuda_batch* b, const std::vector<int>& act, unsigned steps)
+// ev (optional): two events recorded around the launches only, after every graph is built
+int run_concurrent(oems_cuda_batch* b, const std::vector<int>& act, unsigned steps, cudaEvent_t* ev)
 {
     const unsigned full = steps / kGraphSteps, tail = steps % kGraphSteps;
     cudaGraphExec_t g16 = nullptr, g1 = nullptr;
@@ -464,9 +465,12 @@ int run_concurrent(oems_cuda_batch* b, const std::vector<int>& act, unsigned ste
     if (full && (rc = capture_concurrent(b, act, kGraphSteps, &g16))) return rc;
     if (tail && (rc = capture_concurrent(b, act, 1, &g1))) { if (g16) cudaGraphExecDestroy(g16); return rc; }
     cudaError_t e = cudaSuccess;
+    if (ev) cudaEventRecord(ev[0], b->stream);
     for (unsigned r = 0; r < full && e == cudaSuccess; ++r) e = cudaGraphLaunch(g16, b->stream);
     for (unsigned r = 0; r < tail && e == cudaSuccess; ++r) e = cudaGraphLaunch(g1, b->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (ev) cudaEventRecord(ev[1], b->stream);
+    // no wait here: an executable graph destroyed while in flight is freed when it completes, and
+    // the next chunk's graphs are built while this one runs
     if (g16) cudaGraphExecDestroy(g16);
     if (g1) cudaGraphExecDestroy(g1);
     return e == cudaSuccess ? OEMS_OK : bfail(b, OEMS_ERR_CUDA);
@@ -549,11 +553,13 @@ int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned 
             if (rem[k] >= level) a.push_back(k);
         return a;
     };
-    // run `steps` timesteps of the instances in `act` with configuration (mode, block, depth)
+    // run `steps` timesteps of the instances in `act` with configuration (mode, block, depth).
+    // Every chunk descriptor and graph is built first; ev (optional) brackets the launches alone,
+    // so the tuner compares device time, not graph construction.
     bool captured = true;
     auto run_steps = [&](const std::vector<int>& act, unsigned stp, int mode, unsigned block, unsigned depth,
-                         bool use_graph) -> int {
-        if (mode == 3) return run_concurrent(b, act, stp);
+                         bool use_graph, cudaEvent_t* ev) -> int {
+        if (mode == 3) return run_concurrent(b, act, stp, ev);
         std::vector<std::vector<int>> groups;
         if (mode == 2) {
             size_t acc = 0;
@@ -566,31 +572,45 @@ int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned 
         } else {
             groups.push_back(act);
         }
+        struct Prep {
+            Chunk c;
+            cudaGraphExec_t g16, g1;
+        };
+        std::vector<Prep> prep;
+        const unsigned full = stp / kGraphSteps, tail = stp % kGraphSteps;
+        auto release = [&]() {
+            for (auto& p : prep) {
+                if (p.g16) cudaGraphExecDestroy(p.g16);
+                if (p.g1) cudaGraphExecDestroy(p.g1);
+            }
+        };
+        int rc = OEMS_OK;
         for (const auto& grp : groups) {
-            Chunk c{};
-            int rc = upload_chunk(b, grp, block, depth, stp, &c);
-            if (rc) return rc;
-            if (mode == 0) {
-                if ((rc = launch_persistent(b, c, block))) return rc;
-                continue;
-            }
-            if (!use_graph) {
-                if ((rc = launch_phases(b, c, block, stp))) return rc;
-                continue;
-            }
-            const unsigned full = stp / kGraphSteps, tail = stp % kGraphSteps;
-            cudaGraphExec_t g16 = nullptr, g1 = nullptr;
-            if (full && (rc = capture_phases(b, c, block, kGraphSteps, &g16))) return rc;
-            if (tail && (rc = capture_phases(b, c, block, 1, &g1))) { if (g16) cudaGraphExecDestroy(g16); return rc; }
-            cudaError_t e = cudaSuccess;
-            for (unsigned r = 0; r < full && e == cudaSuccess; ++r) e = cudaGraphLaunch(g16, b->stream);
-            for (unsigned r = 0; r < tail && e == cudaSuccess; ++r) e = cudaGraphLaunch(g1, b->stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-            if (g16) cudaGraphExecDestroy(g16);
-            if (g1) cudaGraphExecDestroy(g1);
-            if (e != cudaSuccess) return bfail(b, OEMS_ERR_CUDA);
+            prep.push_back(Prep{Chunk{}, nullptr, nullptr});
+            Prep& p = prep.back();
+            if ((rc = upload_chunk(b, grp, block, depth, stp, &p.c))) break;
+            if (mode == 0 || !use_graph) continue;
+            if (full && (rc = capture_phases(b, p.c, block, kGraphSteps, &p.g16))) break;
+            if (tail && (rc = capture_phases(b, p.c, block, 1, &p.g1))) break;
         }
-        return OEMS_OK;
+        if (rc) { release(); return rc; }
+        if (ev) cudaEventRecord(ev[0], b->stream);
+        cudaError_t e = cudaSuccess;
+        for (auto& p : prep) {
+            if (mode == 0) {
+                if ((rc = launch_persistent(b, p.c, block))) break;
+            } else if (!use_graph) {
+                if ((rc = launch_phases(b, p.c, block, stp))) break;
+            } else {
+                for (unsigned r = 0; r < full && e == cudaSuccess; ++r) e = cudaGraphLaunch(p.g16, b->stream);
+                for (unsigned r = 0; r < tail && e == cudaSuccess; ++r) e = cudaGraphLaunch(p.g1, b->stream);
+                if (e != cudaSuccess) break;
+            }
+        }
+        if (ev) cudaEventRecord(ev[1], b->stream);
+        release();                                  // in-flight graphs are freed on completion
+        if (rc) return rc;
+        return e == cudaSuccess ? OEMS_OK : bfail(b, OEMS_ERR_CUDA);
     };
     unsigned done = 0;
     // ---- autotune on the first chunk (real steps; results do not depend on the configuration)
@@ -603,13 +623,12 @@ int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned 
             cudaEventCreate(&e0);
             cudaEventCreate(&e1);
             float best = 1e30f;
-            int rc = run_steps(act, per, kCands[0].mode, kCands[0].block, kCands[0].depth, true);  // warm
+            int rc = run_steps(act, per, kCands[0].mode, kCands[0].block, kCands[0].depth, true, nullptr);  // warm
             if (rc) return rc;
             done += per;
+            cudaEvent_t ev[2] = {e0, e1};
             for (unsigned c = 0; c < kNumCands; ++c) {
-                cudaEventRecord(e0, b->stream);
-                if ((rc = run_steps(act, per, kCands[c].mode, kCands[c].block, kCands[c].depth, true))) return rc;
-                cudaEventRecord(e1, b->stream);
+                if ((rc = run_steps(act, per, kCands[c].mode, kCands[c].block, kCands[c].depth, true, ev))) return rc;
                 if (cudaEventSynchronize(e1) != cudaSuccess) return bfail(b, OEMS_ERR_CUDA);
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, e0, e1);
@@ -672,7 +691,7 @@ int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned 
         unsigned prev = done;
         for (unsigned level : levels) {
             if (level <= prev) continue;
-            int rc = run_steps(active_at(level), level - prev, b->mode, b->block, b->depth, true);
+            int rc = run_steps(active_at(level), level - prev, b->mode, b->block, b->depth, true, nullptr);
             if (rc) return rc;
             prev = level;
         }

@@ -23,6 +23,9 @@
 #include <vector>
 
 #include "engine_impl.h"
+#include "march.cuh"
+
+#include <cudaTypedefs.h>
 
 using namespace oems;
 
@@ -718,9 +721,18 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
 int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch)
 {
     const FusedDev& f = e->fused[parity];
-    const dim3 grid((e->N[2] + FT_Z - 1) / FT_Z, (e->N[1] + FT_Y - 1) / FT_Y, (e->N[0] + f.xchunk - 1) / f.xchunk);
-    if (e->compressed) k_step_fused<true><<<grid, FT_BLOCK, 0, e->stream>>>(f);
-    else k_step_fused<false><<<grid, FT_BLOCK, 0, e->stream>>>(f);
+    if (e->use_march) {
+        if (e->march_minb == 2)
+            k_step_march<2><<<e->march_grid, e->march_threads, e->march_smem, e->stream>>>(e->march[parity],
+                                                                                        e->march_map[parity]);
+        else
+            k_step_march<1><<<e->march_grid, e->march_threads, e->march_smem, e->stream>>>(e->march[parity],
+                                                                                        e->march_map[parity]);
+    } else {
+        const dim3 grid((e->N[2] + FT_Z - 1) / FT_Z, (e->N[1] + FT_Y - 1) / FT_Y, (e->N[0] + f.xchunk - 1) / f.xchunk);
+        if (e->compressed) k_step_fused<true><<<grid, FT_BLOCK, 0, e->stream>>>(f);
+        else k_step_fused<false><<<grid, FT_BLOCK, 0, e->stream>>>(f);
+    }
     // processing on the fields this step wrote
     GridDev g = e->grid;
     g.V = f.Vo;
@@ -858,6 +870,85 @@ static int setup_fused(oems_cuda_engine* e)
         f1.g.upml[r].vflux = e->vflux2[r];
         f1.vflux_o[r] = e->grid.upml[r].vflux;
     }
+    return OEMS_OK;
+}
+
+// cuTensorMapEncodeTiled from the driver (the runtime exports no wrapper)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// rows per tile and x-planes per block of the plane march; OEMS_CUDA_MARCH_TY / _XCHUNK override
+static void march_shape(const oems_cuda_engine* e, unsigned& ty, unsigned& xchunk, unsigned& smem)
+{
+    const unsigned Pz = e->Pz, G = Pz / 4;
+    auto bytes_of = [&](unsigned t) {
+        const unsigned slot = ((3u * (t + 2) * Pz + 31u) & ~31u), vbuf = ((3u * (t + 1) * Pz + 31u) & ~31u);
+        return 4u * (3u * slot + 2u * vbuf) + 8u * MARCH_SLOTS;
+    };
+    // the largest tile of at most 512 threads (one block per SM: the kernel holds about 108
+    // registers a thread) within the 227 KB of shared memory a block may have
+    ty = 1;
+    for (unsigned t = 1; t < 64 && (t + 2) * G <= 512 && t < e->N[1]; ++t)
+        if (bytes_of(t + 1) <= 227u * 1024u) ty = t + 1;
+    const char* s = getenv("OEMS_CUDA_MARCH_TY");
+    if (s && atoi(s) > 0) ty = (unsigned)atoi(s);
+    while (ty > 1 && ((ty + 1) * G > 512 || bytes_of(ty) > 227u * 1024u)) --ty;
+    const unsigned long long tiles = (e->N[1] + ty - 1) / ty;
+    // about four waves of one block per SM on a 152-SM GPU, 4..64 planes per block
+    xchunk = (unsigned)std::min<unsigned long long>(64, std::max<unsigned long long>(4, e->N[0] * tiles / 608));
+    const char* xc = getenv("OEMS_CUDA_MARCH_XCHUNK");
+    if (xc && atoi(xc) > 0) xchunk = (unsigned)atoi(xc);
+    smem = bytes_of(ty);
+}
+
+// the plane march on top of the fused step's buffers (setup_fused must have run)
+static int setup_march(oems_cuda_engine* e)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return fail(e, OEMS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    unsigned ty, xchunk, smem;
+    march_shape(e, ty, xchunk, smem);
+    int rc;
+    if ((rc = dalloc(e, &e->d_march_err, 1, true))) return rc;
+    const unsigned Pz = e->Pz;
+    for (int p = 0; p < 2; ++p) {
+        MarchDev& m = e->march[p];
+        m.f = e->fused[p];
+        m.ty = ty;
+        m.groups = Pz / 4;
+        m.xchunk = xchunk;
+        m.slot_floats = (3u * (ty + 2) * Pz + 31u) & ~31u;
+        m.box_bytes = 12u * (ty + 2) * Pz;
+        m.vbuf_floats = (3u * (ty + 1) * Pz + 31u) & ~31u;
+        m.err = e->d_march_err;
+        // I of the input set as [3][Nx][Ny][Pz]; one box = all z, ty + 2 rows, one plane, 3 components
+        const cuuint64_t dims[4] = {Pz, e->N[1], e->N[0], 3};
+        const cuuint64_t strides[3] = {(cuuint64_t)Pz * 4, (cuuint64_t)e->N[1] * Pz * 4, (cuuint64_t)e->S * 4};
+        const cuuint32_t box[4] = {Pz, ty + 2, 1, 3};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        const CUresult r = enc(&e->march_map[p], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)m.f.g.I, dims, strides, box,
+                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(e, OEMS_ERR_CUDA, "cuTensorMapEncodeTiled failed for the plane march");
+    }
+    e->march_threads = (((ty + 1) * (Pz / 4)) + 31u) & ~31u;
+    e->march_smem = smem;
+    e->march_grid = dim3((e->N[1] + ty - 1) / ty, (e->N[0] + xchunk - 1) / xchunk);
+    const char* mb = getenv("OEMS_CUDA_MARCH_MINB");
+    e->march_minb = (mb && mb[0] == '2') ? 2 : 1;
+    CK(cudaFuncSetAttribute(k_step_march<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_step_march<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return OEMS_OK;
 }
 
@@ -1333,6 +1424,21 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
                        3ull * e->S < (1ull << 32);        // the staged-plane offsets are 32-bit
         if (e->use_fused && (rc = setup_fused(e))) return rc;
     }
+    // OEMS_CUDA_MARCH=1: the fused step as the TMA-staged plane march, where the engine is
+    // compressed, has no hook at all but the soft sources and its z lines fit one TMA box
+    {
+        const char* env = getenv("OEMS_CUDA_MARCH");
+        const bool want = env && env[0] == '1';
+        const bool fits = e->compressed && e->grid.nupml == 0 && e->mur.empty() && e->lor.empty() && !e->has_tfsf &&
+                          !e->rlc.count && !e->cyl_closed && e->Pz <= 256 && e->K % 2 == 0 &&
+                          e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC;
+        if (want && fits) {
+            if (!e->use_fused && (rc = setup_fused(e))) return rc;
+            e->use_fused = true;
+            if ((rc = setup_march(e))) return rc;
+            e->use_march = true;
+        }
+    }
     if ((rc = capture(e, 1, &e->graph1, false))) return rc;
     if ((rc = capture(e, e->K, &e->graphK, e->use_fused))) return rc;
     e->inited = true;
@@ -1363,6 +1469,11 @@ int oems_cuda_sync(oems_cuda_engine* e)
 {
     if (!e) return OEMS_ERR_ARG;
     CK(cudaStreamSynchronize(e->stream));
+    if (e->d_march_err) {                          // a plane-march block gave up on a copy
+        unsigned err = 0;
+        CK(cudaMemcpy(&err, e->d_march_err, sizeof(err), cudaMemcpyDeviceToHost));
+        if (err) return fail(e, OEMS_ERR_DEVICE, "plane march: a TMA copy did not complete in time");
+    }
     return OEMS_OK;
 }
 

@@ -1,5 +1,6 @@
 // engine_impl.h -- private definition of the engine handle, shared by engine.cu and batch.cu.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -9,6 +10,7 @@
 #include "../../include/oems_cuda.h"
 #include "kernels.cuh"
 #include "fused.cuh"
+#include "march_dev.h"
 
 using namespace oems;
 
@@ -174,6 +176,15 @@ struct oems_cuda_engine {
     float* vflux2[OEMS_MAX_UPML] = {};
     FusedDev fused[2]{};
     unsigned fused_launches = 0;
+    // TMA-staged plane march (march.cuh): the fused step's buffers and parities, one kernel per
+    // step, for compressed engines with PEC/PMC walls only; the maps describe I of sets A and B
+    bool use_march = false;
+    MarchDev march[2]{};
+    CUtensorMap march_map[2]{};                 // 64-byte aligned by its own declaration
+    dim3 march_grid{1, 1, 1};
+    unsigned march_threads = 0, march_smem = 0;
+    int march_minb = 1;
+    unsigned* d_march_err = nullptr;
 };
 
 // enqueue one fused timestep on e->stream: parity 0 reads set A and writes B, parity 1 the reverse

@@ -30,21 +30,13 @@
 #include <cuda.h>
 
 #include "fused.cuh"
+#include "march_dev.h"
 
 namespace oems {
 
 constexpr int MARCH_SLOTS = 3;
-constexpr unsigned MARCH_SPIN_LIMIT = 1u << 26;
-
-struct MarchDev {
-    FusedDev f;            // input set (f.g), output buffers, sources, step counter
-    unsigned ty;           // output rows per tile
-    unsigned groups;       // float4 groups per row (Pz / 4)
-    unsigned xchunk;       // x-planes per block
-    unsigned slot_floats;  // floats of one ring slot: 3 * (ty + 2) * Pz
-    unsigned vbuf_floats;  // floats of one V' buffer: 3 * (ty + 1) * Pz
-    unsigned* err;         // device error flag
-};
+constexpr unsigned MARCH_SPIN_LIMIT = 1u << 26;        // tries of one wait, at most
+constexpr unsigned long long MARCH_WAIT_NS = 2000000000ull;   // and two seconds of %globaltimer
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -59,10 +51,18 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned
                  : "memory");
 }
 
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // bounded wait for phase `parity` of the barrier; false when the limit ran out
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity)
 {
     const unsigned a = smem_addr(bar);
+    unsigned long long t0 = 0;
     for (unsigned it = 0; it < MARCH_SPIN_LIMIT; ++it) {
         unsigned done;
         asm volatile(
@@ -73,6 +73,11 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((it & 63u) == 63u) {
+            const unsigned long long now = global_ns();
+            if (!t0) t0 = now;
+            else if (now - t0 > MARCH_WAIT_NS) return false;
+        }
     }
     return false;
 }
@@ -94,8 +99,8 @@ __device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cas
 
 // V'(x, y, z0..z0+3): update_v_cell's arithmetic on the staged planes Ic = I_old(x), Ip = I_old(x-1)
 // (slot rows: slot row r holds y = y0 - 1 + r), then the soft sources
-__device__ __forceinline__ float4* march_v(const MarchDev& m, const float* Ic, const float* Ip, unsigned x, unsigned y,
-                                           unsigned z0, unsigned r, const float4 vold[3], uint4 ci, int ts, float4 out[3])
+__device__ __forceinline__ void march_v(const MarchDev& m, const float* Ic, const float* Ip, unsigned x, unsigned y,
+                                        unsigned z0, unsigned r, const float4 vold[3], uint4 ci, int ts, float4 out[3])
 {
     const FusedDev& f = m.f;
     const GridDev& g = f.g;
@@ -129,7 +134,6 @@ __device__ __forceinline__ float4* march_v(const MarchDev& m, const float* Ic, c
         set4(out[1], k, v[1]);
         set4(out[2], k, v[2]);
     }
-    return nullptr;
 }
 
 // I'(x, y, z0..z0+3) from V'(x) (Vp), V'(x+1) (Vc) and I_old(x) (slot Ip): update_i_cell's
@@ -176,19 +180,22 @@ __device__ __forceinline__ void st4(float* p, const float4 v) { *reinterpret_cas
 // Grid: (tiles of ty rows along y, chunks of xchunk planes along x).  Block: (ty+1) * groups
 // threads, rounded up to warps.  Dynamic shared memory: three I ring slots, two V' buffers and
 // the three mbarriers (host: march_smem_bytes).
-__global__ void __launch_bounds__(1024) k_step_march(const __grid_constant__ MarchDev m,
+// MINB: blocks per SM the register budget is sized for (1: about 108 registers a thread, no
+// spills; 2: 64 registers)
+template <int MINB>
+__global__ void __launch_bounds__(512, MINB) k_step_march(const __grid_constant__ MarchDev m,
                                                      const __grid_constant__ CUtensorMap mapI)
 {
     extern __shared__ __align__(128) float smem[];
     const FusedDev& f = m.f;
     const GridDev& g = f.g;
     const unsigned Pz = g.Pz, G = m.groups, ty = m.ty;
-    float* slot[MARCH_SLOTS];
-    for (int s = 0; s < MARCH_SLOTS; ++s) slot[s] = smem + s * m.slot_floats;
-    float* vbuf[2] = {smem + MARCH_SLOTS * m.slot_floats, smem + MARCH_SLOTS * m.slot_floats + m.vbuf_floats};
-    unsigned long long* bar =
-        reinterpret_cast<unsigned long long*>(smem + MARCH_SLOTS * m.slot_floats + 2 * m.vbuf_floats);
-    const unsigned bytes = m.slot_floats * 4u;
+    // ring slot s at smem + s * slot_floats, V' buffer b after the ring (no pointer arrays: they
+    // would be indexed at run time and live in local memory)
+    const unsigned SF = m.slot_floats, VF = m.vbuf_floats;
+    float* const vbase = smem + MARCH_SLOTS * SF;
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(vbase + 2 * VF);
+    const unsigned bytes = m.box_bytes;
 
     const unsigned t = threadIdx.x;
     const unsigned rv = t / G, gz = t - rv * G, z0 = gz * 4;
@@ -206,18 +213,21 @@ __global__ void __launch_bounds__(1024) k_step_march(const __grid_constant__ Mar
     const int ts = (int)*f.numTS;
 
     // ring slot of plane q: (q - xa + 1) % 3 (the -x neighbour plane of xa sits in slot 0); each
-    // slot's barrier completes once per load, so its phase is the load count of that slot, mod 2
-    unsigned phase[MARCH_SLOTS] = {0u, 0u, 0u};
+    // slot's barrier completes once per load, so its phase is the load count of that slot, mod 2.
+    // Every thread waits on the barriers itself (the completed phase makes the copied data
+    // visible to it); the per-plane __syncthreads_and makes the verdict of a bounded wait uniform.
+    unsigned phase = 0u, pending = 0u;                      // bit s: slot s's phase / a copy in flight
     if (t == 0) {
         for (int s = 0; s < MARCH_SLOTS; ++s) mbar_init(&bar[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     if (t == 0) {
-        march_load(&mapI, slot[0], &bar[0], bytes, (int)y0, (int)(xa > 0 ? xa - 1 : 0));
-        march_load(&mapI, slot[1], &bar[1], bytes, (int)y0, (int)xa);
-        if (xa + 1 < xend) march_load(&mapI, slot[2], &bar[2], bytes, (int)y0, (int)(xa + 1));
+        march_load(&mapI, smem, &bar[0], bytes, (int)y0, (int)(xa > 0 ? xa - 1 : 0));
+        march_load(&mapI, smem + SF, &bar[1], bytes, (int)y0, (int)xa);
+        if (xa + 1 < xend) march_load(&mapI, smem + 2 * SF, &bar[2], bytes, (int)y0, (int)(xa + 1));
     }
+    pending = xa + 1 < xend ? 7u : 3u;
     bool ok = true;
     // register queue: V_old and the class index of the next plane
     float4 vq[3] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
@@ -229,12 +239,22 @@ __global__ void __launch_bounds__(1024) k_step_march(const __grid_constant__ Mar
         vq[2] = ldg4(g.V + 2 * S + o);
         cq = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     }
-    ok = mbar_wait(&bar[0], phase[0]);
-    phase[0] ^= 1u;
-    for (unsigned x = xa; x < xend && ok; ++x) {
-        const int sc = (int)((x - xa + 1) % MARCH_SLOTS), sp = (int)((x - xa) % MARCH_SLOTS);
-        if (!mbar_wait(&bar[sc], phase[sc])) { ok = false; break; }
-        phase[sc] ^= 1u;
+    bool w = mbar_wait(&bar[0], 0u);
+    if (w) {                                                // a copy whose wait ran out is still in flight
+        pending &= ~1u;
+        phase ^= 1u;
+    }
+    for (unsigned x = xa; x < xend; ++x) {
+        const unsigned sc = (x - xa + 1) % MARCH_SLOTS, sp = (x - xa) % MARCH_SLOTS;
+        if (w) {
+            w = mbar_wait(&bar[sc], (phase >> sc) & 1u);
+            if (w) {
+                pending &= ~(1u << sc);
+                phase ^= 1u << sc;
+            }
+        }
+        const float* Ic = smem + sc * SF;
+        float* Ipl = smem + sp * SF;
         float4 vcur[3] = {vq[0], vq[1], vq[2]};
         const uint4 ccur = cq;
         if (inV && x + 1 < xend) {                          // next plane's V_old and classes
@@ -244,11 +264,11 @@ __global__ void __launch_bounds__(1024) k_step_march(const __grid_constant__ Mar
             vq[2] = ldg4(g.V + 2 * S + o);
             cq = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
         }
-        float* Vc = vbuf[(x - xa) & 1];
-        const float* Vp = vbuf[(x - xa + 1) & 1];
-        if (inV) {
+        float* Vc = vbase + ((x - xa) & 1u) * VF;
+        const float* Vp = vbase + ((x - xa + 1) & 1u) * VF;
+        if (inV && w) {
             float4 out[3];
-            march_v(m, slot[sc], slot[sp], x, y, z0, rv + 1, vcur, ccur, ts, out);
+            march_v(m, Ic, Ipl, x, y, z0, rv + 1, vcur, ccur, ts, out);
 #pragma unroll
             for (int c = 0; c < 3; ++c) st4(Vc + (c * (ty + 1) + rv) * Pz + z0, out[c]);
             if (ownV && x < xb) {
@@ -258,17 +278,20 @@ __global__ void __launch_bounds__(1024) k_step_march(const __grid_constant__ Mar
                 st4(f.Vo + 2 * S + o, out[2]);
             }
         }
-        __syncthreads();
+        if (!__syncthreads_and(w)) {
+            ok = false;
+            break;
+        }
         if (x > xa && ownV) {
             const unsigned long long o = (x - 1) * plane + yz;
             float4 out[3];
             if (inI) {
-                march_i(m, Vp, Vc, slot[sp], x - 1, y, z0, rv, cprev, ts, out);
+                march_i(m, Vp, Vc, Ipl, x - 1, y, z0, rv, cprev, ts, out);
             } else {                                        // I is never updated on this row: carry it over
                 const unsigned r = rv + 1, rows = ty + 2;
-                out[0] = lds4(slot[sp] + (0 * rows + r) * Pz + z0);
-                out[1] = lds4(slot[sp] + (1 * rows + r) * Pz + z0);
-                out[2] = lds4(slot[sp] + (2 * rows + r) * Pz + z0);
+                out[0] = lds4(Ipl + (0 * rows + r) * Pz + z0);
+                out[1] = lds4(Ipl + (1 * rows + r) * Pz + z0);
+                out[2] = lds4(Ipl + (2 * rows + r) * Pz + z0);
             }
             st4(f.Io + o, out[0]);
             st4(f.Io + S + o, out[1]);
@@ -276,18 +299,22 @@ __global__ void __launch_bounds__(1024) k_step_march(const __grid_constant__ Mar
         }
         __syncthreads();
         // slot sp (plane x-1) is free: plane x+2 goes there
-        if (t == 0 && x + 2 < xend) march_load(&mapI, slot[sp], &bar[sp], bytes, (int)y0, (int)(x + 2));
+        if (x + 2 < xend) {
+            if (t == 0) march_load(&mapI, Ipl, &bar[sp], bytes, (int)y0, (int)(x + 2));
+            pending |= 1u << sp;
+        }
         cprev = ccur;
     }
     if (!ok) {
         if (t == 0) atomicOr(m.err, 1u);
         // wait (bounded) for this block's copies still in flight before the block ends
-        for (int s = 0; s < MARCH_SLOTS; ++s) mbar_wait(&bar[s], phase[s]);
+        for (unsigned s = 0; s < MARCH_SLOTS; ++s)
+            if ((pending >> s) & 1u) mbar_wait(&bar[s], (phase >> s) & 1u);
         return;
     }
     if (xb == g.Nx && ownV) {                               // the last plane: I is never updated
         const unsigned x = g.Nx - 1;
-        const float* Il = slot[(x - xa + 1) % MARCH_SLOTS];
+        const float* Il = smem + ((x - xa + 1) % MARCH_SLOTS) * SF;
         const unsigned r = rv + 1, rows = ty + 2;
         const unsigned long long o = x * plane + yz;
         st4(f.Io + o, lds4(Il + (0 * rows + r) * Pz + z0));

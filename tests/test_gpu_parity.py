@@ -100,6 +100,34 @@ def test_fused_step_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, st
     assert not bad, (name, bad)
 
 
+MARCH_CASES = [
+    ("cube40", lambda: configs.plain_cube(n=40, steps=300), 300),
+    ("cube33_lanes", lambda: configs.plain_cube(n=33, steps=260), 260),
+    ("mixed_pec_pmc", lambda: configs.small_mixed(n=(30, 27, 37), bc=(0, 1, 1, 0, 0, 1), pml=0, dispersive=False,
+                                                  steps=220), 220),
+    ("stress_pec", lambda: configs.stress(shape=(44, 38, 30), steps=160, nblocks=16, bc=(0,) * 6, dispersive=False),
+     160),
+]
+
+
+@pytest.mark.parametrize("ty,xchunk", [(None, None), ("1", "4"), ("3", "5"), ("6", "64")])
+@pytest.mark.parametrize("name,fn,steps", MARCH_CASES)
+def test_march_step_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, steps, ty, xchunk):
+    """The TMA-staged plane march (OEMS_CUDA_MARCH=1): one kernel per step with I staged by
+    cp.async.bulk.tensor, at the default tile and at tiles and x-chunks that leave partial tiles
+    and chunks, mixed with single separate-kernel steps by the uneven chunks."""
+    monkeypatch.setenv("OEMS_CUDA_MARCH", "1")
+    if ty:
+        monkeypatch.setenv("OEMS_CUDA_MARCH_TY", ty)
+        monkeypatch.setenv("OEMS_CUDA_MARCH_XCHUNK", xchunk)
+    op = fn()
+    g, r = _run_pair(op, steps, chunks=(1, 7, 16, 33))
+    assert g.launches_per_step() == 2                      # march step + processing
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, (name, bad)
+
+
 @pytest.mark.parametrize("name,fn,steps", [c for c in CASES if c[0] in ("smoke", "mixed", "mixed_mur_all", "mur_corners",
                                                                         "mur_corners_lanes", "stress_small")])
 def test_separate_mur_hooks_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, steps):
