@@ -496,7 +496,8 @@ def main():
     achieved = ALG_BYTES_PER_CELL_HALF * cells / (avg_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
     tr = _traffic_from_profiles(dom)
-    roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    kname = eng.update_kernels()[0 if dom == "update_v" else 1]
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": tr * cells if tr is not None else None,
                 "alg_bytes_per_launch": ALG_BYTES_PER_CELL_HALF * cells,

@@ -403,6 +403,11 @@ int oems_cuda_restore(oems_cuda_engine* eng, const void* host, size_t bytes);
 /* Number of kernel launches issued per timestep by the captured step graph. */
 int oems_cuda_launches_per_step(const oems_cuda_engine* eng, unsigned int* launches);
 
+/* The kernels that carry the voltage and current updates in this engine's configuration (after
+ * oems_cuda_init), e.g. "k_update_v4w" / "k_update_i4", or "k_step_march" for both: NUL-terminated
+ * names written into `volt` and `curr`, each buffer `cap` bytes. */
+int oems_cuda_update_kernels(oems_cuda_engine* eng, char* volt, char* curr, size_t cap);
+
 /* Run n_steps through the captured step graph and return their device time in ms (CUDA events
  * on the engine stream). */
 int oems_cuda_timed_iterate(oems_cuda_engine* eng, unsigned int n_steps, float* ms);

@@ -69,6 +69,7 @@ CUDA_ONLY = {
     "snapshot": (I, [P, P, SZ]),
     "restore": (I, [P, P, SZ]),
     "launches_per_step": (I, [P, PU]),
+    "update_kernels": (I, [P, C.c_char_p, C.c_char_p, SZ]),
     "timed_iterate": (I, [P, U, PF]),
     "profile_steps": (I, [P, U, PF, PU]),
     "read_probe_range": (I, [P, I, SZ, SZ, PD]),

@@ -640,11 +640,16 @@ static void launch_v(const dim3& grid, cudaStream_t s, const GridDev& g, const M
     k_update_v<C, U, M, IX><<<grid, 256, 0, s>>>(g, m, ts);
 }
 
-void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
+void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** name)
 {
     const GridDev& g = e->grid;
     const MurDev& m = e->murdev;
     const unsigned* ts = e->d_numTS;
+    // name != nullptr: report the kernel this configuration launches, launch nothing
+    auto go = [&](const char* n) {
+        if (name) *name = n;
+        return name == nullptr;
+    };
     // the voltage update carries the Mur pre/post hooks when there are walls
     const bool mur = !curr && !e->mur.empty() && !e->mur_separate;
     if (e->use_split) {
@@ -652,6 +657,7 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
         if (sp.v4 && !mur) {
             // the region blocks, then the main box four cells per thread (the two write disjoint
             // cells; as separate launches each gets its own register budget)
+            if (!go("k_update_split+k_update_box4")) return;
             const unsigned rb = sp.first_block[sp.nreg];
             if (rb) {
                 if (curr) k_update_split<true, true><<<rb, 256, 0, s>>>(g, sp, m, ts);
@@ -664,6 +670,7 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
             return;
         }
         const unsigned blocks = sp.main_blocks + sp.first_block[sp.nreg];
+        if (!go("k_update_split")) return;
         if (!blocks) return;
         if (e->compressed) {
             if (curr) k_update_split<true, true><<<blocks, 256, 0, s>>>(g, sp, m, ts);
@@ -684,37 +691,46 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s)
         const dim3 gv((plane + 255) / 256, e->N[0]);
         const int mode = !mur ? 0 : (m.lanes ? 2 : 1);
         if (up) {
+            if (!go("k_update_v")) return;
             if (e->compressed) { if (mode) launch_v<true, true, 1>(gv, s, g, m, ts); else launch_v<true, true, 0>(gv, s, g, m, ts); }
             else { if (mode) launch_v<false, true, 1>(gv, s, g, m, ts); else launch_v<false, true, 0>(gv, s, g, m, ts); }
         } else if (e->compressed) {
-            if (o32 && e->vec4 && mode == 0) {
+            if (o32 && e->vec4 && (mode == 0 || (mode == 2 && e->mur_v4))) {
                 const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
-                k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
+                if (mode == 2) { if (go("k_update_v4w")) k_update_v4w<unsigned><<<gv4, 256, 0, s>>>(g, m, ts); }
+                else if (go("k_update_v4")) k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
             } else if (o32) {
+                if (!go("k_update_v")) return;
                 if (mode == 2) launch_v<true, false, 2, unsigned>(gv, s, g, m, ts);
                 else if (mode == 1) launch_v<true, false, 1, unsigned>(gv, s, g, m, ts);
                 else launch_v<true, false, 0, unsigned>(gv, s, g, m, ts);
             } else {
+                if (!go("k_update_v")) return;
                 if (mode == 2) launch_v<true, false, 2>(gv, s, g, m, ts);
                 else if (mode == 1) launch_v<true, false, 1>(gv, s, g, m, ts);
                 else launch_v<true, false, 0>(gv, s, g, m, ts);
             }
         } else {
+            if (!go("k_update_v")) return;
             if (mode == 2) launch_v<false, false, 2>(gv, s, g, m, ts);
             else if (mode == 1) launch_v<false, false, 1>(gv, s, g, m, ts);
             else launch_v<false, false, 0>(gv, s, g, m, ts);
         }
     } else {
         const dim3 gi((plane + 255) / 256, e->N[0] - 1);
-        if (up) { if (e->compressed) k_update_i<true, true><<<gi, 256, 0, s>>>(g); else k_update_i<false, true><<<gi, 256, 0, s>>>(g); }
-        else if (e->compressed) {
+        if (up) {
+            if (!go("k_update_i")) return;
+            if (e->compressed) k_update_i<true, true><<<gi, 256, 0, s>>>(g); else k_update_i<false, true><<<gi, 256, 0, s>>>(g);
+        } else if (e->compressed) {
             if (o32 && e->vec4) {
                 const dim3 gi4((plane / 4 + 255) / 256, e->N[0] - 1);
-                k_update_i4<unsigned><<<gi4, 256, 0, s>>>(g);
-            } else if (o32) k_update_i<true, false, unsigned><<<gi, 256, 0, s>>>(g);
-            else k_update_i<true, false><<<gi, 256, 0, s>>>(g);
-        }
-        else k_update_i<false, false><<<gi, 256, 0, s>>>(g);
+                if (go("k_update_i4")) k_update_i4<unsigned><<<gi4, 256, 0, s>>>(g);
+            } else {
+                if (!go("k_update_i")) return;
+                if (o32) k_update_i<true, false, unsigned><<<gi, 256, 0, s>>>(g);
+                else k_update_i<true, false><<<gi, 256, 0, s>>>(g);
+            }
+        } else if (go("k_update_i")) k_update_i<false, false><<<gi, 256, 0, s>>>(g);
     }
 }
 
@@ -1109,6 +1125,13 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         bool always = true;
         for (const auto& m : e->mur) always = always && m.start_ts == 0;
         md.lanes = (!e->mur.empty() && !e->mur_separate && md.nz >= 0 && g.nupml == 0 && always) ? 1 : 0;
+        // the float4 form of the lane-parallel hooks (k_update_v4w): each z wall's line and shift
+        // in one group of four z, no group with two walls; OEMS_CUDA_MUR_V4=0 keeps the one-cell form
+        bool groups_ok = md.nz >= 0;
+        for (int q = 0; q < md.nz && groups_ok; ++q) groups_ok = (md.z[q].line >> 2) == (md.z[q].shift >> 2);
+        if (md.nz == 2) groups_ok = groups_ok && (md.z[0].line >> 2) != (md.z[1].line >> 2);
+        const char* mv = getenv("OEMS_CUDA_MUR_V4");
+        e->mur_v4 = md.lanes && groups_ok && !(mv && mv[0] == '0');
     }
 
     // cylinder extension
@@ -1529,6 +1552,22 @@ int oems_cuda_profile_steps(oems_cuda_engine* e, unsigned int n, float* ms, unsi
     if (ms) for (int k = 0; k < OEMS_KC_COUNT; ++k) ms[k] = acc[k];
     if (launches) for (int k = 0; k < OEMS_KC_COUNT; ++k) launches[k] = cnt[k];
     return rc;
+}
+
+int oems_cuda_update_kernels(oems_cuda_engine* e, char* volt, char* curr, size_t cap)
+{
+    if (!e || !volt || !curr || !cap) return OEMS_ERR_ARG;
+    if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
+    const char *v = "", *i = "";
+    if (e->use_march) v = i = "k_step_march";
+    else if (e->use_fused) v = i = "k_step_fused";
+    else {
+        launch_update(e, false, e->stream, &v);
+        launch_update(e, true, e->stream, &i);
+    }
+    snprintf(volt, cap, "%s", v);
+    snprintf(curr, cap, "%s", i);
+    return OEMS_OK;
 }
 
 int oems_cuda_launches_per_step(const oems_cuda_engine* e, unsigned int* l)

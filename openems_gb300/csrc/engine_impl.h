@@ -166,6 +166,8 @@ struct oems_cuda_engine {
     bool mur_separate = false;
     // float4 forms of the update kernels (4 z cells per thread) where they exist
     bool vec4 = true;
+    // the voltage update with the Mur hooks in the float4 form (k_update_v4w)
+    bool mur_v4 = false;
 
     // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
     // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
@@ -193,7 +195,8 @@ int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch);
 // the split for update range R (V: the mesh, I: one cell less per axis)
 void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp);
 // one update launch (V or I) of the engine's kernel configuration on stream s
-void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s);
+// name != nullptr: only report the kernel name this configuration launches
+void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** name = nullptr);
 // per-cell coefficient classes of dense N-I-J-K arrays on the device (compress.cu): 0 = built,
 // 1 = more than `cap` classes, else an OEMS error code
 int compress_dense_device(oems_cuda_engine* e, const float* vv, const float* vi, const float* ii, const float* iv,

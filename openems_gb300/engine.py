@@ -326,6 +326,13 @@ class Engine_CUDA(EngineBase):
         self._ck(self.lib.launches_per_step(self.h, C.byref(n)), "launches_per_step")
         return n.value
 
+    def update_kernels(self):
+        """(voltage, current) update kernel names of this engine's configuration."""
+        v = C.create_string_buffer(64)
+        i = C.create_string_buffer(64)
+        self._ck(self.lib.update_kernels(self.h, v, i, 64), "update_kernels")
+        return v.value.decode(), i.value.decode()
+
     def timed_iterate(self, n: int) -> float:
         ms = C.c_float()
         self._ck(self.lib.timed_iterate(self.h, int(n), C.byref(ms)), "timed_iterate")
