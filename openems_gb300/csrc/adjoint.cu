@@ -43,7 +43,21 @@ struct InjList {
     const int* comp;                  // [count] component
     const int* row;                   // [count] source row (objective probe)
     const double* coef;               // [count] weight * sign
+    // the groups of four z of the split's main box (k_adj_box4_*) holding a source cell: their
+    // offsets (z a multiple of four); the float4 kernels leave them to blocks of their own
+    const unsigned long long* grp;
+    unsigned ngrp;
 };
+
+// true when one of the list's cells lies in the group of four at offset o
+__device__ __forceinline__ bool group_has_source(const InjList& L, unsigned long long o)
+{
+    for (unsigned k = 0; k < L.count; ++k) {
+        const unsigned long long c = L.cell[k];
+        if (c >= o && c < o + 4) return true;
+    }
+    return false;
+}
 
 struct AdjDev {
     GridDev g;
@@ -282,14 +296,10 @@ __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
 // adj_u_cell / adj_w_cell's arithmetic per lane, with the float4 loads of the forward's
 // update_*4_cells.  Lane k is cell z0 + k; groups start on multiples of four, and lanes outside
 // the box's z range are computed but not stored (their cells belong to the region blocks).
-__global__ void __launch_bounds__(256, 4) k_adj_box4_u(AdjDev a, SplitDev sp)
+// one group of four of the U update in k_adj_box4<true>; SRC: the group holds source cells of injI
+template <bool SRC>
+__device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp, unsigned x, unsigned y, unsigned z0)
 {
-    unsigned t = blockIdx.x * 256u + threadIdx.x;
-    if (t >= sp.main_cells4) return;
-    const unsigned z0 = sp.z4 + ((t % sp.n4) << 2);
-    t /= sp.n4;
-    const unsigned y = sp.lo[1] + t % sp.n[1];
-    const unsigned x = sp.lo[0] + t / sp.n[1];
     unsigned mask = 0u;
 #pragma unroll
     for (int k = 0; k < 4; ++k) mask |= (z0 + k >= sp.lo[2] && z0 + k < sp.lo[2] + sp.n[2]) ? (1u << k) : 0u;
@@ -305,7 +315,6 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_u(AdjDev a, SplitDev sp)
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 u0 = ld4(a.U + o), u1 = ld4(a.U + (S + o)), u2 = ld4(a.U + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
-    const bool src = a.injI.count && (unsigned long long)o + 3 >= a.injI.lo && (unsigned long long)o <= a.injI.hi;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const unsigned z = z0 + k;
@@ -315,7 +324,7 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_u(AdjDev a, SplitDev sp)
             fadd(fsub(fsub(z > 0 ? f4(w1, k) : 0.f, a1z), y > 0 ? f4(w2, k) : 0.f), f4(w2y, k)),
             fadd(fsub(fsub(x > 0 ? f4(w2, k) : 0.f, f4(w2x, k)), z > 0 ? f4(w0, k) : 0.f), a0z),
             fadd(fsub(fsub(y > 0 ? f4(w0, k) : 0.f, f4(w0y, k)), x > 0 ? f4(w1, k) : 0.f), f4(w1x, k))};
-        if (src) add_sources(a, a.injI, (unsigned long long)o + k, d);
+        if (SRC) add_sources(a, a.injI, (unsigned long long)o + k, d);
         set4(u0, k, fadd(fmul(ca.x, f4(u0, k)), fmul(ca.w, d[0])));
         set4(u1, k, fadd(fmul(ca.y, f4(u1, k)), fmul(cb.x, d[1])));
         set4(u2, k, fadd(fmul(ca.z, f4(u2, k)), fmul(cb.y, d[2])));
@@ -325,14 +334,10 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_u(AdjDev a, SplitDev sp)
     st4_masked(a.U + (2 * S + o), u2, mask);
 }
 
-__global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
+// one group of four of the W update in k_adj_box4<false>; SRC: the group holds source cells of injV
+template <bool SRC>
+__device__ __forceinline__ void adj_w4_group(const AdjDev& a, const SplitDev& sp, unsigned x, unsigned y, unsigned z0)
 {
-    unsigned t = blockIdx.x * 256u + threadIdx.x;
-    if (t >= sp.main_cells4) return;
-    const unsigned z0 = sp.z4 + ((t % sp.n4) << 2);
-    t /= sp.n4;
-    const unsigned y = sp.lo[1] + t % sp.n[1];
-    const unsigned x = sp.lo[0] + t / sp.n[1];
     unsigned mask = 0u;
 #pragma unroll
     for (int k = 0; k < 4; ++k) mask |= (z0 + k >= sp.lo[2] && z0 + k < sp.lo[2] + sp.n[2]) ? (1u << k) : 0u;
@@ -348,9 +353,6 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 n0 = ld4(a.W + o), n1 = ld4(a.W + (S + o)), n2 = ld4(a.W + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
-    const bool src = a.injV.count && (unsigned long long)o + 3 >= a.injV.lo && (unsigned long long)o <= a.injV.hi;
-    const unsigned bx = x - a.b0[0], by = y - a.b0[1];
-    const bool inbox = bx < a.bn[0] && by < a.bn[1];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const unsigned z = z0 + k;
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
             fadd(fsub(fsub(f4(u1, k), z ? b1z : 0.f), f4(u2, k)), y ? f4(u2y, k) : 0.f),
             fsub(fadd(fsub(f4(u2, k), x ? f4(u2x, k) : 0.f), z ? b0z : 0.f), f4(u0, k)),
             fadd(fsub(fsub(f4(u0, k), y ? f4(u0y, k) : 0.f), f4(u1, k)), x ? f4(u1x, k) : 0.f)};
-        if (src) add_sources(a, a.injV, (unsigned long long)o + k, gs);
+        if (SRC) add_sources(a, a.injV, (unsigned long long)o + k, gs);
         const float vv[3] = {ca.x, ca.y, ca.z}, vi[3] = {ca.w, cb.x, cb.y};
         const float wn[3] = {fadd(fmul(vv[0], f4(n0, k)), fmul(vi[0], gs[0])),
                              fadd(fmul(vv[1], f4(n1, k)), fmul(vi[1], gs[1])),
@@ -369,22 +371,70 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4_w(AdjDev a, SplitDev sp)
         set4(n0, k, wn[0]);
         set4(n1, k, wn[1]);
         set4(n2, k, wn[2]);
-        const unsigned bz = z - a.b0[2];
-        if (inbox && bz < a.bn[2] && (mask & (1u << k))) {
-            const unsigned kb = (bx * a.bn[1] + by) * a.bn[2] + bz;
-#pragma unroll
-            for (int m = 0; m < 3; ++m) {
-                if (vi[m] == 0.f) continue;                     // PEC edge: no dependence
-                const float b = fmul(wn[m], __frcp_rn(vi[m]));
-                const unsigned kk = m * a.B + kb;
-                a.gvv[kk] += (double)fmul(b, __ldg(a.fv + kk));
-                a.gvi[kk] += (double)fmul(b, __ldg(a.fc + kk));
-            }
-        }
     }
     st4_masked(a.W + o, n0, mask);
     st4_masked(a.W + (S + o), n1, mask);
     st4_masked(a.W + (2 * S + o), n2, mask);
+}
+
+// The design-box gradient sums of adj_w_cell for the cells k_adj_box4<false> updated (the box lies
+// outside every UPML region, so all of it is in the split's main box): one thread per design
+// cell, reading back the new W.  Apart from the streaming kernel it keeps that kernel free of the
+// box's dependent loads and double-precision sums; the values, and their order per sum, are
+// adj_w_cell's.
+__global__ void __launch_bounds__(256) k_adj_grad(AdjDev a)
+{
+    const unsigned kb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kb >= a.B) return;
+    const GridDev& g = a.g;
+    const unsigned bz = kb % a.bn[2], by = (kb / a.bn[2]) % a.bn[1], bx = kb / (a.bn[2] * a.bn[1]);
+    const unsigned x = a.b0[0] + bx, y = a.b0[1] + by, z = a.b0[2] + bz;
+    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
+    float vv[3], vi[3];
+    coef_v(g, o, vv, vi);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        if (vi[m] == 0.f) continue;                             // PEC edge: no dependence
+        const float b = fmul(a.W[m * g.S + o], __frcp_rn(vi[m]));
+        const unsigned kk = m * a.B + kb;
+        a.gvv[kk] += (double)fmul(b, __ldg(a.fv + kk));
+        a.gvi[kk] += (double)fmul(b, __ldg(a.fc + kk));
+    }
+}
+
+// The main box four cells per thread.  The groups that hold a source cell are skipped and left to
+// k_adj_box4_src: without the source code these threads fit 64 registers with no spills (with it
+// inlined, even in blocks of their own, the kernel spills).
+template <bool CURR>
+__global__ void __launch_bounds__(256, 4) k_adj_box4(AdjDev a, SplitDev sp)
+{
+    const InjList& L = CURR ? a.injI : a.injV;
+    const GridDev& g = a.g;
+    unsigned t = blockIdx.x * 256u + threadIdx.x;
+    if (t >= sp.main_cells4) return;
+    const unsigned z0 = sp.z4 + ((t % sp.n4) << 2);
+    t /= sp.n4;
+    const unsigned y = sp.lo[1] + t % sp.n[1];
+    const unsigned x = sp.lo[0] + t / sp.n[1];
+    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z0;
+    if (L.count && o + 3 >= L.lo && o <= L.hi && group_has_source(L, o)) return;
+    if (CURR) adj_u4_group<false>(a, sp, x, y, z0);
+    else adj_w4_group<false>(a, sp, x, y, z0);
+}
+
+// the main-box groups that hold a source cell, one thread each
+template <bool CURR>
+__global__ void __launch_bounds__(64) k_adj_box4_src(AdjDev a, SplitDev sp)
+{
+    const InjList& L = CURR ? a.injI : a.injV;
+    const GridDev& g = a.g;
+    const unsigned j = blockIdx.x * 64u + threadIdx.x;
+    if (j >= L.ngrp) return;
+    const unsigned long long og = L.grp[j];
+    const unsigned long long row = og / g.Pz;
+    const unsigned z0 = (unsigned)(og - row * g.Pz), y = (unsigned)(row % g.Ny), x = (unsigned)(row / g.Ny);
+    if (CURR) adj_u4_group<true>(a, sp, x, y, z0);
+    else adj_w4_group<true>(a, sp, x, y, z0);
 }
 
 // V^n and K_V I^n (the arithmetic of update_v_cell) in the design box, into slot
@@ -577,6 +627,30 @@ int build_injection(oems_cuda_engine* e, unsigned nprobe, const int* ids, int ty
     cudaMemcpyAsync(dr, row.data(), row.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream);
     cudaMemcpyAsync(dw, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, e->stream);
     L.cell = dc; L.comp = dm; L.row = dr; L.coef = dw;
+    // the main-box groups of four that hold a source cell (for k_adj_box4)
+    const SplitDev& sp = type == 0 ? e->splitV : e->splitI;
+    std::vector<unsigned long long> grp;
+    if (e->use_split && sp.v4) {
+        for (const unsigned long long c : cell) {
+            const unsigned long long r = c / e->Pz;
+            const unsigned z = (unsigned)(c - r * e->Pz), y = (unsigned)(r % e->N[1]), x = (unsigned)(r / e->N[1]);
+            const unsigned z0 = z & ~3u;
+            if (x >= sp.lo[0] && x < sp.lo[0] + sp.n[0] && y >= sp.lo[1] && y < sp.lo[1] + sp.n[1] && z0 >= sp.z4 &&
+                (z0 - sp.z4) / 4 < sp.n4)
+                grp.push_back(r * e->Pz + z0);
+        }
+        std::sort(grp.begin(), grp.end());
+        grp.erase(std::unique(grp.begin(), grp.end()), grp.end());
+    }
+    if (!grp.empty()) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, grp.size() * sizeof(unsigned long long)) != cudaSuccess)
+            return afail(e, OEMS_ERR_NOMEM, "adjoint source allocation");
+        tmp.push_back(q);
+        cudaMemcpyAsync(q, grp.data(), grp.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, e->stream);
+        L.grp = static_cast<const unsigned long long*>(q);
+        L.ngrp = (unsigned)grp.size();
+    }
     return OEMS_OK;
 }
 
@@ -764,10 +838,16 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
                     else k_adj_split<false><<<rblk, 256, 0, rst>>>(d, *sp[h]);
                 }
                 if (sp[h]->main_blocks4) {
-                    if (h == 0) k_adj_box4_u<<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
-                    else k_adj_box4_w<<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
+                    const unsigned ng = h == 0 ? d.injI.ngrp : d.injV.ngrp;
+                    if (h == 0) k_adj_box4<true><<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
+                    else k_adj_box4<false><<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
+                    if (ng) {
+                        if (h == 0) k_adj_box4_src<true><<<(ng + 63) / 64, 64, 0, rst>>>(d, *sp[h]);
+                        else k_adj_box4_src<false><<<(ng + 63) / 64, 64, 0, rst>>>(d, *sp[h]);
+                    }
                 }
             }
+            if (d.B) k_adj_grad<<<(d.B + 255) / 256, 256, 0, rst>>>(d);
         } else if (e->use_split) {
             if (bu) k_adj_split<true><<<bu, 256, 0, rst>>>(d, e->splitI);
             if (bw) k_adj_split<false><<<bw, 256, 0, rst>>>(d, e->splitV);

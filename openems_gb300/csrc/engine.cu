@@ -697,7 +697,12 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
         } else if (e->compressed) {
             if (o32 && e->vec4 && (mode == 0 || (mode == 2 && e->mur_v4))) {
                 const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
-                if (mode == 2) { if (go("k_update_v4w")) k_update_v4w<unsigned><<<gv4, 256, 0, s>>>(g, m, ts); }
+                if (mode == 2) {
+                    // the interior blocks, then one thread per direct column's z-wall group
+                    const unsigned walls = m.nz > 0 ? (e->N[1] * (unsigned)m.nz + 255) / 256 : 0;
+                    const dim3 gw(gv4.x + walls, e->N[0]);
+                    if (go("k_update_v4w")) k_update_v4w<unsigned><<<gw, 256, 0, s>>>(g, m, ts, gv4.x);
+                }
                 else if (go("k_update_v4")) k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
             } else if (o32) {
                 if (!go("k_update_v")) return;

@@ -554,44 +554,76 @@ __global__ void __launch_bounds__(256) k_update_v4(GridDev g)
     update_v4_cells<IX>(g, x, y, z0);
 }
 
-// k_update_v4 with the Mur walls' pre/post voltage hooks (FDTD/extensions/engine_ext_mur_abc.cpp:
-// 83-149) in the lane-parallel form (MurDev::lanes: every wall active from step 0).  The host
-// chooses it when each z wall's line and shift lie in one group of four z and no group holds
-// two walls.
-// - A column on an x/y wall line or shift (outside the windows: whole rows and planes, so whole
-//   warps) runs its four cells through the one-cell form of mode 2, which carries every hook.
-// - Every other column is direct: its z walls need no buffer.  The thread whose group holds a z
-//   wall's line and shift has V_old(line), V_old(shift) and V_new(shift) in registers and forms
-//     b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift)
-//   as the line's final tangential value, in the same float4 store.  Its two coefficient loads
-//   are issued with the field loads (predicated, no branch), so no warp waits on them alone.
+// Four cells (x, y, z0..z0+3) of a column on an x/y wall line or shift: the float4 update, then
+// per lane the hooks of mode 2 (mur_cell for the x/y walls, mur_z_keep / mur_z_shift for the z
+// walls) on the lane's old and new values, and a store of the lanes and components the hooks
+// leave to this update.  The lines' tangential components stay unwritten, so the shift lanes
+// (of other threads, and of this one for a z wall) read their old values from memory.
 template <typename IX = unsigned>
-__global__ void __launch_bounds__(256, 4) k_update_v4w(GridDev g, MurDev m, const unsigned* __restrict__ numTS)
+__device__ __forceinline__ void mur_wall_v4(const GridDev& g, const MurDev& m, unsigned ts, unsigned x, unsigned y,
+                                            unsigned z0)
 {
-    const unsigned x = blockIdx.y;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned pz4 = g.Pz >> 2;
-    const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
-    if (y >= g.Ny || z0 >= g.Nz) return;
-    if (mur_wall_cell<2>(m, x, y, 0u)) {
-        const unsigned ts = __ldg(numTS);
-        for (unsigned k = 0; k < 4u && z0 + k < g.Nz; ++k)
-            update_v_cell<true, false, false, 2, IX>(g, x, y, z0 + k, -2, 0, &m, ts);
-        return;
+    const IX S = (IX)g.S;
+    const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
+    const IX sx = x ? (IX)g.Ny * g.Pz : (IX)0;
+    const IX sy = y ? (IX)g.Pz : (IX)0;
+    const float* __restrict__ I = g.I;
+    float* __restrict__ V = g.V;
+    const float4 i0 = ldg4(I + o), i1 = ldg4(I + (S + o)), i2 = ldg4(I + (2 * S + o));
+    const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
+    const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
+    const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const float4 v0 = ld4(V + o), v1 = ld4(V + (S + o)), v2 = ld4(V + (2 * S + o));
+    float4 n0 = v0, n1 = v1, n2 = v2;
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    unsigned m0 = 15u, m1 = 15u, m2 = 15u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (z0 + k >= g.Nz) break;
+        const float4 ca = __ldg(g.tabV + 2 * cls[k]), cb = __ldg(g.tabV + 2 * cls[k] + 1);
+        const float i1z = k ? f4(i1, k - 1) : i1m, i0z = k ? f4(i0, k - 1) : i0m;
+        const float c0 = fadd(fsub(fsub(f4(i2, k), f4(i2y, k)), f4(i1, k)), i1z);
+        const float c1 = fadd(fsub(fsub(f4(i0, k), i0z), f4(i2, k)), f4(i2x, k));
+        const float c2 = fadd(fsub(fsub(f4(i1, k), f4(i1x, k)), f4(i0, k)), f4(i0y, k));
+        set4(n0, k, fadd(fmul(f4(v0, k), ca.x), fmul(ca.w, c0)));
+        set4(n1, k, fadd(fmul(f4(v1, k), ca.y), fmul(cb.x, c1)));
+        set4(n2, k, fadd(fmul(f4(v2, k), ca.z), fmul(cb.y, c2)));
+        const unsigned z = z0 + k;
+        unsigned keep = mur_cell<2>(g, m, ts, x, y, z, (unsigned long long)o + k, f4(v0, k), f4(v1, k), f4(v2, k),
+                                    f4(n0, k), f4(n1, k), f4(n2, k));
+        keep &= mur_z_keep(m, z);
+        mur_z_shift(g, m, x, y, z, (unsigned long long)o + k, f4(v0, k), f4(v1, k), f4(n0, k), f4(n1, k));
+        if (!(keep & 1u)) m0 &= ~(1u << k);
+        if (!(keep & 2u)) m1 &= ~(1u << k);
+        if (!(keep & 4u)) m2 &= ~(1u << k);
     }
-    // the z wall whose line lies in this group (selects, not a run-time index into the parameters)
-    const bool qa = m.nz > 0 && (m.z[0].line >> 2) == (z0 >> 2);
-    const bool qb = !qa && m.nz > 1 && (m.z[1].line >> 2) == (z0 >> 2);
-    const bool zw = qa || qb;
-    const unsigned kl = (qb ? m.z[1].line : m.z[0].line) - z0, ks = (qb ? m.z[1].shift : m.z[0].shift) - z0;
-    const float* cPp = qb ? m.z[1].cP : m.z[0].cP;
-    const float* cPPp = qb ? m.z[1].cPP : m.z[0].cPP;
+    st4_masked(V + o, n0, m0);                  // lanes past Nz-1 are padding: they keep their zero
+    st4_masked(V + (S + o), n1, m1);
+    st4_masked(V + (2 * S + o), n2, m2);
+}
+
+// the z wall whose line lies in the group of four z starting at z0, or -1
+__device__ __forceinline__ int mur_z_group(const MurDev& m, unsigned z0)
+{
+    if (m.nz > 0 && (m.z[0].line >> 2) == (z0 >> 2)) return 0;
+    if (m.nz > 1 && (m.z[1].line >> 2) == (z0 >> 2)) return 1;
+    return -1;
+}
+
+// The group of four z holding z wall q's line and shift in a direct column (inside both x/y
+// windows): the float4 update, with the wall's hooks on registers.  The thread has V_old(line),
+// V_old(shift) and V_new(shift) and forms
+//     b = (V_old(shift) - cP * V_old(line)) + cP * V_new(shift)
+// as the line's final tangential values, in the same float4 store (no wall buffer).
+template <typename IX = unsigned>
+__device__ __forceinline__ void mur_zwall_v4(const GridDev& g, const MurDev& m, unsigned x, unsigned y, unsigned q)
+{
+    const MurWallDev& W = q ? m.z[1] : m.z[0];
+    const unsigned z0 = W.line & ~3u;
+    const int kl = (int)(W.line - z0), ks = (int)(W.shift - z0);
     const unsigned kc = x * g.Ny + y;
-    float cP = 0.f, cPP = 0.f;
-    if (zw) {
-        cP = __ldg(cPp + kc);
-        cPP = __ldg(cPPp + kc);
-    }
+    const float cP = __ldg(W.cP + kc), cPP = __ldg(W.cPP + kc);
     const IX S = (IX)g.S;
     const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
     const IX sx = x ? (IX)g.Ny * g.Pz : (IX)0;
@@ -605,8 +637,8 @@ __global__ void __launch_bounds__(256, 4) k_update_v4w(GridDev g, MurDev m, cons
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
     // pre-voltage part, from the old values
-    const float pre0 = fsub(f4(n0, (int)ks), fmul(cP, f4(n0, (int)kl)));
-    const float pre1 = fsub(f4(n1, (int)ks), fmul(cPP, f4(n1, (int)kl)));
+    const float pre0 = fsub(f4(n0, ks), fmul(cP, f4(n0, kl)));
+    const float pre1 = fsub(f4(n1, ks), fmul(cPP, f4(n1, kl)));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -620,13 +652,48 @@ __global__ void __launch_bounds__(256, 4) k_update_v4w(GridDev g, MurDev m, cons
         set4(n1, k, fadd(fmul(f4(n1, k), ca.y), fmul(cb.x, c1)));
         set4(n2, k, fadd(fmul(f4(n2, k), ca.z), fmul(cb.y, c2)));
     }
-    if (zw) {                                   // post-voltage part and the apply of a direct column
-        set4(n0, (int)kl, fadd(pre0, fmul(cP, f4(n0, (int)ks))));
-        set4(n1, (int)kl, fadd(pre1, fmul(cPP, f4(n1, (int)ks))));
-    }
+    // post-voltage part and the apply of a direct column
+    set4(n0, kl, fadd(pre0, fmul(cP, f4(n0, ks))));
+    set4(n1, kl, fadd(pre1, fmul(cPP, f4(n1, ks))));
     *reinterpret_cast<float4*>(V + o) = n0;     // lanes past Nz-1 are padding: they keep their zero
     *reinterpret_cast<float4*>(V + (S + o)) = n1;
     *reinterpret_cast<float4*>(V + (2 * S + o)) = n2;
+}
+
+// k_update_v4 with the Mur walls' pre/post voltage hooks (FDTD/extensions/engine_ext_mur_abc.cpp:
+// 83-149) in the lane-parallel form (MurDev::lanes: every wall active from step 0).  The host
+// chooses it when each z wall's line and shift lie in one group of four z and no group holds
+// two walls.  The first `interior` blocks of a plane map its groups as k_update_v4 does:
+// - a column on an x/y wall line or shift (outside the windows: whole rows and planes, so whole
+//   warps) runs mur_wall_v4: the float4 update with mode 2's hooks lane by lane;
+// - in every other (direct) column, a group holding a z wall's line is left to the wall blocks,
+//   and the others run the plain float4 update, which then carries no hook code at all.
+// The blocks after them take one direct column's z-wall group per thread (mur_zwall_v4).  The
+// wall work thus sits in warps of its own, and the streaming warps keep k_update_v4's registers
+// and loads in flight.
+template <typename IX = unsigned>
+__global__ void __launch_bounds__(256, 4) k_update_v4w(GridDev g, MurDev m, const unsigned* __restrict__ numTS,
+                                                       unsigned interior)
+{
+    const unsigned x = blockIdx.y;
+    if (blockIdx.x < interior) {
+        const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+        const unsigned pz4 = g.Pz >> 2;
+        const unsigned y = t / pz4, z0 = (t - y * pz4) << 2;
+        if (y >= g.Ny || z0 >= g.Nz) return;
+        if (mur_wall_cell<2>(m, x, y, 0u)) {
+            mur_wall_v4<IX>(g, m, __ldg(numTS), x, y, z0);
+            return;
+        }
+        if (mur_z_group(m, z0) >= 0) return;
+        update_v4_cells<IX>(g, x, y, z0);
+        return;
+    }
+    const unsigned t = (blockIdx.x - interior) * blockDim.x + threadIdx.x;
+    const unsigned nz = (unsigned)m.nz;
+    const unsigned y = t / nz, q = t - y * nz;
+    if (y >= g.Ny || mur_wall_cell<2>(m, x, y, 0u)) return;
+    mur_zwall_v4<IX>(g, m, x, y, q);
 }
 
 template <bool COMPRESSED, bool UPML, typename IX = unsigned long long>
