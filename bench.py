@@ -187,10 +187,11 @@ def cpu_thread_sweep(op, budget_s, nproc):
     return out
 
 
-def measure_config(name, steps, e2e_steps=200):
+def measure_config(name, steps, e2e_steps=200, cpu_budget=0.0):
     """One more configuration on the GPU: device-timed MCells/s over `steps` replayed steps, and
     MCells/s end to end through the C ABI (iterate(1) + a synchronous read of every probe's new
-    sample per step, openEMS's processing loop)."""
+    sample per step, openEMS's processing loop); with cpu_budget > 0 also the CPU engine on every
+    host core for about that many seconds of steps."""
     from openems_gb300.engine import Engine_CUDA
     from openems_gb300.operator import build_device
     t0 = time.perf_counter()
@@ -218,6 +219,10 @@ def measure_config(name, steps, e2e_steps=200):
            "l2": "field state %.0f MB against a 129 MB L2: largely L2-resident, so no HBM fraction is claimed"
                  % state_mb}
     eng.close()
+    if cpu_budget > 0:
+        nproc = os.cpu_count() or 1
+        v, n, sec, kind = cpu_baseline(op, 100000, cpu_budget, nproc)
+        out["cpu"] = {"mcells_s": round(v, 1), "steps": n, "seconds": round(sec, 2), "cores": nproc, "kind": kind}
     return out
 
 
@@ -289,6 +294,30 @@ def measure_batched(count):
             "total_cells": sum(cells), "steps_min_max": [min(steps), max(steps)], "tuned": cfg,
             "series_equal_serial_spot_check": same, "build_s": round(t_build, 1),
             "serial_per_instance_cells_steps_s": per_inst}
+
+
+def batch_launch_case(count=32, steps=40):
+    """The batched-form instances for an ncu launch list: the largest instance alone for 48 steps
+    (its own split kernels from its graphs), then all `count` together for `steps` steps in
+    per-phase launches (one launch per phase over every instance)."""
+    from openems_gb300 import configs
+    from openems_gb300.batch import BatchEngine
+    from openems_gb300.engine import Engine_CUDA
+    inst = [configs.batch_instance(1000 + k) for k in range(count)]
+    big = max(range(count), key=lambda k: np.prod(inst[k][0].num_lines))
+    e = Engine_CUDA(inst[big][0], 64)
+    e.IterateTS(48)
+    e.sync()
+    kernels = e.update_kernels()
+    e.close()
+    engines = [Engine_CUDA(op, steps + 8) for op, _ in inst]
+    be = BatchEngine(engines)
+    be.run([steps] * count, block_size=256, depth=1 | 0x80000000)
+    cfg = be.config()
+    be.close()
+    for x in engines:
+        x.close()
+    return {"serial_instance": int(big), "lines": inst[big][0].num_lines.tolist(), "kernels": kernels, "batch": cfg}
 
 
 def measure_adjoint(steps=8000):
@@ -559,7 +588,9 @@ def main():
 
     others = None
     if rank == 0 and not args.no_configs:
-        others = {"plain_100": measure_config("plain", 2000), "patch_160x160x80": measure_config("patch", 1000)}
+        cb = 0.0 if args.no_cpu_baseline else 3.0
+        others = {"plain_100": measure_config("plain", 2000, cpu_budget=cb),
+                  "patch_160x160x80": measure_config("patch", 1000, cpu_budget=cb)}
 
     base = None
     sweep = None

@@ -43,21 +43,7 @@ struct InjList {
     const int* comp;                  // [count] component
     const int* row;                   // [count] source row (objective probe)
     const double* coef;               // [count] weight * sign
-    // the groups of four z of the split's main box (k_adj_box4_*) holding a source cell: their
-    // offsets (z a multiple of four); the float4 kernels leave them to blocks of their own
-    const unsigned long long* grp;
-    unsigned ngrp;
 };
-
-// true when one of the list's cells lies in the group of four at offset o
-__device__ __forceinline__ bool group_has_source(const InjList& L, unsigned long long o)
-{
-    for (unsigned k = 0; k < L.count; ++k) {
-        const unsigned long long c = L.cell[k];
-        if (c >= o && c < o + 4) return true;
-    }
-    return false;
-}
 
 struct AdjDev {
     GridDev g;
@@ -253,6 +239,113 @@ __global__ void __launch_bounds__(256) k_adj_w(AdjDev a)
     adj_w_cell(a, blockIdx.y, y, z, -2, 0);
 }
 
+// The UPML regions four z cells per thread (the forward's k_update_reg4 groups: aligned to four
+// z in the mesh, lanes outside the region computed but not stored): adj_u_cell / adj_w_cell's
+// region branch lane by lane, with 16-byte loads of the adjoint fields and, where the region's
+// z rows are whole groups, of the region-local adjoint arrays.  U lanes at z = Nz-1 (and groups at
+// x = Nx-1 or y = Ny-1) are not updated.
+template <bool CURR>
+__global__ void __launch_bounds__(256, 1) k_adj_reg4(const __grid_constant__ AdjDev a, const __grid_constant__ SplitDev sp)
+{
+    const GridDev& g = a.g;
+    const unsigned b = blockIdx.x;
+    int r = 0;
+    while (r + 1 < (int)sp.nreg && b >= sp.first4[r + 1]) ++r;
+    const UpmlDev& u = g.upml[r];
+    const unsigned j = (b - sp.first4[r]) * 256u + threadIdx.x;
+    if (j >= u.nl[0] * u.nl[1] * reg_groups_per_row(u)) return;
+    const RegGroup q = reg_group(u, j);
+    const unsigned x = q.x, y = q.y, z0 = q.z0;
+    if (CURR && (x + 1 >= g.Nx || y + 1 >= g.Ny)) return;
+    unsigned mask = q.mask;
+    if (CURR)
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (z0 + k + 1 >= g.Nz) mask &= ~(1u << k);
+    const unsigned S = (unsigned)g.S, n = u.n;
+    const unsigned o = (x * g.Ny + y) * g.Pz + z0;
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    unsigned ucl[4];
+    ld_cls(u.cls + q.loc0, q.vec, mask, ucl);
+    // the cell's adjoint state (lI / lV) and the flux adjoint (lphi / lpsi), region-local
+    float* const ls = (CURR ? a.lI[r] : a.lV[r]) + q.loc0;
+    float* const lf = (CURR ? a.lphi[r] : a.lpsi[r]) + q.loc0;
+    float4 s0 = ld_lanes(ls, q.vec, mask), s1 = ld_lanes(ls + n, q.vec, mask), s2 = ld_lanes(ls + 2 * n, q.vec, mask);
+    float4 f0 = ld_lanes(lf, q.vec, mask), f1 = ld_lanes(lf + n, q.vec, mask), f2 = ld_lanes(lf + 2 * n, q.vec, mask);
+    float4 d0, d1, d2;                          // K^T of the other adjoint field, lane by lane
+    if (CURR) {
+        const float* __restrict__ W = a.W;
+        const unsigned sx = g.Ny * g.Pz, sy = g.Pz;
+        const float4 w0 = ldg4(W + o), w1 = ldg4(W + (S + o)), w2 = ldg4(W + (2 * S + o));
+        const float w1z4 = __ldg(W + (S + o + 4)), w0z4 = __ldg(W + (o + 4));
+        const float4 w2y = ldg4(W + (2 * S + o + sy)), w0y = ldg4(W + (o + sy));
+        const float4 w2x = ldg4(W + (2 * S + o + sx)), w1x = ldg4(W + (S + o + sx));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned z = z0 + k;
+            const float a1z = k < 3 ? f4(w1, k + 1) : w1z4, a0z = k < 3 ? f4(w0, k + 1) : w0z4;
+            set4(d0, k, fadd(fsub(fsub(z > 0 ? f4(w1, k) : 0.f, a1z), y > 0 ? f4(w2, k) : 0.f), f4(w2y, k)));
+            set4(d1, k, fadd(fsub(fsub(x > 0 ? f4(w2, k) : 0.f, f4(w2x, k)), z > 0 ? f4(w0, k) : 0.f), a0z));
+            set4(d2, k, fadd(fsub(fsub(y > 0 ? f4(w0, k) : 0.f, f4(w0y, k)), x > 0 ? f4(w1, k) : 0.f), f4(w1x, k)));
+        }
+    } else {
+        const float* __restrict__ U = a.U;
+        const unsigned sx = x ? g.Ny * g.Pz : 0u, sy = y ? g.Pz : 0u;
+        const float4 u0 = ldg4(U + o), u1 = ldg4(U + (S + o)), u2 = ldg4(U + (2 * S + o));
+        const float u1m = z0 ? __ldg(U + (S + o - 1)) : 0.f, u0m = z0 ? __ldg(U + (o - 1)) : 0.f;
+        const float4 u2y = ldg4(U + (2 * S + o - sy)), u0y = ldg4(U + (o - sy));
+        const float4 u2x = ldg4(U + (2 * S + o - sx)), u1x = ldg4(U + (S + o - sx));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned z = z0 + k;
+            const float b1z = k ? f4(u1, k - 1) : u1m, b0z = k ? f4(u0, k - 1) : u0m;
+            set4(d0, k, fadd(fsub(fsub(f4(u1, k), z ? b1z : 0.f), f4(u2, k)), y ? f4(u2y, k) : 0.f));
+            set4(d1, k, fsub(fadd(fsub(f4(u2, k), x ? f4(u2x, k) : 0.f), z ? b0z : 0.f), f4(u0, k)));
+            set4(d2, k, fadd(fsub(fsub(f4(u0, k), y ? f4(u0y, k) : 0.f), f4(u1, k)), x ? f4(u1x, k) : 0.f));
+        }
+    }
+    const InjList& L = CURR ? a.injI : a.injV;
+    const bool src = L.count && (unsigned long long)o + 3 >= L.lo && (unsigned long long)o <= L.hi;
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    const float4* tab = CURR ? g.tabI : g.tabV;
+    float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0, o2 = o0;   // the new U / W
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!(mask & (1u << k))) continue;
+        float dd[3] = {f4(d0, k), f4(d1, k), f4(d2, k)};
+        if (src) add_sources(a, L, (unsigned long long)o + k, dd);
+        const float4 ca = __ldg(tab + 2 * cls[k]), cb = __ldg(tab + 2 * cls[k] + 1);
+        const float4* t = u.ctab + 6u * ucl[k] + (CURR ? 3 : 0);
+        const float4 pa = __ldg(t), pb = __ldg(t + 1), pd = __ldg(t + 2);
+        const float pc[9] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w, pd.x};
+        const float cd[3] = {ca.x, ca.y, ca.z}, cs[3] = {ca.w, cb.x, cb.y};   // (ii, iv) or (vv, vi)
+        const float st[3] = {f4(s0, k), f4(s1, k), f4(s2, k)};
+        const float fl[3] = {f4(f0, k), f4(f1, k), f4(f2, k)};
+        float on[3], fn[3], sn[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const float lam = fadd(st[m], dd[m]);               // adjoint of the field after the step
+            const float lin = fadd(fmul(pc[6 + m], lam), fl[m]);   // post^T: F = h + fn*flux
+            on[m] = fmul(cs[m], lin);
+            fn[m] = fsub(fmul(cd[m], lin), fmul(pc[3 + m], lam));  // pre^T: f = c*F - fo*flux
+            sn[m] = fmul(pc[m], lam);
+        }
+        set4(o0, k, on[0]); set4(o1, k, on[1]); set4(o2, k, on[2]);
+        set4(f0, k, fn[0]); set4(f1, k, fn[1]); set4(f2, k, fn[2]);
+        set4(s0, k, sn[0]); set4(s1, k, sn[1]); set4(s2, k, sn[2]);
+    }
+    float* __restrict__ F = CURR ? a.U : a.W;
+    st4_masked(F + o, o0, mask);
+    st4_masked(F + (S + o), o1, mask);
+    st4_masked(F + (2 * S + o), o2, mask);
+    st_lanes(lf, f0, q.vec, mask);
+    st_lanes(lf + n, f1, q.vec, mask);
+    st_lanes(lf + 2 * n, f2, q.vec, mask);
+    st_lanes(ls, s0, q.vec, mask);
+    st_lanes(ls + n, s1, q.vec, mask);
+    st_lanes(ls + 2 * n, s2, q.vec, mask);
+}
+
 // the engine's UPML work split (k_update_split): the region blocks first, then the blocks of the
 // cells outside every region (a launch of the first first_block[nreg] blocks covers the regions
 // alone, followed by k_adj_box4_* over the main box)
@@ -296,8 +389,7 @@ __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
 // adj_u_cell / adj_w_cell's arithmetic per lane, with the float4 loads of the forward's
 // update_*4_cells.  Lane k is cell z0 + k; groups start on multiples of four, and lanes outside
 // the box's z range are computed but not stored (their cells belong to the region blocks).
-// one group of four of the U update in k_adj_box4<true>; SRC: the group holds source cells of injI
-template <bool SRC>
+// one group of four of the U update in k_adj_box4<true>
 __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp, unsigned x, unsigned y, unsigned z0)
 {
     unsigned mask = 0u;
@@ -315,6 +407,7 @@ __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 u0 = ld4(a.U + o), u1 = ld4(a.U + (S + o)), u2 = ld4(a.U + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    const bool src = a.injI.count && (unsigned long long)o + 3 >= a.injI.lo && (unsigned long long)o <= a.injI.hi;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const unsigned z = z0 + k;
@@ -324,7 +417,7 @@ __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp
             fadd(fsub(fsub(z > 0 ? f4(w1, k) : 0.f, a1z), y > 0 ? f4(w2, k) : 0.f), f4(w2y, k)),
             fadd(fsub(fsub(x > 0 ? f4(w2, k) : 0.f, f4(w2x, k)), z > 0 ? f4(w0, k) : 0.f), a0z),
             fadd(fsub(fsub(y > 0 ? f4(w0, k) : 0.f, f4(w0y, k)), x > 0 ? f4(w1, k) : 0.f), f4(w1x, k))};
-        if (SRC) add_sources(a, a.injI, (unsigned long long)o + k, d);
+        if (src) add_sources(a, a.injI, (unsigned long long)o + k, d);
         set4(u0, k, fadd(fmul(ca.x, f4(u0, k)), fmul(ca.w, d[0])));
         set4(u1, k, fadd(fmul(ca.y, f4(u1, k)), fmul(cb.x, d[1])));
         set4(u2, k, fadd(fmul(ca.z, f4(u2, k)), fmul(cb.y, d[2])));
@@ -334,8 +427,7 @@ __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp
     st4_masked(a.U + (2 * S + o), u2, mask);
 }
 
-// one group of four of the W update in k_adj_box4<false>; SRC: the group holds source cells of injV
-template <bool SRC>
+// one group of four of the W update in k_adj_box4<false>
 __device__ __forceinline__ void adj_w4_group(const AdjDev& a, const SplitDev& sp, unsigned x, unsigned y, unsigned z0)
 {
     unsigned mask = 0u;
@@ -353,6 +445,7 @@ __device__ __forceinline__ void adj_w4_group(const AdjDev& a, const SplitDev& sp
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 n0 = ld4(a.W + o), n1 = ld4(a.W + (S + o)), n2 = ld4(a.W + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    const bool src = a.injV.count && (unsigned long long)o + 3 >= a.injV.lo && (unsigned long long)o <= a.injV.hi;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const unsigned z = z0 + k;
@@ -363,7 +456,7 @@ __device__ __forceinline__ void adj_w4_group(const AdjDev& a, const SplitDev& sp
             fadd(fsub(fsub(f4(u1, k), z ? b1z : 0.f), f4(u2, k)), y ? f4(u2y, k) : 0.f),
             fsub(fadd(fsub(f4(u2, k), x ? f4(u2x, k) : 0.f), z ? b0z : 0.f), f4(u0, k)),
             fadd(fsub(fsub(f4(u0, k), y ? f4(u0y, k) : 0.f), f4(u1, k)), x ? f4(u1x, k) : 0.f)};
-        if (SRC) add_sources(a, a.injV, (unsigned long long)o + k, gs);
+        if (src) add_sources(a, a.injV, (unsigned long long)o + k, gs);
         const float vv[3] = {ca.x, ca.y, ca.z}, vi[3] = {ca.w, cb.x, cb.y};
         const float wn[3] = {fadd(fmul(vv[0], f4(n0, k)), fmul(vi[0], gs[0])),
                              fadd(fmul(vv[1], f4(n1, k)), fmul(vi[1], gs[1])),
@@ -402,39 +495,18 @@ __global__ void __launch_bounds__(256) k_adj_grad(AdjDev a)
     }
 }
 
-// The main box four cells per thread.  The groups that hold a source cell are skipped and left to
-// k_adj_box4_src: without the source code these threads fit 64 registers with no spills (with it
-// inlined, even in blocks of their own, the kernel spills).
+// The main box four cells per thread (the groups holding probe sources add them inline).
 template <bool CURR>
 __global__ void __launch_bounds__(256, 4) k_adj_box4(AdjDev a, SplitDev sp)
 {
-    const InjList& L = CURR ? a.injI : a.injV;
-    const GridDev& g = a.g;
     unsigned t = blockIdx.x * 256u + threadIdx.x;
     if (t >= sp.main_cells4) return;
     const unsigned z0 = sp.z4 + ((t % sp.n4) << 2);
     t /= sp.n4;
     const unsigned y = sp.lo[1] + t % sp.n[1];
     const unsigned x = sp.lo[0] + t / sp.n[1];
-    const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z0;
-    if (L.count && o + 3 >= L.lo && o <= L.hi && group_has_source(L, o)) return;
-    if (CURR) adj_u4_group<false>(a, sp, x, y, z0);
-    else adj_w4_group<false>(a, sp, x, y, z0);
-}
-
-// the main-box groups that hold a source cell, one thread each
-template <bool CURR>
-__global__ void __launch_bounds__(64) k_adj_box4_src(AdjDev a, SplitDev sp)
-{
-    const InjList& L = CURR ? a.injI : a.injV;
-    const GridDev& g = a.g;
-    const unsigned j = blockIdx.x * 64u + threadIdx.x;
-    if (j >= L.ngrp) return;
-    const unsigned long long og = L.grp[j];
-    const unsigned long long row = og / g.Pz;
-    const unsigned z0 = (unsigned)(og - row * g.Pz), y = (unsigned)(row % g.Ny), x = (unsigned)(row / g.Ny);
-    if (CURR) adj_u4_group<true>(a, sp, x, y, z0);
-    else adj_w4_group<true>(a, sp, x, y, z0);
+    if (CURR) adj_u4_group(a, sp, x, y, z0);
+    else adj_w4_group(a, sp, x, y, z0);
 }
 
 // V^n and K_V I^n (the arithmetic of update_v_cell) in the design box, into slot
@@ -488,8 +560,11 @@ struct oems_adjoint_state {
     cudaStream_t rs = nullptr;
     cudaEvent_t ev_recomputed[2] = {nullptr, nullptr};
     cudaEvent_t ev_reversed[2] = {nullptr, nullptr};
-    // UPML split with a float4 main box (k_adj_box4_*)
+    // UPML split with a float4 main box (k_adj_box4): the design-box sums (k_adj_grad) run on
+    // `gs`, after ev_w (W of the step done), and the next W update waits for ev_grad
     bool box4 = false;
+    cudaStream_t gs = nullptr;
+    cudaEvent_t ev_w = nullptr, ev_grad = nullptr;
     float fwd_ms = 0.f, bwd_ms = 0.f;
     unsigned launches_per_reverse_step = 0;
 };
@@ -627,30 +702,6 @@ int build_injection(oems_cuda_engine* e, unsigned nprobe, const int* ids, int ty
     cudaMemcpyAsync(dr, row.data(), row.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream);
     cudaMemcpyAsync(dw, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, e->stream);
     L.cell = dc; L.comp = dm; L.row = dr; L.coef = dw;
-    // the main-box groups of four that hold a source cell (for k_adj_box4)
-    const SplitDev& sp = type == 0 ? e->splitV : e->splitI;
-    std::vector<unsigned long long> grp;
-    if (e->use_split && sp.v4) {
-        for (const unsigned long long c : cell) {
-            const unsigned long long r = c / e->Pz;
-            const unsigned z = (unsigned)(c - r * e->Pz), y = (unsigned)(r % e->N[1]), x = (unsigned)(r / e->N[1]);
-            const unsigned z0 = z & ~3u;
-            if (x >= sp.lo[0] && x < sp.lo[0] + sp.n[0] && y >= sp.lo[1] && y < sp.lo[1] + sp.n[1] && z0 >= sp.z4 &&
-                (z0 - sp.z4) / 4 < sp.n4)
-                grp.push_back(r * e->Pz + z0);
-        }
-        std::sort(grp.begin(), grp.end());
-        grp.erase(std::unique(grp.begin(), grp.end()), grp.end());
-    }
-    if (!grp.empty()) {
-        void* q = nullptr;
-        if (cudaMalloc(&q, grp.size() * sizeof(unsigned long long)) != cudaSuccess)
-            return afail(e, OEMS_ERR_NOMEM, "adjoint source allocation");
-        tmp.push_back(q);
-        cudaMemcpyAsync(q, grp.data(), grp.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, e->stream);
-        L.grp = static_cast<const unsigned long long*>(q);
-        L.ngrp = (unsigned)grp.size();
-    }
     return OEMS_OK;
 }
 
@@ -719,6 +770,10 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess)
         return afail(e, OEMS_ERR_CUDA, "adjoint events");
     s->box4 = e->use_split && e->compressed && e->splitI.v4 && e->splitV.v4;
+    if (s->box4 && (cudaStreamCreateWithFlags(&s->gs, cudaStreamNonBlocking) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&s->ev_w, cudaEventDisableTiming) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&s->ev_grad, cudaEventDisableTiming) != cudaSuccess))
+        return afail(e, OEMS_ERR_CUDA, "adjoint gradient stream");
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) return afail(e, OEMS_ERR_CUDA, "adjoint setup sync");
     return OEMS_OK;
 }
@@ -829,25 +884,31 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         d.fv = slot;
         d.fc = slot + 3 * d.B;
         if (e->use_split && s->box4) {
-            // per half-step: the region blocks, then the main box four cells per thread
+            // per half-step: the region blocks, then the main box four cells per thread. The
+            // design-box sums of step n run on the side stream, beside the U update of step n-1
+            // (which only reads W); the W update of step n-1 waits for them.
             const SplitDev* sp[2] = {&e->splitI, &e->splitV};
             for (int h = 0; h < 2; ++h) {
-                const unsigned rblk = sp[h]->first_block[sp[h]->nreg];
-                if (rblk) {
+                if (h == 1) cudaStreamWaitEvent(rst, s->ev_grad, 0);
+                if (sp[h]->reg4) {
+                    const unsigned rblk = sp[h]->first4[sp[h]->nreg];
+                    if (h == 0) k_adj_reg4<true><<<rblk, 256, 0, rst>>>(d, *sp[h]);
+                    else k_adj_reg4<false><<<rblk, 256, 0, rst>>>(d, *sp[h]);
+                } else if (const unsigned rblk = sp[h]->first_block[sp[h]->nreg]) {
                     if (h == 0) k_adj_split<true><<<rblk, 256, 0, rst>>>(d, *sp[h]);
                     else k_adj_split<false><<<rblk, 256, 0, rst>>>(d, *sp[h]);
                 }
                 if (sp[h]->main_blocks4) {
-                    const unsigned ng = h == 0 ? d.injI.ngrp : d.injV.ngrp;
                     if (h == 0) k_adj_box4<true><<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
                     else k_adj_box4<false><<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
-                    if (ng) {
-                        if (h == 0) k_adj_box4_src<true><<<(ng + 63) / 64, 64, 0, rst>>>(d, *sp[h]);
-                        else k_adj_box4_src<false><<<(ng + 63) / 64, 64, 0, rst>>>(d, *sp[h]);
-                    }
                 }
             }
-            if (d.B) k_adj_grad<<<(d.B + 255) / 256, 256, 0, rst>>>(d);
+            if (d.B) {
+                cudaEventRecord(s->ev_w, rst);
+                cudaStreamWaitEvent(s->gs, s->ev_w, 0);
+                k_adj_grad<<<(d.B + 255) / 256, 256, 0, s->gs>>>(d);
+                cudaEventRecord(s->ev_grad, s->gs);
+            }
         } else if (e->use_split) {
             if (bu) k_adj_split<true><<<bu, 256, 0, rst>>>(d, e->splitI);
             if (bw) k_adj_split<false><<<bw, 256, 0, rst>>>(d, e->splitV);
@@ -889,14 +950,17 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
             cudaStreamWaitEvent(s->rs, s->ev_recomputed[seg & 1], 0);
             const float* base = s->fac + (seg & 1) * half;
             for (int n = (int)a1 - 1; n >= (int)a0; --n) reverse((unsigned)n, base + (size_t)(n % s->K) * 6 * d.B, s->rs);
+            if (s->ev_grad) cudaStreamWaitEvent(s->rs, s->ev_grad, 0);   // the sums read this half too
             cudaEventRecord(s->ev_reversed[seg & 1], s->rs);
             if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
         }
         // the gradients, the timing event and the state restore follow the last sweep
+        if (s->ev_grad) cudaStreamWaitEvent(s->rs, s->ev_grad, 0);
         cudaEventRecord(s->ev_reversed[0], s->rs);
         cudaStreamWaitEvent(st, s->ev_reversed[0], 0);
     } else {
         for (int n = (int)N - 1; n >= 0; --n) reverse((unsigned)n, s->fac + (size_t)n * 6 * d.B, st);
+        if (s->ev_grad) cudaStreamWaitEvent(st, s->ev_grad, 0);
         if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
     }
     s->launches_per_reverse_step = lps;
@@ -912,6 +976,7 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         cudaStreamSynchronize(st);
     }
     if (s->rs) cudaStreamSynchronize(s->rs);
+    if (s->gs) cudaStreamSynchronize(s->gs);
     release();
     d.src = nullptr;
     d.injV = InjList{};
@@ -943,5 +1008,8 @@ void oems_adjoint_free(oems_adjoint_state* s)
         if (s->ev_reversed[b]) cudaEventDestroy(s->ev_reversed[b]);
     }
     if (s->rs) cudaStreamDestroy(s->rs);
+    if (s->ev_w) cudaEventDestroy(s->ev_w);
+    if (s->ev_grad) cudaEventDestroy(s->ev_grad);
+    if (s->gs) cudaStreamDestroy(s->gs);
     delete s;
 }

@@ -632,6 +632,18 @@ void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp)
     sp.main_blocks4 = (sp.main_cells4 + 255) / 256;
     sp.first_block[0] = 0;
     for (int r = 0; r < g.nupml; ++r) sp.first_block[r + 1] = sp.first_block[r] + (g.upml[r].n + 255) / 256;
+    // the regions four z cells per thread (k_update_reg4): each region on z rows of whole groups
+    // of four, its coefficients in classes; OEMS_CUDA_REG4=0 keeps the one-cell region blocks
+    const char* r4 = getenv("OEMS_CUDA_REG4");
+    sp.reg4 = (sp.v4 && g.nupml > 0 && !(r4 && r4[0] == '0')) ? 1 : 0;
+    sp.first4[0] = 0;
+    for (int r = 0; r < g.nupml; ++r) {
+        const UpmlDev& u = g.upml[r];
+        if (!u.cls) sp.reg4 = 0;
+        const unsigned zs = u.start[2], ze = zs + u.nl[2];
+        const unsigned groups = u.nl[0] * u.nl[1] * ((((ze + 3u) & ~3u) - (zs & ~3u)) / 4u);
+        sp.first4[r + 1] = sp.first4[r] + (groups + 255) / 256;
+    }
 }
 
 template <bool C, bool U, int M, typename IX = unsigned long long>
@@ -657,9 +669,11 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
         if (sp.v4 && !mur) {
             // the region blocks, then the main box four cells per thread (the two write disjoint
             // cells; as separate launches each gets its own register budget)
-            if (!go("k_update_split+k_update_box4")) return;
-            const unsigned rb = sp.first_block[sp.nreg];
-            if (rb) {
+            if (!go(sp.reg4 ? "k_update_reg4+k_update_box4" : "k_update_split+k_update_box4")) return;
+            if (sp.reg4) {
+                if (curr) k_update_reg4<true><<<sp.first4[sp.nreg], 256, 0, s>>>(g, sp);
+                else k_update_reg4<false><<<sp.first4[sp.nreg], 256, 0, s>>>(g, sp);
+            } else if (const unsigned rb = sp.first_block[sp.nreg]) {
                 if (curr) k_update_split<true, true><<<rb, 256, 0, s>>>(g, sp, m, ts);
                 else k_update_split<true, false><<<rb, 256, 0, s>>>(g, sp, m, ts);
             }

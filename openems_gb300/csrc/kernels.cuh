@@ -724,6 +724,8 @@ struct SplitDev {
     unsigned main_cells4, main_blocks4;        // groups of four and their blocks when v4
     unsigned nreg;
     unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1])
+    int reg4;                                  // 1: the regions four z cells per thread (k_update_reg4)
+    unsigned first4[OEMS_MAX_UPML + 1];        // region r: its blocks of groups of four
 };
 
 // The compressed-operator form without Mur hooks fits 32 registers (a few bytes spill to L1), so
@@ -785,6 +787,175 @@ __global__ void __launch_bounds__(256) k_update_box4(GridDev g, SplitDev sp)
     for (int k = 0; k < 4; ++k) mask |= (z + k >= zlo && z + k < zhi) ? (1u << k) : 0u;
     if (CURR) update_i4_cells<unsigned>(g, x, y, z, mask);
     else update_v4_cells<unsigned>(g, x, y, z, mask);
+}
+
+// Region-local arrays (fluxes, classes) in the float4 region kernels: a group's four lanes are
+// four consecutive local offsets starting at p (lane 0).  When the region's z rows start and end
+// on multiples of four (`vec`) they are one aligned vector; otherwise the lanes of `mask` are
+// read and written one by one (p may then point before the row: masked lanes are not touched).
+__device__ __forceinline__ float4 ld_lanes(const float* p, bool vec, unsigned mask)
+{
+    if (vec) return ld4(p);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (mask & 1u) v.x = p[0];
+    if (mask & 2u) v.y = p[1];
+    if (mask & 4u) v.z = p[2];
+    if (mask & 8u) v.w = p[3];
+    return v;
+}
+
+__device__ __forceinline__ void st_lanes(float* p, const float4 v, bool vec, unsigned mask)
+{
+    if (vec && mask == 15u) {
+        *reinterpret_cast<float4*>(p) = v;
+        return;
+    }
+    if (mask & 1u) p[0] = v.x;
+    if (mask & 2u) p[1] = v.y;
+    if (mask & 4u) p[2] = v.z;
+    if (mask & 8u) p[3] = v.w;
+}
+
+__device__ __forceinline__ void ld_cls(const unsigned short* p, bool vec, unsigned mask, unsigned c[4])
+{
+    if (vec) {
+        const ushort4 u = __ldg(reinterpret_cast<const ushort4*>(p));
+        c[0] = u.x; c[1] = u.y; c[2] = u.z; c[3] = u.w;
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) c[k] = (mask & (1u << k)) ? __ldg(p + k) : 0u;
+}
+
+// A UPML region's groups of four z (aligned to multiples of four in the mesh, like the main box):
+// groups per z row, and the group `j` of the region as (x, y, z0, local offset of lane 0, lane
+// mask of the cells inside the region)
+struct RegGroup {
+    unsigned x, y, z0, mask;
+    int loc0;
+    bool vec;
+};
+
+__device__ __forceinline__ unsigned reg_groups_per_row(const UpmlDev& u)
+{
+    const unsigned zs = u.start[2], ze = zs + u.nl[2];
+    return (((ze + 3u) & ~3u) - (zs & ~3u)) >> 2;
+}
+
+__device__ __forceinline__ RegGroup reg_group(const UpmlDev& u, unsigned j)
+{
+    const unsigned ngz = reg_groups_per_row(u);
+    const unsigned row = j / ngz, gz = j - row * ngz;
+    const unsigned zs = u.start[2], ze = zs + u.nl[2];
+    RegGroup q;
+    q.z0 = (zs & ~3u) + (gz << 2);
+    q.x = u.start[0] + row / u.nl[1];
+    q.y = u.start[1] + row % u.nl[1];
+    q.mask = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q.mask |= (q.z0 + k >= zs && q.z0 + k < ze) ? (1u << k) : 0u;
+    q.loc0 = (int)(row * u.nl[2]) + (int)q.z0 - (int)zs;
+    q.vec = (zs % 4u == 0u) && (u.nl[2] % 4u == 0u);
+    return q;
+}
+
+// The UPML regions four z cells per thread: update_v_cell / update_i_cell's UPML branch lane by
+// lane.  Groups are aligned to multiples of four z in the mesh, so every field and class-index
+// load is a 16-byte vector; lanes outside the region are computed on the side and not stored
+// (they belong to another region or the main box), and the region-local fluxes and classes are
+// vectors when the region's z rows are whole groups (ld_lanes).  Current lanes at z = Nz-1 (and
+// groups at x = Nx-1 or y = Ny-1) are not updated, as in the one-cell form.
+template <bool CURR>
+__global__ void __launch_bounds__(256) k_update_reg4(const __grid_constant__ GridDev g, const __grid_constant__ SplitDev sp)
+{
+    const unsigned b = blockIdx.x;
+    int r = 0;
+    while (r + 1 < (int)sp.nreg && b >= sp.first4[r + 1]) ++r;
+    const UpmlDev& u = g.upml[r];
+    const unsigned j = (b - sp.first4[r]) * 256u + threadIdx.x;
+    if (j >= u.nl[0] * u.nl[1] * reg_groups_per_row(u)) return;
+    const RegGroup q = reg_group(u, j);
+    const unsigned x = q.x, y = q.y, z0 = q.z0;
+    if (CURR && (x + 1 >= g.Nx || y + 1 >= g.Ny)) return;
+    unsigned mask = q.mask;
+    if (CURR)
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (z0 + k + 1 >= g.Nz) mask &= ~(1u << k);
+    const unsigned S = (unsigned)g.S, n = u.n;
+    const unsigned o = (x * g.Ny + y) * g.Pz + z0;
+    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    unsigned ucl[4];
+    ld_cls(u.cls + q.loc0, q.vec, mask, ucl);
+    float* __restrict__ flux = CURR ? u.iflux : u.vflux;
+    float* const f0p = flux + q.loc0;
+    float4 fl0 = ld_lanes(f0p, q.vec, mask), fl1 = ld_lanes(f0p + n, q.vec, mask), fl2 = ld_lanes(f0p + 2 * n, q.vec, mask);
+    float4 c0v, c1v, c2v;                       // curls, lane by lane
+    float4 a0, a1, a2;                          // the field being updated
+    float* __restrict__ F;
+    if (CURR) {
+        const float* __restrict__ V = g.V;
+        F = g.I;
+        const unsigned sx = g.Ny * g.Pz, sy = g.Pz;
+        const float4 w0 = ldg4(V + o), w1 = ldg4(V + (S + o)), w2 = ldg4(V + (2 * S + o));
+        const float4 w2y = ldg4(V + (2 * S + o + sy)), w0y = ldg4(V + (o + sy));
+        const float4 w2x = ldg4(V + (2 * S + o + sx)), w1x = ldg4(V + (S + o + sx));
+        const float w0z4 = z0 + 4 < g.Pz ? __ldg(V + (o + 4)) : 0.f, w1z4 = z0 + 4 < g.Pz ? __ldg(V + (S + o + 4)) : 0.f;
+        a0 = ld4(F + o); a1 = ld4(F + (S + o)); a2 = ld4(F + (2 * S + o));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float v1z = k < 3 ? f4(w1, k + 1) : w1z4, v0z = k < 3 ? f4(w0, k + 1) : w0z4;
+            set4(c0v, k, fadd(fsub(fsub(f4(w2, k), f4(w2y, k)), f4(w1, k)), v1z));
+            set4(c1v, k, fadd(fsub(fsub(f4(w0, k), v0z), f4(w2, k)), f4(w2x, k)));
+            set4(c2v, k, fadd(fsub(fsub(f4(w1, k), f4(w1x, k)), f4(w0, k)), f4(w0y, k)));
+        }
+    } else {
+        const float* __restrict__ I = g.I;
+        F = g.V;
+        const unsigned sx = x ? g.Ny * g.Pz : 0u, sy = y ? g.Pz : 0u;
+        const float4 i0 = ldg4(I + o), i1 = ldg4(I + (S + o)), i2 = ldg4(I + (2 * S + o));
+        const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
+        const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
+        const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
+        a0 = ld4(F + o); a1 = ld4(F + (S + o)); a2 = ld4(F + (2 * S + o));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float i1z = k ? f4(i1, k - 1) : i1m, i0z = k ? f4(i0, k - 1) : i0m;
+            set4(c0v, k, fadd(fsub(fsub(f4(i2, k), f4(i2y, k)), f4(i1, k)), i1z));
+            set4(c1v, k, fadd(fsub(fsub(f4(i0, k), i0z), f4(i2, k)), f4(i2x, k)));
+            set4(c2v, k, fadd(fsub(fsub(f4(i1, k), f4(i1x, k)), f4(i0, k)), f4(i0y, k)));
+        }
+    }
+    const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    const float4* tab = CURR ? g.tabI : g.tabV;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!(mask & (1u << k))) continue;
+        const float4 ca = __ldg(tab + 2 * cls[k]), cb = __ldg(tab + 2 * cls[k] + 1);
+        const float4* t = u.ctab + 6u * ucl[k] + (CURR ? 3 : 0);
+        const float4 pa = __ldg(t), pb = __ldg(t + 1), pd = __ldg(t + 2);
+        const float pc[9] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w, pd.x};
+        const float cvv[3] = {ca.x, ca.y, ca.z}, cvi[3] = {ca.w, cb.x, cb.y};
+        const float fin[3] = {f4(a0, k), f4(a1, k), f4(a2, k)};
+        const float cc[3] = {f4(c0v, k), f4(c1v, k), f4(c2v, k)};
+        const float fx[3] = {f4(fl0, k), f4(fl1, k), f4(fl2, k)};
+        float out[3], nf[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            // pre: f = c*F - fo*flux; F = flux; flux = f.  update.  post: h = flux; flux = F; F = h + fn*flux
+            const float f = fsub(fmul(pc[m], fin[m]), fmul(pc[3 + m], fx[m]));
+            nf[m] = fadd(fmul(fx[m], cvv[m]), fmul(cvi[m], cc[m]));
+            out[m] = fadd(f, fmul(pc[6 + m], nf[m]));
+        }
+        set4(a0, k, out[0]); set4(a1, k, out[1]); set4(a2, k, out[2]);
+        set4(fl0, k, nf[0]); set4(fl1, k, nf[1]); set4(fl2, k, nf[2]);
+    }
+    st4_masked(F + o, a0, mask);
+    st4_masked(F + (S + o), a1, mask);
+    st4_masked(F + (2 * S + o), a2, mask);
+    st_lanes(f0p, fl0, q.vec, mask);
+    st_lanes(f0p + n, fl1, q.vec, mask);
+    st_lanes(f0p + 2 * n, fl2, q.vec, mask);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -145,6 +145,26 @@ def test_separate_mur_hooks_bit_exact_against_oracle(cuda_lib, monkeypatch, name
     assert not bad, (name, bad)
 
 
+REG4_CASES = [
+    ("patch_pml8", lambda: configs.patch(shape=(56, 52, 36), steps=220, with_nf2ff=False), 220),
+    ("plane_wave_pml4", lambda: configs.plane_wave(n=(28, 24, 32), pml=4, steps=200), 200),
+    ("mixed_upml_pml4", lambda: configs.small_mixed(n=(26, 22, 24), bc=(3, 3, 3, 3, 3, 3), pml=4, dispersive=False,
+                                                    steps=180), 180),
+]
+
+
+@pytest.mark.parametrize("name,fn,steps", REG4_CASES)
+def test_upml_regions_float4_bit_exact_against_oracle(cuda_lib, name, fn, steps):
+    """UPML regions four z cells per thread (k_update_reg4), mixed with single steps: the fields,
+    probes and dumps equal the oracle's bit for bit."""
+    op = fn()
+    g, r = _run_pair(op, steps, chunks=(1, 7, 16, 33))
+    assert g.update_kernels()[0].startswith("k_update_reg4"), g.update_kernels()
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, (name, bad)
+
+
 def test_dense_operator_path_equals_compressed(cuda_lib):
     op = configs.small_mixed(steps=120)
     a = Engine_CUDA(op, 120)
