@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <new>
 #include <vector>
 
@@ -43,7 +44,21 @@ struct InjList {
     const int* comp;                  // [count] component
     const int* row;                   // [count] source row (objective probe)
     const double* coef;               // [count] weight * sign
+    // the split main box's groups of four z (k_adj_box4) that hold a source cell: their offsets (z
+    // a multiple of four).  The float4 box kernel skips them; blocks of their own update them.
+    const unsigned long long* grp;
+    unsigned ngrp;
 };
+
+// true when one of the list's cells lies in the group of four at offset o
+__device__ __forceinline__ bool group_has_source(const InjList& L, unsigned long long o)
+{
+    for (unsigned k = 0; k < L.count; ++k) {
+        const unsigned long long c = L.cell[k];
+        if (c >= o && c < o + 4) return true;
+    }
+    return false;
+}
 
 struct AdjDev {
     GridDev g;
@@ -62,6 +77,13 @@ struct AdjDev {
     const double* src;    // [rows][stride]
     unsigned stride;
     unsigned n;           // forward step being reversed; sources of sample n+1 enter
+    // graph replay of the reverse sweep: n from device counters instead (nctr for the update
+    // kernels, gctr for the design-box sums, each stepped down on its own stream), the factors
+    // of step n in slot (n % fK) of fbase
+    const unsigned* nctr;
+    const unsigned* gctr;
+    const float* fbase;
+    unsigned fK;
     InjList injV, injI;
 };
 
@@ -95,7 +117,8 @@ __device__ __forceinline__ void add_sources(const AdjDev& a, const InjList& L, u
     if (L.count == 0 || o < L.lo || o > L.hi) return;
     for (unsigned k = 0; k < L.count; ++k)
         if (L.cell[k] == o) {
-            const float v = (float)(a.src[(unsigned long long)L.row[k] * a.stride + a.n + 1] * L.coef[k]);
+            const unsigned n = a.nctr ? *a.nctr : a.n;
+            const float v = (float)(a.src[(unsigned long long)L.row[k] * a.stride + n + 1] * L.coef[k]);
             const int m = L.comp[k];                       // constant indices keep s in registers
             if (m == 0) s[0] = fadd(s[0], v);
             else if (m == 1) s[1] = fadd(s[1], v);
@@ -245,10 +268,18 @@ __global__ void __launch_bounds__(256) k_adj_w(AdjDev a)
 // z rows are whole groups, of the region-local adjoint arrays.  U lanes at z = Nz-1 (and groups at
 // x = Nx-1 or y = Ny-1) are not updated.
 template <bool CURR>
+__device__ __forceinline__ void adj_src_group(const AdjDev& a, const SplitDev& sp, unsigned j);
+
+template <bool CURR>
 __global__ void __launch_bounds__(256, 1) k_adj_reg4(const __grid_constant__ AdjDev a, const __grid_constant__ SplitDev sp)
 {
     const GridDev& g = a.g;
     const unsigned b = blockIdx.x;
+    if (b >= sp.first4[sp.nreg]) {                  // the main box's source groups (k_adj_box4 skips them)
+        const unsigned j = (b - sp.first4[sp.nreg]) * 256u + threadIdx.x;
+        if (j < (CURR ? a.injI.ngrp : a.injV.ngrp)) adj_src_group<CURR>(a, sp, j);
+        return;
+    }
     int r = 0;
     while (r + 1 < (int)sp.nreg && b >= sp.first4[r + 1]) ++r;
     const UpmlDev& u = g.upml[r];
@@ -389,7 +420,8 @@ __global__ void __launch_bounds__(256, 6) k_adj_split(AdjDev a, SplitDev sp)
 // adj_u_cell / adj_w_cell's arithmetic per lane, with the float4 loads of the forward's
 // update_*4_cells.  Lane k is cell z0 + k; groups start on multiples of four, and lanes outside
 // the box's z range are computed but not stored (their cells belong to the region blocks).
-// one group of four of the U update in k_adj_box4<true>
+// one group of four of the U update in k_adj_box4<true>; SRC: it may hold source cells of injI
+template <bool SRC>
 __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp, unsigned x, unsigned y, unsigned z0)
 {
     unsigned mask = 0u;
@@ -407,7 +439,7 @@ __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 u0 = ld4(a.U + o), u1 = ld4(a.U + (S + o)), u2 = ld4(a.U + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
-    const bool src = a.injI.count && (unsigned long long)o + 3 >= a.injI.lo && (unsigned long long)o <= a.injI.hi;
+    const bool src = SRC && a.injI.count && (unsigned long long)o + 3 >= a.injI.lo && (unsigned long long)o <= a.injI.hi;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const unsigned z = z0 + k;
@@ -427,7 +459,8 @@ __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp
     st4_masked(a.U + (2 * S + o), u2, mask);
 }
 
-// one group of four of the W update in k_adj_box4<false>
+// one group of four of the W update in k_adj_box4<false>; SRC: it may hold source cells of injV
+template <bool SRC>
 __device__ __forceinline__ void adj_w4_group(const AdjDev& a, const SplitDev& sp, unsigned x, unsigned y, unsigned z0)
 {
     unsigned mask = 0u;
@@ -445,7 +478,7 @@ __device__ __forceinline__ void adj_w4_group(const AdjDev& a, const SplitDev& sp
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 n0 = ld4(a.W + o), n1 = ld4(a.W + (S + o)), n2 = ld4(a.W + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
-    const bool src = a.injV.count && (unsigned long long)o + 3 >= a.injV.lo && (unsigned long long)o <= a.injV.hi;
+    const bool src = SRC && a.injV.count && (unsigned long long)o + 3 >= a.injV.lo && (unsigned long long)o <= a.injV.hi;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const unsigned z = z0 + k;
@@ -483,6 +516,9 @@ __global__ void __launch_bounds__(256) k_adj_grad(AdjDev a)
     const unsigned bz = kb % a.bn[2], by = (kb / a.bn[2]) % a.bn[1], bx = kb / (a.bn[2] * a.bn[1]);
     const unsigned x = a.b0[0] + bx, y = a.b0[1] + by, z = a.b0[2] + bz;
     const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
+    const float* fv = a.fv;
+    if (a.gctr) fv = a.fbase + (size_t)(*a.gctr % a.fK) * 6u * a.B;
+    const float* fc = fv + 3u * a.B;
     float vv[3], vi[3];
     coef_v(g, o, vv, vi);
 #pragma unroll
@@ -490,12 +526,14 @@ __global__ void __launch_bounds__(256) k_adj_grad(AdjDev a)
         if (vi[m] == 0.f) continue;                             // PEC edge: no dependence
         const float b = fmul(a.W[m * g.S + o], __frcp_rn(vi[m]));
         const unsigned kk = m * a.B + kb;
-        a.gvv[kk] += (double)fmul(b, __ldg(a.fv + kk));
-        a.gvi[kk] += (double)fmul(b, __ldg(a.fc + kk));
+        a.gvv[kk] += (double)fmul(b, __ldg(fv + kk));
+        a.gvi[kk] += (double)fmul(b, __ldg(fc + kk));
     }
 }
 
-// The main box four cells per thread (the groups holding probe sources add them inline).
+// The main box four cells per thread.  The groups that hold a probe source are left to blocks of
+// their own (in the region launch, or k_adj_box4_src): without the source code the streaming
+// threads fit 64 registers with no spills.
 template <bool CURR>
 __global__ void __launch_bounds__(256, 4) k_adj_box4(AdjDev a, SplitDev sp)
 {
@@ -505,8 +543,31 @@ __global__ void __launch_bounds__(256, 4) k_adj_box4(AdjDev a, SplitDev sp)
     t /= sp.n4;
     const unsigned y = sp.lo[1] + t % sp.n[1];
     const unsigned x = sp.lo[0] + t / sp.n[1];
-    if (CURR) adj_u4_group(a, sp, x, y, z0);
-    else adj_w4_group(a, sp, x, y, z0);
+    const InjList& L = CURR ? a.injI : a.injV;
+    const unsigned long long o = ((unsigned long long)x * a.g.Ny + y) * a.g.Pz + z0;
+    if (L.count && o + 3 >= L.lo && o <= L.hi && group_has_source(L, o)) return;
+    if (CURR) adj_u4_group<false>(a, sp, x, y, z0);
+    else adj_w4_group<false>(a, sp, x, y, z0);
+}
+
+// the main-box group j of the source-group list: its update with the sources
+template <bool CURR>
+__device__ __forceinline__ void adj_src_group(const AdjDev& a, const SplitDev& sp, unsigned j)
+{
+    const InjList& L = CURR ? a.injI : a.injV;
+    const unsigned long long og = L.grp[j];
+    const unsigned long long row = og / a.g.Pz;
+    const unsigned z0 = (unsigned)(og - row * a.g.Pz), y = (unsigned)(row % a.g.Ny), x = (unsigned)(row / a.g.Ny);
+    if (CURR) adj_u4_group<true>(a, sp, x, y, z0);
+    else adj_w4_group<true>(a, sp, x, y, z0);
+}
+
+// the source groups alone (splits whose regions run one cell per thread)
+template <bool CURR>
+__global__ void __launch_bounds__(64) k_adj_box4_src(AdjDev a, SplitDev sp)
+{
+    const unsigned j = blockIdx.x * 64u + threadIdx.x;
+    if (j < (CURR ? a.injI.ngrp : a.injV.ngrp)) adj_src_group<CURR>(a, sp, j);
 }
 
 // V^n and K_V I^n (the arithmetic of update_v_cell) in the design box, into slot
@@ -541,6 +602,11 @@ __global__ void k_inc(unsigned* c)
     if (threadIdx.x == 0 && blockIdx.x == 0) *c += 1u;
 }
 
+__global__ void k_dec(unsigned* c)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *c -= 1u;
+}
+
 }  // namespace
 
 struct oems_adjoint_state {
@@ -564,7 +630,13 @@ struct oems_adjoint_state {
     // `gs`, after ev_w (W of the step done), and the next W update waits for ev_grad
     bool box4 = false;
     cudaStream_t gs = nullptr;
-    cudaEvent_t ev_w = nullptr, ev_grad = nullptr;
+    cudaEvent_t ev_w = nullptr, ev_grad = nullptr, ev_grad_c = nullptr;
+    // the float4 region kernels on a branch of their own beside the main box
+    cudaStream_t rr = nullptr;
+    cudaEvent_t ev_rfork = nullptr, ev_rjoin = nullptr;
+    // graph replay of the reverse sweep: the step counters of the update kernels and of the sums
+    unsigned* rev_n = nullptr;
+    unsigned* rev_ng = nullptr;
     float fwd_ms = 0.f, bwd_ms = 0.f;
     unsigned launches_per_reverse_step = 0;
 };
@@ -590,24 +662,55 @@ int aalloc(oems_cuda_engine* e, oems_adjoint_state* s, T** p, size_t count)
     return OEMS_OK;
 }
 
+// device-to-device copy of `bytes` (a multiple of 4) as 16-byte vectors where both ends allow it;
+// as a kernel it streams at HBM rate, where a device-to-device cudaMemcpyAsync took about 0.6 ms
+// per 130 MB checkpoint
+__global__ void k_copy(float* __restrict__ dst, const float* __restrict__ src, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool vec = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0;
+    if (vec) {
+        const size_t n4 = n / 4;
+        for (size_t k = i; k < n4; k += stride)
+            reinterpret_cast<float4*>(dst)[k] = __ldg(reinterpret_cast<const float4*>(src) + k);
+        for (size_t k = n4 * 4 + i; k < n; k += stride) dst[k] = src[k];
+    } else {
+        for (size_t k = i; k < n; k += stride) dst[k] = src[k];
+    }
+}
+
 int copy_state(oems_cuda_engine* e, oems_adjoint_state* s, char* ck, bool save)
 {
     size_t off = 0;
     for (const auto& r : s->regions) {
-        const cudaError_t c = save ? cudaMemcpyAsync(ck + off, r.first, r.second, cudaMemcpyDeviceToDevice, e->stream)
-                                   : cudaMemcpyAsync(r.first, ck + off, r.second, cudaMemcpyDeviceToDevice, e->stream);
-        if (c != cudaSuccess) return afail(e, OEMS_ERR_CUDA, "checkpoint copy");
-        off += r.second;
+        float* dst = reinterpret_cast<float*>(save ? ck + off : static_cast<char*>(r.first));
+        const float* src = reinterpret_cast<const float*>(save ? static_cast<const char*>(r.first) : ck + off);
+        const size_t n = r.second / sizeof(float);
+        const unsigned blocks = (unsigned)std::min<size_t>(152 * 8, (n / 4 + 255) / 256 + 1);
+        k_copy<<<blocks, 256, 0, e->stream>>>(dst, src, n);
+        if (cudaGetLastError() != cudaSuccess) return afail(e, OEMS_ERR_CUDA, "checkpoint copy");
+        off += (r.second + 255) & ~(size_t)255;          // every region on a 256-byte boundary
     }
     return OEMS_OK;
 }
 
-// one forward step without processing, the step counter being rec_numTS; returns the launches
-unsigned recompute_step(oems_cuda_engine* e, oems_adjoint_state* s)
+// kernels of one recompute step (recompute_step)
+unsigned recompute_launches(const oems_cuda_engine* e)
+{
+    const unsigned per_update = (e->use_split && e->splitV.v4) ? 2u : 1u;
+    return 2 * per_update + 1 + (e->excV.count ? 1u : 0u) + (e->excI.count ? 1u : 0u);
+}
+
+// one forward step without processing, the step counter being rec_numTS; returns the launches.
+// fac != nullptr: the voltage update writes the design-box factors of this step itself.
+unsigned recompute_step(oems_cuda_engine* e, oems_adjoint_state* s, const FacOut* fac = nullptr)
 {
     cudaStream_t st = e->stream;
-    unsigned L = 3;
-    launch_update(e, false, st);
+    // two update launches (the split's region kernel and main box count two each) and k_inc
+    const unsigned per_update = (e->use_split && e->splitV.v4) ? 2u : 1u;
+    unsigned L = 2 * per_update + 1;
+    launch_update(e, false, st, nullptr, fac);
     if (e->excV.count) { k_excitation<<<(e->excV.count + 127) / 128, 128, 0, st>>>(e->dV, e->excV, s->rec_numTS); ++L; }
     launch_update(e, true, st);
     if (e->excI.count) { k_excitation<<<(e->excI.count + 127) / 128, 128, 0, st>>>(e->dI, e->excI, s->rec_numTS); ++L; }
@@ -702,6 +805,30 @@ int build_injection(oems_cuda_engine* e, unsigned nprobe, const int* ids, int ty
     cudaMemcpyAsync(dr, row.data(), row.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream);
     cudaMemcpyAsync(dw, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, e->stream);
     L.cell = dc; L.comp = dm; L.row = dr; L.coef = dw;
+    // the main-box groups of four that hold a source cell (k_adj_box4 leaves them out)
+    const SplitDev& sp = type == 0 ? e->splitV : e->splitI;
+    std::vector<unsigned long long> grp;
+    if (e->use_split && sp.v4) {
+        for (const unsigned long long c : cell) {
+            const unsigned long long r = c / e->Pz;
+            const unsigned z = (unsigned)(c - r * e->Pz), y = (unsigned)(r % e->N[1]), x = (unsigned)(r / e->N[1]);
+            const unsigned z0 = z & ~3u;
+            if (x >= sp.lo[0] && x < sp.lo[0] + sp.n[0] && y >= sp.lo[1] && y < sp.lo[1] + sp.n[1] && z0 >= sp.z4 &&
+                (z0 - sp.z4) / 4 < sp.n4)
+                grp.push_back(r * e->Pz + z0);
+        }
+        std::sort(grp.begin(), grp.end());
+        grp.erase(std::unique(grp.begin(), grp.end()), grp.end());
+    }
+    if (!grp.empty()) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, grp.size() * sizeof(unsigned long long)) != cudaSuccess)
+            return afail(e, OEMS_ERR_NOMEM, "adjoint source allocation");
+        tmp.push_back(q);
+        cudaMemcpyAsync(q, grp.data(), grp.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, e->stream);
+        L.grp = static_cast<const unsigned long long*>(q);
+        L.ngrp = (unsigned)grp.size();
+    }
     return OEMS_OK;
 }
 
@@ -736,7 +863,7 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
         s->regions.push_back({e->grid.upml[r].vflux, 3ull * e->grid.upml[r].n * sizeof(float)});
         s->regions.push_back({e->grid.upml[r].iflux, 3ull * e->grid.upml[r].n * sizeof(float)});
     }
-    for (const auto& r : s->regions) s->state_bytes += r.second;
+    for (const auto& r : s->regions) s->state_bytes += (r.second + 255) & ~(size_t)255;
     AdjDev& d = s->dev;
     d.g = e->grid;
     int rc;
@@ -767,13 +894,19 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
                 return afail(e, OEMS_ERR_CUDA, "adjoint events");
     }
     if ((rc = aalloc(e, s, &s->rec_numTS, 1))) return rc;
+    if ((rc = aalloc(e, s, &s->rev_n, 2))) return rc;
+    s->rev_ng = s->rev_n + 1;
     if (cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess)
         return afail(e, OEMS_ERR_CUDA, "adjoint events");
     s->box4 = e->use_split && e->compressed && e->splitI.v4 && e->splitV.v4;
     if (s->box4 && (cudaStreamCreateWithFlags(&s->gs, cudaStreamNonBlocking) != cudaSuccess ||
                     cudaEventCreateWithFlags(&s->ev_w, cudaEventDisableTiming) != cudaSuccess ||
-                    cudaEventCreateWithFlags(&s->ev_grad, cudaEventDisableTiming) != cudaSuccess))
-        return afail(e, OEMS_ERR_CUDA, "adjoint gradient stream");
+                    cudaEventCreateWithFlags(&s->ev_grad, cudaEventDisableTiming) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&s->ev_grad_c, cudaEventDisableTiming) != cudaSuccess ||
+                    cudaStreamCreateWithFlags(&s->rr, cudaStreamNonBlocking) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&s->ev_rfork, cudaEventDisableTiming) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&s->ev_rjoin, cudaEventDisableTiming) != cudaSuccess))
+        return afail(e, OEMS_ERR_CUDA, "adjoint side streams");
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) return afail(e, OEMS_ERR_CUDA, "adjoint setup sync");
     return OEMS_OK;
 }
@@ -876,40 +1009,67 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     const dim3 gu((plane + 255) / 256, e->N[0] - 1), gw((plane + 255) / 256, e->N[0]);
     const unsigned fb = (d.B + 255) / 256;
     rc = OEMS_OK;
-    unsigned lps = 2;
+    // kernels per reverse step: the adjoint updates (+ the design-box sums and, in graph replay,
+    // the two counter steps) and, in checkpoint mode, the recompute (+ the factor launch when the
+    // voltage update does not record them)
+    unsigned lps = (e->use_split && s->box4) ? 4u + (d.B ? 1u : 0u) : 2u;
+    if (s->K) {
+        const unsigned rec = recompute_launches(e);
+        lps += rec + (s->box4 ? 0u : 1u);
+        if (s->box4 && s->K % 16 == 0) lps += 1u + (d.B ? 1u : 0u);
+    }
     const unsigned bu = e->splitI.main_blocks + e->splitI.first_block[e->splitI.nreg];
     const unsigned bw = e->splitV.main_blocks + e->splitV.first_block[e->splitV.nreg];
+    // one reverse step of the float4 split on rst.  wait_grad: the W update waits for the previous
+    // step's design-box sums (in a captured graph the first step's wait is the graph boundary);
+    // ctr: the sums' counter to step down after them (graph replay)
+    auto reverse_box4 = [&](const AdjDev& dd, cudaStream_t rst, bool wait_grad, unsigned* gctr, cudaEvent_t evg) {
+        const SplitDev* sp[2] = {&e->splitI, &e->splitV};
+        for (int h = 0; h < 2; ++h) {
+            if (h == 1 && wait_grad) cudaStreamWaitEvent(rst, evg, 0);
+            const unsigned ng = h == 0 ? dd.injI.ngrp : dd.injV.ngrp;
+            if (sp[h]->reg4) {
+                cudaEventRecord(s->ev_rfork, rst);
+                cudaStreamWaitEvent(s->rr, s->ev_rfork, 0);
+                const unsigned rblk = sp[h]->first4[sp[h]->nreg] + (ng + 255) / 256;
+                if (h == 0) k_adj_reg4<true><<<rblk, 256, 0, s->rr>>>(dd, *sp[h]);
+                else k_adj_reg4<false><<<rblk, 256, 0, s->rr>>>(dd, *sp[h]);
+            } else {
+                if (const unsigned rblk = sp[h]->first_block[sp[h]->nreg]) {
+                    if (h == 0) k_adj_split<true><<<rblk, 256, 0, rst>>>(dd, *sp[h]);
+                    else k_adj_split<false><<<rblk, 256, 0, rst>>>(dd, *sp[h]);
+                }
+                if (ng) {
+                    if (h == 0) k_adj_box4_src<true><<<(ng + 63) / 64, 64, 0, rst>>>(dd, *sp[h]);
+                    else k_adj_box4_src<false><<<(ng + 63) / 64, 64, 0, rst>>>(dd, *sp[h]);
+                }
+            }
+            if (sp[h]->main_blocks4) {
+                if (h == 0) k_adj_box4<true><<<sp[h]->main_blocks4, 256, 0, rst>>>(dd, *sp[h]);
+                else k_adj_box4<false><<<sp[h]->main_blocks4, 256, 0, rst>>>(dd, *sp[h]);
+            }
+            if (sp[h]->reg4) {
+                cudaEventRecord(s->ev_rjoin, s->rr);
+                cudaStreamWaitEvent(rst, s->ev_rjoin, 0);
+            }
+        }
+        if (dd.B) {
+            cudaEventRecord(s->ev_w, rst);
+            cudaStreamWaitEvent(s->gs, s->ev_w, 0);
+            k_adj_grad<<<(dd.B + 255) / 256, 256, 0, s->gs>>>(dd);
+            if (gctr) k_dec<<<1, 32, 0, s->gs>>>(gctr);
+            cudaEventRecord(evg, s->gs);
+        }
+    };
     auto reverse = [&](unsigned n, const float* slot, cudaStream_t rst) {
         d.n = n;
         d.fv = slot;
         d.fc = slot + 3 * d.B;
         if (e->use_split && s->box4) {
-            // per half-step: the region blocks, then the main box four cells per thread. The
-            // design-box sums of step n run on the side stream, beside the U update of step n-1
-            // (which only reads W); the W update of step n-1 waits for them.
-            const SplitDev* sp[2] = {&e->splitI, &e->splitV};
-            for (int h = 0; h < 2; ++h) {
-                if (h == 1) cudaStreamWaitEvent(rst, s->ev_grad, 0);
-                if (sp[h]->reg4) {
-                    const unsigned rblk = sp[h]->first4[sp[h]->nreg];
-                    if (h == 0) k_adj_reg4<true><<<rblk, 256, 0, rst>>>(d, *sp[h]);
-                    else k_adj_reg4<false><<<rblk, 256, 0, rst>>>(d, *sp[h]);
-                } else if (const unsigned rblk = sp[h]->first_block[sp[h]->nreg]) {
-                    if (h == 0) k_adj_split<true><<<rblk, 256, 0, rst>>>(d, *sp[h]);
-                    else k_adj_split<false><<<rblk, 256, 0, rst>>>(d, *sp[h]);
-                }
-                if (sp[h]->main_blocks4) {
-                    if (h == 0) k_adj_box4<true><<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
-                    else k_adj_box4<false><<<sp[h]->main_blocks4, 256, 0, rst>>>(d, *sp[h]);
-                }
-            }
-            if (d.B) {
-                cudaEventRecord(s->ev_w, rst);
-                cudaStreamWaitEvent(s->gs, s->ev_w, 0);
-                k_adj_grad<<<(d.B + 255) / 256, 256, 0, s->gs>>>(d);
-                cudaEventRecord(s->ev_grad, s->gs);
-            }
-        } else if (e->use_split) {
+            reverse_box4(d, rst, true, nullptr, s->ev_grad);
+            return;
+        }
+        if (e->use_split) {
             if (bu) k_adj_split<true><<<bu, 256, 0, rst>>>(d, e->splitI);
             if (bw) k_adj_split<false><<<bw, 256, 0, rst>>>(d, e->splitV);
         } else {
@@ -926,20 +1086,81 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         // coefficients, the factors and its own adjoint arrays, the recompute the engine state.
         const unsigned nseg = (N + s->K - 1) / s->K;
         const size_t half = (size_t)s->K * 6 * d.B;
+        auto fac_out = [&](unsigned hb) {
+            return FacOut{s->fac + hb * half, s->rec_numTS, s->K, {d.b0[0], d.b0[1], d.b0[2]},
+                          {d.bn[0], d.bn[1], d.bn[2]}, d.B};
+        };
+        // With the float4 split the voltage update records the factors itself (the design box lies
+        // in its main box), and the recompute of a whole segment replays a captured graph of 16
+        // steps per factor half (the step counter and the slot come from device memory).
+        constexpr unsigned RG = 16;
+        cudaGraphExec_t rgraph[2] = {nullptr, nullptr};
+        if (s->box4 && s->K % RG == 0) {
+            for (unsigned hb = 0; hb < 2 && rc == OEMS_OK; ++hb) {
+                const FacOut fo = fac_out(hb);
+                cudaGraph_t graph = nullptr;
+                if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                    rc = afail(e, OEMS_ERR_CUDA, "recompute graph capture");
+                    break;
+                }
+                for (unsigned j = 0; j < RG; ++j) recompute_step(e, s, &fo);
+                if (cudaStreamEndCapture(st, &graph) != cudaSuccess ||
+                    cudaGraphInstantiate(&rgraph[hb], graph, 0) != cudaSuccess)
+                    rc = afail(e, OEMS_ERR_CUDA, "recompute graph");
+                if (graph) cudaGraphDestroy(graph);
+            }
+        }
+        // the reverse sweep of a whole segment likewise replays a graph of 16 reverse steps per
+        // factor half, n coming from the device counters (set at the segment's start)
+        cudaGraphExec_t vgraph[2] = {nullptr, nullptr};
+        if (s->box4 && s->K % RG == 0 && rc == OEMS_OK) {
+            for (unsigned hb = 0; hb < 2 && rc == OEMS_OK; ++hb) {
+                AdjDev dg = d;
+                dg.nctr = s->rev_n;
+                dg.gctr = d.B ? s->rev_ng : nullptr;
+                dg.fbase = s->fac + hb * half;
+                dg.fK = s->K;
+                cudaGraph_t graph = nullptr;
+                if (cudaStreamBeginCapture(s->rs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                    rc = afail(e, OEMS_ERR_CUDA, "reverse graph capture");
+                    break;
+                }
+                // (an event of its own: the direct steps never wait on one recorded in a capture)
+                for (unsigned j = 0; j < RG; ++j) {
+                    reverse_box4(dg, s->rs, j > 0, dg.gctr ? s->rev_ng : nullptr, s->ev_grad_c);
+                    k_dec<<<1, 32, 0, s->rs>>>(s->rev_n);
+                }
+                if (d.B) cudaStreamWaitEvent(s->rs, s->ev_grad_c, 0);   // the last sums rejoin the graph
+                if (cudaStreamEndCapture(s->rs, &graph) != cudaSuccess ||
+                    cudaGraphInstantiate(&vgraph[hb], graph, 0) != cudaSuccess)
+                    rc = afail(e, OEMS_ERR_CUDA, "reverse graph");
+                if (graph) cudaGraphDestroy(graph);
+            }
+        }
         auto recompute = [&](unsigned seg) -> int {
             const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
             float* base = s->fac + (seg & 1u) * half;
             int r2;
             if ((r2 = copy_state(e, s, s->ckpt[seg], false))) return r2;
             cudaMemcpyAsync(s->rec_numTS, &a0, sizeof(unsigned), cudaMemcpyHostToDevice, st);
-            for (unsigned n = a0; n < a1; ++n) {
-                k_adj_factors<<<fb, 256, 0, st>>>(d, base, s->rec_numTS, s->K);
-                lps = 3 + recompute_step(e, s);
+            const FacOut fo = fac_out(seg & 1u);
+            unsigned n = a0;
+            if (rgraph[seg & 1u])
+                for (; n + RG <= a1; n += RG)
+                    if (cudaGraphLaunch(rgraph[seg & 1u], st) != cudaSuccess)
+                        return afail(e, OEMS_ERR_CUDA, "recompute graph launch");
+            for (; n < a1; ++n) {
+                if (s->box4) {
+                    recompute_step(e, s, &fo);
+                } else {
+                    k_adj_factors<<<fb, 256, 0, st>>>(d, base, s->rec_numTS, s->K);
+                    recompute_step(e, s);
+                }
             }
             cudaEventRecord(s->ev_recomputed[seg & 1u], st);
             return OEMS_OK;
         };
-        rc = recompute(nseg - 1);
+        if (rc == OEMS_OK) rc = recompute(nseg - 1);
         for (int seg = (int)nseg - 1; seg >= 0 && rc == OEMS_OK; --seg) {
             const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
             if (seg > 0) {
@@ -949,7 +1170,20 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
             }
             cudaStreamWaitEvent(s->rs, s->ev_recomputed[seg & 1], 0);
             const float* base = s->fac + (seg & 1) * half;
-            for (int n = (int)a1 - 1; n >= (int)a0; --n) reverse((unsigned)n, base + (size_t)(n % s->K) * 6 * d.B, s->rs);
+            if (vgraph[seg & 1] && a1 - a0 == s->K) {
+                // the previous direct step's sums first; then n = a1-1 down to a0 from the counters
+                cudaStreamWaitEvent(s->rs, s->ev_grad, 0);
+                const unsigned start[2] = {a1 - 1, a1 - 1};
+                cudaMemcpyAsync(s->rev_n, start, sizeof(start), cudaMemcpyHostToDevice, s->rs);
+                for (unsigned r = 0; r < s->K / RG; ++r)
+                    if (cudaGraphLaunch(vgraph[seg & 1], s->rs) != cudaSuccess) {
+                        rc = afail(e, OEMS_ERR_CUDA, "reverse graph launch");
+                        break;
+                    }
+            } else {
+                for (int n = (int)a1 - 1; n >= (int)a0; --n)
+                    reverse((unsigned)n, base + (size_t)(n % s->K) * 6 * d.B, s->rs);
+            }
             if (s->ev_grad) cudaStreamWaitEvent(s->rs, s->ev_grad, 0);   // the sums read this half too
             cudaEventRecord(s->ev_reversed[seg & 1], s->rs);
             if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
@@ -958,6 +1192,10 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         if (s->ev_grad) cudaStreamWaitEvent(s->rs, s->ev_grad, 0);
         cudaEventRecord(s->ev_reversed[0], s->rs);
         cudaStreamWaitEvent(st, s->ev_reversed[0], 0);
+        for (auto& x : rgraph)
+            if (x) cudaGraphExecDestroy(x);             // freed when their last launch completes
+        for (auto& x : vgraph)
+            if (x) cudaGraphExecDestroy(x);
     } else {
         for (int n = (int)N - 1; n >= 0; --n) reverse((unsigned)n, s->fac + (size_t)n * 6 * d.B, st);
         if (s->ev_grad) cudaStreamWaitEvent(st, s->ev_grad, 0);
@@ -977,6 +1215,7 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     }
     if (s->rs) cudaStreamSynchronize(s->rs);
     if (s->gs) cudaStreamSynchronize(s->gs);
+    if (s->rr) cudaStreamSynchronize(s->rr);
     release();
     d.src = nullptr;
     d.injV = InjList{};
@@ -1010,6 +1249,10 @@ void oems_adjoint_free(oems_adjoint_state* s)
     if (s->rs) cudaStreamDestroy(s->rs);
     if (s->ev_w) cudaEventDestroy(s->ev_w);
     if (s->ev_grad) cudaEventDestroy(s->ev_grad);
+    if (s->ev_grad_c) cudaEventDestroy(s->ev_grad_c);
     if (s->gs) cudaStreamDestroy(s->gs);
+    if (s->ev_rfork) cudaEventDestroy(s->ev_rfork);
+    if (s->ev_rjoin) cudaEventDestroy(s->ev_rjoin);
+    if (s->rr) cudaStreamDestroy(s->rr);
     delete s;
 }

@@ -185,6 +185,12 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     if (e->graphK) cudaGraphExecDestroy(e->graphK);
     oems_adjoint_free(e->adj);
     for (void* p : e->allocs) cudaFree(p);
+    if (e->stream_r) {
+        cudaStreamSynchronize(e->stream_r);
+        cudaStreamDestroy(e->stream_r);
+    }
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -652,7 +658,7 @@ static void launch_v(const dim3& grid, cudaStream_t s, const GridDev& g, const M
     k_update_v<C, U, M, IX><<<grid, 256, 0, s>>>(g, m, ts);
 }
 
-void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** name)
+void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** name, const FacOut* fac)
 {
     const GridDev& g = e->grid;
     const MurDev& m = e->murdev;
@@ -670,16 +676,27 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
             // the region blocks, then the main box four cells per thread (the two write disjoint
             // cells; as separate launches each gets its own register budget)
             if (!go(sp.reg4 ? "k_update_reg4+k_update_box4" : "k_update_split+k_update_box4")) return;
+            // the region kernel on the branch stream when there is one (joined below)
+            cudaStream_t rs = e->stream_r ? e->stream_r : s;
+            if (e->stream_r) {
+                cudaEventRecord(e->ev_fork, s);
+                cudaStreamWaitEvent(rs, e->ev_fork, 0);
+            }
             if (sp.reg4) {
-                if (curr) k_update_reg4<true><<<sp.first4[sp.nreg], 256, 0, s>>>(g, sp);
-                else k_update_reg4<false><<<sp.first4[sp.nreg], 256, 0, s>>>(g, sp);
+                if (curr) k_update_reg4<true><<<sp.first4[sp.nreg], 256, 0, rs>>>(g, sp);
+                else k_update_reg4<false><<<sp.first4[sp.nreg], 256, 0, rs>>>(g, sp);
             } else if (const unsigned rb = sp.first_block[sp.nreg]) {
-                if (curr) k_update_split<true, true><<<rb, 256, 0, s>>>(g, sp, m, ts);
-                else k_update_split<true, false><<<rb, 256, 0, s>>>(g, sp, m, ts);
+                if (curr) k_update_split<true, true><<<rb, 256, 0, rs>>>(g, sp, m, ts);
+                else k_update_split<true, false><<<rb, 256, 0, rs>>>(g, sp, m, ts);
             }
             if (sp.main_blocks4) {
                 if (curr) k_update_box4<true><<<sp.main_blocks4, 256, 0, s>>>(g, sp);
+                else if (fac) k_update_box4<false, true><<<sp.main_blocks4, 256, 0, s>>>(g, sp, *fac);
                 else k_update_box4<false><<<sp.main_blocks4, 256, 0, s>>>(g, sp);
+            }
+            if (e->stream_r) {
+                cudaEventRecord(e->ev_join, rs);
+                cudaStreamWaitEvent(s, e->ev_join, 0);
             }
             return;
         }
@@ -1058,6 +1075,15 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         const unsigned RI[3] = {e->N[0] - 1, e->N[1] - 1, e->N[2] - 1};
         make_split(e, RV, e->splitV);
         make_split(e, RI, e->splitI);
+        // the region kernel and the main box run as two branches (a fork/join in the graphs), so
+        // the latency-bound region blocks overlap the streaming box; OEMS_CUDA_SPLIT_BRANCH=0
+        // runs them one after the other on the engine stream
+        const char* br = getenv("OEMS_CUDA_SPLIT_BRANCH");
+        if (e->splitV.v4 && !(br && br[0] == '0')) {
+            CK(cudaStreamCreateWithFlags(&e->stream_r, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+        }
     }
 
     // excitation

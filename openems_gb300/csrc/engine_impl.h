@@ -161,6 +161,9 @@ struct oems_cuda_engine {
     // UPML work split of the update launches (used when the engine has UPML regions)
     bool use_split = false;
     SplitDev splitV{}, splitI{};
+    // float4 split: the region kernel's branch stream and its fork/join events
+    cudaStream_t stream_r = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // Mur pre/post hooks as separate launches (k_mur phases 0/1) instead of inside the voltage
     // update; set by OEMS_CUDA_MUR_SEPARATE=1 at init
     bool mur_separate = false;
@@ -195,8 +198,11 @@ int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch);
 // the split for update range R (V: the mesh, I: one cell less per axis)
 void make_split(const oems_cuda_engine* e, const unsigned R[3], SplitDev& sp);
 // one update launch (V or I) of the engine's kernel configuration on stream s
-// name != nullptr: only report the kernel name this configuration launches
-void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** name = nullptr);
+// name != nullptr: only report the kernel name this configuration launches.  fac != nullptr: the
+// voltage update's float4 main box also writes the design-box factors of the reverse sweep (used
+// by the recomputation when the engine runs the split with a float4 main box)
+void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** name = nullptr,
+                   const FacOut* fac = nullptr);
 // per-cell coefficient classes of dense N-I-J-K arrays on the device (compress.cu): 0 = built,
 // 1 = more than `cap` classes, else an OEMS error code
 int compress_dense_device(oems_cuda_engine* e, const float* vv, const float* vi, const float* ii, const float* iv,

@@ -508,9 +508,19 @@ __global__ void __launch_bounds__(256) k_update_i4(GridDev g)
 // every warp holding one wall thread, and a register spill or an exposed coefficient load with it.)
 // four voltage cells (x, y, z0..z0+3) of the compressed operator without UPML and Mur hooks;
 // only the lanes of `mask` are stored
-template <typename IX = unsigned>
+// Optional output of the voltage update for the reverse sweep's recomputation: V^n and K_V I^n of
+// the cells of a design box, into slot (*counter % modulo) of `base` (each slot [2][3][B]: V, then
+// K_V I; design cell kb = (bx * bn[1] + by) * bn[2] + bz), exactly the values the update uses.
+struct FacOut {
+    float* base;
+    const unsigned* counter;
+    unsigned modulo;
+    unsigned b0[3], bn[3], B;
+};
+
+template <typename IX = unsigned, bool FAC = false>
 __device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, unsigned y, unsigned z0,
-                                                unsigned mask = 15u)
+                                                unsigned mask = 15u, const FacOut* fo = nullptr)
 {
     const IX S = (IX)g.S;
     const IX o = ((IX)x * g.Ny + y) * g.Pz + z0;
@@ -526,6 +536,11 @@ __device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, un
     const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
     float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
+    // FAC: this row's design cells (the box's rows are x, y inside it; lanes z inside it)
+    const unsigned fbx = x - (FAC ? fo->b0[0] : 0u), fby = y - (FAC ? fo->b0[1] : 0u);
+    const bool frow = FAC && fbx < fo->bn[0] && fby < fo->bn[1];
+    float* fslot = nullptr;
+    if (frow) fslot = fo->base + (size_t)(__ldg(fo->counter) % fo->modulo) * 6u * fo->B;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (z0 + k >= g.Nz) break;
@@ -534,6 +549,18 @@ __device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, un
         const float c0 = fadd(fsub(fsub(f4(i2, k), f4(i2y, k)), f4(i1, k)), i1z);
         const float c1 = fadd(fsub(fsub(f4(i0, k), i0z), f4(i2, k)), f4(i2x, k));
         const float c2 = fadd(fsub(fsub(f4(i1, k), f4(i1x, k)), f4(i0, k)), f4(i0y, k));
+        if (frow) {
+            const unsigned bz = z0 + k - fo->b0[2];
+            if (bz < fo->bn[2] && (mask & (1u << k))) {
+                const unsigned kb = (fbx * fo->bn[1] + fby) * fo->bn[2] + bz, B = fo->B;
+                fslot[kb] = f4(n0, k);
+                fslot[B + kb] = f4(n1, k);
+                fslot[2 * B + kb] = f4(n2, k);
+                fslot[3 * B + kb] = c0;
+                fslot[4 * B + kb] = c1;
+                fslot[5 * B + kb] = c2;
+            }
+        }
         set4(n0, k, fadd(fmul(f4(n0, k), ca.x), fmul(ca.w, c0)));
         set4(n1, k, fadd(fmul(f4(n1, k), ca.y), fmul(cb.x, c1)));
         set4(n2, k, fadd(fmul(f4(n2, k), ca.z), fmul(cb.y, c2)));
@@ -772,8 +799,9 @@ __global__ void __launch_bounds__(256, (COMPRESSED && !MUR) ? 8 : 1)
 // The main box of a UPML split, four z cells per thread (compressed operator, no Mur hooks).
 // Groups of four start on multiples of four (z4 = lo[2] rounded down); lanes outside the box's
 // z range are computed but not stored (their cells belong to the region blocks).
-template <bool CURR>
-__global__ void __launch_bounds__(256) k_update_box4(GridDev g, SplitDev sp)
+// FAC (voltage update only): also the design-box factors of the reverse sweep's recomputation
+template <bool CURR, bool FAC = false>
+__global__ void __launch_bounds__(256, 4) k_update_box4(GridDev g, SplitDev sp, FacOut fo = FacOut{})
 {
     unsigned t = blockIdx.x * 256u + threadIdx.x;
     if (t >= sp.main_cells4) return;
@@ -786,7 +814,7 @@ __global__ void __launch_bounds__(256) k_update_box4(GridDev g, SplitDev sp)
 #pragma unroll
     for (int k = 0; k < 4; ++k) mask |= (z + k >= zlo && z + k < zhi) ? (1u << k) : 0u;
     if (CURR) update_i4_cells<unsigned>(g, x, y, z, mask);
-    else update_v4_cells<unsigned>(g, x, y, z, mask);
+    else update_v4_cells<unsigned, FAC>(g, x, y, z, mask, &fo);
 }
 
 // Region-local arrays (fluxes, classes) in the float4 region kernels: a group's four lanes are
