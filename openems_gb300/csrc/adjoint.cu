@@ -609,6 +609,12 @@ __global__ void k_dec(unsigned* c)
 
 }  // namespace
 
+// checkpoint mode: factor buffers of K slots each (24 B per design edge triple and step: 400 MB
+// per buffer for 64x64x16 design cells at K = 256).  The forward run keeps the factors of its last
+// FB-1 segments, which the reverse sweep then needs not recompute, and the recompute of the others
+// runs up to FB-1 segments ahead of the sweep.
+constexpr unsigned FB = 6;
+
 struct oems_adjoint_state {
     unsigned K = 256;                                 // 0: record mode
     unsigned steps = 0;
@@ -622,10 +628,10 @@ struct oems_adjoint_state {
     size_t state_bytes = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     // checkpoint mode: the reverse sweep of segment k runs on `rs` while the engine stream
-    // recomputes segment k-1 into the other half of the factor slots (2K slots)
+    // recomputes the segments below it into the other factor buffers (FB x K slots)
     cudaStream_t rs = nullptr;
-    cudaEvent_t ev_recomputed[2] = {nullptr, nullptr};
-    cudaEvent_t ev_reversed[2] = {nullptr, nullptr};
+    cudaEvent_t ev_recomputed[FB] = {};
+    cudaEvent_t ev_reversed[FB] = {};
     // UPML split with a float4 main box (k_adj_box4): the design-box sums (k_adj_grad) run on
     // `gs`, after ev_w (W of the step done), and the next W update waits for ev_grad
     bool box4 = false;
@@ -637,6 +643,9 @@ struct oems_adjoint_state {
     // graph replay of the reverse sweep: the step counters of the update kernels and of the sums
     unsigned* rev_n = nullptr;
     unsigned* rev_ng = nullptr;
+    // checkpoint mode: segments from this one on had their factors recorded by the forward run
+    // (until a reverse sweep overwrites those slots)
+    unsigned recorded_from = ~0u;
     float fwd_ms = 0.f, bwd_ms = 0.f;
     unsigned launches_per_reverse_step = 0;
 };
@@ -720,8 +729,12 @@ unsigned recompute_step(oems_cuda_engine* e, oems_adjoint_state* s, const FacOut
 
 // forward run that records the factors of every step (record mode): graphs of 1 and 16 steps,
 // each step preceded by the factor kernel writing slot numTS
-int record_forward(oems_cuda_engine* e, oems_adjoint_state* s, unsigned steps)
+// base/modulo: the factors of step numTS go to slot numTS % modulo of base (record mode: all of
+// s->fac, one slot per step; checkpoint mode: the last segments, into their factor buffers)
+int record_forward(oems_cuda_engine* e, oems_adjoint_state* s, unsigned steps, float* base = nullptr,
+                   unsigned modulo = 0xFFFFFFFFu)
 {
+    if (!base) base = s->fac;
     const unsigned KG = 16;
     cudaGraphExec_t gx[2] = {nullptr, nullptr};
     const unsigned counts[2] = {1, KG};
@@ -732,7 +745,7 @@ int record_forward(oems_cuda_engine* e, oems_adjoint_state* s, unsigned steps)
             return afail(e, OEMS_ERR_CUDA, "record capture");
         int rc = OEMS_OK;
         for (unsigned j = 0; j < counts[k] && rc == OEMS_OK; ++j) {
-            k_adj_factors<<<fb, 256, 0, e->stream>>>(s->dev, s->fac, e->d_numTS, 0xFFFFFFFFu);
+            k_adj_factors<<<fb, 256, 0, e->stream>>>(s->dev, base, e->d_numTS, modulo);
             unsigned L = 0;
             rc = enqueue_step(e, &L);
         }
@@ -884,11 +897,11 @@ int oems_cuda_adjoint_setup(oems_cuda_engine* e, unsigned int checkpoint_every, 
     if ((rc = aalloc(e, s, &d.gvv, 3ull * d.B))) return rc;
     if ((rc = aalloc(e, s, &d.gvi, 3ull * d.B))) return rc;
     if (s->K) {
-        s->fac_slots = 2ull * s->K;
+        s->fac_slots = (size_t)FB * s->K;
         if ((rc = aalloc(e, s, &s->fac, s->fac_slots * 6ull * d.B))) return rc;
         if (cudaStreamCreateWithFlags(&s->rs, cudaStreamNonBlocking) != cudaSuccess)
             return afail(e, OEMS_ERR_CUDA, "adjoint stream");
-        for (int b = 0; b < 2; ++b)
+        for (unsigned b = 0; b < FB; ++b)
             if (cudaEventCreateWithFlags(&s->ev_recomputed[b], cudaEventDisableTiming) != cudaSuccess ||
                 cudaEventCreateWithFlags(&s->ev_reversed[b], cudaEventDisableTiming) != cudaSuccess)
                 return afail(e, OEMS_ERR_CUDA, "adjoint events");
@@ -939,10 +952,17 @@ int oems_cuda_adjoint_forward(oems_cuda_engine* e, unsigned int steps)
     cudaEventRecord(s->ev[0], e->stream);
     int rc = OEMS_OK;
     if (s->K) {
+        // the last FB-1 segments also record their factors, into their factor buffers, so the
+        // reverse sweep starts on them without recomputing them
+        const unsigned nrec = std::min(nseg, FB - 1);
+        const size_t half = (size_t)s->K * 6 * s->dev.B;
         for (unsigned k = 0; k < nseg && rc == OEMS_OK; ++k) {
             if ((rc = copy_state(e, s, s->ckpt[k], true))) break;
-            rc = oems_cuda_iterate(e, std::min(s->K, steps - k * s->K));
+            const unsigned len = std::min(s->K, steps - k * s->K);
+            if (k + nrec >= nseg) rc = record_forward(e, s, len, s->fac + (k % FB) * half, s->K);
+            else rc = oems_cuda_iterate(e, len);
         }
+        s->recorded_from = nseg - nrec;
     } else {
         rc = record_forward(e, s, steps);
     }
@@ -1079,11 +1099,12 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     };
     if (s->K) {
         // Two-stage pipeline over the segments, last to first. The engine stream restores
-        // checkpoint k and recomputes segment k, recording its factors into half k % 2 of the
-        // slots; the reverse stream then sweeps segment k from those factors while the engine
-        // stream already recomputes segment k-1 into the other half (after the sweep of segment
-        // k+1 has released it). The two streams share nothing else: the sweep reads the
-        // coefficients, the factors and its own adjoint arrays, the recompute the engine state.
+        // checkpoint k and recomputes segment k, recording its factors into buffer k % FB; the
+        // reverse stream then sweeps segment k from those factors while the engine stream already
+        // recomputes the segments below it, up to FB-1 ahead (a buffer is reused once the sweep
+        // of its previous segment has released it). The two streams share nothing else: the
+        // sweep reads the coefficients, the factors and its own adjoint arrays, the recompute the
+        // engine state.  The last FB-1 segments were recorded by the forward run.
         const unsigned nseg = (N + s->K - 1) / s->K;
         const size_t half = (size_t)s->K * 6 * d.B;
         auto fac_out = [&](unsigned hb) {
@@ -1094,9 +1115,9 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         // in its main box), and the recompute of a whole segment replays a captured graph of 16
         // steps per factor half (the step counter and the slot come from device memory).
         constexpr unsigned RG = 16;
-        cudaGraphExec_t rgraph[2] = {nullptr, nullptr};
+        cudaGraphExec_t rgraph[FB] = {};
         if (s->box4 && s->K % RG == 0) {
-            for (unsigned hb = 0; hb < 2 && rc == OEMS_OK; ++hb) {
+            for (unsigned hb = 0; hb < FB && rc == OEMS_OK; ++hb) {
                 const FacOut fo = fac_out(hb);
                 cudaGraph_t graph = nullptr;
                 if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
@@ -1112,9 +1133,9 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         }
         // the reverse sweep of a whole segment likewise replays a graph of 16 reverse steps per
         // factor half, n coming from the device counters (set at the segment's start)
-        cudaGraphExec_t vgraph[2] = {nullptr, nullptr};
+        cudaGraphExec_t vgraph[FB] = {};
         if (s->box4 && s->K % RG == 0 && rc == OEMS_OK) {
-            for (unsigned hb = 0; hb < 2 && rc == OEMS_OK; ++hb) {
+            for (unsigned hb = 0; hb < FB && rc == OEMS_OK; ++hb) {
                 AdjDev dg = d;
                 dg.nctr = s->rev_n;
                 dg.gctr = d.B ? s->rev_ng : nullptr;
@@ -1138,16 +1159,20 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
             }
         }
         auto recompute = [&](unsigned seg) -> int {
+            if (seg >= s->recorded_from) {                  // recorded by the forward run
+                cudaEventRecord(s->ev_recomputed[seg % FB], st);
+                return OEMS_OK;
+            }
             const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
-            float* base = s->fac + (seg & 1u) * half;
+            float* base = s->fac + (seg % FB) * half;
             int r2;
             if ((r2 = copy_state(e, s, s->ckpt[seg], false))) return r2;
             cudaMemcpyAsync(s->rec_numTS, &a0, sizeof(unsigned), cudaMemcpyHostToDevice, st);
-            const FacOut fo = fac_out(seg & 1u);
+            const FacOut fo = fac_out(seg % FB);
             unsigned n = a0;
-            if (rgraph[seg & 1u])
+            if (rgraph[seg % FB])
                 for (; n + RG <= a1; n += RG)
-                    if (cudaGraphLaunch(rgraph[seg & 1u], st) != cudaSuccess)
+                    if (cudaGraphLaunch(rgraph[seg % FB], st) != cudaSuccess)
                         return afail(e, OEMS_ERR_CUDA, "recompute graph launch");
             for (; n < a1; ++n) {
                 if (s->box4) {
@@ -1157,26 +1182,29 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
                     recompute_step(e, s);
                 }
             }
-            cudaEventRecord(s->ev_recomputed[seg & 1u], st);
+            cudaEventRecord(s->ev_recomputed[seg % FB], st);
             return OEMS_OK;
         };
-        if (rc == OEMS_OK) rc = recompute(nseg - 1);
+        // the first FB-1 segments of the sweep, then one more ahead per swept segment
+        for (int seg = (int)nseg - 1; seg >= (int)nseg - (int)(FB - 1) && seg >= 0 && rc == OEMS_OK; --seg)
+            rc = recompute((unsigned)seg);
         for (int seg = (int)nseg - 1; seg >= 0 && rc == OEMS_OK; --seg) {
             const unsigned a0 = seg * s->K, a1 = std::min(N, a0 + s->K);
-            if (seg > 0) {
-                // segment seg-1 reuses the half of segment seg+1: wait for that sweep
-                if (seg + 1 < (int)nseg) cudaStreamWaitEvent(st, s->ev_reversed[(seg + 1) & 1], 0);
-                if ((rc = recompute(seg - 1))) break;
+            const int ahead = seg - (int)(FB - 1);
+            if (ahead >= 0) {
+                // segment `ahead` reuses the buffer of segment ahead+FB: wait for that sweep
+                if (ahead + (int)FB < (int)nseg) cudaStreamWaitEvent(st, s->ev_reversed[(ahead + FB) % FB], 0);
+                if ((rc = recompute((unsigned)ahead))) break;
             }
-            cudaStreamWaitEvent(s->rs, s->ev_recomputed[seg & 1], 0);
-            const float* base = s->fac + (seg & 1) * half;
-            if (vgraph[seg & 1] && a1 - a0 == s->K) {
+            cudaStreamWaitEvent(s->rs, s->ev_recomputed[seg % FB], 0);
+            const float* base = s->fac + (seg % FB) * half;
+            if (vgraph[seg % FB] && a1 - a0 == s->K) {
                 // the previous direct step's sums first; then n = a1-1 down to a0 from the counters
                 cudaStreamWaitEvent(s->rs, s->ev_grad, 0);
                 const unsigned start[2] = {a1 - 1, a1 - 1};
                 cudaMemcpyAsync(s->rev_n, start, sizeof(start), cudaMemcpyHostToDevice, s->rs);
                 for (unsigned r = 0; r < s->K / RG; ++r)
-                    if (cudaGraphLaunch(vgraph[seg & 1], s->rs) != cudaSuccess) {
+                    if (cudaGraphLaunch(vgraph[seg % FB], s->rs) != cudaSuccess) {
                         rc = afail(e, OEMS_ERR_CUDA, "reverse graph launch");
                         break;
                     }
@@ -1185,7 +1213,7 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
                     reverse((unsigned)n, base + (size_t)(n % s->K) * 6 * d.B, s->rs);
             }
             if (s->ev_grad) cudaStreamWaitEvent(s->rs, s->ev_grad, 0);   // the sums read this half too
-            cudaEventRecord(s->ev_reversed[seg & 1], s->rs);
+            cudaEventRecord(s->ev_reversed[seg % FB], s->rs);
             if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
         }
         // the gradients, the timing event and the state restore follow the last sweep
@@ -1202,6 +1230,8 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         if (cudaGetLastError() != cudaSuccess) rc = afail(e, OEMS_ERR_CUDA, "adjoint launch");
     }
     s->launches_per_reverse_step = lps;
+    // the recompute of earlier segments reused the recorded halves: a later sweep recomputes all
+    if (s->K && s->recorded_from != ~0u && s->recorded_from > 0) s->recorded_from = ~0u;
     // leave the engine at its forward end state
     if (rc == OEMS_OK && s->K) rc = copy_state(e, s, s->ckpt.back(), false);
     if (rc == OEMS_OK) {
@@ -1242,7 +1272,7 @@ void oems_adjoint_free(oems_adjoint_state* s)
     for (void* p : s->allocs) cudaFree(p);
     for (cudaEvent_t ev : s->ev)
         if (ev) cudaEventDestroy(ev);
-    for (int b = 0; b < 2; ++b) {
+    for (unsigned b = 0; b < FB; ++b) {
         if (s->ev_recomputed[b]) cudaEventDestroy(s->ev_recomputed[b]);
         if (s->ev_reversed[b]) cudaEventDestroy(s->ev_reversed[b]);
     }
