@@ -126,6 +126,10 @@ def build_workload(name, shape=None):
         shape = tuple(shape) if shape else (512, 512, 256)
         return (configs.stress(shape=shape, steps=100000),
                 "stress %dx%dx%d lines, 64 random blocks (10%% Drude/Lorentz), Mur x6, 4 sources" % shape)
+    if name == "stress_upml":
+        shape = tuple(shape) if shape else (512, 512, 256)
+        return (configs.stress(shape=shape, steps=100000, bc=(3,) * 6, dispersive=False),
+                "stress %dx%dx%d lines, 64 random blocks, UPML 8 x6, 4 sources" % shape)
     if name == "patch":
         return configs.patch(steps=100000), "patch 160x160x80 graded, UPML 8, 50 Ohm port, NF2FF 3 freqs"
     if name == "plain":
@@ -445,7 +449,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="stress", choices=["stress", "patch", "plain", "design"])
+    ap.add_argument("--workload", default="stress", choices=["stress", "stress_upml", "patch", "plain", "design"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--shape", default=None, help="mesh lines of the stress workload, e.g. 256,256,192")
@@ -524,7 +528,7 @@ def main():
     avg_ms = kms[di] / max(kcnt[di], 1)
     achieved = ALG_BYTES_PER_CELL_HALF * cells / (avg_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
-    tr = _traffic_from_profiles(dom)
+    tr = _traffic_from_profiles(dom) if args.workload == "stress" else None   # measured for that mesh
     kname = eng.update_kernels()[0 if dom == "update_v" else 1]
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
