@@ -543,6 +543,23 @@ class _Painter:
         m = np.broadcast_to(m, tuple(i.size for i in idx))
         return idx, m
 
+    def paint_bbox(self, cx, cy, cz):
+        """paint() over the smallest index box that holds every sample point inside one of the
+        primitives (all other points are background): (map of that box, its index offsets)."""
+        cs = (np.asarray(cx), np.asarray(cy), np.asarray(cz))
+        lo = [None] * 3
+        hi = [None] * 3
+        for rec in self.recs:
+            for k in range(3):
+                idx = np.nonzero((cs[k] >= rec[0][k]) & (cs[k] <= rec[1][k]))[0]
+                if idx.size:
+                    lo[k] = int(idx[0]) if lo[k] is None else min(lo[k], int(idx[0]))
+                    hi[k] = int(idx[-1]) if hi[k] is None else max(hi[k], int(idx[-1]))
+        if any(v is None for v in lo):
+            return np.full((0, 0, 0), -1, np.int32), (0, 0, 0)
+        m = self.paint(cs[0][lo[0]:hi[0] + 1], cs[1][lo[1]:hi[1] + 1], cs[2][lo[2]:hi[2] + 1])
+        return m, (lo[0], lo[1], lo[2])
+
     def paint(self, cx, cy, cz):
         """Return int32 array [len(cx),len(cy),len(cz)] of property indices (-1 = background)."""
         out = np.full((len(cx), len(cy), len(cz)), -1, np.int32)
@@ -1248,16 +1265,18 @@ class Operator:
         vrec, crec = [], []
         if painter.props:
             for n in range(3):
-                # electric: Yee point of the main mesh, skip pos[n] >= N-1
+                # electric: Yee point of the main mesh, skip pos[n] >= N-1 (painted only over the
+                # index box that holds the excitation primitives: the rest is background)
                 cs = [self.L[0], self.L[1], self.L[2]]
                 cs[n] = self.dl[n]
-                m = painter.paint(*cs)
+                m, (ox, oy, oz) = painter.paint_bbox(*cs)
                 valid = np.ones(m.shape, bool)
                 sl = [slice(None)] * 3
-                sl[n] = slice(int(self.N[n]) - 1, None)
+                sl[n] = slice(max(0, int(self.N[n]) - 1 - (ox, oy, oz)[n]), None)
                 valid[tuple(sl)] = False
-                for x, y, z in zip(*np.nonzero((m >= 0) & valid)):
-                    prop = painter.props[m[x, y, z]]
+                for sx, sy, sz in zip(*np.nonzero((m >= 0) & valid)):
+                    x, y, z = int(sx) + ox, int(sy) + oy, int(sz) + oz
+                    prop = painter.props[m[sx, sy, sz]]
                     et = prop.params["exc_type"]
                     if et not in (0, 1):
                         continue
@@ -1274,11 +1293,13 @@ class Operator:
                 # magnetic: dual Yee point, skip the last H line in every direction
                 cs = [self.dl[0], self.dl[1], self.dl[2]]
                 cs[n] = self.L[n]
-                m = painter.paint(*cs)
+                m, (ox, oy, oz) = painter.paint_bbox(*cs)
                 valid = np.zeros(m.shape, bool)
-                valid[:-1, :-1, :-1] = True
-                for x, y, z in zip(*np.nonzero((m >= 0) & valid)):
-                    prop = painter.props[m[x, y, z]]
+                valid[:max(0, int(self.N[0]) - 1 - ox), :max(0, int(self.N[1]) - 1 - oy),
+                      :max(0, int(self.N[2]) - 1 - oz)] = True
+                for sx, sy, sz in zip(*np.nonzero((m >= 0) & valid)):
+                    x, y, z = int(sx) + ox, int(sy) + oy, int(sz) + oz
+                    prop = painter.props[m[sx, sy, sz]]
                     et = prop.params["exc_type"]
                     if et not in (2, 3):
                         continue
@@ -2000,6 +2021,21 @@ class Operator:
         painter = self._matmetal
         dT = self.dT
         Nx = int(self.N[0])
+        Ny, Nz = int(self.N[1]), int(self.N[2])
+        # the index box that holds every sample point (primary or dual line) inside a dispersive
+        # primitive: outside it no edge can be dispersive, so only this box is painted
+        box = []
+        for k in range(3):
+            hit = np.zeros(int(self.N[k]), bool)
+            for rec in painter.recs:
+                if rec[4].kind == MATERIAL and rec[4].params.get("lorentz"):
+                    for c in (np.asarray(self.L[k]), np.asarray(self.dl[k])):
+                        hit |= (c >= rec[0][k]) & (c <= rec[1][k])
+            idx = np.nonzero(hit)[0]
+            box.append((int(idx[0]), int(idx[-1]) + 1) if idx.size else (0, 0))
+        (bx0, bx1), (y0, y1), (z0, z1) = box
+        if bx1 <= bx0 or y1 <= y0 or z1 <= z0:
+            return []
         orders = []
         for o in range(order_max):
             def ptab(key):
@@ -2014,28 +2050,28 @@ class Operator:
 
             def slab(x0, x1):
                 per_n = []
-                on_mask = np.zeros((x1 - x0,) + tuple(int(v) for v in self.N[1:]), bool)
+                on_mask = np.zeros((x1 - x0, y1 - y0, z1 - z0), bool)
                 flags = [False, False, False, False]
                 for n in range(3):
                     # voltage part: main Yee point, skip pos[n] >= N-1 and edges with VI == 0
-                    cs = [self.L[0][x0:x1], self.L[1], self.L[2]]
+                    cs = [self.L[0][x0:x1], self.L[1][y0:y1], self.L[2][z0:z1]]
                     if n == 0:
                         cs[0] = self.dl[0][x0:x1]
                     else:
-                        cs[n] = self.dl[n]
+                        cs[n] = self.dl[n][(y0, z0)[n - 1]:(y1, z1)[n - 1]]
                     m = painter.paint(*cs)
-                    valid = self.vi[n, x0:x1] != 0
+                    valid = self.vi[n, x0:x1, y0:y1, z0:z1] != 0
                     if n == 0:
                         if x1 == Nx:
                             valid[-1] = False
                     else:
                         sl = [slice(None)] * 3
-                        sl[n] = slice(int(self.N[n]) - 1, None)
+                        sl[n] = slice(max(0, int(self.N[n]) - 1 - (y0, z0)[n - 1]), None)
                         valid[tuple(sl)] = False
                     wp = tab["eps_plasma"][m] * 2 * PI
                     trel = tab["eps_relax"][m]
                     wl = tab["eps_pole"][m] * 2 * PI
-                    C = self.EC_C[n, x0:x1].astype(np.float64)
+                    C = self.EC_C[n, x0:x1, y0:y1, z0:z1].astype(np.float64)
                     with np.errstate(divide="ignore", invalid="ignore"):
                         LD = np.where(valid & (wp > 0) & (C > 0), 1 / (wp * wp * C), 0.0)
                         RD = np.where((LD > 0) & (trel > 0), LD / np.where(trel > 0, trel, 1), 0.0)
@@ -2043,21 +2079,23 @@ class Operator:
                     flags[0] |= bool((LD > 0).any())
                     flags[2] |= bool((CL > 0).any())
                     # current part: dual Yee point, skip the last H lines and IV == 0
-                    cs = [self.dl[0][x0:x1], self.dl[1], self.dl[2]]
+                    cs = [self.dl[0][x0:x1], self.dl[1][y0:y1], self.dl[2][z0:z1]]
                     if n == 0:
                         cs[0] = self.L[0][x0:x1]
                     else:
-                        cs[n] = self.L[n]
+                        cs[n] = self.L[n][(y0, z0)[n - 1]:(y1, z1)[n - 1]]
                     m2 = painter.paint(*cs)
-                    valid2 = self.iv[n, x0:x1] != 0
+                    valid2 = self.iv[n, x0:x1, y0:y1, z0:z1] != 0
                     if x1 == Nx:
                         valid2[-1] = False
-                    valid2[:, -1, :] = False
-                    valid2[:, :, -1] = False
+                    if y1 == Ny:
+                        valid2[:, -1, :] = False
+                    if z1 == Nz:
+                        valid2[:, :, -1] = False
                     wpm = tab["mue_plasma"][m2] * 2 * PI
                     trelm = tab["mue_relax"][m2]
                     wlm = tab["mue_pole"][m2] * 2 * PI
-                    Lh = self.EC_L[n, x0:x1].astype(np.float64)
+                    Lh = self.EC_L[n, x0:x1, y0:y1, z0:z1].astype(np.float64)
                     with np.errstate(divide="ignore", invalid="ignore"):
                         CD = np.where(valid2 & (wpm > 0) & (Lh > 0), 1 / (wpm * wpm * Lh), 0.0)
                         GD = np.where((CD > 0) & (trelm > 0), CD / np.where(trelm > 0, trelm, 1), 0.0)
@@ -2073,8 +2111,8 @@ class Operator:
                 with np.errstate(divide="ignore", invalid="ignore"):
                     for n in range(3):
                         LD, RD, CL, CD, GD, LL = (t[sel] for t in per_n[n])
-                        VI = self.vi[n, x0:x1][sel].astype(np.float64)
-                        IV = self.iv[n, x0:x1][sel].astype(np.float64)
+                        VI = self.vi[n, x0:x1, y0:y1, z0:z1][sel].astype(np.float64)
+                        IV = self.iv[n, x0:x1, y0:y1, z0:z1][sel].astype(np.float64)
                         drude = LD > 0
                         tabs["v_int"][n] = np.where(drude, (2.0 * LD - dT * RD) / (2.0 * LD + dT * RD), 1.0)
                         tabs["v_ext"][n] = np.where(drude, dT / (LD + dT * RD / 2.0) * VI, 0.0)
@@ -2083,9 +2121,11 @@ class Operator:
                         tabs["v_lor"][n] = np.where(CL > 0, dT / CL / VI, 0.0)
                         tabs["i_lor"][n] = np.where(LL > 0, dT / LL / IV, 0.0)
                 pos[0] += x0
+                pos[1] += y0
+                pos[2] += z0
                 return pos.astype(np.uint32), tabs, flags
 
-            parts = _parallel(slab, _slabs(Nx, 2 * (os.cpu_count() or 1)))
+            parts = _parallel(slab, [(bx0 + a, bx0 + b) for a, b in _slabs(bx1 - bx0, 2 * (os.cpu_count() or 1))])
             pos = np.concatenate([p[0] for p in parts], axis=1)
             tabs = {k: np.concatenate([p[1][k] for p in parts], axis=1) for k in parts[0][1]}
             fl = [any(p[2][i] for p in parts) for i in range(4)]

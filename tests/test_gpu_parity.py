@@ -145,6 +145,26 @@ def test_separate_mur_hooks_bit_exact_against_oracle(cuda_lib, monkeypatch, name
     assert not bad, (name, bad)
 
 
+def test_mur_float4_inner_z_walls_bit_exact_against_oracle(cuda_lib):
+    """k_update_v4w with z walls away from the row ends (lines 4 / 27 of 30, each with its shift in
+    the same group of four): the wall groups sit inside the rows, between streaming groups.  The
+    walls are placed by hand, which the oracle models the same way."""
+    import dataclasses
+    op = configs.stress(shape=(40, 36, 30), steps=140, nblocks=16)
+    walls = []
+    for w in op.mur:
+        if w.ny == 2:
+            lo = w.line_nr < w.line_nr_shift
+            w = dataclasses.replace(w, line_nr=4 if lo else 27, line_nr_shift=5 if lo else 26)
+        walls.append(w)
+    op.mur = walls
+    g, r = _run_pair(op, 140, chunks=(1, 7, 16, 33))
+    assert g.update_kernels()[0] == "k_update_v4w"
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, bad
+
+
 REG4_CASES = [
     ("patch_pml8", lambda: configs.patch(shape=(56, 52, 36), steps=220, with_nf2ff=False), 220),
     ("plane_wave_pml4", lambda: configs.plane_wave(n=(28, 24, 32), pml=4, steps=200), 200),
