@@ -773,27 +773,20 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
 int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch)
 {
     const FusedDev& f = e->fused[parity];
-    if (e->use_march) {
-        if (e->march_minb == 2)
-            k_step_march<2><<<e->march_grid, e->march_threads, e->march_smem, e->stream>>>(e->march[parity],
-                                                                                        e->march_map[parity]);
-        else
-            k_step_march<1><<<e->march_grid, e->march_threads, e->march_smem, e->stream>>>(e->march[parity],
-                                                                                        e->march_map[parity]);
-    } else {
-        const dim3 grid((e->N[2] + FT_Z - 1) / FT_Z, (e->N[1] + FT_Y - 1) / FT_Y, (e->N[0] + f.xchunk - 1) / f.xchunk);
-        if (e->compressed) k_step_fused<true><<<grid, FT_BLOCK, 0, e->stream>>>(f);
-        else k_step_fused<false><<<grid, FT_BLOCK, 0, e->stream>>>(f);
-    }
+    if (e->march_minb == 2)
+        k_step_march<2><<<e->march_grid, e->march_threads, e->march_smem, e->stream>>>(e->march[parity],
+                                                                                    e->march_map[parity]);
+    else
+        k_step_march<1><<<e->march_grid, e->march_threads, e->march_smem, e->stream>>>(e->march[parity],
+                                                                                    e->march_map[parity]);
     // processing on the fields this step wrote
     GridDev g = e->grid;
     g.V = f.Vo;
     g.I = f.Io;
-    for (int r = 0; r < g.nupml; ++r) g.upml[r].vflux = f.vflux_o[r];
     k_step_end<<<e->stepend_blocks, 256, 0, e->stream>>>(g, e->stepend);
     if (nlaunch) *nlaunch = 2;
     cudaError_t c = cudaGetLastError();
-    if (c != cudaSuccess) return cuda_fail(e, c, "fused step launch");
+    if (c != cudaSuccess) return cuda_fail(e, c, "one-kernel step launch");
     return OEMS_OK;
 }
 
@@ -879,8 +872,6 @@ static int setup_fused(oems_cuda_engine* e)
     int rc;
     if ((rc = dalloc(e, &e->dV2, 3 * e->S, true))) return rc;
     if ((rc = dalloc(e, &e->dI2, 3 * e->S, true))) return rc;
-    for (int r = 0; r < e->grid.nupml; ++r)
-        if ((rc = dalloc(e, &e->vflux2[r], 3 * (size_t)e->grid.upml[r].n, true))) return rc;
     FusedDev base{};
     base.excV = e->excV;
     base.excI = e->excI;
@@ -902,9 +893,6 @@ static int setup_fused(oems_cuda_engine* e)
     };
     if ((rc = cells(e->exc_voff, &base.srcV_cell, base.srcV_lo, base.srcV_hi))) return rc;
     if ((rc = cells(e->exc_ioff, &base.srcI_cell, base.srcI_lo, base.srcI_hi))) return rc;
-    // x-planes per block: about 8 blocks per SM of a 152-SM GPU, 4..64 planes
-    const unsigned long long tiles = (unsigned long long)((e->N[2] + FT_Z - 1) / FT_Z) * ((e->N[1] + FT_Y - 1) / FT_Y);
-    base.xchunk = (unsigned)std::min<unsigned long long>(64, std::max<unsigned long long>(4, e->N[0] * tiles / 1216));
     FusedDev& f0 = e->fused[0];
     FusedDev& f1 = e->fused[1];
     f0 = base;
@@ -917,11 +905,6 @@ static int setup_fused(oems_cuda_engine* e)
     f1.g.I = e->dI2;
     f1.Vo = e->dV;
     f1.Io = e->dI;
-    for (int r = 0; r < e->grid.nupml; ++r) {
-        f0.vflux_o[r] = e->vflux2[r];
-        f1.g.upml[r].vflux = e->vflux2[r];
-        f1.vflux_o[r] = e->grid.upml[r].vflux;
-    }
     return OEMS_OK;
 }
 
@@ -1480,19 +1463,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(e->stream));
     }
-    // OEMS_CUDA_FUSED=1 replaces the K-step graph by the fused one-kernel step, for engines where
-    // no hook reads neighbouring lines between the half-steps (Mur walls, dispersive materials).
-    // It moves 38 % fewer bytes but its plane-serial march is latency-bound and slower than the
-    // separate update kernels on GB300, so it is not the default.
-    {
-        const char* env = getenv("OEMS_CUDA_FUSED");
-        e->use_fused = env && env[0] == '1' && e->mur.empty() && e->lor.empty() && !e->has_tfsf && !e->rlc.count &&
-                       !e->cyl_closed &&
-                       e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC && e->K % 2 == 0 &&
-                       3ull * e->S < (1ull << 32);        // the staged-plane offsets are 32-bit
-        if (e->use_fused && (rc = setup_fused(e))) return rc;
-    }
-    // OEMS_CUDA_MARCH=1: the fused step as the TMA-staged plane march, where the engine is
+    // OEMS_CUDA_MARCH=1: one kernel per step, the TMA-staged plane march, where the engine is
     // compressed, has no hook at all but the soft sources and its z lines fit one TMA box
     {
         const char* env = getenv("OEMS_CUDA_MARCH");
@@ -1501,7 +1472,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
                           !e->rlc.count && !e->cyl_closed && e->Pz <= 256 && e->K % 2 == 0 &&
                           e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC;
         if (want && fits) {
-            if (!e->use_fused && (rc = setup_fused(e))) return rc;
+            if ((rc = setup_fused(e))) return rc;
             e->use_fused = true;
             if ((rc = setup_march(e))) return rc;
             e->use_march = true;
@@ -1605,7 +1576,6 @@ int oems_cuda_update_kernels(oems_cuda_engine* e, char* volt, char* curr, size_t
     if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
     const char *v = "", *i = "";
     if (e->use_march) v = i = "k_step_march";
-    else if (e->use_fused) v = i = "k_step_fused";
     else {
         launch_update(e, false, e->stream, &v);
         launch_update(e, true, e->stream, &i);

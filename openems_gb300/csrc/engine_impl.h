@@ -172,16 +172,14 @@ struct oems_cuda_engine {
     // the voltage update with the Mur hooks in the float4 form (k_update_v4w)
     bool mur_v4 = false;
 
-    // fused one-kernel step (engines without Mur walls and dispersive materials): the K-step
-    // graph alternates buffer sets A (dV, dI, UPML vflux) and B; K is even, so the state is in A
-    // whenever the host sees it
+    // one-kernel step (the plane march, march.cuh): the K-step graph alternates buffer sets A
+    // (dV, dI) and B (dV2, dI2); K is even, so the state is in A whenever the host sees it
     bool use_fused = false;
     float* dV2 = nullptr;
     float* dI2 = nullptr;
-    float* vflux2[OEMS_MAX_UPML] = {};
     FusedDev fused[2]{};
     unsigned fused_launches = 0;
-    // TMA-staged plane march (march.cuh): the fused step's buffers and parities, one kernel per
+    // TMA-staged plane march (march.cuh): the buffer sets and parities above, one kernel per
     // step, for compressed engines with PEC/PMC walls only; the maps describe I of sets A and B
     bool use_march = false;
     MarchDev march[2]{};
@@ -192,7 +190,7 @@ struct oems_cuda_engine {
     unsigned* d_march_err = nullptr;
 };
 
-// enqueue one fused timestep on e->stream: parity 0 reads set A and writes B, parity 1 the reverse
+// enqueue one one-kernel timestep on e->stream: parity 0 reads set A and writes B, parity 1 the reverse
 int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch);
 
 // the split for update range R (V: the mesh, I: one cell less per axis)

@@ -84,22 +84,6 @@ def test_bit_exact_against_oracle(cuda_lib, name, fn, steps):
     assert g.GetNumberOfTimesteps() == steps
 
 
-@pytest.mark.parametrize("name,fn,steps", [c for c in CASES if c[0] in ("cube40", "patch_small")] +
-                         [("design_small", lambda: configs.DesignCase(lines=(44, 44, 34), design=(8, 8, 4), gap=8,
-                                                                      steps=120, seed=2).build(
-                             np.full((8, 8, 4), 3.0))[1], 120)])
-def test_fused_step_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, steps):
-    """The opt-in fused one-kernel step (ping-pong buffers inside the 16-step graph, mixed with
-    single separate-kernel steps by the uneven chunks)."""
-    monkeypatch.setenv("OEMS_CUDA_FUSED", "1")
-    op = fn()
-    g, r = _run_pair(op, steps, chunks=(1, 7, 16, 33))
-    assert g.launches_per_step() == 2                      # fused step + processing
-    res = compare_engines(g, r)
-    bad = [k for k, v in res.items() if not v]
-    assert not bad, (name, bad)
-
-
 MARCH_CASES = [
     ("cube40", lambda: configs.plain_cube(n=40, steps=300), 300),
     ("cube33_lanes", lambda: configs.plain_cube(n=33, steps=260), 260),
