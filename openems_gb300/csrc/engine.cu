@@ -183,6 +183,7 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     td_free(e);
     if (e->graph1) cudaGraphExecDestroy(e->graph1);
     if (e->graphK) cudaGraphExecDestroy(e->graphK);
+    if (e->graphK_alt) cudaGraphExecDestroy(e->graphK_alt);
     oems_adjoint_free(e->adj);
     for (void* p : e->allocs) cudaFree(p);
     if (e->stream_r) {
@@ -940,8 +941,9 @@ static void march_shape(const oems_cuda_engine* e, unsigned& ty, unsigned& xchun
     if (s && atoi(s) > 0) ty = (unsigned)atoi(s);
     while (ty > 1 && ((ty + 1) * G > 512 || bytes_of(ty) > 227u * 1024u)) --ty;
     const unsigned long long tiles = (e->N[1] + ty - 1) / ty;
-    // about four waves of one block per SM on a 152-SM GPU, 4..64 planes per block
-    xchunk = (unsigned)std::min<unsigned long long>(64, std::max<unsigned long long>(4, e->N[0] * tiles / 608));
+    // 32 planes per block (the fastest chunk on 256^3 and 512x512x256 meshes; 16 and 64 were
+    // slower), fewer on small meshes so that every one of the 152 SMs gets a block: 4..32
+    xchunk = (unsigned)std::min<unsigned long long>(32, std::max<unsigned long long>(4, e->N[0] * tiles / 152));
     const char* xc = getenv("OEMS_CUDA_MARCH_XCHUNK");
     if (xc && atoi(xc) > 0) xchunk = (unsigned)atoi(xc);
     smem = bytes_of(ty);
@@ -1463,22 +1465,29 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(e->stream));
     }
-    // OEMS_CUDA_MARCH=1: one kernel per step, the TMA-staged plane march, where the engine is
-    // compressed, has no hook at all but the soft sources and its z lines fit one TMA box
+    // The TMA-staged plane march (one kernel per step) applies where the engine is compressed,
+    // has no hook but the soft sources and its z lines fit one TMA box.  OEMS_CUDA_MARCH=1 always
+    // uses it, =0 never; otherwise both K-step graphs are captured and the first long iterate
+    // times one of each and keeps the faster (both give the same bits).
+    bool tune = false;
     {
         const char* env = getenv("OEMS_CUDA_MARCH");
-        const bool want = env && env[0] == '1';
+        const bool force = env && env[0] == '1', never = env && env[0] == '0';
         const bool fits = e->compressed && e->grid.nupml == 0 && e->mur.empty() && e->lor.empty() && !e->has_tfsf &&
                           !e->rlc.count && !e->cyl_closed && e->Pz <= 256 && e->K % 2 == 0 &&
                           e->excV.count <= (unsigned)FT_MAX_SRC && e->excI.count <= (unsigned)FT_MAX_SRC;
-        if (want && fits) {
+        if (fits && (force || (!never && !e->has_td))) {
             if ((rc = setup_fused(e))) return rc;
-            e->use_fused = true;
             if ((rc = setup_march(e))) return rc;
-            e->use_march = true;
+            e->use_fused = e->use_march = force;
+            tune = !force;
         }
     }
     if ((rc = capture(e, 1, &e->graph1, false))) return rc;
+    if (tune) {
+        if ((rc = capture(e, e->K, &e->graphK_alt, true))) return rc;       // the march
+        e->march_tune = true;
+    }
     if ((rc = capture(e, e->K, &e->graphK, e->use_fused))) return rc;
     e->inited = true;
     // time-domain dumps: start the writer and hand it the numTS = 0 samples
@@ -1498,6 +1507,28 @@ int oems_cuda_iterate(oems_cuda_engine* e, unsigned int n)
     CK(cudaSetDevice(e->device));
     if (e->has_td) return td_iterate(e, n);
     unsigned done = 0;
+    if (e->march_tune && n >= 4 * e->K) {
+        // one warm-up launch of each, then one timed launch of each (real steps, same results)
+        cudaEvent_t ev[3];
+        for (auto& x : ev) CK(cudaEventCreate(&x));
+        CK(cudaGraphLaunch(e->graphK_alt, e->stream));
+        CK(cudaGraphLaunch(e->graphK, e->stream));
+        CK(cudaEventRecord(ev[0], e->stream));
+        CK(cudaGraphLaunch(e->graphK_alt, e->stream));
+        CK(cudaEventRecord(ev[1], e->stream));
+        CK(cudaGraphLaunch(e->graphK, e->stream));
+        CK(cudaEventRecord(ev[2], e->stream));
+        CK(cudaEventSynchronize(ev[2]));
+        cudaEventElapsedTime(&e->march_tune_ms[0], ev[0], ev[1]);
+        cudaEventElapsedTime(&e->march_tune_ms[1], ev[1], ev[2]);
+        for (auto& x : ev) cudaEventDestroy(x);
+        if (e->march_tune_ms[0] < e->march_tune_ms[1]) {
+            std::swap(e->graphK, e->graphK_alt);
+            e->use_fused = e->use_march = true;
+        }
+        e->march_tune = false;
+        done = 4 * e->K;
+    }
     while (n - done >= e->K) { CK(cudaGraphLaunch(e->graphK, e->stream)); done += e->K; }
     while (done < n) { CK(cudaGraphLaunch(e->graph1, e->stream)); ++done; }
     e->host_numTS += n;

@@ -188,6 +188,11 @@ struct oems_cuda_engine {
     unsigned march_threads = 0, march_smem = 0;
     int march_minb = 1;
     unsigned* d_march_err = nullptr;
+    // the march and the separate kernels both captured, the faster chosen on the first iterate
+    // that runs at least four K-step graphs (OEMS_CUDA_MARCH unset); graphK_alt holds the other
+    bool march_tune = false;
+    cudaGraphExec_t graphK_alt = nullptr;
+    float march_tune_ms[2] = {0.f, 0.f};   // one K-step graph: march, separate kernels
 };
 
 // enqueue one one-kernel timestep on e->stream: parity 0 reads set A and writes B, parity 1 the reverse

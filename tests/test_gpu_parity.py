@@ -129,6 +129,19 @@ def test_separate_mur_hooks_bit_exact_against_oracle(cuda_lib, monkeypatch, name
     assert not bad, (name, bad)
 
 
+@pytest.mark.parametrize("name,fn,steps", MARCH_CASES[:2])
+def test_march_autotune_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, steps):
+    """Without OEMS_CUDA_MARCH the first long iterate times the plane march against the separate
+    kernels and keeps the faster; either way the results equal the oracle's bit for bit."""
+    monkeypatch.delenv("OEMS_CUDA_MARCH", raising=False)
+    op = fn()
+    g, r = _run_pair(op, steps, chunks=(steps - 13, 13))
+    assert g.update_kernels()[0] in ("k_step_march", "k_update_v4"), g.update_kernels()
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, (name, bad)
+
+
 def test_mur_float4_inner_z_walls_bit_exact_against_oracle(cuda_lib):
     """k_update_v4w with z walls away from the row ends (lines 4 / 27 of 30, each with its shift in
     the same group of four): the wall groups sit inside the rows, between streaming groups.  The
