@@ -203,8 +203,8 @@ def measure_config(name, steps, e2e_steps=200, cpu_budget=0.0):
         op, desc = build_workload(name)
     t_build = time.perf_counter() - t0
     cells = float(np.prod(op.num_lines.astype(np.float64)))
-    eng = Engine_CUDA(op, steps + e2e_steps + 16)
-    eng.IterateTS(5)
+    eng = Engine_CUDA(op, steps + e2e_steps + 96)
+    eng.IterateTS(80)               # warm-up; also where the engine picks its step form (>= 4 graphs)
     eng.sync()
     ms = eng.timed_iterate(steps)
     pids = eng.vprobe_ids + eng.iprobe_ids
