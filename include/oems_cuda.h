@@ -310,11 +310,15 @@ int oems_cuda_energy_noalloc(const float* volt_dev, const float* curr_dev, const
 typedef struct oems_cuda_batch oems_cuda_batch;
 int oems_cuda_batch_create(oems_cuda_engine* const* engines, unsigned int count, oems_cuda_batch** out);
 
-/* Advance instance k by steps[k] timesteps (uneven counts allowed). Each chunk of steps over the
- * instances active throughout it is one persistent cooperative launch; the launches are
- * captured in one CUDA graph. block_size/depth = 0 lets the built-in autotuner time the
- * candidate (block size, x-planes per work item) pairs on the first steps and keep the
- * fastest. Results are bit-identical to running each engine alone with oems_cuda_iterate. */
+/* Advance instance k by steps[k] timesteps (uneven counts allowed), in chunks over the instances
+ * active throughout each chunk. Execution modes: persistent cooperative launches (one per
+ * chunk, all chunks in one CUDA graph); per-phase launches over every instance (depth flag
+ * 0x80000000) or over L2-sized instance groups (0xC0000000); concurrent graph branches, one per
+ * instance with its own step kernels (0x20000000), or the same over L2-sized groups
+ * (0x10000000). block_size/depth = 0 lets the built-in autotuner time the candidate (mode,
+ * block size, x-planes per work item) sets on the first steps and keep the fastest (the tuning
+ * steps are real steps). Results are bit-identical to running each engine alone with
+ * oems_cuda_iterate. */
 int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned int block_size, unsigned int depth);
 
 /* The configuration in use, whether the launches ran from a captured graph, and the autotuner's

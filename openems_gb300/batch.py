@@ -25,6 +25,7 @@ class BatchEngine:
     PHASES = 0x80000000      # depth flag: per-phase launches instead of one persistent launch
     GROUPED = 0xC0000000     # depth flag: per-phase launches over L2-sized instance groups
     CONCURRENT = 0x20000000  # depth flag: one graph branch per instance with its own step kernels
+    CONCURRENT_GROUPED = 0x10000000  # depth flag: CONCURRENT over L2-sized instance groups
 
     def run(self, steps: Sequence[int], block_size: int = 0, depth: int = 0):
         st = (C.c_uint * len(steps))(*[int(s) for s in steps])
@@ -38,13 +39,15 @@ class BatchEngine:
         ms = (C.c_float * 16)()
         self.lib.batch_config(self.h, C.byref(b), C.byref(d), C.byref(g), ms, C.byref(n))
         mode = "persistent"
-        if d.value & 0x20000000:
+        if d.value & 0x10000000:
+            mode = "concurrent per-instance graph branches, L2-sized groups"
+        elif d.value & 0x20000000:
             mode = "concurrent per-instance graph branches"
         elif d.value & 0x40000000:
             mode = "per-phase launches, L2-sized groups"
         elif d.value & 0x80000000:
             mode = "per-phase launches"
-        return {"block_size": b.value, "depth": d.value & 0x1FFFFFFF, "mode": mode,
+        return {"block_size": b.value, "depth": d.value & 0x0FFFFFFF, "mode": mode,
                 "graph": bool(g.value), "tune_ms": [ms[i] for i in range(n.value)]}
 
     def close(self):

@@ -290,10 +290,10 @@ struct Cand {
 // mode 0: one persistent launch per chunk; 1: per-phase launches over every active instance;
 // 2: per-phase launches over L2-sized groups of instances (each group runs the chunk's steps
 // while its state stays in L2, then the next group); 3: concurrent graph branches, one per
-// instance, each running that instance's own step kernels
+// instance, each running that instance's own step kernels; 4: mode 3 over L2-sized groups
 const Cand kCands[] = {{0, 128, 1}, {0, 256, 4}, {0, 512, 4},
                        {1, 128, 1}, {1, 256, 1}, {1, 256, 2}, {1, 512, 1},
-                       {2, 128, 1}, {2, 256, 1}, {2, 256, 2}, {2, 512, 1}, {3, 256, 1}};
+                       {2, 128, 1}, {2, 256, 1}, {2, 256, 2}, {2, 512, 1}, {3, 256, 1}, {4, 256, 1}};
 constexpr unsigned kNumCands = sizeof(kCands) / sizeof(kCands[0]);
 constexpr unsigned kGraphSteps = 16;
 
@@ -476,6 +476,41 @@ int run_concurrent(oems_cuda_batch* b, const std::vector<int>& act, unsigned ste
     return e == cudaSuccess ? OEMS_OK : bfail(b, OEMS_ERR_CUDA);
 }
 
+// mode 4: the instances in groups whose state fits the L2; each group runs the chunk's steps as
+// concurrent per-instance branches (mode 3) before the next group starts.  Every group's graphs
+// are built first; ev (optional) brackets the launches alone.
+int run_concurrent_groups(oems_cuda_batch* b, const std::vector<std::vector<int>>& groups, unsigned steps,
+                          cudaEvent_t* ev)
+{
+    const unsigned full = steps / kGraphSteps, tail = steps % kGraphSteps;
+    std::vector<std::pair<cudaGraphExec_t, cudaGraphExec_t>> gx;
+    int rc = OEMS_OK;
+    for (const auto& grp : groups) {
+        cudaGraphExec_t g16 = nullptr, g1 = nullptr;
+        if (full && (rc = capture_concurrent(b, grp, kGraphSteps, &g16))) break;
+        if (tail && (rc = capture_concurrent(b, grp, 1, &g1))) {
+            if (g16) cudaGraphExecDestroy(g16);
+            break;
+        }
+        gx.push_back({g16, g1});
+    }
+    cudaError_t e = cudaSuccess;
+    if (rc == OEMS_OK) {
+        if (ev) cudaEventRecord(ev[0], b->stream);
+        for (const auto& g : gx) {
+            for (unsigned r = 0; r < full && e == cudaSuccess; ++r) e = cudaGraphLaunch(g.first, b->stream);
+            for (unsigned r = 0; r < tail && e == cudaSuccess; ++r) e = cudaGraphLaunch(g.second, b->stream);
+        }
+        if (ev) cudaEventRecord(ev[1], b->stream);
+    }
+    for (const auto& g : gx) {                      // freed when their launches complete
+        if (g.first) cudaGraphExecDestroy(g.first);
+        if (g.second) cudaGraphExecDestroy(g.second);
+    }
+    if (rc) return rc;
+    return e == cudaSuccess ? OEMS_OK : bfail(b, OEMS_ERR_CUDA);
+}
+
 }  // namespace
 
 extern "C" {
@@ -540,8 +575,9 @@ int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned 
     if (block_size) {
         if (block_size % 32 || block_size > 512) return OEMS_ERR_ARG;
         b->block = block_size;
-        b->mode = (depth & 0x20000000u) ? 3 : (depth & 0x40000000u) ? 2 : ((depth & 0x80000000u) ? 1 : 0);
-        b->depth = (depth & 0x1FFFFFFFu) ? (depth & 0x1FFFFFFFu) : 1;
+        b->mode = (depth & 0x10000000u) ? 4 : (depth & 0x20000000u) ? 3 : (depth & 0x40000000u) ? 2
+                                                                                          : ((depth & 0x80000000u) ? 1 : 0);
+        b->depth = (depth & 0x0FFFFFFFu) ? (depth & 0x0FFFFFFFu) : 1;
     }
     if (cudaMemsetAsync(b->bar, 0, sizeof(GridBar), b->stream) != cudaSuccess) return bfail(b, OEMS_ERR_CUDA);
     std::vector<unsigned> levels(rem.begin(), rem.end());
@@ -561,14 +597,18 @@ int oems_cuda_batch_run(oems_cuda_batch* b, const unsigned int* steps, unsigned 
                          bool use_graph, cudaEvent_t* ev) -> int {
         if (mode == 3) return run_concurrent(b, act, stp, ev);
         std::vector<std::vector<int>> groups;
-        if (mode == 2) {
+        if (mode == 2 || mode == 4) {
+            // consecutive instances while their state fits the budget (mode 4: the whole L2,
+            // mode 2: 60 % of it)
+            const size_t budget = mode == 4 ? b->l2_budget / 6 * 10 : b->l2_budget;
             size_t acc = 0;
             for (int k : act) {
                 const size_t bytes = instance_bytes(b->eng[k]);
-                if (groups.empty() || acc + bytes > b->l2_budget) { groups.emplace_back(); acc = 0; }
+                if (groups.empty() || acc + bytes > budget) { groups.emplace_back(); acc = 0; }
                 groups.back().push_back(k);
                 acc += bytes;
             }
+            if (mode == 4) return run_concurrent_groups(b, groups, stp, ev);
         } else {
             groups.push_back(act);
         }
@@ -712,7 +752,7 @@ int oems_cuda_batch_config(const oems_cuda_batch* b, unsigned int* block_size, u
     if (block_size) *block_size = b->block;
     if (depth)
         *depth = b->depth | (b->mode == 1 ? 0x80000000u : 0u) | (b->mode == 2 ? 0xC0000000u : 0u) |
-                 (b->mode == 3 ? 0x20000000u : 0u);
+                 (b->mode == 3 ? 0x20000000u : 0u) | (b->mode == 4 ? 0x10000000u : 0u);
     if (used_graph) *used_graph = b->used_graph ? 1 : 0;
     if (tune_ms) for (unsigned c = 0; c < b->ncand; ++c) tune_ms[c] = b->tune_ms[c];
     if (ncand) *ncand = b->ncand;

@@ -32,7 +32,7 @@ def _check(serial, batched):
 
 
 @pytest.mark.parametrize("block,depth", [(0, 0), (256, 1), (128, 4), (512, 2), (256, 0x80000001), (128, 0x80000002), (256, 0xC0000001), (512, 0xC0000002),
-                                         (256, 0x20000001)])
+                                         (256, 0x20000001), (256, 0x10000001)])
 def test_batch_equals_serial(cuda_lib, block, depth):
     inst = _instances()
     total = [2 * s for _, s in inst]
@@ -47,5 +47,5 @@ def test_batch_equals_serial(cuda_lib, block, depth):
     cfg = be.config()
     assert cfg["block_size"] in (128, 256, 512)
     if block == 0:
-        assert len(cfg["tune_ms"]) == 12 and min(cfg["tune_ms"]) > 0
+        assert len(cfg["tune_ms"]) == 13 and min(cfg["tune_ms"]) > 0
     be.close()
