@@ -133,7 +133,8 @@ def build_workload(name, shape=None):
     if name == "patch":
         return configs.patch(steps=100000), "patch 160x160x80 graded, UPML 8, 50 Ohm port, NF2FF 3 freqs"
     if name == "plain":
-        return configs.plain_cube(n=100, steps=100000), "plain 100^3, vacuum, PEC, soft Ez, V/I probes"
+        n = int(shape[0]) if shape else 100
+        return configs.plain_cube(n=n, steps=100000), "plain %d^3, vacuum, PEC, soft Ez, V/I probes" % n
     if name == "design":
         case = configs.DesignCase(steps=100000)
         return (case.build(case.eps0)[1],
