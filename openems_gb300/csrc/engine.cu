@@ -729,7 +729,10 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
         } else if (e->compressed) {
             if (o32 && e->vec4 && (mode == 0 || (mode == 2 && e->mur_v4))) {
                 const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
-                if (mode == 2) {
+                if (mode == 2 && m.park) {
+                    // every direct-column group streams; the z walls' hooks run around this launch
+                    if (go("k_update_v4w<park>")) k_update_v4w<unsigned, true><<<gv4, 256, 0, s>>>(g, m, ts, gv4.x);
+                } else if (mode == 2) {
                     // the interior blocks, then one thread per direct column's z-wall group
                     const unsigned walls = m.nz > 0 ? (e->N[1] * (unsigned)m.nz + 255) / 256 : 0;
                     const dim3 gw(gv4.x + walls, e->N[0]);
@@ -812,10 +815,16 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
     // the Mur pre/post hooks run inside the voltage update unless mur_separate
     const bool mur_sep = !e->mur.empty() && e->mur_separate;
     if (mur_sep) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 0, e->d_numTS); post(); ++L; }
+    // park mode: the direct columns' z-wall hooks around the voltage update (one thread per wall
+    // and column)
+    const bool park = e->murdev.park != 0;
+    const unsigned park_blocks = park ? ((unsigned)e->murdev.nz * g.Nx * g.Ny + 255) / 256 : 0;
+    if (park) { pre(OEMS_KC_MUR); k_mur_zsave<<<park_blocks, blk, 0, s>>>(g, e->murdev); post(); ++L; }
     pre(OEMS_KC_UPDATE_V);
     launch_update(e, false, s);
     post();
     ++L;
+    if (park) { pre(OEMS_KC_MUR); k_mur_zpost<<<park_blocks, blk, 0, s>>>(g, e->murdev); post(); ++L; }
     const unsigned cyl_v = g.Nx * g.Nz, cyl_i = (g.Nx - 1) * (g.Nz - 1);
     if (e->cyl.closed) {   // post-voltage hook, priority 1e5: before TFSF and Mur
         pre(OEMS_KC_MUR);
@@ -1162,6 +1171,14 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         if (md.nz == 2) groups_ok = groups_ok && (md.z[0].line >> 2) != (md.z[1].line >> 2);
         const char* mv = getenv("OEMS_CUDA_MUR_V4");
         e->mur_v4 = md.lanes && groups_ok && !(mv && mv[0] == '0');
+        // park mode of the float4 form (OEMS_CUDA_MUR_PARK=1): the direct columns' z-wall hooks as
+        // k_mur_zsave before and k_mur_zpost after the update.  The update itself then streams
+        // every group, but the two wall-plane kernels read one sector per z row at a row stride
+        // and cost more than they save, so the default keeps the hooks inside the update.
+        const char* mp = getenv("OEMS_CUDA_MUR_PARK");
+        md.park = (e->mur_v4 && md.nz > 0 && mp && mp[0] == '1') ? 1 : 0;
+        md.zsave = nullptr;
+        if (md.park && (rc = dalloc(e, &md.zsave, 2 * (size_t)md.nz * e->N[0] * e->N[1], true))) return rc;
     }
 
     // cylinder extension

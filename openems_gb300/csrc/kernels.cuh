@@ -120,6 +120,11 @@ struct MurDev {
     int nz;
     MurWallDev z[2];
     int lanes;
+    // park = 1: the voltage update runs the plain float4 form in the direct columns too, and the
+    // z walls' hooks there are k_mur_zsave (before the update) and k_mur_zpost (after it); zsave
+    // holds [nz][2][Nx*Ny]: the pre-update Mur value of tangential components 0 and 1
+    int park;
+    float* zsave;
 };
 
 // Where the Mur pre and post voltage hooks (engine_ext_mur_abc.cpp:83-149) run: inside the
@@ -698,7 +703,10 @@ __device__ __forceinline__ void mur_zwall_v4(const GridDev& g, const MurDev& m, 
 // The blocks after them take one direct column's z-wall group per thread (mur_zwall_v4).  The
 // wall work thus sits in warps of its own, and the streaming warps keep k_update_v4's registers
 // and loads in flight.
-template <typename IX = unsigned>
+// PARK: the direct columns' z-wall groups are updated like every other group (their hooks are
+// k_mur_zsave / k_mur_zpost around this launch), so the streaming blocks carry no wall test and
+// there are no wall blocks.
+template <typename IX = unsigned, bool PARK = false>
 __global__ void __launch_bounds__(256, 4) k_update_v4w(GridDev g, MurDev m, const unsigned* __restrict__ numTS,
                                                        unsigned interior)
 {
@@ -712,10 +720,11 @@ __global__ void __launch_bounds__(256, 4) k_update_v4w(GridDev g, MurDev m, cons
             mur_wall_v4<IX>(g, m, __ldg(numTS), x, y, z0);
             return;
         }
-        if (mur_z_group(m, z0) >= 0) return;
+        if (!PARK && mur_z_group(m, z0) >= 0) return;
         update_v4_cells<IX>(g, x, y, z0);
         return;
     }
+    if (PARK) return;
     const unsigned t = (blockIdx.x - interior) * blockDim.x + threadIdx.x;
     const unsigned nz = (unsigned)m.nz;
     const unsigned y = t / nz, q = t - y * nz;
@@ -1155,6 +1164,54 @@ static __global__ void k_lumped_rlc(float* __restrict__ V, RlcDev r, const unsig
     r.j[s0 * n + k] = fsub(fsub(fmul(ib0, fsub(vd0, vd2)), fmul(fmul(b1, ib0), j1)), fmul(fmul(b2, ib0), j2));
     r.vd[s0 * n + k] = vd0;
     V[o] = vd0;
+}
+
+// The z walls' hooks of the direct columns in park mode, around the voltage update: one thread per
+// (wall, column), consecutive threads on consecutive y, so the coefficient tables and the saved
+// values are read and written coalesced (the field values sit one per z row).  The reference's
+// pre-voltage hook and post-voltage hook with the apply folded in
+// (FDTD/extensions/engine_ext_mur_abc.cpp:83-178):
+//   k_mur_zsave (before): pre = V_old(shift) - cP * V_old(line), per tangential component;
+//   k_mur_zpost (after):  V(line) = pre + cP * V_new(shift).
+// The same values and operation order as the shift-lane form inside the update (mur_z_shift).
+__device__ __forceinline__ bool mur_zpark_item(const GridDev& g, const MurDev& m, unsigned t, unsigned& k,
+                                               unsigned& q, unsigned long long& ol, unsigned long long& os)
+{
+    const unsigned nn = g.Nx * g.Ny;
+    q = t / nn;
+    if (q >= (unsigned)m.nz) return false;
+    k = t - q * nn;
+    const unsigned x = k / g.Ny, y = k - x * g.Ny;
+    if (!mur_z_direct(m, x, y)) return false;              // x/y wall columns: the update's own hooks
+    const MurWallDev& W = q ? m.z[1] : m.z[0];
+    const unsigned long long row = (unsigned long long)k * g.Pz;
+    ol = row + W.line;
+    os = row + W.shift;
+    return true;
+}
+
+static __global__ void k_mur_zsave(GridDev g, MurDev m)
+{
+    unsigned k, q;
+    unsigned long long ol, os;
+    if (!mur_zpark_item(g, m, blockIdx.x * blockDim.x + threadIdx.x, k, q, ol, os)) return;
+    const MurWallDev& W = q ? m.z[1] : m.z[0];
+    const unsigned nn = g.Nx * g.Ny;
+    float* sv = m.zsave + (size_t)q * 2 * nn;
+    sv[k] = fsub(g.V[os], fmul(__ldg(W.cP + k), g.V[ol]));
+    sv[nn + k] = fsub(g.V[g.S + os], fmul(__ldg(W.cPP + k), g.V[g.S + ol]));
+}
+
+static __global__ void k_mur_zpost(GridDev g, MurDev m)
+{
+    unsigned k, q;
+    unsigned long long ol, os;
+    if (!mur_zpark_item(g, m, blockIdx.x * blockDim.x + threadIdx.x, k, q, ol, os)) return;
+    const MurWallDev& W = q ? m.z[1] : m.z[0];
+    const unsigned nn = g.Nx * g.Ny;
+    const float* sv = m.zsave + (size_t)q * 2 * nn;
+    g.V[ol] = fadd(sv[k], fmul(__ldg(W.cP + k), g.V[os]));
+    g.V[g.S + ol] = fadd(sv[nn + k], fmul(__ldg(W.cPP + k), g.V[g.S + os]));
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -142,11 +142,14 @@ def test_march_autotune_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn
     assert not bad, (name, bad)
 
 
-def test_mur_float4_inner_z_walls_bit_exact_against_oracle(cuda_lib):
+@pytest.mark.parametrize("park", ["1", "0"])
+def test_mur_float4_inner_z_walls_bit_exact_against_oracle(cuda_lib, monkeypatch, park):
     """k_update_v4w with z walls away from the row ends (lines 4 / 27 of 30, each with its shift in
     the same group of four): the wall groups sit inside the rows, between streaming groups.  The
-    walls are placed by hand, which the oracle models the same way."""
+    walls are placed by hand, which the oracle models the same way.  park = 1: the direct columns'
+    z-wall hooks as k_mur_zsave / k_mur_zpost around the update; park = 0: inside it."""
     import dataclasses
+    monkeypatch.setenv("OEMS_CUDA_MUR_PARK", park)
     op = configs.stress(shape=(40, 36, 30), steps=140, nblocks=16)
     walls = []
     for w in op.mur:
@@ -156,7 +159,7 @@ def test_mur_float4_inner_z_walls_bit_exact_against_oracle(cuda_lib):
         walls.append(w)
     op.mur = walls
     g, r = _run_pair(op, 140, chunks=(1, 7, 16, 33))
-    assert g.update_kernels()[0] == "k_update_v4w"
+    assert g.update_kernels()[0] == ("k_update_v4w<park>" if park == "1" else "k_update_v4w")
     res = compare_engines(g, r)
     bad = [k for k, v in res.items() if not v]
     assert not bad, bad
