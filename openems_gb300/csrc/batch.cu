@@ -441,7 +441,8 @@ int capture_concurrent(oems_cuda_batch* b, const std::vector<int>& act, unsigned
     for (size_t i = 0; i < act.size() && rc == OEMS_OK; ++i) {
         oems_cuda_engine* e = b->eng[act[i]];
         if (cudaStreamWaitEvent(e->stream, fork, 0) != cudaSuccess) { rc = OEMS_ERR_CUDA; break; }
-        for (unsigned s = 0; s < steps && rc == OEMS_OK; ++s) rc = enqueue_step(e, nullptr);
+        for (unsigned s = 0; s < steps && rc == OEMS_OK; ++s)
+            rc = enqueue_step(e, nullptr, nullptr, (s == 0 ? 1u : 0u) | (s + 1 == steps ? 2u : 0u));
         if (rc == OEMS_OK && (cudaEventRecord(join[i], e->stream) != cudaSuccess ||
                               cudaStreamWaitEvent(b->stream, join[i], 0) != cudaSuccess))
             rc = OEMS_ERR_CUDA;

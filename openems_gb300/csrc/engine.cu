@@ -20,6 +20,8 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "engine_impl.h"
@@ -794,8 +796,14 @@ int enqueue_fused_step(oems_cuda_engine* e, int parity, unsigned* nlaunch)
     return OEMS_OK;
 }
 
-int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
+int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof, unsigned seq)
 {
+    // seq bit 0: first step of the enqueued sequence, bit 1: last.  Inside a sequence the
+    // dispersive apply of one step and the pre of the next run as one k_lorentz_carry launch at
+    // the end of the half-step; a sequence starts with the plain pre and ends with the plain
+    // apply, so between sequences the ADE state is the reference's.
+    const bool carry_v = e->lor_carry_v && !(seq & 2), pre_v = !e->lor_carry_v || (seq & 1);
+    const bool carry_i = e->lor_carry_i && !(seq & 2), pre_i = !e->lor_carry_i || (seq & 1);
     const GridDev& g = e->grid;
     const dim3 blk(256);
     unsigned L = 0;
@@ -808,7 +816,8 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
         if (prof && prof->n < 64) { cudaEventRecord(prof->ev[2 * prof->n + 1], s); ++prof->n; }
     };
     // ---- voltages
-    for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
+    if (pre_v)
+        for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
     unsigned mur_pts = 0;
     for (const auto& m : e->mur) mur_pts = std::max<unsigned>(mur_pts, (unsigned)m.cP.size());
     const dim3 mur_grid((mur_pts + 255) / 256, (unsigned)e->mur.size());
@@ -843,11 +852,15 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
         k_lumped_rlc<<<(e->rlc.count + 127) / 128, 128, 0, s>>>(e->dV, e->rlc, e->d_numTS);
         post(); ++L;
     }
-    for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
+    if (!carry_v)
+        for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
     if (!e->mur.empty()) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 2, e->d_numTS); post(); ++L; }
     if (e->excV.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excV.count + 127) / 128, 128, 0, s>>>(e->dV, e->excV, e->d_numTS); post(); ++L; }
+    if (carry_v)
+        for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_carry<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
     // ---- currents
-    for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
+    if (pre_i)
+        for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
     pre(OEMS_KC_UPDATE_I);
     launch_update(e, true, s);
     post();
@@ -862,8 +875,11 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof)
         k_tfsf<<<(e->tfsfI.ntarget + 255) / 256, blk, 0, s>>>(e->dI, e->tfsfI, e->d_numTS);
         post(); ++L;
     }
-    for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
+    if (!carry_i)
+        for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
     if (e->excI.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excI.count + 127) / 128, 128, 0, s>>>(e->dI, e->excI, e->d_numTS); post(); ++L; }
+    if (carry_i)
+        for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_carry<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
     // ---- processing + numTS
     pre(OEMS_KC_STEP_END);
     k_step_end<<<e->stepend_blocks, blk, 0, s>>>(g, e->stepend); ++L;
@@ -1003,9 +1019,13 @@ static int capture(oems_cuda_engine* e, unsigned steps, cudaGraphExec_t* out, bo
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     int rc = OEMS_OK;
-    for (unsigned s = 0; s < steps && rc == OEMS_OK; ++s)
+    for (unsigned s = 0; s < steps && rc == OEMS_OK; ++s) {
+        const unsigned seq = (s == 0 ? 1u : 0u) | (s + 1 == steps ? 2u : 0u);
+        // launches per step: a step inside the sequence where there is one
+        const bool count = s == (steps > 2 ? 1u : 0u);
         rc = fused ? enqueue_fused_step(e, (int)(s & 1), s == 0 ? &e->fused_launches : nullptr)
-                   : enqueue_step(e, s == 0 ? &e->launches : nullptr);
+                   : enqueue_step(e, count ? &e->launches : nullptr, nullptr, seq);
+    }
     cudaError_t c = cudaStreamEndCapture(e->stream, &graph);
     if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
     if (c != cudaSuccess) return cuda_fail(e, c, "cudaStreamEndCapture");
@@ -1251,15 +1271,72 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     }
 
     // Lorentz / Drude orders
+    std::unordered_set<unsigned long long> exc_v(e->exc_voff.begin(), e->exc_voff.end());
+    std::unordered_set<unsigned long long> exc_i(e->exc_ioff.begin(), e->exc_ioff.end());
+    {
+        const char* lc = getenv("OEMS_CUDA_LOR_CARRY");
+        const bool on = !(lc && lc[0] == '0');
+        // the carried apply moves past the Mur apply: only where the walls' components are in skip.
+        // One order only: a position in two orders takes both applies before either pre.
+        const bool one = e->lor.size() <= 1;
+        e->lor_carry_v = on && one && (e->mur.empty() || e->murdev.lanes);
+        e->lor_carry_i = on && one;
+    }
     for (const auto& l : e->lor) {
         std::vector<unsigned long long> off(l.count);
         for (unsigned i = 0; i < l.count; ++i) off[i] = cell_off(e, 0, l.pos[i], l.pos[l.count + i], l.pos[2 * l.count + i]);
+        // 32-bit offsets when every component's offset fits
+        const bool o32 = 3ull * e->S < (1ull << 32);
         unsigned long long* doff = nullptr;
-        if ((rc = dupload(e, &doff, off.data(), off.size()))) return rc;
+        unsigned* doff32 = nullptr;
+        if (o32) {
+            std::vector<unsigned> o(off.begin(), off.end());
+            if ((rc = dupload(e, &doff32, o.data(), o.size()))) return rc;
+        } else if ((rc = dupload(e, &doff, off.data(), off.size()))) return rc;
+        // an excitation edge among the positions' components keeps the apply in its own place
+        for (unsigned i = 0; i < l.count; ++i)
+            for (unsigned n = 0; n < 3; ++n) {
+                if (l.von && exc_v.count(off[i] + n * e->S)) e->lor_carry_v = false;
+                if (l.con && exc_i.count(off[i] + n * e->S)) e->lor_carry_i = false;
+            }
         const size_t m = 3 * (size_t)l.count;
+        // coefficient classes: each position's nine coefficients (int, ext, lor per component)
+        // as an index into a table of distinct tuples, bit-exact (keys are the float bits)
+        auto classes = [&](const std::vector<float>& ci, const std::vector<float>& ce, const std::vector<float>& cl,
+                           bool lor, LorDev& d) -> int {
+            std::unordered_map<std::string, unsigned> seen;
+            std::vector<unsigned short> cls(l.count);
+            std::vector<float> tab;
+            std::string key(36, '\0');
+            for (unsigned i = 0; i < l.count; ++i) {
+                float t[9];
+                for (unsigned n = 0; n < 3; ++n) {
+                    t[n] = ci[n * l.count + i];
+                    t[3 + n] = ce[n * l.count + i];
+                    t[6 + n] = lor ? cl[n * l.count + i] : 0.f;
+                }
+                memcpy(&key[0], t, 36);
+                auto it = seen.find(key);
+                if (it == seen.end()) {
+                    if (seen.size() >= 65536) return OEMS_OK;         // too many: raw arrays
+                    it = seen.emplace(key, (unsigned)seen.size()).first;
+                    tab.insert(tab.end(), t, t + 9);
+                    tab.insert(tab.end(), 3, 0.f);
+                }
+                cls[i] = (unsigned short)it->second;
+            }
+            unsigned short* dc = nullptr;
+            float* dt = nullptr;
+            int r2;
+            if ((r2 = dupload(e, &dc, cls.data(), cls.size()))) return r2;
+            if ((r2 = dupload(e, &dt, tab.data(), tab.size()))) return r2;
+            d.cls = dc;
+            d.ctab = reinterpret_cast<const float4*>(dt);
+            return OEMS_OK;
+        };
         if (l.von) {
             LorDev d{};
-            d.count = l.count; d.off = doff; d.lor = l.vlon;
+            d.count = l.count; d.off = doff; d.off32 = doff32; d.lor = l.vlon;
             if (e->murdev.lanes) {
                 // the voltage update writes final Mur values: the apply leaves every component an
                 // (always active) wall owns alone, as the reference's later Mur apply overwrites it
@@ -1275,23 +1352,29 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
                 if (any && (rc = dupload(e, &dsk, sk.data(), sk.size()))) return rc;
                 d.skip = dsk;
             }
-            float *ci, *ce, *cl = nullptr;
-            if ((rc = dupload(e, &ci, l.vint.data(), m))) return rc;
-            if ((rc = dupload(e, &ce, l.vext.data(), m))) return rc;
-            if (l.vlon && (rc = dupload(e, &cl, l.vlor.data(), m))) return rc;
-            d.c_int = ci; d.c_ext = ce; d.c_lor = cl;
+            if ((rc = classes(l.vint, l.vext, l.vlor, l.vlon, d))) return rc;
+            if (!d.cls) {
+                float *ci, *ce, *cl = nullptr;
+                if ((rc = dupload(e, &ci, l.vint.data(), m))) return rc;
+                if ((rc = dupload(e, &ce, l.vext.data(), m))) return rc;
+                if (l.vlon && (rc = dupload(e, &cl, l.vlor.data(), m))) return rc;
+                d.c_int = ci; d.c_ext = ce; d.c_lor = cl;
+            }
             if ((rc = dalloc(e, &d.ade, m, true, true))) return rc;
             if (l.vlon && (rc = dalloc(e, &d.lade, m, true, true))) return rc;
             e->lorV.push_back(d);
         }
         if (l.con) {
             LorDev d{};
-            d.count = l.count; d.off = doff; d.lor = l.clon;
-            float *ci, *ce, *cl = nullptr;
-            if ((rc = dupload(e, &ci, l.iint.data(), m))) return rc;
-            if ((rc = dupload(e, &ce, l.iext.data(), m))) return rc;
-            if (l.clon && (rc = dupload(e, &cl, l.ilor.data(), m))) return rc;
-            d.c_int = ci; d.c_ext = ce; d.c_lor = cl;
+            d.count = l.count; d.off = doff; d.off32 = doff32; d.lor = l.clon;
+            if ((rc = classes(l.iint, l.iext, l.ilor, l.clon, d))) return rc;
+            if (!d.cls) {
+                float *ci, *ce, *cl = nullptr;
+                if ((rc = dupload(e, &ci, l.iint.data(), m))) return rc;
+                if ((rc = dupload(e, &ce, l.iext.data(), m))) return rc;
+                if (l.clon && (rc = dupload(e, &cl, l.ilor.data(), m))) return rc;
+                d.c_int = ci; d.c_ext = ce; d.c_lor = cl;
+            }
             if ((rc = dalloc(e, &d.ade, m, true, true))) return rc;
             if (l.clon && (rc = dalloc(e, &d.lade, m, true, true))) return rc;
             e->lorI.push_back(d);
@@ -1600,7 +1683,7 @@ int oems_cuda_profile_steps(oems_cuda_engine* e, unsigned int n, float* ms, unsi
     int rc = OEMS_OK;
     for (unsigned st = 0; st < n && rc == OEMS_OK; ++st) {
         prof.n = 0;
-        rc = enqueue_step(e, nullptr, &prof);
+        rc = enqueue_step(e, nullptr, &prof, (st == 0 ? 1u : 0u) | (st + 1 == n ? 2u : 0u));
         if (rc) break;
         ++e->host_numTS;
         cudaError_t c = cudaEventSynchronize(prof.ev[2 * prof.n - 1]);

@@ -171,6 +171,8 @@ struct oems_cuda_engine {
     bool vec4 = true;
     // the voltage update with the Mur hooks in the float4 form (k_update_v4w)
     bool mur_v4 = false;
+    // dispersive apply + next pre as one launch inside enqueued sequences (k_lorentz_carry)
+    bool lor_carry_v = false, lor_carry_i = false;
 
     // one-kernel step (the plane march, march.cuh): the K-step graph alternates buffer sets A
     // (dV, dI) and B (dV2, dI2); K is even, so the state is in A whenever the host sees it
@@ -220,4 +222,4 @@ struct StepProfiler {
 };
 
 // enqueue one timestep of `e` on e->stream (defined in engine.cu)
-int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof = nullptr);
+int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof = nullptr, unsigned seq = 3);

@@ -1275,49 +1275,123 @@ static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __r
 struct LorDev {
     unsigned count;
     const unsigned char* skip;       // optional: bit n set = the apply leaves component n alone
-    const unsigned long long* off;   // field offset of component 0 at each position
+    const unsigned long long* off;   // field offset of component 0 at each position (or off32)
+    const unsigned* off32;           // the same in 32 bits when every offset fits (off is null)
     int lor;                         // Lorentz pole term on
-    const float* c_int;              // [3][count]
+    const float* c_int;              // [3][count] (null when cls is set)
     const float* c_ext;
     const float* c_lor;
+    const unsigned short* cls;       // per position: coefficient class, or null
+    const float4* ctab;              // [class][3]: int 0..2, ext 0..2, lor 0..2, pad
     float* ade;                      // [3][count]
     float* lade;
 };
+
+__device__ __forceinline__ unsigned long long lor_off(const LorDev& l, unsigned i)
+{
+    return l.off32 ? (unsigned long long)__ldg(l.off32 + i) : __ldg(l.off + i);
+}
+
+// the position's coefficients of component n: int, ext, lor
+struct LorCoef {
+    float ci[3], ce[3], cl[3];
+};
+__device__ __forceinline__ LorCoef lor_coef(const LorDev& l, unsigned i)
+{
+    LorCoef c;
+    if (l.cls) {
+        const float4* t = l.ctab + 3u * __ldg(l.cls + i);
+        const float4 a = __ldg(t), b = __ldg(t + 1), d = __ldg(t + 2);
+        c.ci[0] = a.x; c.ci[1] = a.y; c.ci[2] = a.z;
+        c.ce[0] = a.w; c.ce[1] = b.x; c.ce[2] = b.y;
+        c.cl[0] = b.z; c.cl[1] = b.w; c.cl[2] = d.x;
+    } else {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const unsigned k = n * l.count + i;
+            c.ci[n] = __ldg(l.c_int + k);
+            c.ce[n] = __ldg(l.c_ext + k);
+            c.cl[n] = l.lor ? __ldg(l.c_lor + k) : 0.f;
+        }
+    }
+    return c;
+}
+
+// the pre hook of one component: the ADE current from the field before the update (a the ADE
+// value, la the pole term's, f the field value); returns the new ADE value, la updated in place
+__device__ __forceinline__ float lor_pre_one(const LorDev& l, const LorCoef& c, int n, float a, float& la, float f)
+{
+    if (l.lor) {
+        la = fadd(la, fmul(c.cl[n], a));
+        a = fmul(a, c.ci[n]);
+        return fadd(a, fmul(c.ce[n], fsub(f, la)));
+    }
+    a = fmul(a, c.ci[n]);
+    return fadd(a, fmul(c.ce[n], f));
+}
 
 static __global__ void k_lorentz_pre(const float* __restrict__ F, unsigned long long S, LorDev l)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= l.count) return;
-    const unsigned long long o = l.off[i];
+    const unsigned long long o = lor_off(l, i);
+    const LorCoef c = lor_coef(l, i);
+    float f[3], a[3], la[3];
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
-        const unsigned k = n * l.count + i;
-        const float f = F[o + n * S];
-        float a = l.ade[k];
-        if (l.lor) {
-            const float la = fadd(l.lade[k], fmul(l.c_lor[k], a));
-            l.lade[k] = la;
-            a = fmul(a, l.c_int[k]);
-            a = fadd(a, fmul(l.c_ext[k], fsub(f, la)));
-        } else {
-            a = fmul(a, l.c_int[k]);
-            a = fadd(a, fmul(l.c_ext[k], f));
-        }
-        l.ade[k] = a;
+        f[n] = F[o + n * S];
+        a[n] = l.ade[n * l.count + i];
+        la[n] = l.lor ? l.lade[n * l.count + i] : 0.f;
+    }
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        l.ade[n * l.count + i] = lor_pre_one(l, c, n, a[n], la[n], f[n]);
+        if (l.lor) l.lade[n * l.count + i] = la[n];
     }
 }
 
+// the apply hook: F -= ade
 static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long S, LorDev l)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= l.count) return;
-    const unsigned long long o = l.off[i];
+    const unsigned long long o = lor_off(l, i);
     const unsigned sk = l.skip ? l.skip[i] : 0u;
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
         if (sk & (1u << n)) continue;
         const unsigned long long q = o + n * S;
         F[q] = fsub(F[q], l.ade[n * l.count + i]);
+    }
+}
+
+// This step's apply and the next step's pre in one pass, launched at the end of the field's
+// half-step (after every later apply hook: the host allows it only where no excitation edge is a
+// position's component and the Mur walls' components are in skip).  Between the two nothing
+// else writes the field at these positions, so the pre reads the same values as it would at the
+// start of the next half-step; the ADE values stay in registers between them.
+static __global__ void k_lorentz_carry(float* __restrict__ F, unsigned long long S, LorDev l)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= l.count) return;
+    const unsigned long long o = lor_off(l, i);
+    const unsigned sk = l.skip ? l.skip[i] : 0u;
+    const LorCoef c = lor_coef(l, i);
+    float f[3], a[3], la[3];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        f[n] = F[o + n * S];
+        a[n] = l.ade[n * l.count + i];
+        la[n] = l.lor ? l.lade[n * l.count + i] : 0.f;
+    }
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        if (!(sk & (1u << n))) {
+            f[n] = fsub(f[n], a[n]);
+            F[o + n * S] = f[n];
+        }
+        l.ade[n * l.count + i] = lor_pre_one(l, c, n, a[n], la[n], f[n]);
+        if (l.lor) l.lade[n * l.count + i] = la[n];
     }
 }
 

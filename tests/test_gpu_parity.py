@@ -118,6 +118,7 @@ def test_separate_mur_hooks_bit_exact_against_oracle(cuda_lib, monkeypatch, name
     """The Mur pre/post hooks as separate launches (OEMS_CUDA_MUR_SEPARATE=1) instead of inside
     the voltage update: the same fields, bit for bit, with two more launches per step."""
     op = fn()
+    monkeypatch.setenv("OEMS_CUDA_LOR_CARRY", "0")     # separate Mur hooks keep the dispersive apply apart
     fused = Engine_CUDA(op, steps)
     n_fused = fused.launches_per_step()
     fused.close()
@@ -163,6 +164,32 @@ def test_mur_float4_inner_z_walls_bit_exact_against_oracle(cuda_lib, monkeypatch
     res = compare_engines(g, r)
     bad = [k for k, v in res.items() if not v]
     assert not bad, bad
+
+
+@pytest.mark.parametrize("seed", [20261204, 3])
+@pytest.mark.parametrize("carry", ["1", "0"])
+def test_lorentz_carry_bit_exact_against_oracle(cuda_lib, monkeypatch, carry, seed):
+    """Inside a captured sequence the dispersive apply of one step and the pre of the next run as
+    one launch at the end of the half-step (k_lorentz_carry); OEMS_CUDA_LOR_CARRY=0 keeps them
+    apart.  Either way, over mixed chunk lengths, the fields, probes and dumps equal the oracle's
+    bit for bit.  The carried form has one launch less per step inside a sequence, except where a
+    source edge lies on a dispersive position (seed 20261204: its excitation must follow the
+    apply, so the apply keeps its place)."""
+    monkeypatch.setenv("OEMS_CUDA_LOR_CARRY", carry)
+    op = configs.stress(shape=(40, 36, 30), steps=150, nblocks=16, seed=seed)
+    assert len(op.lorentz) == 1
+    pos = set(map(tuple, np.asarray(op.lorentz[0].pos).T.tolist()))
+    src_on_lor = any(tuple(p) in pos for p in np.asarray(op.exc.volt_index).T.tolist())
+    assert src_on_lor == (seed == 20261204)
+    g, r = _run_pair(op, 150, chunks=(1, 7, 16, 33))
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, bad
+    monkeypatch.setenv("OEMS_CUDA_LOR_CARRY", "0")
+    plain = Engine_CUDA(op, 10)
+    n_plain = plain.launches_per_step()
+    plain.close()
+    assert g.launches_per_step() == n_plain - (1 if carry == "1" and not src_on_lor else 0)
 
 
 REG4_CASES = [
