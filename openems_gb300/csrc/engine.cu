@@ -21,7 +21,6 @@
 #include <memory>
 #include <string>
 #include <unordered_map>
-#include <unordered_set>
 #include <vector>
 
 #include "engine_impl.h"
@@ -852,12 +851,23 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof, uns
         k_lumped_rlc<<<(e->rlc.count + 127) / 128, 128, 0, s>>>(e->dV, e->rlc, e->d_numTS);
         post(); ++L;
     }
-    if (!carry_v)
-        for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
-    if (!e->mur.empty()) { pre(OEMS_KC_MUR); k_mur<<<mur_grid, blk, 0, s>>>(g, e->murdev, 2, e->d_numTS); post(); ++L; }
-    if (e->excV.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excV.count + 127) / 128, 128, 0, s>>>(e->dV, e->excV, e->d_numTS); post(); ++L; }
-    if (carry_v)
-        for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_carry<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
+    const unsigned mur_blocks = e->mur.empty() ? 0u : e->murdev.afirst[e->murdev.nwall];
+    if (carry_v && e->vtail) {
+        // Mur apply, dispersive carry and excitation in one launch
+        const LorDev& l = e->lorV[0];
+        const unsigned lor0 = mur_blocks, exc0 = lor0 + (l.count + 255) / 256;
+        const unsigned blocks = exc0 + (e->excV.count + 255) / 256;
+        pre(OEMS_KC_LORENTZ);
+        k_vtail<<<blocks, blk, 0, s>>>(g, e->murdev, l, e->excV, e->d_numTS, lor0, exc0);
+        post(); ++L;
+    } else {
+        if (!carry_v)
+            for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_apply<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
+        if (mur_blocks) { pre(OEMS_KC_MUR); k_mur_apply<<<mur_blocks, blk, 0, s>>>(g, e->murdev, e->d_numTS); post(); ++L; }
+        if (e->excV.count) { pre(OEMS_KC_EXCITE); k_excitation<<<(e->excV.count + 127) / 128, 128, 0, s>>>(e->dV, e->excV, e->d_numTS); post(); ++L; }
+        if (carry_v)
+            for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_carry<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
+    }
     // ---- currents
     if (pre_i)
         for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
@@ -1128,8 +1138,20 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         d.line = m.line; d.shift = m.shift; d.start_ts = m.start_ts;
         d.n1 = e->N[d.nyP]; d.n2 = e->N[d.nyPP];
         float *cp, *cpp;
-        if ((rc = dupload(e, &cp, m.cP.data(), m.cP.size()))) return rc;
-        if ((rc = dupload(e, &cpp, m.cPP.data(), m.cPP.size()))) return rc;
+        if (d.nyP == 2) {
+            // tables with z tangential go up z fastest ([n2][n1], mur_k)
+            std::vector<float> tP(m.cP.size()), tPP(m.cPP.size());
+            for (unsigned i = 0; i < d.n1; ++i)
+                for (unsigned j = 0; j < d.n2; ++j) {
+                    tP[(size_t)j * d.n1 + i] = m.cP[(size_t)i * d.n2 + j];
+                    tPP[(size_t)j * d.n1 + i] = m.cPP[(size_t)i * d.n2 + j];
+                }
+            if ((rc = dupload(e, &cp, tP.data(), tP.size()))) return rc;
+            if ((rc = dupload(e, &cpp, tPP.data(), tPP.size()))) return rc;
+        } else {
+            if ((rc = dupload(e, &cp, m.cP.data(), m.cP.size()))) return rc;
+            if ((rc = dupload(e, &cpp, m.cPP.data(), m.cPP.size()))) return rc;
+        }
         d.cP = cp; d.cPP = cpp;
         if ((rc = dalloc(e, &d.bP, m.cP.size(), true, true))) return rc;
         if ((rc = dalloc(e, &d.bPP, m.cP.size(), true, true))) return rc;
@@ -1199,6 +1221,28 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         md.park = (e->mur_v4 && md.nz > 0 && mp && mp[0] == '1') ? 1 : 0;
         md.zsave = nullptr;
         if (md.park && (rc = dalloc(e, &md.zsave, 2 * (size_t)md.nz * e->N[0] * e->N[1], true))) return rc;
+        // the flat apply: with the lane-parallel form a z wall's apply visits only the columns
+        // that are not direct (the update stores the direct ones' final values)
+        md.zedge = nullptr;
+        md.nzedge = 0;
+        if (md.lanes && md.first[3] > md.first[2]) {
+            std::vector<unsigned> edge;
+            for (unsigned x = 0; x < e->N[0]; ++x)
+                for (unsigned y = 0; y < e->N[1]; ++y) {
+                    const bool direct = (x - md.lo[0] <= md.span[0]) && (y - md.lo[1] <= md.span[1]);
+                    if (!direct) edge.push_back(x * e->N[1] + y);
+                }
+            md.nzedge = (unsigned)edge.size();
+            unsigned* de = nullptr;
+            if (!edge.empty() && (rc = dupload(e, &de, edge.data(), edge.size()))) return rc;
+            md.zedge = de;
+        }
+        md.afirst[0] = 0;
+        for (int w = 0; w < md.nwall; ++w) {
+            const MurWallDev& d = md.w[w];
+            const unsigned pts = (md.lanes && d.ny == 2 && md.zedge) ? md.nzedge : d.n1 * d.n2;
+            md.afirst[w + 1] = md.afirst[w] + (pts + 255) / 256;
+        }
     }
 
     // cylinder extension
@@ -1271,8 +1315,14 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     }
 
     // Lorentz / Drude orders
-    std::unordered_set<unsigned long long> exc_v(e->exc_voff.begin(), e->exc_voff.end());
-    std::unordered_set<unsigned long long> exc_i(e->exc_ioff.begin(), e->exc_ioff.end());
+    // the cells (component 0 offsets) of the excitation edges, sorted
+    auto exc_cells = [&](const std::vector<unsigned long long>& off) {
+        std::vector<unsigned long long> c;
+        for (auto o : off) c.push_back(o % e->S);
+        std::sort(c.begin(), c.end());
+        return c;
+    };
+    const std::vector<unsigned long long> exc_v = exc_cells(e->exc_voff), exc_i = exc_cells(e->exc_ioff);
     {
         const char* lc = getenv("OEMS_CUDA_LOR_CARRY");
         const bool on = !(lc && lc[0] == '0');
@@ -1294,20 +1344,21 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
             if ((rc = dupload(e, &doff32, o.data(), o.size()))) return rc;
         } else if ((rc = dupload(e, &doff, off.data(), off.size()))) return rc;
         // an excitation edge among the positions' components keeps the apply in its own place
-        for (unsigned i = 0; i < l.count; ++i)
-            for (unsigned n = 0; n < 3; ++n) {
-                if (l.von && exc_v.count(off[i] + n * e->S)) e->lor_carry_v = false;
-                if (l.con && exc_i.count(off[i] + n * e->S)) e->lor_carry_i = false;
-            }
+        for (unsigned i = 0; i < l.count; ++i) {
+            if (l.von && !exc_v.empty() && std::binary_search(exc_v.begin(), exc_v.end(), off[i])) e->lor_carry_v = false;
+            if (l.con && !exc_i.empty() && std::binary_search(exc_i.begin(), exc_i.end(), off[i])) e->lor_carry_i = false;
+        }
         const size_t m = 3 * (size_t)l.count;
         // coefficient classes: each position's nine coefficients (int, ext, lor per component)
         // as an index into a table of distinct tuples, bit-exact (keys are the float bits)
         auto classes = [&](const std::vector<float>& ci, const std::vector<float>& ce, const std::vector<float>& cl,
                            bool lor, LorDev& d) -> int {
-            std::unordered_map<std::string, unsigned> seen;
             std::vector<unsigned short> cls(l.count);
-            std::vector<float> tab;
-            std::string key(36, '\0');
+            std::vector<float> tab;                                // 12 floats per class
+            std::vector<int> slot(1u << 17, -1);                   // open addressing over class ids
+            unsigned ncls = 0;
+            uint32_t prev[9];
+            int prev_c = -1;
             for (unsigned i = 0; i < l.count; ++i) {
                 float t[9];
                 for (unsigned n = 0; n < 3; ++n) {
@@ -1315,15 +1366,28 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
                     t[3 + n] = ce[n * l.count + i];
                     t[6 + n] = lor ? cl[n * l.count + i] : 0.f;
                 }
-                memcpy(&key[0], t, 36);
-                auto it = seen.find(key);
-                if (it == seen.end()) {
-                    if (seen.size() >= 65536) return OEMS_OK;         // too many: raw arrays
-                    it = seen.emplace(key, (unsigned)seen.size()).first;
+                uint32_t w[9];
+                memcpy(w, t, sizeof w);
+                if (prev_c >= 0 && !memcmp(w, prev, sizeof w)) { cls[i] = (unsigned short)prev_c; continue; }
+                uint64_t h = 1469598103934665603ull;
+                for (int k = 0; k < 9; ++k) h = (h ^ w[k]) * 1099511628211ull;
+                const size_t mask = slot.size() - 1;
+                size_t q = (size_t)(h ^ (h >> 29)) & mask;
+                int c = -1;
+                while (slot[q] >= 0) {
+                    if (!memcmp(&tab[12 * (size_t)slot[q]], t, sizeof t)) { c = slot[q]; break; }
+                    q = (q + 1) & mask;
+                }
+                if (c < 0) {
+                    if (ncls >= 65536 || 2 * (ncls + 1) > slot.size()) return OEMS_OK;   // too many: raw arrays
+                    c = (int)ncls++;
+                    slot[q] = c;
                     tab.insert(tab.end(), t, t + 9);
                     tab.insert(tab.end(), 3, 0.f);
                 }
-                cls[i] = (unsigned short)it->second;
+                cls[i] = (unsigned short)c;
+                memcpy(prev, w, sizeof w);
+                prev_c = c;
             }
             unsigned short* dc = nullptr;
             float* dt = nullptr;
@@ -1379,6 +1443,23 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
             if (l.clon && (rc = dalloc(e, &d.lade, m, true, true))) return rc;
             e->lorI.push_back(d);
         }
+    }
+
+    // the voltage half-step's end as one launch inside sequences (k_vtail): the Mur apply, the
+    // dispersive carry and the excitation touch disjoint values
+    e->vtail = false;
+    if (e->lor_carry_v && e->lorV.size() == 1 && !e->lorV[0].skip) {
+        bool ok = true;
+        const unsigned long long plane = (unsigned long long)e->N[1] * e->Pz;
+        for (auto o : e->exc_voff) {
+            const unsigned n = (unsigned)(o / e->S);
+            const unsigned long long c = o % e->S;
+            const unsigned p[3] = {(unsigned)(c / plane), (unsigned)((c / e->Pz) % e->N[1]), (unsigned)(c % e->Pz)};
+            for (const auto& w : e->mur)
+                if (p[w.ny] == w.line && (int)n != w.ny) ok = false;
+        }
+        const char* vt = getenv("OEMS_CUDA_VTAIL");
+        e->vtail = ok && !(vt && vt[0] == '0');
     }
 
     // probes: term lists in the reference's summation order + phasor tables

@@ -173,6 +173,7 @@ struct oems_cuda_engine {
     bool mur_v4 = false;
     // dispersive apply + next pre as one launch inside enqueued sequences (k_lorentz_carry)
     bool lor_carry_v = false, lor_carry_i = false;
+    bool vtail = false;              // k_vtail: Mur apply + carry + excitation as one launch
 
     // one-kernel step (the plane march, march.cuh): the K-step graph alternates buffer sets A
     // (dV, dI) and B (dV2, dI2); K is even, so the state is in A whenever the host sees it

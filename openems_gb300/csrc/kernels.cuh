@@ -96,8 +96,8 @@ __device__ __forceinline__ int upml_find(const GridDev& g, unsigned x, unsigned 
 }
 
 // Mur walls (FDTD/extensions/engine_ext_mur_abc.cpp:83-178): wall w updates the two tangential
-// components on mesh line `line` of axis ny from the neighbouring line `shift`; the tables and
-// the wall buffers bP/bPP are indexed k = pos[nyP] * n2 + pos[nyPP].
+// components on mesh line `line` of axis ny from the neighbouring line `shift`; the wall
+// buffers bP/bPP and tables cP/cPP are indexed k = mur_k(pos[nyP], pos[nyPP]).
 struct MurWallDev {
     int ny, nyP, nyPP;
     unsigned line, shift, start_ts, n1, n2;
@@ -125,6 +125,12 @@ struct MurDev {
     // holds [nz][2][Nx*Ny]: the pre-update Mur value of tangential components 0 and 1
     int park;
     float* zsave;
+    // the apply as one flat launch (k_mur_apply, k_vtail): wall wi's points are the blocks
+    // [afirst[wi], afirst[wi + 1]); a z wall of the lane-parallel form covers only the columns
+    // in zedge (k = x*Ny + y, the columns that are not direct)
+    unsigned afirst[OEMS_MAX_MUR + 1];
+    const unsigned* zedge;
+    unsigned nzedge;
 };
 
 // Where the Mur pre and post voltage hooks (engine_ext_mur_abc.cpp:83-149) run: inside the
@@ -135,6 +141,14 @@ struct MurDev {
 // unwritten: the wall's apply (k_mur) overwrites them after the dispersive apply hooks, so the
 // raw value is never observed, and V_old(line) can still be read from memory by the shift cell
 // while the launch runs.
+
+// the index of a wall point in the wall's tables (cP, cPP, bP, bPP), iP / iPP its coordinates
+// along nyP / nyPP: z fastest where z is tangential (the host stores those walls' tables
+// transposed), so the threads that walk z touch consecutive entries
+__device__ __forceinline__ unsigned mur_k(const MurWallDev& d, unsigned iP, unsigned iPP)
+{
+    return d.nyP == 2 ? iPP * d.n1 + iP : iP * d.n2 + iPP;
+}
 
 // true when a coordinate of the cell lies outside its axis window (a possible line or shift);
 // NA = 2 checks x and y only
@@ -170,7 +184,7 @@ __device__ __forceinline__ unsigned mur_cell(const GridDev& g, const MurDev& m, 
             if (c == d.line) keep &= ~((1u << aP) | (1u << aPP));
             if (c == d.shift) {
                 const unsigned long long ol = o + (unsigned long long)((long long)d.line - (long long)d.shift) * stride;
-                const unsigned k = iP * d.n2 + iPP;
+                const unsigned k = mur_k(d, iP, iPP);
                 const float lP = g.V[(unsigned long long)aP * g.S + ol];
                 const float lPP = g.V[(unsigned long long)aPP * g.S + ol];
                 const float cP = __ldg(d.cP + k), cPP = __ldg(d.cPP + k);
@@ -1011,11 +1025,10 @@ struct ExcDev {
     unsigned period;                 // 0 = aperiodic
 };
 
-static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsigned* __restrict__ numTS)
+__device__ __forceinline__ void exc_point(float* __restrict__ F, const ExcDev& e, unsigned k, unsigned numTS)
 {
-    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= e.count) return;
-    const int ts = (int)*numTS;
+    const int ts = (int)numTS;
     const int p = e.period ? (int)e.period : ts + 1;
     int exc_pos = ts - (int)e.delay[k];
     exc_pos *= (exc_pos > 0);
@@ -1023,6 +1036,11 @@ static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsig
     exc_pos *= (exc_pos < (int)e.length);
     const unsigned long long o = e.off[k];
     F[o] = fadd(F[o], fmul(e.amp[k], e.sig[exc_pos]));
+}
+
+static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsigned* __restrict__ numTS)
+{
+    exc_point(F, e, blockIdx.x * blockDim.x + threadIdx.x, *numTS);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1215,13 +1233,54 @@ static __global__ void k_mur_zpost(GridDev g, MurDev m)
 }
 
 // ---------------------------------------------------------------------------------------------
-// Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:83-178) as separate launches: phase
-// 0 = pre (before the voltage update), 1 = post (after it), 2 = apply (after the dispersive apply
-// hooks).  With the hooks inside the voltage update (mur_cell / mur_z_*) only phase 2 runs.  A
-// single launch covers every wall: blockIdx.y = wall, threads over the wall plane [n1][n2].
+// Engine_Ext_Mur_ABC (FDTD/extensions/engine_ext_mur_abc.cpp:83-178) as separate launches: k_mur
+// phase 0 = pre (before the voltage update), 1 = post (after it), one launch for every wall
+// (blockIdx.y = wall, threads over the wall plane [n1][n2]); k_mur_apply = the apply (after the
+// dispersive apply hooks), one flat launch.  With the hooks inside the voltage update
+// (mur_cell / mur_z_*) only the apply runs.
 __device__ __forceinline__ unsigned long long mur_off(const GridDev& g, int comp, const unsigned p[3])
 {
     return (unsigned long long)comp * g.S + ((unsigned long long)p[0] * g.Ny + p[1]) * g.Pz + p[2];
+}
+
+// the apply of wall wi at point t of its plane, or of its t-th listed column (zedge)
+__device__ __forceinline__ void mur_apply_point(const GridDev& g, const MurDev& m, int wi, unsigned t, unsigned ts)
+{
+    const MurWallDev& w = m.w[wi];
+    if (ts < w.start_ts) return;              // Engine_Ext_Mur_ABC::IsActive
+    const bool listed = m.lanes && w.ny == 2 && m.zedge;
+    unsigned i, j;
+    if (listed) {
+        if (t >= m.nzedge) return;
+        const unsigned c = __ldg(m.zedge + t);
+        i = c / w.n2;
+        j = c - i * w.n2;
+    } else {
+        if (t >= w.n1 * w.n2) return;
+        // consecutive threads walk the tangential axis that is contiguous in memory (z when it
+        // is tangential, else y); the small per-wall tables are L2-resident either way
+        if (w.nyP == 2) { i = t % w.n1; j = t / w.n1; }
+        else { i = t / w.n2; j = t - i * w.n2; }
+    }
+    const unsigned k = mur_k(w, i, j);
+    unsigned pos[3];
+    pos[w.ny] = w.line;
+    pos[w.nyP] = i;
+    pos[w.nyPP] = j;
+    // a direct column of the lane-parallel z-wall form holds its final value already
+    if (!listed && m.lanes && w.ny == 2 && mur_z_direct(m, pos[0], pos[1])) return;
+    // walls are applied in reverse insertion order, so on shared edges the wall with the
+    // lowest index is the last writer; skip components a lower active wall also writes
+    bool wP = true, wPP = true;
+    for (int q = 0; q < wi; ++q) {
+        const MurWallDev& o = m.w[q];
+        if (ts < o.start_ts || pos[o.ny] != o.line) continue;
+        if (w.nyP != o.ny) wP = false;
+        if (w.nyPP != o.ny) wPP = false;
+    }
+    float* V = g.V;
+    if (wP) V[mur_off(g, w.nyP, pos)] = w.bP[k];
+    if (wPP) V[mur_off(g, w.nyPP, pos)] = w.bPP[k];
 }
 
 static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __restrict__ numTS)
@@ -1238,7 +1297,7 @@ static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __r
     unsigned i, j;
     if (w.nyP == 2) { i = t % w.n1; j = t / w.n1; }
     else { i = t / w.n2; j = t - i * w.n2; }
-    const unsigned k = i * w.n2 + j;
+    const unsigned k = mur_k(w, i, j);
     unsigned pos[3], ps[3];
     pos[w.ny] = w.line; ps[w.ny] = w.shift;
     pos[w.nyP] = ps[w.nyP] = i;
@@ -1252,21 +1311,16 @@ static __global__ void k_mur(GridDev g, MurDev m, int phase, const unsigned* __r
     if (phase == 1) {
         w.bP[k] = fadd(w.bP[k], fmul(w.cP[k], V[mur_off(g, w.nyP, ps)]));
         w.bPP[k] = fadd(w.bPP[k], fmul(w.cPP[k], V[mur_off(g, w.nyPP, ps)]));
-        return;
     }
-    // a direct column of the lane-parallel z-wall form holds its final value already
-    if (m.lanes && w.ny == 2 && mur_z_direct(m, pos[0], pos[1])) return;
-    // walls are applied in reverse insertion order, so on shared edges the wall with the
-    // lowest index is the last writer; skip components a lower active wall also writes
-    bool wP = true, wPP = true;
-    for (int q = 0; q < wi; ++q) {
-        const MurWallDev& o = m.w[q];
-        if (ts < o.start_ts || pos[o.ny] != o.line) continue;
-        if (w.nyP != o.ny) wP = false;
-        if (w.nyPP != o.ny) wPP = false;
-    }
-    if (wP) V[mur_off(g, w.nyP, pos)] = w.bP[k];
-    if (wPP) V[mur_off(g, w.nyPP, pos)] = w.bPP[k];
+}
+
+// the flat apply launch: every wall's points (or listed columns) in one 1-D grid
+static __global__ void k_mur_apply(GridDev g, MurDev m, const unsigned* __restrict__ numTS)
+{
+    const unsigned b = blockIdx.x;
+    int wi = 0;
+    while (wi + 1 < m.nwall && b >= m.afirst[wi + 1]) ++wi;
+    mur_apply_point(g, m, wi, (b - m.afirst[wi]) * blockDim.x + threadIdx.x, *numTS);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1370,9 +1424,8 @@ static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long
 // position's component and the Mur walls' components are in skip).  Between the two nothing
 // else writes the field at these positions, so the pre reads the same values as it would at the
 // start of the next half-step; the ADE values stay in registers between them.
-static __global__ void k_lorentz_carry(float* __restrict__ F, unsigned long long S, LorDev l)
+__device__ __forceinline__ void lor_carry_point(float* __restrict__ F, unsigned long long S, const LorDev& l, unsigned i)
 {
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= l.count) return;
     const unsigned long long o = lor_off(l, i);
     const unsigned sk = l.skip ? l.skip[i] : 0u;
@@ -1392,6 +1445,31 @@ static __global__ void k_lorentz_carry(float* __restrict__ F, unsigned long long
         }
         l.ade[n * l.count + i] = lor_pre_one(l, c, n, a[n], la[n], f[n]);
         if (l.lor) l.lade[n * l.count + i] = la[n];
+    }
+}
+
+static __global__ void k_lorentz_carry(float* __restrict__ F, unsigned long long S, LorDev l)
+{
+    lor_carry_point(F, S, l, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// The end of a voltage half-step inside a sequence as one launch: the Mur apply (blocks
+// [0, lor0)), the dispersive carry ([lor0, exc0)) and the excitation (from exc0).  The host
+// allows it only where the three touch disjoint values: no dispersive position on a Mur line
+// (skip is empty), no excitation edge on a dispersive position or on a Mur line's tangential
+// component; the order among them then does not matter.
+static __global__ void k_vtail(GridDev g, MurDev m, LorDev l, ExcDev x, const unsigned* __restrict__ numTS,
+                               unsigned lor0, unsigned exc0)
+{
+    const unsigned b = blockIdx.x;
+    if (b < lor0) {
+        int wi = 0;
+        while (wi + 1 < m.nwall && b >= m.afirst[wi + 1]) ++wi;
+        mur_apply_point(g, m, wi, (b - m.afirst[wi]) * blockDim.x + threadIdx.x, *numTS);
+    } else if (b < exc0) {
+        lor_carry_point(g.V, g.S, l, (b - lor0) * blockDim.x + threadIdx.x);
+    } else {
+        exc_point(g.V, x, (b - exc0) * blockDim.x + threadIdx.x, *numTS);
     }
 }
 

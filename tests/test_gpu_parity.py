@@ -192,6 +192,29 @@ def test_lorentz_carry_bit_exact_against_oracle(cuda_lib, monkeypatch, carry, se
     assert g.launches_per_step() == n_plain - (1 if carry == "1" and not src_on_lor else 0)
 
 
+@pytest.mark.parametrize("seed", [1, 3])
+@pytest.mark.parametrize("vtail", ["1", "0"])
+def test_voltage_tail_one_launch_bit_exact_against_oracle(cuda_lib, monkeypatch, vtail, seed):
+    """Inside a sequence the Mur apply, the dispersive carry and the excitation of the voltage
+    half-step run as one launch (k_vtail) where they touch disjoint values; OEMS_CUDA_VTAIL=0
+    keeps three launches.  Both equal the oracle bit for bit over mixed chunk lengths.  Seed 3
+    puts a dispersive position on the z = 0 wall line, which keeps the launches apart."""
+    monkeypatch.setenv("OEMS_CUDA_VTAIL", vtail)
+    op = configs.stress(shape=(40, 36, 30), steps=150, nblocks=16, seed=seed)
+    pos = np.asarray(op.lorentz[0].pos)
+    on_wall = any(bool(np.any(pos[w.ny] == w.line_nr)) for w in op.mur)
+    g, r = _run_pair(op, 150, chunks=(1, 7, 16, 33))
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, bad
+    monkeypatch.setenv("OEMS_CUDA_VTAIL", "0")
+    sep = Engine_CUDA(op, 10)
+    n_sep = sep.launches_per_step()
+    sep.close()
+    assert on_wall == (seed == 3)
+    assert g.launches_per_step() == n_sep - (2 if vtail == "1" and not on_wall else 0), on_wall
+
+
 REG4_CASES = [
     ("patch_pml8", lambda: configs.patch(shape=(56, 52, 36), steps=220, with_nf2ff=False), 220),
     ("plane_wave_pml4", lambda: configs.plane_wave(n=(28, 24, 32), pml=4, steps=200), 200),
