@@ -194,6 +194,7 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->pcache.pin) cudaFreeHost(e->pcache.pin);
     delete e;
 }
 
@@ -1865,11 +1866,47 @@ int oems_cuda_read_probe_range(oems_cuda_engine* e, int id, size_t first, size_t
     if (!e->inited) return fail(e, OEMS_ERR_STATE, "engine not initialised");
     const ProbeDev& d = e->probe_dev[id];
     if (first + count > d.nslots) return fail(e, OEMS_ERR_ARG, "probe slot range out of bounds");
-    if (count) {
+    if (!count) return OEMS_OK;
+    if (count > 64) {
         CK(cudaMemcpyAsync(out, d.series + first * d.ncomp, count * d.ncomp * sizeof(double),
                            cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
+        return OEMS_OK;
     }
+    // short ranges (a processing loop reading each probe's newest samples): the first read after
+    // a step fetches the same slot range of every probe into pinned memory with one
+    // synchronisation; the other probes' reads of that range are served from it until the engine
+    // steps again or is restored
+    ProbeCache& c = e->pcache;
+    const bool hit = c.valid && c.ts == e->host_numTS && c.gen == e->series_gen && c.first == first &&
+                     c.count == count && c.off[id] != SIZE_MAX;
+    if (!hit) {
+        c.valid = false;
+        c.off.assign(e->probe_dev.size(), SIZE_MAX);
+        size_t need = 0;
+        for (size_t j = 0; j < e->probe_dev.size(); ++j)
+            if (first + count <= e->probe_dev[j].nslots) { c.off[j] = need; need += count * e->probe_dev[j].ncomp; }
+        if (need > c.cap) {
+            if (c.pin) cudaFreeHost(c.pin);
+            c.pin = nullptr;
+            c.cap = 0;
+            CK(cudaMallocHost(&c.pin, need * sizeof(double)));
+            c.cap = need;
+        }
+        for (size_t j = 0; j < e->probe_dev.size(); ++j)
+            if (c.off[j] != SIZE_MAX) {
+                const ProbeDev& q = e->probe_dev[j];
+                CK(cudaMemcpyAsync(c.pin + c.off[j], q.series + first * q.ncomp, count * q.ncomp * sizeof(double),
+                                   cudaMemcpyDeviceToHost, e->stream));
+            }
+        CK(cudaStreamSynchronize(e->stream));
+        c.valid = true;
+        c.ts = e->host_numTS;
+        c.gen = e->series_gen;
+        c.first = first;
+        c.count = count;
+    }
+    memcpy(out, c.pin + c.off[id], count * d.ncomp * sizeof(double));
     return OEMS_OK;
 }
 
@@ -1952,6 +1989,7 @@ int oems_cuda_restore(oems_cuda_engine* e, const void* host, size_t bytes)
     }
     CK(cudaStreamSynchronize(e->stream));
     memcpy(&e->host_numTS, p, sizeof(unsigned));
+    ++e->series_gen;                 // the probe series changed under an unchanged step count
     return OEMS_OK;
 }
 

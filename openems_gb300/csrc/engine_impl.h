@@ -3,6 +3,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <string>
 #include <utility>
 #include <vector>
@@ -21,6 +22,15 @@ const double kPI = 3.14159265358979323846;  // M_PI as used by Common/processint
 struct UpmlHost {
     unsigned start[3], nl[3];
     std::vector<float> tab[6];  // vv, vvfo, vvfn, ii, iifo, iifn
+};
+struct ProbeCache {
+    double* pin = nullptr;           // pinned host copy of slots [first, first + count) per probe
+    size_t cap = 0;
+    std::vector<size_t> off;         // per probe: offset in pin, or SIZE_MAX
+    bool valid = false;
+    unsigned long long ts = 0;
+    unsigned gen = 0;
+    size_t first = 0, count = 0;
 };
 struct MurHost {
     int ny;
@@ -173,7 +183,10 @@ struct oems_cuda_engine {
     bool mur_v4 = false;
     // dispersive apply + next pre as one launch inside enqueued sequences (k_lorentz_carry)
     bool lor_carry_v = false, lor_carry_i = false;
-    bool vtail = false;              // k_vtail: Mur apply + carry + excitation as one launch
+    bool vtail = false;
+    // newest-sample reads of the probes (oems_cuda_read_probe_range): one pinned fetch per step
+    ProbeCache pcache;
+    unsigned series_gen = 0;         // bumped by restore              // k_vtail: Mur apply + carry + excitation as one launch
 
     // one-kernel step (the plane march, march.cuh): the K-step graph alternates buffer sets A
     // (dV, dI) and B (dV2, dI2); K is even, so the state is in A whenever the host sees it

@@ -215,6 +215,38 @@ def test_voltage_tail_one_launch_bit_exact_against_oracle(cuda_lib, monkeypatch,
     assert g.launches_per_step() == n_sep - (2 if vtail == "1" and not on_wall else 0), on_wall
 
 
+def test_probe_range_newest_samples_and_restore(cuda_lib):
+    """oems_cuda_read_probe_range over single slots, step by step (the processing-loop pattern the
+    engine serves from one pinned fetch per step), equals the full series; after a restore to an
+    earlier step and a different field, a read at the same step count returns the new samples."""
+    op = configs.small_mixed(steps=60)
+    g = Engine_CUDA(op, 60)
+    pids = g.vprobe_ids + g.iprobe_ids
+    assert len(pids) >= 2
+    got = {p: [] for p in pids}
+    blob = None
+    for ts in range(1, 41):
+        g.IterateTS(1)
+        if ts == 20:
+            blob = g.snapshot()
+        for p in pids:
+            got[p].append(g.probe_range(p, ts, 1).copy())
+    for p in pids:
+        full = g.probe_series(p)
+        assert bits_equal(np.concatenate(got[p]), np.asarray(full)[1:41].ravel()), p
+    g.restore(blob)
+    g.IterateTS(1)
+    before = {p: g.probe_range(p, 21, 1).copy() for p in pids}     # the same step count as below
+    g.restore(blob)
+    g.write_field(0, 2.0 * g.read_field(0))
+    g.write_field(1, 2.0 * g.read_field(1))
+    g.IterateTS(1)
+    after = {p: g.probe_range(p, 21, 1).copy() for p in pids}
+    assert any(not bits_equal(before[p], after[p]) for p in pids)
+    for p in pids:
+        assert bits_equal(after[p], np.asarray(g.probe_series(p))[21:22].ravel()), p
+
+
 REG4_CASES = [
     ("patch_pml8", lambda: configs.patch(shape=(56, 52, 36), steps=220, with_nf2ff=False), 220),
     ("plane_wave_pml4", lambda: configs.plane_wave(n=(28, 24, 32), pml=4, steps=200), 200),
