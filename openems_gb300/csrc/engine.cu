@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -195,6 +196,7 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->stream) cudaStreamDestroy(e->stream);
     if (e->pcache.pin) cudaFreeHost(e->pcache.pin);
+    if (e->latest_host) cudaFreeHost(e->latest_host);
     delete e;
 }
 
@@ -1554,6 +1556,22 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         }
         e->probe_dev.push_back(d);
     }
+    // mapped host memory for the probes' newest samples: [nprobe][3] values, then [nprobe] slots
+    if (!e->probe_dev.empty()) {
+        const size_t np = e->probe_dev.size();
+        void* h = nullptr;
+        CK(cudaHostAlloc(&h, np * (3 * sizeof(double) + sizeof(unsigned)), cudaHostAllocMapped));
+        e->latest_host = static_cast<double*>(h);
+        e->latest_slot_host = reinterpret_cast<unsigned*>(e->latest_host + 3 * np);
+        for (size_t j = 0; j < np; ++j) e->latest_slot_host[j] = UINT_MAX;
+        void* dv = nullptr;
+        CK(cudaHostGetDevicePointer(&dv, h, 0));
+        double* dl = static_cast<double*>(dv);
+        for (size_t j = 0; j < np; ++j) {
+            e->probe_dev[j].latest = dl + 3 * j;
+            e->probe_dev[j].latest_slot = reinterpret_cast<unsigned*>(dl + 3 * np) + j;
+        }
+    }
 
     // FD dumps
     std::vector<unsigned> block0(1, 1u);
@@ -1867,6 +1885,15 @@ int oems_cuda_read_probe_range(oems_cuda_engine* e, int id, size_t first, size_t
     const ProbeDev& d = e->probe_dev[id];
     if (first + count > d.nslots) return fail(e, OEMS_ERR_ARG, "probe slot range out of bounds");
     if (!count) return OEMS_OK;
+    if (count == 1 && e->latest_host) {
+        // the newest sample: after the synchronisation the step-end kernel's copy in mapped
+        // memory is current
+        CK(cudaStreamSynchronize(e->stream));
+        if (e->latest_slot_host[id] == first) {
+            memcpy(out, e->latest_host + 3 * (size_t)id, d.ncomp * sizeof(double));
+            return OEMS_OK;
+        }
+    }
     if (count > 64) {
         CK(cudaMemcpyAsync(out, d.series + first * d.ncomp, count * d.ncomp * sizeof(double),
                            cudaMemcpyDeviceToHost, e->stream));
@@ -1990,6 +2017,8 @@ int oems_cuda_restore(oems_cuda_engine* e, const void* host, size_t bytes)
     CK(cudaStreamSynchronize(e->stream));
     memcpy(&e->host_numTS, p, sizeof(unsigned));
     ++e->series_gen;                 // the probe series changed under an unchanged step count
+    if (e->latest_slot_host)
+        for (size_t j = 0; j < e->probe_dev.size(); ++j) e->latest_slot_host[j] = UINT_MAX;
     return OEMS_OK;
 }
 

@@ -186,6 +186,8 @@ struct oems_cuda_engine {
     bool vtail = false;
     // newest-sample reads of the probes (oems_cuda_read_probe_range): one pinned fetch per step
     ProbeCache pcache;
+    double* latest_host = nullptr;   // mapped: each probe's newest sample (ProbeDev::latest)
+    unsigned* latest_slot_host = nullptr;
     unsigned series_gen = 0;         // bumped by restore              // k_vtail: Mur apply + carry + excitation as one launch
 
     // one-kernel step (the plane march, march.cuh): the K-step graph alternates buffer sets A

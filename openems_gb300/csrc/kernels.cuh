@@ -1491,6 +1491,10 @@ struct ProbeDev {
     const double2* phasor;           // [nsamp][nf] = exp(-2j*pi*f*t)
     double* dft;                     // [nf][ncomp][2]
     double dt;
+    // newest sample in mapped host memory (device address), with its slot: a host read of the
+    // newest slot needs no copy after the stream synchronisation
+    double* latest;                  // [ncomp]
+    unsigned* latest_slot;
 };
 
 struct DumpDev {
@@ -1525,7 +1529,13 @@ static __device__ void probe_record(const ProbeDev& p, unsigned ts, unsigned c, 
 {
     if (do_td) {
         const unsigned slot = ts / p.interval;
-        if (slot < p.nslots) p.series[(unsigned long long)slot * p.ncomp + c] = a;
+        if (slot < p.nslots) {
+            p.series[(unsigned long long)slot * p.ncomp + c] = a;
+            if (p.latest) {
+                p.latest[c] = a;
+                if (c == 0) *p.latest_slot = slot;
+            }
+        }
     }
     if (do_fd) {
         const unsigned smp = ts / p.fd_interval;

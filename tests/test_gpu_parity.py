@@ -221,7 +221,7 @@ def test_probe_range_newest_samples_and_restore(cuda_lib):
     earlier step and a different field, a read at the same step count returns the new samples."""
     op = configs.small_mixed(steps=60)
     g = Engine_CUDA(op, 60)
-    pids = g.vprobe_ids + g.iprobe_ids
+    pids = g.vprobe_ids + g.iprobe_ids + g.fprobe_ids
     assert len(pids) >= 2
     got = {p: [] for p in pids}
     blob = None
@@ -233,7 +233,7 @@ def test_probe_range_newest_samples_and_restore(cuda_lib):
             got[p].append(g.probe_range(p, ts, 1).copy())
     for p in pids:
         full = g.probe_series(p)
-        assert bits_equal(np.concatenate(got[p]), np.asarray(full)[1:41].ravel()), p
+        assert bits_equal(np.concatenate(got[p]).ravel(), np.asarray(full)[1:41].ravel()), p
     g.restore(blob)
     g.IterateTS(1)
     before = {p: g.probe_range(p, 21, 1).copy() for p in pids}     # the same step count as below
@@ -244,7 +244,7 @@ def test_probe_range_newest_samples_and_restore(cuda_lib):
     after = {p: g.probe_range(p, 21, 1).copy() for p in pids}
     assert any(not bits_equal(before[p], after[p]) for p in pids)
     for p in pids:
-        assert bits_equal(after[p], np.asarray(g.probe_series(p))[21:22].ravel()), p
+        assert bits_equal(after[p].ravel(), np.asarray(g.probe_series(p))[21:22].ravel()), p
 
 
 REG4_CASES = [
