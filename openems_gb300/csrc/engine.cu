@@ -855,13 +855,14 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof, uns
         post(); ++L;
     }
     const unsigned mur_blocks = e->mur.empty() ? 0u : e->murdev.afirst[e->murdev.nwall];
-    if (carry_v && e->vtail) {
-        // Mur apply, dispersive carry and excitation in one launch
+    if (e->vtail) {
+        // Mur apply, dispersive carry (or the apply at a sequence's end) and excitation in one launch
         const LorDev& l = e->lorV[0];
         const unsigned lor0 = mur_blocks, exc0 = lor0 + (l.count + 255) / 256;
         const unsigned blocks = exc0 + (e->excV.count + 255) / 256;
         pre(OEMS_KC_LORENTZ);
-        k_vtail<<<blocks, blk, 0, s>>>(g, e->murdev, l, e->excV, e->d_numTS, lor0, exc0);
+        if (carry_v) k_vtail<true><<<blocks, blk, 0, s>>>(g, e->murdev, l, e->excV, e->d_numTS, lor0, exc0);
+        else k_vtail<false><<<blocks, blk, 0, s>>>(g, e->murdev, l, e->excV, e->d_numTS, lor0, exc0);
         post(); ++L;
     } else {
         if (!carry_v)
@@ -1448,8 +1449,9 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         }
     }
 
-    // the voltage half-step's end as one launch inside sequences (k_vtail): the Mur apply, the
-    // dispersive carry and the excitation touch disjoint values
+    // the voltage half-step's end as one launch (k_vtail): the Mur apply, the dispersive carry
+    // (inside a sequence) or apply (its last step, a single step) and the excitation touch
+    // disjoint values
     e->vtail = false;
     if (e->lor_carry_v && e->lorV.size() == 1 && !e->lorV[0].skip) {
         bool ok = true;

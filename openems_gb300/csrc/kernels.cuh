@@ -1405,9 +1405,8 @@ static __global__ void k_lorentz_pre(const float* __restrict__ F, unsigned long 
 }
 
 // the apply hook: F -= ade
-static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long S, LorDev l)
+__device__ __forceinline__ void lor_apply_point(float* __restrict__ F, unsigned long long S, const LorDev& l, unsigned i)
 {
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= l.count) return;
     const unsigned long long o = lor_off(l, i);
     const unsigned sk = l.skip ? l.skip[i] : 0u;
@@ -1417,6 +1416,11 @@ static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long
         const unsigned long long q = o + n * S;
         F[q] = fsub(F[q], l.ade[n * l.count + i]);
     }
+}
+
+static __global__ void k_lorentz_apply(float* __restrict__ F, unsigned long long S, LorDev l)
+{
+    lor_apply_point(F, S, l, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // This step's apply and the next step's pre in one pass, launched at the end of the field's
@@ -1453,13 +1457,15 @@ static __global__ void k_lorentz_carry(float* __restrict__ F, unsigned long long
     lor_carry_point(F, S, l, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// The end of a voltage half-step inside a sequence as one launch: the Mur apply (blocks
-// [0, lor0)), the dispersive carry ([lor0, exc0)) and the excitation (from exc0).  The host
-// allows it only where the three touch disjoint values: no dispersive position on a Mur line
-// (skip is empty), no excitation edge on a dispersive position or on a Mur line's tangential
-// component; the order among them then does not matter.
-static __global__ void k_vtail(GridDev g, MurDev m, LorDev l, ExcDev x, const unsigned* __restrict__ numTS,
-                               unsigned lor0, unsigned exc0)
+// The end of a voltage half-step as one launch: the Mur apply (blocks [0, lor0)), the
+// dispersive carry (CARRY, inside a sequence) or apply (the sequence's last step) ([lor0, exc0))
+// and the excitation (from exc0).  The host allows it only where the three touch disjoint
+// values: one dispersive order, no dispersive position on a Mur line (skip is empty), no
+// excitation edge on a dispersive position or on a Mur line's tangential component; the order
+// among them then does not matter.
+template <bool CARRY>
+__global__ void k_vtail(GridDev g, MurDev m, LorDev l, ExcDev x, const unsigned* __restrict__ numTS, unsigned lor0,
+                        unsigned exc0)
 {
     const unsigned b = blockIdx.x;
     if (b < lor0) {
@@ -1467,7 +1473,9 @@ static __global__ void k_vtail(GridDev g, MurDev m, LorDev l, ExcDev x, const un
         while (wi + 1 < m.nwall && b >= m.afirst[wi + 1]) ++wi;
         mur_apply_point(g, m, wi, (b - m.afirst[wi]) * blockDim.x + threadIdx.x, *numTS);
     } else if (b < exc0) {
-        lor_carry_point(g.V, g.S, l, (b - lor0) * blockDim.x + threadIdx.x);
+        const unsigned i = (b - lor0) * blockDim.x + threadIdx.x;
+        if (CARRY) lor_carry_point(g.V, g.S, l, i);
+        else lor_apply_point(g.V, g.S, l, i);
     } else {
         exc_point(g.V, x, (b - exc0) * blockDim.x + threadIdx.x, *numTS);
     }
