@@ -263,7 +263,10 @@ int oems_cuda_read_probe(oems_cuda_engine* eng, int probe_id, double* out, size_
 
 /* Slots [first, first+count) of a probe time series (same slot meaning as above). Used by a
  * caller that, like ProcessingArray::Process (Common/processing.cpp:355-366), fetches the newest
- * samples after every IterateTS chunk. */
+ * samples after every IterateTS chunk. Synchronises the engine stream. The newest sample
+ * (count = 1, the slot of the last step) comes from a mapped host copy the step writes, with no
+ * device copy; other short ranges (count <= 64) are fetched for every probe at once into pinned
+ * memory and served from there until the engine steps again or is restored. */
 int oems_cuda_read_probe_range(oems_cuda_engine* eng, int probe_id, size_t first, size_t count, double* out);
 
 /* Probe DFT: out[2*f], out[2*f+1] = real, imag at frequency f (double). */
