@@ -39,7 +39,14 @@ struct Mesh {
     const double* hi;
     const double* par;           // [nrec][4] eps_r, kappa, mu_r, sigma
     double bg[4];
+    // record masks: bit r of mask[((ax * 3 + kind) * Nmax + i) * W + r / 64] is set when the
+    // sample coordinate of kind `kind` at index i of axis ax lies in record r's [lo, hi] along ax
+    // (the same double compares as a direct test); kinds: SAMPLE_HALF, SAMPLE_QUP, SAMPLE_QDN
+    const unsigned long long* mask;
+    unsigned W, Nmax;
 };
+
+enum { SAMPLE_HALF = 0, SAMPLE_QUP = 1, SAMPLE_QDN = 2 };
 
 // GetRawDiscDelta (FDTD/operator.cpp:1256-1266) for index i (may be -1 or >= N-1)
 __device__ __forceinline__ double raw_delta(const double* L, unsigned N, int i)
@@ -64,13 +71,45 @@ __device__ __forceinline__ double dual_delta(const double* L, unsigned N, int i)
     return i == 0 ? ds(L[1], L[0]) : ds(dual_line(L, N, i), dual_line(L, N, i - 1));
 }
 
-// the material parameters at a point: the last paint record containing it, else the background
-__device__ __forceinline__ const double* lookup(const Mesh& m, double x, double y, double z)
+// the sample coordinates of the quarter-cell averaging (FDTD/operator.cpp:1447-1564 as
+// restated): half a cell up, a quarter up, a quarter down from line i
+__device__ __forceinline__ double sample_coord(const double* L, unsigned N, int i, int kind)
 {
-    for (int r = (int)m.nrec - 1; r >= 0; --r) {
-        const double* lo = m.lo + 3 * r;
-        const double* hi = m.hi + 3 * r;
-        if (x >= lo[0] && x <= hi[0] && y >= lo[1] && y <= hi[1] && z >= lo[2] && z <= hi[2]) return m.par + 4 * r;
+    if (kind == SAMPLE_HALF) return da(L[i], dm(raw_delta(L, N, i), 0.5));
+    if (kind == SAMPLE_QUP) return da(L[i], dm(raw_delta(L, N, i), 0.25));
+    return ds(L[i], dm(raw_delta(L, N, i - 1), 0.25));
+}
+
+// one thread per (axis, kind, index, mask word)
+__global__ void k_masks(Mesh m, unsigned long long* mask)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned w = t % m.W, rest = t / m.W;
+    const unsigned i = rest % m.Nmax, ak = rest / m.Nmax;
+    if (ak >= 9) return;
+    const int ax = (int)(ak / 3), kind = (int)(ak % 3);
+    unsigned long long bits = 0ull;
+    if (i < m.N[ax]) {
+        const double c = sample_coord(m.L[ax], m.N[ax], (int)i, kind);
+        for (unsigned b = 0; b < 64; ++b) {
+            const unsigned r = w * 64 + b;
+            if (r >= m.nrec) break;
+            if (c >= m.lo[3 * r + ax] && c <= m.hi[3 * r + ax]) bits |= 1ull << b;
+        }
+    }
+    mask[t] = bits;
+}
+
+// the material parameters at a sample point given by its per-axis (index, kind): the last paint
+// record containing it, else the background
+__device__ __forceinline__ const double* lookup(const Mesh& m, const unsigned idx[3], const int kind[3])
+{
+    const unsigned long long* p0 = m.mask + ((size_t)(0 * 3 + kind[0]) * m.Nmax + idx[0]) * m.W;
+    const unsigned long long* p1 = m.mask + ((size_t)(1 * 3 + kind[1]) * m.Nmax + idx[1]) * m.W;
+    const unsigned long long* p2 = m.mask + ((size_t)(2 * 3 + kind[2]) * m.Nmax + idx[2]) * m.W;
+    for (int w = (int)m.W - 1; w >= 0; --w) {
+        const unsigned long long b = __ldg(p0 + w) & __ldg(p1 + w) & __ldg(p2 + w);
+        if (b) return m.par + 4 * (64 * w + 63 - __clzll((long long)b));
     }
     return m.bg;
 }
@@ -99,22 +138,19 @@ __global__ void k_ec(Mesh m, int n, ECOut o)
     const int i = (int)idx[a], j = (int)idx[p], k = (int)idx[pp];
     const double u = m.unit;
     auto wmain = [&](int ax, int q) -> double { return q >= 0 ? dm(main_delta(m.L[ax], m.N[ax], q), u) : 0.0; };
-    // sample coordinates (FDTD/operator.cpp:1447-1564 as restated)
-    const double cn = da(L[i], dm(raw_delta(L, N, i), 0.5));
-    const double cp_up = da(Lp[j], dm(raw_delta(Lp, Np, j), 0.25));
-    const double cp_dn = ds(Lp[j], dm(raw_delta(Lp, Np, j - 1), 0.25));
-    const double cpp_up = da(Lpp[k], dm(raw_delta(Lpp, Npp, k), 0.25));
-    const double cpp_dn = ds(Lpp[k], dm(raw_delta(Lpp, Npp, k - 1), 0.25));
+    // the four quarter-cell samples: half a cell up along n, a quarter up / down across
+    // (sample_coord; the records containing each come from the per-axis masks)
     const double Wp = wmain(p, j), WpM = wmain(p, j - 1), Wpp = wmain(pp, k), WppM = wmain(pp, k - 1);
-    const double scp[4] = {cp_up, cp_dn, cp_up, cp_dn}, scpp[4] = {cpp_up, cpp_up, cpp_dn, cpp_dn};
+    const int kp[4] = {SAMPLE_QUP, SAMPLE_QDN, SAMPLE_QUP, SAMPLE_QDN};
+    const int kpp[4] = {SAMPLE_QUP, SAMPLE_QUP, SAMPLE_QDN, SAMPLE_QDN};
     const double swa[4] = {Wp, WpM, Wp, WpM}, swb[4] = {Wpp, Wpp, WppM, WppM};
     double eps_acc = 0.0, kap_acc = 0.0, area = 0.0;
     for (int q = 0; q < 4; ++q) {
-        double c3[3];
-        c3[a] = cn;
-        c3[p] = scp[q];
-        c3[pp] = scpp[q];
-        const double* par = lookup(m, c3[0], c3[1], c3[2]);
+        int k3[3];
+        k3[a] = SAMPLE_HALF;
+        k3[p] = kp[q];
+        k3[pp] = kpp[q];
+        const double* par = lookup(m, idx, k3);
         const double A = dm(swa[q], swb[q]);
         if (q == 0) {
             eps_acc = dm(par[0], A);
@@ -129,16 +165,14 @@ __global__ void k_ec(Mesh m, int n, ECOut o)
     const double e0 = dm(eps_acc, dd(kEPS0, area));
     const double e1 = dd(kap_acc, area);
     // mu and sigma: two samples along n at the cell centres across
-    const double cpm = da(Lp[j], dm(raw_delta(Lp, Np, j), 0.5));
-    const double cppm = da(Lpp[k], dm(raw_delta(Lpp, Npp, k), 0.5));
     const double Ddn = wmain(a, i - 1), Dup = wmain(a, i);
-    double c3[3];
-    c3[a] = ds(L[i], dm(raw_delta(L, N, i - 1), 0.25));
-    c3[p] = cpm;
-    c3[pp] = cppm;
-    const double* pdn = lookup(m, c3[0], c3[1], c3[2]);
-    c3[a] = da(L[i], dm(raw_delta(L, N, i), 0.25));
-    const double* pup = lookup(m, c3[0], c3[1], c3[2]);
+    int k3[3];
+    k3[a] = SAMPLE_QDN;
+    k3[p] = SAMPLE_HALF;
+    k3[pp] = SAMPLE_HALF;
+    const double* pdn = lookup(m, idx, k3);
+    k3[a] = SAMPLE_QUP;
+    const double* pup = lookup(m, idx, k3);
     double e2 = dd(Ddn, pdn[2]);
     double e3 = pdn[3] != 0.0 ? dd(Ddn, pdn[3]) : 0.0;
     double length = Ddn;
@@ -316,6 +350,15 @@ int oems_cuda_opbuild_create(const unsigned int num_lines[3], const double* line
     m.lo = lo;
     m.hi = hi;
     m.par = par;
+    // the per-axis record masks of the sample coordinates
+    m.W = std::max(1u, (nrec + 63) / 64);
+    m.Nmax = std::max(num_lines[0], std::max(num_lines[1], num_lines[2]));
+    const size_t nmask = 9ull * m.Nmax * m.W;
+    unsigned long long* mk = ob_alloc<unsigned long long>(b, nmask);
+    if (!mk) return ob_fail(b, OEMS_ERR_NOMEM, "opbuild: allocation");
+    k_masks<<<(unsigned)((nmask + 255) / 256), 256>>>(m, mk);
+    if (cudaGetLastError() != cudaSuccess) return ob_fail(b, OEMS_ERR_CUDA, "opbuild: mask kernel");
+    m.mask = mk;
     return OEMS_OK;
 }
 

@@ -2022,19 +2022,27 @@ class Operator:
         dT = self.dT
         Nx = int(self.N[0])
         Ny, Nz = int(self.N[1]), int(self.N[2])
-        # the index box that holds every sample point (primary or dual line) inside a dispersive
-        # primitive: outside it no edge can be dispersive, so only this box is painted
-        box = []
-        for k in range(3):
-            hit = np.zeros(int(self.N[k]), bool)
-            for rec in painter.recs:
-                if rec[4].kind == MATERIAL and rec[4].params.get("lorentz"):
-                    for c in (np.asarray(self.L[k]), np.asarray(self.dl[k])):
-                        hit |= (c >= rec[0][k]) & (c <= rec[1][k])
-            idx = np.nonzero(hit)[0]
-            box.append((int(idx[0]), int(idx[-1]) + 1) if idx.size else (0, 0))
-        (bx0, bx1), (y0, y1), (z0, z1) = box
-        if bx1 <= bx0 or y1 <= y0 or z1 <= z0:
+        # per dispersive primitive, the index box that holds its sample points (primary or dual
+        # lines): outside these boxes no edge can be dispersive, so only they are painted (the
+        # painted material at a point depends only on the point, so boxes that overlap give the
+        # same values there, merged below)
+        boxes = []
+        for rec in painter.recs:
+            if not (rec[4].kind == MATERIAL and rec[4].params.get("lorentz")):
+                continue
+            b = []
+            for k in range(3):
+                hit = np.zeros(int(self.N[k]), bool)
+                for c in (np.asarray(self.L[k]), np.asarray(self.dl[k])):
+                    hit |= (c >= rec[0][k]) & (c <= rec[1][k])
+                idx = np.nonzero(hit)[0]
+                if not idx.size:
+                    b = None
+                    break
+                b.append((int(idx[0]), int(idx[-1]) + 1))
+            if b:
+                boxes.append(b)
+        if not boxes:
             return []
         orders = []
         for o in range(order_max):
@@ -2048,7 +2056,7 @@ class Operator:
                 return np.array(vals + [0.0], np.float64)
             tab = {k: ptab(k) for k in ("eps_plasma", "eps_relax", "eps_pole", "mue_plasma", "mue_relax", "mue_pole")}
 
-            def slab(x0, x1):
+            def slab(x0, x1, y0, y1, z0, z1):
                 per_n = []
                 on_mask = np.zeros((x1 - x0, y1 - y0, z1 - z0), bool)
                 flags = [False, False, False, False]
@@ -2125,10 +2133,21 @@ class Operator:
                 pos[2] += z0
                 return pos.astype(np.uint32), tabs, flags
 
-            parts = _parallel(slab, [(bx0 + a, bx0 + b) for a, b in _slabs(bx1 - bx0, 2 * (os.cpu_count() or 1))])
+            vol = sum((b[0][1] - b[0][0]) * (b[1][1] - b[1][0]) * (b[2][1] - b[2][0]) for b in boxes)
+            per_task = max(1, vol // (2 * (os.cpu_count() or 1)))
+            tasks = []
+            for (bx0, bx1), (y0, y1), (z0, z1) in boxes:
+                nparts = max(1, ((bx1 - bx0) * (y1 - y0) * (z1 - z0)) // per_task)
+                tasks += [(bx0 + a, bx0 + b, y0, y1, z0, z1) for a, b in _slabs(bx1 - bx0, nparts)]
+            parts = _parallel(slab, tasks)
             pos = np.concatenate([p[0] for p in parts], axis=1)
             tabs = {k: np.concatenate([p[1][k] for p in parts], axis=1) for k in parts[0][1]}
             fl = [any(p[2][i] for p in parts) for i in range(4)]
+            # the reference's x-major scan order, each position once
+            lin = (pos[0].astype(np.int64) * Ny + pos[1]) * Nz + pos[2]
+            _, first = np.unique(lin, return_index=True)
+            pos = np.ascontiguousarray(pos[:, first])
+            tabs = {k: np.ascontiguousarray(v[:, first]) for k, v in tabs.items()}
             orders.append(LorentzOrder(pos, fl[0], fl[1], fl[2], fl[3], **tabs))
         return orders
 
