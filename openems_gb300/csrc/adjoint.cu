@@ -77,11 +77,13 @@ struct AdjDev {
     const double* src;    // [rows][stride]
     unsigned stride;
     unsigned n;           // forward step being reversed; sources of sample n+1 enter
-    // graph replay of the reverse sweep: n from device counters instead (nctr for the update
-    // kernels, gctr for the design-box sums, each stepped down on its own stream), the factors
-    // of step n in slot (n % fK) of fbase
+    // graph replay of the reverse sweep: n from device counters instead, n = counter - noff
+    // (nctr for the update kernels, gctr for the design-box sums; noff is the step's place in
+    // the captured graph, and each counter is stepped down once per replay on its own stream),
+    // the factors of step n in slot (n % fK) of fbase
     const unsigned* nctr;
     const unsigned* gctr;
+    unsigned noff;
     const float* fbase;
     unsigned fK;
     InjList injV, injI;
@@ -117,7 +119,7 @@ __device__ __forceinline__ void add_sources(const AdjDev& a, const InjList& L, u
     if (L.count == 0 || o < L.lo || o > L.hi) return;
     for (unsigned k = 0; k < L.count; ++k)
         if (L.cell[k] == o) {
-            const unsigned n = a.nctr ? *a.nctr : a.n;
+            const unsigned n = a.nctr ? *a.nctr - a.noff : a.n;
             const float v = (float)(a.src[(unsigned long long)L.row[k] * a.stride + n + 1] * L.coef[k]);
             const int m = L.comp[k];                       // constant indices keep s in registers
             if (m == 0) s[0] = fadd(s[0], v);
@@ -271,7 +273,7 @@ template <bool CURR>
 __device__ __forceinline__ void adj_src_group(const AdjDev& a, const SplitDev& sp, unsigned j);
 
 template <bool CURR>
-__global__ void __launch_bounds__(256, 1) k_adj_reg4(const __grid_constant__ AdjDev a, const __grid_constant__ SplitDev sp)
+__global__ void __launch_bounds__(256, 3) k_adj_reg4(const __grid_constant__ AdjDev a, const __grid_constant__ SplitDev sp)
 {
     const GridDev& g = a.g;
     const unsigned b = blockIdx.x;
@@ -517,7 +519,7 @@ __global__ void __launch_bounds__(256) k_adj_grad(AdjDev a)
     const unsigned x = a.b0[0] + bx, y = a.b0[1] + by, z = a.b0[2] + bz;
     const unsigned long long o = ((unsigned long long)x * g.Ny + y) * g.Pz + z;
     const float* fv = a.fv;
-    if (a.gctr) fv = a.fbase + (size_t)(*a.gctr % a.fK) * 6u * a.B;
+    if (a.gctr) fv = a.fbase + (size_t)((*a.gctr - a.noff) % a.fK) * 6u * a.B;
     const float* fc = fv + 3u * a.B;
     float vv[3], vi[3];
     coef_v(g, o, vv, vi);
@@ -597,14 +599,14 @@ __global__ void k_adj_factors(AdjDev a, float* base, const unsigned* counter, un
     fv[2 * a.B + kb] = g.V[2 * S + o];
 }
 
-__global__ void k_inc(unsigned* c)
+__global__ void k_inc(unsigned* c, unsigned by = 1u)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *c += 1u;
+    if (threadIdx.x == 0 && blockIdx.x == 0) *c += by;
 }
 
-__global__ void k_dec(unsigned* c)
+__global__ void k_dec(unsigned* c, unsigned by = 1u)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *c -= 1u;
+    if (threadIdx.x == 0 && blockIdx.x == 0) *c -= by;
 }
 
 }  // namespace
@@ -713,17 +715,26 @@ unsigned recompute_launches(const oems_cuda_engine* e)
 
 // one forward step without processing, the step counter being rec_numTS; returns the launches.
 // fac != nullptr: the voltage update writes the design-box factors of this step itself.
-unsigned recompute_step(oems_cuda_engine* e, oems_adjoint_state* s, const FacOut* fac = nullptr)
+// toff: the step's place after the counter (inside a captured run of steps whose counter is
+// stepped once at its end; inc = false leaves the counter to that)
+unsigned recompute_step(oems_cuda_engine* e, oems_adjoint_state* s, const FacOut* fac = nullptr, unsigned toff = 0,
+                        bool inc = true)
 {
     cudaStream_t st = e->stream;
     // two update launches (the split's region kernel and main box count two each) and k_inc
     const unsigned per_update = (e->use_split && e->splitV.v4) ? 2u : 1u;
-    unsigned L = 2 * per_update + 1;
+    unsigned L = 2 * per_update + (inc ? 1u : 0u);
     launch_update(e, false, st, nullptr, fac);
-    if (e->excV.count) { k_excitation<<<(e->excV.count + 127) / 128, 128, 0, st>>>(e->dV, e->excV, s->rec_numTS); ++L; }
+    if (e->excV.count) {
+        k_excitation<<<(e->excV.count + 127) / 128, 128, 0, st>>>(e->dV, e->excV, s->rec_numTS, toff);
+        ++L;
+    }
     launch_update(e, true, st);
-    if (e->excI.count) { k_excitation<<<(e->excI.count + 127) / 128, 128, 0, st>>>(e->dI, e->excI, s->rec_numTS); ++L; }
-    k_inc<<<1, 32, 0, st>>>(s->rec_numTS);
+    if (e->excI.count) {
+        k_excitation<<<(e->excI.count + 127) / 128, 128, 0, st>>>(e->dI, e->excI, s->rec_numTS, toff);
+        ++L;
+    }
+    if (inc) k_inc<<<1, 32, 0, st>>>(s->rec_numTS);
     return L;
 }
 
@@ -1036,7 +1047,7 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
     if (s->K) {
         const unsigned rec = recompute_launches(e);
         lps += rec + (s->box4 ? 0u : 1u);
-        if (s->box4 && s->K % 16 == 0) lps += 1u + (d.B ? 1u : 0u);
+        // (graph replay adds two counter launches per 16 steps)
     }
     const unsigned bu = e->splitI.main_blocks + e->splitI.first_block[e->splitI.nreg];
     const unsigned bw = e->splitV.main_blocks + e->splitV.first_block[e->splitV.nreg];
@@ -1118,13 +1129,18 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
         cudaGraphExec_t rgraph[FB] = {};
         if (s->box4 && s->K % RG == 0) {
             for (unsigned hb = 0; hb < FB && rc == OEMS_OK; ++hb) {
-                const FacOut fo = fac_out(hb);
+                FacOut fo = fac_out(hb);
                 cudaGraph_t graph = nullptr;
                 if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
                     rc = afail(e, OEMS_ERR_CUDA, "recompute graph capture");
                     break;
                 }
-                for (unsigned j = 0; j < RG; ++j) recompute_step(e, s, &fo);
+                // step j runs at counter + j; the counter steps once at the end
+                for (unsigned j = 0; j < RG; ++j) {
+                    fo.coff = j;
+                    recompute_step(e, s, &fo, j, false);
+                }
+                k_inc<<<1, 32, 0, st>>>(s->rec_numTS, RG);
                 if (cudaStreamEndCapture(st, &graph) != cudaSuccess ||
                     cudaGraphInstantiate(&rgraph[hb], graph, 0) != cudaSuccess)
                     rc = afail(e, OEMS_ERR_CUDA, "recompute graph");
@@ -1146,12 +1162,18 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
                     rc = afail(e, OEMS_ERR_CUDA, "reverse graph capture");
                     break;
                 }
-                // (an event of its own: the direct steps never wait on one recorded in a capture)
+                // (an event of its own: the direct steps never wait on one recorded in a capture);
+                // step j reverses n = counter - j, and the counters step down by RG at the end
                 for (unsigned j = 0; j < RG; ++j) {
-                    reverse_box4(dg, s->rs, j > 0, dg.gctr ? s->rev_ng : nullptr, s->ev_grad_c);
-                    k_dec<<<1, 32, 0, s->rs>>>(s->rev_n);
+                    dg.noff = j;
+                    reverse_box4(dg, s->rs, j > 0, nullptr, s->ev_grad_c);
                 }
-                if (d.B) cudaStreamWaitEvent(s->rs, s->ev_grad_c, 0);   // the last sums rejoin the graph
+                k_dec<<<1, 32, 0, s->rs>>>(s->rev_n, RG);
+                if (d.B) {
+                    k_dec<<<1, 32, 0, s->gs>>>(s->rev_ng, RG);                // after the last sums
+                    cudaEventRecord(s->ev_grad_c, s->gs);
+                    cudaStreamWaitEvent(s->rs, s->ev_grad_c, 0);            // the sums rejoin the graph
+                }
                 if (cudaStreamEndCapture(s->rs, &graph) != cudaSuccess ||
                     cudaGraphInstantiate(&vgraph[hb], graph, 0) != cudaSuccess)
                     rc = afail(e, OEMS_ERR_CUDA, "reverse graph");

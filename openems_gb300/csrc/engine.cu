@@ -194,6 +194,12 @@ void oems_cuda_destroy(oems_cuda_engine* e)
     }
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
+    if (e->stream_se) {
+        cudaStreamSynchronize(e->stream_se);
+        cudaStreamDestroy(e->stream_se);
+    }
+    for (cudaEvent_t ev : {e->ev_se_fork, e->ev_se_a, e->ev_se_b})
+        if (ev) cudaEventDestroy(ev);
     if (e->stream) cudaStreamDestroy(e->stream);
     if (e->pcache.pin) cudaFreeHost(e->pcache.pin);
     if (e->latest_host) cudaFreeHost(e->latest_host);
@@ -835,6 +841,14 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof, uns
     launch_update(e, false, s);
     post();
     ++L;
+    // the split step end (inside sequences; a single step keeps the one launch): the previous
+    // step's current-side part ran beside this voltage update; it bumps numTS, which the hooks
+    // below read
+    const bool se_split = e->se_split && !prof && seq != 3;
+    if (se_split && e->se_pending) {
+        cudaStreamWaitEvent(s, e->ev_se_b, 0);
+        e->se_pending = false;
+    }
     if (park) { pre(OEMS_KC_MUR); k_mur_zpost<<<park_blocks, blk, 0, s>>>(g, e->murdev); post(); ++L; }
     const unsigned cyl_v = g.Nx * g.Nz, cyl_i = (g.Nx - 1) * (g.Nz - 1);
     if (e->cyl.closed) {   // post-voltage hook, priority 1e5: before TFSF and Mur
@@ -873,6 +887,14 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof, uns
             for (const auto& l : e->lorV) { pre(OEMS_KC_LORENTZ); k_lorentz_carry<<<(l.count + 255) / 256, blk, 0, s>>>(e->dV, e->S, l); post(); ++L; }
     }
     // ---- currents
+    if (se_split) {
+        // the voltage-side probes and dumps beside the current update (which does not write V)
+        cudaEventRecord(e->ev_se_fork, s);
+        cudaStreamWaitEvent(e->stream_se, e->ev_se_fork, 0);
+        k_step_end<<<e->stepend_blocks, blk, 0, e->stream_se>>>(g, e->stepend, 0);
+        cudaEventRecord(e->ev_se_a, e->stream_se);
+        ++L;
+    }
     if (pre_i)
         for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_pre<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
     pre(OEMS_KC_UPDATE_I);
@@ -895,9 +917,25 @@ int enqueue_step(oems_cuda_engine* e, unsigned* nlaunch, StepProfiler* prof, uns
     if (carry_i)
         for (const auto& l : e->lorI) { pre(OEMS_KC_LORENTZ); k_lorentz_carry<<<(l.count + 255) / 256, blk, 0, s>>>(e->dI, e->S, l); post(); ++L; }
     // ---- processing + numTS
-    pre(OEMS_KC_STEP_END);
-    k_step_end<<<e->stepend_blocks, blk, 0, s>>>(g, e->stepend); ++L;
-    post();
+    if (se_split) {
+        // the voltage side is done before the next voltage update; the current side (and the
+        // numTS bump) runs beside it, joined there (or here at a sequence's last step)
+        cudaStreamWaitEvent(s, e->ev_se_a, 0);
+        cudaEventRecord(e->ev_se_fork, s);
+        cudaStreamWaitEvent(e->stream_se, e->ev_se_fork, 0);
+        k_step_end<<<e->stepend_blocks, blk, 0, e->stream_se>>>(g, e->stepend, 1);
+        cudaEventRecord(e->ev_se_b, e->stream_se);
+        ++L;
+        e->se_pending = true;
+        if (seq & 2) {
+            cudaStreamWaitEvent(s, e->ev_se_b, 0);
+            e->se_pending = false;
+        }
+    } else {
+        pre(OEMS_KC_STEP_END);
+        k_step_end<<<e->stepend_blocks, blk, 0, s>>>(g, e->stepend); ++L;
+        post();
+    }
     if (nlaunch) *nlaunch = L;
     cudaError_t c = cudaGetLastError();
     if (c != cudaSuccess) return cuda_fail(e, c, "kernel launch");
@@ -1652,6 +1690,20 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     s.numTS = e->d_numTS;
     s.blocks_done = e->d_blocks_done;
     e->stepend_blocks = block0.back();
+    // the step end in two parts beside the updates (OEMS_CUDA_SE_SPLIT=0: one launch at the end):
+    // only where no hook before the voltage excitation reads numTS (no Mur, TFSF or lumped RLC)
+    // and the time-domain dump pipeline is off
+    {
+        const char* ss = getenv("OEMS_CUDA_SE_SPLIT");
+        e->se_split = e->mur.empty() && !e->has_tfsf && e->rlc_host.off.empty() && !e->has_td &&
+                      !(ss && ss[0] == '0');
+        if (e->se_split) {
+            CK(cudaStreamCreateWithFlags(&e->stream_se, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&e->ev_se_fork, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&e->ev_se_a, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&e->ev_se_b, cudaEventDisableTiming));
+        }
+    }
 
     // energy scratch
     e->energy_blocks = 1024;

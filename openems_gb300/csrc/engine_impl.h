@@ -183,12 +183,17 @@ struct oems_cuda_engine {
     bool mur_v4 = false;
     // dispersive apply + next pre as one launch inside enqueued sequences (k_lorentz_carry)
     bool lor_carry_v = false, lor_carry_i = false;
-    bool vtail = false;
+    bool vtail = false;              // k_vtail: Mur apply + carry + excitation as one launch
     // newest-sample reads of the probes (oems_cuda_read_probe_range): one pinned fetch per step
     ProbeCache pcache;
     double* latest_host = nullptr;   // mapped: each probe's newest sample (ProbeDev::latest)
     unsigned* latest_slot_host = nullptr;
-    unsigned series_gen = 0;         // bumped by restore              // k_vtail: Mur apply + carry + excitation as one launch
+    unsigned series_gen = 0;         // bumped by restore
+    // the step end in two parts on a side stream (k_step_end part 0 beside the current update,
+    // part 1 beside the next voltage update); se_pending: part 1 forked, not yet joined
+    bool se_split = false, se_pending = false;
+    cudaStream_t stream_se = nullptr;
+    cudaEvent_t ev_se_fork = nullptr, ev_se_a = nullptr, ev_se_b = nullptr;
 
     // one-kernel step (the plane march, march.cuh): the K-step graph alternates buffer sets A
     // (dV, dI) and B (dV2, dI2); K is even, so the state is in A whenever the host sees it

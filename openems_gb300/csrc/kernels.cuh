@@ -535,6 +535,7 @@ struct FacOut {
     const unsigned* counter;
     unsigned modulo;
     unsigned b0[3], bn[3], B;
+    unsigned coff;               // the slot is (*counter + coff) % modulo
 };
 
 template <typename IX = unsigned, bool FAC = false>
@@ -559,7 +560,7 @@ __device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, un
     const unsigned fbx = x - (FAC ? fo->b0[0] : 0u), fby = y - (FAC ? fo->b0[1] : 0u);
     const bool frow = FAC && fbx < fo->bn[0] && fby < fo->bn[1];
     float* fslot = nullptr;
-    if (frow) fslot = fo->base + (size_t)(__ldg(fo->counter) % fo->modulo) * 6u * fo->B;
+    if (frow) fslot = fo->base + (size_t)((__ldg(fo->counter) + fo->coff) % fo->modulo) * 6u * fo->B;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (z0 + k >= g.Nz) break;
@@ -1038,9 +1039,11 @@ __device__ __forceinline__ void exc_point(float* __restrict__ F, const ExcDev& e
     F[o] = fadd(F[o], fmul(e.amp[k], e.sig[exc_pos]));
 }
 
-static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsigned* __restrict__ numTS)
+// toff: added to the step counter (steps of a captured run whose counter moves once at its end)
+static __global__ void k_excitation(float* __restrict__ F, ExcDev e, const unsigned* __restrict__ numTS,
+                                    unsigned toff = 0)
 {
-    exc_point(F, e, blockIdx.x * blockDim.x + threadIdx.x, *numTS);
+    exc_point(F, e, blockIdx.x * blockDim.x + threadIdx.x, *numTS + toff);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1671,17 +1674,25 @@ static __device__ void dump_field(const GridDev& g, const DumpDev& d, const unsi
 // One launch: block 0 warps evaluate the probes; blocks [dump_block0[k], dump_block0[k+1])
 // handle dump k (one thread per box position, all frequencies).  The last block to finish
 // increments numTS (threadfence + completion counter), so every block read the same ts.
-static __global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s)
+// part -1: everything; part 0: the probes and dumps that read V (voltage and E-field probes, E
+// dumps); part 1: those that read I (current and H-field probes, H dumps) and the numTS
+// increment.  The parts let the engine run part 0 beside the current update (which does not
+// write V) and part 1 beside the next voltage update (which does not write I).
+static __global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s, int part = -1)
 {
     const unsigned ts = *s.numTS + 1;   // the step just completed
     if (blockIdx.x == 0) {
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        for (int p = warp; p < s.nprobe; p += blockDim.x >> 5) probe_eval(g, s.probes[p], ts, lane);
+        for (int p = warp; p < s.nprobe; p += blockDim.x >> 5) {
+            const ProbeDev& q = s.probes[p];
+            const int side = (q.type == 1 || q.type == 3) ? 1 : 0;
+            if (part < 0 || part == side) probe_eval(g, q, ts, lane);
+        }
     } else {
         // find the dump of this block
         int k = 0;
         while (k + 1 < s.ndump && blockIdx.x >= s.dump_block0[k + 1]) ++k;
-        if (s.ndump > 0) {
+        if (s.ndump > 0 && (part < 0 || part == (s.dumps[k].field == 1 ? 1 : 0))) {
             const DumpDev& d = s.dumps[k];
             const unsigned q = (blockIdx.x - s.dump_block0[k]) * blockDim.x + threadIdx.x;
             if (d.td) {
@@ -1722,6 +1733,7 @@ static __global__ void __launch_bounds__(256) k_step_end(GridDev g, StepEndDev s
         }
     }
     // completion: last block bumps numTS
+    if (part == 0) return;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();

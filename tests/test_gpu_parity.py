@@ -247,6 +247,26 @@ def test_probe_range_newest_samples_and_restore(cuda_lib):
         assert bits_equal(after[p].ravel(), np.asarray(g.probe_series(p))[21:22].ravel()), p
 
 
+@pytest.mark.parametrize("split", ["1", "0"])
+def test_split_step_end_bit_exact_against_oracle(cuda_lib, monkeypatch, split):
+    """Without Mur, TFSF or lumped RLC the step end runs as two parts on a side stream: the
+    voltage-side probes and dumps beside the current update, the current side (and the step
+    counter) beside the next voltage update.  Probes, FD dumps and fields equal the oracle's bit
+    for bit over mixed chunk lengths either way; the split costs one launch more per step."""
+    monkeypatch.setenv("OEMS_CUDA_SE_SPLIT", split)
+    op = configs.patch(shape=(56, 52, 36), steps=250)
+    assert not op.mur and (op.vprobes or op.iprobes)
+    g, r = _run_pair(op, 250, chunks=(1, 7, 16, 33))
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, bad
+    monkeypatch.setenv("OEMS_CUDA_SE_SPLIT", "0")
+    one = Engine_CUDA(op, 10)
+    n_one = one.launches_per_step()
+    one.close()
+    assert g.launches_per_step() == n_one + (1 if split == "1" else 0)
+
+
 REG4_CASES = [
     ("patch_pml8", lambda: configs.patch(shape=(56, 52, 36), steps=220, with_nf2ff=False), 220),
     ("plane_wave_pml4", lambda: configs.plane_wave(n=(28, 24, 32), pml=4, steps=200), 200),
