@@ -492,10 +492,6 @@ def main():
         op, desc = build_workload(args.workload, shape)
     t_build = time.perf_counter() - t_build
     t_build_host = None
-    if rank == 0 and dev == "cuda" and not args.no_cpu_baseline:
-        t0 = time.perf_counter()
-        build_workload(args.workload, shape)
-        t_build_host = time.perf_counter() - t0
 
     dist = None
     if world > 1:
@@ -617,6 +613,13 @@ def main():
                 "sample": f"{n} timesteps of the full {desc} workload ({sec:.1f} s, setup excluded)"}
         if not args.no_cpu_sweep:
             sweep = cpu_thread_sweep(op, args.sweep_budget, threads)
+
+    # the host build for comparison, last: its several GB of temporary arrays would otherwise
+    # disturb the allocations of the whole-job measurement above
+    if rank == 0 and dev == "cuda" and not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        build_workload(args.workload, shape)
+        t_build_host = time.perf_counter() - t0
 
     if rank == 0:
         line = {
