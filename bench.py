@@ -192,6 +192,28 @@ def cpu_thread_sweep(op, budget_s, nproc):
     return out
 
 
+def processing_loop(eng, steps, slot):
+    """openEMS's processing loop through the C ABI: per step oems_cuda_iterate(1), then a read of
+    every probe's newest sample.  Python's cyclic garbage collector is paused for the loop (it
+    allocates only the small result arrays): a collection sweeping the objects the earlier
+    measurements left behind would otherwise land in the timing.  Returns the wall seconds."""
+    import gc
+    pids = eng.vprobe_ids + eng.iprobe_ids
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            eng.IterateTS(1)
+            slot += 1
+            for pid in pids:
+                eng.probe_range(pid, slot, 1)
+        return time.perf_counter() - t0
+    finally:
+        if was:
+            gc.enable()
+
+
 def measure_config(name, steps, e2e_steps=200, cpu_budget=0.0):
     """One more configuration on the GPU: device-timed MCells/s over `steps` replayed steps, and
     MCells/s end to end through the C ABI (iterate(1) + a synchronous read of every probe's new
@@ -208,15 +230,7 @@ def measure_config(name, steps, e2e_steps=200, cpu_budget=0.0):
     eng.IterateTS(80)               # warm-up; also where the engine picks its step form (>= 4 graphs)
     eng.sync()
     ms = eng.timed_iterate(steps)
-    pids = eng.vprobe_ids + eng.iprobe_ids
-    slot = eng.GetNumberOfTimesteps()
-    t1 = time.perf_counter()
-    for _ in range(e2e_steps):
-        eng.IterateTS(1)
-        slot += 1
-        for pid in pids:
-            eng.probe_range(pid, slot, 1)
-    e2e_s = time.perf_counter() - t1
+    e2e_s = processing_loop(eng, e2e_steps, eng.GetNumberOfTimesteps())
     state_mb = 24 * cells / 1e6
     out = {"workload": desc, "cells": cells, "steps": steps, "mcells_s": cells * steps / (ms / 1e3) / 1e6,
            "ms_per_step": ms / steps, "e2e_mcells_s": cells * e2e_steps / e2e_s / 1e6, "e2e_steps": e2e_steps,
@@ -263,14 +277,8 @@ def measure_batched(count):
     loop_s = 0.0
     for op, s in inst:
         e = Engine_CUDA(op, s)
-        pids = e.vprobe_ids + e.iprobe_ids
         e.sync()
-        t = time.perf_counter()
-        for k in range(1, s + 1):
-            e.IterateTS(1)
-            for pid in pids:
-                e.probe_range(pid, k, 1)
-        loop_s += time.perf_counter() - t
+        loop_s += processing_loop(e, s, 0)
         e.close()
     engines = [Engine_CUDA(op, s) for op, s in inst]
     for e in engines:
@@ -546,14 +554,7 @@ def main():
 
     # ---- end to end through the C ABI: iterate(1) + D2H of the newest probe samples -------
     pids = eng.vprobe_ids + eng.iprobe_ids
-    slot = eng.GetNumberOfTimesteps()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        eng.IterateTS(1)
-        slot += 1
-        for pid in pids:
-            eng.probe_range(pid, slot, 1)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = processing_loop(eng, e2e_steps, eng.GetNumberOfTimesteps())
     e2e = {"value": cells * e2e_steps / e2e_s / 1e6 * world, "unit": "MCells/s", "h2d_bytes_per_step": 0,
            "d2h_bytes_per_step": 8 * len(pids), "steps": e2e_steps,
            "note": "per step: oems_cuda_iterate(1) then oems_cuda_read_probe_range of every probe (synchronous)"}
@@ -570,13 +571,7 @@ def main():
         t1 = time.perf_counter()
         jeng = Engine_CUDA(jop, args.job_steps + 2)
         t2 = time.perf_counter()
-        jp = jeng.vprobe_ids + jeng.iprobe_ids
-        jslot = 0
-        for _ in range(args.job_steps):
-            jeng.IterateTS(1)
-            jslot += 1
-            for pid in jp:
-                jeng.probe_range(pid, jslot, 1)
+        processing_loop(jeng, args.job_steps, 0)
         t3 = time.perf_counter()
         jeng.close()
         t4 = time.perf_counter()
