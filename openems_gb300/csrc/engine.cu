@@ -172,6 +172,7 @@ int oems_cuda_create(const unsigned int num_lines[3], double dt, int device, oem
     if ((rc = dalloc(e, &e->dV, 3 * (size_t)e->S, true, true))) return rc;
     if ((rc = dalloc(e, &e->dI, 3 * (size_t)e->S, true, true))) return rc;
     if ((rc = dalloc(e, &e->d_numTS, 1, true, true))) return rc;
+    if ((rc = dalloc(e, &e->d_zero, 1, true))) return rc;
     if ((rc = dalloc(e, &e->d_blocks_done, 1, true))) return rc;
     CK(cudaStreamSynchronize(e->stream));
     return OEMS_OK;
@@ -673,7 +674,10 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
 {
     const GridDev& g = e->grid;
     const MurDev& m = e->murdev;
-    const unsigned* ts = e->d_numTS;
+    // the lane-parallel Mur form has every wall active from step 0, so its hooks' activity test
+    // reads a constant 0 instead of the step counter (which a concurrent step-end part may be
+    // advancing)
+    const unsigned* ts = m.lanes ? e->d_zero : e->d_numTS;
     // name != nullptr: report the kernel this configuration launches, launch nothing
     auto go = [&](const char* n) {
         if (name) *name = n;
@@ -1691,12 +1695,12 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     s.blocks_done = e->d_blocks_done;
     e->stepend_blocks = block0.back();
     // the step end in two parts beside the updates (OEMS_CUDA_SE_SPLIT=0: one launch at the end):
-    // only where no hook before the voltage excitation reads numTS (no Mur, TFSF or lumped RLC)
-    // and the time-domain dump pipeline is off
+    // only where nothing in the voltage update reads numTS (no TFSF or lumped RLC, Mur only in
+    // the lane-parallel form, which reads a constant) and the time-domain dump pipeline is off
     {
         const char* ss = getenv("OEMS_CUDA_SE_SPLIT");
-        e->se_split = e->mur.empty() && !e->has_tfsf && e->rlc_host.off.empty() && !e->has_td &&
-                      !(ss && ss[0] == '0');
+        const bool mur_ok = e->mur.empty() || (e->murdev.lanes && !e->mur_separate);
+        e->se_split = mur_ok && !e->has_tfsf && e->rlc_host.off.empty() && !e->has_td && !(ss && ss[0] == '0');
         if (e->se_split) {
             CK(cudaStreamCreateWithFlags(&e->stream_se, cudaStreamNonBlocking));
             CK(cudaEventCreateWithFlags(&e->ev_se_fork, cudaEventDisableTiming));

@@ -143,6 +143,7 @@ struct oems_cuda_engine {
     bool inited = false;
     unsigned max_ts = 0;
     unsigned* d_numTS = nullptr;
+    unsigned* d_zero = nullptr;       // a device 0 (the lane-parallel Mur hooks' step)
     unsigned* d_blocks_done = nullptr;
     unsigned host_numTS = 0;
     GridDev grid{};

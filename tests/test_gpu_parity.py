@@ -119,6 +119,7 @@ def test_separate_mur_hooks_bit_exact_against_oracle(cuda_lib, monkeypatch, name
     the voltage update: the same fields, bit for bit, with two more launches per step."""
     op = fn()
     monkeypatch.setenv("OEMS_CUDA_LOR_CARRY", "0")     # separate Mur hooks keep the dispersive apply apart
+    monkeypatch.setenv("OEMS_CUDA_SE_SPLIT", "0")      # and the step end in one launch
     fused = Engine_CUDA(op, steps)
     n_fused = fused.launches_per_step()
     fused.close()
