@@ -92,7 +92,7 @@ struct AdjDev {
 __device__ __forceinline__ void coef_v(const GridDev& g, unsigned long long o, float vv[3], float vi[3])
 {
     if (g.idx) {
-        const unsigned c = __ldg(g.idx + o);
+        const unsigned c = op_cls(g, o);
         const float4 a = __ldg(g.tabV + 2 * c), b = __ldg(g.tabV + 2 * c + 1);
         vv[0] = a.x; vv[1] = a.y; vv[2] = a.z; vi[0] = a.w; vi[1] = b.x; vi[2] = b.y;
     } else {
@@ -104,7 +104,7 @@ __device__ __forceinline__ void coef_v(const GridDev& g, unsigned long long o, f
 __device__ __forceinline__ void coef_i(const GridDev& g, unsigned long long o, float ii[3], float iv[3])
 {
     if (g.idx) {
-        const unsigned c = __ldg(g.idx + o);
+        const unsigned c = op_cls(g, o);
         const float4 a = __ldg(g.tabI + 2 * c), b = __ldg(g.tabI + 2 * c + 1);
         ii[0] = a.x; ii[1] = a.y; ii[2] = a.z; iv[0] = a.w; iv[1] = b.x; iv[2] = b.y;
     } else {
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(256, 3) k_adj_reg4(const __grid_constant__ Adj
             if (z0 + k + 1 >= g.Nz) mask &= ~(1u << k);
     const unsigned S = (unsigned)g.S, n = u.n;
     const unsigned o = (x * g.Ny + y) * g.Pz + z0;
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     unsigned ucl[4];
     ld_cls(u.cls + q.loc0, q.vec, mask, ucl);
     // the cell's adjoint state (lI / lV) and the flux adjoint (lphi / lpsi), region-local
@@ -438,7 +438,7 @@ __device__ __forceinline__ void adj_u4_group(const AdjDev& a, const SplitDev& sp
     const float w1z4 = __ldg(W + (S + o + 4)), w0z4 = __ldg(W + (o + 4));
     const float4 w2y = ldg4(W + (2 * S + o + sy)), w0y = ldg4(W + (o + sy));
     const float4 w2x = ldg4(W + (2 * S + o + sx)), w1x = ldg4(W + (S + o + sx));
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     float4 u0 = ld4(a.U + o), u1 = ld4(a.U + (S + o)), u2 = ld4(a.U + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
     const bool src = SRC && a.injI.count && (unsigned long long)o + 3 >= a.injI.lo && (unsigned long long)o <= a.injI.hi;
@@ -477,7 +477,7 @@ __device__ __forceinline__ void adj_w4_group(const AdjDev& a, const SplitDev& sp
     const float u1m = z0 ? __ldg(U + (S + o - 1)) : 0.f, u0m = z0 ? __ldg(U + (o - 1)) : 0.f;
     const float4 u2y = ldg4(U + (2 * S + o - sy)), u0y = ldg4(U + (o - sy));
     const float4 u2x = ldg4(U + (2 * S + o - sx)), u1x = ldg4(U + (S + o - sx));
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     float4 n0 = ld4(a.W + o), n1 = ld4(a.W + (S + o)), n2 = ld4(a.W + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
     const bool src = SRC && a.injV.count && (unsigned long long)o + 3 >= a.injV.lo && (unsigned long long)o <= a.injV.hi;

@@ -1104,6 +1104,19 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     g.V = e->dV; g.I = e->dI;
     g.idx = e->didx; g.tabV = e->dtabV; g.tabI = e->dtabI;
     g.vv = e->dvv; g.vi = e->dvi; g.ii = e->dii; g.iv = e->div;
+    // the class index in 16 bits where every class fits: 2 bytes less per cell and half-step for
+    // every update kernel (OEMS_CUDA_IDX16=0 keeps the 32-bit index)
+    g.idx16 = nullptr;
+    {
+        const char* ix = getenv("OEMS_CUDA_IDX16");
+        if (e->compressed && e->didx && e->nclasses <= 65536u && !(ix && ix[0] == '0')) {
+            unsigned short* d16 = nullptr;
+            if ((rc = dalloc(e, &d16, (size_t)e->S, false))) return rc;
+            k_narrow_index<<<(unsigned)((e->S + 255) / 256), 256, 0, e->stream>>>(d16, e->didx, e->S);
+            CK(cudaGetLastError());
+            g.idx16 = d16;
+        }
+    }
 
     // float4 update kernels (OEMS_CUDA_SCALAR=1 keeps the one-cell-per-thread form)
     {

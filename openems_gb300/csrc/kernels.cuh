@@ -42,6 +42,7 @@ struct GridDev {
     float* I;
     // coefficients: compressed (idx != nullptr) or dense
     const unsigned* idx;        // [Nx][Ny][Pz]
+    const unsigned short* idx16;  // the same in 16 bits when every class fits; read instead of idx
     const float4* tabV;         // [U][2]: (vv0,vv1,vv2,vi0) (vi1,vi2,-,-)
     const float4* tabI;         // [U][2]: (ii0,ii1,ii2,iv0) (iv1,iv2,-,-)
     const float* vv;            // dense [3][S]
@@ -51,6 +52,28 @@ struct GridDev {
     int nupml;
     UpmlDev upml[OEMS_MAX_UPML];
 };
+
+// the 16-bit copy of the class index (every class < 65,536)
+static __global__ void k_narrow_index(unsigned short* __restrict__ dst, const unsigned* __restrict__ src,
+                                      unsigned long long n)
+{
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (unsigned short)src[i];
+}
+
+// the operator class of cell o, and of the four cells o..o+3 (o a multiple of 4)
+__device__ __forceinline__ unsigned op_cls(const GridDev& g, unsigned long long o)
+{
+    return g.idx16 ? (unsigned)__ldg(g.idx16 + o) : __ldg(g.idx + o);
+}
+__device__ __forceinline__ uint4 op_cls4(const GridDev& g, unsigned long long o)
+{
+    if (g.idx16) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(g.idx16 + o));
+        return make_uint4(v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16);
+    }
+    return __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+}
 
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
@@ -296,7 +319,7 @@ __device__ __forceinline__ void update_v_cell(const GridDev& g, unsigned x, unsi
 
     float vv0, vv1, vv2, vi0, vi1, vi2;
     if (COMPRESSED) {
-        const unsigned c = __ldg(g.idx + o);
+        const unsigned c = op_cls(g, o);
         const float4 a = __ldg(g.tabV + 2 * c), b = __ldg(g.tabV + 2 * c + 1);
         vv0 = a.x; vv1 = a.y; vv2 = a.z; vi0 = a.w; vi1 = b.x; vi2 = b.y;
     } else {
@@ -373,7 +396,7 @@ __device__ __forceinline__ void update_i_cell(const GridDev& g, unsigned x, unsi
 
     float ii0, ii1, ii2, iv0, iv1, iv2;
     if (COMPRESSED) {
-        const unsigned c = __ldg(g.idx + o);
+        const unsigned c = op_cls(g, o);
         const float4 a = __ldg(g.tabI + 2 * c), b = __ldg(g.tabI + 2 * c + 1);
         ii0 = a.x; ii1 = a.y; ii2 = a.z; iv0 = a.w; iv1 = b.x; iv2 = b.y;
     } else {
@@ -487,7 +510,7 @@ __device__ __forceinline__ void update_i4_cells(const GridDev& g, unsigned x, un
     const float4 w2y = ldg4(V + (2 * S + o + sy)), w0y = ldg4(V + (o + sy));
     const float4 w2x = ldg4(V + (2 * S + o + sx)), w1x = ldg4(V + (S + o + sx));
     const float w0z4 = __ldg(V + (o + 4)), w1z4 = __ldg(V + (S + o + 4));
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     float4 a0 = ld4(I + o), a1 = ld4(I + (S + o)), a2 = ld4(I + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
 #pragma unroll
@@ -553,7 +576,7 @@ __device__ __forceinline__ void update_v4_cells(const GridDev& g, unsigned x, un
     const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
     // the float before the vector; at z = 0 the cell's own value
     const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
     // FAC: this row's design cells (the box's rows are x, y inside it; lanes z inside it)
@@ -620,7 +643,7 @@ __device__ __forceinline__ void mur_wall_v4(const GridDev& g, const MurDev& m, u
     const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
     const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
     const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     const float4 v0 = ld4(V + o), v1 = ld4(V + (S + o)), v2 = ld4(V + (2 * S + o));
     float4 n0 = v0, n1 = v1, n2 = v2;
     const unsigned cls[4] = {ci.x, ci.y, ci.z, ci.w};
@@ -681,7 +704,7 @@ __device__ __forceinline__ void mur_zwall_v4(const GridDev& g, const MurDev& m, 
     const float4 i2y = ldg4(I + (2 * S + o - sy)), i0y = ldg4(I + (o - sy));
     const float4 i2x = ldg4(I + (2 * S + o - sx)), i1x = ldg4(I + (S + o - sx));
     const float i1m = z0 ? __ldg(I + (S + o - 1)) : i1.x, i0m = z0 ? __ldg(I + (o - 1)) : i0.x;
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     float4 n0 = ld4(V + o), n1 = ld4(V + (S + o)), n2 = ld4(V + (2 * S + o));
     // pre-voltage part, from the old values
     const float pre0 = fsub(f4(n0, ks), fmul(cP, f4(n0, kl)));
@@ -938,7 +961,7 @@ __global__ void __launch_bounds__(256, 3) k_update_reg4(const __grid_constant__ 
             if (z0 + k + 1 >= g.Nz) mask &= ~(1u << k);
     const unsigned S = (unsigned)g.S, n = u.n;
     const unsigned o = (x * g.Ny + y) * g.Pz + z0;
-    const uint4 ci = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+    const uint4 ci = op_cls4(g, o);
     unsigned ucl[4];
     ld_cls(u.cls + q.loc0, q.vec, mask, ucl);
     float* __restrict__ flux = CURR ? u.iflux : u.vflux;

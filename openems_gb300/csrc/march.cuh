@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(512, MINB) k_step_march(const __grid_constant_
         vq[0] = ldg4(g.V + o);
         vq[1] = ldg4(g.V + S + o);
         vq[2] = ldg4(g.V + 2 * S + o);
-        cq = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+        cq = op_cls4(g, o);
     }
     bool w = mbar_wait(&bar[0], 0u);
     if (w) {                                                // a copy whose wait ran out is still in flight
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(512, MINB) k_step_march(const __grid_constant_
             vq[0] = ldg4(g.V + o);
             vq[1] = ldg4(g.V + S + o);
             vq[2] = ldg4(g.V + 2 * S + o);
-            cq = __ldg(reinterpret_cast<const uint4*>(g.idx + o));
+            cq = op_cls4(g, o);
         }
         float* Vc = vbase + ((x - xa) & 1u) * VF;
         const float* Vp = vbase + ((x - xa + 1) & 1u) * VF;

@@ -268,6 +268,27 @@ def test_split_step_end_bit_exact_against_oracle(cuda_lib, monkeypatch, split):
     assert g.launches_per_step() == n_one + (1 if split == "1" else 0)
 
 
+IDX_CASES = [
+    ("stress_small", lambda: configs.stress(shape=(40, 36, 30), steps=150, nblocks=16, seed=1), 150),
+    ("patch_small", lambda: configs.patch(shape=(56, 52, 36), steps=220), 220),
+    ("mixed", configs.small_mixed, 200),
+]
+
+
+@pytest.mark.parametrize("narrow", ["1", "0"])
+@pytest.mark.parametrize("name,fn,steps", IDX_CASES)
+def test_class_index_widths_bit_exact_against_oracle(cuda_lib, monkeypatch, name, fn, steps, narrow):
+    """The operator class index read in 16 bits where every class fits (default) or in 32 bits
+    (OEMS_CUDA_IDX16=0): float4, one-cell, UPML and Mur kernels all equal the oracle bit for bit."""
+    monkeypatch.setenv("OEMS_CUDA_IDX16", narrow)
+    op = fn()
+    g, r = _run_pair(op, steps, chunks=(1, 7, 16, 33))
+    assert 1 < g.operator_classes() <= 65536
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, (name, bad)
+
+
 REG4_CASES = [
     ("patch_pml8", lambda: configs.patch(shape=(56, 52, 36), steps=220, with_nf2ff=False), 220),
     ("plane_wave_pml4", lambda: configs.plane_wave(n=(28, 24, 32), pml=4, steps=200), 200),
