@@ -742,17 +742,18 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
             else { if (mode) launch_v<false, true, 1>(gv, s, g, m, ts); else launch_v<false, true, 0>(gv, s, g, m, ts); }
         } else if (e->compressed) {
             if (o32 && e->vec4 && (mode == 0 || (mode == 2 && e->mur_v4))) {
-                const dim3 gv4((plane / 4 + 255) / 256, e->N[0]);
+                const unsigned vb = e->v4_block;
+                const dim3 gv4((plane / 4 + vb - 1) / vb, e->N[0]);
                 if (mode == 2 && m.park) {
                     // every direct-column group streams; the z walls' hooks run around this launch
-                    if (go("k_update_v4w<park>")) k_update_v4w<unsigned, true><<<gv4, 256, 0, s>>>(g, m, ts, gv4.x);
+                    if (go("k_update_v4w<park>")) k_update_v4w<unsigned, true><<<gv4, vb, 0, s>>>(g, m, ts, gv4.x);
                 } else if (mode == 2) {
                     // the interior blocks, then one thread per direct column's z-wall group
-                    const unsigned walls = m.nz > 0 ? (e->N[1] * (unsigned)m.nz + 255) / 256 : 0;
+                    const unsigned walls = m.nz > 0 ? (e->N[1] * (unsigned)m.nz + vb - 1) / vb : 0;
                     const dim3 gw(gv4.x + walls, e->N[0]);
-                    if (go("k_update_v4w")) k_update_v4w<unsigned><<<gw, 256, 0, s>>>(g, m, ts, gv4.x);
+                    if (go("k_update_v4w")) k_update_v4w<unsigned><<<gw, vb, 0, s>>>(g, m, ts, gv4.x);
                 }
-                else if (go("k_update_v4")) k_update_v4<unsigned><<<gv4, 256, 0, s>>>(g);
+                else if (go("k_update_v4")) k_update_v4<unsigned><<<gv4, vb, 0, s>>>(g);
             } else if (o32) {
                 if (!go("k_update_v")) return;
                 if (mode == 2) launch_v<true, false, 2, unsigned>(gv, s, g, m, ts);
@@ -777,8 +778,9 @@ void launch_update(oems_cuda_engine* e, bool curr, cudaStream_t s, const char** 
             if (e->compressed) k_update_i<true, true><<<gi, 256, 0, s>>>(g); else k_update_i<false, true><<<gi, 256, 0, s>>>(g);
         } else if (e->compressed) {
             if (o32 && e->vec4) {
-                const dim3 gi4((plane / 4 + 255) / 256, e->N[0] - 1);
-                if (go("k_update_i4")) k_update_i4<unsigned><<<gi4, 256, 0, s>>>(g);
+                const unsigned tb = e->i4_block;
+                const dim3 gi4((plane / 4 + tb - 1) / tb, e->N[0] - 1);
+                if (go("k_update_i4")) k_update_i4<unsigned><<<gi4, tb, 0, s>>>(g);
             } else {
                 if (!go("k_update_i")) return;
                 if (o32) k_update_i<true, false, unsigned><<<gi, 256, 0, s>>>(g);
@@ -1122,6 +1124,13 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
     {
         const char* sc = getenv("OEMS_CUDA_SCALAR");
         e->vec4 = !(sc && sc[0] == '1');
+        // threads per block of the float4 updates: 128 measured faster than 256 on 512x512x256
+        // (the voltage update with the Mur walls 0.408 -> 0.394 ms, the current update 0.392 ->
+        // 0.387 ms); OEMS_CUDA_I4_BLOCK / OEMS_CUDA_V4_BLOCK = 256 restores the larger blocks
+        const char* tb = getenv("OEMS_CUDA_I4_BLOCK");
+        e->i4_block = (tb && atoi(tb) == 256) ? 256u : 128u;
+        const char* vb = getenv("OEMS_CUDA_V4_BLOCK");
+        e->v4_block = (vb && atoi(vb) == 256) ? 256u : 128u;
     }
 
     // UPML

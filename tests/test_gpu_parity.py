@@ -268,6 +268,20 @@ def test_split_step_end_bit_exact_against_oracle(cuda_lib, monkeypatch, split):
     assert g.launches_per_step() == n_one + (1 if split == "1" else 0)
 
 
+@pytest.mark.parametrize("block", ["256", "128"])
+def test_float4_block_sizes_bit_exact_against_oracle(cuda_lib, monkeypatch, block):
+    """The float4 voltage and current updates at 128 threads per block (default) and 256
+    (OEMS_CUDA_V4_BLOCK / OEMS_CUDA_I4_BLOCK): the Mur wall blocks follow the block size."""
+    monkeypatch.setenv("OEMS_CUDA_V4_BLOCK", block)
+    monkeypatch.setenv("OEMS_CUDA_I4_BLOCK", block)
+    op = configs.stress(shape=(40, 36, 30), steps=140, nblocks=16, seed=1)
+    g, r = _run_pair(op, 140, chunks=(1, 7, 16, 33))
+    assert g.update_kernels() == ("k_update_v4w", "k_update_i4")
+    res = compare_engines(g, r)
+    bad = [k for k, v in res.items() if not v]
+    assert not bad, bad
+
+
 IDX_CASES = [
     ("stress_small", lambda: configs.stress(shape=(40, 36, 30), steps=150, nblocks=16, seed=1), 150),
     ("patch_small", lambda: configs.patch(shape=(56, 52, 36), steps=220), 220),
