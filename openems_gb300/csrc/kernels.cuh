@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(256, (COMPRESSED && !MUR) ? 8 : 1)
 template <bool CURR, bool FAC = false>
 __global__ void __launch_bounds__(256, 4) k_update_box4(GridDev g, SplitDev sp, FacOut fo = FacOut{})
 {
-    unsigned t = blockIdx.x * 256u + threadIdx.x;
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= sp.main_cells4) return;
     const unsigned z = sp.z4 + ((t % sp.n4) << 2);
     t /= sp.n4;
