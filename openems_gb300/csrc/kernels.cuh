@@ -799,7 +799,8 @@ struct SplitDev {
     unsigned nreg;
     unsigned first_block[OEMS_MAX_UPML + 1];   // region r: blocks [first_block[r], first_block[r+1])
     int reg4;                                  // 1: the regions four z cells per thread (k_update_reg4)
-    unsigned first4[OEMS_MAX_UPML + 1];        // region r: its blocks of groups of four
+    unsigned first4[OEMS_MAX_UPML + 1];        // region r: its blocks of groups of four (256 threads)
+    unsigned first4h[OEMS_MAX_UPML + 1];       // the same for blocks of 128 threads
 };
 
 // The compressed-operator form without Mur hooks fits 32 registers (a few bytes spill to L1), so
@@ -946,10 +947,11 @@ template <bool CURR>
 __global__ void __launch_bounds__(256, 3) k_update_reg4(const __grid_constant__ GridDev g, const __grid_constant__ SplitDev sp)
 {
     const unsigned b = blockIdx.x;
+    const unsigned* fblk = blockDim.x == 128u ? sp.first4h : sp.first4;
     int r = 0;
-    while (r + 1 < (int)sp.nreg && b >= sp.first4[r + 1]) ++r;
+    while (r + 1 < (int)sp.nreg && b >= fblk[r + 1]) ++r;
     const UpmlDev& u = g.upml[r];
-    const unsigned j = (b - sp.first4[r]) * 256u + threadIdx.x;
+    const unsigned j = (b - fblk[r]) * blockDim.x + threadIdx.x;
     if (j >= u.nl[0] * u.nl[1] * reg_groups_per_row(u)) return;
     const RegGroup q = reg_group(u, j);
     const unsigned x = q.x, y = q.y, z0 = q.z0;

@@ -269,14 +269,20 @@ def test_split_step_end_bit_exact_against_oracle(cuda_lib, monkeypatch, split):
 
 
 @pytest.mark.parametrize("block", ["256", "128"])
-def test_float4_block_sizes_bit_exact_against_oracle(cuda_lib, monkeypatch, block):
-    """The float4 voltage and current updates at 128 threads per block (default) and 256
-    (OEMS_CUDA_V4_BLOCK / OEMS_CUDA_I4_BLOCK): the Mur wall blocks follow the block size."""
-    monkeypatch.setenv("OEMS_CUDA_V4_BLOCK", block)
-    monkeypatch.setenv("OEMS_CUDA_I4_BLOCK", block)
-    op = configs.stress(shape=(40, 36, 30), steps=140, nblocks=16, seed=1)
+@pytest.mark.parametrize("upml", [False, True])
+def test_float4_block_sizes_bit_exact_against_oracle(cuda_lib, monkeypatch, block, upml):
+    """The float4 update kernels at 128 threads per block (default) and 256 (OEMS_CUDA_V4_BLOCK,
+    _I4_BLOCK, _BOX4_BLOCK, _REG4_BLOCK): the Mur wall blocks and the UPML region offsets follow
+    the block size."""
+    for k in ("V4", "I4", "BOX4", "REG4"):
+        monkeypatch.setenv(f"OEMS_CUDA_{k}_BLOCK", block)
+    if upml:
+        op = configs.patch(shape=(56, 52, 36), steps=140, with_nf2ff=False)
+    else:
+        op = configs.stress(shape=(40, 36, 30), steps=140, nblocks=16, seed=1)
     g, r = _run_pair(op, 140, chunks=(1, 7, 16, 33))
-    assert g.update_kernels() == ("k_update_v4w", "k_update_i4")
+    want = ("k_update_reg4+k_update_box4",) * 2 if upml else ("k_update_v4w", "k_update_i4")
+    assert g.update_kernels() == want
     res = compare_engines(g, r)
     bad = [k for k, v in res.items() if not v]
     assert not bad, bad
