@@ -277,15 +277,16 @@ __global__ void __launch_bounds__(256, 3) k_adj_reg4(const __grid_constant__ Adj
 {
     const GridDev& g = a.g;
     const unsigned b = blockIdx.x;
-    if (b >= sp.first4[sp.nreg]) {                  // the main box's source groups (k_adj_box4 skips them)
-        const unsigned j = (b - sp.first4[sp.nreg]) * 256u + threadIdx.x;
+    const unsigned* fblk = blockDim.x == 128u ? sp.first4h : sp.first4;
+    if (b >= fblk[sp.nreg]) {                       // the main box's source groups (k_adj_box4 skips them)
+        const unsigned j = (b - fblk[sp.nreg]) * blockDim.x + threadIdx.x;
         if (j < (CURR ? a.injI.ngrp : a.injV.ngrp)) adj_src_group<CURR>(a, sp, j);
         return;
     }
     int r = 0;
-    while (r + 1 < (int)sp.nreg && b >= sp.first4[r + 1]) ++r;
+    while (r + 1 < (int)sp.nreg && b >= fblk[r + 1]) ++r;
     const UpmlDev& u = g.upml[r];
-    const unsigned j = (b - sp.first4[r]) * 256u + threadIdx.x;
+    const unsigned j = (b - fblk[r]) * blockDim.x + threadIdx.x;
     if (j >= u.nl[0] * u.nl[1] * reg_groups_per_row(u)) return;
     const RegGroup q = reg_group(u, j);
     const unsigned x = q.x, y = q.y, z0 = q.z0;
@@ -539,7 +540,7 @@ __global__ void __launch_bounds__(256) k_adj_grad(AdjDev a)
 template <bool CURR>
 __global__ void __launch_bounds__(256, 4) k_adj_box4(AdjDev a, SplitDev sp)
 {
-    unsigned t = blockIdx.x * 256u + threadIdx.x;
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= sp.main_cells4) return;
     const unsigned z0 = sp.z4 + ((t % sp.n4) << 2);
     t /= sp.n4;
@@ -1062,9 +1063,11 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
             if (sp[h]->reg4) {
                 cudaEventRecord(s->ev_rfork, rst);
                 cudaStreamWaitEvent(s->rr, s->ev_rfork, 0);
-                const unsigned rblk = sp[h]->first4[sp[h]->nreg] + (ng + 255) / 256;
-                if (h == 0) k_adj_reg4<true><<<rblk, 256, 0, s->rr>>>(dd, *sp[h]);
-                else k_adj_reg4<false><<<rblk, 256, 0, s->rr>>>(dd, *sp[h]);
+                const unsigned tb = e->adj_reg_block;
+                const unsigned rblk = (tb == 128u ? sp[h]->first4h[sp[h]->nreg] : sp[h]->first4[sp[h]->nreg]) +
+                                      (ng + tb - 1) / tb;
+                if (h == 0) k_adj_reg4<true><<<rblk, tb, 0, s->rr>>>(dd, *sp[h]);
+                else k_adj_reg4<false><<<rblk, tb, 0, s->rr>>>(dd, *sp[h]);
             } else {
                 if (const unsigned rblk = sp[h]->first_block[sp[h]->nreg]) {
                     if (h == 0) k_adj_split<true><<<rblk, 256, 0, rst>>>(dd, *sp[h]);
@@ -1076,8 +1079,9 @@ int oems_cuda_adjoint_backward(oems_cuda_engine* e, unsigned int nprobe, const i
                 }
             }
             if (sp[h]->main_blocks4) {
-                if (h == 0) k_adj_box4<true><<<sp[h]->main_blocks4, 256, 0, rst>>>(dd, *sp[h]);
-                else k_adj_box4<false><<<sp[h]->main_blocks4, 256, 0, rst>>>(dd, *sp[h]);
+                const unsigned tb = e->adj_box_block, nb = (sp[h]->main_cells4 + tb - 1) / tb;
+                if (h == 0) k_adj_box4<true><<<nb, tb, 0, rst>>>(dd, *sp[h]);
+                else k_adj_box4<false><<<nb, tb, 0, rst>>>(dd, *sp[h]);
             }
             if (sp[h]->reg4) {
                 cudaEventRecord(s->ev_rjoin, s->rr);

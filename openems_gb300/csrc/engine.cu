@@ -1142,6 +1142,10 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         // and of the UPML region kernel (patch 47.2 -> 45.8 us per step); OEMS_CUDA_REG4_BLOCK=256
         const char* rb = getenv("OEMS_CUDA_REG4_BLOCK");
         e->reg_block = (rb && atoi(rb) == 256) ? 256u : 128u;
+        // the reverse sweep's main box and regions (1,384 -> 1,360 ms for the 8,000-step design
+        // run; OEMS_CUDA_ADJ_BLOCK=256 restores the larger blocks)
+        const char* ab = getenv("OEMS_CUDA_ADJ_BLOCK");
+        e->adj_box_block = e->adj_reg_block = (ab && atoi(ab) == 256) ? 256u : 128u;
     }
 
     // UPML

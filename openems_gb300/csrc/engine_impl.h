@@ -186,6 +186,7 @@ struct oems_cuda_engine {
     unsigned v4_block = 128;         // threads per block of k_update_v4 / k_update_v4w
     unsigned box_block = 128;        // threads per block of k_update_box4
     unsigned reg_block = 128;        // threads per block of k_update_reg4 (128 or 256)
+    unsigned adj_box_block = 128, adj_reg_block = 128;   // the same for k_adj_box4 / k_adj_reg4
     // dispersive apply + next pre as one launch inside enqueued sequences (k_lorentz_carry)
     bool lor_carry_v = false, lor_carry_i = false;
     bool vtail = false;              // k_vtail: Mur apply + carry + excitation as one launch
