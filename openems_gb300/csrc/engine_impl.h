@@ -183,7 +183,7 @@ struct oems_cuda_engine {
     // the voltage update with the Mur hooks in the float4 form (k_update_v4w)
     bool mur_v4 = false;
     unsigned i4_block = 128;         // threads per block of k_update_i4
-    unsigned v4_block = 128;         // threads per block of k_update_v4 / k_update_v4w
+    unsigned v4_block = 64;          // threads per block of k_update_v4 / k_update_v4w
     unsigned box_block = 128;        // threads per block of k_update_box4
     unsigned reg_block = 128;        // threads per block of k_update_reg4 (128 or 256)
     unsigned adj_box_block = 128, adj_reg_block = 128;   // the same for k_adj_box4 / k_adj_reg4

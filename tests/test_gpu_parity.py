@@ -268,12 +268,12 @@ def test_split_step_end_bit_exact_against_oracle(cuda_lib, monkeypatch, split):
     assert g.launches_per_step() == n_one + (1 if split == "1" else 0)
 
 
-@pytest.mark.parametrize("block", ["256", "128"])
+@pytest.mark.parametrize("block", ["256", "128", "64"])
 @pytest.mark.parametrize("upml", [False, True])
 def test_float4_block_sizes_bit_exact_against_oracle(cuda_lib, monkeypatch, block, upml):
-    """The float4 update kernels at 128 threads per block (default) and 256 (OEMS_CUDA_V4_BLOCK,
-    _I4_BLOCK, _BOX4_BLOCK, _REG4_BLOCK): the Mur wall blocks and the UPML region offsets follow
-    the block size."""
+    """The float4 update kernels at 64, 128 and 256 threads per block (OEMS_CUDA_V4_BLOCK,
+    _I4_BLOCK, _BOX4_BLOCK, _REG4_BLOCK; the UPML kernels take 128 or 256): the Mur wall blocks
+    and the UPML region offsets follow the block size."""
     for k in ("V4", "I4", "BOX4", "REG4"):
         monkeypatch.setenv(f"OEMS_CUDA_{k}_BLOCK", block)
     if upml:
