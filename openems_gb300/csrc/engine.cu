@@ -1142,8 +1142,7 @@ int oems_cuda_init(oems_cuda_engine* e, unsigned int max_ts)
         e->v4_block = block_env("OEMS_CUDA_V4_BLOCK", 64u);
         // and of the UPML main box (design mesh 92.2 -> 91.2 us per step, 512x512x256 with UPML
         // 1.075 -> 1.059 ms); OEMS_CUDA_BOX4_BLOCK=256 restores the larger blocks
-        const char* bb = getenv("OEMS_CUDA_BOX4_BLOCK");
-        e->box_block = (bb && atoi(bb) == 256) ? 256u : 128u;
+        e->box_block = block_env("OEMS_CUDA_BOX4_BLOCK", 128u);
         // and of the UPML region kernel (patch 47.2 -> 45.8 us per step); OEMS_CUDA_REG4_BLOCK=256
         const char* rb = getenv("OEMS_CUDA_REG4_BLOCK");
         e->reg_block = (rb && atoi(rb) == 256) ? 256u : 128u;
